@@ -1,0 +1,219 @@
+/*
+ * rheogpu.h — C ABI of the GB300 rheoFoam time-step library (librheogpu.so).
+ *
+ * One context owns one device mesh, one case (boundary conditions, model,
+ * solver controls) and the device-resident fields of that case.  Host arrays
+ * crossing this boundary are in OpenFOAM's own layout: cell fields are AoS
+ * (vector x,y,z; symmTensor xx,xy,xz,yy,yz,zz; tensor xx..zz row-major),
+ * surface fields are per internal face in upper-triangular face order, then
+ * per boundary face patch by patch.  No pointer is retained past a call.
+ *
+ * Reference interfaces replaced (paths inside fppimenta/rheoTool, of90/src):
+ *   rt_constitutive_correct  constitutiveEq::correct(alpha*, gradU*)
+ *                            libs/constitutiveEquations/constitutiveEqs/
+ *                            constitutiveEq/constitutiveEq.H:343-347, as done by
+ *                            Oldroyd-B/Oldroyd-BLog/Oldroyd_BLog.C:127-179,
+ *                            Giesekus/GiesekusLog/GiesekusLog.C:128-176,
+ *                            PTT/PTTLog/PTTLog.C:176-268,
+ *                            FENE-P/FENE-PLog/FENE_PLog.C:128-182
+ *   rt_ldu_solve             lduMatrix::solver::solve(psi, source, cmpt) of
+ *                            OpenFOAM's PCG/DIC and PBiCGStab/DILU, reached
+ *                            through sparseSolver<Type>::solve
+ *                            (libs/sparseMatrixSolvers/segregated/sparseSolver.H:
+ *                            200-205, openFoamSolver/openFoamSolver.C:46-53)
+ *   rt_step                  one segregated time step of rheoFoam
+ *                            (solvers/rheoFoam/rheoFoam.C:147-154: UEqn.H,
+ *                            pEqn.H, constEq.correct())
+ *   rt_residual              sparseSolver<Type>::getFoamResiduals
+ *                            (libs/sparseMatrixSolvers/segregated/sparseSolver.C:
+ *                            129-180)
+ *   rt_mesh_upload           the fvMesh / lduAddressing a solver is built on
+ *   rt_field_set / _get      GeometricField construction / write
+ *
+ * Errors are integer status codes; no C++ exception crosses this boundary.
+ */
+#ifndef RHEOGPU_H
+#define RHEOGPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------- */
+#define RT_OK        0
+#define RT_EINVAL    1   /* bad argument, size or state                        */
+#define RT_ENOCONV   2   /* a Krylov solve hit maxIter without converging      */
+#define RT_ENAN      3   /* a NaN/Inf appeared in a residual or field          */
+#define RT_ETIMEOUT  4   /* a bounded device-side wait ran out                 */
+#define RT_EOOM      5   /* device allocation failed / admission refused       */
+#define RT_ECUDA     6   /* a CUDA runtime call failed                          */
+#define RT_ENOTREADY 7   /* mesh / case not uploaded yet                        */
+typedef int32_t rt_status;
+
+typedef struct rt_ctx rt_ctx;
+
+/* ---- mesh --------------------------------------------------------------- */
+typedef struct {
+    int32_t nCells, nFaces, nBFaces, nPatches;
+    const int32_t *owner, *neighbour;          /* nFaces, owner < neighbour   */
+    const double *Sf;                           /* 3*nFaces face area vectors  */
+    const double *magSf;                        /* nFaces                      */
+    const double *Cf;                           /* 3*nFaces face centres       */
+    const double *weights;                      /* nFaces owner weights        */
+    const double *deltaCoeffs;                  /* nFaces 1/|C_N - C_P|        */
+    const double *C;                            /* 3*nCells cell centres       */
+    const double *V;                            /* nCells volumes              */
+    const int32_t *bCell;                       /* nBFaces face cells          */
+    const double *bSf, *bmagSf, *bCf;           /* 3*nB, nB, 3*nB              */
+    const double *bDeltaCoeffs;                 /* nB 1/|Cf - C_P|             */
+    const int32_t *patchStart, *patchSize;      /* nPatches                    */
+    int32_t solveDir[3];                        /* 0 for an empty direction    */
+} rt_mesh_desc;
+
+/* ---- boundary conditions (one kind per patch and field) ---------------- */
+#define RT_BC_FIXED     0   /* fixedValue                                      */
+#define RT_BC_ZEROGRAD  1   /* zeroGradient                                    */
+#define RT_BC_LINEXTRAP 2   /* linearExtrapolation (rheoTool, tau only)        */
+
+typedef struct {
+    const int32_t *U, *p, *theta, *tau;   /* nPatches kinds each                */
+    const double *Ub;                     /* 3*nBFaces values of fixed U faces  */
+    const double *pb;                     /* nBFaces                            */
+    const double *thetab;                 /* 6*nBFaces                          */
+    const double *taub;                   /* 6*nBFaces                          */
+} rt_bc_desc;
+
+/* ---- constitutive model ----------------------------------------------- */
+#define RT_MODEL_OLDROYDB_LOG 0   /* type Oldroyd-BLog                          */
+#define RT_MODEL_GIESEKUS_LOG 1   /* type GiesekusLog                           */
+#define RT_MODEL_PTT_LOG      2   /* type PTTLog                                */
+#define RT_MODEL_FENEP_LOG    3   /* type FENE-PLog                             */
+#define RT_PTT_LINEAR 0
+#define RT_PTT_EXP    1
+#define RT_STAB_NONE     0
+#define RT_STAB_BSD      1
+#define RT_STAB_COUPLING 2
+
+typedef struct {
+    int32_t model, pttFunction, stabilization, pad_;
+    double rho, etaS, etaP, lambda;
+    double alpha;     /* Giesekus mobility                                    */
+    double epsilon;   /* PTT extensibility                                    */
+    double zeta;      /* PTT slip                                             */
+    double L2;        /* FENE-P squared extensibility                         */
+} rt_model_params;
+
+/* ---- linear solvers ----------------------------------------------------- */
+#define RT_SOLVER_PCG       0
+#define RT_SOLVER_PBICGSTAB 1
+#define RT_PRECOND_NONE     0
+#define RT_PRECOND_DIC      1
+#define RT_PRECOND_DILU     2
+#define RT_PRECOND_DIAGONAL 3
+
+typedef struct {
+    int32_t solver, preconditioner;
+    double tolerance, relTol;
+    int32_t minIter, maxIter;
+} rt_solver_ctl;
+
+typedef struct {
+    double initialResidual, finalResidual;
+    int32_t nIterations, converged, singular, pad_;
+} rt_solver_perf;
+
+/* ---- case control ---------------------------------------------------- */
+#define RT_LIM_NONE     -1
+#define RT_LIM_UPWIND    0
+#define RT_LIM_CUBISTA   1
+#define RT_LIM_MINMOD    2
+#define RT_LIM_SMART     3
+#define RT_LIM_WACEB     4
+#define RT_LIM_SUPERBEE  5
+
+#define RT_PREC_FP64  0   /* plain form: FP64 throughout                       */
+#define RT_PREC_MIXED 1   /* FP32 Krylov + FP64 refinement, FP32 constitutive  */
+
+typedef struct {
+    double deltaT;
+    int32_t divU, divTheta;          /* RT_LIM_* for div(phi,U), div(phi,theta) */
+    int32_t pRefCell, needReference; /* needReference: p has no fixed patch    */
+    double pRefValue;
+    rt_solver_ctl solverU, solverP, solverTheta;
+    int32_t precision, pad_;
+} rt_case_ctl;
+
+typedef struct {
+    rt_solver_perf U[3], p, theta[6];
+    double contErrSumLocal, contErrGlobal;
+} rt_step_perf;
+
+/* ---- field identifiers for rt_field_set / rt_field_get --------------- */
+#define RT_FIELD_U       0   /* 3 comps, internal + boundary                   */
+#define RT_FIELD_P       1   /* 1                                              */
+#define RT_FIELD_PHI     2   /* surface: nFaces internal + nBFaces boundary     */
+#define RT_FIELD_THETA   3   /* 6                                              */
+#define RT_FIELD_TAU     4   /* 6                                              */
+#define RT_FIELD_EIGVALS 5   /* 3: diagonal of eigVals (= exp of eigenvalues)  */
+#define RT_FIELD_EIGVECS 6   /* 9: eigenvectors as columns, row-major tensor   */
+
+/* ---- entry points ------------------------------------------------------- */
+rt_status rt_ctx_create(rt_ctx **ctx, int32_t device);
+rt_status rt_ctx_destroy(rt_ctx *ctx);
+const char *rt_last_error(const rt_ctx *ctx);
+const char *rt_status_string(rt_status s);
+
+rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *mesh);
+rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
+                        const rt_model_params *model, const rt_case_ctl *ctl);
+/* internal: ncmpt*nCells AoS (may be NULL); boundary: ncmpt*nBFaces AoS (may
+ * be NULL).  For RT_FIELD_PHI internal is nFaces long. */
+rt_status rt_field_set(rt_ctx *ctx, int32_t field, const double *internal,
+                       const double *boundary);
+rt_status rt_field_get(rt_ctx *ctx, int32_t field, double *internal,
+                       double *boundary);
+
+/* Solve ncmpt systems that share one LDU matrix on the uploaded mesh's
+ * addressing.  diag/source/psi are complete (boundary coefficients already
+ * added, as lduMatrix::solver receives them).  source and psi hold ncmpt
+ * blocks of nCells (component-major).  perf gets ncmpt entries. */
+rt_status rt_ldu_solve(rt_ctx *ctx, const double *diag, const double *upper,
+                       const double *lower, const double *source, double *psi,
+                       int32_t ncmpt, const rt_solver_ctl *ctl,
+                       rt_solver_perf *perf);
+
+/* OpenFOAM-normalised residual of one component (sparseSolver.C:129-180). */
+rt_status rt_residual(rt_ctx *ctx, const double *diag, const double *upper,
+                      const double *lower, const double *source,
+                      const double *psi, double *residual);
+
+/* One constitutiveEq::correct() on the device-resident U, phi, theta, eig
+ * fields; gradU (9*nCells AoS) may be NULL (then fvc::grad(U) is used).
+ * thetaPerf gets 6 entries (components not solved have nIterations = -1). */
+rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU,
+                                  rt_solver_perf *thetaPerf);
+
+/* nSteps segregated rheoFoam time steps; perf (may be NULL) gets the last. */
+rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf);
+
+/* Gauss-linear gradient of one scalar field with boundary values
+ * (fvc::grad): psi nCells, psib nBFaces, grad 3*nCells AoS. */
+rt_status rt_op_grad(rt_ctx *ctx, const double *psi, const double *psib,
+                     double *grad);
+
+/* Per-cell symmetric 3x3 eigendecomposition of theta (6*n AoS): eigVals gets
+ * exp(eigenvalues) ascending (3*n), eigVecs the eigenvectors as columns (9*n)
+ * (constitutiveEq::calcEig, constitutiveEq.C:360-428). */
+rt_status rt_op_eig(rt_ctx *ctx, int32_t n, const double *theta,
+                    double *eigVals, double *eigVecs);
+
+/* Wait for all work of the context. */
+rt_status rt_sync(rt_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RHEOGPU_H */

@@ -1,0 +1,141 @@
+"""ctypes binding of the FP64 CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py as the checker.  The product (rheotool_gb300) never
+imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from rheotool_gb300 import abi
+from rheotool_gb300.case import Case, Fields
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+_dp = C.POINTER(C.c_double)
+
+
+class or_state(C.Structure):
+    _fields_ = [(n, _dp) for n in ("U", "Ub", "p", "pb", "phi", "phib", "theta", "thetab",
+                                   "tau", "taub", "eigVals", "eigVecs")]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
+            os.path.join(HERE, "oracle.c")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "-B" if force else "liboracle.so"])
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        P = C.POINTER
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_grad.argtypes = [P(abi.rt_mesh_desc), _dp, _dp, _dp]
+        L.or_ldu_solve.argtypes = [P(abi.rt_mesh_desc), _dp, _dp, _dp, _dp, _dp,
+                                   P(abi.rt_solver_ctl), P(abi.rt_solver_perf)]
+        L.or_ldu_solve.restype = C.c_int
+        L.or_residual.argtypes = [P(abi.rt_mesh_desc), _dp, _dp, _dp, _dp, _dp]
+        L.or_residual.restype = C.c_double
+        L.or_eig.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.or_eig3.argtypes = [_dp, _dp, _dp]
+        L.or_constitutive_correct.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc),
+                                              P(abi.rt_model_params), P(abi.rt_case_ctl),
+                                              P(or_state), _dp, P(abi.rt_solver_perf)]
+        L.or_constitutive_correct.restype = C.c_int
+        L.or_step.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params),
+                              P(abi.rt_case_ctl), P(or_state), C.c_int, P(abi.rt_step_perf)]
+        L.or_step.restype = C.c_int
+        L.or_init_fields.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(or_state)]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().or_set_threads(int(n))
+
+
+def _state(f: Fields) -> or_state:
+    s = or_state()
+    for name, _ in or_state._fields_:
+        a = getattr(f, name)
+        assert a.dtype == np.float64 and a.flags.c_contiguous, name
+        setattr(s, name, a.ctypes.data_as(_dp))
+    return s
+
+
+class Oracle:
+    """FP64 CPU restatement of one case (same Case object as the GPU path)."""
+
+    def __init__(self, case: Case, fields: Fields = None):
+        self.case = case
+        self.md, self.bd, self.mp, self.ctl = case.descriptors()
+        self.f = fields if fields is not None else Fields.zeros(case.mesh)
+        if fields is None:
+            lib().or_init_fields(C.byref(self.md), C.byref(self.bd), C.byref(_state(self.f)))
+
+    def step(self, n: int = 1) -> abi.rt_step_perf:
+        perf = abi.rt_step_perf()
+        st = lib().or_step(C.byref(self.md), C.byref(self.bd), C.byref(self.mp), C.byref(self.ctl),
+                           C.byref(_state(self.f)), int(n), C.byref(perf))
+        if st != 0:
+            raise RuntimeError(f"oracle step failed: {abi.STATUS_NAMES.get(st, st)}")
+        return perf
+
+    def constitutive_correct(self, gradU: np.ndarray = None):
+        perf = (abi.rt_solver_perf * 6)()
+        g = None if gradU is None else np.ascontiguousarray(gradU, dtype=np.float64)
+        st = lib().or_constitutive_correct(C.byref(self.md), C.byref(self.bd), C.byref(self.mp),
+                                           C.byref(self.ctl), C.byref(_state(self.f)),
+                                           None if g is None else g.ctypes.data_as(_dp), perf)
+        if st != 0:
+            raise RuntimeError(f"oracle constitutive correct failed: {st}")
+        return list(perf)
+
+    def grad(self, psi: np.ndarray, psib: np.ndarray) -> np.ndarray:
+        g = np.zeros((self.case.mesh.nCells, 3))
+        lib().or_grad(C.byref(self.md), abi.dptr(np.ascontiguousarray(psi, dtype=np.float64)),
+                      abi.dptr(np.ascontiguousarray(psib, dtype=np.float64)), abi.dptr(g))
+        return g
+
+    def ldu_solve(self, diag, upper, lower, source, psi, ctl) -> abi.rt_solver_perf:
+        """One-component lduMatrix::solver solve; psi is updated in place."""
+        perf = abi.rt_solver_perf()
+        c = ctl.to_c() if hasattr(ctl, "to_c") else ctl
+        lib().or_ldu_solve(C.byref(self.md), abi.dptr(diag), abi.dptr(upper), abi.dptr(lower),
+                           abi.dptr(source), abi.dptr(psi), C.byref(c), C.byref(perf))
+        return perf
+
+    def residual(self, diag, upper, lower, source, psi) -> float:
+        return lib().or_residual(C.byref(self.md), abi.dptr(diag), abi.dptr(upper),
+                                 abi.dptr(lower), abi.dptr(source), abi.dptr(psi))
+
+
+def eig(theta: np.ndarray):
+    """Per-cell calcEig of an (n, 6) symmTensor array -> (exp(mu) (n,3), vecs (n,9))."""
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    n = theta.shape[0]
+    vals = np.zeros((n, 3))
+    vecs = np.zeros((n, 9))
+    lib().or_eig(n, abi.dptr(theta), abi.dptr(vals), abi.dptr(vecs))
+    return vals, vecs
+
+
+def eig3(s) -> tuple:
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    mu = np.zeros(3)
+    V = np.zeros(9)
+    lib().or_eig3(abi.dptr(s), abi.dptr(mu), abi.dptr(V))
+    return mu, V.reshape(3, 3)

@@ -1,0 +1,171 @@
+"""ctypes mirror of ``include/rheogpu.h`` and the loader of ``librheogpu.so``.
+
+The structures below are field-for-field copies of the C declarations; the
+library itself is the CUDA build in this package directory.  Loading fails
+loudly when the shared object is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBNAME = os.path.join(HERE, "librheogpu.so")
+
+RT_OK, RT_EINVAL, RT_ENOCONV, RT_ENAN, RT_ETIMEOUT, RT_EOOM, RT_ECUDA, RT_ENOTREADY = range(8)
+RT_BC_FIXED, RT_BC_ZEROGRAD, RT_BC_LINEXTRAP = 0, 1, 2
+RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG = 0, 1, 2, 3
+RT_PTT_LINEAR, RT_PTT_EXP = 0, 1
+RT_STAB_NONE, RT_STAB_BSD, RT_STAB_COUPLING = 0, 1, 2
+RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB = 0, 1
+RT_PRECOND_NONE, RT_PRECOND_DIC, RT_PRECOND_DILU, RT_PRECOND_DIAGONAL = 0, 1, 2, 3
+RT_LIM_NONE, RT_LIM_UPWIND, RT_LIM_CUBISTA, RT_LIM_MINMOD, RT_LIM_SMART, RT_LIM_WACEB, RT_LIM_SUPERBEE = -1, 0, 1, 2, 3, 4, 5
+RT_PREC_FP64, RT_PREC_MIXED = 0, 1
+RT_FIELD_U, RT_FIELD_P, RT_FIELD_PHI, RT_FIELD_THETA, RT_FIELD_TAU, RT_FIELD_EIGVALS, RT_FIELD_EIGVECS = range(7)
+
+MODEL_NAMES = {
+    "Oldroyd-BLog": RT_MODEL_OLDROYDB_LOG,
+    "GiesekusLog": RT_MODEL_GIESEKUS_LOG,
+    "PTTLog": RT_MODEL_PTT_LOG,
+    "FENE-PLog": RT_MODEL_FENEP_LOG,
+}
+LIMITER_NAMES = {
+    "none": RT_LIM_NONE, "upwind": RT_LIM_UPWIND, "cubista": RT_LIM_CUBISTA,
+    "minmod": RT_LIM_MINMOD, "smart": RT_LIM_SMART, "waceb": RT_LIM_WACEB,
+    "superbee": RT_LIM_SUPERBEE,
+}
+STATUS_NAMES = {0: "RT_OK", 1: "RT_EINVAL", 2: "RT_ENOCONV", 3: "RT_ENAN",
+                4: "RT_ETIMEOUT", 5: "RT_EOOM", 6: "RT_ECUDA", 7: "RT_ENOTREADY"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class rt_mesh_desc(C.Structure):
+    _fields_ = [
+        ("nCells", C.c_int32), ("nFaces", C.c_int32), ("nBFaces", C.c_int32), ("nPatches", C.c_int32),
+        ("owner", _ip), ("neighbour", _ip),
+        ("Sf", _dp), ("magSf", _dp), ("Cf", _dp), ("weights", _dp), ("deltaCoeffs", _dp),
+        ("C", _dp), ("V", _dp),
+        ("bCell", _ip), ("bSf", _dp), ("bmagSf", _dp), ("bCf", _dp), ("bDeltaCoeffs", _dp),
+        ("patchStart", _ip), ("patchSize", _ip),
+        ("solveDir", C.c_int32 * 3),
+    ]
+
+
+class rt_bc_desc(C.Structure):
+    _fields_ = [
+        ("U", _ip), ("p", _ip), ("theta", _ip), ("tau", _ip),
+        ("Ub", _dp), ("pb", _dp), ("thetab", _dp), ("taub", _dp),
+    ]
+
+
+class rt_model_params(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32), ("pttFunction", C.c_int32), ("stabilization", C.c_int32), ("pad_", C.c_int32),
+        ("rho", C.c_double), ("etaS", C.c_double), ("etaP", C.c_double), ("lambda_", C.c_double),
+        ("alpha", C.c_double), ("epsilon", C.c_double), ("zeta", C.c_double), ("L2", C.c_double),
+    ]
+
+
+class rt_solver_ctl(C.Structure):
+    _fields_ = [
+        ("solver", C.c_int32), ("preconditioner", C.c_int32),
+        ("tolerance", C.c_double), ("relTol", C.c_double),
+        ("minIter", C.c_int32), ("maxIter", C.c_int32),
+    ]
+
+
+class rt_solver_perf(C.Structure):
+    _fields_ = [
+        ("initialResidual", C.c_double), ("finalResidual", C.c_double),
+        ("nIterations", C.c_int32), ("converged", C.c_int32), ("singular", C.c_int32), ("pad_", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return dict(initialResidual=self.initialResidual, finalResidual=self.finalResidual,
+                    nIterations=self.nIterations, converged=bool(self.converged),
+                    singular=bool(self.singular))
+
+
+class rt_case_ctl(C.Structure):
+    _fields_ = [
+        ("deltaT", C.c_double),
+        ("divU", C.c_int32), ("divTheta", C.c_int32),
+        ("pRefCell", C.c_int32), ("needReference", C.c_int32),
+        ("pRefValue", C.c_double),
+        ("solverU", rt_solver_ctl), ("solverP", rt_solver_ctl), ("solverTheta", rt_solver_ctl),
+        ("precision", C.c_int32), ("pad_", C.c_int32),
+    ]
+
+
+class rt_step_perf(C.Structure):
+    _fields_ = [
+        ("U", rt_solver_perf * 3), ("p", rt_solver_perf), ("theta", rt_solver_perf * 6),
+        ("contErrSumLocal", C.c_double), ("contErrGlobal", C.c_double),
+    ]
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+def optr(a):
+    """double* or NULL"""
+    return None if a is None else dptr(a)
+
+
+_lib = None
+
+
+def load_library(path: str = LIBNAME):
+    """Load librheogpu.so (built by ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    sig = {
+        "rt_ctx_create": ([P(vp), C.c_int32], C.c_int32),
+        "rt_ctx_destroy": ([vp], C.c_int32),
+        "rt_last_error": ([vp], C.c_char_p),
+        "rt_status_string": ([C.c_int32], C.c_char_p),
+        "rt_mesh_upload": ([vp, P(rt_mesh_desc)], C.c_int32),
+        "rt_case_setup": ([vp, P(rt_bc_desc), P(rt_model_params), P(rt_case_ctl)], C.c_int32),
+        "rt_field_set": ([vp, C.c_int32, _dp, _dp], C.c_int32),
+        "rt_field_get": ([vp, C.c_int32, _dp, _dp], C.c_int32),
+        "rt_ldu_solve": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int32, P(rt_solver_ctl), P(rt_solver_perf)], C.c_int32),
+        "rt_residual": ([vp, _dp, _dp, _dp, _dp, _dp, _dp], C.c_int32),
+        "rt_constitutive_correct": ([vp, _dp, P(rt_solver_perf)], C.c_int32),
+        "rt_step": ([vp, C.c_int32, P(rt_step_perf)], C.c_int32),
+        "rt_op_grad": ([vp, _dp, _dp, _dp], C.c_int32),
+        "rt_op_eig": ([vp, C.c_int32, _dp, _dp, _dp], C.c_int32),
+        "rt_sync": ([vp], C.c_int32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def header_symbols(header: str) -> list:
+    """Names of the functions declared in a C header (``rt_...(``)."""
+    import re
+    txt = open(header).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(rt_[a-z_0-9]+)\s*\(", txt)))

@@ -1,0 +1,247 @@
+"""Case description: mesh + boundary conditions + constitutive model + the
+``fvSolution``/``fvSchemes``/``controlDict`` entries the time step reads.
+
+The keys mirror rheoTool's dictionaries one to one:
+``constant/constitutiveProperties`` (``type``, ``rho``, ``etaS``, ``etaP``,
+``lambda``, ``alpha``, ``epsilon``, ``zeta``, ``L2``, ``stabilization``,
+``destructionFunctionType``; read in e.g. ``GiesekusLog.C:93-120`` and
+``constitutiveEq::checkForStab``), ``system/fvSolution`` (``solver``,
+``preconditioner``, ``tolerance``, ``relTol``, ``minIter``, ``maxIter``,
+``pRefCell``, ``pRefValue``) and ``system/fvSchemes``
+(``div(phi,U)``/``div(phi,theta)`` ``GaussDefCmpw <limiter>``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Callable, Dict, Optional, Tuple, Union
+
+import numpy as np
+
+from . import abi
+from .mesh import Mesh, cavity_mesh, contraction_mesh, channel_mesh
+
+BC_KINDS = {"fixedValue": abi.RT_BC_FIXED, "zeroGradient": abi.RT_BC_ZEROGRAD,
+            "linearExtrapolation": abi.RT_BC_LINEXTRAP}
+SOLVERS = {"PCG": abi.RT_SOLVER_PCG, "PBiCGStab": abi.RT_SOLVER_PBICGSTAB}
+PRECONDS = {"none": abi.RT_PRECOND_NONE, "DIC": abi.RT_PRECOND_DIC,
+            "DILU": abi.RT_PRECOND_DILU, "diagonal": abi.RT_PRECOND_DIAGONAL}
+STABS = {"none": abi.RT_STAB_NONE, "BSD": abi.RT_STAB_BSD, "coupling": abi.RT_STAB_COUPLING}
+
+
+@dataclass
+class SolverControl:
+    solver: str = "PBiCGStab"
+    preconditioner: str = "DILU"
+    tolerance: float = 1e-10
+    relTol: float = 0.0
+    minIter: int = 0
+    maxIter: int = 1000
+
+    def to_c(self) -> abi.rt_solver_ctl:
+        return abi.rt_solver_ctl(SOLVERS[self.solver], PRECONDS[self.preconditioner],
+                                 self.tolerance, self.relTol, self.minIter, self.maxIter)
+
+
+@dataclass
+class Model:
+    type: str = "Oldroyd-BLog"
+    rho: float = 1.0
+    etaS: float = 0.5
+    etaP: float = 0.5
+    lambda_: float = 1.0
+    alpha: float = 0.0
+    epsilon: float = 0.0
+    zeta: float = 0.0
+    L2: float = 100.0
+    stabilization: str = "coupling"
+    destructionFunctionType: str = "linear"
+
+    def to_c(self) -> abi.rt_model_params:
+        if self.type not in abi.MODEL_NAMES:
+            raise ValueError(f"Unknown constitutiveEq type {self.type}; valid: "
+                             f"{sorted(abi.MODEL_NAMES)}")
+        ptt = abi.RT_PTT_EXP if self.destructionFunctionType == "exponential" else abi.RT_PTT_LINEAR
+        return abi.rt_model_params(abi.MODEL_NAMES[self.type], ptt, STABS[self.stabilization], 0,
+                                   self.rho, self.etaS, self.etaP, self.lambda_, self.alpha,
+                                   self.epsilon, self.zeta, self.L2)
+
+
+Value = Union[float, Tuple[float, ...], Callable[[np.ndarray], np.ndarray]]
+
+
+@dataclass
+class Case:
+    mesh: Mesh
+    model: Model
+    bcs: Dict[str, Dict[str, Tuple[str, Optional[Value]]]]   # patch -> field -> (kind, value)
+    deltaT: float = 1e-3
+    divU: str = "cubista"
+    divTheta: str = "cubista"
+    solverU: SolverControl = field(default_factory=lambda: SolverControl("PBiCGStab", "DILU", 1e-10))
+    solverP: SolverControl = field(default_factory=lambda: SolverControl("PCG", "DIC", 1e-8, maxIter=800))
+    solverTheta: SolverControl = field(default_factory=lambda: SolverControl("PBiCGStab", "DILU", 1e-10))
+    pRefCell: int = 0
+    pRefValue: float = 0.0
+    precision: int = abi.RT_PREC_FP64
+    name: str = "case"
+
+    # ------------------------------------------------------------------
+    def _field_bc(self, fld: str, ncomp: int):
+        m = self.mesh
+        kinds = np.zeros(len(m.patches), np.int32)
+        vals = np.zeros((m.nBFaces, ncomp))
+        for p, patch in enumerate(m.patches):
+            kind, val = self.bcs[patch.name][fld]
+            kinds[p] = BC_KINDS[kind]
+            if val is None:
+                continue
+            sl = slice(patch.start, patch.start + patch.size)
+            if callable(val):
+                vals[sl] = np.asarray(val(m.bCf[sl])).reshape(patch.size, ncomp)
+            else:
+                vals[sl] = np.broadcast_to(np.asarray(val, dtype=np.float64), (patch.size, ncomp))
+        return kinds, np.ascontiguousarray(vals)
+
+    @property
+    def needReference(self) -> bool:
+        return all(self.bcs[p.name]["p"][0] != "fixedValue" for p in self.mesh.patches)
+
+    def descriptors(self):
+        """(rt_mesh_desc, rt_bc_desc, rt_model_params, rt_case_ctl); the numpy
+        arrays behind the pointers are kept alive on ``self``."""
+        m = self.mesh
+        keep = []
+
+        def d(a):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return abi.dptr(a)
+
+        def i(a):
+            a = np.ascontiguousarray(a, dtype=np.int32)
+            keep.append(a)
+            return abi.iptr(a)
+
+        md = abi.rt_mesh_desc()
+        md.nCells, md.nFaces, md.nBFaces, md.nPatches = m.nCells, m.nFaces, m.nBFaces, len(m.patches)
+        md.owner, md.neighbour = i(m.owner), i(m.neighbour)
+        md.Sf, md.magSf, md.Cf = d(m.Sf), d(m.magSf), d(m.Cf)
+        md.weights, md.deltaCoeffs = d(m.w), d(m.deltaCoeffs)
+        md.C, md.V = d(m.C), d(m.V)
+        md.bCell, md.bSf, md.bmagSf, md.bCf, md.bDeltaCoeffs = i(m.bCell), d(m.bSf), d(m.bmagSf), d(m.bCf), d(m.bDelta)
+        md.patchStart = i(np.array([p.start for p in m.patches]))
+        md.patchSize = i(np.array([p.size for p in m.patches]))
+        for k in range(3):
+            md.solveDir[k] = int(m.solveDir[k])
+
+        kU, Ub = self._field_bc("U", 3)
+        kP, pb = self._field_bc("p", 1)
+        kT, thb = self._field_bc("theta", 6)
+        kTa, tab = self._field_bc("tau", 6)
+        bd = abi.rt_bc_desc(i(kU), i(kP), i(kT), i(kTa), d(Ub), d(pb.reshape(-1)), d(thb), d(tab))
+        mp = self.model.to_c()
+        ctl = abi.rt_case_ctl()
+        ctl.deltaT = self.deltaT
+        ctl.divU = abi.LIMITER_NAMES[self.divU]
+        ctl.divTheta = abi.LIMITER_NAMES[self.divTheta]
+        ctl.pRefCell = self.pRefCell
+        ctl.needReference = int(self.needReference)
+        ctl.pRefValue = self.pRefValue
+        ctl.solverU = self.solverU.to_c()
+        ctl.solverP = self.solverP.to_c()
+        ctl.solverTheta = self.solverTheta.to_c()
+        ctl.precision = self.precision
+        self._keep = keep
+        return md, bd, mp, ctl
+
+
+# ---------------------------------------------------------------------------
+# Workload builders
+# ---------------------------------------------------------------------------
+WALL_VE = {"U": ("fixedValue", (0.0, 0.0, 0.0)), "p": ("zeroGradient", None),
+           "theta": ("zeroGradient", None), "tau": ("linearExtrapolation", 0.0)}
+
+
+def lid_profile(Cf: np.ndarray) -> np.ndarray:
+    """Steady lid velocity U = (16 x^2 (1-x)^2, 0, 0)."""
+    x = Cf[:, 0]
+    u = np.zeros((Cf.shape[0], 3))
+    u[:, 0] = 16.0 * x ** 2 * (1.0 - x) ** 2
+    return u
+
+
+def cavity_case(n: int = 64, model: str = "Oldroyd-BLog", Wi: float = 0.5, beta: float = 0.5,
+                Re: float = 0.01, dt: float = 1e-3, **model_kw) -> Case:
+    """Lid-driven cavity: U_lid = 16x^2(1-x)^2, lambda = Wi (U = L = 1),
+    etaS = beta, etaP = 1 - beta, rho = Re (eta0 = 1); Euler, GaussDefCmpw
+    cubista, p PCG-DIC 1e-8, U/theta PBiCGStab-DILU 1e-10."""
+    mesh = cavity_mesh(n)
+    mdl = Model(model, rho=Re, etaS=beta, etaP=1.0 - beta, lambda_=Wi, **model_kw)
+    bcs = {
+        "movingLid": dict(WALL_VE, U=("fixedValue", lid_profile)),
+        "fixedWalls": dict(WALL_VE),
+    }
+    return Case(mesh, mdl, bcs, deltaT=dt, name=f"cavity{n}_{model}")
+
+
+def contraction_case(mesh: Optional[Mesh] = None, model: str = "GiesekusLog", Wi: float = 2.0,
+                     beta: float = 1.0 / 9.0, rho: float = 0.01, alpha: float = 0.1,
+                     U_in: float = 0.25, dt: float = 5e-3, **model_kw) -> Case:
+    """3-D 4:1 planar contraction, Giesekus-Log alpha = 0.1, beta = 1/9,
+    Wi = lambda U_d / H = 2 with U_d = 4 U_in = 1 and H = 1."""
+    mesh = mesh if mesh is not None else contraction_mesh()
+    U_d = 4.0 * U_in
+    mdl = Model(model, rho=rho, etaS=beta, etaP=1.0 - beta, lambda_=Wi * 1.0 / U_d,
+                alpha=alpha, **model_kw)
+    bcs = {
+        "inlet": {"U": ("fixedValue", (U_in, 0.0, 0.0)), "p": ("zeroGradient", None),
+                  "theta": ("fixedValue", 0.0), "tau": ("fixedValue", 0.0)},
+        "outlet": {"U": ("zeroGradient", None), "p": ("fixedValue", 0.0),
+                   "theta": ("zeroGradient", None), "tau": ("zeroGradient", None)},
+        "walls": dict(WALL_VE),
+    }
+    return Case(mesh, mdl, bcs, deltaT=dt, name=f"contraction{mesh.nCells}_{model}")
+
+
+def channel_case(mesh: Optional[Mesh] = None, model: str = "Oldroyd-BLog", U_in: float = 1.0,
+                 dt: float = 1e-2, lambda_: float = 0.1, beta: float = 0.5, rho: float = 0.01,
+                 **model_kw) -> Case:
+    mesh = mesh if mesh is not None else channel_mesh()
+    mdl = Model(model, rho=rho, etaS=beta, etaP=1.0 - beta, lambda_=lambda_, **model_kw)
+    bcs = {
+        "inlet": {"U": ("fixedValue", (U_in, 0.0, 0.0)), "p": ("zeroGradient", None),
+                  "theta": ("fixedValue", 0.0), "tau": ("fixedValue", 0.0)},
+        "outlet": {"U": ("zeroGradient", None), "p": ("fixedValue", 0.0),
+                   "theta": ("zeroGradient", None), "tau": ("zeroGradient", None)},
+        "walls": dict(WALL_VE),
+    }
+    return Case(mesh, mdl, bcs, deltaT=dt, name=f"channel_{model}")
+
+
+@dataclass
+class Fields:
+    """Host copy of the state of a case (OpenFOAM AoS layout)."""
+    U: np.ndarray
+    Ub: np.ndarray
+    p: np.ndarray
+    pb: np.ndarray
+    phi: np.ndarray
+    phib: np.ndarray
+    theta: np.ndarray
+    thetab: np.ndarray
+    tau: np.ndarray
+    taub: np.ndarray
+    eigVals: np.ndarray
+    eigVecs: np.ndarray
+
+    @staticmethod
+    def zeros(mesh: Mesh) -> "Fields":
+        N, nF, nB = mesh.nCells, mesh.nFaces, mesh.nBFaces
+        z = lambda *s: np.zeros(s)
+        return Fields(U=z(N, 3), Ub=z(nB, 3), p=z(N), pb=z(nB), phi=z(nF), phib=z(nB),
+                      theta=z(N, 6), thetab=z(nB, 6), tau=z(N, 6), taub=z(nB, 6),
+                      eigVals=np.ones((N, 3)), eigVecs=np.tile(np.eye(3).reshape(9), (N, 1)))
+
+    def copy(self) -> "Fields":
+        return Fields(**{k: v.copy() for k, v in self.__dict__.items()})

@@ -1,0 +1,463 @@
+// ctx.cu — C-ABI entry points: context, mesh upload, case setup, field I/O.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+#include "rt_internal.h"
+
+using namespace rt;
+
+namespace {
+
+__global__ void k_aos2soa(int n, int nc, const double *__restrict__ in, double *__restrict__ out) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n * nc) return;
+    int i = (int)(t / nc), k = (int)(t % nc);
+    out[(long long)k * n + i] = in[t];
+}
+
+__global__ void k_soa2aos(int n, int nc, const double *__restrict__ in, double *__restrict__ out) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n * nc) return;
+    int i = (int)(t / nc), k = (int)(t % nc);
+    out[t] = in[(long long)k * n + i];
+}
+
+template <class F>
+rt_status guarded(rt_ctx *ctx, F &&f) {
+    if (!ctx) return RT_EINVAL;
+    try {
+        return f();
+    } catch (const Error &e) {
+        ctx->lastError = e.msg;
+        return e.status;
+    } catch (const std::exception &e) {
+        ctx->lastError = e.what();
+        return RT_EINVAL;
+    }
+}
+
+// host AoS (n x nc) -> device SoA, through a staging buffer
+void upload_soa(rt_ctx *ctx, const double *h, int n, int nc, DBuf<double> &dst) {
+    dst.alloc((size_t)n * nc);
+    if (n == 0) return;
+    if (nc == 1) {
+        RT_CUDA(cudaMemcpyAsync(dst.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        return;
+    }
+    DBuf<double> st;
+    st.upload(h, (size_t)n * nc, ctx->stream);
+    k_aos2soa<<<nblocks((long long)n * nc), RT_BLOCK, 0, ctx->stream>>>(n, nc, st.p, dst.p);
+    RT_CHECK_LAUNCH();
+    RT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void download_aos(rt_ctx *ctx, const DBuf<double> &src, int n, int nc, double *h) {
+    if (n == 0) return;
+    if (nc == 1) {
+        RT_CUDA(cudaMemcpyAsync(h, src.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return;
+    }
+    DBuf<double> st;
+    st.alloc((size_t)n * nc);
+    k_soa2aos<<<nblocks((long long)n * nc), RT_BLOCK, 0, ctx->stream>>>(n, nc, src.p, st.p);
+    RT_CHECK_LAUNCH();
+    RT_CUDA(cudaMemcpyAsync(h, st.p, sizeof(double) * n * nc, cudaMemcpyDeviceToHost, ctx->stream));
+    RT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+template <class T>
+void upload_vec(rt_ctx *ctx, const std::vector<T> &v, DBuf<T> &d) {
+    d.upload(v.data(), v.size(), ctx->stream);
+}
+
+std::vector<double> aos_to_soa_host(const double *a, int n, int nc) {
+    std::vector<double> o((size_t)n * nc);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < nc; ++k) o[(size_t)k * n + i] = a[(size_t)i * nc + k];
+    return o;
+}
+
+}  // namespace
+
+namespace rt {
+void launch_count(rt_ctx *ctx, int n) { ctx->kernelLaunches += n; }
+}  // namespace rt
+
+extern "C" {
+
+const char *rt_status_string(rt_status s) {
+    switch (s) {
+    case RT_OK: return "RT_OK";
+    case RT_EINVAL: return "RT_EINVAL";
+    case RT_ENOCONV: return "RT_ENOCONV";
+    case RT_ENAN: return "RT_ENAN";
+    case RT_ETIMEOUT: return "RT_ETIMEOUT";
+    case RT_EOOM: return "RT_EOOM";
+    case RT_ECUDA: return "RT_ECUDA";
+    case RT_ENOTREADY: return "RT_ENOTREADY";
+    default: return "unknown";
+    }
+}
+
+rt_status rt_ctx_create(rt_ctx **out, int32_t device) {
+    if (!out) return RT_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return RT_ECUDA;
+    if (device < 0 || device >= n) return RT_EINVAL;
+    rt_ctx *ctx = new rt_ctx();
+    ctx->device = device;
+    rt_status s = guarded(ctx, [&]() -> rt_status {
+        RT_CUDA(cudaSetDevice(device));
+        RT_CUDA(cudaDeviceGetAttribute(&ctx->numSMs, cudaDevAttrMultiProcessorCount, device));
+        RT_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        reduce_init(ctx);
+        return RT_OK;
+    });
+    if (s != RT_OK) {
+        delete ctx;
+        return s;
+    }
+    *out = ctx;
+    return RT_OK;
+}
+
+rt_status rt_ctx_destroy(rt_ctx *ctx) {
+    if (!ctx) return RT_EINVAL;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->red.hostResult) cudaFreeHost(ctx->red.hostResult);
+    cudaStream_t st = ctx->stream;
+    delete ctx;   // DBuf destructors free device memory
+    if (st) cudaStreamDestroy(st);
+    return RT_OK;
+}
+
+const char *rt_last_error(const rt_ctx *ctx) { return ctx ? ctx->lastError.c_str() : "null context"; }
+
+rt_status rt_sync(rt_ctx *ctx) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return RT_OK;
+    });
+}
+
+rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(md && md->nCells > 0 && md->nFaces >= 0 && md->nBFaces >= 0 && md->nPatches >= 0,
+                   RT_EINVAL, "bad mesh sizes");
+        RT_CUDA(cudaSetDevice(ctx->device));
+        const int N = md->nCells, F = md->nFaces, NB = md->nBFaces;
+        // ---- validate addressing -------------------------------------------
+        for (int f = 0; f < F; ++f) {
+            int o = md->owner[f], n = md->neighbour[f];
+            RT_REQUIRE(o >= 0 && n < N && o < n, RT_EINVAL, "face " + std::to_string(f) + ": need 0 <= owner < neighbour < nCells");
+            if (f > 0) {
+                int po = md->owner[f - 1], pn = md->neighbour[f - 1];
+                RT_REQUIRE(po < o || (po == o && pn < n), RT_EINVAL, "faces are not in upper-triangular order");
+            }
+        }
+        for (int b = 0; b < NB; ++b)
+            RT_REQUIRE(md->bCell[b] >= 0 && md->bCell[b] < N, RT_EINVAL, "bad boundary face cell");
+        int acc = 0;
+        for (int p = 0; p < md->nPatches; ++p) {
+            RT_REQUIRE(md->patchStart[p] == acc && md->patchSize[p] >= 0, RT_EINVAL, "patches must tile the boundary faces in order");
+            acc += md->patchSize[p];
+        }
+        RT_REQUIRE(acc == NB, RT_EINVAL, "patch sizes do not add up to nBFaces");
+
+        DevMesh &m = ctx->mesh;
+        m.N = N; m.F = F; m.NB = NB; m.nPatches = md->nPatches;
+        for (int k = 0; k < 3; ++k) m.solveDir[k] = md->solveDir[k];
+        cudaStream_t s = ctx->stream;
+        m.owner.upload(md->owner, F, s);
+        m.neighbour.upload(md->neighbour, F, s);
+        upload_vec(ctx, aos_to_soa_host(md->Sf, F, 3), m.Sf);
+        m.magSf.upload(md->magSf, F, s);
+        m.w.upload(md->weights, F, s);
+        m.deltaCoeffs.upload(md->deltaCoeffs, F, s);
+        upload_vec(ctx, aos_to_soa_host(md->C, N, 3), m.C);
+        m.V.upload(md->V, N, s);
+        m.bCell.upload(md->bCell, NB, s);
+        upload_vec(ctx, aos_to_soa_host(md->bSf, NB, 3), m.bSf);
+        m.bmagSf.upload(md->bmagSf, NB, s);
+        m.bDelta.upload(md->bDeltaCoeffs, NB, s);
+        {
+            std::vector<double> ctf((size_t)3 * NB);
+            for (int b = 0; b < NB; ++b)
+                for (int d = 0; d < 3; ++d)
+                    ctf[(size_t)d * NB + b] = md->bCf[3 * b + d] - md->C[3 * md->bCell[b] + d];
+            upload_vec(ctx, ctf, m.bCtoF);
+        }
+        m.patchStartH.assign(md->patchStart, md->patchStart + md->nPatches);
+        m.patchSizeH.assign(md->patchSize, md->patchSize + md->nPatches);
+        {
+            std::vector<int> bp(NB);
+            for (int p = 0; p < md->nPatches; ++p)
+                for (int i = 0; i < md->patchSize[p]; ++i) bp[md->patchStart[p] + i] = p;
+            upload_vec(ctx, bp, m.bPatch);
+        }
+        // ---- ELL adjacency in face order ---------------------------------
+        std::vector<int> cnt(N, 0);
+        for (int f = 0; f < F; ++f) { cnt[md->owner[f]]++; cnt[md->neighbour[f]]++; }
+        int ns = 0;
+        for (int c = 0; c < N; ++c) ns = std::max(ns, cnt[c]);
+        m.nSlots = ns;
+        std::vector<int> ef((size_t)std::max(ns, 1) * N, -1), en((size_t)std::max(ns, 1) * N, -1);
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int f = 0; f < F; ++f) {
+            int o = md->owner[f], n = md->neighbour[f];
+            ef[(size_t)cnt[o] * N + o] = f; en[(size_t)cnt[o] * N + o] = n; cnt[o]++;
+            ef[(size_t)cnt[n] * N + n] = f; en[(size_t)cnt[n] * N + n] = o; cnt[n]++;
+        }
+        upload_vec(ctx, ef, m.ellFace);
+        upload_vec(ctx, en, m.ellNbr);
+        // ---- boundary CSR ----------------------------------------------------
+        std::vector<int> bs(N + 1, 0), bl(NB);
+        for (int b = 0; b < NB; ++b) bs[md->bCell[b] + 1]++;
+        for (int c = 0; c < N; ++c) bs[c + 1] += bs[c];
+        {
+            std::vector<int> pos(bs.begin(), bs.end() - 1);
+            for (int b = 0; b < NB; ++b) bl[pos[md->bCell[b]]++] = b;
+        }
+        upload_vec(ctx, bs, m.bStart);
+        upload_vec(ctx, bl, m.bList);
+        std::vector<int> bc;
+        for (int c = 0; c < N; ++c) if (bs[c + 1] > bs[c]) bc.push_back(c);
+        m.nBCells = (int)bc.size();
+        upload_vec(ctx, bc, m.bCells);
+        // ---- level schedule ------------------------------------------------
+        std::vector<int> lev(N, 0);
+        for (int f = 0; f < F; ++f) {
+            int o = md->owner[f], n = md->neighbour[f];
+            lev[n] = std::max(lev[n], lev[o] + 1);
+        }
+        int nl = 0;
+        for (int c = 0; c < N; ++c) nl = std::max(nl, lev[c] + 1);
+        m.nLevels = nl;
+        m.levelStartH.assign(nl + 1, 0);
+        for (int c = 0; c < N; ++c) m.levelStartH[lev[c] + 1]++;
+        for (int l = 0; l < nl; ++l) m.levelStartH[l + 1] += m.levelStartH[l];
+        std::vector<int> lc(N), pos(m.levelStartH.begin(), m.levelStartH.end() - 1);
+        for (int c = 0; c < N; ++c) lc[pos[lev[c]]++] = c;
+        upload_vec(ctx, lc, m.levelCells);
+        // ---- scratch ---------------------------------------------------------
+        size_t need = (size_t)N * 160 + (size_t)F * 24 + (size_t)NB * 96 + 4096;
+        ctx->work.a.alloc(need);
+        RT_CUDA(cudaStreamSynchronize(s));
+        ctx->meshReady = true;
+        ctx->cs.ready = false;
+        return RT_OK;
+    });
+}
+
+rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params *mp,
+                        const rt_case_ctl *ctl) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
+        RT_REQUIRE(bc && mp && ctl, RT_EINVAL, "null argument");
+        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_FENEP_LOG, RT_EINVAL,
+                   "unknown constitutive model");
+        RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
+        RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
+        RT_REQUIRE(ctl->divU >= RT_LIM_NONE && ctl->divU <= RT_LIM_SUPERBEE &&
+                       ctl->divTheta >= RT_LIM_NONE && ctl->divTheta <= RT_LIM_SUPERBEE,
+                   RT_EINVAL, "unknown GaussDefCmpw limiter");
+        RT_REQUIRE(mp->model != RT_MODEL_FENEP_LOG || mp->L2 > 3.0, RT_EINVAL, "FENE-P needs L2 > 3");
+        DevMesh &m = ctx->mesh;
+        DevCase &c = ctx->cs;
+        RT_REQUIRE(ctl->pRefCell >= 0 && ctl->pRefCell < m.N, RT_EINVAL, "pRefCell out of range");
+        c.mp = *mp;
+        c.ctl = *ctl;
+        const int P = m.nPatches, NB = m.NB, N = m.N;
+        c.kindU.assign(bc->U, bc->U + P);
+        c.kindP.assign(bc->p, bc->p + P);
+        c.kindTheta.assign(bc->theta, bc->theta + P);
+        c.kindTau.assign(bc->tau, bc->tau + P);
+        for (int p = 0; p < P; ++p) {
+            RT_REQUIRE(c.kindU[p] == RT_BC_FIXED || c.kindU[p] == RT_BC_ZEROGRAD, RT_EINVAL, "U: unsupported BC");
+            RT_REQUIRE(c.kindP[p] == RT_BC_FIXED || c.kindP[p] == RT_BC_ZEROGRAD, RT_EINVAL, "p: unsupported BC");
+            RT_REQUIRE(c.kindTheta[p] == RT_BC_FIXED || c.kindTheta[p] == RT_BC_ZEROGRAD, RT_EINVAL, "theta: unsupported BC");
+            RT_REQUIRE(c.kindTau[p] >= RT_BC_FIXED && c.kindTau[p] <= RT_BC_LINEXTRAP, RT_EINVAL, "tau: unsupported BC");
+        }
+        auto per_face = [&](const std::vector<int> &k, DBuf<int> &d) {
+            std::vector<int> v(NB);
+            for (int p = 0; p < P; ++p)
+                for (int i = 0; i < m.patchSizeH[p]; ++i) v[m.patchStartH[p] + i] = k[p];
+            upload_vec(ctx, v, d);
+        };
+        per_face(c.kindU, c.bkU);
+        per_face(c.kindP, c.bkP);
+        per_face(c.kindTheta, c.bkTh);
+        per_face(c.kindTau, c.bkTau);
+        upload_soa(ctx, bc->Ub, NB, 3, c.UbFixed);
+        upload_soa(ctx, bc->pb, NB, 1, c.pbFixed);
+        upload_soa(ctx, bc->thetab, NB, 6, c.thetabFixed);
+        upload_soa(ctx, bc->taub, NB, 6, c.taubFixed);
+        // state: U = p = theta = tau = 0, eigVals = eigVecs = I
+        c.U.alloc(3 * (size_t)N); c.U.zero(ctx->stream);
+        c.p.alloc(N); c.p.zero(ctx->stream);
+        c.theta.alloc(6 * (size_t)N); c.theta.zero(ctx->stream);
+        c.tau.alloc(6 * (size_t)N); c.tau.zero(ctx->stream);
+        c.Ub.alloc(3 * (size_t)NB); c.pb.alloc(NB); c.thetab.alloc(6 * (size_t)NB); c.taub.alloc(6 * (size_t)NB);
+        c.phi.alloc(m.F); c.phib.alloc(NB);
+        c.eigVals.alloc(3 * (size_t)N);
+        c.eigVecs.alloc(9 * (size_t)N);
+        init_fields(ctx);
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        c.ready = true;
+        return RT_OK;
+    });
+}
+
+static void field_info(rt_ctx *ctx, int field, DBuf<double> **in, DBuf<double> **bd, int *nc, int *nIn) {
+    DevCase &c = ctx->cs;
+    *nIn = ctx->mesh.N;
+    switch (field) {
+    case RT_FIELD_U: *in = &c.U; *bd = &c.Ub; *nc = 3; break;
+    case RT_FIELD_P: *in = &c.p; *bd = &c.pb; *nc = 1; break;
+    case RT_FIELD_PHI: *in = &c.phi; *bd = &c.phib; *nc = 1; *nIn = ctx->mesh.F; break;
+    case RT_FIELD_THETA: *in = &c.theta; *bd = &c.thetab; *nc = 6; break;
+    case RT_FIELD_TAU: *in = &c.tau; *bd = &c.taub; *nc = 6; break;
+    case RT_FIELD_EIGVALS: *in = &c.eigVals; *bd = nullptr; *nc = 3; break;
+    case RT_FIELD_EIGVECS: *in = &c.eigVecs; *bd = nullptr; *nc = 9; break;
+    default: throw Error{RT_EINVAL, "unknown field id"};
+    }
+}
+
+rt_status rt_field_set(rt_ctx *ctx, int32_t field, const double *internal, const double *boundary) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
+        DBuf<double> *in, *bd;
+        int nc, nIn;
+        field_info(ctx, field, &in, &bd, &nc, &nIn);
+        if (internal) upload_soa(ctx, internal, nIn, nc, *in);
+        if (boundary) {
+            RT_REQUIRE(bd != nullptr, RT_EINVAL, "field has no boundary values");
+            upload_soa(ctx, boundary, ctx->mesh.NB, nc, *bd);
+        }
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return RT_OK;
+    });
+}
+
+rt_status rt_field_get(rt_ctx *ctx, int32_t field, double *internal, double *boundary) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
+        DBuf<double> *in, *bd;
+        int nc, nIn;
+        field_info(ctx, field, &in, &bd, &nc, &nIn);
+        if (internal) download_aos(ctx, *in, nIn, nc, internal);
+        if (boundary) {
+            RT_REQUIRE(bd != nullptr, RT_EINVAL, "field has no boundary values");
+            download_aos(ctx, *bd, ctx->mesh.NB, nc, boundary);
+        }
+        return RT_OK;
+    });
+}
+
+rt_status rt_ldu_solve(rt_ctx *ctx, const double *diag, const double *upper, const double *lower,
+                       const double *source, double *psi, int32_t ncmpt, const rt_solver_ctl *ctl,
+                       rt_solver_perf *perf) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
+        RT_REQUIRE(ncmpt >= 1 && ncmpt <= 6, RT_EINVAL, "ncmpt must be 1..6");
+        RT_REQUIRE(diag && upper && lower && source && psi && ctl && perf, RT_EINVAL, "null argument");
+        RT_REQUIRE(ctl->solver == RT_SOLVER_PCG || ctl->solver == RT_SOLVER_PBICGSTAB, RT_EINVAL, "unknown solver");
+        RT_REQUIRE(ctl->preconditioner >= RT_PRECOND_NONE && ctl->preconditioner <= RT_PRECOND_DIAGONAL,
+                   RT_EINVAL, "unknown preconditioner");
+        const int N = ctx->mesh.N, F = ctx->mesh.F;
+        DBuf<double> d, u, l, b, x;
+        cudaStream_t s = ctx->stream;
+        d.upload(diag, N, s);
+        u.upload(upper, F, s);
+        l.upload(lower, F, s);
+        b.upload(source, (size_t)ncmpt * N, s);
+        x.upload(psi, (size_t)ncmpt * N, s);
+        SolveArgs a{d.p, u.p, l.p, b.p, x.p, ncmpt, (1u << ncmpt) - 1u, *ctl};
+        rt_status st = ldu_solve_device(ctx, a, perf);
+        RT_CUDA(cudaMemcpyAsync(psi, x.p, sizeof(double) * ncmpt * N, cudaMemcpyDeviceToHost, s));
+        RT_CUDA(cudaStreamSynchronize(s));
+        return st;
+    });
+}
+
+rt_status rt_residual(rt_ctx *ctx, const double *diag, const double *upper, const double *lower,
+                      const double *source, const double *psi, double *residual) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
+        RT_REQUIRE(diag && upper && lower && source && psi && residual, RT_EINVAL, "null argument");
+        const int N = ctx->mesh.N, F = ctx->mesh.F;
+        DBuf<double> d, u, l, b, x;
+        cudaStream_t s = ctx->stream;
+        d.upload(diag, N, s);
+        u.upload(upper, F, s);
+        l.upload(lower, F, s);
+        b.upload(source, N, s);
+        x.upload(psi, N, s);
+        *residual = residual_device(ctx, d.p, u.p, l.p, b.p, x.p);
+        return RT_OK;
+    });
+}
+
+rt_status rt_op_grad(rt_ctx *ctx, const double *psi, const double *psib, double *grad) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
+        RT_REQUIRE(psi && psib && grad, RT_EINVAL, "null argument");
+        const int N = ctx->mesh.N, NB = ctx->mesh.NB;
+        DBuf<double> x, xb, g;
+        x.upload(psi, N, ctx->stream);
+        xb.upload(psib, NB, ctx->stream);
+        g.alloc(3 * (size_t)N);
+        grad_scalar(ctx, x.p, xb.p, g.p);
+        download_aos(ctx, g, N, 3, grad);
+        return RT_OK;
+    });
+}
+
+rt_status rt_op_eig(rt_ctx *ctx, int32_t n, const double *theta, double *eigVals, double *eigVecs) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(n >= 0 && theta && eigVals && eigVecs, RT_EINVAL, "bad argument");
+        if (n == 0) return RT_OK;
+        DBuf<double> th, ev, vv;
+        upload_soa(ctx, theta, n, 6, th);
+        ev.alloc(3 * (size_t)n);
+        vv.alloc(9 * (size_t)n);
+        eig_cells(ctx, n, th.p, ev.p, vv.p);
+        download_aos(ctx, ev, n, 3, eigVals);
+        download_aos(ctx, vv, n, 9, eigVecs);
+        return RT_OK;
+    });
+}
+
+rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *thetaPerf) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
+        RT_REQUIRE(thetaPerf, RT_EINVAL, "null perf");
+        DBuf<double> g;
+        if (gradU) upload_soa(ctx, gradU, ctx->mesh.N, 9, g);
+        rt_status st = constitutive_correct(ctx, gradU ? g.p : nullptr, thetaPerf);
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return st;
+    });
+}
+
+rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
+        RT_REQUIRE(nSteps >= 0, RT_EINVAL, "nSteps must be >= 0");
+        rt_step_perf local{};
+        rt_status st = RT_OK;
+        for (int i = 0; i < nSteps && st == RT_OK; ++i) {
+            local = rt_step_perf{};
+            st = step_once(ctx, &local);
+        }
+        if (perf) *perf = local;
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return st;
+    });
+}
+
+}  // extern "C"

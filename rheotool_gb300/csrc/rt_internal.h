@@ -1,0 +1,200 @@
+// rt_internal.h — device-side data structures shared by the librheogpu
+// translation units.  All device fields are structure-of-arrays: a field with
+// nc components over n entries is one allocation laid out component-major
+// (component k of entry i at [k*n + i]), so every kernel reads and writes
+// contiguous, coalesced runs of doubles.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/rheogpu.h"
+
+#define RT_BLOCK 256
+
+namespace rt {
+
+// ---------------------------------------------------------------------------
+// error plumbing: every CUDA call goes through RT_CUDA, which records the
+// failing call in the context and returns RT_ECUDA to the C caller.
+// ---------------------------------------------------------------------------
+struct Error {
+    rt_status status;
+    std::string msg;
+};
+
+#define RT_CUDA(call)                                                              \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            throw ::rt::Error{RT_ECUDA, std::string(#call) + ": " +                \
+                                            cudaGetErrorString(e_)};               \
+    } while (0)
+
+#define RT_CHECK_LAUNCH() RT_CUDA(cudaGetLastError())
+
+#define RT_REQUIRE(cond, code, what)                                               \
+    do {                                                                           \
+        if (!(cond)) throw ::rt::Error{(code), (what)};                            \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Error{RT_EOOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+        }
+        n = count;
+    }
+    void zero(cudaStream_t s) {
+        if (p) RT_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    void upload(const T *h, size_t count, cudaStream_t s) {
+        alloc(count);
+        if (count) RT_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    operator T *() const { return p; }
+};
+
+// ---------------------------------------------------------------------------
+// mesh: LDU addressing + geometry + cell-centric adjacency
+// ---------------------------------------------------------------------------
+struct DevMesh {
+    int N = 0, F = 0, NB = 0, nPatches = 0;
+    int nSlots = 0;          // max internal faces per cell (ELL width)
+    int solveDir[3] = {1, 1, 1};
+    // faces (F)
+    DBuf<int> owner, neighbour;
+    DBuf<double> Sf;         // 3F SoA
+    DBuf<double> magSf, w, deltaCoeffs;
+    // cells (N)
+    DBuf<double> C;          // 3N SoA
+    DBuf<double> V;
+    // boundary faces (NB)
+    DBuf<int> bCell;
+    DBuf<double> bSf;        // 3NB SoA
+    DBuf<double> bmagSf, bDelta;
+    DBuf<double> bCtoF;      // 3NB SoA, Cf - C_P
+    DBuf<int> bPatch;
+    // ELL adjacency: slot s of cell c at [s*N + c], sorted by face index,
+    // padding -1 at the end
+    DBuf<int> ellFace, ellNbr;
+    // boundary faces of each cell, CSR over cells in boundary-face order
+    DBuf<int> bStart, bList;
+    // cells that own at least one boundary face
+    DBuf<int> bCells;
+    int nBCells = 0;
+    // level schedule for the triangular sweeps: cells sorted by level,
+    // level(c) = 1 + max(level of lower neighbours)
+    int nLevels = 0;
+    std::vector<int> levelStartH;
+    DBuf<int> levelCells;
+    // host copies needed by the host-side orchestration
+    std::vector<int> patchStartH, patchSizeH;
+};
+
+// ---------------------------------------------------------------------------
+// case + device fields
+// ---------------------------------------------------------------------------
+struct DevCase {
+    bool ready = false;
+    rt_model_params mp{};
+    rt_case_ctl ctl{};
+    std::vector<int> kindU, kindP, kindTheta, kindTau;   // per patch
+    DBuf<int> bkU, bkP, bkTh, bkTau;                      // per boundary face
+    DBuf<double> UbFixed, pbFixed, thetabFixed, taubFixed;
+    // state (SoA)
+    DBuf<double> U, Ub, p, pb, phi, phib, theta, thetab, tau, taub, eigVals, eigVecs;
+};
+
+// scratch arrays of the step, allocated once per mesh
+struct Work {
+    DBuf<double> a;   // generic pool, carved by the step code
+    size_t used = 0;
+    double *take(size_t n) {
+        size_t al = (n + 31) & ~size_t(31);
+        if (used + al > a.n) throw Error{RT_EOOM, "work pool exhausted"};
+        double *p = a.p + used;
+        used += al;
+        return p;
+    }
+};
+
+// reduction buffers
+struct Reduce {
+    int nBlocks = 0;
+    DBuf<double> partial;   // [8 slots][6 comps][nBlocks]
+    DBuf<double> result;    // [8 slots][6 comps]
+    double *hostResult = nullptr;  // pinned
+};
+
+}  // namespace rt
+
+struct rt_ctx {
+    int device = 0;
+    int numSMs = 0;
+    cudaStream_t stream = nullptr;
+    std::string lastError;
+    rt::DevMesh mesh;
+    rt::DevCase cs;
+    rt::Reduce red;
+    rt::Work work;
+    rt::DBuf<double> kws;        // Krylov workspace: 8 vectors x 6 comps x N + rD
+    rt::DBuf<double> scal;       // device scalars of the Krylov loops [32 slots][8]
+    bool meshReady = false;
+    long long kernelLaunches = 0;
+};
+
+namespace rt {
+
+// kernels and host helpers implemented across the .cu files -----------------
+// krylov.cu
+struct SolveArgs {
+    const double *diag, *upper, *lower;   // complete matrix (device)
+    const double *source;                 // nc*N component-major (device)
+    double *psi;                          // nc*N (device)
+    int nc;
+    unsigned validMask;                   // components to solve
+    rt_solver_ctl ctl;
+};
+rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf);
+double residual_device(rt_ctx *ctx, const double *diag, const double *upper,
+                       const double *lower, const double *b, const double *x);
+void reduce_init(rt_ctx *ctx);
+
+// fv.cu
+void grad_scalar(rt_ctx *ctx, const double *x, const double *xb, double *g);
+void launch_count(rt_ctx *ctx, int n = 1);
+
+// constitutive.cu
+void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double *eigVecs);
+rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf);
+
+// step.cu
+rt_status step_once(rt_ctx *ctx, rt_step_perf *perf);
+void init_fields(rt_ctx *ctx);
+
+inline int nblocks(long long n, int b = RT_BLOCK) { return (int)((n + b - 1) / b); }
+
+}  // namespace rt
