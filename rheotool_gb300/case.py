@@ -172,11 +172,11 @@ def lid_profile(Cf: np.ndarray) -> np.ndarray:
 
 
 def cavity_case(n: int = 64, model: str = "Oldroyd-BLog", Wi: float = 0.5, beta: float = 0.5,
-                Re: float = 0.01, dt: float = 1e-3, **model_kw) -> Case:
+                Re: float = 0.01, dt: float = 1e-3, mesh: Optional[Mesh] = None, **model_kw) -> Case:
     """Lid-driven cavity: U_lid = 16x^2(1-x)^2, lambda = Wi (U = L = 1),
     etaS = beta, etaP = 1 - beta, rho = Re (eta0 = 1); Euler, GaussDefCmpw
     cubista, p PCG-DIC 1e-8, U/theta PBiCGStab-DILU 1e-10."""
-    mesh = cavity_mesh(n)
+    mesh = cavity_mesh(n) if mesh is None else mesh
     mdl = Model(model, rho=Re, etaS=beta, etaP=1.0 - beta, lambda_=Wi, **model_kw)
     bcs = {
         "movingLid": dict(WALL_VE, U=("fixedValue", lid_profile)),

@@ -1,0 +1,304 @@
+"""Known-answer tests that pin the FP64 CPU oracle.
+
+The reference (rheoTool on OpenFOAM v9 + Eigen) cannot be built here and ships
+no golden fields, so the oracle is pinned by closed-form rheology, by the
+conformation-tensor form of each model integrated independently with scipy,
+by dense linear algebra, and by exactness properties of the discretisation.
+The committed golden vectors in tests/golden/ freeze these results.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from oracle.pyoracle import Oracle
+from rheotool_gb300.case import Fields, SolverControl, cavity_case, contraction_case, channel_case
+from rheotool_gb300.mesh import cavity_mesh, contraction_mesh
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+# ---------------------------------------------------------------------------
+# eigen decomposition
+# ---------------------------------------------------------------------------
+def test_eig3_matches_numpy():
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        s = rng.normal(size=6) * rng.choice([1e-3, 1.0, 30.0])
+        mu, V = pyoracle.eig3(s)
+        A = np.array([[s[0], s[1], s[2]], [s[1], s[3], s[4]], [s[2], s[4], s[5]]])
+        w = np.linalg.eigvalsh(A)
+        scale = max(np.abs(w).max(), 1e-300)
+        assert np.max(np.abs(mu - w)) < 1e-14 * scale * 10
+        assert np.max(np.abs(V @ np.diag(mu) @ V.T - A)) < 1e-13 * scale * 10
+        assert np.max(np.abs(V.T @ V - np.eye(3))) < 1e-14
+        assert np.all(np.diff(mu) >= 0)
+
+
+def test_eig3_exact_cases():
+    mu, V = pyoracle.eig3([0, 0, 0, 0, 0, 0])
+    assert np.array_equal(mu, [0, 0, 0]) and np.array_equal(V, np.eye(3))
+    mu, V = pyoracle.eig3([3.0, 0, 0, 1.0, 0, 2.0])
+    assert np.array_equal(mu, [1.0, 2.0, 3.0])
+    assert np.array_equal(np.abs(V), np.eye(3)[:, [1, 2, 0]])
+    # a 2-D conformation keeps e_z exactly and its eigenvalue exactly
+    mu, V = pyoracle.eig3([0.3, 0.7, 0.0, -0.2, 0.0, 0.0])
+    k = int(np.argmax(np.abs(V[2])))
+    assert V[2, k] in (1.0, -1.0) and mu[k] == 0.0
+    assert np.all(V[:2, k] == 0.0) and np.all(V[2, [i for i in range(3) if i != k]] == 0.0)
+
+
+# ---------------------------------------------------------------------------
+# LDU solvers against dense solves
+# ---------------------------------------------------------------------------
+def dense(mesh, diag, upper, lower):
+    A = np.diag(diag)
+    A[mesh.neighbour, mesh.owner] = lower
+    A[mesh.owner, mesh.neighbour] = upper
+    return A
+
+
+def test_pcg_dic_matches_dense_solve():
+    mesh = cavity_mesh(9)
+    rng = np.random.default_rng(2)
+    g = 1.0 + rng.random(mesh.nFaces)
+    diag = np.zeros(mesh.nCells)
+    np.subtract.at(diag, mesh.owner, g)
+    np.subtract.at(diag, mesh.neighbour, g)
+    diag[0] *= 2.0                     # setReference makes it definite
+    b = rng.normal(size=mesh.nCells)
+    x = np.zeros(mesh.nCells)
+    o = Oracle(cavity_case(9))
+    p = o.ldu_solve(diag, g, g, b, x, SolverControl("PCG", "DIC", 1e-13, 0, 0, 1000))
+    xd = np.linalg.solve(dense(mesh, diag, g, g), b)
+    assert p.converged
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+    # DIC must beat no preconditioning
+    x2 = np.zeros(mesh.nCells)
+    p2 = o.ldu_solve(diag, g, g, b, x2, SolverControl("PCG", "none", 1e-13, 0, 0, 1000))
+    assert p.nIterations < p2.nIterations
+
+
+@pytest.mark.parametrize("pre", ["DILU", "diagonal", "none"])
+def test_pbicgstab_matches_dense_solve(pre):
+    mesh = contraction_mesh(6, 5, 4, 2, 3, 2.0, 2.0)
+    rng = np.random.default_rng(3)
+    phi = rng.normal(size=mesh.nFaces)
+    u = (phi >= 0).astype(float)
+    lower = -u * phi - 1.0
+    upper = (1 - u) * phi - 1.0
+    diag = np.zeros(mesh.nCells)
+    np.subtract.at(diag, mesh.owner, lower)
+    np.subtract.at(diag, mesh.neighbour, upper)
+    diag += 0.5
+    b = rng.normal(size=mesh.nCells)
+    x = np.zeros(mesh.nCells)
+    p = Oracle(contraction_case(mesh)).ldu_solve(diag, upper, lower, b, x,
+                                                  SolverControl("PBiCGStab", pre, 1e-13, 0, 0, 2000))
+    xd = np.linalg.solve(dense(mesh, diag, upper, lower), b)
+    assert p.converged
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+
+
+def test_dilu_preconditioner_is_exact_for_tridiagonal():
+    # D-ILU of a tridiagonal matrix has no fill-in: one application solves it
+    mesh = cavity_mesh(1, ny=12)       # a 1 x 12 column: tridiagonal LDU
+    rng = np.random.default_rng(4)
+    lower = -1.0 - rng.random(mesh.nFaces)
+    upper = -1.0 - rng.random(mesh.nFaces)
+    diag = 4.0 + rng.random(mesh.nCells)
+    b = rng.normal(size=mesh.nCells)
+    x = np.zeros(mesh.nCells)
+    p = Oracle(cavity_case(mesh=mesh)).ldu_solve(diag, upper, lower, b, x,
+                                         SolverControl("PBiCGStab", "DILU", 1e-14, 0, 0, 10))
+    assert p.nIterations == 1
+    assert np.allclose(x, np.linalg.solve(dense(mesh, diag, upper, lower), b), rtol=1e-12)
+
+
+def test_residual_normalisation_definition():
+    mesh = cavity_mesh(5)
+    rng = np.random.default_rng(5)
+    diag = 4.0 + rng.random(mesh.nCells)
+    upper = -rng.random(mesh.nFaces)
+    lower = -rng.random(mesh.nFaces)
+    b = rng.normal(size=mesh.nCells)
+    x = rng.normal(size=mesh.nCells)
+    A = dense(mesh, diag, upper, lower)
+    Ax = A @ x
+    pA = A.sum(1) * x.mean()
+    nf = np.sum(np.abs(Ax - pA) + np.abs(b - pA)) + 1e-20
+    ref = np.sum(np.abs(b - Ax)) / nf
+    got = Oracle(cavity_case(5)).residual(diag, upper, lower, b, x)
+    assert abs(got - ref) < 1e-13 * ref
+
+
+# ---------------------------------------------------------------------------
+# discretisation exactness
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mesh_fn", [lambda: cavity_mesh(7), lambda: contraction_mesh(6, 5, 4, 2, 3, 2.0, 2.0)])
+def test_gauss_gradient_exact_for_linear_fields(mesh_fn):
+    mesh = mesh_fn()
+    a = np.array([0.3, -1.7, 2.2])
+    if mesh.solveDir[2] == 0:
+        a[2] = 0.0
+    psi = mesh.C @ a + 0.5
+    psib = mesh.bCf @ a + 0.5
+    case = cavity_case(7) if mesh.solveDir[2] == 0 else contraction_case(mesh)
+    g = Oracle(case).grad(psi, psib)
+    assert np.max(np.abs(g - a)) < 1e-11
+
+
+# ---------------------------------------------------------------------------
+# homogeneous flows (0-D driver, rheoTestFoam style): imposed grad U
+# ---------------------------------------------------------------------------
+def zero_d(model, lam, etaP, dt, **kw):
+    """Four uniform cells with phi = 0 and an imposed grad U.  theta starts at
+    diag(1e-8, -1e-8, 0): from exactly theta = 0 with R = I, decomposeGradU
+    gives B = 0 and Omega.theta - theta.Omega = 0 under pure shear, so the
+    log-conformation update (rheoTool's as well) would stay at rest."""
+    case = cavity_case(2, model=model, Wi=lam, beta=1.0 - etaP, Re=1.0, dt=dt, **kw)
+    f = Fields.zeros(case.mesh)
+    f.theta[:, 0], f.theta[:, 3] = 1e-8, -1e-8
+    f.eigVals[:, 0], f.eigVals[:, 1] = np.exp(1e-8), np.exp(-1e-8)
+    o = Oracle(case, f)
+    return case, o
+
+
+def shear_L(rate, n):
+    L = np.zeros((n, 9))
+    L[:, 3] = rate            # d u_x / d y
+    return L
+
+
+def test_oldroydb_startup_shear_closed_form():
+    lam, etaP, rate = 0.5, 0.7, 2.0
+    dt = lam / 2000
+    case, o = zero_d("Oldroyd-BLog", lam, etaP, dt)
+    L = shear_L(rate, case.mesh.nCells)
+    t = 0.0
+    for _ in range(2000):
+        o.constitutive_correct(L)
+        t += dt
+    txy = o.f.tau[:, 1].mean()
+    exact = etaP * rate * (1.0 - np.exp(-t / lam))
+    assert abs(txy - exact) < 2e-3 * exact
+
+
+def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
+    """Steady simple shear of the conformation-tensor form, integrated with
+    scipy (an independent formulation of the same model)."""
+    from scipy.integrate import solve_ivp
+    kap = np.zeros((3, 3))
+    kap[0, 1] = rate
+    I = np.eye(3)
+
+    def rhs(t, y):
+        A = y.reshape(3, 3)
+        if model == "Oldroyd-BLog":
+            g = A - I
+        elif model == "GiesekusLog":
+            g = (A - I) + alpha * (A - I) @ (A - I)
+        elif model == "PTTLog":
+            g = (1.0 + eps * (np.trace(A) - 3.0)) * (A - I)
+        else:
+            f = L2 / (L2 - np.trace(A))
+            a = L2 / (L2 - 3.0)
+            g = f * A - a * I
+        return (kap @ A + A @ kap.T - g / lam).reshape(-1)
+
+    sol = solve_ivp(rhs, (0, 60 * lam), I.reshape(-1), rtol=1e-12, atol=1e-14, method="LSODA")
+    A = sol.y[:, -1].reshape(3, 3)
+    if model == "FENE-PLog":
+        return (L2 / (L2 - np.trace(A))) * A - (L2 / (L2 - 3.0)) * I
+    return A - I
+
+
+@pytest.mark.parametrize("model,kw,ckw", [
+    ("Oldroyd-BLog", {}, {}),
+    ("GiesekusLog", {"alpha": 0.3}, {"alpha": 0.3}),
+    ("PTTLog", {"epsilon": 0.25}, {"eps": 0.25}),
+    ("FENE-PLog", {"L2": 100.0}, {"L2": 100.0}),
+])
+def test_steady_shear_matches_conformation_form(model, kw, ckw):
+    lam, etaP, rate = 1.0, 0.8, 1.5
+    dt = lam / 40
+    case, o = zero_d(model, lam, etaP, dt, **kw)
+    L = shear_L(rate, case.mesh.nCells)
+    for _ in range(int(60 * lam / dt)):
+        o.constitutive_correct(L)
+    tau = o.f.tau.mean(0)
+    ref = (etaP / lam) * conformation_steady(model, lam, rate, **ckw)
+    got = np.array([tau[0], tau[1], tau[2], tau[3], tau[4], tau[5]])
+    want = np.array([ref[0, 0], ref[0, 1], ref[0, 2], ref[1, 1], ref[1, 2], ref[2, 2]])
+    assert np.max(np.abs(got - want)) < 1e-7 * np.abs(want).max()
+    if model == "Oldroyd-BLog":
+        assert abs(tau[1] - etaP * rate) < 1e-8
+        assert abs((tau[0] - tau[3]) - 2 * etaP * lam * rate ** 2) < 1e-7
+
+
+# ---------------------------------------------------------------------------
+# time-step invariants
+# ---------------------------------------------------------------------------
+def test_step_conserves_mass_contraction():
+    case = contraction_case(contraction_mesh(8, 6, 4, 3, 3, 3.0, 3.0), dt=0.02)
+    o = Oracle(case)
+    perf = o.step(3)
+    assert perf.p.converged
+    m = case.mesh
+    div = np.zeros(m.nCells)
+    np.add.at(div, m.owner, o.f.phi)
+    np.subtract.at(div, m.neighbour, o.f.phi)
+    np.add.at(div, m.bCell, o.f.phib)
+    inflow = -o.f.phib[o.f.phib < 0].sum()
+    assert np.abs(div).sum() < 1e-6 * inflow
+    # global balance: what enters leaves
+    assert abs(o.f.phib.sum()) < 1e-6 * inflow
+
+
+def test_step_2d_keeps_out_of_plane_components_zero():
+    case = cavity_case(10, model="GiesekusLog", alpha=0.2)
+    o = Oracle(case)
+    perf = o.step(4)
+    assert np.all(o.f.U[:, 2] == 0.0)
+    assert np.all(o.f.theta[:, [2, 4]] == 0.0)
+    assert np.all(o.f.theta[:, 5] == 0.0)
+    assert perf.U[2].nIterations == -1 and perf.theta[2].nIterations == -1
+
+
+def test_poiseuille_channel_oldroydb():
+    """Fully developed Oldroyd-B channel flow: U is the Newtonian parabola of
+    eta0 and tau_xy = etaP dU/dy (2-D channel, inlet plug flow)."""
+    from rheotool_gb300.mesh import channel_mesh
+    mesh = channel_mesh(nx=30, ny=16, L=6.0, H=1.0, two_d=True)
+    case = channel_case(mesh, model="Oldroyd-BLog", U_in=1.0, dt=0.02, lambda_=0.1, beta=0.5)
+    o = Oracle(case)
+    o.step(150)
+    ij = mesh.cellIJK
+    col = ij[:, 0] == 24
+    y = mesh.C[col, 1]
+    order = np.argsort(y)
+    u = o.f.U[col, 0][order]
+    y = y[order]
+    exact = 6.0 * y * (1.0 - y)
+    assert np.max(np.abs(u - exact)) < 2e-2
+    dudy = 6.0 * (1.0 - 2.0 * y)
+    txy = o.f.tau[col, 1][order]
+    assert np.max(np.abs(txy - 0.5 * dudy)) < 6e-2
+
+
+# ---------------------------------------------------------------------------
+# golden vectors (frozen oracle output, regenerated by tests/golden/make_golden.py)
+# ---------------------------------------------------------------------------
+def test_golden_cavity_oracle():
+    path = os.path.join(GOLDEN, "cavity16_oldroydb_10steps.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden file missing")
+    g = np.load(path)
+    case = cavity_case(16)
+    o = Oracle(case)
+    o.step(10)
+    for name in ("U", "p", "theta", "tau", "phi"):
+        ref = g[name]
+        assert np.linalg.norm(getattr(o.f, name) - ref) <= 1e-12 * np.linalg.norm(ref), name
