@@ -1,0 +1,302 @@
+#!/usr/bin/env python
+"""bench.py — throughput of the rheoFoam segregated time step on GB300.
+
+Workload (one "step" = one rheoFoam time step: UEqn, SIMPLEC pEqn with a
+PCG-DIC pressure solve, GiesekusLog constitutive update with six
+PBiCGStab-DILU theta solves): 3-D planar 4:1 contraction, 1,000,000 hex cells,
+Giesekus-Log alpha = 0.1, Wi = 2, beta = 1/9, FP64 plain path, synthetic
+mesh and inputs (no dataset exists for it).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is device-timed (CUDA events on the library's
+stream) whole-job cell-steps/s with all fields resident in HBM; `e2e` is the
+same metric through the C ABI with host buffers (each step uploads U, p, phi
+and downloads U, p, phi, tau); `roofline` is for the operation with the
+largest device time, measured live with CUDA events; `cpu_baseline` is the
+FP64 CPU oracle on a bounded sample of the same workload.
+`--impl reference` times the reference algorithm on the host cores: the
+reference itself (rheoTool on OpenFOAM v9) cannot be built here, so its FP64
+CPU restatement (oracle/) runs instead, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s (1M-cell Giesekus)"
+UNIT = "cell-steps/s"
+WORKLOAD = ("3-D planar 4:1 contraction, 1,000,000 hex cells (266x100x50 bounding grid, graded), "
+            "GiesekusLog alpha=0.1, Wi=2, beta=1/9, rho=0.01, dt=5e-3, Euler, GaussDefCmpw cubista, "
+            "p PCG-DIC 1e-8, U/theta PBiCGStab-DILU 1e-10, FP64 plain path")
+SAMPLE_DIMS = dict(nx_up=67, nx_down=66, ny_in=25, ny_out=13, nz=25)   # 126,675 cells
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--small", action="store_true", help="126,675-cell sample instead of 1M (testing)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_case(small: bool):
+    from rheotool_gb300.case import contraction_case
+    from rheotool_gb300.mesh import contraction_mesh
+    if small:
+        return contraction_case(contraction_mesh(**SAMPLE_DIMS))
+    return contraction_case()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(index)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except Exception:
+            self.p.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(seconds: float, warm: int = 1):
+    """FP64 CPU oracle on the 126,675-cell sample, all host threads."""
+    from oracle import pyoracle
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    case = make_case(True)
+    o = pyoracle.Oracle(case)
+    if warm:
+        o.step(warm)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.step(1)
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    cells = case.mesh.nCells
+    return {"value": cells * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"same contraction/Giesekus case at {cells:,} cells (1/8 of the 1M mesh), "
+                      f"{n} time steps after {warm} warm-up step(s), FP64 oracle (serial face loops and "
+                      f"Krylov sweeps, OpenMP over cell-local loops), {dt:.1f} s"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    case = make_case(True)
+    o = pyoracle.Oracle(case)
+    if args.warmup:
+        o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    cells = case.mesh.nCells
+    v = cells * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample_cells": cells},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{cells:,}-cell sample of the contraction case, {args.steps} steps; "
+                                   "rheoTool/OpenFOAM v9 is not buildable here, its FP64 restatement runs"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import numpy as np
+    from rheotool_gb300 import abi
+    from rheotool_gb300.runtime import Context
+
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+        pg = tdist
+
+    case = make_case(args.small)
+    N, F, NB = case.mesh.nCells, case.mesh.nFaces, case.mesh.nBFaces
+    ctx = Context(local)
+    ctx.setup_case(case)
+    if args.warmup:
+        ctx.step(args.warmup)
+    ctx.sync()
+    if pg:
+        pg.barrier()
+    clk = Clocks(local)
+    k0 = ctx.kernel_count()
+    ctx.timer_start()
+    perf = ctx.step(args.steps)
+    ms = ctx.timer_stop()
+    launches = ctx.kernel_count() - k0
+    clocks = clk.stop()
+    if pg:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t[0])
+        pg.barrier()
+    total_cells = N * args.steps * world
+    value = total_cells / (ms * 1e-3)
+
+    # ---- roofline of the dominant operation (live CUDA events) ------------
+    roof = None
+    prof = {}
+    if not args.no_profile:
+        ctx.profile(True)
+        ctx.step(2)
+        prof = ctx.profile_report()
+        ctx.profile(False)
+        leaves = {k: v for k, v in prof.items() if not k.startswith("solve_") and v[2] > 0}
+        if leaves:
+            name = max(leaves, key=lambda k: leaves[k][1])
+            n, tms, by = leaves[name]
+            peak, src = peaks()
+            achieved = (by / n) / (tms / n * 1e-3) / 1e9
+            traffic = None
+            tp = os.path.join(ROOT, "profiles", "traffic.json")
+            if os.path.exists(tp):
+                try:
+                    tj = json.load(open(tp))
+                    if name in tj:
+                        traffic = tj[name]["dram_bytes_per_cell"] * N
+                except Exception:
+                    traffic = None
+            roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
+                    "traffic": traffic, "algorithmic_bytes_per_launch": by / n,
+                    "launches_per_2_steps": n, "avg_launch_ms": tms / n,
+                    "share_of_profiled_time": tms / max(sum(v[1] for k, v in prof.items()
+                                                            if not k.startswith("solve_")), 1e-30)}
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    e2e = None
+    if not args.no_e2e:
+        try:
+            import torch
+            pin = lambda shape: torch.zeros(shape, dtype=torch.float64, pin_memory=True).numpy()
+        except Exception:
+            pin = lambda shape: np.zeros(shape)
+        U, Ub, p, pb = pin((N, 3)), pin((NB, 3)), pin(N), pin(NB)
+        phi, phib, tau = pin(F), pin(NB), pin((N, 6))
+        # start from the current device state
+        for fid, a, b in ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib)):
+            ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a), abi.dptr(b))
+        ke = max(2, min(args.steps, 5))
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            for fid, a, b in ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib)):
+                ctx.lib.rt_field_set(ctx._ctx, fid, abi.dptr(a), abi.dptr(b))
+            ctx.step(1)
+            for fid, a, b in ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib)):
+                ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a), abi.dptr(b))
+            ctx.lib.rt_field_get(ctx._ctx, abi.RT_FIELD_TAU, abi.dptr(tau), None)
+        dt = time.perf_counter() - t0
+        h2d = 8 * (3 * N + 3 * NB + N + NB + F + NB)
+        d2h = h2d + 8 * 6 * N
+        e2e = {"value": N * ke * world / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "steps": ke, "path": "rt_field_set(U,p,phi) + rt_step(1) + rt_field_get(U,p,phi,tau), pinned host"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu = cpu_baseline(args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD if not args.small else WORKLOAD.replace("1,000,000", f"{N:,}"),
+                       "cells": N, "faces": F, "parallelism": f"replicas x{world} (independent cases)",
+                       "l2": "inputs larger than L2: the step touches ~2 GB of fields and matrices per step",
+                       "iterations_last_step": {"p": perf.p.nIterations,
+                                                "U": [perf.U[k].nIterations for k in range(3)],
+                                                "theta": [perf.theta[k].nIterations for k in range(6)]}},
+            "clocks": clocks, "gpu_launches": launches, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
+            "profile_ms_2_steps": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

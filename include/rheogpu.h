@@ -167,6 +167,19 @@ const char *rt_last_error(const rt_ctx *ctx);
 const char *rt_status_string(rt_status s);
 
 rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *mesh);
+
+/* Optional structure of the uploaded mesh (no reference counterpart: blockMesh
+ * numbers the cells of a block this way but OpenFOAM does not record it).
+ * cellIJK (3*nCells) gives each cell's position in an nx x ny x nz box; cells
+ * must be numbered lexicographically (i fastest) and every internal face must
+ * join box neighbours, else RT_EINVAL and the mesh stays unstructured.  A
+ * structured mesh gets the systolic DIC/DILU sweeps. */
+rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const int32_t *cellIJK);
+
+/* Options.  RT_OPT_SWEEP: 0 auto (systolic when structured), 1 level-scheduled
+ * sweeps, 2 structured systolic sweeps. */
+#define RT_OPT_SWEEP 1
+rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);
 /* internal: ncmpt*nCells AoS (may be NULL); boundary: ncmpt*nBFaces AoS (may
@@ -212,6 +225,18 @@ rt_status rt_op_eig(rt_ctx *ctx, int32_t n, const double *theta,
 
 /* Wait for all work of the context. */
 rt_status rt_sync(rt_ctx *ctx);
+
+/* Timing on the context stream (no reference counterpart: instrumentation,
+ * like the per-step ExecutionTime print of rheoFoam.C:166-168).
+ * rt_timer_start/stop bracket a region with CUDA events; rt_profile_enable
+ * turns on named per-operation event pairs, rt_profile_report writes one
+ * line "name launches device_ms algorithmic_bytes" per operation and clears
+ * them; rt_kernel_count returns the number of kernels launched so far. */
+rt_status rt_timer_start(rt_ctx *ctx);
+rt_status rt_timer_stop(rt_ctx *ctx, double *ms);
+rt_status rt_profile_enable(rt_ctx *ctx, int32_t on);
+rt_status rt_profile_report(rt_ctx *ctx, char *buf, int32_t len);
+rt_status rt_kernel_count(rt_ctx *ctx, int64_t *n);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,8 @@ RT_PRECOND_NONE, RT_PRECOND_DIC, RT_PRECOND_DILU, RT_PRECOND_DIAGONAL = 0, 1, 2,
 RT_LIM_NONE, RT_LIM_UPWIND, RT_LIM_CUBISTA, RT_LIM_MINMOD, RT_LIM_SMART, RT_LIM_WACEB, RT_LIM_SUPERBEE = -1, 0, 1, 2, 3, 4, 5
 RT_PREC_FP64, RT_PREC_MIXED = 0, 1
 RT_FIELD_U, RT_FIELD_P, RT_FIELD_PHI, RT_FIELD_THETA, RT_FIELD_TAU, RT_FIELD_EIGVALS, RT_FIELD_EIGVECS = range(7)
+RT_OPT_SWEEP = 1
+SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {
     "Oldroyd-BLog": RT_MODEL_OLDROYDB_LOG,
@@ -154,6 +156,13 @@ def load_library(path: str = LIBNAME):
         "rt_op_grad": ([vp, _dp, _dp, _dp], C.c_int32),
         "rt_op_eig": ([vp, C.c_int32, _dp, _dp, _dp], C.c_int32),
         "rt_sync": ([vp], C.c_int32),
+        "rt_mesh_set_ijk": ([vp, C.c_int32, C.c_int32, C.c_int32, _ip], C.c_int32),
+        "rt_set_option": ([vp, C.c_int32, C.c_int64], C.c_int32),
+        "rt_timer_start": ([vp], C.c_int32),
+        "rt_timer_stop": ([vp, P(C.c_double)], C.c_int32),
+        "rt_profile_enable": ([vp, C.c_int32], C.c_int32),
+        "rt_profile_report": ([vp, C.c_char_p, C.c_int32], C.c_int32),
+        "rt_kernel_count": ([vp, P(C.c_int64)], C.c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -349,25 +349,45 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
     double *dS = W.take(N), *bS = W.take(6 * (size_t)N);
     double *val = W.take(6 * (size_t)NB + 6);
 
-    k_theta_rhs<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, G, cs.eigVecs.p, cs.eigVals.p, cs.theta.p, rhs, fP);
-    RT_CHECK_LAUNCH();
+    {
+        ProfScope ps(ctx, "theta_rhs", (double)N * (72.0 + 72.0 + 24.0 + 48.0 + 48.0));
+        k_theta_rhs<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, G, cs.eigVecs.p, cs.eigVals.p, cs.theta.p, rhs, fP);
+        RT_CHECK_LAUNCH();
+    }
     RT_CUDA(cudaMemcpyAsync(theta0, cs.theta.p, sizeof(double) * 6 * N, cudaMemcpyDeviceToDevice, s));
-    grad_field(ctx, 6, cs.theta.p, cs.thetab.p, gth);
-    convection(ctx, cs.ctl.divTheta, 6, cs.phi.p, cs.phib.p, cs.theta.p, cs.thetab.p, cs.bkTh.p, gth, lower,
-               upper, diagC, srcC, intC, bouC, flux);
+    const double fpc = (double)F / N;
+    {
+        ProfScope ps(ctx, "grad", (double)N * (48.0 + fpc * 16.0 + 72.0 + 144.0));
+        grad_field(ctx, 6, cs.theta.p, cs.thetab.p, gth);
+    }
+    {
+        ProfScope ps(ctx, "convection", (double)N * (48.0 + 144.0 + 24.0 + fpc * (8.0 + 8.0 + 16.0 + 16.0 + 2 * 48.0) + 8.0 + 48.0));
+        convection(ctx, cs.ctl.divTheta, 6, cs.phi.p, cs.phib.p, cs.theta.p, cs.thetab.p, cs.bkTh.p, gth, lower,
+                   upper, diagC, srcC, intC, bouC, flux);
+    }
     MeshView m = view(mesh);
     k_theta_assemble<<<nblocks(N), RT_BLOCK, 0, s>>>(m, 1.0 / cs.ctl.deltaT, diagC, srcC, theta0, rhs, intC, bouC,
                                                       dS, bS);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
     SolveArgs a{dS, upper, lower, bS, cs.theta.p, 6, theta_valid_mask(mesh), cs.ctl.solverTheta};
-    rt_status st = ldu_solve_device(ctx, a, perf);
+    rt_status st;
+    {
+        ProfScope ps(ctx, "solve_theta");
+        st = ldu_solve_device(ctx, a, perf);
+    }
     correct_bc(ctx, cs.bkTh.p, 6, cs.theta.p, cs.thetab.p);
-    eig_cells(ctx, N, cs.theta.p, cs.eigVals.p, cs.eigVecs.p);
-    k_tau<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, cs.eigVecs.p, cs.eigVals.p, fP, cs.tau.p);
-    RT_CHECK_LAUNCH();
-    launch_count(ctx);
-    tau_correct_bc(ctx, val);
+    {
+        ProfScope ps(ctx, "eig", (double)N * (48.0 + 72.0 + 24.0));
+        eig_cells(ctx, N, cs.theta.p, cs.eigVals.p, cs.eigVecs.p);
+    }
+    {
+        ProfScope ps(ctx, "tau", (double)N * (72.0 + 24.0 + 48.0));
+        k_tau<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, cs.eigVecs.p, cs.eigVals.p, fP, cs.tau.p);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+        tau_correct_bc(ctx, val);
+    }
     W.used = mark;
     return st;
 }

@@ -45,11 +45,11 @@ void upload_soa(rt_ctx *ctx, const double *h, int n, int nc, DBuf<double> &dst) 
         RT_CUDA(cudaMemcpyAsync(dst.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
         return;
     }
-    DBuf<double> st;
-    st.upload(h, (size_t)n * nc, ctx->stream);
-    k_aos2soa<<<nblocks((long long)n * nc), RT_BLOCK, 0, ctx->stream>>>(n, nc, st.p, dst.p);
+    size_t cnt = (size_t)n * nc;
+    if (ctx->stage.n < cnt) ctx->stage.alloc(cnt);
+    RT_CUDA(cudaMemcpyAsync(ctx->stage.p, h, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->stream));
+    k_aos2soa<<<nblocks((long long)cnt), RT_BLOCK, 0, ctx->stream>>>(n, nc, ctx->stage.p, dst.p);
     RT_CHECK_LAUNCH();
-    RT_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 void download_aos(rt_ctx *ctx, const DBuf<double> &src, int n, int nc, double *h) {
@@ -59,11 +59,11 @@ void download_aos(rt_ctx *ctx, const DBuf<double> &src, int n, int nc, double *h
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
         return;
     }
-    DBuf<double> st;
-    st.alloc((size_t)n * nc);
-    k_soa2aos<<<nblocks((long long)n * nc), RT_BLOCK, 0, ctx->stream>>>(n, nc, src.p, st.p);
+    size_t cnt = (size_t)n * nc;
+    if (ctx->stage.n < cnt) ctx->stage.alloc(cnt);
+    k_soa2aos<<<nblocks((long long)cnt), RT_BLOCK, 0, ctx->stream>>>(n, nc, src.p, ctx->stage.p);
     RT_CHECK_LAUNCH();
-    RT_CUDA(cudaMemcpyAsync(h, st.p, sizeof(double) * n * nc, cudaMemcpyDeviceToHost, ctx->stream));
+    RT_CUDA(cudaMemcpyAsync(h, ctx->stage.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, ctx->stream));
     RT_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
@@ -129,6 +129,9 @@ rt_status rt_ctx_destroy(rt_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->red.hostResult) cudaFreeHost(ctx->red.hostResult);
+    for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
+    if (ctx->tStart) cudaEventDestroy(ctx->tStart);
+    if (ctx->tStop) cudaEventDestroy(ctx->tStop);
     cudaStream_t st = ctx->stream;
     delete ctx;   // DBuf destructors free device memory
     if (st) cudaStreamDestroy(st);
@@ -169,6 +172,7 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
         RT_REQUIRE(acc == NB, RT_EINVAL, "patch sizes do not add up to nBFaces");
 
         DevMesh &m = ctx->mesh;
+        m.sm.on = false;
         m.N = N; m.F = F; m.NB = NB; m.nPatches = md->nPatches;
         for (int k = 0; k < 3; ++k) m.solveDir[k] = md->solveDir[k];
         cudaStream_t s = ctx->stream;
@@ -250,6 +254,80 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
         ctx->meshReady = true;
         ctx->cs.ready = false;
         return RT_OK;
+    });
+}
+
+rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const int32_t *cellIJK) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
+        RT_REQUIRE(nx > 0 && ny > 0 && nz > 0 && cellIJK, RT_EINVAL, "bad box dimensions");
+        DevMesh &m = ctx->mesh;
+        StructMesh &s = m.sm;
+        s.on = false;
+        const int N = m.N, F = m.F;
+        const long long box = (long long)nx * ny * nz;
+        std::vector<int> at((size_t)box, -1);
+        long long prev = -1;
+        for (int c = 0; c < N; ++c) {
+            int i = cellIJK[3 * c], j = cellIJK[3 * c + 1], k = cellIJK[3 * c + 2];
+            RT_REQUIRE(i >= 0 && i < nx && j >= 0 && j < ny && k >= 0 && k < nz, RT_EINVAL, "cell outside the box");
+            long long key = ((long long)k * ny + j) * nx + i;
+            RT_REQUIRE(key > prev, RT_EINVAL, "cells are not numbered lexicographically (i fastest)");
+            prev = key;
+            at[(size_t)key] = c;
+        }
+        // faces must join box neighbours; record the face of each direction
+        std::vector<int> own(F), nei(F);
+        RT_CUDA(cudaMemcpy(own.data(), m.owner.p, sizeof(int) * F, cudaMemcpyDeviceToHost));
+        RT_CUDA(cudaMemcpy(nei.data(), m.neighbour.p, sizeof(int) * F, cudaMemcpyDeviceToHost));
+        std::vector<int> lo((size_t)3 * N, -1), hi((size_t)3 * N, -1);
+        for (int f = 0; f < F; ++f) {
+            int o = own[f], n = nei[f];
+            int di = cellIJK[3 * n] - cellIJK[3 * o], dj = cellIJK[3 * n + 1] - cellIJK[3 * o + 1],
+                dk = cellIJK[3 * n + 2] - cellIJK[3 * o + 2];
+            int dir = (di == 0 && dj == 0 && dk == 1) ? 0 : (di == 0 && dj == 1 && dk == 0) ? 1
+                      : (di == 1 && dj == 0 && dk == 0) ? 2 : -1;   // 0 z, 1 y, 2 x
+            RT_REQUIRE(dir >= 0, RT_EINVAL, "face " + std::to_string(f) + " does not join box neighbours");
+            RT_REQUIRE(hi[(size_t)dir * N + o] < 0 && lo[(size_t)dir * N + n] < 0, RT_EINVAL, "duplicate face");
+            hi[(size_t)dir * N + o] = f;
+            lo[(size_t)dir * N + n] = f;
+        }
+        s.nx = nx; s.ny = ny; s.nz = nz;
+        s.nJB = (ny + 31) / 32;
+        s.T = nx + 31;
+        s.nSkew = (long long)nz * s.nJB * s.T * 32;
+        std::vector<int> cellOf((size_t)s.nSkew, -1);
+        for (int k = 0; k < nz; ++k)
+            for (int jb = 0; jb < s.nJB; ++jb)
+                for (int t = 0; t < s.T; ++t)
+                    for (int l = 0; l < 32; ++l) {
+                        int i = t - l, j = jb * 32 + l;
+                        if (i < 0 || i >= nx || j >= ny) continue;
+                        long long e = (((long long)k * s.nJB + jb) * s.T + t) * 32 + l;
+                        cellOf[(size_t)e] = at[((size_t)k * ny + j) * nx + i];
+                    }
+        upload_vec(ctx, cellOf, s.cellOf);
+        upload_vec(ctx, lo, s.faceLo);
+        upload_vec(ctx, hi, s.faceHi);
+        s.sync.alloc(SYNC_PROGRESS + (size_t)nz * s.nJB);
+        s.data.alloc((size_t)(12 + 6) * s.nSkew);
+        s.data.zero(ctx->stream);
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        s.on = true;
+        return RT_OK;
+    });
+}
+
+rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
+    return guarded(ctx, [&]() -> rt_status {
+        switch (option) {
+        case RT_OPT_SWEEP:
+            RT_REQUIRE(value >= 0 && value <= 2, RT_EINVAL, "RT_OPT_SWEEP: 0 auto, 1 levels, 2 structured");
+            ctx->sweepMode = (int)value;
+            return RT_OK;
+        default:
+            return RT_EINVAL;
+        }
     });
 }
 

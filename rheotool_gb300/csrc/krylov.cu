@@ -22,6 +22,7 @@
 #include <cstring>
 
 #include "rt_internal.h"
+#include "sweep.h"
 
 namespace rt {
 
@@ -482,7 +483,13 @@ struct Solver {
         RT_CUDA(cudaStreamSynchronize(st));
     }
 
+    static int pop(unsigned m) { return __builtin_popcount(m); }
+
     void amul(unsigned mask, const double *x, double *y) {
+        // algorithmic bytes per cell: diag 8, lower+upper 2*(F/N)*8, face
+        // addressing 2*(F/N)*4, x and y 16 per component
+        const double fpc = (double)ctx->mesh.F / N;
+        ProfScope ps(ctx, "amul", (double)N * (8.0 + fpc * 24.0 + 16.0 * pop(mask)));
         k_amul<<<nblocks(N), RT_BLOCK, 0, st>>>(e, mask, a.diag, a.upper, a.lower, x, y);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
@@ -490,16 +497,28 @@ struct Solver {
 
     void dot(unsigned mask, const double *x, const double *y, const double *x2 = nullptr,
              const double *y2 = nullptr) {
+        ProfScope ps(ctx, "dot", (double)N * 8.0 * (x2 ? 4 : 2) * pop(mask));
         k_dot<<<nB, RT_BLOCK, 0, st>>>(N, mask, x, y, x2, y2, ctx->red.partial.p, nB);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
         finalize(x2 ? 2 : 1, mask);
     }
 
+    bool systolic() const {
+        int pre = a.ctl.preconditioner;
+        return ctx->mesh.sm.on && ctx->sweepMode != 1 && (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU);
+    }
+
     void compute_rd(double *rD) {
         const DevMesh &m = ctx->mesh;
         int pre = a.ctl.preconditioner;
-        if (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU) {
+        if (systolic()) {
+            const double fpc = (double)m.F / N;
+            ProfScope ps(ctx, "dilu_rD", (double)N * (16.0 + fpc * 28.0));
+            skew_prepare(ctx, a.diag, a.upper, a.lower);
+        } else if (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU) {
+            const double fpc = (double)m.F / N;
+            ProfScope ps(ctx, "dilu_rD", (double)N * (16.0 + fpc * 28.0));
             for (int l = 0; l < m.nLevels; ++l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
                 k_rd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, a.diag,
@@ -526,7 +545,15 @@ struct Solver {
         } else if (pre == RT_PRECOND_DIAGONAL) {
             k_diag_apply<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, rD, r, w);
             launch_count(ctx);
+        } else if (systolic()) {
+            const double fpc = (double)m.F / N;
+            ProfScope ps(ctx, "dilu_precondition", (double)N * (16.0 + fpc * 32.0 + 32.0 * pop(mask)));
+            skew_precondition(ctx, a.nc, mask, r, w);
         } else {
+            // per application (forward + backward): rD 16, coefficients
+            // 2*(F/N)*8, addressing 2*(F/N)*8, r 8 + w 8 + w 16 per component
+            const double fpc = (double)m.F / N;
+            ProfScope ps(ctx, "dilu_precondition", (double)N * (16.0 + fpc * 32.0 + 32.0 * pop(mask)));
             for (int l = 0; l < m.nLevels; ++l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
                 k_fwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD,
@@ -734,6 +761,8 @@ rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf
     b.validMask = mask;
     rt_status st = RT_OK;
     if (mask) st = (a.ctl.solver == RT_SOLVER_PCG) ? run_pcg(ctx, b, perf) : run_pbicgstab(ctx, b, perf);
+    rt_status sw = skew_check(ctx);
+    if (sw != RT_OK) return sw;
     for (int k = 0; k < a.nc; ++k) {
         if (!((mask >> k) & 1u)) continue;
         const double fin = perf[k].finalResidual, init = perf[k].initialResidual;

@@ -77,10 +77,48 @@ struct DBuf {
     operator T *() const { return p; }
 };
 
+constexpr int SYNC_WORK = 0, SYNC_ERROR = 1, SYNC_PROGRESS = 2;
+
+// raw view passed to the kernels; every array has nSkew entries in the
+// skewed (block, step, lane) layout, wS has 6 components of nSkew
+struct SkewView {
+    int nx, ny, nz, nJB, T;
+    long long nSkew;
+    const int *cellOf;
+    double *D, *Pz, *Py, *Px, *rDraw;
+    double *rDinv, *Az, *Ay, *Ax, *Bz, *By, *Bx;
+    double *wS;
+};
+
+struct StructMesh {
+    bool on = false;
+    int nx = 0, ny = 0, nz = 0, nJB = 0, T = 0;
+    long long nSkew = 0;
+    DBuf<int> cellOf;          // nSkew: cell of each skewed entry, -1 outside the mesh
+    DBuf<int> faceLo, faceHi;  // 3*N: face to the (z, y, x) lower / upper neighbour, -1 if none
+    DBuf<int> sync;            // work counter, error flag, per-block progress
+    DBuf<double> data;         // 13 + 6 arrays of nSkew doubles
+    bool pendingCheck = false;
+
+    SkewView view() {
+        SkewView v;
+        v.nx = nx; v.ny = ny; v.nz = nz; v.nJB = nJB; v.T = T; v.nSkew = nSkew;
+        v.cellOf = cellOf.p;
+        double *p = data.p;
+        double **slots[] = {&v.D, &v.Pz, &v.Py, &v.Px, &v.rDraw, &v.rDinv, &v.Az, &v.Ay, &v.Ax,
+                            &v.Bz, &v.By, &v.Bx};
+        for (int i = 0; i < 12; ++i) *slots[i] = p + (size_t)i * nSkew;
+        v.wS = p + (size_t)12 * nSkew;
+        return v;
+    }
+};
+
+
 // ---------------------------------------------------------------------------
 // mesh: LDU addressing + geometry + cell-centric adjacency
 // ---------------------------------------------------------------------------
 struct DevMesh {
+    StructMesh sm;               // structured (box-lexicographic) description, optional
     int N = 0, F = 0, NB = 0, nPatches = 0;
     int nSlots = 0;          // max internal faces per cell (ELL width)
     int solveDir[3] = {1, 1, 1};
@@ -149,9 +187,24 @@ struct Reduce {
     double *hostResult = nullptr;  // pinned
 };
 
+// CUDA-event profiler: named scopes on the context stream, aggregated at
+// report time (launches, device milliseconds, algorithmic bytes)
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t next = 0;
+    struct Rec {
+        const char *name;
+        size_t a, b;
+        double bytes;
+    };
+    std::vector<Rec> recs;
+};
+
 }  // namespace rt
 
 struct rt_ctx {
+    int sweepMode = 0;           // 0 auto, 1 level-scheduled, 2 structured systolic
     int device = 0;
     int numSMs = 0;
     cudaStream_t stream = nullptr;
@@ -162,6 +215,9 @@ struct rt_ctx {
     rt::Work work;
     rt::DBuf<double> kws;        // Krylov workspace: 8 vectors x 6 comps x N + rD
     rt::DBuf<double> scal;       // device scalars of the Krylov loops [32 slots][8]
+    rt::DBuf<double> stage;      // staging for AoS <-> SoA field transfers
+    rt::Prof prof;
+    cudaEvent_t tStart = nullptr, tStop = nullptr;
     bool meshReady = false;
     long long kernelLaunches = 0;
 };
@@ -196,5 +252,16 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf);
 void init_fields(rt_ctx *ctx);
 
 inline int nblocks(long long n, int b = RT_BLOCK) { return (int)((n + b - 1) / b); }
+
+// prof.cu
+int prof_begin(rt_ctx *ctx, const char *name);
+void prof_end(rt_ctx *ctx, int rec, double bytes);
+struct ProfScope {
+    rt_ctx *ctx;
+    int rec;
+    double bytes;
+    ProfScope(rt_ctx *c, const char *name, double b = 0.0) : ctx(c), rec(prof_begin(c, name)), bytes(b) {}
+    ~ProfScope() { prof_end(ctx, rec, bytes); }
+};
 
 }  // namespace rt

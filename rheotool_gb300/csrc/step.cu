@@ -504,11 +504,18 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
 
     // ---------------- UEqn ----------------
     double *G = W.take(9 * (size_t)N);
-    grad_field(ctx, 3, cs.U.p, cs.Ub.p, G);
+    const double fpc = (double)F / N;
+    {
+        ProfScope ps(ctx, "grad", (double)N * (24.0 + 72.0 + fpc * 16.0 + 72.0 + 72.0));
+        grad_field(ctx, 3, cs.U.p, cs.Ub.p, G);
+    }
     double *lower = W.take(F), *upper = W.take(F), *diagC = W.take(N), *srcC = W.take(3 * (size_t)N);
     double *intC = W.take(3 * (size_t)NB), *bouC = W.take(3 * (size_t)NB), *flux = W.take(3 * (size_t)F);
-    convection(ctx, ctl.divU, 3, cs.phi.p, cs.phib.p, cs.U.p, cs.Ub.p, cs.bkU.p, G, lower, upper, diagC, srcC,
-               intC, bouC, flux);
+    {
+        ProfScope ps(ctx, "convection", (double)N * (24.0 + 72.0 + 24.0 + fpc * (8.0 + 8.0 + 16.0 + 16.0 + 2 * 24.0) + 8.0 + 24.0));
+        convection(ctx, ctl.divU, 3, cs.phi.p, cs.phib.p, cs.U.p, cs.Ub.p, cs.bkU.p, G, lower, upper, diagC, srcC,
+                   intC, bouC, flux);
+    }
     double gam, kG = 0.0;
     if (mp.stabilization == RT_STAB_COUPLING || mp.stabilization == RT_STAB_BSD) {
         gam = (mp.etaP + mp.etaS) / mp.rho;
@@ -517,6 +524,7 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
         gam = mp.etaS / mp.rho;
     }
     double *expl = W.take(3 * (size_t)N);
+    ProfScope psMom(ctx, "mom_assembly", (double)N * (48.0 + 72.0 + 24.0 + 24.0 + 8.0 + 24.0 + 24.0 + 24.0 + 8.0 + 24.0) + F * 32.0);
     k_divtau_expl<<<gN, RT_BLOCK, 0, s>>>(m, mp.stabilization, mp.rho, kG, cs.tau.p, cs.taub.p, G, cs.U.p, cs.Ub.p,
                                           expl);
     double *diag = W.take(N), *src = W.take(3 * (size_t)N);
@@ -535,12 +543,19 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     for (int k = 0; k < 3; ++k)
         if (mesh.solveDir[k]) maskU |= 1u << k;
     SolveArgs ua{dS, upper, lower, bS, cs.U.p, 3, maskU, ctl.solverU};
-    rt_status st = ldu_solve_device(ctx, ua, perf->U);
+    prof_end(ctx, psMom.rec, psMom.bytes);
+    psMom.rec = -1;
+    rt_status st;
+    {
+        ProfScope ps(ctx, "solve_U");
+        st = ldu_solve_device(ctx, ua, perf->U);
+    }
     if (st != RT_OK && st != RT_ENOCONV) return st;
     correct_bc(ctx, cs.bkU.p, 3, cs.U.p, cs.Ub.p);
 
     // ---------------- pEqn ----------------
     double *rAU = W.take(N), *rAtU = W.take(N), *HbyA = W.take(3 * (size_t)N), *H = W.take(3 * (size_t)N);
+    ProfScope psP(ctx, "p_assembly", (double)N * (8.0 + 24.0 + 24.0 + 24.0 + 24.0 + 8.0 + 8.0 + 24.0) + F * 48.0);
     k_AH<<<gN, RT_BLOCK, 0, s>>>(m, diag, lower, upper, src, intC, bouC, cs.U.p, rAU, HbyA, rAtU, H);
     double *HbyAb = W.take(3 * (size_t)NB);
     if (NB) k_HbyA_bnd<<<gB, RT_BLOCK, 0, s>>>(NB, N, cs.bkU.p, mesh.bCell.p, cs.Ub.p, rAU, H, HbyAb);
@@ -568,9 +583,16 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     RT_CHECK_LAUNCH();
     launch_count(ctx, 3);
     SolveArgs pa{pd, pu, pu, ps, cs.p.p, 1, 1u, ctl.solverP};
-    rt_status sp = ldu_solve_device(ctx, pa, &perf->p);
+    prof_end(ctx, psP.rec, psP.bytes);
+    psP.rec = -1;
+    rt_status sp;
+    {
+        ProfScope pss(ctx, "solve_p");
+        sp = ldu_solve_device(ctx, pa, &perf->p);
+    }
     if (sp != RT_OK && sp != RT_ENOCONV) return sp;
     correct_bc(ctx, cs.bkP.p, 1, cs.p.p, cs.pb.p);
+    ProfScope psC(ctx, "U_correction", (double)N * (24.0 + 16.0 + 48.0 + 24.0) + F * 40.0);
     k_phi_update<<<nblocks(std::max(F, NB)), RT_BLOCK, 0, s>>>(m, phiHbyA, phiHbyAb, pu, pIntC, pBouC, cs.p.p,
                                                                 cs.phi.p, cs.phib.p);
     double *gp2 = W.take(3 * (size_t)N);
@@ -579,6 +601,8 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
     correct_bc(ctx, cs.bkU.p, 3, cs.U.p, cs.Ub.p);
+    prof_end(ctx, psC.rec, psC.bytes);
+    psC.rec = -1;
     perf->contErrSumLocal = 0.0;
     perf->contErrGlobal = 0.0;
 

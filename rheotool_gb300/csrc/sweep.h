@@ -1,0 +1,15 @@
+// sweep.h — structured-mesh data for the systolic DIC/DILU sweeps (sweep.cu).
+#pragma once
+
+#include "rt_internal.h"
+
+namespace rt {
+
+// per matrix: rD recurrence and the premultiplied sweep coefficients
+void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
+// w = M^-1 r for the masked components (nc <= 6), forward then backward
+void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
+// RT_ETIMEOUT if a bounded wait of the last sweeps ran out
+rt_status skew_check(rt_ctx *ctx);
+
+}  // namespace rt

@@ -74,6 +74,18 @@ class Context:
         from .case import Case as _Case  # noqa: F401
         md = _mesh_desc(mesh, self)
         self._check(self.lib.rt_mesh_upload(self._ctx, C.byref(md)), "rt_mesh_upload")
+        ijk = getattr(mesh, "cellIJK", None)
+        if ijk is not None and getattr(mesh, "shape", None) is not None:
+            nx, ny, nz = mesh.shape
+            a = np.ascontiguousarray(ijk, dtype=np.int32)
+            self._check(self.lib.rt_mesh_set_ijk(self._ctx, nx, ny, nz, abi.iptr(a)), "rt_mesh_set_ijk")
+
+    def set_option(self, option: int, value: int):
+        self._check(self.lib.rt_set_option(self._ctx, int(option), int(value)), "rt_set_option")
+
+    def set_sweep(self, mode: int):
+        """abi.SWEEP_AUTO / SWEEP_LEVELS / SWEEP_SYSTOLIC for the DIC/DILU sweeps."""
+        self.set_option(abi.RT_OPT_SWEEP, mode)
 
     def setup_case(self, case: Case, fields: Optional[Fields] = None):
         if self.mesh is not case.mesh:
@@ -164,6 +176,33 @@ class Context:
 
     def sync(self):
         self._check(self.lib.rt_sync(self._ctx), "rt_sync")
+
+    # ---- timing on the context stream ---------------------------------
+    def timer_start(self):
+        self._check(self.lib.rt_timer_start(self._ctx), "rt_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._check(self.lib.rt_timer_stop(self._ctx, C.byref(ms)), "rt_timer_stop")
+        return ms.value
+
+    def profile(self, on: bool):
+        self._check(self.lib.rt_profile_enable(self._ctx, int(bool(on))), "rt_profile_enable")
+
+    def profile_report(self) -> dict:
+        """{name: (launches, device_ms, algorithmic_bytes)} since the last report."""
+        buf = C.create_string_buffer(1 << 16)
+        self._check(self.lib.rt_profile_report(self._ctx, buf, len(buf)), "rt_profile_report")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms, by = line.split()
+            out[name] = (int(n), float(ms), float(by))
+        return out
+
+    def kernel_count(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.rt_kernel_count(self._ctx, C.byref(n)), "rt_kernel_count")
+        return n.value
 
 
 def _mesh_desc(mesh, keeper) -> abi.rt_mesh_desc:

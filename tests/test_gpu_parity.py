@@ -194,6 +194,37 @@ def test_pbicgstab_multi_rhs_matches_oracle(ctx, precond):
         assert rel(xg[k], xo) < 1e-9 or np.abs(xo).max() == 0
 
 
+SWEEP_MESHES = {
+    "cavity20": lambda: cavity_mesh(20),                              # one j-block, one plane
+    "cavity70": lambda: cavity_mesh(70),                              # three j-blocks
+    "contraction3d": lambda: contraction_mesh(12, 10, 30, 10, 6, 4.0, 4.0),   # holes, 2 j-blocks, 6 planes
+}
+
+
+@pytest.mark.parametrize("mesh_name", sorted(SWEEP_MESHES))
+@pytest.mark.parametrize("solver,pre,asym,nc", [("PCG", "DIC", 0.0, 1), ("PBiCGStab", "DILU", 3.0, 3)])
+def test_systolic_sweeps_equal_level_sweeps(ctx, mesh_name, solver, pre, asym, nc):
+    """The structured systolic DIC/DILU sweeps evaluate the recurrences in the
+    level-scheduled (and sequential) order of operations: same bits."""
+    mesh = SWEEP_MESHES[mesh_name]()
+    rng = np.random.default_rng(21)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=asym)
+    b = rng.normal(size=(nc, mesh.nCells)) * mesh.V
+    ctl = SolverControl(solver, pre, 1e-12, 0.0, 0, 500)
+    ctx.upload_mesh(mesh)
+    out = {}
+    try:
+        for mode in (abi.SWEEP_LEVELS, abi.SWEEP_SYSTOLIC):
+            ctx.set_sweep(mode)
+            x = np.zeros((nc, mesh.nCells))
+            perf = ctx.ldu_solve(diag, upper, lower, b, x, ctl)
+            out[mode] = (x, [p.nIterations for p in perf])
+    finally:
+        ctx.set_sweep(abi.SWEEP_AUTO)
+    assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
+    assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
+
+
 def test_solver_reports_non_convergence(ctx):
     mesh = small_contraction()
     rng = np.random.default_rng(13)
