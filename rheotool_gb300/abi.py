@@ -25,6 +25,7 @@ RT_LIM_NONE, RT_LIM_UPWIND, RT_LIM_CUBISTA, RT_LIM_MINMOD, RT_LIM_SMART, RT_LIM_
 RT_PREC_FP64, RT_PREC_MIXED = 0, 1
 RT_FIELD_U, RT_FIELD_P, RT_FIELD_PHI, RT_FIELD_THETA, RT_FIELD_TAU, RT_FIELD_EIGVALS, RT_FIELD_EIGVECS = range(7)
 RT_OPT_SWEEP = 1
+RT_OPT_SWEEP_PLANES = 2
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {

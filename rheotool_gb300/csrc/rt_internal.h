@@ -87,17 +87,19 @@ struct SkewView {
     const int *cellOf;
     double *D, *Pz, *Py, *Px, *rDraw;
     double *rDinv, *Az, *Ay, *Ax, *Bz, *By, *Bx;
-    double *wS;
+    double *wS;   // 6 components
+    double *rS;   // 6 components
 };
 
 struct StructMesh {
     bool on = false;
     int nx = 0, ny = 0, nz = 0, nJB = 0, T = 0;
+    int KC = 1;                // planes per CTA of the systolic sweeps
     long long nSkew = 0;
     DBuf<int> cellOf;          // nSkew: cell of each skewed entry, -1 outside the mesh
     DBuf<int> faceLo, faceHi;  // 3*N: face to the (z, y, x) lower / upper neighbour, -1 if none
     DBuf<int> sync;            // work counter, error flag, per-block progress
-    DBuf<double> data;         // 13 + 6 arrays of nSkew doubles
+    DBuf<double> data;         // 12 + 6 + 6 arrays of nSkew doubles
     bool pendingCheck = false;
 
     SkewView view() {
@@ -109,6 +111,7 @@ struct StructMesh {
                             &v.Bz, &v.By, &v.Bx};
         for (int i = 0; i < 12; ++i) *slots[i] = p + (size_t)i * nSkew;
         v.wS = p + (size_t)12 * nSkew;
+        v.rS = p + (size_t)18 * nSkew;
         return v;
     }
 };
