@@ -294,7 +294,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         }
         s.nx = nx; s.ny = ny; s.nz = nz;
         s.nJB = (ny + 31) / 32;
-        s.T = nx + 31;
+        s.T = ((nx + 31 + 7) / 8) * 8;   // steps per block, padded to whole chunks
         s.nSkew = (long long)nz * s.nJB * s.T * 32;
         std::vector<int> cellOf((size_t)s.nSkew, -1);
         for (int k = 0; k < nz; ++k)

@@ -80,14 +80,36 @@ __device__ __forceinline__ int spin_global(const int *c, int need, int *sync, lo
 
 }  // namespace
 
+// Ring depths (steps) of the shared-memory hand-offs, per chunk size P.
+template <int P> struct Ring { static constexpr int R = (P >= 4) ? 4 * P : 4; static constexpr int RJ = 64; };
+
+template <int NC, int P>
+constexpr size_t ring_bytes(int nW) {
+    return (size_t)nW * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
+}
+
 // MODE 0: forward application, 1: backward application, 2: rD recurrence.
 // Warp w = o * nJB + jo of a CTA handles plane position o, j-block jo.
+// Values cross warps of the CTA through shared rings: ringK[w][step % R]
+// holds all 32 lanes of a step for the next plane, ringJ[w][step % RJ] lane
+// 31 for the next j-block.  A producer never runs more than a ring ahead of
+// its consumers (bounded back-pressure), so a slot is never overwritten before
+// it was read; a consumer never waits for more than a chunk ahead of itself,
+// so the two waits cannot close a cycle.  Values for the next CTA go through
+// the global skewed array wS, published with release/acquire counters.
+// Invalid entries (outside the mesh, padding) have zero coefficients and zero
+// right-hand sides, so every lane runs the same branch-free recurrence.
 template <int MODE, int NC, int P>
 __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, double *__restrict__ w, int N,
                                                   int *sync, long long maxSpin, int KC) {
+    constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ;
+    extern __shared__ double smem[];
     __shared__ int s_grp;
     __shared__ volatile int s_prog[16];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nW = blockDim.x >> 5;
+    double *ringK = smem;                                   // [nW][R][32][NC]
+    double *ringJ = smem + (size_t)nW * R * 32 * NC;        // [nW][RJ][NC]
     if (threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
     if (threadIdx.x < 16) s_prog[threadIdx.x] = 0;
     __syncthreads();
@@ -101,8 +123,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
     const int T = g.T;
     int *gprog = sync + SYNC_PROGRESS;
     if (k < 0 || k >= g.nz) {
-        // a plane beyond the mesh in a partial group: nothing to do
-        if (lane == 0) s_prog[wid] = T;
+        if (lane == 0) s_prog[wid] = T;       // a plane beyond the mesh: nothing to do
         return;
     }
     const bool crossProducer = (o == KC - 1);
@@ -112,53 +133,60 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
     const int depKw = (o > 0) ? wid - g.nJB : -1;
     const int kd = (MODE == 1) ? k + 1 : k - 1;
     const int depKg = (o == 0 && kd >= 0 && kd < g.nz) ? kd * g.nJB + jb : -1;
-    const bool hasK = (MODE == 1) ? (k + 1 < g.nz) : (k > 0);
     const int depJw = (jo > 0) ? wid - 1 : -1;
-    constexpr int PF = 4 * P;   // prefetch distance in steps
-    int seenK = 0, seenJ = 0, fail = 0;
+    const int consK = (o + 1 < KC && wid + g.nJB < nW) ? wid + g.nJB : -1;   // in-CTA consumers
+    const int consJ = (jo + 1 < g.nJB) ? wid + 1 : -1;
+    // entry of step t: e0 + t * st
+    const long long e0 = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 + (31 - lane)
+                                     : (long long)blk * BS + lane;
+    const long long st = (MODE == 1) ? -32 : 32;
+    // prefetch assignment: lane -> (array a, step offset s)
+    const int pfA = lane >> 2, pfS = lane & 3;
+    const char *pfBase = nullptr;
+    long long pfStride = 0;
+    {
+        const long long eb = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 : (long long)blk * BS;
+        const double *arr = nullptr;
+        if (MODE == 2) arr = pfA == 0 ? g.D : pfA == 1 ? g.Pz : pfA == 2 ? g.Py : pfA == 3 ? g.Px : nullptr;
+        else if (MODE == 0) arr = pfA == 0 ? g.Az : pfA == 1 ? g.Ay : pfA == 2 ? g.Ax : pfA == 3 ? g.rDinv
+                                : pfA == 4 ? g.rS : nullptr;
+        else arr = pfA == 0 ? g.Bz : pfA == 1 ? g.By : pfA == 2 ? g.Bx : pfA == 3 ? g.wS : nullptr;
+        if (arr) { pfBase = (const char *)(arr + eb); pfStride = st * 8; }
+        else if (pfA == 7) { pfBase = (const char *)(g.cellOf + eb); pfStride = st * 4; }
+    }
+    int seenK = 0, seenJ = 0, seenCK = 0, seenCJ = 0, fail = 0;
     double yprev[NC];
 #pragma unroll
     for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? 1.0 : 0.0;
 
     for (int t0 = 0; t0 < T; t0 += P) {
-        const int te = min(T, t0 + P);          // chunk [t0, te)
-        // ---- prefetch the coefficients of a later chunk into L1
-        {
-            const int tp = t0 + PF + (lane & (P - 1));
-            if (tp < T) {
-                const long long ep = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1 - tp) * 32
-                                                 : (long long)blk * BS + (long long)tp * 32;
-                // lanes share out (array, step) pairs; a step line is 256 bytes
-                for (int which = lane / P; which < 8; which += 32 / P) {
-                    const void *pa = nullptr;
-                    if (MODE == 2) {
-                        switch (which) {
-                        case 0: pa = g.D + ep; break;
-                        case 1: pa = g.Pz + ep; break;
-                        case 2: pa = g.Py + ep; break;
-                        case 3: pa = g.Px + ep; break;
-                        default: break;
-                        }
-                    } else {
-                        switch (which) {
-                        case 0: pa = (MODE == 0 ? g.Az : g.Bz) + ep; break;
-                        case 1: pa = (MODE == 0 ? g.Ay : g.By) + ep; break;
-                        case 2: pa = (MODE == 0 ? g.Ax : g.Bx) + ep; break;
-                        case 3: pa = (MODE == 0 ? g.rDinv : g.wS) + ep; break;
-                        case 4: pa = (MODE == 0 ? g.rS + ep : nullptr); break;
-                        default: break;
-                        }
-                    }
-                    if (pa) {
-                        pf_l1(pa);
-                        pf_l1((const double *)pa + 16);
-                    }
-                    if (which == 7) pf_l1(g.cellOf + ep);
-                }
+        const int te = t0 + P;                      // T is a multiple of P
+        // ---- L1 prefetch two chunks ahead
+        if (pfBase) {
+            const int tp = t0 + 2 * P + pfS;
+            if (pfS < P && tp < T) {
+                const char *pp = pfBase + tp * pfStride;
+                pf_l1(pp);
+                if (pfA != 7) pf_l1(pp + 128);     // a step line is 256 bytes
             }
         }
-        // ---- wait: previous plane through step te, previous j-block through te + 31
-        if (hasK && seenK < te) {
+        // ---- back-pressure: consumers must have read the slots this chunk overwrites
+        if (consK >= 0 && seenCK < te - R) {
+            int v = 0;
+            if (lane == 0) v = spin_shared(s_prog + consK, te - R, sync, maxSpin);
+            v = __shfl_sync(0xffffffffu, v, 0);
+            if (v < 0) { fail = 1; break; }
+            seenCK = v;
+        }
+        if (consJ >= 0 && seenCJ < te - RJ - 31) {
+            int v = 0;
+            if (lane == 0) v = spin_shared(s_prog + consJ, te - RJ - 31, sync, maxSpin);
+            v = __shfl_sync(0xffffffffu, v, 0);
+            if (v < 0) { fail = 1; break; }
+            seenCJ = v;
+        }
+        // ---- dependencies: previous plane through te, previous j-block through te + 31
+        if ((depKw >= 0 || depKg >= 0) && seenK < te) {
             int v = 0;
             if (lane == 0) {
                 if (depKw >= 0) v = spin_shared(s_prog + depKw, te, sync, maxSpin);
@@ -167,7 +195,6 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
             v = __shfl_sync(0xffffffffu, v, 0);
             if (v < 0) { fail = 1; break; }
             seenK = v;
-            __threadfence_block();
         }
         if (depJw >= 0 && seenJ < min(T, te + 31)) {
             int v = 0;
@@ -175,83 +202,69 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
             v = __shfl_sync(0xffffffffu, v, 0);
             if (v < 0) { fail = 1; break; }
             seenJ = v;
-            __threadfence_block();
         }
-        // ---- loads of the chunk (independent of the recurrence)
-        long long e[P];
-        int cell[P];
+        __threadfence_block();
+        // ---- loads of the chunk
         double c0[P], c1[P], c2[P], c3[P];
         double rk[P][NC], wk[P][NC], wj[P][NC];
+        int cell[P];
 #pragma unroll
         for (int s = 0; s < P; ++s) {
             const int t = t0 + s;
-            const bool in = t < te;
-            e[s] = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1 - t) * 32 + (31 - lane)
-                               : (long long)blk * BS + (long long)t * 32 + lane;
-            cell[s] = in ? g.cellOf[e[s]] : -1;
-            const bool jOK = (depJw >= 0) && (t + 31 < T) && lane == 0 && in;
-            long long eJ = 0;
-            if (jOK) eJ = (MODE == 1) ? (long long)(blk + 1) * BS + (long long)(T - 1 - (t + 31)) * 32
-                                      : (long long)(blk - 1) * BS + (long long)(t + 31) * 32 + 31;
+            const long long e = e0 + t * st;
+            cell[s] = (MODE == 1) ? g.cellOf[e] : 0;
             if (MODE == 2) {
-                c0[s] = in ? g.D[e[s]] : 1.0;
-                c1[s] = in ? g.Pz[e[s]] : 0.0;
-                c2[s] = in ? g.Py[e[s]] : 0.0;
-                c3[s] = in ? g.Px[e[s]] : 0.0;
-                wk[s][0] = (in && hasK) ? __ldcg(g.rDraw + e[s] - KS) : 1.0;
-                wj[s][0] = jOK ? __ldcg(g.rDraw + eJ) : 1.0;
+                c0[s] = g.D[e]; c1[s] = g.Pz[e]; c2[s] = g.Py[e]; c3[s] = g.Px[e];
             } else {
-                c0[s] = in ? ((MODE == 0) ? g.Az[e[s]] : g.Bz[e[s]]) : 0.0;
-                c1[s] = in ? ((MODE == 0) ? g.Ay[e[s]] : g.By[e[s]]) : 0.0;
-                c2[s] = in ? ((MODE == 0) ? g.Ax[e[s]] : g.Bx[e[s]]) : 0.0;
-                c3[s] = (in && MODE == 0) ? g.rDinv[e[s]] : 0.0;
-                const long long eK = (MODE == 1) ? e[s] + KS : e[s] - KS;
+                c0[s] = (MODE == 0) ? g.Az[e] : g.Bz[e];
+                c1[s] = (MODE == 0) ? g.Ay[e] : g.By[e];
+                c2[s] = (MODE == 0) ? g.Ax[e] : g.Bx[e];
+                c3[s] = (MODE == 0) ? g.rDinv[e] : 0.0;
+            }
+            const double zk = (MODE == 2) ? 1.0 : 0.0;
 #pragma unroll
-                for (int q = 0; q < NC; ++q) {
-                    const long long oq = (long long)q * g.nSkew;
-                    const bool on = in && ((mask >> q) & 1u);
-                    rk[s][q] = on ? ((MODE == 0) ? g.rS[oq + e[s]] : g.wS[oq + e[s]]) : 0.0;
-                    wk[s][q] = (on && hasK) ? __ldcg(g.wS + oq + eK) : 0.0;
-                    wj[s][q] = (on && jOK) ? __ldcg(g.wS + oq + eJ) : 0.0;
-                }
+            for (int q = 0; q < NC; ++q) {
+                const long long oq = (long long)q * g.nSkew;
+                if (MODE == 0) rk[s][q] = g.rS[oq + e];
+                else if (MODE == 1) rk[s][q] = g.wS[oq + e];
+                else rk[s][q] = 0.0;
+                double *kv = (MODE == 2) ? g.rDraw : g.wS + oq;
+                if (depKw >= 0) wk[s][q] = ringK[(((size_t)depKw * R + (t & (R - 1))) * 32 + lane) * NC + q];
+                else if (depKg >= 0) wk[s][q] = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
+                else wk[s][q] = zk;
+                wj[s][q] = (depJw >= 0 && t + 31 < T) ? ringJ[((size_t)depJw * RJ + ((t + 31) & (RJ - 1))) * NC + q]
+                                                      : zk;
             }
         }
-        // ---- the recurrence
+        // ---- the recurrence (order of operations of the sequential sweep)
 #pragma unroll
         for (int s = 0; s < P; ++s) {
             const int t = t0 + s;
-            double yup[NC];
+            const long long e = e0 + t * st;
 #pragma unroll
-            for (int q = 0; q < NC; ++q) yup[q] = __shfl_up_sync(0xffffffffu, yprev[q], 1);
-            if (t >= te) break;
-            const bool jOK = (depJw >= 0) && (t + 31 < T);
-            if (MODE == 2) {
-                double v = 1.0;
-                if (cell[s] >= 0) {
+            for (int q = 0; q < NC; ++q) {
+                const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
+                const double yj = (lane > 0) ? yup : wj[s][q];
+                double v;
+                if (MODE == 2) {
                     v = c0[s];
-                    if (hasK) v -= c1[s] / wk[s][0];
-                    const double yj = (lane > 0) ? yup[0] : (jOK ? wj[s][0] : 1.0);
+                    v -= c1[s] / wk[s][q];
                     v -= c2[s] / yj;
-                    v -= c3[s] / yprev[0];
-                }
-                g.rDraw[e[s]] = v;
-                yprev[0] = v;
-            } else {
-#pragma unroll
-                for (int q = 0; q < NC; ++q) {
-                    if (!((mask >> q) & 1u)) continue;
-                    double acc = 0.0;
-                    if (cell[s] >= 0) {
-                        acc = (MODE == 0) ? c3[s] * rk[s][q] : rk[s][q];
-                        if (hasK) acc -= c0[s] * wk[s][q];
-                        const double yj = (lane > 0) ? yup[q] : (jOK ? wj[s][q] : 0.0);
-                        acc -= c1[s] * yj;
-                        acc -= c2[s] * yprev[q];
-                        if (MODE == 1) w[(long long)q * N + cell[s]] = acc;
+                    v -= c3[s] / yprev[q];
+                    g.rDraw[e] = v;
+                } else {
+                    v = (MODE == 0) ? c3[s] * rk[s][q] : rk[s][q];
+                    v -= c0[s] * wk[s][q];
+                    v -= c1[s] * yj;
+                    v -= c2[s] * yprev[q];
+                    if ((mask >> q) & 1u) {
+                        g.wS[(long long)q * g.nSkew + e] = v;
+                        if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = v;
                     }
-                    g.wS[(long long)q * g.nSkew + e[s]] = acc;
-                    yprev[q] = acc;
                 }
+                if (consK >= 0) ringK[(((size_t)wid * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
+                if (consJ >= 0 && lane == 31) ringJ[((size_t)wid * RJ + (t & (RJ - 1))) * NC + q] = v;
+                yprev[q] = v;
             }
         }
         // ---- publish
@@ -327,22 +340,30 @@ __global__ void k_skew_premul(SkewView g, const int *__restrict__ faceLo, const 
 
 namespace {
 
+template <int MODE, int NC, int P>
+void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int KC) {
+    StructMesh &s = ctx->mesh.sm;
+    const int nW = KC * g.nJB;
+    const size_t shm = ring_bytes<NC, P>(nW);
+    static bool attr = false;   // per instantiation
+    if (!attr) {
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ring_bytes<NC, P>(16)));
+        attr = true;
+    }
+    const int nGroups = (g.nz + KC - 1) / KC;
+    k_systolic<MODE, NC, P><<<nGroups, 32 * nW, shm, ctx->stream>>>(g, mask, w, ctx->mesh.N, s.sync.p,
+                                                                     1ll << 26, KC);
+}
+
 template <int MODE>
 void launch_mode(rt_ctx *ctx, const SkewView &g, int nc, unsigned mask, double *w) {
     StructMesh &s = ctx->mesh.sm;
     RT_CUDA(cudaMemsetAsync(s.sync.p, 0, sizeof(int) * (SYNC_PROGRESS + g.nz * g.nJB), ctx->stream));
-    const long long maxSpin = 1ll << 26;
     const int KC = s.KC;
-    const int nGroups = (g.nz + KC - 1) / KC;
-    dim3 grid(nGroups), block(32 * KC * g.nJB);
-    const int N = ctx->mesh.N;
-    cudaStream_t st = ctx->stream;
-    if (MODE == 2 || nc == 1)
-        k_systolic<MODE, 1, 4><<<grid, block, 0, st>>>(g, mask, w, N, s.sync.p, maxSpin, KC);
-    else if (nc <= 3)
-        k_systolic<MODE, 3, 2><<<grid, block, 0, st>>>(g, mask, w, N, s.sync.p, maxSpin, KC);
-    else
-        k_systolic<MODE, 6, 1><<<grid, block, 0, st>>>(g, mask, w, N, s.sync.p, maxSpin, KC);
+    if (MODE == 2 || nc == 1) launch_one<MODE, 1, 4>(ctx, g, mask, w, KC);
+    else if (nc <= 3) launch_one<MODE, 3, 2>(ctx, g, mask, w, KC);
+    else launch_one<MODE, 6, 2>(ctx, g, mask, w, KC);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
     s.pendingCheck = true;
