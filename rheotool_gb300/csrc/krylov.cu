@@ -186,7 +186,7 @@ __global__ void k_rd_level(Ell e, int l0, int l1, const int *__restrict__ cells,
         int nb = e.nbr[s * e.N + c];
         if (nb < 0 || nb > c) break;          // lower neighbours come first
         int f = e.face[s * e.N + c];
-        r -= upper[f] * lower[f] / rD[nb];
+        r = __dsub_rn(r, __ddiv_rn(__dmul_rn(upper[f], lower[f]), rD[nb]));
     }
     rD[c] = r;
 }
@@ -212,12 +212,12 @@ __global__ void k_fwd_level(Ell e, int l0, int l1, const int *__restrict__ cells
     for (int k = 0; k < 6; ++k) {
         if (!((mask >> k) & 1u)) continue;
         size_t o = (size_t)k * N;
-        double acc = rd * r[o + c];
+        double acc = __dmul_rn(rd, r[o + c]);
         for (int s = 0; s < e.nSlots; ++s) {
             int nb = e.nbr[s * N + c];
             if (nb < 0 || nb > c) break;
             int f = e.face[s * N + c];
-            acc -= rd * lower[f] * w[o + nb];
+            acc = __fma_rn(-__dmul_rn(rd, lower[f]), w[o + nb], acc);
         }
         w[o + c] = acc;
     }
@@ -242,7 +242,7 @@ __global__ void k_bwd_level(Ell e, int l0, int l1, const int *__restrict__ cells
             int nb = e.nbr[s * N + c];
             if (nb < c) break;                // upper neighbours are the last slots
             int f = e.face[s * N + c];
-            acc -= rd * upper[f] * w[o + nb];
+            acc = __fma_rn(-__dmul_rn(rd, upper[f]), w[o + nb], acc);
         }
         w[o + c] = acc;
     }
@@ -253,7 +253,7 @@ __global__ void k_diag_apply(int N, unsigned mask, const double *__restrict__ rD
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
     for (int k = 0; k < 6; ++k)
-        if ((mask >> k) & 1u) w[(size_t)k * N + c] = rD[c] * r[(size_t)k * N + c];
+        if ((mask >> k) & 1u) w[(size_t)k * N + c] = __dmul_rn(rD[c], r[(size_t)k * N + c]);
 }
 
 __global__ void k_copy(int N, unsigned mask, const double *__restrict__ r, double *__restrict__ w) {

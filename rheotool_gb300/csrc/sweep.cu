@@ -248,15 +248,15 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                 double v;
                 if (MODE == 2) {
                     v = c0[s];
-                    v -= c1[s] / wk[s][q];
-                    v -= c2[s] / yj;
-                    v -= c3[s] / yprev[q];
+                    v = __dsub_rn(v, __ddiv_rn(c1[s], wk[s][q]));
+                    v = __dsub_rn(v, __ddiv_rn(c2[s], yj));
+                    v = __dsub_rn(v, __ddiv_rn(c3[s], yprev[q]));
                     g.rDraw[e] = v;
                 } else {
-                    v = (MODE == 0) ? c3[s] * rk[s][q] : rk[s][q];
-                    v -= c0[s] * wk[s][q];
-                    v -= c1[s] * yj;
-                    v -= c2[s] * yprev[q];
+                    v = (MODE == 0) ? __dmul_rn(c3[s], rk[s][q]) : rk[s][q];
+                    v = __fma_rn(-c0[s], wk[s][q], v);
+                    v = __fma_rn(-c1[s], yj, v);
+                    v = __fma_rn(-c2[s], yprev[q], v);
                     if ((mask >> q) & 1u) {
                         g.wS[(long long)q * g.nSkew + e] = v;
                         if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = v;
@@ -305,9 +305,9 @@ __global__ void k_skew_setup(SkewView g, const int *__restrict__ faceLo, int N, 
     if (c >= 0) {
         d = diag[c];
         int fz = faceLo[c], fy = faceLo[N + c], fx = faceLo[2 * N + c];
-        if (fz >= 0) pz = upper[fz] * lower[fz];
-        if (fy >= 0) py = upper[fy] * lower[fy];
-        if (fx >= 0) px = upper[fx] * lower[fx];
+        if (fz >= 0) pz = __dmul_rn(upper[fz], lower[fz]);
+        if (fy >= 0) py = __dmul_rn(upper[fy], lower[fy]);
+        if (fx >= 0) px = __dmul_rn(upper[fx], lower[fx]);
     }
     g.D[e] = d;
     g.Pz[e] = pz;
