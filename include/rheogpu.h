@@ -178,7 +178,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
 
 /* Options.  RT_OPT_SWEEP: 0 auto (systolic when structured), 1 level-scheduled
  * sweeps, 2 structured systolic sweeps.  RT_OPT_SWEEP_PLANES: planes per CTA
- * of the systolic sweeps (1 .. 32/ceil(ny/32)). */
+ * of the systolic sweeps, one CTA per plane (1 .. 16). */
 #define RT_OPT_SWEEP 1
 #define RT_OPT_SWEEP_PLANES 2
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);

@@ -310,7 +310,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         upload_vec(ctx, lo, s.faceLo);
         upload_vec(ctx, hi, s.faceHi);
         RT_REQUIRE(s.nJB <= 16, RT_EINVAL, "structured sweeps need ny <= 512");
-        s.KC = std::max(1, std::min(nz, 16 / s.nJB));
+        s.KC = std::max(1, std::min(nz, 8));   // planes (CTAs) per thread-block cluster
         s.sync.alloc(SYNC_PROGRESS + (size_t)nz * s.nJB);
         s.data.alloc((size_t)(12 + 6 + 6) * s.nSkew);
         s.data.zero(ctx->stream);
@@ -330,7 +330,7 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
         case RT_OPT_SWEEP_PLANES: {
             StructMesh &s = ctx->mesh.sm;
             RT_REQUIRE(s.on, RT_ENOTREADY, "mesh is not structured");
-            RT_REQUIRE(value >= 1 && value * s.nJB <= 16, RT_EINVAL, "planes per CTA: 1 .. 16/nJB");
+            RT_REQUIRE(value >= 1 && value <= 16, RT_EINVAL, "planes per cluster: 1 .. 16");
             s.KC = (int)std::min<int64_t>(value, s.nz);
             return RT_OK;
         }

@@ -30,12 +30,15 @@
 // Per-entry data live in a "skewed" layout, entry (block, step, lane), so the
 // 32 lanes of a step touch 32 consecutive doubles.  The backward sweep walks
 // the same layout in reverse (lanes mirrored).
+#include <cooperative_groups.h>
 #include <cuda/atomic>
 
 #include "rt_internal.h"
 #include "sweep.h"
 
 namespace rt {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -80,210 +83,258 @@ __device__ __forceinline__ int spin_global(const int *c, int need, int *sync, lo
 
 }  // namespace
 
-// Ring depths (steps) of the shared-memory hand-offs, per chunk size P.
-template <int P> struct Ring { static constexpr int R = (P >= 4) ? 4 * P : 4; static constexpr int RJ = 64; };
+__device__ __forceinline__ int ld_acquire_cluster(const int *p) {
+    int v;
+    asm volatile("ld.acquire.cluster.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_cluster(int *p, int v) {
+    asm volatile("st.release.cluster.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void fence_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
+
+// bounded spin of lane 0 on a counter of this CTA's shared memory that other
+// CTAs of the cluster (or warps of this CTA) advance; -1 after a timeout
+__device__ __forceinline__ int spin_cluster(const int *c, int need, int *sync, long long maxSpin) {
+    long long spins = 0;
+    int v = ld_acquire_cluster(c);
+    while (v < need) {
+        if ((++spins & 255) == 0 && (spins > maxSpin || load_acquire(sync + SYNC_ERROR))) {
+            atomicExch(sync + SYNC_ERROR, 1);
+            return -1;
+        }
+        v = ld_acquire_cluster(c);
+    }
+    return v;
+}
+
+// Ring depths (steps) of the hand-offs for chunk size P.
+template <int P> struct Ring {
+    static constexpr int R = (P >= 4) ? 4 * P : 4;   // plane ring, at least two chunks
+    static constexpr int RJ = 64;                    // j-block ring
+};
 
 template <int NC, int P>
-constexpr size_t ring_bytes(int nW) {
-    return (size_t)nW * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
+size_t ring_bytes(int nJB) {
+    return (size_t)nJB * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
 }
 
 // MODE 0: forward application, 1: backward application, 2: rD recurrence.
-// Warp w = o * nJB + jo of a CTA handles plane position o, j-block jo.
-// Values cross warps of the CTA through shared rings: ringK[w][step % R]
-// holds all 32 lanes of a step for the next plane, ringJ[w][step % RJ] lane
-// 31 for the next j-block.  A producer never runs more than a ring ahead of
-// its consumers (bounded back-pressure), so a slot is never overwritten before
-// it was read; a consumer never waits for more than a chunk ahead of itself,
-// so the two waits cannot close a cycle.  Values for the next CTA go through
-// the global skewed array wS, published with release/acquire counters.
+//
+// One CTA owns one plane (all its j-blocks, warp = j-block); a thread-block
+// cluster owns CS consecutive planes in processing order, CTA rank r holding
+// the r-th.  The plane-to-plane values move through distributed shared
+// memory: the producer CTA stores each step's 32 lanes straight into the
+// consumer CTA's ring and advances the consumer's counter with a
+// cluster-scope release; the consumer reports its own progress back into the
+// producer's memory, which bounds how far the producer may run ahead (so a
+// ring slot is never overwritten before it is read, and the two waits can
+// never close a cycle).  The j-block hand-off stays inside the CTA (lane 31 of
+// the block below, through a shared ring).  The first plane of a cluster reads
+// the previous cluster's last plane from the global skewed array wS behind a
+// global release/acquire counter.  Clusters take plane groups in dependency
+// order from an atomic counter; all CTAs of a cluster are co-scheduled, and
+// none leaves before the final cluster barrier, so no CTA ever accesses the
+// shared memory of a CTA that has exited.
+//
+// Each SM holds one plane: the FP64 pipe of GB300 retires about two lanes per
+// cycle per SM, so spreading the wavefront over many SMs is what makes it fast.
 // Invalid entries (outside the mesh, padding) have zero coefficients and zero
 // right-hand sides, so every lane runs the same branch-free recurrence.
 template <int MODE, int NC, int P>
 __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, double *__restrict__ w, int N,
-                                                  int *sync, long long maxSpin, int KC) {
+                                                  int *sync, long long maxSpin) {
     constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CS = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
     extern __shared__ double smem[];
     __shared__ int s_grp;
-    __shared__ volatile int s_prog[16];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nW = blockDim.x >> 5;
-    double *ringK = smem;                                   // [nW][R][32][NC]
-    double *ringJ = smem + (size_t)nW * R * 32 * NC;        // [nW][RJ][NC]
-    if (threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
-    if (threadIdx.x < 16) s_prog[threadIdx.x] = 0;
-    __syncthreads();
-    const int nGroups = (g.nz + KC - 1) / KC;
-    const int grp = s_grp;
-    if (grp >= nGroups) return;
-    const int gi = (MODE == 1) ? nGroups - 1 - grp : grp;
-    const int o = wid / g.nJB, jo = wid % g.nJB;
-    const int k = (MODE == 1) ? gi * KC + (KC - 1 - o) : gi * KC + o;
-    const int jb = (MODE == 1) ? g.nJB - 1 - jo : jo;
+    __shared__ int kIn[16], kBack[16], sProg[16];
+    const int lane = threadIdx.x & 31, jo = threadIdx.x >> 5;
+    const int nJB = g.nJB;
+    double *ringK = smem;                                   // [nJB][R][32][NC], filled by the k-producer
+    double *ringJ = smem + (size_t)nJB * R * 32 * NC;       // [nJB][RJ][NC]
+    if (threadIdx.x < 16) { kIn[threadIdx.x] = 0; kBack[threadIdx.x] = 0; sProg[threadIdx.x] = 0; }
+    if (r == 0 && threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
+    cluster.sync();
+    const int grp = *cluster.map_shared_rank(&s_grp, 0);
+    const int nGroups = (g.nz + CS - 1) / CS;
     const int T = g.T;
     int *gprog = sync + SYNC_PROGRESS;
-    if (k < 0 || k >= g.nz) {
-        if (lane == 0) s_prog[wid] = T;       // a plane beyond the mesh: nothing to do
-        return;
-    }
-    const bool crossProducer = (o == KC - 1);
-    const int blk = k * g.nJB + jb;
-    const long long BS = (long long)T * 32;
-    const long long KS = (long long)g.nJB * BS;
-    const int depKw = (o > 0) ? wid - g.nJB : -1;
-    const int kd = (MODE == 1) ? k + 1 : k - 1;
-    const int depKg = (o == 0 && kd >= 0 && kd < g.nz) ? kd * g.nJB + jb : -1;
-    const int depJw = (jo > 0) ? wid - 1 : -1;
-    const int consK = (o + 1 < KC && wid + g.nJB < nW) ? wid + g.nJB : -1;   // in-CTA consumers
-    const int consJ = (jo + 1 < g.nJB) ? wid + 1 : -1;
-    // entry of step t: e0 + t * st
-    const long long e0 = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 + (31 - lane)
-                                     : (long long)blk * BS + lane;
-    const long long st = (MODE == 1) ? -32 : 32;
-    // prefetch assignment: lane -> (array a, step offset s)
-    const int pfA = lane >> 2, pfS = lane & 3;
-    const char *pfBase = nullptr;
-    long long pfStride = 0;
-    {
-        const long long eb = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 : (long long)blk * BS;
-        const double *arr = nullptr;
-        if (MODE == 2) arr = pfA == 0 ? g.D : pfA == 1 ? g.Pz : pfA == 2 ? g.Py : pfA == 3 ? g.Px : nullptr;
-        else if (MODE == 0) arr = pfA == 0 ? g.Az : pfA == 1 ? g.Ay : pfA == 2 ? g.Ax : pfA == 3 ? g.rDinv
-                                : pfA == 4 ? g.rS : nullptr;
-        else arr = pfA == 0 ? g.Bz : pfA == 1 ? g.By : pfA == 2 ? g.Bx : pfA == 3 ? g.wS : nullptr;
-        if (arr) { pfBase = (const char *)(arr + eb); pfStride = st * 8; }
-        else if (pfA == 7) { pfBase = (const char *)(g.cellOf + eb); pfStride = st * 4; }
-    }
-    int seenK = 0, seenJ = 0, seenCK = 0, seenCJ = 0, fail = 0;
-    double yprev[NC];
+    const int gi = (MODE == 1) ? nGroups - 1 - grp : grp;
+    const int k = (MODE == 1) ? gi * CS + (CS - 1 - r) : gi * CS + r;
+    const bool exists = grp < nGroups && k >= 0 && k < g.nz;
+    if (exists) {
+        const int jb = (MODE == 1) ? nJB - 1 - jo : jo;
+        const int blk = k * nJB + jb;
+        const long long BS = (long long)T * 32;
+        const long long KS = (long long)nJB * BS;
+        const bool hasK = (MODE == 1) ? (k + 1 < g.nz) : (k > 0);
+        const bool kLocalProd = hasK && r > 0;
+        const int kGlob = (hasK && r == 0) ? ((MODE == 1) ? k + 1 : k - 1) * nJB + jb : -1;
+        const bool consExists = (MODE == 1) ? (k - 1 >= 0) : (k + 1 < g.nz);
+        const bool kLocalCons = consExists && r + 1 < CS;
+        const bool crossProducer = consExists && r == CS - 1;
+        const int depJ = (jo > 0) ? jo - 1 : -1;
+        const int consJ = (jo + 1 < nJB) ? jo + 1 : -1;
+        double *consRing = kLocalCons ? cluster.map_shared_rank(ringK, r + 1) : nullptr;
+        int *consKin = kLocalCons ? cluster.map_shared_rank(kIn, r + 1) : nullptr;
+        int *prodBack = kLocalProd ? cluster.map_shared_rank(kBack, r - 1) : nullptr;
+        // entry of step t: e0 + t * st
+        const long long e0 = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 + (31 - lane)
+                                         : (long long)blk * BS + lane;
+        const long long st = (MODE == 1) ? -32 : 32;
+        // L1 prefetch assignment: lane -> (array, step offset)
+        const int pfA = lane >> 2, pfS = lane & 3;
+        const char *pfBase = nullptr;
+        long long pfStride = 0;
+        {
+            const long long eb = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 : (long long)blk * BS;
+            const double *arr = nullptr;
+            if (MODE == 2) arr = pfA == 0 ? g.D : pfA == 1 ? g.Pz : pfA == 2 ? g.Py : pfA == 3 ? g.Px : nullptr;
+            else if (MODE == 0) arr = pfA == 0 ? g.Az : pfA == 1 ? g.Ay : pfA == 2 ? g.Ax : pfA == 3 ? g.rDinv
+                                    : pfA == 4 ? g.rS : nullptr;
+            else arr = pfA == 0 ? g.Bz : pfA == 1 ? g.By : pfA == 2 ? g.Bx : pfA == 3 ? g.wS : nullptr;
+            if (arr) { pfBase = (const char *)(arr + eb); pfStride = st * 8; }
+            else if (pfA == 7) { pfBase = (const char *)(g.cellOf + eb); pfStride = st * 4; }
+        }
+        int seenK = 0, seenJ = 0, seenCK = 0, seenCJ = 0, fail = 0;
+        double yprev[NC];
 #pragma unroll
-    for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? 1.0 : 0.0;
+        for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? 1.0 : 0.0;
 
-    for (int t0 = 0; t0 < T; t0 += P) {
-        const int te = t0 + P;                      // T is a multiple of P
-        // ---- L1 prefetch two chunks ahead
-        if (pfBase) {
-            const int tp = t0 + 2 * P + pfS;
-            if (pfS < P && tp < T) {
-                const char *pp = pfBase + tp * pfStride;
-                pf_l1(pp);
-                if (pfA != 7) pf_l1(pp + 128);     // a step line is 256 bytes
-            }
-        }
-        // ---- back-pressure: consumers must have read the slots this chunk overwrites
-        if (consK >= 0 && seenCK < te - R) {
-            int v = 0;
-            if (lane == 0) v = spin_shared(s_prog + consK, te - R, sync, maxSpin);
-            v = __shfl_sync(0xffffffffu, v, 0);
-            if (v < 0) { fail = 1; break; }
-            seenCK = v;
-        }
-        if (consJ >= 0 && seenCJ < te - RJ - 31) {
-            int v = 0;
-            if (lane == 0) v = spin_shared(s_prog + consJ, te - RJ - 31, sync, maxSpin);
-            v = __shfl_sync(0xffffffffu, v, 0);
-            if (v < 0) { fail = 1; break; }
-            seenCJ = v;
-        }
-        // ---- dependencies: previous plane through te, previous j-block through te + 31
-        if ((depKw >= 0 || depKg >= 0) && seenK < te) {
-            int v = 0;
-            if (lane == 0) {
-                if (depKw >= 0) v = spin_shared(s_prog + depKw, te, sync, maxSpin);
-                else v = spin_global(gprog + depKg, te, sync, maxSpin >> 6);
-            }
-            v = __shfl_sync(0xffffffffu, v, 0);
-            if (v < 0) { fail = 1; break; }
-            seenK = v;
-        }
-        if (depJw >= 0 && seenJ < min(T, te + 31)) {
-            int v = 0;
-            if (lane == 0) v = spin_shared(s_prog + depJw, min(T, te + 31), sync, maxSpin);
-            v = __shfl_sync(0xffffffffu, v, 0);
-            if (v < 0) { fail = 1; break; }
-            seenJ = v;
-        }
-        __threadfence_block();
-        // ---- loads of the chunk
-        double c0[P], c1[P], c2[P], c3[P];
-        double rk[P][NC], wk[P][NC], wj[P][NC];
-        int cell[P];
-#pragma unroll
-        for (int s = 0; s < P; ++s) {
-            const int t = t0 + s;
-            const long long e = e0 + t * st;
-            cell[s] = (MODE == 1) ? g.cellOf[e] : 0;
-            if (MODE == 2) {
-                c0[s] = g.D[e]; c1[s] = g.Pz[e]; c2[s] = g.Py[e]; c3[s] = g.Px[e];
-            } else {
-                c0[s] = (MODE == 0) ? g.Az[e] : g.Bz[e];
-                c1[s] = (MODE == 0) ? g.Ay[e] : g.By[e];
-                c2[s] = (MODE == 0) ? g.Ax[e] : g.Bx[e];
-                c3[s] = (MODE == 0) ? g.rDinv[e] : 0.0;
-            }
-            const double zk = (MODE == 2) ? 1.0 : 0.0;
-#pragma unroll
-            for (int q = 0; q < NC; ++q) {
-                const long long oq = (long long)q * g.nSkew;
-                if (MODE == 0) rk[s][q] = g.rS[oq + e];
-                else if (MODE == 1) rk[s][q] = g.wS[oq + e];
-                else rk[s][q] = 0.0;
-                double *kv = (MODE == 2) ? g.rDraw : g.wS + oq;
-                if (depKw >= 0) wk[s][q] = ringK[(((size_t)depKw * R + (t & (R - 1))) * 32 + lane) * NC + q];
-                else if (depKg >= 0) wk[s][q] = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
-                else wk[s][q] = zk;
-                wj[s][q] = (depJw >= 0 && t + 31 < T) ? ringJ[((size_t)depJw * RJ + ((t + 31) & (RJ - 1))) * NC + q]
-                                                      : zk;
-            }
-        }
-        // ---- the recurrence (order of operations of the sequential sweep)
-#pragma unroll
-        for (int s = 0; s < P; ++s) {
-            const int t = t0 + s;
-            const long long e = e0 + t * st;
-#pragma unroll
-            for (int q = 0; q < NC; ++q) {
-                const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
-                const double yj = (lane > 0) ? yup : wj[s][q];
-                double v;
-                if (MODE == 2) {
-                    v = c0[s];
-                    v = __dsub_rn(v, __ddiv_rn(c1[s], wk[s][q]));
-                    v = __dsub_rn(v, __ddiv_rn(c2[s], yj));
-                    v = __dsub_rn(v, __ddiv_rn(c3[s], yprev[q]));
-                    g.rDraw[e] = v;
-                } else {
-                    v = (MODE == 0) ? __dmul_rn(c3[s], rk[s][q]) : rk[s][q];
-                    v = __fma_rn(-c0[s], wk[s][q], v);
-                    v = __fma_rn(-c1[s], yj, v);
-                    v = __fma_rn(-c2[s], yprev[q], v);
-                    if ((mask >> q) & 1u) {
-                        g.wS[(long long)q * g.nSkew + e] = v;
-                        if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = v;
-                    }
+        for (int t0 = 0; t0 < T; t0 += P) {
+            const int te = t0 + P;   // T is a multiple of P
+            if (pfBase) {
+                const int tp = t0 + 2 * P + pfS;
+                if (pfS < P && tp < T) {
+                    const char *pp = pfBase + tp * pfStride;
+                    pf_l1(pp);
+                    if (pfA != 7) pf_l1(pp + 128);   // a step line is 256 bytes
                 }
-                if (consK >= 0) ringK[(((size_t)wid * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
-                if (consJ >= 0 && lane == 31) ringJ[((size_t)wid * RJ + (t & (RJ - 1))) * NC + q] = v;
-                yprev[q] = v;
+            }
+            // ---- back-pressure: consumers have read what this chunk overwrites
+            if (kLocalCons && seenCK < te - R) {
+                int v = 0;
+                if (lane == 0) v = spin_cluster(kBack + jo, te - R, sync, maxSpin);
+                v = __shfl_sync(0xffffffffu, v, 0);
+                if (v < 0) { fail = 1; break; }
+                seenCK = v;
+            }
+            if (consJ >= 0 && seenCJ < te - RJ - 31) {
+                int v = 0;
+                if (lane == 0) v = spin_cluster(sProg + consJ, te - RJ - 31, sync, maxSpin);
+                v = __shfl_sync(0xffffffffu, v, 0);
+                if (v < 0) { fail = 1; break; }
+                seenCJ = v;
+            }
+            // ---- dependencies: previous plane through te, j-block below through te + 31
+            if (hasK && seenK < te) {
+                int v = 0;
+                if (lane == 0)
+                    v = kLocalProd ? spin_cluster(kIn + jo, te, sync, maxSpin)
+                                   : spin_global(gprog + kGlob, te, sync, maxSpin >> 6);
+                v = __shfl_sync(0xffffffffu, v, 0);
+                if (v < 0) { fail = 1; break; }
+                seenK = v;
+            }
+            if (depJ >= 0 && seenJ < min(T, te + 31)) {
+                int v = 0;
+                if (lane == 0) v = spin_cluster(sProg + depJ, min(T, te + 31), sync, maxSpin);
+                v = __shfl_sync(0xffffffffu, v, 0);
+                if (v < 0) { fail = 1; break; }
+                seenJ = v;
+            }
+            fence_cluster();
+            // ---- loads of the chunk
+            double c0[P], c1[P], c2[P], c3[P];
+            double rk[P][NC], wk[P][NC], wj[P][NC];
+            int cell[P];
+#pragma unroll
+            for (int s = 0; s < P; ++s) {
+                const int t = t0 + s;
+                const long long e = e0 + t * st;
+                cell[s] = (MODE == 1) ? g.cellOf[e] : 0;
+                if (MODE == 2) {
+                    c0[s] = g.D[e]; c1[s] = g.Pz[e]; c2[s] = g.Py[e]; c3[s] = g.Px[e];
+                } else {
+                    c0[s] = (MODE == 0) ? g.Az[e] : g.Bz[e];
+                    c1[s] = (MODE == 0) ? g.Ay[e] : g.By[e];
+                    c2[s] = (MODE == 0) ? g.Ax[e] : g.Bx[e];
+                    c3[s] = (MODE == 0) ? g.rDinv[e] : 0.0;
+                }
+                const double zk = (MODE == 2) ? 1.0 : 0.0;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) {
+                    const long long oq = (long long)q * g.nSkew;
+                    if (MODE == 0) rk[s][q] = g.rS[oq + e];
+                    else if (MODE == 1) rk[s][q] = g.wS[oq + e];
+                    else rk[s][q] = 0.0;
+                    const double *kv = (MODE == 2) ? g.rDraw : g.wS + oq;
+                    if (kLocalProd) wk[s][q] = ringK[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q];
+                    else if (kGlob >= 0) wk[s][q] = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
+                    else wk[s][q] = zk;
+                    wj[s][q] = (depJ >= 0 && t + 31 < T) ? ringJ[((size_t)depJ * RJ + ((t + 31) & (RJ - 1))) * NC + q]
+                                                         : zk;
+                }
+            }
+            // ---- the recurrence (order of operations of the sequential sweep)
+#pragma unroll
+            for (int s = 0; s < P; ++s) {
+                const int t = t0 + s;
+                const long long e = e0 + t * st;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) {
+                    const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
+                    const double yj = (lane > 0) ? yup : wj[s][q];
+                    double v;
+                    if (MODE == 2) {
+                        v = c0[s];
+                        v = __dsub_rn(v, __ddiv_rn(c1[s], wk[s][q]));
+                        v = __dsub_rn(v, __ddiv_rn(c2[s], yj));
+                        v = __dsub_rn(v, __ddiv_rn(c3[s], yprev[q]));
+                        g.rDraw[e] = v;
+                    } else {
+                        v = (MODE == 0) ? __dmul_rn(c3[s], rk[s][q]) : rk[s][q];
+                        v = __fma_rn(-c0[s], wk[s][q], v);
+                        v = __fma_rn(-c1[s], yj, v);
+                        v = __fma_rn(-c2[s], yprev[q], v);
+                        if ((mask >> q) & 1u) {
+                            g.wS[(long long)q * g.nSkew + e] = v;
+                            if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = v;
+                        }
+                    }
+                    if (kLocalCons) consRing[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
+                    if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * RJ + (t & (RJ - 1))) * NC + q] = v;
+                    yprev[q] = v;
+                }
+            }
+            // ---- publish
+            fence_cluster();
+            __syncwarp();
+            if (lane == 0) {
+                st_release_cluster(sProg + jo, te);
+                if (kLocalCons) st_release_cluster(consKin + jo, te);
+                if (kLocalProd) st_release_cluster(prodBack + jo, te);
+            }
+            if (crossProducer && ((te % (2 * P)) == 0 || te == T)) {
+                __threadfence();
+                __syncwarp();
+                if (lane == 0) store_release(gprog + blk, te);
             }
         }
-        // ---- publish
-        __threadfence_block();
-        __syncwarp();
-        if (lane == 0) s_prog[wid] = te;
-        if (crossProducer && ((te % (2 * P)) == 0 || te == T)) {
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) store_release(gprog + blk, te);
+        if (fail && lane == 0) {
+            st_release_cluster(sProg + jo, T);
+            if (kLocalCons) st_release_cluster(consKin + jo, T);
+            if (kLocalProd) st_release_cluster(prodBack + jo, T);
+            if (crossProducer) {
+                __threadfence();
+                store_release(gprog + blk, T);
+            }
         }
     }
-    if (fail) {
-        if (lane == 0) s_prog[wid] = T;
-        if (crossProducer) {
-            __threadfence();
-            if (lane == 0) store_release(gprog + blk, T);
-        }
-    }
+    // no CTA may leave while a neighbour can still access its shared memory
+    cluster.sync();
 }
 
 // rS = r gathered into the skewed layout (0 outside the mesh)
@@ -341,29 +392,40 @@ __global__ void k_skew_premul(SkewView g, const int *__restrict__ faceLo, const 
 namespace {
 
 template <int MODE, int NC, int P>
-void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int KC) {
+void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int CS) {
     StructMesh &s = ctx->mesh.sm;
-    const int nW = KC * g.nJB;
-    const size_t shm = ring_bytes<NC, P>(nW);
+    const size_t shm = ring_bytes<NC, P>(g.nJB);
     static bool attr = false;   // per instantiation
     if (!attr) {
         RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)ring_bytes<NC, P>(16)));
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         attr = true;
     }
-    const int nGroups = (g.nz + KC - 1) / KC;
-    k_systolic<MODE, NC, P><<<nGroups, 32 * nW, shm, ctx->stream>>>(g, mask, w, ctx->mesh.N, s.sync.p,
-                                                                     1ll << 26, KC);
+    const int nGroups = (g.nz + CS - 1) / CS;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nGroups * CS);
+    cfg.blockDim = dim3(32 * g.nJB);
+    cfg.dynamicSmemBytes = shm;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<MODE, NC, P>, g, mask, w, ctx->mesh.N, s.sync.p, 1ll << 24));
 }
 
 template <int MODE>
 void launch_mode(rt_ctx *ctx, const SkewView &g, int nc, unsigned mask, double *w) {
     StructMesh &s = ctx->mesh.sm;
     RT_CUDA(cudaMemsetAsync(s.sync.p, 0, sizeof(int) * (SYNC_PROGRESS + g.nz * g.nJB), ctx->stream));
-    const int KC = s.KC;
-    if (MODE == 2 || nc == 1) launch_one<MODE, 1, 4>(ctx, g, mask, w, KC);
-    else if (nc <= 3) launch_one<MODE, 3, 2>(ctx, g, mask, w, KC);
-    else launch_one<MODE, 6, 2>(ctx, g, mask, w, KC);
+    const int CS = s.KC;   // planes (CTAs) per cluster
+    if (MODE == 2 || nc == 1) launch_one<MODE, 1, 4>(ctx, g, mask, w, CS);
+    else if (nc <= 3) launch_one<MODE, 3, 2>(ctx, g, mask, w, CS);
+    else launch_one<MODE, 6, 2>(ctx, g, mask, w, CS);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
     s.pendingCheck = true;
