@@ -245,7 +245,8 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                 if (v < 0) { fail = 1; break; }
                 seenJ = v;
             }
-            fence_cluster();
+            // (lane 0's acquire loads + the warp-wide shuffle order the ring
+            // reads below after the producers' releases)
             // ---- loads of the chunk
             double c0[P], c1[P], c2[P], c3[P];
             double rk[P][NC], wk[P][NC], wj[P][NC];
@@ -279,10 +280,10 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                 }
             }
             // ---- the recurrence (order of operations of the sequential sweep)
+            double out[P][NC];
 #pragma unroll
             for (int s = 0; s < P; ++s) {
                 const int t = t0 + s;
-                const long long e = e0 + t * st;
 #pragma unroll
                 for (int q = 0; q < NC; ++q) {
                     const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
@@ -293,29 +294,40 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                         v = __dsub_rn(v, __ddiv_rn(c1[s], wk[s][q]));
                         v = __dsub_rn(v, __ddiv_rn(c2[s], yj));
                         v = __dsub_rn(v, __ddiv_rn(c3[s], yprev[q]));
-                        g.rDraw[e] = v;
                     } else {
                         v = (MODE == 0) ? __dmul_rn(c3[s], rk[s][q]) : rk[s][q];
                         v = __fma_rn(-c0[s], wk[s][q], v);
                         v = __fma_rn(-c1[s], yj, v);
                         v = __fma_rn(-c2[s], yprev[q], v);
-                        if ((mask >> q) & 1u) {
-                            g.wS[(long long)q * g.nSkew + e] = v;
-                            if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = v;
-                        }
                     }
                     if (kLocalCons) consRing[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
                     if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * RJ + (t & (RJ - 1))) * NC + q] = v;
+                    out[s][q] = v;
                     yprev[q] = v;
                 }
             }
-            // ---- publish
-            fence_cluster();
+            // ---- publish the shared-memory hand-offs: the warp barrier orders
+            // every lane's ring stores before lane 0's cluster-scope release
             __syncwarp();
             if (lane == 0) {
                 st_release_cluster(sProg + jo, te);
                 if (kLocalCons) st_release_cluster(consKin + jo, te);
                 if (kLocalProd) st_release_cluster(prodBack + jo, te);
+            }
+            // ---- global stores after the release, so it never waits for them
+#pragma unroll
+            for (int s = 0; s < P; ++s) {
+                const long long e = e0 + (t0 + s) * st;
+                if (MODE == 2) {
+                    g.rDraw[e] = out[s][0];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) {
+                        if (!((mask >> q) & 1u)) continue;
+                        g.wS[(long long)q * g.nSkew + e] = out[s][q];
+                        if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = out[s][q];
+                    }
+                }
             }
             if (crossProducer && ((te % (2 * P)) == 0 || te == T)) {
                 __threadfence();
