@@ -309,7 +309,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         upload_vec(ctx, cellOf, s.cellOf);
         upload_vec(ctx, lo, s.faceLo);
         upload_vec(ctx, hi, s.faceHi);
-        RT_REQUIRE(s.nJB <= 16, RT_EINVAL, "structured sweeps need ny <= 512");
+        RT_REQUIRE(s.nJB <= 8, RT_EINVAL, "structured sweeps need ny <= 256");
         s.KC = std::max(1, std::min(nz, 8));   // planes (CTAs) per thread-block cluster
         s.sync.alloc(SYNC_PROGRESS + (size_t)nz * s.nJB);
         s.data.alloc((size_t)(12 + 6 + 6) * s.nSkew);

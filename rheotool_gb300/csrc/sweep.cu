@@ -114,10 +114,28 @@ template <int P> struct Ring {
     static constexpr int RJ = 64;                    // j-block ring
 };
 
-template <int NC, int P>
-size_t ring_bytes(int nJB) {
-    return (size_t)nJB * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
+// Per-warp staging of a chunk's coefficients (cp.async, two buffers): NA
+// double arrays of P steps x 32 lanes, plus the cells of the backward sweep.
+template <int MODE, int NC> struct Stage { static constexpr int NA = 4 + NC; };
+
+template <int MODE, int NC, int P>
+size_t sweep_smem_bytes(int nJB) {
+    const size_t rings = (size_t)nJB * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
+    const size_t stage = (size_t)nJB * 2 * P * 32 * (Stage<MODE, NC>::NA * sizeof(double) + sizeof(int));
+    return rings + stage;
 }
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // MODE 0: forward application, 1: backward application, 2: rD recurrence.
 //
@@ -137,14 +155,17 @@ size_t ring_bytes(int nJB) {
 // none leaves before the final cluster barrier, so no CTA ever accesses the
 // shared memory of a CTA that has exited.
 //
-// Each SM holds one plane: the FP64 pipe of GB300 retires about two lanes per
-// cycle per SM, so spreading the wavefront over many SMs is what makes it fast.
+// Latency: a chunk's coefficients are staged into shared memory with cp.async
+// one chunk ahead, and a chunk's global stores are issued one chunk late, so
+// the releases never wait for stores in flight.  The remaining per-step cost
+// is the dependent FP64 chain (one multiply and three fused multiply-adds on
+// a pipe that retires about two FP64 lanes per cycle per SM).
 // Invalid entries (outside the mesh, padding) have zero coefficients and zero
 // right-hand sides, so every lane runs the same branch-free recurrence.
 template <int MODE, int NC, int P>
 __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, double *__restrict__ w, int N,
                                                   int *sync, long long maxSpin) {
-    constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ;
+    constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA;
     cg::cluster_group cluster = cg::this_cluster();
     const int CS = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
     extern __shared__ double smem[];
@@ -153,7 +174,11 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
     const int lane = threadIdx.x & 31, jo = threadIdx.x >> 5;
     const int nJB = g.nJB;
     double *ringK = smem;                                   // [nJB][R][32][NC], filled by the k-producer
-    double *ringJ = smem + (size_t)nJB * R * 32 * NC;       // [nJB][RJ][NC]
+    double *ringJ = ringK + (size_t)nJB * R * 32 * NC;      // [nJB][RJ][NC]
+    double *stage = ringJ + (size_t)nJB * RJ * NC;          // [nJB][2][P][NA][32]
+    int *cstage = (int *)(stage + (size_t)nJB * 2 * P * NA * 32);   // [nJB][2][P][32]
+    double *myStage = stage + (size_t)jo * 2 * P * NA * 32;
+    int *myCStage = cstage + (size_t)jo * 2 * P * 32;
     if (threadIdx.x < 16) { kIn[threadIdx.x] = 0; kBack[threadIdx.x] = 0; sProg[threadIdx.x] = 0; }
     if (r == 0 && threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
     cluster.sync();
@@ -184,34 +209,46 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
         const long long e0 = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 + (31 - lane)
                                          : (long long)blk * BS + lane;
         const long long st = (MODE == 1) ? -32 : 32;
-        // L1 prefetch assignment: lane -> (array, step offset)
-        const int pfA = lane >> 2, pfS = lane & 3;
-        const char *pfBase = nullptr;
-        long long pfStride = 0;
-        {
-            const long long eb = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 : (long long)blk * BS;
-            const double *arr = nullptr;
-            if (MODE == 2) arr = pfA == 0 ? g.D : pfA == 1 ? g.Pz : pfA == 2 ? g.Py : pfA == 3 ? g.Px : nullptr;
-            else if (MODE == 0) arr = pfA == 0 ? g.Az : pfA == 1 ? g.Ay : pfA == 2 ? g.Ax : pfA == 3 ? g.rDinv
-                                    : pfA == 4 ? g.rS : nullptr;
-            else arr = pfA == 0 ? g.Bz : pfA == 1 ? g.By : pfA == 2 ? g.Bx : pfA == 3 ? g.wS : nullptr;
-            if (arr) { pfBase = (const char *)(arr + eb); pfStride = st * 8; }
-            else if (pfA == 7) { pfBase = (const char *)(g.cellOf + eb); pfStride = st * 4; }
-        }
+        // stage the coefficients of the chunk starting at step c0 into buffer b
+        auto stage_chunk = [&](int tc, int b) {
+#pragma unroll
+            for (int s = 0; s < P; ++s) {
+                const long long e = e0 + (tc + s) * st;
+                double *d = myStage + ((size_t)(b * P + s) * NA) * 32 + lane;
+                if (MODE == 2) {
+                    cp_async8(d + 0 * 32, g.D + e); cp_async8(d + 1 * 32, g.Pz + e);
+                    cp_async8(d + 2 * 32, g.Py + e); cp_async8(d + 3 * 32, g.Px + e);
+                } else {
+                    cp_async8(d + 0 * 32, (MODE == 0 ? g.Az : g.Bz) + e);
+                    cp_async8(d + 1 * 32, (MODE == 0 ? g.Ay : g.By) + e);
+                    cp_async8(d + 2 * 32, (MODE == 0 ? g.Ax : g.Bx) + e);
+                    if (MODE == 0) cp_async8(d + 3 * 32, g.rDinv + e);
+#pragma unroll
+                    for (int q = 0; q < NC; ++q)
+                        cp_async8(d + (4 + q) * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + e);
+                    if (MODE == 1) cp_async4(myCStage + (b * P + s) * 32 + lane, g.cellOf + e);
+                }
+            }
+        };
         int seenK = 0, seenJ = 0, seenCK = 0, seenCJ = 0, fail = 0;
         double yprev[NC];
 #pragma unroll
         for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? 1.0 : 0.0;
+        double prevOut[P][NC];
+        int prevCell[P];
+        int prevT0 = -1;
+        stage_chunk(0, 0);
+        cp_async_commit();
 
         for (int t0 = 0; t0 < T; t0 += P) {
             const int te = t0 + P;   // T is a multiple of P
-            if (pfBase) {
-                const int tp = t0 + 2 * P + pfS;
-                if (pfS < P && tp < T) {
-                    const char *pp = pfBase + tp * pfStride;
-                    pf_l1(pp);
-                    if (pfA != 7) pf_l1(pp + 128);   // a step line is 256 bytes
-                }
+            const int buf = (t0 / P) & 1;
+            if (te < T) {
+                stage_chunk(te, buf ^ 1);
+                cp_async_commit();
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
             // ---- back-pressure: consumers have read what this chunk overwrites
             if (kLocalCons && seenCK < te - R) {
@@ -247,58 +284,41 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
             }
             // (lane 0's acquire loads + the warp-wide shuffle order the ring
             // reads below after the producers' releases)
-            // ---- loads of the chunk
-            double c0[P], c1[P], c2[P], c3[P];
-            double rk[P][NC], wk[P][NC], wj[P][NC];
+            // ---- the recurrence (order of operations of the sequential sweep)
+            double out[P][NC];
             int cell[P];
 #pragma unroll
             for (int s = 0; s < P; ++s) {
                 const int t = t0 + s;
-                const long long e = e0 + t * st;
-                cell[s] = (MODE == 1) ? g.cellOf[e] : 0;
-                if (MODE == 2) {
-                    c0[s] = g.D[e]; c1[s] = g.Pz[e]; c2[s] = g.Py[e]; c3[s] = g.Px[e];
-                } else {
-                    c0[s] = (MODE == 0) ? g.Az[e] : g.Bz[e];
-                    c1[s] = (MODE == 0) ? g.Ay[e] : g.By[e];
-                    c2[s] = (MODE == 0) ? g.Ax[e] : g.Bx[e];
-                    c3[s] = (MODE == 0) ? g.rDinv[e] : 0.0;
-                }
+                const double *d = myStage + ((size_t)(buf * P + s) * NA) * 32 + lane;
+                const double c0 = d[0], c1 = d[32], c2 = d[64], c3 = (MODE == 1) ? 0.0 : d[96];
+                cell[s] = (MODE == 1) ? myCStage[(buf * P + s) * 32 + lane] : 0;
                 const double zk = (MODE == 2) ? 1.0 : 0.0;
 #pragma unroll
                 for (int q = 0; q < NC; ++q) {
-                    const long long oq = (long long)q * g.nSkew;
-                    if (MODE == 0) rk[s][q] = g.rS[oq + e];
-                    else if (MODE == 1) rk[s][q] = g.wS[oq + e];
-                    else rk[s][q] = 0.0;
-                    const double *kv = (MODE == 2) ? g.rDraw : g.wS + oq;
-                    if (kLocalProd) wk[s][q] = ringK[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q];
-                    else if (kGlob >= 0) wk[s][q] = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
-                    else wk[s][q] = zk;
-                    wj[s][q] = (depJ >= 0 && t + 31 < T) ? ringJ[((size_t)depJ * RJ + ((t + 31) & (RJ - 1))) * NC + q]
-                                                         : zk;
-                }
-            }
-            // ---- the recurrence (order of operations of the sequential sweep)
-            double out[P][NC];
-#pragma unroll
-            for (int s = 0; s < P; ++s) {
-                const int t = t0 + s;
-#pragma unroll
-                for (int q = 0; q < NC; ++q) {
+                    double wk;
+                    if (kLocalProd) wk = ringK[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q];
+                    else if (kGlob >= 0) {
+                        const long long e = e0 + t * st;
+                        const double *kv = (MODE == 2) ? g.rDraw : g.wS + (long long)q * g.nSkew;
+                        wk = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
+                    } else wk = zk;
+                    const double wj = (depJ >= 0 && t + 31 < T)
+                                          ? ringJ[((size_t)depJ * RJ + ((t + 31) & (RJ - 1))) * NC + q] : zk;
                     const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
-                    const double yj = (lane > 0) ? yup : wj[s][q];
+                    const double yj = (lane > 0) ? yup : wj;
                     double v;
                     if (MODE == 2) {
-                        v = c0[s];
-                        v = __dsub_rn(v, __ddiv_rn(c1[s], wk[s][q]));
-                        v = __dsub_rn(v, __ddiv_rn(c2[s], yj));
-                        v = __dsub_rn(v, __ddiv_rn(c3[s], yprev[q]));
+                        v = c0;
+                        v = __dsub_rn(v, __ddiv_rn(c1, wk));
+                        v = __dsub_rn(v, __ddiv_rn(c2, yj));
+                        v = __dsub_rn(v, __ddiv_rn(c3, yprev[q]));
                     } else {
-                        v = (MODE == 0) ? __dmul_rn(c3[s], rk[s][q]) : rk[s][q];
-                        v = __fma_rn(-c0[s], wk[s][q], v);
-                        v = __fma_rn(-c1[s], yj, v);
-                        v = __fma_rn(-c2[s], yprev[q], v);
+                        const double rk = d[(4 + q) * 32];
+                        v = (MODE == 0) ? __dmul_rn(c3, rk) : rk;
+                        v = __fma_rn(-c0, wk, v);
+                        v = __fma_rn(-c1, yj, v);
+                        v = __fma_rn(-c2, yprev[q], v);
                     }
                     if (kLocalCons) consRing[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
                     if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * RJ + (t & (RJ - 1))) * NC + q] = v;
@@ -314,27 +334,58 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                 if (kLocalCons) st_release_cluster(consKin + jo, te);
                 if (kLocalProd) st_release_cluster(prodBack + jo, te);
             }
-            // ---- global stores after the release, so it never waits for them
+            // ---- the previous chunk's global stores (one chunk late)
+            if (prevT0 >= 0) {
+#pragma unroll
+                for (int s = 0; s < P; ++s) {
+                    const long long e = e0 + (prevT0 + s) * st;
+                    if (MODE == 2) {
+                        g.rDraw[e] = prevOut[s][0];
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < NC; ++q) {
+                            if (!((mask >> q) & 1u)) continue;
+                            g.wS[(long long)q * g.nSkew + e] = prevOut[s][q];
+                            if (MODE == 1 && prevCell[s] >= 0) w[(long long)q * N + prevCell[s]] = prevOut[s][q];
+                        }
+                    }
+                }
+                if (crossProducer && ((t0 % (2 * P)) == 0)) {
+                    __threadfence();
+                    __syncwarp();
+                    if (lane == 0) store_release(gprog + blk, t0);
+                }
+            }
 #pragma unroll
             for (int s = 0; s < P; ++s) {
-                const long long e = e0 + (t0 + s) * st;
+                prevCell[s] = cell[s];
+#pragma unroll
+                for (int q = 0; q < NC; ++q) prevOut[s][q] = out[s][q];
+            }
+            prevT0 = t0;
+        }
+        if (!fail && prevT0 >= 0) {
+#pragma unroll
+            for (int s = 0; s < P; ++s) {
+                const long long e = e0 + (prevT0 + s) * st;
                 if (MODE == 2) {
-                    g.rDraw[e] = out[s][0];
+                    g.rDraw[e] = prevOut[s][0];
                 } else {
 #pragma unroll
                     for (int q = 0; q < NC; ++q) {
                         if (!((mask >> q) & 1u)) continue;
-                        g.wS[(long long)q * g.nSkew + e] = out[s][q];
-                        if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = out[s][q];
+                        g.wS[(long long)q * g.nSkew + e] = prevOut[s][q];
+                        if (MODE == 1 && prevCell[s] >= 0) w[(long long)q * N + prevCell[s]] = prevOut[s][q];
                     }
                 }
             }
-            if (crossProducer && ((te % (2 * P)) == 0 || te == T)) {
+            if (crossProducer) {
                 __threadfence();
                 __syncwarp();
-                if (lane == 0) store_release(gprog + blk, te);
+                if (lane == 0) store_release(gprog + blk, T);
             }
         }
+        cp_async_wait<0>();
         if (fail && lane == 0) {
             st_release_cluster(sProg + jo, T);
             if (kLocalCons) st_release_cluster(consKin + jo, T);
@@ -406,11 +457,11 @@ namespace {
 template <int MODE, int NC, int P>
 void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int CS) {
     StructMesh &s = ctx->mesh.sm;
-    const size_t shm = ring_bytes<NC, P>(g.nJB);
+    const size_t shm = sweep_smem_bytes<MODE, NC, P>(g.nJB);
     static bool attr = false;   // per instantiation
     if (!attr) {
         RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ring_bytes<NC, P>(16)));
+                                     (int)sweep_smem_bytes<MODE, NC, P>(8)));
         RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         attr = true;
     }
