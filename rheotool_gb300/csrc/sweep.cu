@@ -110,8 +110,8 @@ __device__ __forceinline__ int spin_cluster(const int *c, int need, int *sync, l
 
 // Ring depths (steps) of the hand-offs for chunk size P.
 template <int P> struct Ring {
-    static constexpr int R = (P >= 4) ? 4 * P : 4;   // plane ring, at least two chunks
-    static constexpr int RJ = 64;                    // j-block ring
+    static constexpr int R = (P >= 8) ? 2 * P : (P >= 4) ? 4 * P : 4;   // plane ring, at least two chunks
+    static constexpr int RJ = (P >= 8) ? 128 : 64;    // j-block ring (power of two): the consumer lags ~32 + P steps
 };
 
 // Per-warp staging of a chunk's coefficients (cp.async, two buffers): NA
@@ -486,7 +486,7 @@ void launch_mode(rt_ctx *ctx, const SkewView &g, int nc, unsigned mask, double *
     StructMesh &s = ctx->mesh.sm;
     RT_CUDA(cudaMemsetAsync(s.sync.p, 0, sizeof(int) * (SYNC_PROGRESS + g.nz * g.nJB), ctx->stream));
     const int CS = s.KC;   // planes (CTAs) per cluster
-    if (MODE == 2 || nc == 1) launch_one<MODE, 1, 4>(ctx, g, mask, w, CS);
+    if (MODE == 2 || nc == 1) launch_one<MODE, 1, 8>(ctx, g, mask, w, CS);
     else if (nc <= 3) launch_one<MODE, 3, 2>(ctx, g, mask, w, CS);
     else launch_one<MODE, 6, 2>(ctx, g, mask, w, CS);
     RT_CHECK_LAUNCH();
