@@ -118,10 +118,12 @@ template <int P> struct Ring {
 // double arrays of P steps x 32 lanes, plus the cells of the backward sweep.
 template <int MODE, int NC> struct Stage { static constexpr int NA = 4 + NC; };
 
+constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per CTA on sm_100-class parts
+
 template <int MODE, int NC, int P>
 size_t sweep_smem_bytes(int nJB) {
     const size_t rings = (size_t)nJB * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
-    const size_t stage = (size_t)nJB * 2 * P * 32 * (Stage<MODE, NC>::NA * sizeof(double) + sizeof(int));
+    const size_t stage = (size_t)nJB * 3 * P * 32 * (Stage<MODE, NC>::NA * sizeof(double) + sizeof(int));
     return rings + stage;
 }
 
@@ -175,10 +177,10 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
     const int nJB = g.nJB;
     double *ringK = smem;                                   // [nJB][R][32][NC], filled by the k-producer
     double *ringJ = ringK + (size_t)nJB * R * 32 * NC;      // [nJB][RJ][NC]
-    double *stage = ringJ + (size_t)nJB * RJ * NC;          // [nJB][2][P][NA][32]
-    int *cstage = (int *)(stage + (size_t)nJB * 2 * P * NA * 32);   // [nJB][2][P][32]
-    double *myStage = stage + (size_t)jo * 2 * P * NA * 32;
-    int *myCStage = cstage + (size_t)jo * 2 * P * 32;
+    double *stage = ringJ + (size_t)nJB * RJ * NC;          // [nJB][3][P][NA][32]
+    int *cstage = (int *)(stage + (size_t)nJB * 3 * P * NA * 32);   // [nJB][3][P][32]
+    double *myStage = stage + (size_t)jo * 3 * P * NA * 32;
+    int *myCStage = cstage + (size_t)jo * 3 * P * 32;
     if (threadIdx.x < 16) { kIn[threadIdx.x] = 0; kBack[threadIdx.x] = 0; sProg[threadIdx.x] = 0; }
     if (r == 0 && threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
     cluster.sync();
@@ -237,19 +239,17 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
         double prevOut[P][NC];
         int prevCell[P];
         int prevT0 = -1;
+        // three staging buffers: chunk c is staged two chunks ahead, right
+        // after the release of chunk c - 2, so no release waits for it
         stage_chunk(0, 0);
+        cp_async_commit();
+        if (P < T) stage_chunk(P, 1);
         cp_async_commit();
 
         for (int t0 = 0; t0 < T; t0 += P) {
             const int te = t0 + P;   // T is a multiple of P
-            const int buf = (t0 / P) & 1;
-            if (te < T) {
-                stage_chunk(te, buf ^ 1);
-                cp_async_commit();
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
+            const int buf = (t0 / P) % 3;
+            cp_async_wait<1>();      // this chunk's group is complete
             // ---- back-pressure: consumers have read what this chunk overwrites
             if (kLocalCons && seenCK < te - R) {
                 int v = 0;
@@ -334,6 +334,9 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                 if (kLocalCons) st_release_cluster(consKin + jo, te);
                 if (kLocalProd) st_release_cluster(prodBack + jo, te);
             }
+            // ---- stage chunk c + 2 (always commit a group, possibly empty)
+            if (te + P < T) stage_chunk(te + P, ((t0 / P) + 2) % 3);
+            cp_async_commit();
             // ---- the previous chunk's global stores (one chunk late)
             if (prevT0 >= 0) {
 #pragma unroll
@@ -458,12 +461,11 @@ template <int MODE, int NC, int P>
 void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int CS) {
     StructMesh &s = ctx->mesh.sm;
     const size_t shm = sweep_smem_bytes<MODE, NC, P>(g.nJB);
-    static bool attr = false;   // per instantiation
-    if (!attr) {
-        RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sweep_smem_bytes<MODE, NC, P>(8)));
+    static size_t attr = 0;   // per instantiation: dynamic shared memory opted in so far
+    if (shm > attr) {
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
         RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        attr = true;
+        attr = shm;
     }
     const int nGroups = (g.nz + CS - 1) / CS;
     cudaLaunchConfig_t cfg = {};
@@ -486,7 +488,11 @@ void launch_mode(rt_ctx *ctx, const SkewView &g, int nc, unsigned mask, double *
     StructMesh &s = ctx->mesh.sm;
     RT_CUDA(cudaMemsetAsync(s.sync.p, 0, sizeof(int) * (SYNC_PROGRESS + g.nz * g.nJB), ctx->stream));
     const int CS = s.KC;   // planes (CTAs) per cluster
-    if (MODE == 2 || nc == 1) launch_one<MODE, 1, 8>(ctx, g, mask, w, CS);
+    if (MODE == 2 || nc == 1) {
+        // chunks of 8 steps when the staging fits in shared memory, else 4
+        if (sweep_smem_bytes<MODE, 1, 8>(g.nJB) <= kMaxSmem) launch_one<MODE, 1, 8>(ctx, g, mask, w, CS);
+        else launch_one<MODE, 1, 4>(ctx, g, mask, w, CS);
+    }
     else if (nc <= 3) launch_one<MODE, 3, 2>(ctx, g, mask, w, CS);
     else launch_one<MODE, 6, 2>(ctx, g, mask, w, CS);
     RT_CHECK_LAUNCH();
