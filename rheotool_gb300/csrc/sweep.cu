@@ -287,11 +287,19 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
             // ---- the recurrence (order of operations of the sequential sweep)
             double out[P][NC];
             int cell[P];
+            // the terms of a step that do not depend on the previous step (the
+            // right-hand side and the k neighbour) are formed for the whole
+            // chunk first, so only the j and i terms stay on the dependent chain
+            double pre[P][NC], wjv[P][NC], cy[P], cx[P];
 #pragma unroll
             for (int s = 0; s < P; ++s) {
                 const int t = t0 + s;
                 const double *d = myStage + ((size_t)(buf * P + s) * NA) * 32 + lane;
-                const double c0 = d[0], c1 = d[32], c2 = d[64], c3 = (MODE == 1) ? 0.0 : d[96];
+                // staged arrays: MODE 2: D, Pz, Py, Px; MODE 0/1: z, y, x
+                // coefficients, then (MODE 0) 1/rD, then the right-hand sides
+                const double c0 = d[0], c3 = (MODE == 0) ? d[96] : 0.0;
+                cy[s] = (MODE == 2) ? d[64] : d[32];
+                cx[s] = (MODE == 2) ? d[96] : d[64];
                 cell[s] = (MODE == 1) ? myCStage[(buf * P + s) * 32 + lane] : 0;
                 const double zk = (MODE == 2) ? 1.0 : 0.0;
 #pragma unroll
@@ -303,22 +311,31 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
                         const double *kv = (MODE == 2) ? g.rDraw : g.wS + (long long)q * g.nSkew;
                         wk = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
                     } else wk = zk;
-                    const double wj = (depJ >= 0 && t + 31 < T)
-                                          ? ringJ[((size_t)depJ * RJ + ((t + 31) & (RJ - 1))) * NC + q] : zk;
-                    const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
-                    const double yj = (lane > 0) ? yup : wj;
-                    double v;
+                    wjv[s][q] = (depJ >= 0 && t + 31 < T)
+                                    ? ringJ[((size_t)depJ * RJ + ((t + 31) & (RJ - 1))) * NC + q] : zk;
                     if (MODE == 2) {
-                        v = c0;
-                        v = __dsub_rn(v, __ddiv_rn(c1, wk));
-                        v = __dsub_rn(v, __ddiv_rn(c2, yj));
-                        v = __dsub_rn(v, __ddiv_rn(c3, yprev[q]));
+                        pre[s][q] = __dsub_rn(c0, __ddiv_rn(d[32], wk));   // D - Pz / rD(k-1)
                     } else {
                         const double rk = d[(4 + q) * 32];
-                        v = (MODE == 0) ? __dmul_rn(c3, rk) : rk;
-                        v = __fma_rn(-c0, wk, v);
-                        v = __fma_rn(-c1, yj, v);
-                        v = __fma_rn(-c2, yprev[q], v);
+                        const double v0 = (MODE == 0) ? __dmul_rn(c3, rk) : rk;
+                        pre[s][q] = __fma_rn(-c0, wk, v0);
+                    }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < P; ++s) {
+                const int t = t0 + s;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) {
+                    const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
+                    const double yj = (lane > 0) ? yup : wjv[s][q];
+                    double v;
+                    if (MODE == 2) {
+                        v = __dsub_rn(pre[s][q], __ddiv_rn(cy[s], yj));
+                        v = __dsub_rn(v, __ddiv_rn(cx[s], yprev[q]));
+                    } else {
+                        v = __fma_rn(-cy[s], yj, pre[s][q]);
+                        v = __fma_rn(-cx[s], yprev[q], v);
                     }
                     if (kLocalCons) consRing[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
                     if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * RJ + (t & (RJ - 1))) * NC + q] = v;
@@ -330,7 +347,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
             // every lane's ring stores before lane 0's cluster-scope release
             __syncwarp();
             if (lane == 0) {
-                st_release_cluster(sProg + jo, te);
+                if (consJ >= 0 || depJ >= 0) st_release_cluster(sProg + jo, te);
                 if (kLocalCons) st_release_cluster(consKin + jo, te);
                 if (kLocalProd) st_release_cluster(prodBack + jo, te);
             }
