@@ -205,6 +205,21 @@ rt_status rt_residual(rt_ctx *ctx, const double *diag, const double *upper,
                       const double *lower, const double *source,
                       const double *psi, double *residual);
 
+/* rt_residual for callers that cannot allocate device memory (a solver
+ * callback inside another library's Krylov loop, code being captured into a
+ * CUDA graph by its owner, a host whose device memory belongs to its own
+ * pool).  No reference counterpart: an addition of this library.  diag, upper,
+ * lower, source and psi are DEVICE pointers on the context's device (nCells /
+ * nFaces doubles); residual is a host pointer.  The reduction scratch is a
+ * static device array inside the library, so the call allocates nothing; it
+ * limits meshes to 2,097,152 cells (RT_EINVAL beyond).  The first call on a
+ * device resolves that array's address, so make it before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+rt_status rt_residual_noalloc(rt_ctx *ctx, const double *diag, const double *upper,
+                              const double *lower, const double *source,
+                              const double *psi, double *residual);
+
 /* One constitutiveEq::correct() on the device-resident U, phi, theta, eig
  * fields; gradU (9*nCells AoS) may be NULL (then fvc::grad(U) is used).
  * thetaPerf gets 6 entries (components not solved have nIterations = -1). */

@@ -152,6 +152,7 @@ def load_library(path: str = LIBNAME):
         "rt_field_get": ([vp, C.c_int32, _dp, _dp], C.c_int32),
         "rt_ldu_solve": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int32, P(rt_solver_ctl), P(rt_solver_perf)], C.c_int32),
         "rt_residual": ([vp, _dp, _dp, _dp, _dp, _dp, _dp], C.c_int32),
+        "rt_residual_noalloc": ([vp, vp, vp, vp, vp, vp, _dp], C.c_int32),
         "rt_constitutive_correct": ([vp, _dp, P(rt_solver_perf)], C.c_int32),
         "rt_step": ([vp, C.c_int32, P(rt_step_perf)], C.c_int32),
         "rt_op_grad": ([vp, _dp, _dp, _dp], C.c_int32),

@@ -1,0 +1,59 @@
+"""rt_residual_noalloc: the residual entry point for callers that cannot
+allocate device memory (a callback inside another library's Krylov loop, code
+already being captured into a CUDA graph, a host whose device memory is owned
+by its own pool).  The inputs live in device memory the test allocates; the
+library allocates nothing and keeps its reduction scratch in a static device
+array.  Its result must equal rt_residual's (host arrays) to the round-off of
+a different reduction order, on two calls in a row (the second call reuses
+the shared scratch left by the first).
+
+This file is collected last so that a run stopping at the first failure has
+already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(mesh, seed):
+    rng = np.random.default_rng(seed)
+    F, N = mesh.nFaces, mesh.nCells
+    phi = rng.normal(size=F) * mesh.magSf
+    u = (phi >= 0).astype(float)
+    g = mesh.magSf * mesh.deltaCoeffs * (1.0 + rng.random(F))
+    lower = -u * phi - g
+    upper = (1 - u) * phi - g
+    diag = np.zeros(N)
+    np.subtract.at(diag, mesh.owner, lower)
+    np.subtract.at(diag, mesh.neighbour, upper)
+    diag += 3.0 * mesh.V
+    b = rng.normal(size=N) * mesh.V
+    x = rng.normal(size=N)
+    return diag, upper, lower, b, x
+
+
+def test_residual_noalloc_matches_rt_residual():
+    torch = pytest.importorskip("torch")
+    from rheotool_gb300 import abi
+    from rheotool_gb300.mesh import contraction_mesh
+    from rheotool_gb300.runtime import Context
+
+    mesh = contraction_mesh(10, 8, 6, 4, 5, 4.0, 4.0)
+    ctx = Context(0)
+    try:
+        ctx.upload_mesh(mesh)
+        for call, seed in enumerate((101, 202)):
+            diag, upper, lower, b, x = _system(mesh, seed)
+            ref = ctx.residual(diag, upper, lower, b, x)
+            dev = [torch.tensor(a, dtype=torch.float64, device="cuda:0") for a in (diag, upper, lower, b, x)]
+            torch.cuda.synchronize()
+            out = C.c_double(-1.0)
+            st = ctx.lib.rt_residual_noalloc(ctx._ctx, *[C.c_void_p(t.data_ptr()) for t in dev], C.byref(out))
+            assert st == abi.RT_OK, ctx.lib.rt_last_error(ctx._ctx)
+            assert ref > 0
+            assert abs(out.value - ref) <= 1e-12 * ref, (call, out.value, ref)
+    finally:
+        ctx.close()
