@@ -4,20 +4,26 @@
 Workload (one "step" = one rheoFoam time step: UEqn, SIMPLEC pEqn with a
 PCG-DIC pressure solve, GiesekusLog constitutive update with six
 PBiCGStab-DILU theta solves): 3-D planar 4:1 contraction, 1,000,000 hex cells,
-Giesekus-Log alpha = 0.1, Wi = 2, beta = 1/9, FP64 plain path, synthetic
-mesh and inputs (no dataset exists for it).
+Giesekus-Log alpha = 0.1, Wi = 2, beta = 1/9, synthetic mesh and inputs (no
+dataset exists for it).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--precision mixed|fp64]
 
 Prints one JSON line.  `value` is device-timed (CUDA events on the library's
-stream) whole-job cell-steps/s with all fields resident in HBM; `e2e` is the
-same metric through the C ABI with host buffers (each step uploads U, p, phi
-and downloads U, p, phi, tau); `roofline` is for the operation with the
-largest device time, measured live with CUDA events; `cpu_baseline` is the
-FP64 CPU oracle on a bounded sample of the same workload.
-`--impl reference` times the reference algorithm on the host cores: the
-reference itself (rheoTool on OpenFOAM v9) cannot be built here, so its FP64
-CPU restatement (oracle/) runs instead, with all host threads.
+stream) whole-job cell-steps/s of the selected form with all fields resident
+in HBM: by default the mixed-precision form (FP32 Krylov iterations and
+sweeps, FP64 residual replacement, FP64 assembly and constitutive update).
+The FP64 plain path is timed in the same run on the same case (`plain_fp64`)
+and `field_error_vs_fp64` gives each field's relative L2 difference between
+the two forms after the same number of steps from the same initial state.
+`e2e` is the same metric through the C ABI with host buffers (each step
+uploads U, p, phi and downloads U, p, phi, tau); `roofline` is for the
+operation with the largest device time, measured live with CUDA events;
+`cpu_baseline` is the FP64 CPU oracle on a bounded sample of the same
+workload.  `--impl reference` times the reference algorithm on the host
+cores: the reference itself (rheoTool on OpenFOAM v9) cannot be built here,
+so its FP64 CPU restatement (oracle/) runs instead, with all host threads.
 """
 from __future__ import annotations
 
@@ -35,7 +41,7 @@ METRIC = "cell-steps/s (1M-cell Giesekus)"
 UNIT = "cell-steps/s"
 WORKLOAD = ("3-D planar 4:1 contraction, 1,000,000 hex cells (266x100x50 bounding grid, graded), "
             "GiesekusLog alpha=0.1, Wi=2, beta=1/9, rho=0.01, dt=5e-3, Euler, GaussDefCmpw cubista, "
-            "p PCG-DIC 1e-8, U/theta PBiCGStab-DILU 1e-10, FP64 plain path")
+            "p PCG-DIC 1e-8, U/theta PBiCGStab-DILU 1e-10")
 SAMPLE_DIMS = dict(nx_up=67, nx_down=66, ny_in=25, ny_out=13, nz=25)   # 126,675 cells
 
 
@@ -50,6 +56,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="form timed for `value` (the other is timed beside it unless --no-plain)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the second form")
     return ap.parse_args()
 
 
@@ -192,28 +201,58 @@ def main():
 
     case = make_case(args.small)
     N, F, NB = case.mesh.nCells, case.mesh.nFaces, case.mesh.nBFaces
+    prec = abi.RT_PREC_MIXED if args.precision == "mixed" else abi.RT_PREC_FP64
+    other = abi.RT_PREC_FP64 if prec == abi.RT_PREC_MIXED else abi.RT_PREC_MIXED
+
+    def timed(ctx, precision, clocks):
+        case.precision = precision
+        ctx.setup_case(case)
+        if args.warmup:
+            ctx.step(args.warmup)
+        ctx.sync()
+        if pg:
+            pg.barrier()
+        clk = Clocks(local) if clocks else None
+        k0 = ctx.kernel_count()
+        ctx.timer_start()
+        perf = ctx.step(args.steps)
+        ms = ctx.timer_stop()
+        launches = ctx.kernel_count() - k0
+        clocks = clk.stop() if clk else None
+        if pg:
+            import torch
+            t = torch.tensor([ms], dtype=torch.float64)
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            ms = float(t[0])
+            pg.barrier()
+        return ms, perf, launches, clocks
+
+    def iters(perf):
+        return {"p": perf.p.nIterations, "U": [perf.U[k].nIterations for k in range(3)],
+                "theta": [perf.theta[k].nIterations for k in range(6)]}
+
     ctx = Context(local)
-    ctx.setup_case(case)
-    if args.warmup:
-        ctx.step(args.warmup)
-    ctx.sync()
-    if pg:
-        pg.barrier()
-    clk = Clocks(local)
-    k0 = ctx.kernel_count()
-    ctx.timer_start()
-    perf = ctx.step(args.steps)
-    ms = ctx.timer_stop()
-    launches = ctx.kernel_count() - k0
-    clocks = clk.stop()
-    if pg:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t[0])
-        pg.barrier()
+    ms, perf, launches, clocks = timed(ctx, prec, True)
     total_cells = N * args.steps * world
     value = total_cells / (ms * 1e-3)
+
+    # ---- the other form on the same case, same steps; field differences ---
+    second = None
+    field_err = None
+    if not args.no_plain:
+        ctx2 = Context(local)
+        ms2, perf2, _, _ = timed(ctx2, other, False)
+        a, b = ctx.fields(), ctx2.fields()
+        ref, got = (b, a) if prec == abi.RT_PREC_MIXED else (a, b)
+        field_err = {}
+        for name in ("U", "p", "phi", "theta", "tau"):
+            x, y = getattr(got, name), getattr(ref, name)
+            field_err[name] = float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+        second = {"precision": "fp64" if other == abi.RT_PREC_FP64 else "mixed",
+                  "value": total_cells / (ms2 * 1e-3), "ms_per_step": ms2 / args.steps,
+                  "iterations_last_step": iters(perf2)}
+        ctx2.close()
+        case.precision = prec
 
     # ---- roofline of the dominant operation (live CUDA events) ------------
     roof = None
@@ -279,19 +318,27 @@ def main():
         cpu = cpu_baseline(args.cpu_seconds)
 
     if rank == 0:
+        mixed = prec == abi.RT_PREC_MIXED
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD if not args.small else WORKLOAD.replace("1,000,000", f"{N:,}"),
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64 (FP32 Krylov iterations and sweeps, FP64 residual replacement, FP64 assembly)"
+                     if mixed else "f64",
+            "data": "synthetic",
+            "config": {"workload": (WORKLOAD if not args.small else WORKLOAD.replace("1,000,000", f"{N:,}"))
+                                   + (", mixed-precision form" if mixed else ", FP64 plain form"),
                        "cells": N, "faces": F, "parallelism": f"replicas x{world} (independent cases)",
                        "l2": "inputs larger than L2: the step touches ~2 GB of fields and matrices per step",
-                       "iterations_last_step": {"p": perf.p.nIterations,
-                                                "U": [perf.U[k].nIterations for k in range(3)],
-                                                "theta": [perf.theta[k].nIterations for k in range(6)]}},
+                       "iterations_last_step": iters(perf)},
             "clocks": clocks, "gpu_launches": launches, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
-            "profile_ms_2_steps": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         }
+        if second is not None:
+            key = "plain_fp64" if mixed else "mixed_precision"
+            line[key] = second
+            line["speedup_vs_" + key] = value / second["value"]
+            line["field_error_vs_fp64"] = field_err
+        line["profile_ms_2_steps"] = {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
         print(json.dumps(line), flush=True)
     ctx.close()
     if pg:

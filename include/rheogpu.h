@@ -177,10 +177,23 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *mesh);
 rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const int32_t *cellIJK);
 
 /* Options.  RT_OPT_SWEEP: 0 auto (systolic when structured), 1 level-scheduled
- * sweeps, 2 structured systolic sweeps.  RT_OPT_SWEEP_PLANES: planes per CTA
- * of the systolic sweeps, one CTA per plane (1 .. 16). */
+ * sweeps, 2 structured systolic sweeps.  RT_OPT_SWEEP_PLANES: planes per
+ * thread-block cluster of the systolic sweeps, one CTA per plane (1 .. 16).
+ * RT_OPT_PRECISION: RT_PREC_FP64 or RT_PREC_MIXED for rt_ldu_solve (the time
+ * step takes its precision from rt_case_ctl). */
 #define RT_OPT_SWEEP 1
 #define RT_OPT_SWEEP_PLANES 2
+#define RT_OPT_PRECISION 3
+/* RT_OPT_MIXED_PARTS: which parts of the mixed-precision form run in FP32
+ * (bit 1 the Krylov iterations, bit 2 the constitutive algebra; default 3),
+ * for accuracy studies of each part. */
+#define RT_OPT_MIXED_PARTS 4
+/* RT_OPT_MIXED_TIGHTEN: the mixed-precision solves stop when the FP64
+ * residual is below tolerance x 10^-value (default 2): a solve that only just
+ * meets the tolerance can differ from the FP64 iterate by far more than the
+ * FP64 solve differs from the exact solution, so the mixed form iterates a
+ * little further to keep its fields within 1e-6 of the FP64 form. */
+#define RT_OPT_MIXED_TIGHTEN 5
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);
@@ -239,6 +252,36 @@ rt_status rt_op_grad(rt_ctx *ctx, const double *psi, const double *psib,
  * (constitutiveEq::calcEig, constitutiveEq.C:360-428). */
 rt_status rt_op_eig(rt_ctx *ctx, int32_t n, const double *theta,
                     double *eigVals, double *eigVecs);
+
+/* ---- batches of independent cases -------------------------------------
+ * No reference counterpart (rheoFoam runs one case per process): the batched
+ * form steps many independent cases of uneven size as one device mesh, the
+ * disjoint union of the case meshes, uploaded with rt_mesh_upload.
+ *
+ * rt_batch_layout: case c owns cells [cellStart[c], cellStart[c+1]), internal
+ * faces [faceStart[c], faceStart[c+1]) and boundary faces
+ * [bFaceStart[c], bFaceStart[c+1]) (nCases + 1 entries each; no face may join
+ * two cases).  dims (3*nCases: nx, ny, nz) and cellIJK (3*nCells, positions
+ * inside each case's box) are optional; when every case is a lexicographic
+ * 2-D box (nz = 1, ny <= 1024) the DIC/DILU sweeps run one CTA per case.
+ * rt_batch_case_setup: as rt_case_setup, with one model per case and each
+ * case's pressure reference (pRefCell: a cell of that case, or -1 when the
+ * case has a fixed-value pressure patch).  rt_step then steps every case;
+ * rt_batch_step_perf returns each case's solver records of the last step.
+ * Every Krylov solve of a batch is per case: each case has its own scalars
+ * and its own stopping point, as if it were solved alone. */
+rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
+                          const int32_t *faceStart, const int32_t *bFaceStart,
+                          const int32_t *dims, const int32_t *cellIJK);
+rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
+                              const rt_model_params *models, const rt_case_ctl *ctl,
+                              const int32_t *pRefCell, const double *pRefValue);
+rt_status rt_batch_step_perf(rt_ctx *ctx, rt_step_perf *perf);
+
+/* Device memory held by all contexts of this library in the process (bytes):
+ * what an admission controller adds a new case's footprint to.  No reference
+ * counterpart. */
+rt_status rt_device_bytes(int64_t *bytes);
 
 /* Wait for all work of the context. */
 rt_status rt_sync(rt_ctx *ctx);

@@ -26,6 +26,9 @@ RT_PREC_FP64, RT_PREC_MIXED = 0, 1
 RT_FIELD_U, RT_FIELD_P, RT_FIELD_PHI, RT_FIELD_THETA, RT_FIELD_TAU, RT_FIELD_EIGVALS, RT_FIELD_EIGVECS = range(7)
 RT_OPT_SWEEP = 1
 RT_OPT_SWEEP_PLANES = 2
+RT_OPT_PRECISION = 3
+RT_OPT_MIXED_PARTS = 4
+RT_OPT_MIXED_TIGHTEN = 5
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {
@@ -165,6 +168,10 @@ def load_library(path: str = LIBNAME):
         "rt_profile_enable": ([vp, C.c_int32], C.c_int32),
         "rt_profile_report": ([vp, C.c_char_p, C.c_int32], C.c_int32),
         "rt_kernel_count": ([vp, P(C.c_int64)], C.c_int32),
+        "rt_batch_layout": ([vp, C.c_int32, _ip, _ip, _ip, _ip, _ip], C.c_int32),
+        "rt_batch_case_setup": ([vp, P(rt_bc_desc), P(rt_model_params), P(rt_case_ctl), _ip, _dp], C.c_int32),
+        "rt_batch_step_perf": ([vp, P(rt_step_perf)], C.c_int32),
+        "rt_device_bytes": ([P(C.c_int64)], C.c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -55,47 +55,53 @@ __device__ __forceinline__ T3 load9(const double *__restrict__ p, int n, int c) 
 
 // ---------------------------------------------------------------------------
 // cyclic Jacobi on a symmetric 3x3 (same sweep order, skip rule and sort as
-// the FP64 oracle)
+// the FP64 oracle).  FP32 instances (mixed precision) skip a rotation once
+// |a_pq| is below 1e-10 of the diagonal pair, far below what FP32 resolves.
 // ---------------------------------------------------------------------------
-template <int P, int Q>
-__device__ __forceinline__ void jrot(double A[3][3], double R[3][3]) {
+template <class Real> struct JacobiSkip;
+template <> struct JacobiSkip<double> { static constexpr double v = 1e-18; };
+template <> struct JacobiSkip<float> { static constexpr float v = 1e-10f; };
+
+template <int P, int Q, class Real>
+__device__ __forceinline__ void jrot(Real A[3][3], Real R[3][3]) {
     constexpr int K = 3 - P - Q;
-    double apq = A[P][Q];
-    if (fabs(apq) <= 1e-18 * (fabs(A[P][P]) + fabs(A[Q][Q]))) {
-        A[P][Q] = A[Q][P] = 0.0;
+    Real apq = A[P][Q];
+    if (fabs(apq) <= JacobiSkip<Real>::v * (fabs(A[P][P]) + fabs(A[Q][Q]))) {
+        A[P][Q] = A[Q][P] = Real(0);
         return;
     }
-    double th = (A[Q][Q] - A[P][P]) / (2.0 * apq);
-    double t = 1.0 / (fabs(th) + sqrt(th * th + 1.0));
-    if (th < 0.0) t = -t;
-    double c = 1.0 / sqrt(t * t + 1.0);
-    double s = t * c;
-    double app = A[P][P], aqq = A[Q][Q];
+    Real th = (A[Q][Q] - A[P][P]) / (Real(2) * apq);
+    Real t = Real(1) / (fabs(th) + sqrt(th * th + Real(1)));
+    if (th < Real(0)) t = -t;
+    Real c = Real(1) / sqrt(t * t + Real(1));
+    Real s = t * c;
+    Real app = A[P][P], aqq = A[Q][Q];
     A[P][P] = app - t * apq;
     A[Q][Q] = aqq + t * apq;
-    A[P][Q] = A[Q][P] = 0.0;
-    double akp = A[K][P], akq = A[K][Q];
+    A[P][Q] = A[Q][P] = Real(0);
+    Real akp = A[K][P], akq = A[K][Q];
     A[K][P] = A[P][K] = c * akp - s * akq;
     A[K][Q] = A[Q][K] = s * akp + c * akq;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        double rp = R[i][P], rq = R[i][Q];
+        Real rp = R[i][P], rq = R[i][Q];
         R[i][P] = c * rp - s * rq;
         R[i][Q] = s * rp + c * rq;
     }
 }
 
-__device__ __forceinline__ void eig3(const double s[6], double mu[3], double V[9]) {
-    double A[3][3] = {{s[0], s[1], s[2]}, {s[1], s[3], s[4]}, {s[2], s[4], s[5]}};
-    double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+template <class Real>
+__device__ __forceinline__ void eig3(const Real s[6], Real mu[3], Real V[9]) {
+    Real A[3][3] = {{s[0], s[1], s[2]}, {s[1], s[3], s[4]}, {s[2], s[4], s[5]}};
+    Real R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     for (int sweep = 0; sweep < 12; ++sweep) {
-        double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
-        if (off == 0.0) break;
+        Real off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+        if (off == Real(0)) break;
         jrot<0, 1>(A, R);
         jrot<0, 2>(A, R);
         jrot<1, 2>(A, R);
     }
-    double e[3] = {A[0][0], A[1][1], A[2][2]};
+    Real e[3] = {A[0][0], A[1][1], A[2][2]};
     int i0 = 0, i1 = 1, i2 = 2, t;
     // bubble sort of three, strict comparisons (stable)
     if (e[i0] > e[i1]) { t = i0; i0 = i1; i1 = t; }
@@ -134,12 +140,10 @@ void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double 
 // ---------------------------------------------------------------------------
 // theta source: rhs = symm(Omega theta - theta Omega + 2B + S_model)
 // ---------------------------------------------------------------------------
-__global__ void k_theta_rhs(int N, rt_model_params mp, const double *__restrict__ L,
-                            const double *__restrict__ Rv, const double *__restrict__ evv,
-                            const double *__restrict__ theta, double *__restrict__ rhs,
-                            double *__restrict__ fP) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= N) return;
+__device__ __forceinline__ void theta_rhs_cell(int c, int N, const rt_model_params &mp,
+                                               const double *__restrict__ L, const double *__restrict__ Rv,
+                                               const double *__restrict__ evv, const double *__restrict__ theta,
+                                               double *__restrict__ rhs, double *__restrict__ fP) {
     const double lambda = mp.lambda;
     const double zeta = (mp.model == RT_MODEL_PTT_LOG) ? mp.zeta : 0.0;
     T3 Lc = load9(L, N, c), R = load9(Rv, N, c);
@@ -211,6 +215,16 @@ __global__ void k_theta_rhs(int N, rt_model_params mp, const double *__restrict_
     rhs[(size_t)5 * N + c] = Ts.a[8];
 }
 
+__global__ void k_theta_rhs(int N, rt_model_params mp, const int *__restrict__ caseOf,
+                            const rt_model_params *__restrict__ cp, const double *__restrict__ L,
+                            const double *__restrict__ Rv, const double *__restrict__ evv,
+                            const double *__restrict__ theta, double *__restrict__ rhs,
+                            double *__restrict__ fP) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    theta_rhs_cell(c, N, caseOf ? cp[caseOf[c]] : mp, L, Rv, evv, theta, rhs, fP);
+}
+
 // theta matrix: diag = rDeltaT V + diagC; source = rDeltaT theta0 V + srcC + V rhs;
 // complete diagonal/source for the solve (boundary coefficients added)
 __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__restrict__ diagC,
@@ -240,11 +254,9 @@ __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__res
 }
 
 // tau = c (R Lambda R^T - I)   (FENE-P: c (f R Lambda R^T - a I))
-__global__ void k_tau(int N, rt_model_params mp, const double *__restrict__ Rv,
-                      const double *__restrict__ evv, const double *__restrict__ fP,
-                      double *__restrict__ tau) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= N) return;
+__device__ __forceinline__ void tau_cell(int c, int N, const rt_model_params &mp, const double *__restrict__ Rv,
+                                         const double *__restrict__ evv, const double *__restrict__ fP,
+                                         double *__restrict__ tau) {
     double zeta = (mp.model == RT_MODEL_PTT_LOG) ? mp.zeta : 0.0;
     double cP = mp.etaP / mp.lambda;
     if (mp.model == RT_MODEL_PTT_LOG) cP = mp.etaP / (mp.lambda * (1.0 - zeta));
@@ -267,6 +279,223 @@ __global__ void k_tau(int N, rt_model_params mp, const double *__restrict__ Rv,
     tau[(size_t)3 * N + c] = cP * T.a[4];
     tau[(size_t)4 * N + c] = cP * (0.5 * (T.a[5] + T.a[7]));
     tau[(size_t)5 * N + c] = cP * T.a[8];
+}
+
+__global__ void k_tau(int N, rt_model_params mp, const int *__restrict__ caseOf,
+                      const rt_model_params *__restrict__ cp, const double *__restrict__ Rv,
+                      const double *__restrict__ evv, const double *__restrict__ fP,
+                      double *__restrict__ tau) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    tau_cell(c, N, caseOf ? cp[caseOf[c]] : mp, Rv, evv, fP, tau);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision (RT_PREC_MIXED): the cell-local constitutive update with
+// its 3x3 matrix algebra in FP32.  Kept in FP64: the scalar functions of the
+// eigenvalues where FP32 would cancel (eigenvalue gaps, 1/e - 1, e - 1,
+// tr A - 3 and the FENE-P factors, all from the FP64 exp of the eigenvalues),
+// and whole cells whose log-conformation eigenvalues are near-degenerate
+// (gap below kMixGap of their magnitude: decomposeGradU divides by the gap)
+// or large (|mu| above kMixMuHi, high Wi: exp amplifies the FP32 error of mu);
+// those cells run the FP64 code above, bit for bit.  The algebra is
+// regrouped so that no FP32 difference of nearly equal numbers remains:
+// R (Lambda^-1 - I) R^T and R (Lambda - I) R^T are formed from the FP64
+// diagonal differences, which is the same tensor as the reference's
+// R Lambda^-1 R^T - I (R is orthogonal) without its cancellation.
+// ---------------------------------------------------------------------------
+constexpr double kMixGap = 0.1, kMixMuHi = 4.0;
+
+struct F3 {
+    float a[9];
+};
+__device__ __forceinline__ F3 fmul3(const F3 &A, const F3 &B) {
+    F3 C;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            C.a[3 * i + j] = A.a[3 * i] * B.a[j] + A.a[3 * i + 1] * B.a[3 + j] + A.a[3 * i + 2] * B.a[6 + j];
+    return C;
+}
+__device__ __forceinline__ F3 ftr3(const F3 &A) {
+    F3 B;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) B.a[3 * i + j] = A.a[3 * j + i];
+    return B;
+}
+__device__ __forceinline__ F3 fload9(const double *__restrict__ p, int n, int c) {
+    F3 A;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A.a[i] = (float)p[(size_t)i * n + c];
+    return A;
+}
+// R diag(d) R^T
+__device__ __forceinline__ F3 frdr(const F3 &R, float d0, float d1, float d2) {
+    F3 C;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            C.a[3 * i + j] = R.a[3 * i] * d0 * R.a[3 * j] + R.a[3 * i + 1] * d1 * R.a[3 * j + 1] +
+                             R.a[3 * i + 2] * d2 * R.a[3 * j + 2];
+    return C;
+}
+
+// log-conformation eigenvalues (ascending) that FP32 resolves well
+__device__ __forceinline__ bool mix_fp32_ok(double m0, double m1, double m2) {
+    const double scale = fmax(fabs(m0), fabs(m2));
+    const double gap = fmin(m1 - m0, m2 - m1);
+    return scale <= kMixMuHi && gap > kMixGap * scale && isfinite(scale);
+}
+
+__global__ void k_eig_mixed(int n, const double *__restrict__ theta, double *__restrict__ ev,
+                            double *__restrict__ vec) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    float sf[6], muf[3], Vf[9];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) sf[q] = (float)theta[(size_t)q * n + c];
+    eig3(sf, muf, Vf);
+    if (mix_fp32_ok(muf[0], muf[1], muf[2])) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ev[(size_t)k * n + c] = exp((double)muf[k]);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) vec[(size_t)i * n + c] = (double)Vf[i];
+        return;
+    }
+    double s[6], mu[3], V[9];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) s[q] = theta[(size_t)q * n + c];
+    eig3(s, mu, V);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ev[(size_t)k * n + c] = exp(mu[k]);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) vec[(size_t)i * n + c] = V[i];
+}
+
+__global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restrict__ caseOf,
+                                  const rt_model_params *__restrict__ cp, const double *__restrict__ L,
+                                  const double *__restrict__ Rv, const double *__restrict__ evv,
+                                  const double *__restrict__ theta, double *__restrict__ rhs,
+                                  double *__restrict__ fP) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
+    const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
+    if (!mix_fp32_ok(log(e0), log(e1), log(e2))) {
+        theta_rhs_cell(c, N, mp, L, Rv, evv, theta, rhs, fP);
+        return;
+    }
+    const float lambdaInv = (float)(1.0 / mp.lambda);
+    const float zeta = (mp.model == RT_MODEL_PTT_LOG) ? (float)mp.zeta : 0.0f;
+    F3 Lc = fload9(L, N, c), R = fload9(Rv, N, c);
+    F3 Lt = ftr3(Lc);
+    if (mp.model == RT_MODEL_PTT_LOG) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                Lt.a[3 * i + j] = Lt.a[3 * i + j] - zeta * (0.5f * (Lc.a[3 * i + j] + Lc.a[3 * j + i]));
+    }
+    const F3 Rt = ftr3(R);
+    const F3 M = fmul3(fmul3(Rt, Lt), R);
+    const float f0 = (float)e0, f1 = (float)e1, f2 = (float)e2;
+    // omega in the eigenbasis; the gaps in FP64
+    const float g01 = (float)(e1 - e0 + 1e-16), g02 = (float)(e2 - e0 + 1e-16), g12 = (float)(e2 - e1 + 1e-16);
+    F3 om;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) om.a[i] = 0.0f;
+    om.a[1] = (f1 * M.a[1] + f0 * M.a[3]) / g01;
+    om.a[2] = (f2 * M.a[2] + f0 * M.a[6]) / g02;
+    om.a[5] = (f2 * M.a[5] + f1 * M.a[7]) / g12;
+    om.a[3] = -om.a[1]; om.a[6] = -om.a[2]; om.a[7] = -om.a[5];
+    const F3 Om = fmul3(fmul3(R, om), Rt);
+    const F3 B = frdr(R, M.a[0], M.a[4], M.a[8]);
+    // Lambda^-1 - I in FP64
+    const float d0 = (float)(1.0 / e0 - 1.0), d1 = (float)(1.0 / e1 - 1.0), d2 = (float)(1.0 / e2 - 1.0);
+    F3 S;
+    if (mp.model == RT_MODEL_OLDROYDB_LOG) {
+        S = frdr(R, d0, d1, d2);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = lambdaInv * S.a[i];
+    } else if (mp.model == RT_MODEL_GIESEKUS_LOG) {
+        const F3 A = frdr(R, f0, f1, f2);
+        const F3 T = frdr(R, d0, d1, d2);
+        const F3 ATT = fmul3(A, fmul3(T, T));
+        const float alpha = (float)mp.alpha;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = lambdaInv * (T.a[i] - alpha * ATT.a[i]);
+    } else if (mp.model == RT_MODEL_PTT_LOG) {
+        const double trAm3 = (e0 - 1.0) + (e1 - 1.0) + (e2 - 1.0);
+        const double x = (mp.epsilon / (1.0 - mp.zeta)) * trAm3;
+        const float fac = (float)((mp.pttFunction == RT_PTT_EXP) ? exp(x) : 1.0 + x);
+        const F3 T = frdr(R, d0, d1, d2);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = (lambdaInv * T.a[i]) * fac;
+    } else {
+        const double trA = e0 + e1 + e2;
+        const double f = mp.L2 / (mp.L2 - trA);
+        const double a = mp.L2 / (mp.L2 - 3.0);
+        fP[c] = f;
+        // a / e - f in FP64
+        S = frdr(R, (float)(a / e0 - f), (float)(a / e1 - f), (float)(a / e2 - f));
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = lambdaInv * S.a[i];
+    }
+    float th[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) th[q] = (float)theta[(size_t)q * N + c];
+    F3 Th;
+    Th.a[0] = th[0]; Th.a[1] = th[1]; Th.a[2] = th[2];
+    Th.a[3] = th[1]; Th.a[4] = th[3]; Th.a[5] = th[4];
+    Th.a[6] = th[2]; Th.a[7] = th[4]; Th.a[8] = th[5];
+    const F3 OT = fmul3(Om, Th), TO = fmul3(Th, Om);
+    F3 Ts;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Ts.a[i] = OT.a[i] - TO.a[i] + 2.0f * B.a[i] + S.a[i];
+    rhs[c] = Ts.a[0];
+    rhs[(size_t)N + c] = 0.5f * (Ts.a[1] + Ts.a[3]);
+    rhs[(size_t)2 * N + c] = 0.5f * (Ts.a[2] + Ts.a[6]);
+    rhs[(size_t)3 * N + c] = Ts.a[4];
+    rhs[(size_t)4 * N + c] = 0.5f * (Ts.a[5] + Ts.a[7]);
+    rhs[(size_t)5 * N + c] = Ts.a[8];
+}
+
+__global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ caseOf,
+                            const rt_model_params *__restrict__ cp, const double *__restrict__ Rv,
+                            const double *__restrict__ evv, const double *__restrict__ fP,
+                            double *__restrict__ tau) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
+    const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
+    if (!mix_fp32_ok(log(e0), log(e1), log(e2))) {
+        tau_cell(c, N, mp, Rv, evv, fP, tau);
+        return;
+    }
+    double cP = mp.etaP / mp.lambda;
+    if (mp.model == RT_MODEL_PTT_LOG) cP = mp.etaP / (mp.lambda * (1.0 - mp.zeta));
+    const F3 R = fload9(Rv, N, c);
+    F3 T;
+    if (mp.model == RT_MODEL_FENEP_LOG) {
+        // f (R Lambda R^T) - a I = f R (Lambda - I) R^T + (f - a) I
+        const double a = mp.L2 / (mp.L2 - 3.0);
+        const double f = fP[c];
+        T = frdr(R, (float)(f * (e0 - 1.0)), (float)(f * (e1 - 1.0)), (float)(f * (e2 - 1.0)));
+        const float fa = (float)(f - a);
+        T.a[0] += fa; T.a[4] += fa; T.a[8] += fa;
+    } else {
+        T = frdr(R, (float)(e0 - 1.0), (float)(e1 - 1.0), (float)(e2 - 1.0));
+    }
+    tau[c] = cP * (double)T.a[0];
+    tau[(size_t)N + c] = cP * (double)(0.5f * (T.a[1] + T.a[3]));
+    tau[(size_t)2 * N + c] = cP * (double)(0.5f * (T.a[2] + T.a[6]));
+    tau[(size_t)3 * N + c] = cP * (double)T.a[4];
+    tau[(size_t)4 * N + c] = cP * (double)(0.5f * (T.a[5] + T.a[7]));
+    tau[(size_t)5 * N + c] = cP * (double)T.a[8];
 }
 
 // linearExtrapolation: val = tau_P + grad(tau)_P . (Cf - C_P) for the faces
@@ -336,7 +565,7 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
     const int N = mesh.N, F = mesh.F, NB = mesh.NB;
     cudaStream_t s = ctx->stream;
     Work &W = ctx->work;
-    size_t mark = W.used;
+    WorkMark wmark(W);
     double *G = const_cast<double *>(gradU);
     if (!G) {
         G = W.take(9 * (size_t)N);
@@ -348,10 +577,16 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
     double *bouC = W.take(6 * (size_t)NB), *flux = W.take(6 * (size_t)F);
     double *dS = W.take(N), *bS = W.take(6 * (size_t)N);
     double *val = W.take(6 * (size_t)NB + 6);
+    const MeshView mv = view(mesh);
 
     {
         ProfScope ps(ctx, "theta_rhs", (double)N * (72.0 + 72.0 + 24.0 + 48.0 + 48.0));
-        k_theta_rhs<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, G, cs.eigVecs.p, cs.eigVals.p, cs.theta.p, rhs, fP);
+        if (cs.ctl.precision == RT_PREC_MIXED && (ctx->mixedParts & 2))
+            k_theta_rhs_mixed<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, G, cs.eigVecs.p,
+                                                              cs.eigVals.p, cs.theta.p, rhs, fP);
+        else
+            k_theta_rhs<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, G, cs.eigVecs.p,
+                                                        cs.eigVals.p, cs.theta.p, rhs, fP);
         RT_CHECK_LAUNCH();
     }
     RT_CUDA(cudaMemcpyAsync(theta0, cs.theta.p, sizeof(double) * 6 * N, cudaMemcpyDeviceToDevice, s));
@@ -370,7 +605,8 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
                                                       dS, bS);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
-    SolveArgs a{dS, upper, lower, bS, cs.theta.p, 6, theta_valid_mask(mesh), cs.ctl.solverTheta};
+    SolveArgs a{dS, upper, lower, bS, cs.theta.p, 6, theta_valid_mask(mesh), cs.ctl.solverTheta, cs.ctl.precision,
+                2};
     rt_status st;
     {
         ProfScope ps(ctx, "solve_theta");
@@ -379,16 +615,26 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
     correct_bc(ctx, cs.bkTh.p, 6, cs.theta.p, cs.thetab.p);
     {
         ProfScope ps(ctx, "eig", (double)N * (48.0 + 72.0 + 24.0));
-        eig_cells(ctx, N, cs.theta.p, cs.eigVals.p, cs.eigVecs.p);
+        if (cs.ctl.precision == RT_PREC_MIXED && (ctx->mixedParts & 2)) {
+            k_eig_mixed<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.theta.p, cs.eigVals.p, cs.eigVecs.p);
+            RT_CHECK_LAUNCH();
+            launch_count(ctx);
+        } else {
+            eig_cells(ctx, N, cs.theta.p, cs.eigVals.p, cs.eigVecs.p);
+        }
     }
     {
         ProfScope ps(ctx, "tau", (double)N * (72.0 + 24.0 + 48.0));
-        k_tau<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, cs.eigVecs.p, cs.eigVals.p, fP, cs.tau.p);
+        if (cs.ctl.precision == RT_PREC_MIXED && (ctx->mixedParts & 2))
+            k_tau_mixed<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, cs.eigVecs.p,
+                                                        cs.eigVals.p, fP, cs.tau.p);
+        else
+            k_tau<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, cs.eigVecs.p, cs.eigVals.p,
+                                                  fP, cs.tau.p);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
         tau_correct_bc(ctx, val);
     }
-    W.used = mark;
     return st;
 }
 

@@ -1,5 +1,6 @@
 // ctx.cu — C-ABI entry points: context, mesh upload, case setup, field I/O.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 
@@ -129,6 +130,7 @@ rt_status rt_ctx_destroy(rt_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->red.hostResult) cudaFreeHost(ctx->red.hostResult);
+    if (ctx->mesh.batch.hostCount) cudaFreeHost(ctx->mesh.batch.hostCount);
     for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
     if (ctx->tStart) cudaEventDestroy(ctx->tStart);
     if (ctx->tStop) cudaEventDestroy(ctx->tStop);
@@ -250,6 +252,9 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
         // ---- scratch ---------------------------------------------------------
         size_t need = (size_t)N * 160 + (size_t)F * 24 + (size_t)NB * 96 + 4096;
         ctx->work.a.alloc(need);
+        ctx->work.used = 0;
+        m.batch.n = 1;
+        m.batch.sweep2d = false;
         RT_CUDA(cudaStreamSynchronize(s));
         ctx->meshReady = true;
         ctx->cs.ready = false;
@@ -312,6 +317,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         RT_REQUIRE(s.nJB <= 8, RT_EINVAL, "structured sweeps need ny <= 256");
         s.KC = std::max(1, std::min(nz, 8));   // planes (CTAs) per thread-block cluster
         s.sync.alloc(SYNC_PROGRESS + (size_t)nz * s.nJB);
+        s.sync.zero(ctx->stream);
         s.data.alloc((size_t)(12 + 6 + 6) * s.nSkew);
         s.data.zero(ctx->stream);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -334,6 +340,19 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
             s.KC = (int)std::min<int64_t>(value, s.nz);
             return RT_OK;
         }
+        case RT_OPT_MIXED_TIGHTEN:
+            RT_REQUIRE(value >= 0 && value <= 12, RT_EINVAL, "RT_OPT_MIXED_TIGHTEN: decades 0 .. 12");
+            ctx->mixedTighten = std::pow(10.0, -(double)value);
+            return RT_OK;
+        case RT_OPT_MIXED_PARTS:
+            RT_REQUIRE(value >= 0 && value <= 3, RT_EINVAL, "RT_OPT_MIXED_PARTS: bit 1 Krylov, bit 2 constitutive");
+            ctx->mixedParts = (int)value;
+            return RT_OK;
+        case RT_OPT_PRECISION:
+            RT_REQUIRE(value == RT_PREC_FP64 || value == RT_PREC_MIXED, RT_EINVAL,
+                       "RT_OPT_PRECISION: RT_PREC_FP64 or RT_PREC_MIXED");
+            ctx->precision = (int)value;
+            return RT_OK;
         default:
             return RT_EINVAL;
         }
@@ -463,7 +482,7 @@ rt_status rt_ldu_solve(rt_ctx *ctx, const double *diag, const double *upper, con
         l.upload(lower, F, s);
         b.upload(source, (size_t)ncmpt * N, s);
         x.upload(psi, (size_t)ncmpt * N, s);
-        SolveArgs a{d.p, u.p, l.p, b.p, x.p, ncmpt, (1u << ncmpt) - 1u, *ctl};
+        SolveArgs a{d.p, u.p, l.p, b.p, x.p, ncmpt, (1u << ncmpt) - 1u, *ctl, ctx->precision};
         rt_status st = ldu_solve_device(ctx, a, perf);
         RT_CUDA(cudaMemcpyAsync(psi, x.p, sizeof(double) * ncmpt * N, cudaMemcpyDeviceToHost, s));
         RT_CUDA(cudaStreamSynchronize(s));
@@ -548,3 +567,206 @@ rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batches of independent cases
+// ---------------------------------------------------------------------------
+rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart, const int32_t *faceStart,
+                          const int32_t *bFaceStart, const int32_t *dims, const int32_t *cellIJK) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
+        RT_REQUIRE(nCases >= 1 && cellStart && faceStart && bFaceStart, RT_EINVAL, "null argument");
+        DevMesh &m = ctx->mesh;
+        Batch &b = m.batch;
+        const int N = m.N, F = m.F, NB = m.NB, n = nCases;
+        RT_REQUIRE(cellStart[0] == 0 && cellStart[n] == N && faceStart[0] == 0 && faceStart[n] == F &&
+                       bFaceStart[0] == 0 && bFaceStart[n] == NB,
+                   RT_EINVAL, "case ranges must cover the cells, faces and boundary faces");
+        for (int c = 0; c < n; ++c)
+            RT_REQUIRE(cellStart[c + 1] > cellStart[c] && faceStart[c + 1] >= faceStart[c] &&
+                           bFaceStart[c + 1] >= bFaceStart[c],
+                       RT_EINVAL, "case ranges must increase (every case owns a cell)");
+        // every face lies inside its case
+        std::vector<int> own(F), nei(F), bc(NB);
+        if (F) {
+            RT_CUDA(cudaMemcpy(own.data(), m.owner.p, sizeof(int) * F, cudaMemcpyDeviceToHost));
+            RT_CUDA(cudaMemcpy(nei.data(), m.neighbour.p, sizeof(int) * F, cudaMemcpyDeviceToHost));
+        }
+        if (NB) RT_CUDA(cudaMemcpy(bc.data(), m.bCell.p, sizeof(int) * NB, cudaMemcpyDeviceToHost));
+        std::vector<int> caseOf(N);
+        for (int c = 0; c < n; ++c)
+            for (int i = cellStart[c]; i < cellStart[c + 1]; ++i) caseOf[i] = c;
+        for (int c = 0; c < n; ++c) {
+            for (int f = faceStart[c]; f < faceStart[c + 1]; ++f)
+                RT_REQUIRE(caseOf[own[f]] == c && caseOf[nei[f]] == c, RT_EINVAL,
+                           "face " + std::to_string(f) + " leaves its case");
+            for (int f = bFaceStart[c]; f < bFaceStart[c + 1]; ++f)
+                RT_REQUIRE(caseOf[bc[f]] == c, RT_EINVAL, "boundary face " + std::to_string(f) + " leaves its case");
+        }
+        b.n = 1;   // until the layout is complete
+        b.cellStartH.assign(cellStart, cellStart + n + 1);
+        b.faceStartH.assign(faceStart, faceStart + n + 1);
+        b.bStartH.assign(bFaceStart, bFaceStart + n + 1);
+        upload_vec(ctx, caseOf, b.caseOf);
+        upload_vec(ctx, b.cellStartH, b.cellStartD);
+        upload_vec(ctx, b.faceStartH, b.faceStartD);
+        upload_vec(ctx, b.bStartH, b.bStartD);
+        // reduction blocks of RT_BLOCK cells that never straddle two cases
+        std::vector<int> bcase, bc0, bc1, cblk(n + 1, 0);
+        for (int c = 0; c < n; ++c) {
+            cblk[c] = (int)bcase.size();
+            for (int i = cellStart[c]; i < cellStart[c + 1]; i += RT_BLOCK) {
+                bcase.push_back(c);
+                bc0.push_back(i);
+                bc1.push_back(std::min(i + RT_BLOCK, cellStart[c + 1]));
+            }
+        }
+        cblk[n] = (int)bcase.size();
+        b.nBlk = (int)bcase.size();
+        b.caseBlkH = cblk;
+        upload_vec(ctx, bcase, b.blkCase);
+        upload_vec(ctx, bc0, b.blkCell0);
+        upload_vec(ctx, bc1, b.blkCell1);
+        upload_vec(ctx, cblk, b.caseBlk);
+        // structured 2-D cases: the skewed layout of the batched sweeps
+        b.sweep2d = false;
+        bool structured = dims && cellIJK;
+        for (int c = 0; structured && c < n; ++c)
+            structured = dims[3 * c] > 0 && dims[3 * c + 1] > 0 && dims[3 * c + 1] <= 1024 && dims[3 * c + 2] == 1;
+        if (structured) {
+            std::vector<int> lo((size_t)2 * N, -1), hi((size_t)2 * N, -1);
+            std::vector<int> sT(n), sJB(n);
+            std::vector<long long> sOff(n);
+            long long nSkew = 0;
+            int maxJB = 0;
+            for (int c = 0; c < n; ++c) {
+                const int nx = dims[3 * c], ny = dims[3 * c + 1];
+                sJB[c] = (ny + 31) / 32;
+                sT[c] = ((nx + 31 + 7) / 8) * 8;
+                sOff[c] = nSkew;
+                nSkew += (long long)sJB[c] * sT[c] * 32;
+                maxJB = std::max(maxJB, sJB[c]);
+            }
+            std::vector<int> cellOf((size_t)nSkew, -1);
+            for (int c = 0; structured && c < n; ++c) {
+                const int nx = dims[3 * c], ny = dims[3 * c + 1];
+                std::vector<int> at((size_t)nx * ny, -1);
+                long long prev = -1;
+                for (int i = cellStart[c]; i < cellStart[c + 1]; ++i) {
+                    const int ci = cellIJK[3 * i], cj = cellIJK[3 * i + 1], ck = cellIJK[3 * i + 2];
+                    if (ci < 0 || ci >= nx || cj < 0 || cj >= ny || ck != 0) { structured = false; break; }
+                    const long long key = (long long)cj * nx + ci;
+                    if (key <= prev) { structured = false; break; }
+                    prev = key;
+                    at[(size_t)key] = i;
+                }
+                for (int f = faceStart[c]; structured && f < faceStart[c + 1]; ++f) {
+                    const int o = own[f], ne = nei[f];
+                    const int di = cellIJK[3 * ne] - cellIJK[3 * o], dj = cellIJK[3 * ne + 1] - cellIJK[3 * o + 1];
+                    const int dir = (di == 0 && dj == 1) ? 0 : (di == 1 && dj == 0) ? 1 : -1;   // 0 y, 1 x
+                    if (dir < 0 || hi[(size_t)dir * N + o] >= 0 || lo[(size_t)dir * N + ne] >= 0) {
+                        structured = false;
+                        break;
+                    }
+                    hi[(size_t)dir * N + o] = f;
+                    lo[(size_t)dir * N + ne] = f;
+                }
+                for (int jb = 0; structured && jb < sJB[c]; ++jb)
+                    for (int t = 0; t < sT[c]; ++t)
+                        for (int l = 0; l < 32; ++l) {
+                            const int i = t - l, j = jb * 32 + l;
+                            if (i < 0 || i >= nx || j >= ny) continue;
+                            cellOf[(size_t)(sOff[c] + ((long long)jb * sT[c] + t) * 32 + l)] = at[(size_t)j * nx + i];
+                        }
+            }
+            if (structured) {
+                b.nSkew = nSkew;
+                b.maxJB = maxJB;
+                upload_vec(ctx, sT, b.sT);
+                upload_vec(ctx, sJB, b.sJB);
+                upload_vec(ctx, sOff, b.sOff);
+                upload_vec(ctx, cellOf, b.sCell);
+                upload_vec(ctx, lo, b.sFaceLo);
+                upload_vec(ctx, hi, b.sFaceHi);
+                b.sData64.alloc((size_t)21 * nSkew);
+                b.sData64.zero(ctx->stream);
+                b.sData32.alloc((size_t)17 * nSkew);
+                b.sData32.zero(ctx->stream);
+                b.sweep2d = true;
+            }
+        }
+        b.sErr.alloc(1);
+        b.sErr.zero(ctx->stream);
+        const size_t nSeg = (size_t)8 * n;
+        b.segD.alloc(12 * nSeg);
+        b.segD.zero(ctx->stream);
+        b.segI.alloc(6 * nSeg + 8);
+        b.segI.zero(ctx->stream);
+        b.bPartial.alloc((size_t)2 * 6 * b.nBlk);
+        b.bRes.alloc(4 * nSeg);
+        if (!b.hostCount) RT_CUDA(cudaMallocHost(&b.hostCount, sizeof(int)));
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        b.n = n;
+        ctx->batchPerf.assign(n, rt_step_perf{});
+        ctx->cs.ready = false;
+        return RT_OK;
+    });
+}
+
+rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model_params *models,
+                              const rt_case_ctl *ctl, const int32_t *pRefCell, const double *pRefValue) {
+    rt_status st = RT_OK;
+    {
+        rt_status v = guarded(ctx, [&]() -> rt_status {
+            RT_REQUIRE(ctx->meshReady && ctx->mesh.batch.n >= 1, RT_ENOTREADY, "mesh not uploaded");
+            RT_REQUIRE(bcs && models && ctl && pRefCell && pRefValue, RT_EINVAL, "null argument");
+            const Batch &b = ctx->mesh.batch;
+            for (int c = 0; c < b.n; ++c) {
+                const rt_model_params &mp = models[c];
+                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_FENEP_LOG, RT_EINVAL,
+                           "case " + std::to_string(c) + ": unknown constitutive model");
+                RT_REQUIRE(mp.lambda > 0 && mp.rho > 0, RT_EINVAL,
+                           "case " + std::to_string(c) + ": lambda and rho must be positive");
+                RT_REQUIRE(mp.model != RT_MODEL_FENEP_LOG || mp.L2 > 3.0, RT_EINVAL,
+                           "case " + std::to_string(c) + ": FENE-P needs L2 > 3");
+                RT_REQUIRE(pRefCell[c] < 0 || (pRefCell[c] >= b.cellStartH[c] && pRefCell[c] < b.cellStartH[c + 1]),
+                           RT_EINVAL, "case " + std::to_string(c) + ": pRefCell outside the case");
+            }
+            return RT_OK;
+        });
+        if (v != RT_OK) return v;
+    }
+    rt_case_ctl c1 = *ctl;
+    c1.needReference = 0;
+    c1.pRefCell = 0;
+    st = rt_case_setup(ctx, bcs, &models[0], &c1);
+    if (st != RT_OK) return st;
+    return guarded(ctx, [&]() -> rt_status {
+        Batch &b = ctx->mesh.batch;
+        std::vector<rt_model_params> mp(models, models + b.n);
+        std::vector<int> rc(pRefCell, pRefCell + b.n);
+        std::vector<double> rv(pRefValue, pRefValue + b.n);
+        upload_vec(ctx, mp, b.params);
+        upload_vec(ctx, rc, b.refCell);
+        upload_vec(ctx, rv, b.refValue);
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->batchPerf.assign(b.n, rt_step_perf{});
+        return RT_OK;
+    });
+}
+
+rt_status rt_batch_step_perf(rt_ctx *ctx, rt_step_perf *perf) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(perf, RT_EINVAL, "null argument");
+        RT_REQUIRE(ctx->mesh.batch.n > 1 && (int)ctx->batchPerf.size() == ctx->mesh.batch.n, RT_ENOTREADY,
+                   "no batch layout");
+        for (int c = 0; c < ctx->mesh.batch.n; ++c) perf[c] = ctx->batchPerf[c];
+        return RT_OK;
+    });
+}
+
+rt_status rt_device_bytes(int64_t *bytes) {
+    if (!bytes) return RT_EINVAL;
+    *bytes = (int64_t)device_bytes().load();
+    return RT_OK;
+}

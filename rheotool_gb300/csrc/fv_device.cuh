@@ -31,12 +31,45 @@ struct MeshView {
     const double *__restrict__ bmagSf;
     const double *__restrict__ bDelta;
     const double *__restrict__ bCtoF;   // 3NB SoA
+    // batch of cases (null for one case): case of each cell, model of each case
+    const int *__restrict__ caseOf;
+    const rt_model_params *__restrict__ caseParams;
+    const int *__restrict__ refCell;
+    const double *__restrict__ refValue;
 };
 
 inline MeshView view(const DevMesh &m) {
+    const bool b = m.batch.n > 1;
     return MeshView{m.N, m.F, m.NB, m.nSlots, m.owner.p, m.neighbour.p, m.ellFace.p, m.ellNbr.p,
                     m.bStart.p, m.bList.p, m.bCell.p, m.Sf.p, m.magSf.p, m.w.p, m.deltaCoeffs.p,
-                    m.C.p, m.V.p, m.bSf.p, m.bmagSf.p, m.bDelta.p, m.bCtoF.p};
+                    m.C.p, m.V.p, m.bSf.p, m.bmagSf.p, m.bDelta.p, m.bCtoF.p,
+                    b ? m.batch.caseOf.p : nullptr, b ? m.batch.params.p : nullptr,
+                    b ? m.batch.refCell.p : nullptr, b ? m.batch.refValue.p : nullptr};
+}
+
+// the model of cell c: the case's in a batch, else the context's
+__device__ __forceinline__ const rt_model_params &model_of(const MeshView &m, const rt_model_params &mp, int c) {
+    return m.caseOf ? m.caseParams[m.caseOf[c]] : mp;
+}
+
+// momentum-equation coefficients of a model (divTau, constitutiveEq.C:72-132):
+// the implicit laplacian coefficient gam and the explicit one kG
+struct MomCoef {
+    int stab;
+    double rho, gam, kG;
+};
+__host__ __device__ inline MomCoef mom_coef(const rt_model_params &mp) {
+    MomCoef c;
+    c.stab = mp.stabilization;
+    c.rho = mp.rho;
+    if (mp.stabilization == RT_STAB_COUPLING || mp.stabilization == RT_STAB_BSD) {
+        c.gam = (mp.etaP + mp.etaS) / mp.rho;
+        c.kG = mp.etaP / mp.rho;
+    } else {
+        c.gam = mp.etaS / mp.rho;
+        c.kG = 0.0;
+    }
+    return c;
 }
 
 __device__ __forceinline__ double lin_interp(double w, double vP, double vN) {

@@ -21,6 +21,8 @@
 #include <cmath>
 #include <cstring>
 
+#include "batch.h"
+#include "real_ops.cuh"
 #include "rt_internal.h"
 #include "sweep.h"
 
@@ -29,7 +31,7 @@ namespace rt {
 // scalar slots (device array ctx->scal, [slot*8 + comp])
 enum {
     S_NF = 0, S_INIT, S_FIN, S_XBAR, S_A, S_B, S_AOLD, S_ALPHA, S_OMEGA,
-    S_R0R, S_R0ROLD, S_SING, S_T1, S_T2, S_NSLOT
+    S_R0R, S_R0ROLD, S_SING, S_T1, S_T2, S_RST, S_NSLOT
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -201,48 +203,52 @@ __global__ void k_recip_diag(int N, const double *diag, double *rD) {
     if (c < N) rD[c] = 1.0 / diag[c];
 }
 
+// (templated on the real type: FP64 for the plain solvers, FP32 inside the
+// mixed-precision ones)
+template <class Real>
 __global__ void k_fwd_level(Ell e, int l0, int l1, const int *__restrict__ cells, unsigned mask,
-                            const double *__restrict__ rD, const double *__restrict__ lower,
-                            const double *__restrict__ r, double *__restrict__ w) {
+                            const Real *__restrict__ rD, const Real *__restrict__ lower,
+                            const Real *__restrict__ r, Real *__restrict__ w) {
     int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= l1) return;
     int c = cells[t];
     const int N = e.N;
-    const double rd = rD[c];
+    const Real rd = rD[c];
     for (int k = 0; k < 6; ++k) {
         if (!((mask >> k) & 1u)) continue;
         size_t o = (size_t)k * N;
-        double acc = __dmul_rn(rd, r[o + c]);
+        Real acc = r_mul(rd, r[o + c]);
         for (int s = 0; s < e.nSlots; ++s) {
             int nb = e.nbr[s * N + c];
             if (nb < 0 || nb > c) break;
             int f = e.face[s * N + c];
-            acc = __fma_rn(-__dmul_rn(rd, lower[f]), w[o + nb], acc);
+            acc = r_fma(-r_mul(rd, lower[f]), w[o + nb], acc);
         }
         w[o + c] = acc;
     }
 }
 
+template <class Real>
 __global__ void k_bwd_level(Ell e, int l0, int l1, const int *__restrict__ cells, unsigned mask,
-                            const double *__restrict__ rD, const double *__restrict__ upper,
-                            double *__restrict__ w) {
+                            const Real *__restrict__ rD, const Real *__restrict__ upper,
+                            Real *__restrict__ w) {
     int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= l1) return;
     int c = cells[t];
     const int N = e.N;
-    const double rd = rD[c];
+    const Real rd = rD[c];
     // number of used slots
     int ns = 0;
     while (ns < e.nSlots && e.nbr[ns * N + c] >= 0) ++ns;
     for (int k = 0; k < 6; ++k) {
         if (!((mask >> k) & 1u)) continue;
         size_t o = (size_t)k * N;
-        double acc = w[o + c];
+        Real acc = w[o + c];
         for (int s = ns - 1; s >= 0; --s) {
             int nb = e.nbr[s * N + c];
             if (nb < c) break;                // upper neighbours are the last slots
             int f = e.face[s * N + c];
-            acc = __fma_rn(-__dmul_rn(rd, upper[f]), w[o + nb], acc);
+            acc = r_fma(-r_mul(rd, upper[f]), w[o + nb], acc);
         }
         w[o + c] = acc;
     }
@@ -744,6 +750,587 @@ rt_status run_pbicgstab(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
     return RT_OK;
 }
 
+
+// ==========================================================================
+// Mixed precision (RT_PREC_MIXED): the Krylov vectors, the matrix copy used
+// inside the iterations and the preconditioner application are FP32; the
+// scalars, the dot-product accumulations, the solution and the normalised
+// residual stay FP64.  The solution is kept as psi (FP64) + x32 (an FP32
+// correction accumulated since the last residual replacement).  Whenever the
+// recursively updated FP32 residual has dropped by kReplace since the last
+// replacement, claims convergence, or the iteration budget ends, x32 is
+// folded into psi and the residual is recomputed from the FP64 matrix as
+// b - A psi (reliable updates, Sleijpen & van der Vorst 1996; van der Vorst &
+// Ye 2000).  Convergence is only ever declared on that FP64 residual, with
+// the normFactor of the FP64 prologue, so the stopping test is the one of
+// the plain solvers.
+// ==========================================================================
+constexpr double kReplace = 0.1;
+
+// FP32 copy of the matrix in the differences form: the off-diagonal
+// coefficients rounded, and instead of the diagonal the FP64 row sum rounded
+// once.  A x = rowsum_c x_c + sum_f a_f (x_nb - x_c) is the same product, but
+// the rounding no longer breaks the (near-)zero row sums of an assembled
+// OpenFOAM matrix (negSumDiag), which would move the near-null space of a
+// pressure matrix by far more than its smallest eigenvalue.
+__global__ void k_mx_mat32(Ell e, int F, const double *__restrict__ diag, const double *__restrict__ upper,
+                           const double *__restrict__ lower, float *__restrict__ d32, float *__restrict__ u32,
+                           float *__restrict__ l32) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < e.N) d32[i] = (float)row_sum(e, i, diag, upper, lower);
+    if (i < F) {
+        u32[i] = (float)upper[i];
+        l32[i] = (float)lower[i];
+    }
+}
+
+__global__ void k_mx_to32(int n, const double *__restrict__ a, float *__restrict__ b) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// r32 = rA (FP64 prologue residual), x32 = 0, no restart pending
+__global__ void k_mx_start(int N, unsigned mask, const double *__restrict__ rA, float *__restrict__ r32,
+                           float *__restrict__ x32, double *S) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < 6 && ((mask >> c) & 1u)) S[S_RST * 8 + c] = 0.0;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        r32[(size_t)k * N + c] = (float)rA[(size_t)k * N + c];
+        x32[(size_t)k * N + c] = 0.0f;
+    }
+}
+
+// y_c = rowsum_c x_c + sum_f a_f (x_nb - x_c)   (differences form, see k_mx_mat32)
+__device__ __forceinline__ float row_mul32(const Ell &e, int c, const float *__restrict__ rowsum,
+                                           const float *__restrict__ upper, const float *__restrict__ lower,
+                                           const float *__restrict__ x) {
+    const float xc = x[c];
+    float acc = rowsum[c] * xc;
+    for (int s = 0; s < e.nSlots; ++s) {
+        int nb = e.nbr[s * e.N + c];
+        if (nb < 0) break;
+        int f = e.face[s * e.N + c];
+        acc = fmaf(nb > c ? upper[f] : lower[f], x[nb] - xc, acc);
+    }
+    return acc;
+}
+
+__global__ void k_mx_amul(Ell e, unsigned mask, const float *__restrict__ diag, const float *__restrict__ upper,
+                          const float *__restrict__ lower, const float *__restrict__ x, float *__restrict__ y) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= e.N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        y[(size_t)k * e.N + c] = row_mul32(e, c, diag, upper, lower, x + (size_t)k * e.N);
+    }
+}
+
+// dot products of FP32 vectors accumulated in FP64: slot0 = a.b, slot1 = c.d
+__global__ void k_mx_dot(int N, unsigned mask, const float *__restrict__ a, const float *__restrict__ b,
+                         const float *__restrict__ c2, const float *__restrict__ d2, double *partial, int nB) {
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        double v0 = 0.0, v1 = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            v0 += (double)a[o + c] * (double)b[o + c];
+            if (c2) v1 += (double)c2[o + c] * (double)d2[o + c];
+        }
+        store_partial(partial, nB, 0, k, v0);
+        if (c2) store_partial(partial, nB, 1, k, v1);
+    }
+}
+
+__global__ void k_mx_copy(int N, unsigned mask, const float *__restrict__ r, float *__restrict__ w) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((mask >> k) & 1u) w[(size_t)k * N + c] = r[(size_t)k * N + c];
+}
+
+__global__ void k_mx_diag_apply(int N, unsigned mask, const float *__restrict__ rD, const float *__restrict__ r,
+                                float *__restrict__ w) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((mask >> k) & 1u) w[(size_t)k * N + c] = rD[c] * r[(size_t)k * N + c];
+}
+
+// flexible PCG scalars: wArAold = wArA; wArA = w.r; beta = w.(r - r_old) /
+// wArAold = (w.r - alpha_old w.q_old) / wArAold (Polak-Ribiere form: robust
+// to the FP32 preconditioner, which is not exactly the same operator twice)
+__global__ void k_mx_sc_pcg_a(unsigned mask, int first, const double *res, double *S) {
+    int k = threadIdx.x;
+    if (k < 6 && ((mask >> k) & 1u)) {
+        const double aold = S[S_A * 8 + k];
+        S[S_AOLD * 8 + k] = aold;
+        S[S_A * 8 + k] = res[k];
+        if (!first) S[S_B * 8 + k] = (res[k] - S[S_ALPHA * 8 + k] * res[6 + k]) / aold;
+    }
+}
+
+// PCG: p = w (+ beta p)
+__global__ void k_mx_pcg_p(int N, unsigned mask, int first, const double *__restrict__ S,
+                           const float *__restrict__ w, float *__restrict__ p) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        size_t i = (size_t)k * N + c;
+        if (first) p[i] = w[i];
+        else p[i] = fmaf((float)S[S_B * 8 + k], p[i], w[i]);
+    }
+}
+
+// PCG: x += alpha p; r -= alpha q; partial |r| (slot 0)
+__global__ void k_mx_pcg_update(int N, unsigned mask, const double *__restrict__ S, const float *__restrict__ p,
+                                const float *__restrict__ q, float *__restrict__ x, float *__restrict__ r,
+                                double *partial, int nB) {
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const bool sing = S[S_SING * 8 + k] != 0.0;
+        const float alpha = (float)S[S_ALPHA * 8 + k];
+        double v = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            float rr = r[o + c];
+            if (!sing) {
+                x[o + c] = fmaf(alpha, p[o + c], x[o + c]);
+                rr = fmaf(-alpha, q[o + c], rr);
+                r[o + c] = rr;
+            }
+            v += fabs((double)rr);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+}
+
+// psi += x32; x32 = 0
+__global__ void k_mx_fold(int N, unsigned mask, float *__restrict__ x32, double *__restrict__ psi) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        size_t i = (size_t)k * N + c;
+        psi[i] += (double)x32[i];
+        x32[i] = 0.0f;
+    }
+}
+
+// r32 = b - A psi from the FP64 matrix; partial |b - A psi| (slot 0)
+__global__ void k_mx_true_res(Ell e, unsigned mask, const double *__restrict__ diag,
+                              const double *__restrict__ upper, const double *__restrict__ lower,
+                              const double *__restrict__ b, const double *__restrict__ psi,
+                              float *__restrict__ r32, double *partial, int nB) {
+    const int N = e.N;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        double v = 0.0;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            const double r = b[(size_t)k * N + c] - row_mul(e, c, diag, upper, lower, psi + (size_t)k * N);
+            r32[(size_t)k * N + c] = (float)r;
+            v += fabs(r);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+}
+
+// BiCGStab: p = r (first iteration or restart) or r + beta (p - omega Ay)
+__global__ void k_mx_bicg_p(int N, unsigned mask, int first, const double *__restrict__ S,
+                            const float *__restrict__ r, const float *__restrict__ Ay, float *__restrict__ p) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        if (S[S_SING * 8 + k] != 0.0) continue;
+        size_t i = (size_t)k * N + c;
+        if (first || S[S_RST * 8 + k] != 0.0) p[i] = r[i];
+        else {
+            const float beta = (float)S[S_B * 8 + k], omega = (float)S[S_OMEGA * 8 + k];
+            p[i] = fmaf(beta, fmaf(-omega, Ay[i], p[i]), r[i]);
+        }
+    }
+}
+
+// BiCGStab: alpha = r0r / (r0 . Ay); a pending restart is consumed
+__global__ void k_mx_sc_bicg_alpha(unsigned mask, const double *res, double *S) {
+    int k = threadIdx.x;
+    if (k < 6 && ((mask >> k) & 1u)) {
+        S[S_ALPHA * 8 + k] = S[S_R0R * 8 + k] / res[k];
+        S[S_RST * 8 + k] = 0.0;
+    }
+}
+
+__global__ void k_mx_set_rst(unsigned mask, double *S) {
+    int k = threadIdx.x;
+    if (k < 6 && ((mask >> k) & 1u)) S[S_RST * 8 + k] = 1.0;
+}
+
+// BiCGStab: s = r - alpha Ay; partial |s|
+__global__ void k_mx_bicg_s(int N, unsigned mask, const double *__restrict__ S, const float *__restrict__ r,
+                            const float *__restrict__ Ay, float *__restrict__ s, double *partial, int nB) {
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const float alpha = (float)S[S_ALPHA * 8 + k];
+        double v = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            const float sv = fmaf(-alpha, Ay[o + c], r[o + c]);
+            s[o + c] = sv;
+            v += fabs((double)sv);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+}
+
+// x32 += alpha y
+__global__ void k_mx_axpy_alpha(int N, unsigned mask, const double *__restrict__ S, const float *__restrict__ y,
+                                float *__restrict__ x) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((mask >> k) & 1u) {
+            size_t i = (size_t)k * N + c;
+            x[i] = fmaf((float)S[S_ALPHA * 8 + k], y[i], x[i]);
+        }
+}
+
+// x32 += alpha y + omega z; r = s - omega t; partial |r|
+__global__ void k_mx_bicg_update(int N, unsigned mask, const double *__restrict__ S, const float *__restrict__ y,
+                                 const float *__restrict__ z, const float *__restrict__ s,
+                                 const float *__restrict__ t, float *__restrict__ x, float *__restrict__ r,
+                                 double *partial, int nB) {
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const float alpha = (float)S[S_ALPHA * 8 + k], omega = (float)S[S_OMEGA * 8 + k];
+        double v = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            x[o + c] = fmaf(alpha, y[o + c], fmaf(omega, z[o + c], x[o + c]));
+            const float rv = fmaf(-omega, t[o + c], s[o + c]);
+            r[o + c] = rv;
+            v += fabs((double)rv);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+}
+
+// FP32 state of one mixed solve
+struct Mixed : Solver {
+    float *d32, *u32, *l32, *rD32;   // matrix copy, preconditioner diagonal
+    float *vec;                      // FP32 vectors, 6N each
+    double *rD64;
+
+    Mixed(rt_ctx *c, const SolveArgs &args, int nVec) : Solver(c, args) {
+        const size_t V6 = 6 * (size_t)N, F = ctx->mesh.F;
+        ctx->kws32.alloc(9 * V6 + 2 * (size_t)N + 2 * F + 256);
+        float *p = ctx->kws32.p;
+        vec = p;
+        d32 = p + 9 * V6;
+        rD32 = d32 + N;
+        u32 = rD32 + N;
+        l32 = u32 + F;
+        rD64 = ctx->kws.p + 48 * (size_t)N;
+        (void)nVec;
+    }
+    float *v(int i) const { return vec + (size_t)i * 6 * N; }
+
+    // FP32 matrix copy and FP32 preconditioner from the FP64 factorisation
+    void prepare() {
+        const int F = ctx->mesh.F;
+        {
+            ProfScope ps(ctx, "mixed_convert", (double)N * 12.0 + (double)F * 24.0);
+            k_mx_mat32<<<nblocks(std::max(N, F)), RT_BLOCK, 0, st>>>(e, F, a.diag, a.upper, a.lower, d32, u32, l32);
+            RT_CHECK_LAUNCH();
+            launch_count(ctx);
+        }
+        const int pre = a.ctl.preconditioner;
+        if (systolic()) {
+            const double fpc = (double)ctx->mesh.F / N;
+            ProfScope ps(ctx, "dilu_rD", (double)N * (16.0 + fpc * 28.0));
+            skew_prepare32(ctx, a.diag, a.upper, a.lower);
+        } else if (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU || pre == RT_PRECOND_DIAGONAL) {
+            compute_rd(rD64);
+            k_mx_to32<<<nblocks(N), RT_BLOCK, 0, st>>>(N, rD64, rD32);
+            RT_CHECK_LAUNCH();
+            launch_count(ctx);
+        }
+    }
+
+    void precondition32(unsigned mask, const float *r, float *w) {
+        const DevMesh &m = ctx->mesh;
+        const int pre = a.ctl.preconditioner;
+        const double fpc = (double)m.F / N;
+        if (pre == RT_PRECOND_NONE) {
+            k_mx_copy<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, r, w);
+            launch_count(ctx);
+        } else if (pre == RT_PRECOND_DIAGONAL) {
+            k_mx_diag_apply<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, rD32, r, w);
+            launch_count(ctx);
+        } else if (systolic()) {
+            ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 16.0 + 16.0 * pop(mask)));
+            skew_precondition32(ctx, a.nc, mask, r, w);
+        } else {
+            ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 24.0 + 16.0 * pop(mask)));
+            for (int l = 0; l < m.nLevels; ++l) {
+                int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
+                k_fwd_level<float><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD32,
+                                                                          l32, r, w);
+            }
+            for (int l = m.nLevels - 1; l >= 0; --l) {
+                int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
+                k_bwd_level<float><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD32,
+                                                                          u32, w);
+            }
+            launch_count(ctx, 2 * m.nLevels);
+        }
+        RT_CHECK_LAUNCH();
+    }
+
+    void amul32(unsigned mask, const float *x, float *y) {
+        const double fpc = (double)ctx->mesh.F / N;
+        ProfScope ps(ctx, "amul32", (double)N * (4.0 + fpc * 16.0 + 8.0 * pop(mask)));
+        k_mx_amul<<<nblocks(N), RT_BLOCK, 0, st>>>(e, mask, d32, u32, l32, x, y);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+    }
+
+    void dot32(unsigned mask, const float *x, const float *y, const float *x2 = nullptr,
+               const float *y2 = nullptr) {
+        ProfScope ps(ctx, "dot32", (double)N * 4.0 * (x2 ? 4 : 2) * pop(mask));
+        k_mx_dot<<<nB, RT_BLOCK, 0, st>>>(N, mask, x, y, x2, y2, ctx->red.partial.p, nB);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+        finalize(x2 ? 2 : 1, mask);
+    }
+
+    void sync_scalars() {
+        RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, S, sizeof(double) * (S_SING + 1) * 8, cudaMemcpyDeviceToHost,
+                                st));
+        RT_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // fold x32 into psi and replace r32 by b - A psi; S_FIN gets the
+    // normalised FP64 residual of the masked components
+    void replace(unsigned mask, float *x32, float *r32) {
+        if (!mask) return;
+        const double fpc = (double)ctx->mesh.F / N;
+        ProfScope ps(ctx, "residual_replace", (double)N * (8.0 + fpc * 24.0 + 44.0 * pop(mask)));
+        k_mx_fold<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, x32, a.psi);
+        k_mx_true_res<<<nB, RT_BLOCK, 0, st>>>(e, mask, a.diag, a.upper, a.lower, a.source, a.psi, r32,
+                                               ctx->red.partial.p, nB);
+        RT_CHECK_LAUNCH();
+        finalize(1, mask);
+        k_sc_fin<<<1, 32, 0, st>>>(mask, ctx->red.result.p, S);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 3);
+    }
+};
+
+// prologue shared by the mixed solvers; returns the components to iterate
+unsigned mixed_begin(Mixed &mx, const SolveArgs &a, rt_solver_perf *perf, float *r32, float *x32,
+                     double *lastTrue) {
+    rt_ctx *ctx = mx.ctx;
+    const int N = mx.N;
+    double *wA = ctx->kws.p, *rA = ctx->kws.p + 6 * (size_t)N;
+    const unsigned mask = a.validMask;
+    mx.prepare();
+    mx.prologue(mask, wA, rA);
+    k_mx_start<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, mask, rA, r32, x32, mx.S);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, mx.S, sizeof(double) * 3 * 8, cudaMemcpyDeviceToHost, mx.st));
+    RT_CUDA(cudaStreamSynchronize(mx.st));
+    unsigned active = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        perf[k].initialResidual = ctx->red.hostResult[S_INIT * 8 + k];
+        perf[k].finalResidual = ctx->red.hostResult[S_FIN * 8 + k];
+        perf[k].nIterations = 0;
+        perf[k].singular = 0;
+        lastTrue[k] = perf[k].finalResidual;
+        if (a.ctl.minIter > 0 || !mx.conv(perf[k].finalResidual, perf[k].initialResidual)) active |= 1u << k;
+    }
+    return active;
+}
+
+// after an iteration: which components need a residual replacement
+unsigned mixed_replace_set(const Mixed &mx, const SolveArgs &a, unsigned cand, const double *H, int iter,
+                           const rt_solver_perf *perf, const double *lastTrue) {
+    unsigned R = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (!((cand >> k) & 1u)) continue;
+        const double fin = H[S_FIN * 8 + k];
+        if (fin < kReplace * lastTrue[k] || mx.conv(fin, perf[k].initialResidual) || iter >= a.ctl.maxIter ||
+            !std::isfinite(fin))
+            R |= 1u << k;
+    }
+    return R;
+}
+
+rt_status run_pcg_mixed(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    Mixed mx(ctx, a, 5);
+    const int N = mx.N;
+    float *r = mx.v(0), *w = mx.v(1), *p = mx.v(2), *q = mx.v(3), *x = mx.v(4);
+    double lastTrue[6] = {};
+    unsigned active = mixed_begin(mx, a, perf, r, x, lastTrue);
+    int iter = 0;
+    while (active) {
+        mx.precondition32(active, r, w);
+        if (iter == 0) mx.dot32(active, w, r);
+        else mx.dot32(active, w, r, w, q);   // q = A p of the previous iteration
+        k_mx_sc_pcg_a<<<1, 32, 0, mx.st>>>(active, iter == 0, ctx->red.result.p, mx.S);
+        k_mx_pcg_p<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, iter == 0, mx.S, w, p);
+        mx.amul32(active, p, q);
+        mx.dot32(active, q, p);
+        k_sc_pcg_alpha<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
+        k_mx_pcg_update<<<mx.nB, RT_BLOCK, 0, mx.st>>>(N, active, mx.S, p, q, x, r, ctx->red.partial.p, mx.nB);
+        RT_CHECK_LAUNCH();
+        mx.finalize(1, active);
+        k_sc_fin<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 4);
+        mx.sync_scalars();
+        ++iter;
+        double H[(S_SING + 1) * 8];
+        memcpy(H, ctx->red.hostResult, sizeof H);
+        unsigned sing = 0;
+        for (int k = 0; k < 6; ++k)
+            if (((active >> k) & 1u) && H[S_SING * 8 + k] != 0.0) {
+                perf[k].singular = 1;
+                sing |= 1u << k;
+            }
+        const unsigned cand = active & ~sing;
+        const unsigned R = mixed_replace_set(mx, a, cand, H, iter, perf, lastTrue);
+        mx.replace(R, x, r);
+        if (R) {
+            mx.sync_scalars();
+            memcpy(H, ctx->red.hostResult, sizeof H);
+        }
+        unsigned next = 0;
+        for (int k = 0; k < 6; ++k) {
+            if (!((cand >> k) & 1u)) continue;
+            perf[k].finalResidual = H[S_FIN * 8 + k];
+            perf[k].nIterations = iter;
+            if ((R >> k) & 1u) lastTrue[k] = perf[k].finalResidual;
+            const bool conv = ((R >> k) & 1u) && mx.conv(perf[k].finalResidual, perf[k].initialResidual);
+            const bool more = (iter < a.ctl.maxIter && !conv) || iter < a.ctl.minIter;
+            if (more && std::isfinite(perf[k].finalResidual)) next |= 1u << k;
+        }
+        active = next;
+    }
+    // whatever is still in x32 (singular components) goes to psi
+    k_mx_fold<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, a.validMask, x, a.psi);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    return RT_OK;
+}
+
+rt_status run_pbicgstab_mixed(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    Mixed mx(ctx, a, 9);
+    const int N = mx.N;
+    float *r = mx.v(0), *r0 = mx.v(1), *p = mx.v(2), *y = mx.v(3), *Ay = mx.v(4), *s = mx.v(5), *z = mx.v(6),
+          *t = mx.v(7), *x = mx.v(8);
+    double lastTrue[6] = {};
+    unsigned active = mixed_begin(mx, a, perf, r, x, lastTrue);
+    if (!active) return RT_OK;
+    RT_CUDA(cudaMemcpyAsync(r0, r, sizeof(float) * 6 * (size_t)N, cudaMemcpyDeviceToDevice, mx.st));
+    int iter = 0;
+    double H[(S_SING + 1) * 8];
+    while (active) {
+        mx.dot32(active, r0, r);
+        k_sc_bicg_r0r<<<1, 32, 0, mx.st>>>(active, iter, ctx->red.result.p, mx.S);
+        k_mx_bicg_p<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, iter == 0, mx.S, r, Ay, p);
+        mx.precondition32(active, p, y);
+        mx.amul32(active, y, Ay);
+        mx.dot32(active, r0, Ay);
+        k_mx_sc_bicg_alpha<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
+        k_mx_bicg_s<<<mx.nB, RT_BLOCK, 0, mx.st>>>(N, active, mx.S, r, Ay, s, ctx->red.partial.p, mx.nB);
+        RT_CHECK_LAUNCH();
+        mx.finalize(1, active);
+        k_sc_fin<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 5);
+        mx.sync_scalars();
+        memcpy(H, ctx->red.hostResult, sizeof H);
+        // the half-step test: components whose s meets the tolerance take
+        // x += alpha y and have their residual replaced; the FP64 residual
+        // decides whether they stop or restart
+        unsigned half = 0, cont = 0;
+        for (int k = 0; k < 6; ++k) {
+            if (!((active >> k) & 1u)) continue;
+            if (H[S_SING * 8 + k] != 0.0) {
+                perf[k].singular = 1;
+                continue;
+            }
+            if (mx.conv(H[S_FIN * 8 + k], perf[k].initialResidual)) half |= 1u << k;
+            else cont |= 1u << k;
+        }
+        unsigned restart = 0;
+        if (half) {
+            k_mx_axpy_alpha<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, half, mx.S, y, x);
+            RT_CHECK_LAUNCH();
+            launch_count(ctx);
+            mx.replace(half, x, r);
+            mx.sync_scalars();
+            for (int k = 0; k < 6; ++k) {
+                if (!((half >> k) & 1u)) continue;
+                perf[k].finalResidual = ctx->red.hostResult[S_FIN * 8 + k];
+                perf[k].nIterations = iter + 1;
+                lastTrue[k] = perf[k].finalResidual;
+                const bool conv = mx.conv(perf[k].finalResidual, perf[k].initialResidual);
+                if ((!conv || iter + 1 < a.ctl.minIter) && iter + 1 < a.ctl.maxIter &&
+                    std::isfinite(perf[k].finalResidual))
+                    restart |= 1u << k;
+            }
+            if (restart) {
+                k_mx_set_rst<<<1, 32, 0, mx.st>>>(restart, mx.S);
+                RT_CHECK_LAUNCH();
+                launch_count(ctx);
+            }
+        }
+        unsigned next = restart;
+        if (cont) {
+            mx.precondition32(cont, s, z);
+            mx.amul32(cont, z, t);
+            mx.dot32(cont, t, t, t, s);
+            k_sc_bicg_omega<<<1, 32, 0, mx.st>>>(cont, ctx->red.result.p, mx.S);
+            k_mx_bicg_update<<<mx.nB, RT_BLOCK, 0, mx.st>>>(N, cont, mx.S, y, z, s, t, x, r, ctx->red.partial.p,
+                                                            mx.nB);
+            RT_CHECK_LAUNCH();
+            mx.finalize(1, cont);
+            k_sc_fin<<<1, 32, 0, mx.st>>>(cont, ctx->red.result.p, mx.S);
+            RT_CHECK_LAUNCH();
+            launch_count(ctx, 3);
+            mx.sync_scalars();
+            memcpy(H, ctx->red.hostResult, sizeof H);
+            const unsigned R = mixed_replace_set(mx, a, cont, H, iter + 1, perf, lastTrue);
+            mx.replace(R, x, r);
+            if (R) {
+                mx.sync_scalars();
+                memcpy(H, ctx->red.hostResult, sizeof H);
+            }
+            for (int k = 0; k < 6; ++k) {
+                if (!((cont >> k) & 1u)) continue;
+                perf[k].finalResidual = H[S_FIN * 8 + k];
+                perf[k].nIterations = iter + 1;
+                if ((R >> k) & 1u) lastTrue[k] = perf[k].finalResidual;
+                const bool conv = ((R >> k) & 1u) && mx.conv(perf[k].finalResidual, perf[k].initialResidual);
+                const bool more = (iter + 1 < a.ctl.maxIter && !conv) || iter + 1 < a.ctl.minIter;
+                if (more && std::isfinite(perf[k].finalResidual)) next |= 1u << k;
+            }
+        }
+        ++iter;
+        active = next;
+    }
+    k_mx_fold<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, a.validMask, x, a.psi);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    return RT_OK;
+}
+
 }  // namespace
 
 rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
@@ -760,7 +1347,18 @@ rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf
     SolveArgs b = a;
     b.validMask = mask;
     rt_status st = RT_OK;
-    if (mask) st = (a.ctl.solver == RT_SOLVER_PCG) ? run_pcg(ctx, b, perf) : run_pbicgstab(ctx, b, perf);
+    if (mask && ctx->mesh.batch.n > 1) {
+        st = batch_solve(ctx, b, perf);
+    } else if (mask) {
+        const bool pcg = a.ctl.solver == RT_SOLVER_PCG;
+        if (a.precision == RT_PREC_MIXED && (ctx->mixedParts & 1)) {
+            SolveArgs t = b;
+            t.ctl.tolerance *= ctx->mixedTighten;
+            t.ctl.relTol *= ctx->mixedTighten;
+            st = pcg ? run_pcg_mixed(ctx, t, perf) : run_pbicgstab_mixed(ctx, t, perf);
+        }
+        else st = pcg ? run_pcg(ctx, b, perf) : run_pbicgstab(ctx, b, perf);
+    }
     rt_status sw = skew_check(ctx);
     if (sw != RT_OK) return sw;
     for (int k = 0; k < a.nc; ++k) {

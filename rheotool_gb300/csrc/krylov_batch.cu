@@ -1,0 +1,942 @@
+// krylov_batch.cu — PCG (+DIC) and PBiCGStab (+DILU) for a batch of
+// independent cases that share one device mesh (their disjoint union).
+//
+// Every (case, component) pair is a segment with its own Krylov scalars,
+// its own normFactor, iteration count and stopping point, exactly as if the
+// case were solved alone: the matrix of a batch is block diagonal, and every
+// inner product and norm is reduced per case (reduction blocks never straddle
+// two cases; the blocks of a case are summed in a fixed order).  Segments
+// iterate in lock step; a segment that has stopped takes no further updates.
+// The stopping decisions are taken on the device (one thread per segment),
+// so one iteration is a fixed launch sequence: it is captured once into a
+// CUDA graph and replayed, and the host only polls the number of segments
+// still iterating every few iterations.
+//
+// Precision: the vectors are FP32 (RT_PREC_MIXED) or FP64, the scalars and
+// reductions FP64.  As in the single-case mixed solvers, the solution is
+// psi (FP64) + x (a correction in the vector type), folded into psi with the
+// residual recomputed from the FP64 matrix whenever the iterated residual has
+// dropped tenfold, claims convergence or the iteration budget ends; the
+// stopping test uses that FP64 residual.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "batch.h"
+#include "real_ops.cuh"
+
+namespace rt {
+
+namespace {
+
+constexpr double kReplaceB = 0.1;
+
+__device__ __forceinline__ double bsum(double v) {   // valid in thread 0
+    __shared__ double sh[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct BEll {
+    int N, nSlots;
+    const int *__restrict__ face;
+    const int *__restrict__ nbr;
+};
+
+template <class M, class X>
+__device__ __forceinline__ double brow_mul(const BEll &e, int c, const M *__restrict__ diag, const M *__restrict__ upper,
+                                           const M *__restrict__ lower, const X *__restrict__ x) {
+    double acc = (double)diag[c] * (double)x[c];
+    for (int s = 0; s < e.nSlots; ++s) {
+        int nb = e.nbr[s * e.N + c];
+        if (nb < 0) break;
+        int f = e.face[s * e.N + c];
+        acc += (double)(nb > c ? upper[f] : lower[f]) * (double)x[nb];
+    }
+    return acc;
+}
+
+__device__ __forceinline__ double brow_sum(const BEll &e, int c, const double *__restrict__ diag,
+                                           const double *__restrict__ upper, const double *__restrict__ lower) {
+    double acc = diag[c];
+    for (int s = 0; s < e.nSlots; ++s) {
+        int nb = e.nbr[s * e.N + c];
+        if (nb < 0) break;
+        int f = e.face[s * e.N + c];
+        acc += nb > c ? upper[f] : lower[f];
+    }
+    return acc;
+}
+
+struct Ctl {
+    double tol, relTol;
+    int minIter, maxIter;
+};
+__device__ __forceinline__ bool bconv(const Ctl &c, double fin, double init) {
+    return fin < c.tol || (c.relTol > 1e-20 && fin < c.relTol * init);
+}
+
+// ---- reductions ---------------------------------------------------------
+// partial[(slot * 6 + k) * nBlk + blk]; res[slot * nSeg + case * 8 + k]
+__global__ void k_b_fin(int nSlots, unsigned vm, BTab t, const double *__restrict__ partial, double *__restrict__ res) {
+    const int cb = blockIdx.x, k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (k >= 6 || !((vm >> k) & 1u)) return;
+    const int b0 = t.caseBlk[cb], b1 = t.caseBlk[cb + 1];
+    const int nSeg = 8 * t.nCases;
+    for (int slot = 0; slot < nSlots; ++slot) {
+        double v = 0.0;
+        for (int i = b0 + lane; i < b1; i += 32) v += partial[(slot * 6 + k) * t.nBlk + i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) res[slot * nSeg + cb * 8 + k] = v;
+    }
+}
+
+__global__ void k_b_sumx(BTab t, unsigned vm, const double *__restrict__ x, double *partial) {
+    const int blk = blockIdx.x, c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        double s = bsum(in ? x[(size_t)k * t.N + c] : 0.0);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = s;
+    }
+}
+
+// r = b - A psi (FP64) into the vector type; slot 0: normFactor sums, slot 1: |r|
+template <class V>
+__global__ void k_b_init_res(BTab t, BEll e, unsigned vm, const double *__restrict__ diag,
+                             const double *__restrict__ upper, const double *__restrict__ lower,
+                             const double *__restrict__ b, const double *__restrict__ psi,
+                             const double *__restrict__ xsum, const int *__restrict__ caseCell0, V *__restrict__ r,
+                             V *__restrict__ x, double *partial) {
+    const int blk = blockIdx.x, cb = t.blkCase[blk], c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    const int nSeg = 8 * t.nCases;
+    const double nCell = (double)(caseCell0[cb + 1] - caseCell0[cb]);
+    (void)nSeg;
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        double v0 = 0.0, v1 = 0.0;
+        if (in) {
+            const double xbar = xsum[cb * 8 + k] / nCell;
+            const size_t o = (size_t)k * t.N;
+            double ax = brow_mul(e, c, diag, upper, lower, psi + o);
+            double sa = brow_sum(e, c, diag, upper, lower) * xbar;
+            double bb = b[o + c];
+            double rr = bb - ax;
+            r[o + c] = (V)rr;
+            x[o + c] = V(0);
+            v0 = fabs(ax - sa) + fabs(bb - sa);
+            v1 = fabs(rr);
+        }
+        double s0 = bsum(v0);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = s0;
+        double s1 = bsum(v1);
+        if (threadIdx.x == 0) partial[(1 * 6 + k) * t.nBlk + blk] = s1;
+    }
+}
+
+template <class V>
+__global__ void k_b_dot(BTab t, unsigned vm, const int *__restrict__ active, const V *__restrict__ a,
+                        const V *__restrict__ b, const V *__restrict__ c2, const V *__restrict__ d2, double *partial) {
+    const int blk = blockIdx.x, cb = t.blkCase[blk], c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        if (!active[cb * 8 + k]) continue;   // uniform in the block
+        const size_t o = (size_t)k * t.N;
+        double v0 = in ? (double)a[o + c] * (double)b[o + c] : 0.0;
+        double s0 = bsum(v0);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = s0;
+        if (c2) {
+            double v1 = in ? (double)c2[o + c] * (double)d2[o + c] : 0.0;
+            double s1 = bsum(v1);
+            if (threadIdx.x == 0) partial[(1 * 6 + k) * t.nBlk + blk] = s1;
+        }
+    }
+}
+
+// ---- vector kernels (one thread per cell) ----------------------------------
+template <class V, class M>
+__global__ void k_b_amul(BEll e, unsigned vm, const M *__restrict__ diag, const M *__restrict__ upper,
+                         const M *__restrict__ lower, const V *__restrict__ x, V *__restrict__ y) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= e.N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const size_t o = (size_t)k * e.N;
+        const V xc = x[o + c];
+        V acc = V(diag[c]) * xc;
+        for (int s = 0; s < e.nSlots; ++s) {
+            int nb = e.nbr[s * e.N + c];
+            if (nb < 0) break;
+            int f = e.face[s * e.N + c];
+            // FP32: differences form (diag holds the row sums)
+            acc = fma(V(nb > c ? upper[f] : lower[f]), sizeof(V) == 4 ? x[o + nb] - xc : x[o + nb], acc);
+        }
+        y[o + c] = acc;
+    }
+}
+
+template <class V>
+__global__ void k_b_pcg_p(int N, unsigned vm, const int *__restrict__ caseOf, BSeg S, const V *__restrict__ w,
+                          V *__restrict__ p) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int cb = caseOf[c];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const int sg = cb * 8 + k;
+        if (!S.active[sg]) continue;
+        const size_t i = (size_t)k * N + c;
+        if (S.iter[sg] == 0) p[i] = w[i];
+        else p[i] = fma(V(S.beta[sg]), p[i], w[i]);
+    }
+}
+
+template <class V>
+__global__ void k_b_pcg_update(BTab t, unsigned vm, BSeg S, const V *__restrict__ p, const V *__restrict__ q,
+                               V *__restrict__ x, V *__restrict__ r, double *partial) {
+    const int blk = blockIdx.x, cb = t.blkCase[blk], c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const int sg = cb * 8 + k;
+        if (!S.active[sg]) continue;
+        double v = 0.0;
+        if (in) {
+            const size_t i = (size_t)k * t.N + c;
+            V rr = r[i];
+            if (!S.sing[sg]) {
+                const V alpha = V(S.alpha[sg]);
+                x[i] = fma(alpha, p[i], x[i]);
+                rr = fma(-alpha, q[i], rr);
+                r[i] = rr;
+            }
+            v = fabs((double)rr);
+        }
+        double s = bsum(v);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = s;
+    }
+}
+
+// psi += x; x = 0 on the segments flagged in flag[] (all when flag is null)
+template <class V>
+__global__ void k_b_fold(int N, unsigned vm, const int *__restrict__ caseOf, const int *__restrict__ flag,
+                         V *__restrict__ x, double *__restrict__ psi) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int cb = caseOf[c];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u) || (flag && !flag[cb * 8 + k])) continue;
+        const size_t i = (size_t)k * N + c;
+        psi[i] += (double)x[i];
+        x[i] = V(0);
+    }
+}
+
+// r = b - A psi (FP64 matrix) on flagged segments; partial |r|
+template <class V>
+__global__ void k_b_true(BTab t, BEll e, unsigned vm, const int *__restrict__ flag, const double *__restrict__ diag,
+                         const double *__restrict__ upper, const double *__restrict__ lower,
+                         const double *__restrict__ b, const double *__restrict__ psi, V *__restrict__ r,
+                         double *partial) {
+    const int blk = blockIdx.x, cb = t.blkCase[blk], c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u) || !flag[cb * 8 + k]) continue;
+        double v = 0.0;
+        if (in) {
+            const size_t o = (size_t)k * t.N;
+            const double rr = b[o + c] - brow_mul(e, c, diag, upper, lower, psi + o);
+            r[o + c] = (V)rr;
+            v = fabs(rr);
+        }
+        double s = bsum(v);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = s;
+    }
+}
+
+template <class V>
+__global__ void k_b_bicg_p(int N, unsigned vm, const int *__restrict__ caseOf, BSeg S, const V *__restrict__ r,
+                           const V *__restrict__ Ay, V *__restrict__ p) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int cb = caseOf[c];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const int sg = cb * 8 + k;
+        if (!S.active[sg] || S.sing[sg]) continue;
+        const size_t i = (size_t)k * N + c;
+        if (S.iter[sg] == 0 || S.rst[sg]) p[i] = r[i];
+        else p[i] = fma(V(S.beta[sg]), fma(-V(S.omega[sg]), Ay[i], p[i]), r[i]);
+    }
+}
+
+template <class V>
+__global__ void k_b_bicg_s(BTab t, unsigned vm, BSeg S, const V *__restrict__ r, const V *__restrict__ Ay,
+                           V *__restrict__ s, double *partial) {
+    const int blk = blockIdx.x, cb = t.blkCase[blk], c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const int sg = cb * 8 + k;
+        if (!S.active[sg] || S.sing[sg]) continue;
+        double v = 0.0;
+        if (in) {
+            const size_t i = (size_t)k * t.N + c;
+            const V sv = fma(-V(S.alpha[sg]), Ay[i], r[i]);
+            s[i] = sv;
+            v = fabs((double)sv);
+        }
+        double sm = bsum(v);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = sm;
+    }
+}
+
+// x += alpha y on the half-step segments (flag 'half' in S.repl == 2)
+template <class V>
+__global__ void k_b_axpy_half(int N, unsigned vm, const int *__restrict__ caseOf, BSeg S, const V *__restrict__ y,
+                              V *__restrict__ x) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int cb = caseOf[c];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const int sg = cb * 8 + k;
+        if (S.conv[sg] != 2) continue;
+        const size_t i = (size_t)k * N + c;
+        x[i] = fma(V(S.alpha[sg]), y[i], x[i]);
+    }
+}
+
+template <class V>
+__global__ void k_b_bicg_update(BTab t, unsigned vm, BSeg S, const V *__restrict__ y, const V *__restrict__ z,
+                                const V *__restrict__ s, const V *__restrict__ tt, V *__restrict__ x,
+                                V *__restrict__ r, double *partial) {
+    const int blk = blockIdx.x, cb = t.blkCase[blk], c = t.blkCell0[blk] + threadIdx.x;
+    const bool in = c < t.blkCell1[blk];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        const int sg = cb * 8 + k;
+        if (!S.active[sg] || S.sing[sg] || S.conv[sg] == 2) continue;
+        double v = 0.0;
+        if (in) {
+            const size_t i = (size_t)k * t.N + c;
+            const V alpha = V(S.alpha[sg]), omega = V(S.omega[sg]);
+            x[i] = fma(alpha, y[i], fma(omega, z[i], x[i]));
+            const V rv = fma(-omega, tt[i], s[i]);
+            r[i] = rv;
+            v = fabs((double)rv);
+        }
+        double sm = bsum(v);
+        if (threadIdx.x == 0) partial[(0 * 6 + k) * t.nBlk + blk] = sm;
+    }
+}
+
+// ---- per-segment logic (one block, threads stride over the segments) ------
+// S.conv: 0 iterating, 1 converged (stopped), 2 half-step exit pending
+__global__ void k_b_start(int nCases, unsigned vm, Ctl ctl, BSeg S, const double *__restrict__ res) {
+    const int nSeg = 8 * nCases;
+    int cnt = 0;
+    for (int sg = threadIdx.x; sg < nSeg; sg += blockDim.x) {
+        const int k = sg & 7;
+        if (k >= 6 || !((vm >> k) & 1u)) {
+            S.active[sg] = 0;
+            continue;
+        }
+        const double nf = res[0 * nSeg + sg] + 1e-20;
+        const double r0 = res[1 * nSeg + sg] / nf;
+        S.nf[sg] = nf;
+        S.init[sg] = r0;
+        S.fin[sg] = r0;
+        S.last[sg] = r0;
+        S.iter[sg] = 0;
+        S.sing[sg] = 0;
+        S.repl[sg] = 0;
+        S.rst[sg] = 0;
+        S.A[sg] = 1e20;
+        S.r0r[sg] = 0.0;
+        S.alpha[sg] = 0.0;
+        S.omega[sg] = 0.0;
+        const bool c = bconv(ctl, r0, r0);
+        S.conv[sg] = c ? 1 : 0;
+        S.active[sg] = (ctl.minIter > 0 || !c) ? 1 : 0;
+        cnt += S.active[sg];
+    }
+    __shared__ int sc[32];
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) sc[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sc[i];
+        S.count[0] = t;
+    }
+}
+
+// PCG scalars; FP32 vectors use the flexible (Polak-Ribiere) beta
+// w.(r - r_old) / w_old.r_old = (w.r - alpha_old w.q_old) / w_old.r_old
+__global__ void k_b_pcg_a(int nSeg, BSeg S, const double *__restrict__ res, int mixed) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg]) continue;
+        const double aold = S.A[sg];
+        S.Aold[sg] = aold;
+        S.A[sg] = res[sg];
+        S.beta[sg] = mixed ? (res[sg] - S.alpha[sg] * res[nSeg + sg]) / aold : res[sg] / aold;
+    }
+}
+
+__global__ void k_b_pcg_alpha(int nSeg, BSeg S, const double *__restrict__ res) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg]) continue;
+        const double wApA = res[sg];
+        if (fabs(wApA) / S.nf[sg] < 1e-300) {
+            S.sing[sg] = 1;
+            S.alpha[sg] = 0.0;
+        } else {
+            S.alpha[sg] = S.A[sg] / wApA;
+        }
+    }
+}
+
+// after an iteration's residual: count the iteration, stop singular
+// segments; mixed precision flags the residual replacements, FP64 applies the
+// stopping test of the plain solvers to the iterated residual
+__global__ void k_b_iter_fin(int nSeg, Ctl ctl, BSeg S, const double *__restrict__ res, int skipHalf, int mixed) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg]) continue;
+        if (skipHalf && S.conv[sg] == 2) {   // restarted at the half step: counted, no update
+            S.iter[sg] += 1;
+            S.conv[sg] = 0;
+            continue;
+        }
+        if (S.sing[sg]) {
+            S.active[sg] = 0;
+            continue;
+        }
+        const double fin = res[sg] / S.nf[sg];
+        S.fin[sg] = fin;
+        S.iter[sg] += 1;
+        if (mixed) {
+            S.repl[sg] = (fin < kReplaceB * S.last[sg] || bconv(ctl, fin, S.init[sg]) || S.iter[sg] >= ctl.maxIter ||
+                          !isfinite(fin)) ? 1 : 0;
+        } else {
+            const bool c = bconv(ctl, fin, S.init[sg]);
+            const bool more = (S.iter[sg] < ctl.maxIter && !c) || S.iter[sg] < ctl.minIter;
+            S.conv[sg] = c ? 1 : 0;
+            if (!more || !isfinite(fin)) S.active[sg] = 0;
+        }
+    }
+}
+
+// after a residual replacement: FP64 residual, stopping test, count
+__global__ void k_b_after(int nCases, Ctl ctl, BSeg S, const double *__restrict__ res) {
+    const int nSeg = 8 * nCases;
+    int cnt = 0;
+    for (int sg = threadIdx.x; sg < nSeg; sg += blockDim.x) {
+        if (S.active[sg] && S.repl[sg]) {
+            const double fin = res[sg] / S.nf[sg];
+            S.fin[sg] = fin;
+            S.last[sg] = fin;
+            const bool c = bconv(ctl, fin, S.init[sg]);
+            const bool more = (S.iter[sg] < ctl.maxIter && !c) || S.iter[sg] < ctl.minIter;
+            S.conv[sg] = c ? 1 : 0;
+            if (!more || !isfinite(fin)) S.active[sg] = 0;
+        }
+        S.repl[sg] = 0;
+        cnt += S.active[sg];
+    }
+    __shared__ int sc[32];
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) sc[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sc[i];
+        S.count[0] = t;
+    }
+}
+
+// BiCGStab scalars
+__global__ void k_b_bicg_r0r(int nSeg, BSeg S, const double *__restrict__ res) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg]) continue;
+        const double old = S.r0r[sg], r0r = res[sg];
+        S.r0rOld[sg] = old;
+        S.r0r[sg] = r0r;
+        if (fabs(r0r) < 1e-300) { S.sing[sg] = 1; continue; }
+        if (S.iter[sg] > 0 && !S.rst[sg]) {
+            const double om = S.omega[sg];
+            if (fabs(om) < 1e-300) { S.sing[sg] = 1; continue; }
+            S.beta[sg] = (r0r / old) * (S.alpha[sg] / om);
+        }
+    }
+}
+__global__ void k_b_bicg_alpha(int nSeg, BSeg S, const double *__restrict__ res) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg] || S.sing[sg]) continue;
+        S.alpha[sg] = S.r0r[sg] / res[sg];
+        S.rst[sg] = 0;
+    }
+}
+// the half-step test on |s|; singular segments stop here
+__global__ void k_b_bicg_half(int nSeg, Ctl ctl, BSeg S, const double *__restrict__ res, int mixed) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg]) continue;
+        if (S.sing[sg]) {
+            S.active[sg] = 0;
+            continue;
+        }
+        const double fs = res[sg] / S.nf[sg];
+        if (bconv(ctl, fs, S.init[sg])) {
+            S.conv[sg] = 2;
+            S.repl[sg] = mixed ? 1 : 0;
+            if (!mixed) S.fin[sg] = fs;
+        }
+    }
+}
+// after the half step: mixed precision stops or restarts from the FP64
+// residual of the replacement; FP64 stops (the plain solvers' early exit)
+__global__ void k_b_half_after(int nSeg, Ctl ctl, BSeg S, const double *__restrict__ res, int mixed) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg] || S.conv[sg] != 2) continue;
+        if (!mixed) {
+            S.iter[sg] += 1;
+            S.conv[sg] = 1;
+            S.active[sg] = 0;
+            continue;
+        }
+        const double fin = res[sg] / S.nf[sg];
+        S.fin[sg] = fin;
+        S.last[sg] = fin;
+        S.repl[sg] = 0;
+        const int it = S.iter[sg] + 1;
+        const bool c = bconv(ctl, fin, S.init[sg]);
+        if ((c && it >= ctl.minIter) || it >= ctl.maxIter || !isfinite(fin)) {
+            S.iter[sg] = it;
+            S.conv[sg] = c ? 1 : 0;
+            S.active[sg] = 0;
+        } else {
+            S.rst[sg] = 1;   // conv stays 2: the second half is skipped, the iteration counted
+        }
+    }
+}
+__global__ void k_b_bicg_omega(int nSeg, BSeg S, const double *__restrict__ res) {
+    for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
+        if (!S.active[sg] || S.sing[sg] || S.conv[sg] == 2) continue;
+        S.omega[sg] = res[1 * nSeg + sg] / res[sg];
+    }
+}
+
+// ---- level-scheduled sweeps over the union (cases without a 2-D layout) ---
+template <class V>
+__global__ void k_b_fwd_level(BEll e, int l0, int l1, const int *__restrict__ cells, unsigned vm,
+                              const V *__restrict__ rD, const V *__restrict__ lower, const V *__restrict__ r,
+                              V *__restrict__ w) {
+    int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= l1) return;
+    int c = cells[t];
+    const V rd = rD[c];
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        size_t o = (size_t)k * e.N;
+        V acc = r_mul(rd, r[o + c]);
+        for (int s = 0; s < e.nSlots; ++s) {
+            int nb = e.nbr[s * e.N + c];
+            if (nb < 0 || nb > c) break;
+            acc = r_fma(-r_mul(rd, lower[e.face[s * e.N + c]]), w[o + nb], acc);
+        }
+        w[o + c] = acc;
+    }
+}
+template <class V>
+__global__ void k_b_bwd_level(BEll e, int l0, int l1, const int *__restrict__ cells, unsigned vm,
+                              const V *__restrict__ rD, const V *__restrict__ upper, V *__restrict__ w) {
+    int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= l1) return;
+    int c = cells[t];
+    const V rd = rD[c];
+    int ns = 0;
+    while (ns < e.nSlots && e.nbr[ns * e.N + c] >= 0) ++ns;
+    for (int k = 0; k < 6; ++k) {
+        if (!((vm >> k) & 1u)) continue;
+        size_t o = (size_t)k * e.N;
+        V acc = w[o + c];
+        for (int s = ns - 1; s >= 0; --s) {
+            int nb = e.nbr[s * e.N + c];
+            if (nb < c) break;
+            acc = r_fma(-r_mul(rd, upper[e.face[s * e.N + c]]), w[o + nb], acc);
+        }
+        w[o + c] = acc;
+    }
+}
+__global__ void k_b_rd_level(BEll e, int l0, int l1, const int *__restrict__ cells, const double *__restrict__ diag,
+                             const double *__restrict__ upper, const double *__restrict__ lower,
+                             double *__restrict__ rD) {
+    int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= l1) return;
+    int c = cells[t];
+    double r = diag[c];
+    for (int s = 0; s < e.nSlots; ++s) {
+        int nb = e.nbr[s * e.N + c];
+        if (nb < 0 || nb > c) break;
+        int f = e.face[s * e.N + c];
+        r = __dsub_rn(r, __ddiv_rn(__dmul_rn(upper[f], lower[f]), rD[nb]));
+    }
+    rD[c] = r;
+}
+template <class V>
+__global__ void k_b_recip(int N, const double *__restrict__ rD, V *__restrict__ out, int diagOnly,
+                          const double *__restrict__ diag) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < N) out[c] = (V)(1.0 / (diagOnly ? diag[c] : rD[c]));
+}
+// the matrix in the vector type; FP32 stores the row sums in place of the
+// diagonal (differences form: rounding keeps the zero row sums of an
+// assembled matrix), FP64 the diagonal itself
+template <class M>
+__global__ void k_b_mat(BEll e, int F, const double *__restrict__ diag, const double *__restrict__ upper,
+                        const double *__restrict__ lower, M *__restrict__ d, M *__restrict__ u, M *__restrict__ l) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < e.N) d[i] = (M)(sizeof(M) == 4 ? brow_sum(e, i, diag, upper, lower) : diag[i]);
+    if (i < F) {
+        u[i] = (M)upper[i];
+        l[i] = (M)lower[i];
+    }
+}
+template <class V>
+__global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restrict__ w, const V *__restrict__ rD) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((vm >> k) & 1u) w[(size_t)k * N + c] = rD ? rD[c] * r[(size_t)k * N + c] : r[(size_t)k * N + c];
+}
+
+// ---- host side --------------------------------------------------------------
+template <class V>
+struct BSolver {
+    rt_ctx *ctx;
+    const SolveArgs &a;
+    Batch &bt;
+    cudaStream_t st;
+    BTab t;
+    BEll e;
+    BSeg S;
+    Ctl ctl;
+    int N, F, nSeg;
+    int mixed = sizeof(V) == 4;   // FP32 vectors: residual replacement
+    unsigned vm;
+    V *vec, *d32, *u32, *l32, *rD;
+    double *rD64, *partial, *res;
+
+    BSolver(rt_ctx *c, const SolveArgs &args) : ctx(c), a(args), bt(c->mesh.batch) {
+        const DevMesh &m = ctx->mesh;
+        st = ctx->stream;
+        N = m.N;
+        F = m.F;
+        nSeg = 8 * bt.n;
+        vm = a.validMask;
+        t = BTab{N, bt.nBlk, bt.n, bt.blkCase.p, bt.blkCell0.p, bt.blkCell1.p, bt.caseBlk.p, bt.caseOf.p};
+        e = BEll{N, m.nSlots, m.ellFace.p, m.ellNbr.p};
+        ctl = Ctl{a.ctl.tolerance, a.ctl.relTol, a.ctl.minIter, a.ctl.maxIter};
+        double *sd = bt.segD.p;
+        int *si = bt.segI.p;
+        double **dslots[] = {&S.nf, &S.init, &S.fin, &S.xbar, &S.A, &S.Aold, &S.alpha, &S.omega,
+                             &S.r0r, &S.r0rOld, &S.beta, &S.last};
+        for (int i = 0; i < 12; ++i) *dslots[i] = sd + (size_t)i * nSeg;
+        int **islots[] = {&S.active, &S.iter, &S.sing, &S.repl, &S.rst, &S.conv};
+        for (int i = 0; i < 6; ++i) *islots[i] = si + (size_t)i * nSeg;
+        S.count = si + (size_t)6 * nSeg;
+        // vectors: 9 x 6N of V, then the matrix copy and rD
+        const size_t V6 = 6 * (size_t)N;
+        const size_t bytes = sizeof(V) * (9 * V6 + 2 * (size_t)N + 2 * (size_t)F + 64);
+        ctx->kws32.alloc((bytes + sizeof(float) - 1) / sizeof(float));
+        vec = reinterpret_cast<V *>(ctx->kws32.p);
+        d32 = vec + 9 * V6;
+        rD = d32 + N;
+        u32 = rD + N;
+        l32 = u32 + F;
+        ctx->kws.alloc(48 * (size_t)N + 2 * (size_t)N + 64);
+        rD64 = ctx->kws.p + 48 * (size_t)N;
+        partial = bt.bPartial.p;
+        res = bt.bRes.p;
+    }
+    V *v(int i) const { return vec + (size_t)i * 6 * N; }
+    int gridSeg() const { return (nSeg + 255) / 256; }
+
+    void fin(int nSlots, unsigned mask) {
+        k_b_fin<<<bt.n, 192, 0, st>>>(nSlots, mask, t, partial, res);
+        RT_CHECK_LAUNCH();
+    }
+
+    void prepare() {
+        k_b_mat<V><<<nblocks(std::max(N, F)), RT_BLOCK, 0, st>>>(e, F, a.diag, a.upper, a.lower, d32, u32, l32);
+        RT_CHECK_LAUNCH();
+        const int pre = a.ctl.preconditioner;
+        if ((pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU) && bt.sweep2d) {
+            sweep2d_prepare(ctx, a.diag, a.upper, a.lower, sizeof(V) == 4);
+        } else if (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU) {
+            const DevMesh &m = ctx->mesh;
+            for (int l = 0; l < m.nLevels; ++l) {
+                int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
+                k_b_rd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, a.diag, a.upper,
+                                                                     a.lower, rD64);
+            }
+            k_b_recip<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, rD64, rD, 0, a.diag);
+            launch_count(ctx, m.nLevels + 1);
+        } else if (pre == RT_PRECOND_DIAGONAL) {
+            k_b_recip<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, rD64, rD, 1, a.diag);
+            launch_count(ctx);
+        }
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+    }
+
+    void precondition(const V *r, V *w) {
+        const int pre = a.ctl.preconditioner;
+        if (pre == RT_PRECOND_NONE || pre == RT_PRECOND_DIAGONAL) {
+            k_b_copy<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, vm, r, w, pre == RT_PRECOND_DIAGONAL ? rD : nullptr);
+            launch_count(ctx);
+        } else if (bt.sweep2d) {
+            sweep2d_precondition(ctx, a.nc, vm, r, w);
+        } else {
+            const DevMesh &m = ctx->mesh;
+            for (int l = 0; l < m.nLevels; ++l) {
+                int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
+                k_b_fwd_level<V><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, vm, rD, l32, r,
+                                                                        w);
+            }
+            for (int l = m.nLevels - 1; l >= 0; --l) {
+                int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
+                k_b_bwd_level<V><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, vm, rD, u32, w);
+            }
+            launch_count(ctx, 2 * m.nLevels);
+        }
+        RT_CHECK_LAUNCH();
+    }
+
+    void amul(const V *x, V *y) {
+        k_b_amul<V, V><<<nblocks(N), RT_BLOCK, 0, st>>>(e, vm, d32, u32, l32, x, y);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+    }
+    void dot(const V *x, const V *y, const V *x2 = nullptr, const V *y2 = nullptr) {
+        k_b_dot<V><<<bt.nBlk, RT_BLOCK, 0, st>>>(t, vm, S.active, x, y, x2, y2, partial);
+        RT_CHECK_LAUNCH();
+        fin(x2 ? 2 : 1, vm);
+        launch_count(ctx, 2);
+    }
+    // residual replacement of the segments flagged in S.repl
+    void replace(V *x, V *r) {
+        k_b_fold<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, vm, bt.caseOf.p, S.repl, x, a.psi);
+        k_b_true<V><<<bt.nBlk, RT_BLOCK, 0, st>>>(t, e, vm, S.repl, a.diag, a.upper, a.lower, a.source, a.psi, r,
+                                                  partial);
+        RT_CHECK_LAUNCH();
+        fin(1, vm);
+        launch_count(ctx, 3);
+    }
+
+    // x = 0, r = b - A psi, normFactor, initial residuals, active segments
+    void prologue(V *r, V *x) {
+        double *xs = res + 2 * (size_t)nSeg;   // after the two result slots
+        k_b_sumx<<<bt.nBlk, RT_BLOCK, 0, st>>>(t, vm, a.psi, partial);
+        RT_CHECK_LAUNCH();
+        k_b_fin<<<bt.n, 192, 0, st>>>(1, vm, t, partial, xs);
+        k_b_init_res<V><<<bt.nBlk, RT_BLOCK, 0, st>>>(t, e, vm, a.diag, a.upper, a.lower, a.source, a.psi, xs,
+                                                      bt.cellStartD.p, r, x, partial);
+        RT_CHECK_LAUNCH();
+        fin(2, vm);
+        k_b_start<<<1, 1024, 0, st>>>(bt.n, vm, ctl, S, res);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 5);
+    }
+
+    int poll() {
+        RT_CUDA(cudaMemcpyAsync(bt.hostCount, S.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RT_CUDA(cudaStreamSynchronize(st));
+        return *bt.hostCount;
+    }
+
+    void pcg_iteration(V *r, V *w, V *p, V *q, V *x) {
+        precondition(r, w);
+        if (mixed) dot(w, r, w, q);   // q = A p of the previous iteration (unused on the first)
+        else dot(w, r);
+        k_b_pcg_a<<<gridSeg(), 256, 0, st>>>(nSeg, S, res, mixed);
+        k_b_pcg_p<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, vm, bt.caseOf.p, S, w, p);
+        amul(p, q);
+        dot(q, p);
+        k_b_pcg_alpha<<<gridSeg(), 256, 0, st>>>(nSeg, S, res);
+        k_b_pcg_update<V><<<bt.nBlk, RT_BLOCK, 0, st>>>(t, vm, S, p, q, x, r, partial);
+        RT_CHECK_LAUNCH();
+        fin(1, vm);
+        k_b_iter_fin<<<gridSeg(), 256, 0, st>>>(nSeg, ctl, S, res, 0, mixed);
+        RT_CHECK_LAUNCH();
+        replace(x, r);
+        k_b_after<<<1, 1024, 0, st>>>(bt.n, ctl, S, res);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 7);
+    }
+
+    void bicg_iteration(V *r, V *r0, V *p, V *y, V *Ay, V *s, V *z, V *tt, V *x) {
+        dot(r0, r);
+        k_b_bicg_r0r<<<gridSeg(), 256, 0, st>>>(nSeg, S, res);
+        k_b_bicg_p<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, vm, bt.caseOf.p, S, r, Ay, p);
+        precondition(p, y);
+        amul(y, Ay);
+        dot(r0, Ay);
+        k_b_bicg_alpha<<<gridSeg(), 256, 0, st>>>(nSeg, S, res);
+        k_b_bicg_s<V><<<bt.nBlk, RT_BLOCK, 0, st>>>(t, vm, S, r, Ay, s, partial);
+        RT_CHECK_LAUNCH();
+        fin(1, vm);
+        k_b_bicg_half<<<gridSeg(), 256, 0, st>>>(nSeg, ctl, S, res, mixed);
+        k_b_axpy_half<V><<<nblocks(N), RT_BLOCK, 0, st>>>(N, vm, bt.caseOf.p, S, y, x);
+        RT_CHECK_LAUNCH();
+        replace(x, r);
+        k_b_half_after<<<gridSeg(), 256, 0, st>>>(nSeg, ctl, S, res, mixed);
+        precondition(s, z);
+        amul(z, tt);
+        dot(tt, tt, tt, s);
+        k_b_bicg_omega<<<gridSeg(), 256, 0, st>>>(nSeg, S, res);
+        k_b_bicg_update<V><<<bt.nBlk, RT_BLOCK, 0, st>>>(t, vm, S, y, z, s, tt, x, r, partial);
+        RT_CHECK_LAUNCH();
+        fin(1, vm);
+        k_b_iter_fin<<<gridSeg(), 256, 0, st>>>(nSeg, ctl, S, res, 1, mixed);
+        RT_CHECK_LAUNCH();
+        replace(x, r);
+        k_b_after<<<1, 1024, 0, st>>>(bt.n, ctl, S, res);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 12);
+    }
+};
+
+// iterations between two polls of the active count
+constexpr int kPoll = 4;
+
+template <class V>
+rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    BSolver<V> sv(ctx, a);
+    const bool pcg = a.ctl.solver == RT_SOLVER_PCG;
+    V *x = sv.v(8);
+    V *r = sv.v(0);
+    sv.prepare();
+    sv.prologue(r, x);
+    if (!pcg) RT_CUDA(cudaMemcpyAsync(sv.v(1), r, sizeof(V) * 6 * (size_t)sv.N, cudaMemcpyDeviceToDevice, sv.st));
+    else RT_CUDA(cudaMemsetAsync(sv.v(3), 0, sizeof(V) * 6 * (size_t)sv.N, sv.st));   // q before the first A p
+    int active = sv.poll();
+    // one iteration as a CUDA graph, replayed kPoll times between polls
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto body = [&]() {
+        if (pcg) sv.pcg_iteration(r, sv.v(1), sv.v(2), sv.v(3), x);
+        else sv.bicg_iteration(r, sv.v(1), sv.v(2), sv.v(3), sv.v(4), sv.v(5), sv.v(6), sv.v(7), x);
+    };
+    int done = 0;
+    const int cap = a.ctl.maxIter + 2;
+    if (active) {
+        body();   // first iteration eagerly (sets kernel attributes outside any capture)
+        ++done;
+        active = sv.poll();
+    }
+    if (active) {
+        RT_CUDA(cudaStreamBeginCapture(sv.st, cudaStreamCaptureModeThreadLocal));
+        try {
+            body();
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(sv.st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        RT_CUDA(cudaStreamEndCapture(sv.st, &graph));
+        RT_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    }
+    size_t nodes = 0;
+    if (graph) RT_CUDA(cudaGraphGetNodes(graph, nullptr, &nodes));
+    while (active && done < cap) {
+        for (int i = 0; i < kPoll && done < cap; ++i, ++done) {
+            RT_CUDA(cudaGraphLaunch(exec, sv.st));
+            ctx->kernelLaunches += (long long)nodes;
+        }
+        active = sv.poll();
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    // what is left in x (segments stopped as singular) goes to psi
+    k_b_fold<V><<<nblocks(sv.N), RT_BLOCK, 0, sv.st>>>(sv.N, sv.vm, ctx->mesh.batch.caseOf.p, nullptr, x, a.psi);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    // records of every segment
+    Batch &bt = ctx->mesh.batch;
+    const int nSeg = sv.nSeg;
+    bt.hostSegD.resize((size_t)12 * nSeg);
+    bt.hostSegI.resize((size_t)6 * nSeg + 8);
+    RT_CUDA(cudaMemcpyAsync(bt.hostSegD.data(), bt.segD.p, sizeof(double) * 12 * nSeg, cudaMemcpyDeviceToHost,
+                            sv.st));
+    RT_CUDA(cudaMemcpyAsync(bt.hostSegI.data(), bt.segI.p, sizeof(int) * (6 * nSeg + 8), cudaMemcpyDeviceToHost,
+                            sv.st));
+    RT_CUDA(cudaStreamSynchronize(sv.st));
+    const double *init = bt.hostSegD.data() + (size_t)1 * nSeg, *fin = bt.hostSegD.data() + (size_t)2 * nSeg;
+    const int *iter = bt.hostSegI.data() + (size_t)1 * nSeg, *sing = bt.hostSegI.data() + (size_t)2 * nSeg,
+              *conv = bt.hostSegI.data() + (size_t)5 * nSeg;
+    if ((int)ctx->batchPerf.size() != bt.n) ctx->batchPerf.assign(bt.n, rt_step_perf{});
+    for (int k = 0; k < a.nc; ++k) {
+        rt_solver_perf agg{};
+        agg.converged = 1;
+        if (!((a.validMask >> k) & 1u)) {
+            agg.nIterations = -1;
+            perf[k] = agg;
+            continue;
+        }
+        for (int cb = 0; cb < bt.n; ++cb) {
+            const int sg = cb * 8 + k;
+            rt_solver_perf p{};
+            p.initialResidual = init[sg];
+            p.finalResidual = fin[sg];
+            p.nIterations = iter[sg];
+            p.singular = sing[sg];
+            p.converged = (conv[sg] == 1) ? 1 : 0;
+            agg.initialResidual = std::max(agg.initialResidual, p.initialResidual);
+            agg.finalResidual = std::max(agg.finalResidual, p.finalResidual);
+            agg.nIterations = std::max(agg.nIterations, p.nIterations);
+            agg.singular |= p.singular;
+            agg.converged &= p.converged;
+            rt_step_perf &sp = ctx->batchPerf[cb];
+            if (a.stage == 0 && k < 3) sp.U[k] = p;
+            else if (a.stage == 1 && k == 0) sp.p = p;
+            else if (a.stage == 2) sp.theta[k] = p;
+        }
+        perf[k] = agg;
+    }
+    if (a.stage == 2)
+        for (int cb = 0; cb < bt.n; ++cb)
+            for (int k = 0; k < 6; ++k)
+                if (!((a.validMask >> k) & 1u)) ctx->batchPerf[cb].theta[k] = rt_solver_perf{0, 0, -1, 1, 0, 0};
+    if (a.stage == 0)
+        for (int cb = 0; cb < bt.n; ++cb)
+            for (int k = 0; k < 3; ++k)
+                if (!((a.validMask >> k) & 1u)) ctx->batchPerf[cb].U[k] = rt_solver_perf{0, 0, -1, 1, 0, 0};
+    return sweep2d_check(ctx);
+}
+
+}  // namespace
+
+rt_status batch_solve(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    ProfScope ps(ctx, a.stage == 1 ? "batch_solve_p" : a.stage == 0 ? "batch_solve_U" : "batch_solve_theta");
+    if (a.precision == RT_PREC_MIXED && (ctx->mixedParts & 1)) {
+        SolveArgs t = a;
+        t.ctl.tolerance *= ctx->mixedTighten;
+        t.ctl.relTol *= ctx->mixedTighten;
+        return run_batch<float>(ctx, t, perf);
+    }
+    return run_batch<double>(ctx, a, perf);
+}
+
+}  // namespace rt

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -43,6 +45,12 @@ struct Error {
 // ---------------------------------------------------------------------------
 // device buffers
 // ---------------------------------------------------------------------------
+// bytes of device memory held by every DBuf of the process (admission control)
+inline std::atomic<long long> &device_bytes() {
+    static std::atomic<long long> v{0};
+    return v;
+}
+
 template <class T>
 struct DBuf {
     T *p = nullptr;
@@ -52,7 +60,10 @@ struct DBuf {
     DBuf &operator=(const DBuf &) = delete;
     ~DBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaFree(p);
+            device_bytes() -= (long long)(n * sizeof(T));
+        }
         p = nullptr;
         n = 0;
     }
@@ -66,6 +77,7 @@ struct DBuf {
             throw Error{RT_EOOM, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
         }
         n = count;
+        device_bytes() += (long long)(count * sizeof(T));
     }
     void zero(cudaStream_t s) {
         if (p) RT_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
@@ -81,15 +93,18 @@ constexpr int SYNC_WORK = 0, SYNC_ERROR = 1, SYNC_PROGRESS = 2;
 
 // raw view passed to the kernels; every array has nSkew entries in the
 // skewed (block, step, lane) layout, wS has 6 components of nSkew
-struct SkewView {
+template <class Real>
+struct SkewT {
     int nx, ny, nz, nJB, T;
     long long nSkew;
     const int *cellOf;
-    double *D, *Pz, *Py, *Px, *rDraw;
-    double *rDinv, *Az, *Ay, *Ax, *Bz, *By, *Bx;
-    double *wS;   // 6 components
-    double *rS;   // 6 components
+    Real *D, *Pz, *Py, *Px, *rDraw;   // rD recurrence inputs / output (FP64 only)
+    Real *rDinv, *Az, *Ay, *Ax, *Bz, *By, *Bx;
+    Real *wS;   // 6 components
+    Real *rS;   // 6 components
 };
+using SkewView = SkewT<double>;
+using SkewView32 = SkewT<float>;
 
 struct StructMesh {
     bool on = false;
@@ -98,7 +113,9 @@ struct StructMesh {
     long long nSkew = 0;
     DBuf<int> cellOf;          // nSkew: cell of each skewed entry, -1 outside the mesh
     DBuf<int> faceLo, faceHi;  // 3*N: face to the (z, y, x) lower / upper neighbour, -1 if none
-    DBuf<int> sync;            // work counter, error flag, per-block progress
+    DBuf<int> sync;            // work counter, error flag
+    DBuf<unsigned long long> xfer;   // tagged hand-off words between clusters
+    unsigned epoch = 0;        // tag of the current launch's hand-off words
     DBuf<double> data;         // 12 + 6 + 6 arrays of nSkew doubles
     bool pendingCheck = false;
 
@@ -114,8 +131,66 @@ struct StructMesh {
         v.rS = p + (size_t)18 * nSkew;
         return v;
     }
+
+    // FP32 copies of the sweep coefficients and right-hand sides (mixed
+    // precision): 7 coefficient arrays + 6 + 6 component arrays, allocated
+    // on first use
+    DBuf<float> data32;
+    SkewView32 view32() {
+        if (data32.n != (size_t)19 * nSkew) data32.alloc((size_t)19 * nSkew);
+        SkewView32 v;
+        v.nx = nx; v.ny = ny; v.nz = nz; v.nJB = nJB; v.T = T; v.nSkew = nSkew;
+        v.cellOf = cellOf.p;
+        v.D = v.Pz = v.Py = v.Px = v.rDraw = nullptr;
+        float *p = data32.p;
+        float **slots[] = {&v.rDinv, &v.Az, &v.Ay, &v.Ax, &v.Bz, &v.By, &v.Bx};
+        for (int i = 0; i < 7; ++i) *slots[i] = p + (size_t)i * nSkew;
+        v.wS = p + (size_t)7 * nSkew;
+        v.rS = p + (size_t)13 * nSkew;
+        return v;
+    }
 };
 
+
+// ---------------------------------------------------------------------------
+// batch of independent cases: the uploaded mesh is the disjoint union of the
+// case meshes, case b owning a contiguous range of cells, internal faces and
+// boundary faces.  One case (n = 1, caseOf = nullptr) is the plain context.
+// ---------------------------------------------------------------------------
+struct Batch {
+    int n = 1;
+    std::vector<int> cellStartH, faceStartH, bStartH;   // n + 1 each
+    DBuf<int> caseOf;                 // N: case of each cell (batch only)
+    DBuf<int> cellStartD, faceStartD, bStartD;          // n + 1 each, on the device
+    DBuf<rt_model_params> params;     // n: model of each case
+    DBuf<int> refCell;                // n: pRefCell (global) of each case, -1 without reference
+    DBuf<double> refValue;            // n
+    // reduction blocks aligned to cases: block k covers cells
+    // [blkCell0[k], blkCell0[k] + 256) of case blkCase[k] (clipped)
+    int nBlk = 0;
+    std::vector<int> caseBlkH;        // n + 1: first block of each case
+    DBuf<int> blkCase, blkCell0, blkCell1, caseBlk;
+    // structured 2-D cases: skewed layout for the batched sweeps
+    bool sweep2d = false;
+    int maxJB = 0;
+    long long nSkew = 0;
+    std::vector<int> nxH, nyH;
+    DBuf<int> sx, sy, sT, sJB;        // n: box and layout of each case
+    DBuf<long long> sOff;             // n: first skewed entry of each case
+    DBuf<int> sCell;                  // nSkew: global cell, -1 outside the case mesh
+    DBuf<int> sFaceLo, sFaceHi;       // 2*N: face to the (y, x) lower / upper neighbour
+    DBuf<double> sData64;             // D, Py, Px, rDraw, rDinv, Ay, Ax, By, Bx, wS(6), rS(6)
+    DBuf<float> sData32;              // rDinv, Ay, Ax, By, Bx, wS(6), rS(6)
+    DBuf<int> sErr;                   // bounded-wait error flag of the batched sweeps
+    bool sPending = false;
+    // batched Krylov state: per-segment scalars (segment = case * 8 + component),
+    // case-aligned reduction partials and results
+    DBuf<double> segD, bPartial, bRes;
+    DBuf<int> segI;
+    int *hostCount = nullptr;         // pinned
+    std::vector<double> hostSegD;
+    std::vector<int> hostSegI;
+};
 
 // ---------------------------------------------------------------------------
 // mesh: LDU addressing + geometry + cell-centric adjacency
@@ -153,6 +228,7 @@ struct DevMesh {
     DBuf<int> levelCells;
     // host copies needed by the host-side orchestration
     std::vector<int> patchStartH, patchSizeH;
+    Batch batch;
 };
 
 // ---------------------------------------------------------------------------
@@ -180,6 +256,14 @@ struct Work {
         used += al;
         return p;
     }
+};
+
+// gives back everything taken from the pool in its scope, on every exit path
+struct WorkMark {
+    Work &w;
+    size_t mark;
+    explicit WorkMark(Work &x) : w(x), mark(x.used) {}
+    ~WorkMark() { w.used = mark; }
 };
 
 // reduction buffers
@@ -217,6 +301,11 @@ struct rt_ctx {
     rt::Reduce red;
     rt::Work work;
     rt::DBuf<double> kws;        // Krylov workspace: 8 vectors x 6 comps x N + rD
+    rt::DBuf<float> kws32;       // mixed-precision Krylov: FP32 vectors + FP32 matrix
+    int precision = RT_PREC_FP64;   // of standalone rt_ldu_solve calls
+    int mixedParts = 3;             // RT_PREC_MIXED: 1 FP32 Krylov, 2 FP32 constitutive
+    double mixedTighten = 1e-2;     // RT_PREC_MIXED: solves stop at tolerance x this factor
+    std::vector<rt_step_perf> batchPerf;   // per case: the last step's solver records
     rt::DBuf<double> scal;       // device scalars of the Krylov loops [32 slots][8]
     rt::DBuf<double> stage;      // staging for AoS <-> SoA field transfers
     rt::Prof prof;
@@ -236,6 +325,8 @@ struct SolveArgs {
     int nc;
     unsigned validMask;                   // components to solve
     rt_solver_ctl ctl;
+    int precision = RT_PREC_FP64;         // RT_PREC_MIXED: FP32 iterations, FP64 refinement
+    int stage = -1;                       // batch records: 0 U, 1 p, 2 theta, -1 none
 };
 rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf);
 double residual_device(rt_ctx *ctx, const double *diag, const double *upper,

@@ -75,12 +75,15 @@ void init_fields(rt_ctx *ctx) {
 // ---------------------------------------------------------------------------
 // explicit part of divTau: div(tau/rho) - div(kG grad U) (coupling) or
 // - laplacian(kG, U) (BSD), both Gauss linear
-__global__ void k_divtau_expl(MeshView m, int stab, double rho, double kG,
+__global__ void k_divtau_expl(MeshView m, MomCoef mc0,
                               const double *__restrict__ tau, const double *__restrict__ taub,
                               const double *__restrict__ G, const double *__restrict__ U,
                               const double *__restrict__ Ub, double *__restrict__ expl) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
+    const MomCoef mc = m.caseOf ? mom_coef(m.caseParams[m.caseOf[c]]) : mc0;
+    const int stab = mc.stab;
+    const double rho = mc.rho, kG = mc.kG;
     const int N = m.N, NB = m.NB, F = m.F;
     double dt0 = 0.0, dt1 = 0.0, dt2 = 0.0;     // div(tau/rho) sums
     double dg0 = 0.0, dg1 = 0.0, dg2 = 0.0;     // div(kG grad U) or laplacian sums
@@ -164,22 +167,23 @@ __global__ void k_divtau_expl(MeshView m, int stab, double rho, double kG,
 }
 
 // lower/upper -= gam |Sf| deltaCoeffs (the laplacian subtracted)
-__global__ void k_sub_lap(int F, double gam, const double *__restrict__ magSf, const double *__restrict__ delta,
-                          double *__restrict__ lower, double *__restrict__ upper) {
+__global__ void k_sub_lap(MeshView m, double gam0, double *__restrict__ lower, double *__restrict__ upper) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= F) return;
-    double up = gam * magSf[f] * delta[f];
+    if (f >= m.F) return;
+    const double gam = m.caseOf ? mom_coef(m.caseParams[m.caseOf[m.owner[f]]]).gam : gam0;
+    double up = gam * m.magSf[f] * m.delta[f];
     upper[f] -= up;
     lower[f] -= up;
 }
 
 // UEqn diag and source
-__global__ void k_mom_cell(MeshView m, double rDeltaT, double gam, const double *__restrict__ diagC,
+__global__ void k_mom_cell(MeshView m, double rDeltaT, double gam0, const double *__restrict__ diagC,
                            const double *__restrict__ srcC, const double *__restrict__ U0,
                            const double *__restrict__ expl, double *__restrict__ diag,
                            double *__restrict__ src) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
+    const double gam = m.caseOf ? mom_coef(m.caseParams[m.caseOf[c]]).gam : gam0;
     const int N = m.N;
     double ld = 0.0;
     for (int s = 0; s < m.nSlots; ++s) {
@@ -197,16 +201,17 @@ __global__ void k_mom_cell(MeshView m, double rDeltaT, double gam, const double 
 }
 
 // boundary coefficients of UEqn: convection minus laplacian (fixedValue faces)
-__global__ void k_mom_bnd(int NB, double gam, const int *__restrict__ kU, const double *__restrict__ bmagSf,
-                          const double *__restrict__ bDelta, const double *__restrict__ Ub,
+__global__ void k_mom_bnd(MeshView m, double gam0, const int *__restrict__ kU, const double *__restrict__ Ub,
                           double *__restrict__ intC, double *__restrict__ bouC) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int NB = m.NB;
     if (b >= NB) return;
     if (kU[b] != RT_BC_FIXED) return;
-    double gm = gam * bmagSf[b];
+    const double gam = m.caseOf ? mom_coef(m.caseParams[m.caseOf[m.bCell[b]]]).gam : gam0;
+    double gm = gam * m.bmagSf[b];
     for (int k = 0; k < 3; ++k) {
-        intC[(size_t)k * NB + b] -= gm * (-bDelta[b]);
-        bouC[(size_t)k * NB + b] -= -gm * (bDelta[b] * Ub[(size_t)k * NB + b]);
+        intC[(size_t)k * NB + b] -= gm * (-m.bDelta[b]);
+        bouC[(size_t)k * NB + b] -= -gm * (m.bDelta[b] * Ub[(size_t)k * NB + b]);
     }
 }
 
@@ -303,7 +308,7 @@ __global__ void k_phiHbyA(MeshView m, double rDeltaT, const double *__restrict__
                           const double *__restrict__ U0, const double *__restrict__ phi0,
                           const double *__restrict__ rAU, const double *__restrict__ rAtU,
                           const double *__restrict__ p, double *__restrict__ phiHbyA,
-                          double *partial, int nBlk) {
+                          double *partial, int nBlk, double *__restrict__ absPreF) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     double absPre = 0.0;
     if (f < m.F) {
@@ -322,6 +327,7 @@ __global__ void k_phiHbyA(MeshView m, double rDeltaT, const double *__restrict__
         double ddtCorr = cc * rDeltaT * phiCorr;
         double pre = hf + lin_interp(w, rAU[o], rAU[n]) * ddtCorr;
         absPre = fabs(pre);
+        if (absPreF) absPreF[f] = absPre;
         double dr = lin_interp(w, rAtU[o] - rAU[o], rAtU[n] - rAU[n]);
         phiHbyA[f] = pre + dr * (m.delta[f] * (p[n] - p[o])) * m.magSf[f];
     }
@@ -387,6 +393,42 @@ __global__ void k_adjust_corr_phi(int NB, int nPartial, const int *__restrict__ 
             if (kU[b] != RT_BC_FIXED && phiHbyAb[b] > 0.0) phiHbyAb[b] *= corr;
 }
 
+// adjustCorrPhi of a batch: block b treats case b (cases without a pressure
+// reference are left alone), same sums in the same order as above over the
+// case's own boundary faces and internal faces
+__global__ void k_adjust_corr_phi_batch(const int *__restrict__ refCell, const int *__restrict__ bStart,
+                                        const int *__restrict__ fStart, const int *__restrict__ kU,
+                                        const double *__restrict__ absPreF, double *__restrict__ phiHbyAb,
+                                        int *__restrict__ status) {
+    const int cb = blockIdx.x;
+    if (refCell[cb] < 0) return;
+    const int b0 = bStart[cb], b1 = bStart[cb + 1], f0 = fStart[cb], f1 = fStart[cb + 1];
+    __shared__ double sh[4][RT_BLOCK];
+    double mi = 0.0, fo = 0.0, ao = 0.0, tot = 0.0;
+    for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+        double v = phiHbyAb[b];
+        if (v < 0.0) mi -= v;
+        else if (kU[b] == RT_BC_FIXED) fo += v;
+        else ao += v;
+    }
+    for (int f = f0 + threadIdx.x; f < f1; f += blockDim.x) tot += absPreF[f];
+    sh[0][threadIdx.x] = mi; sh[1][threadIdx.x] = fo; sh[2][threadIdx.x] = ao; sh[3][threadIdx.x] = tot;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    double massIn = sh[0][0], fixedOut = sh[1][0], adjOut = sh[2][0], total = 1e-300 + sh[3][0];
+    double corr = 1.0;
+    bool doCorr = fabs(adjOut) > 1e-300 && fabs(adjOut) / total > 1e-15;
+    if (doCorr) corr = (massIn - fixedOut) / adjOut;
+    else if (fabs(fixedOut - massIn) / total > 1e-8 && threadIdx.x == 0 && status) *status = 1;
+    if (doCorr)
+        for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x)
+            if (kU[b] != RT_BC_FIXED && phiHbyAb[b] > 0.0) phiHbyAb[b] *= corr;
+}
+
 // boundary phiHbyA += (rAtU - rAU)_P snGrad(p) |Sf|
 __global__ void k_phiHbyA_bnd_post(MeshView m, const int *__restrict__ kP, const double *__restrict__ rAU,
                                    const double *__restrict__ rAtU, const double *__restrict__ p,
@@ -440,7 +482,13 @@ __global__ void k_pmat_cell(MeshView m, const double *__restrict__ pu, const dou
     for (int i = m.bStart[c]; i < m.bStart[c + 1]; ++i) dv += phiHbyAb[m.bList[i]];
     double v = m.V[c];
     double ps = 0.0 + v * (dv / v);
-    if (needRef && c == refCell) {
+    if (m.caseOf) {
+        const int b = m.caseOf[c];
+        if (m.refCell[b] == c) {
+            ps += pd * m.refValue[b];
+            pd += pd;
+        }
+    } else if (needRef && c == refCell) {
         ps += pd * refValue;
         pd += pd;
     }
@@ -492,7 +540,7 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     cudaStream_t s = ctx->stream;
     MeshView m = view(mesh);
     Work &W = ctx->work;
-    W.used = 0;
+    WorkMark wmark(W);
     const int gN = nblocks(N), gF = nblocks(F), gB = nblocks(std::max(NB, 1));
 
     // old-time fields
@@ -516,21 +564,15 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
         convection(ctx, ctl.divU, 3, cs.phi.p, cs.phib.p, cs.U.p, cs.Ub.p, cs.bkU.p, G, lower, upper, diagC, srcC,
                    intC, bouC, flux);
     }
-    double gam, kG = 0.0;
-    if (mp.stabilization == RT_STAB_COUPLING || mp.stabilization == RT_STAB_BSD) {
-        gam = (mp.etaP + mp.etaS) / mp.rho;
-        kG = mp.etaP / mp.rho;
-    } else {
-        gam = mp.etaS / mp.rho;
-    }
+    const MomCoef mc = mom_coef(mp);
+    const double gam = mc.gam;
     double *expl = W.take(3 * (size_t)N);
     ProfScope psMom(ctx, "mom_assembly", (double)N * (48.0 + 72.0 + 24.0 + 24.0 + 8.0 + 24.0 + 24.0 + 24.0 + 8.0 + 24.0) + F * 32.0);
-    k_divtau_expl<<<gN, RT_BLOCK, 0, s>>>(m, mp.stabilization, mp.rho, kG, cs.tau.p, cs.taub.p, G, cs.U.p, cs.Ub.p,
-                                          expl);
+    k_divtau_expl<<<gN, RT_BLOCK, 0, s>>>(m, mc, cs.tau.p, cs.taub.p, G, cs.U.p, cs.Ub.p, expl);
     double *diag = W.take(N), *src = W.take(3 * (size_t)N);
     k_mom_cell<<<gN, RT_BLOCK, 0, s>>>(m, rDeltaT, gam, diagC, srcC, U0, expl, diag, src);
-    if (F) k_sub_lap<<<gF, RT_BLOCK, 0, s>>>(F, gam, mesh.magSf.p, mesh.deltaCoeffs.p, lower, upper);
-    if (NB) k_mom_bnd<<<gB, RT_BLOCK, 0, s>>>(NB, gam, cs.bkU.p, mesh.bmagSf.p, mesh.bDelta.p, cs.Ub.p, intC, bouC);
+    if (F) k_sub_lap<<<gF, RT_BLOCK, 0, s>>>(m, gam, lower, upper);
+    if (NB) k_mom_bnd<<<gB, RT_BLOCK, 0, s>>>(m, gam, cs.bkU.p, cs.Ub.p, intC, bouC);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 4);
     double *gp = W.take(3 * (size_t)N);
@@ -542,7 +584,7 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     unsigned maskU = 0;
     for (int k = 0; k < 3; ++k)
         if (mesh.solveDir[k]) maskU |= 1u << k;
-    SolveArgs ua{dS, upper, lower, bS, cs.U.p, 3, maskU, ctl.solverU};
+    SolveArgs ua{dS, upper, lower, bS, cs.U.p, 3, maskU, ctl.solverU, ctl.precision, 0};
     prof_end(ctx, psMom.rec, psMom.bytes);
     psMom.rec = -1;
     rt_status st;
@@ -560,12 +602,22 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     double *HbyAb = W.take(3 * (size_t)NB);
     if (NB) k_HbyA_bnd<<<gB, RT_BLOCK, 0, s>>>(NB, N, cs.bkU.p, mesh.bCell.p, cs.Ub.p, rAU, H, HbyAb);
     double *phiHbyA = W.take(F), *phiHbyAb = W.take(NB);
-    double *partial = ctl.needReference ? W.take(gF + 1) : nullptr;
-    if (F) k_phiHbyA<<<gF, RT_BLOCK, 0, s>>>(m, rDeltaT, HbyA, U0, phi0, rAU, rAtU, cs.p.p, phiHbyA, partial, gF);
+    const bool batched = mesh.batch.n > 1;
+    double *partial = (ctl.needReference && !batched) ? W.take(gF + 1) : nullptr;
+    double *absPreF = batched ? W.take(F + 1) : nullptr;
+    if (F)
+        k_phiHbyA<<<gF, RT_BLOCK, 0, s>>>(m, rDeltaT, HbyA, U0, phi0, rAU, rAtU, cs.p.p, phiHbyA, partial, gF,
+                                          absPreF);
     if (NB) k_phiHbyA_bnd_pre<<<gB, RT_BLOCK, 0, s>>>(m, rDeltaT, cs.bkU.p, HbyAb, U0b, phi0b, rAU, phiHbyAb);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 4);
-    if (ctl.needReference && NB) {
+    if (batched) {
+        const Batch &bt = mesh.batch;
+        k_adjust_corr_phi_batch<<<bt.n, RT_BLOCK, 0, s>>>(bt.refCell.p, bt.bStartD.p, bt.faceStartD.p, cs.bkU.p,
+                                                          absPreF, phiHbyAb, nullptr);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+    } else if (ctl.needReference && NB) {
         k_adjust_corr_phi<<<1, RT_BLOCK, 0, s>>>(NB, F ? gF : 0, cs.bkU.p, partial, phiHbyAb, nullptr);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
@@ -582,7 +634,7 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
                                         ctl.pRefValue, pd, ps);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 3);
-    SolveArgs pa{pd, pu, pu, ps, cs.p.p, 1, 1u, ctl.solverP};
+    SolveArgs pa{pd, pu, pu, ps, cs.p.p, 1, 1u, ctl.solverP, ctl.precision, 1};
     prof_end(ctx, psP.rec, psP.bytes);
     psP.rec = -1;
     rt_status sp;

@@ -5,34 +5,38 @@
 // neighbours are (i,j,k-1), (i,j-1,k), (i-1,j,k) in increasing face order, its
 // upper neighbours (i+1,j,k), (i,j+1,k), (i,j,k+1).  The sequential D-ILU
 // recurrences of OpenFOAM (rD, forward, backward; face-ordered accumulation)
-// are evaluated here in exactly that order of operations, so the result equals
-// the level-scheduled sweep bit for bit (and the sequential sweep up to FMA
-// contraction).
+// are evaluated here in exactly that order of operations, so the FP64 result
+// equals the level-scheduled sweep bit for bit (and the sequential sweep up to
+// FMA contraction).  The same kernel runs in FP32 for the mixed-precision
+// solvers (coefficients rounded from the FP64 factorisation).
 //
 // Work decomposition: rows (j,k) are grouped in blocks of 32 consecutive j in
 // one plane k.  A warp owns a block; at step t lane l updates cell i = t - l of
 // row j = 32 jb + l.  The i-1 value is the lane's own previous result
 // (register) and the j-1 value lane l-1's previous result (shuffle).  Lane 0
 // reads j-1 from the j-block below (step t + 31) and every lane reads k-1 from
-// the block of the previous plane (same step): those come through memory
-// behind progress counters.  The steps are taken in chunks of P: a chunk
-// waits once, issues all its loads at once (one memory latency per chunk) and
-// publishes once.
+// the block of the previous plane (same step).  The steps are taken in chunks
+// of P: a chunk waits once, reads its staged coefficients and publishes once.
 //
-// A CTA owns KC consecutive planes with all their j-blocks; waits inside the
-// CTA use shared-memory counters and block-scope fences, only the first plane
-// of a CTA waits on the previous CTA's last plane through a global counter
-// (release / acquire).  CTAs take plane groups in dependency order from an
-// atomic counter, so a CTA only waits on groups owned by running CTAs: no
-// deadlock.  Every wait is bounded; a timeout sets an error flag, marks the
-// block finished and the host reports RT_ETIMEOUT.
+// One CTA owns one plane (warp = j-block); a thread-block cluster owns CS
+// consecutive planes.  Values handed to another warp (plane to plane through
+// distributed shared memory, j-block to j-block through shared memory,
+// cluster to cluster through global memory) travel as tagged 64-bit words, so
+// a consumer waits on the data itself and no fence or release/acquire pair
+// sits on the dependency chain.  Clusters take plane groups in dependency
+// order from an atomic counter, so a cluster only waits on groups owned by
+// running clusters: no deadlock.  Every wait is bounded; a timeout sets an
+// error flag, every other wait gives up on seeing it, and the host reports
+// RT_ETIMEOUT.
 //
 // Per-entry data live in a "skewed" layout, entry (block, step, lane), so the
-// 32 lanes of a step touch 32 consecutive doubles.  The backward sweep walks
+// 32 lanes of a step touch 32 consecutive values.  The backward sweep walks
 // the same layout in reverse (lanes mirrored).
-#include <cooperative_groups.h>
-#include <cuda/atomic>
+#include <algorithm>
 
+#include <cooperative_groups.h>
+
+#include "real_ops.cuh"
 #include "rt_internal.h"
 #include "sweep.h"
 
@@ -40,25 +44,80 @@ namespace rt {
 
 namespace cg = cooperative_groups;
 
-namespace {
+// ---- tagged hand-off words ------------------------------------------------
+// A value handed to another warp travels with the step it belongs to, packed
+// into one 64-bit word (32-bit payload in the low half, 32-bit tag in the
+// high half) that is written and read with single-copy-atomic 64-bit
+// accesses: a reader sees either the old word (wrong tag) or the new one
+// (value and tag together), so no fence, release or acquire is needed.  An
+// FP64 value travels as two words (its high and low halves), each tagged.
+// Ring slots inside a launch carry tag = step + 1 (the rings are cleared at
+// launch); the global hand-off between clusters carries the launch's epoch,
+// so words left by an earlier launch never match.
+typedef unsigned long long u64;
+template <class Real> struct Words;
+template <> struct Words<float> { static constexpr int W = 1; };
+template <> struct Words<double> { static constexpr int W = 2; };
 
-__device__ __forceinline__ int load_acquire(const int *p) {
-    cuda::atomic_ref<int, cuda::thread_scope_device> a(*const_cast<int *>(p));
-    return a.load(cuda::memory_order_acquire);
+__device__ __forceinline__ void put_word(volatile u64 *p, unsigned payload, unsigned tag) {
+    *p = ((u64)tag << 32) | (u64)payload;
 }
-__device__ __forceinline__ void store_release(int *p, int v) {
-    cuda::atomic_ref<int, cuda::thread_scope_device> a(*p);
-    a.store(v, cuda::memory_order_release);
+__device__ __forceinline__ void put(volatile u64 *p, float v, unsigned tag) { put_word(p, __float_as_uint(v), tag); }
+__device__ __forceinline__ void put(volatile u64 *p, double v, unsigned tag) {
+    put_word(p, (unsigned)__double2hiint(v), tag);
+    put_word(p + 1, (unsigned)__double2loint(v), tag);
 }
-__device__ __forceinline__ void pf_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ bool get(const volatile u64 *p, unsigned tag, float &v) {
+    const u64 a = *p;
+    if ((unsigned)(a >> 32) != tag) return false;
+    v = __uint_as_float((unsigned)a);
+    return true;
+}
+__device__ __forceinline__ bool get(const volatile u64 *p, unsigned tag, double &v) {
+    const u64 a = p[0], b = p[1];
+    if ((unsigned)(a >> 32) != tag || (unsigned)(b >> 32) != tag) return false;
+    v = __hiloint2double((int)(unsigned)a, (int)(unsigned)b);
+    return true;
+}
 
-// lane 0 spins on a shared counter (bounded); returns the value seen, or
-// -1 after a timeout (error flag set)
-__device__ __forceinline__ int spin_shared(volatile int *c, int need, int *sync, long long maxSpin) {
+__device__ __forceinline__ bool unpack(const u64 *w, unsigned tag, float &v) {
+    if ((unsigned)(w[0] >> 32) != tag) return false;
+    v = __uint_as_float((unsigned)w[0]);
+    return true;
+}
+__device__ __forceinline__ bool unpack(const u64 *w, unsigned tag, double &v) {
+    if ((unsigned)(w[0] >> 32) != tag || (unsigned)(w[1] >> 32) != tag) return false;
+    v = __hiloint2double((int)(unsigned)w[0], (int)(unsigned)w[1]);
+    return true;
+}
+
+// prefetch bytes (a multiple of 16, 16-byte aligned) into L2
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// bounded wait of one lane for a tagged value; false after a timeout or when
+// another warp has failed (the error flag is then set)
+template <class Real>
+__device__ __forceinline__ bool wait_get(const volatile u64 *p, unsigned tag, Real &v, int *sync, long long maxSpin,
+                                         bool sleep) {
+    long long spins = 0;
+    while (!get(p, tag, v)) {
+        if ((++spins & 63) == 0 && (spins > maxSpin || *(volatile int *)(sync + SYNC_ERROR))) {
+            atomicExch(sync + SYNC_ERROR, 1);
+            return false;
+        }
+        if (sleep) __nanosleep(64);
+    }
+    return true;
+}
+
+// bounded wait of lane 0 on a progress counter; -1 after a timeout
+__device__ __forceinline__ int wait_count(const volatile int *c, int need, int *sync, long long maxSpin) {
     long long spins = 0;
     int v = *c;
     while (v < need) {
-        if ((++spins & 1023) == 0 && (spins > maxSpin || load_acquire(sync + SYNC_ERROR))) {
+        if ((++spins & 255) == 0 && (spins > maxSpin || *(volatile int *)(sync + SYNC_ERROR))) {
             atomicExch(sync + SYNC_ERROR, 1);
             return -1;
         }
@@ -67,180 +126,137 @@ __device__ __forceinline__ int spin_shared(volatile int *c, int need, int *sync,
     return v;
 }
 
-__device__ __forceinline__ int spin_global(const int *c, int need, int *sync, long long maxSpin) {
-    long long spins = 0;
-    int v = load_acquire(c);
-    while (v < need) {
-        if (++spins > maxSpin || load_acquire(sync + SYNC_ERROR)) {
-            atomicExch(sync + SYNC_ERROR, 1);
-            return -1;
-        }
-        if (spins > 16) __nanosleep(32);
-        v = load_acquire(c);
-    }
-    return v;
-}
-
-}  // namespace
-
-__device__ __forceinline__ int ld_acquire_cluster(const int *p) {
-    int v;
-    asm volatile("ld.acquire.cluster.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_cluster(int *p, int v) {
-    asm volatile("st.release.cluster.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ void fence_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
-
-// bounded spin of lane 0 on a counter of this CTA's shared memory that other
-// CTAs of the cluster (or warps of this CTA) advance; -1 after a timeout
-__device__ __forceinline__ int spin_cluster(const int *c, int need, int *sync, long long maxSpin) {
-    long long spins = 0;
-    int v = ld_acquire_cluster(c);
-    while (v < need) {
-        if ((++spins & 255) == 0 && (spins > maxSpin || load_acquire(sync + SYNC_ERROR))) {
-            atomicExch(sync + SYNC_ERROR, 1);
-            return -1;
-        }
-        v = ld_acquire_cluster(c);
-    }
-    return v;
-}
-
-// Ring depths (steps) of the hand-offs for chunk size P.
+// Ring depths (steps, powers of two) of the hand-offs for chunk size P.
 template <int P> struct Ring {
-    static constexpr int R = (P >= 8) ? 2 * P : (P >= 4) ? 4 * P : 4;   // plane ring, at least two chunks
-    static constexpr int RJ = (P >= 8) ? 128 : 64;    // j-block ring (power of two): the consumer lags ~32 + P steps
+    static constexpr int R = (P >= 4) ? 16 : 8;       // plane ring: at least two chunks
+    static constexpr int RJ = (P >= 8) ? 128 : 64;    // j-block ring: the consumer lags ~32 + P steps
 };
 
-// Per-warp staging of a chunk's coefficients (cp.async, two buffers): NA
-// double arrays of P steps x 32 lanes, plus the cells of the backward sweep.
+// Per-warp staging of a chunk's coefficients (cp.async, three buffers): NA
+// arrays of P steps x 32 lanes, plus the cells of the backward sweep.
 template <int MODE, int NC> struct Stage { static constexpr int NA = 4 + NC; };
 
 constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per CTA on sm_100-class parts
+constexpr int kPre = 8;                   // L2 prefetch distance (chunks)
 
-template <int MODE, int NC, int P>
+template <class Real, int MODE, int NC, int P>
 size_t sweep_smem_bytes(int nJB) {
-    const size_t rings = (size_t)nJB * (Ring<P>::R * 32 * NC + Ring<P>::RJ * NC) * sizeof(double);
-    const size_t stage = (size_t)nJB * 3 * P * 32 * (Stage<MODE, NC>::NA * sizeof(double) + sizeof(int));
+    constexpr int VW = NC * Words<Real>::W;
+    const size_t rings = (size_t)nJB * (Ring<P>::R * 32 + Ring<P>::RJ) * VW * sizeof(u64);
+    const size_t stage = (size_t)nJB * 3 * P * 32 * (Stage<MODE, NC>::NA * sizeof(Real) + sizeof(int));
     return rings + stage;
 }
 
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
-                 "l"(gmem));
-}
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
-                 "l"(gmem));
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem), "n"(BYTES));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// MODE 0: forward application, 1: backward application, 2: rD recurrence.
+// MODE 0: forward application, 1: backward application, 2: rD recurrence
+// (FP64 only).
 //
-// One CTA owns one plane (all its j-blocks, warp = j-block); a thread-block
-// cluster owns CS consecutive planes in processing order, CTA rank r holding
-// the r-th.  The plane-to-plane values move through distributed shared
-// memory: the producer CTA stores each step's 32 lanes straight into the
-// consumer CTA's ring and advances the consumer's counter with a
-// cluster-scope release; the consumer reports its own progress back into the
-// producer's memory, which bounds how far the producer may run ahead (so a
-// ring slot is never overwritten before it is read, and the two waits can
-// never close a cycle).  The j-block hand-off stays inside the CTA (lane 31 of
-// the block below, through a shared ring).  The first plane of a cluster reads
-// the previous cluster's last plane from the global skewed array wS behind a
-// global release/acquire counter.  Clusters take plane groups in dependency
-// order from an atomic counter; all CTAs of a cluster are co-scheduled, and
-// none leaves before the final cluster barrier, so no CTA ever accesses the
-// shared memory of a CTA that has exited.
+// The producer CTA of a plane writes each step's 32 lanes, tagged, straight
+// into the consumer CTA's ring (distributed shared memory); each consumer lane
+// waits on its own slot.  The consumer reports its progress back into the
+// producer's shared memory after each chunk, which bounds how far the
+// producer may run ahead (so a slot is never overwritten before it is read;
+// the two waits can never close a cycle).  The j-block hand-off stays inside
+// the CTA (lane 31 of the block below, through a tagged shared ring).  The
+// first plane of a cluster reads the previous cluster's last plane from a
+// tagged global array (one entry per boundary, block, step and lane, written
+// once per launch).  All CTAs of a cluster are co-scheduled, and none leaves
+// before the final cluster barrier, so no CTA ever touches the shared memory
+// of a CTA that has exited.
 //
 // Latency: a chunk's coefficients are staged into shared memory with cp.async
-// one chunk ahead, and a chunk's global stores are issued one chunk late, so
-// the releases never wait for stores in flight.  The remaining per-step cost
-// is the dependent FP64 chain (one multiply and three fused multiply-adds on
-// a pipe that retires about two FP64 lanes per cycle per SM).
-// Invalid entries (outside the mesh, padding) have zero coefficients and zero
-// right-hand sides, so every lane runs the same branch-free recurrence.
-template <int MODE, int NC, int P>
-__global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, double *__restrict__ w, int N,
-                                                  int *sync, long long maxSpin) {
-    constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA;
+// two chunks ahead; the terms of a step that do not depend on the previous
+// step are formed for the whole chunk first, so only the j and i terms stay
+// on the dependent chain.  Invalid entries (outside the mesh, padding) have
+// zero coefficients and zero right-hand sides, so every lane runs the same
+// branch-free recurrence.
+template <class Real, int MODE, int NC, int P>
+__global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
+                                                  int *sync, u64 *__restrict__ xfer, unsigned epoch,
+                                                  long long maxSpin) {
+    constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA, W = Words<Real>::W;
+    constexpr int VW = NC * W;   // words per (step, lane)
     cg::cluster_group cluster = cg::this_cluster();
     const int CS = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
-    extern __shared__ double smem[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_grp;
-    __shared__ int kIn[16], kBack[16], sProg[16];
+    __shared__ int kBack[16], jProg[16];
     const int lane = threadIdx.x & 31, jo = threadIdx.x >> 5;
     const int nJB = g.nJB;
-    double *ringK = smem;                                   // [nJB][R][32][NC], filled by the k-producer
-    double *ringJ = ringK + (size_t)nJB * R * 32 * NC;      // [nJB][RJ][NC]
-    double *stage = ringJ + (size_t)nJB * RJ * NC;          // [nJB][3][P][NA][32]
-    int *cstage = (int *)(stage + (size_t)nJB * 3 * P * NA * 32);   // [nJB][3][P][32]
-    double *myStage = stage + (size_t)jo * 3 * P * NA * 32;
+    u64 *ringK = reinterpret_cast<u64 *>(smem_raw);                 // [nJB][R][32][VW], written by the k-producer
+    u64 *ringJ = ringK + (size_t)nJB * R * 32 * VW;                  // [nJB][RJ][VW]
+    Real *stage = reinterpret_cast<Real *>(ringJ + (size_t)nJB * RJ * VW);   // [nJB][3][P][NA][32]
+    int *cstage = (int *)(stage + (size_t)nJB * 3 * P * NA * 32);    // [nJB][3][P][32]
+    Real *myStage = stage + (size_t)jo * 3 * P * NA * 32;
     int *myCStage = cstage + (size_t)jo * 3 * P * 32;
-    if (threadIdx.x < 16) { kIn[threadIdx.x] = 0; kBack[threadIdx.x] = 0; sProg[threadIdx.x] = 0; }
+    for (size_t i = threadIdx.x; i < (size_t)nJB * (R * 32 + RJ) * VW; i += blockDim.x) ringK[i] = 0ull;
+    if (threadIdx.x < 16) { kBack[threadIdx.x] = 0; jProg[threadIdx.x] = 0; }
     if (r == 0 && threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
     cluster.sync();
     const int grp = *cluster.map_shared_rank(&s_grp, 0);
     const int nGroups = (g.nz + CS - 1) / CS;
     const int T = g.T;
-    int *gprog = sync + SYNC_PROGRESS;
     const int gi = (MODE == 1) ? nGroups - 1 - grp : grp;
     const int k = (MODE == 1) ? gi * CS + (CS - 1 - r) : gi * CS + r;
     const bool exists = grp < nGroups && k >= 0 && k < g.nz;
     if (exists) {
         const int jb = (MODE == 1) ? nJB - 1 - jo : jo;
-        const int blk = k * nJB + jb;
         const long long BS = (long long)T * 32;
-        const long long KS = (long long)nJB * BS;
+        const int blk = k * nJB + jb;
         const bool hasK = (MODE == 1) ? (k + 1 < g.nz) : (k > 0);
         const bool kLocalProd = hasK && r > 0;
-        const int kGlob = (hasK && r == 0) ? ((MODE == 1) ? k + 1 : k - 1) * nJB + jb : -1;
+        const bool kGlob = hasK && r == 0;
         const bool consExists = (MODE == 1) ? (k - 1 >= 0) : (k + 1 < g.nz);
         const bool kLocalCons = consExists && r + 1 < CS;
         const bool crossProducer = consExists && r == CS - 1;
+        // cluster boundaries: b separates plane groups b and b + 1
+        const int bIn = (MODE == 1) ? gi : gi - 1, bOut = (MODE == 1) ? gi - 1 : gi;
         const int depJ = (jo > 0) ? jo - 1 : -1;
         const int consJ = (jo + 1 < nJB) ? jo + 1 : -1;
-        double *consRing = kLocalCons ? cluster.map_shared_rank(ringK, r + 1) : nullptr;
-        int *consKin = kLocalCons ? cluster.map_shared_rank(kIn, r + 1) : nullptr;
+        u64 *consRing = kLocalCons ? cluster.map_shared_rank(ringK, r + 1) : nullptr;
         int *prodBack = kLocalProd ? cluster.map_shared_rank(kBack, r - 1) : nullptr;
         // entry of step t: e0 + t * st
         const long long e0 = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 + (31 - lane)
                                          : (long long)blk * BS + lane;
         const long long st = (MODE == 1) ? -32 : 32;
-        // stage the coefficients of the chunk starting at step c0 into buffer b
+        auto xslot = [&](int b, int t, int q) -> u64 * {
+            return xfer + ((((size_t)b * nJB + jb) * T + t) * 32 + lane) * VW + q * W;
+        };
+        constexpr int RB = (int)sizeof(Real);
+        // stage the coefficients of the chunk starting at step tc into buffer b
         auto stage_chunk = [&](int tc, int b) {
 #pragma unroll
             for (int s = 0; s < P; ++s) {
                 const long long e = e0 + (tc + s) * st;
-                double *d = myStage + ((size_t)(b * P + s) * NA) * 32 + lane;
+                Real *d = myStage + ((size_t)(b * P + s) * NA) * 32 + lane;
                 if (MODE == 2) {
-                    cp_async8(d + 0 * 32, g.D + e); cp_async8(d + 1 * 32, g.Pz + e);
-                    cp_async8(d + 2 * 32, g.Py + e); cp_async8(d + 3 * 32, g.Px + e);
+                    cp_async<RB>(d + 0 * 32, g.D + e); cp_async<RB>(d + 1 * 32, g.Pz + e);
+                    cp_async<RB>(d + 2 * 32, g.Py + e); cp_async<RB>(d + 3 * 32, g.Px + e);
                 } else {
-                    cp_async8(d + 0 * 32, (MODE == 0 ? g.Az : g.Bz) + e);
-                    cp_async8(d + 1 * 32, (MODE == 0 ? g.Ay : g.By) + e);
-                    cp_async8(d + 2 * 32, (MODE == 0 ? g.Ax : g.Bx) + e);
-                    if (MODE == 0) cp_async8(d + 3 * 32, g.rDinv + e);
+                    cp_async<RB>(d + 0 * 32, (MODE == 0 ? g.Az : g.Bz) + e);
+                    cp_async<RB>(d + 1 * 32, (MODE == 0 ? g.Ay : g.By) + e);
+                    cp_async<RB>(d + 2 * 32, (MODE == 0 ? g.Ax : g.Bx) + e);
+                    if (MODE == 0) cp_async<RB>(d + 3 * 32, g.rDinv + e);
 #pragma unroll
                     for (int q = 0; q < NC; ++q)
-                        cp_async8(d + (4 + q) * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + e);
-                    if (MODE == 1) cp_async4(myCStage + (b * P + s) * 32 + lane, g.cellOf + e);
+                        cp_async<RB>(d + (4 + q) * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + e);
+                    if (MODE == 1) cp_async<4>(myCStage + (b * P + s) * 32 + lane, g.cellOf + e);
                 }
             }
         };
-        int seenK = 0, seenJ = 0, seenCK = 0, seenCJ = 0, fail = 0;
-        double yprev[NC];
+        int seenCK = 0, seenCJ = 0, fail = 0;
+        Real yprev[NC];
 #pragma unroll
-        for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? 1.0 : 0.0;
-        double prevOut[P][NC];
-        int prevCell[P];
-        int prevT0 = -1;
-        // three staging buffers: chunk c is staged two chunks ahead, right
-        // after the release of chunk c - 2, so no release waits for it
+        for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? Real(1) : Real(0);
+        // three staging buffers: chunk c is staged two chunks ahead
         stage_chunk(0, 0);
         cp_async_commit();
         if (P < T) stage_chunk(P, 1);
@@ -253,167 +269,173 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
             // ---- back-pressure: consumers have read what this chunk overwrites
             if (kLocalCons && seenCK < te - R) {
                 int v = 0;
-                if (lane == 0) v = spin_cluster(kBack + jo, te - R, sync, maxSpin);
+                if (lane == 0) v = wait_count(kBack + jo, te - R, sync, maxSpin);
                 v = __shfl_sync(0xffffffffu, v, 0);
                 if (v < 0) { fail = 1; break; }
                 seenCK = v;
             }
             if (consJ >= 0 && seenCJ < te - RJ - 31) {
                 int v = 0;
-                if (lane == 0) v = spin_cluster(sProg + consJ, te - RJ - 31, sync, maxSpin);
+                if (lane == 0) v = wait_count(jProg + consJ, te - RJ - 31, sync, maxSpin);
                 v = __shfl_sync(0xffffffffu, v, 0);
                 if (v < 0) { fail = 1; break; }
                 seenCJ = v;
             }
-            // ---- dependencies: previous plane through te, j-block below through te + 31
-            if (hasK && seenK < te) {
-                int v = 0;
-                if (lane == 0)
-                    v = kLocalProd ? spin_cluster(kIn + jo, te, sync, maxSpin)
-                                   : spin_global(gprog + kGlob, te, sync, maxSpin >> 6);
-                v = __shfl_sync(0xffffffffu, v, 0);
-                if (v < 0) { fail = 1; break; }
-                seenK = v;
+            // ---- L2 prefetch of the chunk kPre chunks ahead (one lane, one
+            // contiguous range per array)
+            if (lane == 0 && t0 + kPre * P < T) {
+                const int tp = t0 + kPre * P;
+                const long long lo = (MODE == 1) ? e0 - 31 + (long long)(tp + P - 1) * st : e0 + (long long)tp * st;
+                const unsigned bytes = (unsigned)(P * 32 * sizeof(Real));
+                if (MODE == 2) {
+                    prefetch_l2(g.D + lo, bytes); prefetch_l2(g.Pz + lo, bytes);
+                    prefetch_l2(g.Py + lo, bytes); prefetch_l2(g.Px + lo, bytes);
+                } else {
+                    prefetch_l2((MODE == 0 ? g.Az : g.Bz) + lo, bytes);
+                    prefetch_l2((MODE == 0 ? g.Ay : g.By) + lo, bytes);
+                    prefetch_l2((MODE == 0 ? g.Ax : g.Bx) + lo, bytes);
+                    if (MODE == 0) prefetch_l2(g.rDinv + lo, bytes);
+#pragma unroll
+                    for (int q = 0; q < NC; ++q)
+                        prefetch_l2((MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo, bytes);
+                    if (MODE == 1) prefetch_l2(g.cellOf + lo, (unsigned)(P * 32 * sizeof(int)));
+                }
             }
-            if (depJ >= 0 && seenJ < min(T, te + 31)) {
-                int v = 0;
-                if (lane == 0) v = spin_cluster(sProg + depJ, min(T, te + 31), sync, maxSpin);
-                v = __shfl_sync(0xffffffffu, v, 0);
-                if (v < 0) { fail = 1; break; }
-                seenJ = v;
+            // ---- the hand-off values of the chunk: every load is issued
+            // first, then the tags are checked (a word not there yet is waited for)
+            Real wkv[P][NC], wjv[P][NC];
+            bool ok = true;
+            const Real zk = (MODE == 2) ? Real(1) : Real(0);
+            if (kLocalProd || kGlob) {
+                u64 kw[P][VW];
+#pragma unroll
+                for (int s = 0; s < P; ++s) {
+                    const volatile u64 *src = kLocalProd
+                        ? ringK + (((size_t)jo * R + ((t0 + s) & (R - 1))) * 32 + lane) * VW
+                        : xslot(bIn, t0 + s, 0);
+#pragma unroll
+                    for (int j = 0; j < VW; ++j) kw[s][j] = src[j];
+                }
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) {
+                        const unsigned tag = kLocalProd ? (unsigned)(t0 + s + 1) : epoch;
+                        if (!unpack(&kw[s][q * W], tag, wkv[s][q])) {
+                            const volatile u64 *src = kLocalProd
+                                ? ringK + (((size_t)jo * R + ((t0 + s) & (R - 1))) * 32 + lane) * VW + q * W
+                                : xslot(bIn, t0 + s, q);
+                            ok &= wait_get(src, tag, wkv[s][q], sync, kLocalProd ? maxSpin : maxSpin >> 4, kGlob);
+                        }
+                    }
+            } else {
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) wkv[s][q] = zk;
             }
-            // (lane 0's acquire loads + the warp-wide shuffle order the ring
-            // reads below after the producers' releases)
-            // ---- the recurrence (order of operations of the sequential sweep)
-            double out[P][NC];
+#pragma unroll
+            for (int s = 0; s < P; ++s)
+#pragma unroll
+                for (int q = 0; q < NC; ++q) wjv[s][q] = zk;
+            if (depJ >= 0 && lane == 0) {
+                u64 jw[P][VW];
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int j = 0; j < VW; ++j)
+                        jw[s][j] = (t0 + s + 31 < T) ? ringJ[((size_t)depJ * RJ + ((t0 + s + 31) & (RJ - 1))) * VW + j]
+                                                     : 0ull;
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+                    if (t0 + s + 31 < T)
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            if (!unpack(&jw[s][q * W], (unsigned)(t0 + s + 32), wjv[s][q]))
+                                ok &= wait_get(ringJ + ((size_t)depJ * RJ + ((t0 + s + 31) & (RJ - 1))) * VW + q * W,
+                                               (unsigned)(t0 + s + 32), wjv[s][q], sync, maxSpin, false);
+            }
+            // ---- the terms that do not depend on the previous step
+            Real out[P][NC];
             int cell[P];
-            // the terms of a step that do not depend on the previous step (the
-            // right-hand side and the k neighbour) are formed for the whole
-            // chunk first, so only the j and i terms stay on the dependent chain
-            double pre[P][NC], wjv[P][NC], cy[P], cx[P];
+            Real pre[P][NC], cy[P], cx[P];
 #pragma unroll
             for (int s = 0; s < P; ++s) {
-                const int t = t0 + s;
-                const double *d = myStage + ((size_t)(buf * P + s) * NA) * 32 + lane;
-                // staged arrays: MODE 2: D, Pz, Py, Px; MODE 0/1: z, y, x
-                // coefficients, then (MODE 0) 1/rD, then the right-hand sides
-                const double c0 = d[0], c3 = (MODE == 0) ? d[96] : 0.0;
+                const Real *d = myStage + ((size_t)(buf * P + s) * NA) * 32 + lane;
+                const Real c0 = d[0], c3 = (MODE == 0) ? d[96] : Real(0);
                 cy[s] = (MODE == 2) ? d[64] : d[32];
                 cx[s] = (MODE == 2) ? d[96] : d[64];
                 cell[s] = (MODE == 1) ? myCStage[(buf * P + s) * 32 + lane] : 0;
-                const double zk = (MODE == 2) ? 1.0 : 0.0;
 #pragma unroll
                 for (int q = 0; q < NC; ++q) {
-                    double wk;
-                    if (kLocalProd) wk = ringK[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q];
-                    else if (kGlob >= 0) {
-                        const long long e = e0 + t * st;
-                        const double *kv = (MODE == 2) ? g.rDraw : g.wS + (long long)q * g.nSkew;
-                        wk = __ldcg(kv + ((MODE == 1) ? e + KS : e - KS));
-                    } else wk = zk;
-                    wjv[s][q] = (depJ >= 0 && t + 31 < T)
-                                    ? ringJ[((size_t)depJ * RJ + ((t + 31) & (RJ - 1))) * NC + q] : zk;
+                    const Real wk = wkv[s][q];
                     if (MODE == 2) {
-                        pre[s][q] = __dsub_rn(c0, __ddiv_rn(d[32], wk));   // D - Pz / rD(k-1)
+                        pre[s][q] = r_sub(c0, r_div(d[32], wk));   // D - Pz / rD(k-1)
                     } else {
-                        const double rk = d[(4 + q) * 32];
-                        const double v0 = (MODE == 0) ? __dmul_rn(c3, rk) : rk;
-                        pre[s][q] = __fma_rn(-c0, wk, v0);
+                        const Real rk = d[(4 + q) * 32];
+                        const Real v0 = (MODE == 0) ? r_mul(c3, rk) : rk;
+                        pre[s][q] = r_fma(-c0, wk, v0);
                     }
                 }
             }
+            if (__any_sync(0xffffffffu, !ok)) { fail = 1; break; }
+            // ---- the recurrence (order of operations of the sequential sweep)
 #pragma unroll
             for (int s = 0; s < P; ++s) {
                 const int t = t0 + s;
 #pragma unroll
                 for (int q = 0; q < NC; ++q) {
-                    const double yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
-                    const double yj = (lane > 0) ? yup : wjv[s][q];
-                    double v;
+                    const Real yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
+                    const Real yj = (lane > 0) ? yup : wjv[s][q];
+                    Real v;
                     if (MODE == 2) {
-                        v = __dsub_rn(pre[s][q], __ddiv_rn(cy[s], yj));
-                        v = __dsub_rn(v, __ddiv_rn(cx[s], yprev[q]));
+                        v = r_sub(pre[s][q], r_div(cy[s], yj));
+                        v = r_sub(v, r_div(cx[s], yprev[q]));
                     } else {
-                        v = __fma_rn(-cy[s], yj, pre[s][q]);
-                        v = __fma_rn(-cx[s], yprev[q], v);
+                        v = r_fma(-cy[s], yj, pre[s][q]);
+                        v = r_fma(-cx[s], yprev[q], v);
                     }
-                    if (kLocalCons) consRing[(((size_t)jo * R + (t & (R - 1))) * 32 + lane) * NC + q] = v;
-                    if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * RJ + (t & (RJ - 1))) * NC + q] = v;
+                    if (kLocalCons)
+                        put(consRing + (((size_t)jo * R + (t & (R - 1))) * 32 + lane) * VW + q * W, v,
+                            (unsigned)(t + 1));
+                    if (consJ >= 0 && lane == 31)
+                        put(ringJ + ((size_t)jo * RJ + (t & (RJ - 1))) * VW + q * W, v, (unsigned)(t + 1));
+                    if (crossProducer) put(xslot(bOut, t, q), v, epoch);
                     out[s][q] = v;
                     yprev[q] = v;
                 }
             }
-            // ---- publish the shared-memory hand-offs: the warp barrier orders
-            // every lane's ring stores before lane 0's cluster-scope release
+            // ---- progress for the producers' back-pressure (after every lane
+            // has consumed its hand-off values of this chunk)
             __syncwarp();
             if (lane == 0) {
-                if (consJ >= 0 || depJ >= 0) st_release_cluster(sProg + jo, te);
-                if (kLocalCons) st_release_cluster(consKin + jo, te);
-                if (kLocalProd) st_release_cluster(prodBack + jo, te);
+                if (kLocalProd) *(volatile int *)(prodBack + jo) = te;
+                if (depJ >= 0) *(volatile int *)(jProg + jo) = te;
             }
             // ---- stage chunk c + 2 (always commit a group, possibly empty)
             if (te + P < T) stage_chunk(te + P, ((t0 / P) + 2) % 3);
             cp_async_commit();
-            // ---- the previous chunk's global stores (one chunk late)
-            if (prevT0 >= 0) {
-#pragma unroll
-                for (int s = 0; s < P; ++s) {
-                    const long long e = e0 + (prevT0 + s) * st;
-                    if (MODE == 2) {
-                        g.rDraw[e] = prevOut[s][0];
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < NC; ++q) {
-                            if (!((mask >> q) & 1u)) continue;
-                            g.wS[(long long)q * g.nSkew + e] = prevOut[s][q];
-                            if (MODE == 1 && prevCell[s] >= 0) w[(long long)q * N + prevCell[s]] = prevOut[s][q];
-                        }
-                    }
-                }
-                if (crossProducer && ((t0 % (2 * P)) == 0)) {
-                    __threadfence();
-                    __syncwarp();
-                    if (lane == 0) store_release(gprog + blk, t0);
-                }
-            }
+            // ---- this chunk's results
 #pragma unroll
             for (int s = 0; s < P; ++s) {
-                prevCell[s] = cell[s];
-#pragma unroll
-                for (int q = 0; q < NC; ++q) prevOut[s][q] = out[s][q];
-            }
-            prevT0 = t0;
-        }
-        if (!fail && prevT0 >= 0) {
-#pragma unroll
-            for (int s = 0; s < P; ++s) {
-                const long long e = e0 + (prevT0 + s) * st;
+                const long long e = e0 + (t0 + s) * st;
                 if (MODE == 2) {
-                    g.rDraw[e] = prevOut[s][0];
+                    g.rDraw[e] = out[s][0];
                 } else {
 #pragma unroll
                     for (int q = 0; q < NC; ++q) {
                         if (!((mask >> q) & 1u)) continue;
-                        g.wS[(long long)q * g.nSkew + e] = prevOut[s][q];
-                        if (MODE == 1 && prevCell[s] >= 0) w[(long long)q * N + prevCell[s]] = prevOut[s][q];
+                        g.wS[(long long)q * g.nSkew + e] = out[s][q];
+                        if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = out[s][q];
                     }
                 }
             }
-            if (crossProducer) {
-                __threadfence();
-                __syncwarp();
-                if (lane == 0) store_release(gprog + blk, T);
-            }
         }
         cp_async_wait<0>();
+        // a failed warp lets the producers that wait on its progress go
         if (fail && lane == 0) {
-            st_release_cluster(sProg + jo, T);
-            if (kLocalCons) st_release_cluster(consKin + jo, T);
-            if (kLocalProd) st_release_cluster(prodBack + jo, T);
-            if (crossProducer) {
-                __threadfence();
-                store_release(gprog + blk, T);
-            }
+            if (kLocalProd) *(volatile int *)(prodBack + jo) = T;
+            if (depJ >= 0) *(volatile int *)(jProg + jo) = T;
         }
     }
     // no CTA may leave while a neighbour can still access its shared memory
@@ -421,12 +443,13 @@ __global__ void __launch_bounds__(512) k_systolic(SkewView g, unsigned mask, dou
 }
 
 // rS = r gathered into the skewed layout (0 outside the mesh)
-__global__ void k_skew_gather(SkewView g, unsigned mask, int nc, const double *__restrict__ r, int N) {
+template <class Real>
+__global__ void k_skew_gather(SkewT<Real> g, unsigned mask, int nc, const Real *__restrict__ r, int N) {
     long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= g.nSkew) return;
     int c = g.cellOf[e];
     for (int q = 0; q < nc; ++q)
-        if ((mask >> q) & 1u) g.rS[(long long)q * g.nSkew + e] = c >= 0 ? r[(long long)q * N + c] : 0.0;
+        if ((mask >> q) & 1u) g.rS[(long long)q * g.nSkew + e] = c >= 0 ? r[(long long)q * N + c] : Real(0);
 }
 
 // gather the skewed per-entry coefficients of one matrix
@@ -472,19 +495,37 @@ __global__ void k_skew_premul(SkewView g, const int *__restrict__ faceLo, const 
     g.Bz[e] = bz; g.By[e] = by; g.Bx[e] = bx;
 }
 
+// FP32 copies of the FP64 sweep coefficients
+__global__ void k_skew_to32(SkewView g, SkewView32 h) {
+    long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= g.nSkew) return;
+    h.rDinv[e] = (float)g.rDinv[e];
+    h.Az[e] = (float)g.Az[e]; h.Ay[e] = (float)g.Ay[e]; h.Ax[e] = (float)g.Ax[e];
+    h.Bz[e] = (float)g.Bz[e]; h.By[e] = (float)g.By[e]; h.Bx[e] = (float)g.Bx[e];
+}
+
 namespace {
 
-template <int MODE, int NC, int P>
-void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int CS) {
+template <class Real, int MODE, int NC, int P>
+void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
     StructMesh &s = ctx->mesh.sm;
-    const size_t shm = sweep_smem_bytes<MODE, NC, P>(g.nJB);
+    const size_t shm = sweep_smem_bytes<Real, MODE, NC, P>(g.nJB);
     static size_t attr = 0;   // per instantiation: dynamic shared memory opted in so far
     if (shm > attr) {
-        RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-        RT_CUDA(cudaFuncSetAttribute(k_systolic<MODE, NC, P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)shm));
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                     1));
         attr = shm;
     }
     const int nGroups = (g.nz + CS - 1) / CS;
+    // tagged hand-off between clusters: (boundaries) x blocks x steps x lanes x words
+    const size_t words = (size_t)std::max(1, nGroups - 1) * g.nJB * g.T * 32 * NC * Words<Real>::W;
+    if (s.xfer.n < words) {
+        s.xfer.alloc(words);
+        s.xfer.zero(ctx->stream);
+    }
+    if (++s.epoch == 0) s.epoch = 1;   // 0 marks a cleared word
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nGroups * CS);
     cfg.blockDim = dim3(32 * g.nJB);
@@ -497,21 +538,37 @@ void launch_one(rt_ctx *ctx, const SkewView &g, unsigned mask, double *w, int CS
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<MODE, NC, P>, g, mask, w, ctx->mesh.N, s.sync.p, 1ll << 24));
+    RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<Real, MODE, NC, P>, g, mask, w, ctx->mesh.N, s.sync.p, s.xfer.p,
+                               s.epoch, 1ll << 24));
 }
 
-template <int MODE>
-void launch_mode(rt_ctx *ctx, const SkewView &g, int nc, unsigned mask, double *w) {
-    StructMesh &s = ctx->mesh.sm;
-    RT_CUDA(cudaMemsetAsync(s.sync.p, 0, sizeof(int) * (SYNC_PROGRESS + g.nz * g.nJB), ctx->stream));
-    const int CS = s.KC;   // planes (CTAs) per cluster
-    if (MODE == 2 || nc == 1) {
-        // chunks of 8 steps when the staging fits in shared memory, else 4
-        if (sweep_smem_bytes<MODE, 1, 8>(g.nJB) <= kMaxSmem) launch_one<MODE, 1, 8>(ctx, g, mask, w, CS);
-        else launch_one<MODE, 1, 4>(ctx, g, mask, w, CS);
+// chunk size: the largest of 8, 4, 2, 1 steps whose staging and rings fit
+template <class Real, int MODE, int NC>
+void launch_fit(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
+    if constexpr (NC == 1) {
+        if (sweep_smem_bytes<Real, MODE, NC, 8>(g.nJB) <= kMaxSmem) {
+            launch_one<Real, MODE, NC, 8>(ctx, g, mask, w, CS);
+            return;
+        }
     }
-    else if (nc <= 3) launch_one<MODE, 3, 2>(ctx, g, mask, w, CS);
-    else launch_one<MODE, 6, 2>(ctx, g, mask, w, CS);
+    // (FP64 six-component chunks of 4 steps would spill registers)
+    if (!(sizeof(Real) == 8 && NC == 6) && sweep_smem_bytes<Real, MODE, NC, 4>(g.nJB) <= kMaxSmem) {
+        if constexpr (!(sizeof(Real) == 8 && NC == 6)) launch_one<Real, MODE, NC, 4>(ctx, g, mask, w, CS);
+    } else if (sweep_smem_bytes<Real, MODE, NC, 2>(g.nJB) <= kMaxSmem) launch_one<Real, MODE, NC, 2>(ctx, g, mask, w, CS);
+    else launch_one<Real, MODE, NC, 1>(ctx, g, mask, w, CS);
+}
+
+template <class Real, int MODE>
+void launch_mode(rt_ctx *ctx, const SkewT<Real> &g, int nc, unsigned mask, Real *w) {
+    StructMesh &s = ctx->mesh.sm;
+    // the group counter restarts; the error flag stays until skew_check reads it
+    RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
+    const int CS = s.KC;   // planes (CTAs) per cluster
+    if (MODE == 2 || nc == 1) launch_fit<Real, MODE, 1>(ctx, g, mask, w, CS);
+    else if constexpr (MODE != 2) {
+        if (nc <= 3) launch_fit<Real, MODE, 3>(ctx, g, mask, w, CS);
+        else launch_fit<Real, MODE, 6>(ctx, g, mask, w, CS);
+    }
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
     s.pendingCheck = true;
@@ -526,7 +583,7 @@ void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const do
     k_skew_setup<<<nb, RT_BLOCK, 0, ctx->stream>>>(g, s.faceLo.p, ctx->mesh.N, diag, upper, lower);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
-    launch_mode<2>(ctx, g, 1, 1u, nullptr);
+    launch_mode<double, 2>(ctx, g, 1, 1u, (double *)nullptr);
     k_skew_premul<<<nb, RT_BLOCK, 0, ctx->stream>>>(g, s.faceLo.p, s.faceHi.p, ctx->mesh.N, upper, lower);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
@@ -534,11 +591,30 @@ void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const do
 
 void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
     SkewView g = ctx->mesh.sm.view();
-    k_skew_gather<<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
+    k_skew_gather<double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
-    launch_mode<0>(ctx, g, nc, mask, w);
-    launch_mode<1>(ctx, g, nc, mask, w);
+    launch_mode<double, 0>(ctx, g, nc, mask, w);
+    launch_mode<double, 1>(ctx, g, nc, mask, w);
+}
+
+void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const double *lower) {
+    skew_prepare(ctx, diag, upper, lower);
+    StructMesh &s = ctx->mesh.sm;
+    SkewView g = s.view();
+    SkewView32 h = s.view32();
+    k_skew_to32<<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, h);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+}
+
+void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, float *w) {
+    SkewView32 g = ctx->mesh.sm.view32();
+    k_skew_gather<float><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    launch_mode<float, 0>(ctx, g, nc, mask, w);
+    launch_mode<float, 1>(ctx, g, nc, mask, w);
 }
 
 rt_status skew_check(rt_ctx *ctx) {
@@ -548,6 +624,7 @@ rt_status skew_check(rt_ctx *ctx) {
     RT_CUDA(cudaMemcpyAsync(&err, s.sync.p + SYNC_ERROR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     RT_CUDA(cudaStreamSynchronize(ctx->stream));
     s.pendingCheck = false;
+    if (err) RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_ERROR, 0, sizeof(int), ctx->stream));
     return err ? RT_ETIMEOUT : RT_OK;
 }
 

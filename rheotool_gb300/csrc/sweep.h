@@ -9,6 +9,10 @@ namespace rt {
 void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
 // w = M^-1 r for the masked components (nc <= 6), forward then backward
 void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
+// mixed precision: skew_prepare, then FP32 copies of the sweep coefficients
+void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
+// FP32 w = M^-1 r with the coefficients of the last skew_prepare32
+void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, float *w);
 // RT_ETIMEOUT if a bounded wait of the last sweeps ran out
 rt_status skew_check(rt_ctx *ctx);
 

@@ -286,7 +286,7 @@ def cavity_mesh(n: int = 64, ny: Optional[int] = None) -> Mesh:
 def contraction_mesh(nx_up: int = 134, nx_down: int = 132, ny_in: int = 50,
                      ny_out: int = 25, nz: int = 50, L_up: float = 20.0,
                      L_down: float = 20.0, depth: float = 2.0,
-                     name: Optional[str] = None) -> Mesh:
+                     name: Optional[str] = None, two_d: bool = False) -> Mesh:
     """3-D planar 4:1 contraction: upstream channel y in [-4, 4], downstream
     y in [-1, 1] (H = 1), depth ``depth`` in z, the contraction plane at x = 0.
 
@@ -295,8 +295,11 @@ def contraction_mesh(nx_up: int = 134, nx_down: int = 132, ny_in: int = 50,
     contraction plane in x, towards the re-entrant corners y = +-1 and towards
     the z walls.  Patches: ``inlet`` (x = -L_up), ``outlet`` (x = L_down) and
     ``walls`` (everything else).  The default sizes give exactly 1,000,000
-    cells: 50 * (134 * 100 + 132 * 50).
+    cells: 50 * (134 * 100 + 132 * 50).  ``two_d``: one cell thick with empty
+    front and back (the planar 2-D contraction; nz is then 1).
     """
+    if two_d:
+        nz = 1
     xs_up = graded_nodes(-L_up, 0.0, nx_up, 1.0 / 20.0)
     xs_dn = graded_nodes(0.0, L_down, nx_down, 20.0)
     xs = np.concatenate([xs_up, xs_dn[1:]])
@@ -304,7 +307,7 @@ def contraction_mesh(nx_up: int = 134, nx_down: int = 132, ny_in: int = 50,
     y_mid = two_sided_nodes(-1.0, 1.0, ny_in, 4.0)
     y_hi = graded_nodes(1.0, 4.0, ny_out, 8.0)
     ys = np.concatenate([y_lo, y_mid[1:], y_hi[1:]])
-    zs = two_sided_nodes(0.0, depth, nz, 4.0)
+    zs = np.array([0.0, depth]) if two_d else two_sided_nodes(0.0, depth, nz, 4.0)
     nx, ny = len(xs) - 1, len(ys) - 1
     active = np.ones((nz, ny, nx), dtype=bool)
     # holes: downstream (i >= nx_up) outside the narrow channel
@@ -321,7 +324,7 @@ def contraction_mesh(nx_up: int = 134, nx_down: int = 132, ny_in: int = 50,
 
     N = nz * (nx_up * ny + nx_down * ny_in)
     return structured_mesh(xs, ys, zs, patch_of, ["inlet", "outlet", "walls"],
-                           active=active, name=name or f"contraction{N}")
+                           active=active, empty_z=two_d, name=name or f"contraction{N}")
 
 
 def channel_mesh(nx: int = 20, ny: int = 16, nz: int = 4, L: float = 4.0,

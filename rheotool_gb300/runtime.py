@@ -87,6 +87,11 @@ class Context:
         """abi.SWEEP_AUTO / SWEEP_LEVELS / SWEEP_SYSTOLIC for the DIC/DILU sweeps."""
         self.set_option(abi.RT_OPT_SWEEP, mode)
 
+    def set_precision(self, precision: int):
+        """abi.RT_PREC_FP64 / RT_PREC_MIXED for standalone ldu_solve calls
+        (the time step takes its precision from the case control)."""
+        self.set_option(abi.RT_OPT_PRECISION, precision)
+
     def setup_case(self, case: Case, fields: Optional[Fields] = None):
         if self.mesh is not case.mesh:
             self.upload_mesh(case.mesh)

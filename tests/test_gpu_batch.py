@@ -1,0 +1,124 @@
+"""Batched form: many independent cases of uneven size stepped as one device
+mesh, through the C ABI.
+
+Each case of a batch must give what it gives alone.  In FP64 the batch runs
+the plain solvers' arithmetic per case, so each case's fields match the FP64
+oracle at the plain path's bar (1e-9 relative L2, or the oracle's own
+round-off sensitivity where a case is ill-conditioned).  In the mixed form a
+case in a batch and the same case alone differ only by the grouping of their
+reductions, so both satisfy the mixed form's bar against the oracle.
+"""
+import numpy as np
+import pytest
+
+from rheotool_gb300 import abi
+from rheotool_gb300.batch import BatchContext, cavity_sweep, union_mesh
+from rheotool_gb300.case import cavity_case, contraction_case
+from rheotool_gb300.mesh import contraction_mesh
+
+from test_gpu_parity import TOL_STEP, oracle_run, rel, step_bar
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ("U", "p", "phi", "theta", "tau")
+
+
+def small_sweep(precision):
+    cases = cavity_sweep(n_cases=6, n_min=8, n_max=20, seed=7, dt=5e-3, precision=precision)
+    return cases
+
+
+def test_batch_fp64_matches_oracle_per_case():
+    cases = small_sweep(abi.RT_PREC_FP64)
+    bt = BatchContext(cases)
+    try:
+        bt.step(4)
+        got = bt.fields()
+        perf = bt.case_perf()
+    finally:
+        bt.ctx.close()
+    for i, c in enumerate(cases):
+        ref = oracle_run(c, 4)
+        errs = {n: rel(getattr(got[i], n), getattr(ref, n)) for n in NAMES}
+        if all(e < TOL_STEP for e in errs.values()):
+            continue
+        bar = step_bar(c, 4, ref, NAMES)
+        for n in NAMES:
+            assert errs[n] < bar[n], (i, c.model.type, n, errs[n], bar[n])
+    assert all(p.p.converged for p in perf)
+
+
+def test_batch_case_equals_case_alone_fp64(ctx):
+    """Iteration counts and fields of each case: in the batch as alone."""
+    cases = small_sweep(abi.RT_PREC_FP64)
+    bt = BatchContext(cases)
+    try:
+        bt.step(3)
+        got = bt.fields()
+        perf = bt.case_perf()
+    finally:
+        bt.ctx.close()
+    for i, c in enumerate(cases):
+        ctx.setup_case(c)
+        pa = ctx.step(3)
+        alone = ctx.fields()
+        assert abs(perf[i].p.nIterations - pa.p.nIterations) <= 1, (i, perf[i].p.nIterations, pa.p.nIterations)
+        for k in range(2):
+            assert abs(perf[i].U[k].nIterations - pa.U[k].nIterations) <= 1
+        for n in NAMES:
+            assert rel(getattr(got[i], n), getattr(alone, n)) < 1e-8, (i, n)
+
+
+def test_batch_mixed_within_mixed_bar():
+    from test_gpu_mixed import TOL_MIXED, _tightened
+    import copy
+    cases = small_sweep(abi.RT_PREC_MIXED)
+    bt = BatchContext(cases)
+    try:
+        bt.step(4)
+        got = bt.fields()
+    finally:
+        bt.ctx.close()
+    for i, c in enumerate(cases):
+        ref = oracle_run(c, 4)
+        tight = copy.copy(c)
+        tight.solverU, tight.solverP, tight.solverTheta = (_tightened(c.solverU), _tightened(c.solverP),
+                                                            _tightened(c.solverTheta))
+        ref_t = oracle_run(tight, 4)
+        for n in NAMES:
+            floor = rel(getattr(ref_t, n), getattr(ref, n))
+            err = rel(getattr(got[i], n), getattr(ref, n))
+            assert err < max(TOL_MIXED, 3.0 * floor), (i, n, err, floor)
+
+
+def test_batch_level_sweeps_for_unstructured_cases():
+    """A batch whose cases carry no 2-D box layout (here 3-D contractions)
+    uses the level-scheduled sweeps over the union: same per-case results."""
+    meshes = [contraction_mesh(8, 6, 6, 4, 3, 4.0, 4.0), contraction_mesh(10, 8, 6, 4, 4, 4.0, 4.0)]
+    cases = [contraction_case(m) for m in meshes]
+    for c in cases:
+        c.precision = abi.RT_PREC_FP64
+    bt = BatchContext(cases)
+    try:
+        bt.step(2)
+        got = bt.fields()
+    finally:
+        bt.ctx.close()
+    for i, c in enumerate(cases):
+        ref = oracle_run(c, 2)
+        for n in NAMES:
+            assert rel(getattr(got[i], n), getattr(ref, n)) < TOL_STEP, (i, n)
+
+
+def test_batch_layout_rejects_a_face_across_cases(ctx):
+    from rheotool_gb300.runtime import RheoGpuError, _mesh_desc
+    import ctypes as C
+    cases = small_sweep(abi.RT_PREC_FP64)[:2]
+    u, cs, fs, bs = union_mesh([c.mesh for c in cases])
+    md = _mesh_desc(u, ctx)
+    ctx._check(ctx.lib.rt_mesh_upload(ctx._ctx, C.byref(md)), "rt_mesh_upload")
+    bad = cs.copy()
+    bad[1] += 1                       # the first face of case 1 now joins two cases
+    st = ctx.lib.rt_batch_layout(ctx._ctx, 2, abi.iptr(bad), abi.iptr(fs), abi.iptr(bs), None, None)
+    assert st == abi.RT_EINVAL
+    ctx.mesh = None
