@@ -59,6 +59,12 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="form timed for `value` (the other is timed beside it unless --no-plain)")
     ap.add_argument("--no-plain", action="store_true", help="skip the second form")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched cavity sweep")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
+    ap.add_argument("--batch-cases", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -152,6 +158,101 @@ def cpu_baseline(seconds: float, warm: int = 1):
             "sample": f"same contraction/Giesekus case at {cells:,} cells (1/8 of the 1M mesh), "
                       f"{n} time steps after {warm} warm-up step(s), FP64 oracle (serial face loops and "
                       f"Krylov sweeps, OpenMP over cell-local loops), {dt:.1f} s"}
+
+
+def run_batched(args):
+    """Batched form: the parametric cavity sweep (independent 2-D cavities,
+    side 32..192, Oldroyd-B / Giesekus / FENE-P, Wi 0.1..4) as one device
+    mesh in the mixed form, against the FP64 plain path running a sample of
+    the same cases one at a time."""
+    import numpy as np
+    from rheotool_gb300 import abi
+    from rheotool_gb300.batch import BatchContext, cavity_sweep
+    from rheotool_gb300.runtime import Context
+    cases = cavity_sweep(args.batch_cases, 32, 192, precision=abi.RT_PREC_MIXED)
+    bt = BatchContext(cases)
+    bt.step(2)
+    bt.ctx.sync()
+    k0 = bt.ctx.kernel_count()
+    bt.ctx.timer_start()
+    bt.step(args.batch_steps)
+    ms = bt.ctx.timer_stop()
+    launches = bt.ctx.kernel_count() - k0
+    cells = bt.nCells
+    value = cells * args.batch_steps / (ms * 1e-3)
+    perf = bt.case_perf()
+    bt.ctx.close()
+    # the plain path: 16 of the cases, one context each, FP64, same protocol
+    import copy
+    sample = [copy.copy(cases[i]) for i in range(0, len(cases), max(1, len(cases) // 16))][:16]
+    tot_ms, tot_cells = 0.0, 0
+    for c in sample:
+        c.precision = abi.RT_PREC_FP64
+        ctx = Context(0)
+        ctx.setup_case(c)
+        ctx.step(2)
+        ctx.sync()
+        ctx.timer_start()
+        ctx.step(3)
+        tot_ms += ctx.timer_stop()
+        tot_cells += c.mesh.nCells * 3
+        ctx.close()
+    plain = tot_cells / (tot_ms * 1e-3)
+    return {"workload": f"{len(cases)} independent 2-D cavities, side 32..192 (uniform), "
+                        "models Oldroyd-B / Giesekus alpha=0.1 / FENE-P L2=100, Wi log-uniform 0.1..4, "
+                        "beta 0.1..0.9, Re 0.01, dt 1e-3; mixed-precision form, one device mesh",
+            "cases": len(cases), "cells": cells, "steps": args.batch_steps, "value": value,
+            "unit": UNIT, "ms_per_step": ms / args.batch_steps, "gpu_launches": launches,
+            "time_to_solution_200_steps_s": 200 * ms / args.batch_steps * 1e-3,
+            "p_iterations_max": max(p.p.nIterations for p in perf),
+            "plain_fp64_one_case_at_a_time": {"value": plain, "unit": UNIT,
+                                              "sample": f"{len(sample)} of the cases, 3 timed steps each"},
+            "speedup_vs_plain_fp64": value / plain}
+
+
+def run_served(args):
+    """Served form: a Poisson request stream (50 requests/s) of 2-D cavity and
+    2-D contraction cases (16k..65k cells), each a fixed number of steps,
+    served by the continuous-batching loop in the mixed form; the same stream
+    served one request at a time by the FP64 plain path for comparison."""
+    import copy
+    import numpy as np
+    from rheotool_gb300 import abi
+    from rheotool_gb300.case import cavity_case, contraction_case
+    from rheotool_gb300.mesh import cavity_mesh, contraction_mesh
+    from rheotool_gb300.serve import poisson_run
+    rng = np.random.default_rng(20261203)
+    meshes = {("cav", n): cavity_mesh(n) for n in (128, 160, 192, 224, 256)}
+    for nx, ny in ((60, 20), (90, 30), (120, 40)):
+        meshes[("con", nx)] = contraction_mesh(nx, nx, 2 * ny, ny, two_d=True)
+    keys = list(meshes)
+    cases = []
+    for i in range(args.serve_requests):
+        key = keys[int(rng.integers(0, len(keys)))]
+        m = meshes[key]
+        if key[0] == "cav":
+            c = cavity_case(m.shape[0], model="GiesekusLog", Wi=float(rng.uniform(0.5, 2.0)), dt=1e-3, mesh=m,
+                            alpha=0.1)
+        else:
+            c = contraction_case(m, dt=2e-3)
+        c.precision = abi.RT_PREC_MIXED
+        cases.append(c)
+    served = poisson_run(cases, args.serve_steps, rate=50.0, slots=4, batch_cells=40000, batch_max=8,
+                         quantum=5, hbm_budget=64 << 30)
+    plain_cases = []
+    for c in cases:
+        c2 = copy.copy(c)
+        c2.precision = abi.RT_PREC_FP64
+        plain_cases.append(c2)
+    plain = poisson_run(plain_cases, args.serve_steps, rate=50.0, slots=1, batch_cells=0, quantum=5,
+                        hbm_budget=64 << 30)
+    strip = lambda d: {k: v for k, v in d.items() if k != "requests_list"}
+    return {"workload": f"{len(cases)} requests, Poisson 50/s, 2-D cavity (128..256 side) and 2-D contraction "
+                        f"(7k..29k cells) Giesekus cases, {args.serve_steps} steps each; mixed form, 4 slots, "
+                        "small cases batched",
+            "served": strip(served), "plain_fp64_one_request_at_a_time": strip(plain),
+            "speedup_p50": plain["p50_s"] / served["p50_s"] if served["p50_s"] else None,
+            "speedup_throughput": served["cell_steps_per_s"] / plain["cell_steps_per_s"]}
 
 
 def run_reference(args, rank):
@@ -313,6 +414,10 @@ def main():
         e2e = {"value": N * ke * world / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "steps": ke, "path": "rt_field_set(U,p,phi) + rt_step(1) + rt_field_get(U,p,phi,tau), pinned host"}
 
+    ctx.close()
+    batched = None if (args.no_batch or args.small) else run_batched(args)
+    served = None if (args.no_serve or args.small) else run_served(args)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         cpu = cpu_baseline(args.cpu_seconds)
@@ -339,8 +444,11 @@ def main():
             line["speedup_vs_" + key] = value / second["value"]
             line["field_error_vs_fp64"] = field_err
         line["profile_ms_2_steps"] = {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+        if batched is not None:
+            line["batched"] = batched
+        if served is not None:
+            line["served"] = served
         print(json.dumps(line), flush=True)
-    ctx.close()
     if pg:
         pg.destroy_process_group()
 

@@ -472,8 +472,6 @@ struct Solver {
         nB = ctx->red.nBlocks;
     }
 
-    int rblocks() const { return std::min(nB, nblocks(N)); }
-
     // finalize nSlots reduction slots of the masked comps into red.result
     void finalize(int nSlots, unsigned mask) {
         // blocks beyond rblocks() left stale partials: zero them by using only
@@ -482,11 +480,6 @@ struct Solver {
         k_finalize<<<nSlots * 6, RT_BLOCK, 0, st>>>(nB, nSlots, mask, ctx->red.partial.p, ctx->red.result.p);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
-    }
-
-    void fetch(const double *dev, int count) {
-        RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, dev, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
-        RT_CUDA(cudaStreamSynchronize(st));
     }
 
     static int pop(unsigned m) { return __builtin_popcount(m); }
@@ -752,18 +745,20 @@ rt_status run_pbicgstab(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
 
 
 // ==========================================================================
-// Mixed precision (RT_PREC_MIXED): the Krylov vectors, the matrix copy used
-// inside the iterations and the preconditioner application are FP32; the
-// scalars, the dot-product accumulations, the solution and the normalised
-// residual stay FP64.  The solution is kept as psi (FP64) + x32 (an FP32
-// correction accumulated since the last residual replacement).  Whenever the
-// recursively updated FP32 residual has dropped by kReplace since the last
-// replacement, claims convergence, or the iteration budget ends, x32 is
-// folded into psi and the residual is recomputed from the FP64 matrix as
-// b - A psi (reliable updates, Sleijpen & van der Vorst 1996; van der Vorst &
-// Ye 2000).  Convergence is only ever declared on that FP64 residual, with
-// the normFactor of the FP64 prologue, so the stopping test is the one of
-// the plain solvers.
+// Mixed precision (RT_PREC_MIXED).  PBiCGStab (momentum and theta): the
+// Krylov vectors, the matrix copy used inside the iterations and the
+// preconditioner application are FP32; the scalars, the dot-product
+// accumulations, the solution and the normalised residual stay FP64.  The
+// solution is kept as psi (FP64) + x32 (an FP32 correction accumulated since
+// the last residual replacement).  Whenever the recursively updated FP32
+// residual has dropped by kReplace since the last replacement, claims
+// convergence, or the iteration budget ends, x32 is folded into psi and the
+// residual is recomputed from the FP64 matrix as b - A psi (reliable updates,
+// Sleijpen & van der Vorst 1996; van der Vorst & Ye 2000).  Convergence is
+// only ever declared on that FP64 residual, with the normFactor of the FP64
+// prologue.  PCG (pressure) keeps FP64 vectors and applies only the DIC
+// preconditioner in FP32 (run_pcg_flex32): the pressure matrix is too
+// ill-conditioned for FP32 Krylov vectors to keep their conjugacy.
 // ==========================================================================
 constexpr double kReplace = 0.1;
 
@@ -859,52 +854,43 @@ __global__ void k_mx_diag_apply(int N, unsigned mask, const float *__restrict__ 
 }
 
 // flexible PCG scalars: wArAold = wArA; wArA = w.r; beta = w.(r - r_old) /
-// wArAold = (w.r - alpha_old w.q_old) / wArAold (Polak-Ribiere form: robust
-// to the FP32 preconditioner, which is not exactly the same operator twice)
+// wArAold = -alpha_old w.q_old / wArAold, since r - r_old = -alpha_old q_old
+// (Polak-Ribiere form; equal to wArA / wArAold in exact arithmetic, robust to
+// the FP32 preconditioner, which is not exactly the same operator twice)
 __global__ void k_mx_sc_pcg_a(unsigned mask, int first, const double *res, double *S) {
     int k = threadIdx.x;
     if (k < 6 && ((mask >> k) & 1u)) {
         const double aold = S[S_A * 8 + k];
         S[S_AOLD * 8 + k] = aold;
         S[S_A * 8 + k] = res[k];
-        if (!first) S[S_B * 8 + k] = (res[k] - S[S_ALPHA * 8 + k] * res[6 + k]) / aold;
+        if (!first) S[S_B * 8 + k] = -S[S_ALPHA * 8 + k] * res[6 + k] / aold;
     }
 }
 
-// PCG: p = w (+ beta p)
-__global__ void k_mx_pcg_p(int N, unsigned mask, int first, const double *__restrict__ S,
-                           const float *__restrict__ w, float *__restrict__ p) {
+// flexible PCG: p = z (+ beta p), beta from k_mx_sc_pcg_a
+__global__ void k_pcg_p_flex(int N, unsigned mask, int first, const double *__restrict__ S,
+                             const double *__restrict__ z, double *__restrict__ p) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
     for (int k = 0; k < 6; ++k) {
         if (!((mask >> k) & 1u)) continue;
         size_t i = (size_t)k * N + c;
-        if (first) p[i] = w[i];
-        else p[i] = fmaf((float)S[S_B * 8 + k], p[i], w[i]);
+        p[i] = first ? z[i] : fma(S[S_B * 8 + k], p[i], z[i]);
     }
 }
 
-// PCG: x += alpha p; r -= alpha q; partial |r| (slot 0)
-__global__ void k_mx_pcg_update(int N, unsigned mask, const double *__restrict__ S, const float *__restrict__ p,
-                                const float *__restrict__ q, float *__restrict__ x, float *__restrict__ r,
-                                double *partial, int nB) {
-    for (int k = 0; k < 6; ++k) {
-        if (!((mask >> k) & 1u)) continue;
-        const bool sing = S[S_SING * 8 + k] != 0.0;
-        const float alpha = (float)S[S_ALPHA * 8 + k];
-        double v = 0.0;
-        size_t o = (size_t)k * N;
-        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
-            float rr = r[o + c];
-            if (!sing) {
-                x[o + c] = fmaf(alpha, p[o + c], x[o + c]);
-                rr = fmaf(-alpha, q[o + c], rr);
-                r[o + c] = rr;
-            }
-            v += fabs((double)rr);
-        }
-        store_partial(partial, nB, 0, k, v);
-    }
+// FP64 <-> FP32 copies of the masked components
+__global__ void k_mx_d2f(int N, unsigned mask, const double *__restrict__ a, float *__restrict__ b) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((mask >> k) & 1u) b[(size_t)k * N + c] = (float)a[(size_t)k * N + c];
+}
+__global__ void k_mx_f2d(int N, unsigned mask, const float *__restrict__ a, double *__restrict__ b) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((mask >> k) & 1u) b[(size_t)k * N + c] = (double)a[(size_t)k * N + c];
 }
 
 // psi += x32; x32 = 0
@@ -1170,61 +1156,67 @@ unsigned mixed_replace_set(const Mixed &mx, const SolveArgs &a, unsigned cand, c
     return R;
 }
 
-rt_status run_pcg_mixed(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
-    Mixed mx(ctx, a, 5);
+// Mixed form of the pressure solve: PCG with FP64 vectors and scalars and
+// the DIC preconditioner applied in FP32.  The FP32 sweeps make the
+// preconditioner a slightly different operator at every application, so beta
+// takes the flexible (Polak-Ribiere) form; the iterates keep FP64
+// conjugacy, which an ill-conditioned pressure matrix needs (FP32 Krylov
+// vectors lose it and stall).  Stopping test and records as run_pcg.
+rt_status run_pcg_flex32(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    Mixed mx(ctx, a, 2);
     const int N = mx.N;
-    float *r = mx.v(0), *w = mx.v(1), *p = mx.v(2), *q = mx.v(3), *x = mx.v(4);
-    double lastTrue[6] = {};
-    unsigned active = mixed_begin(mx, a, perf, r, x, lastTrue);
+    double *ws = ctx->kws.p;
+    double *wA = ws, *rA = ws + 6 * (size_t)N, *pA = ws + 12 * (size_t)N, *zA = ws + 18 * (size_t)N;
+    float *r32 = mx.v(0), *z32 = mx.v(1);
+    const unsigned mask = a.validMask;
+    mx.prepare();
+    mx.prologue(mask, wA, rA);
+    RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, mx.S, sizeof(double) * 3 * 8, cudaMemcpyDeviceToHost, mx.st));
+    RT_CUDA(cudaStreamSynchronize(mx.st));
+    unsigned active = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        perf[k].initialResidual = ctx->red.hostResult[S_INIT * 8 + k];
+        perf[k].finalResidual = ctx->red.hostResult[S_FIN * 8 + k];
+        perf[k].nIterations = 0;
+        perf[k].singular = 0;
+        if (a.ctl.minIter > 0 || !mx.conv(perf[k].finalResidual, perf[k].initialResidual)) active |= 1u << k;
+    }
     int iter = 0;
     while (active) {
-        mx.precondition32(active, r, w);
-        if (iter == 0) mx.dot32(active, w, r);
-        else mx.dot32(active, w, r, w, q);   // q = A p of the previous iteration
+        k_mx_d2f<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, rA, r32);
+        mx.precondition32(active, r32, z32);
+        k_mx_f2d<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, z32, zA);
+        if (iter == 0) mx.dot(active, zA, rA);
+        else mx.dot(active, zA, rA, zA, wA);   // wA = A p of the previous iteration
         k_mx_sc_pcg_a<<<1, 32, 0, mx.st>>>(active, iter == 0, ctx->red.result.p, mx.S);
-        k_mx_pcg_p<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, iter == 0, mx.S, w, p);
-        mx.amul32(active, p, q);
-        mx.dot32(active, q, p);
+        k_pcg_p_flex<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, iter == 0, mx.S, zA, pA);
+        mx.amul(active, pA, wA);
+        mx.dot(active, wA, pA);
         k_sc_pcg_alpha<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
-        k_mx_pcg_update<<<mx.nB, RT_BLOCK, 0, mx.st>>>(N, active, mx.S, p, q, x, r, ctx->red.partial.p, mx.nB);
+        k_pcg_update<<<mx.nB, RT_BLOCK, 0, mx.st>>>(N, active, mx.S, pA, wA, a.psi, rA, ctx->red.partial.p, mx.nB);
         RT_CHECK_LAUNCH();
         mx.finalize(1, active);
         k_sc_fin<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
         RT_CHECK_LAUNCH();
-        launch_count(ctx, 4);
+        launch_count(ctx, 7);
         mx.sync_scalars();
+        const double *H = ctx->red.hostResult;
         ++iter;
-        double H[(S_SING + 1) * 8];
-        memcpy(H, ctx->red.hostResult, sizeof H);
-        unsigned sing = 0;
-        for (int k = 0; k < 6; ++k)
-            if (((active >> k) & 1u) && H[S_SING * 8 + k] != 0.0) {
-                perf[k].singular = 1;
-                sing |= 1u << k;
-            }
-        const unsigned cand = active & ~sing;
-        const unsigned R = mixed_replace_set(mx, a, cand, H, iter, perf, lastTrue);
-        mx.replace(R, x, r);
-        if (R) {
-            mx.sync_scalars();
-            memcpy(H, ctx->red.hostResult, sizeof H);
-        }
-        unsigned next = 0;
         for (int k = 0; k < 6; ++k) {
-            if (!((cand >> k) & 1u)) continue;
+            if (!((active >> k) & 1u)) continue;
+            if (H[S_SING * 8 + k] != 0.0) {
+                perf[k].singular = 1;
+                active &= ~(1u << k);
+                continue;
+            }
             perf[k].finalResidual = H[S_FIN * 8 + k];
             perf[k].nIterations = iter;
-            if ((R >> k) & 1u) lastTrue[k] = perf[k].finalResidual;
-            const bool conv = ((R >> k) & 1u) && mx.conv(perf[k].finalResidual, perf[k].initialResidual);
-            const bool more = (iter < a.ctl.maxIter && !conv) || iter < a.ctl.minIter;
-            if (more && std::isfinite(perf[k].finalResidual)) next |= 1u << k;
+            const bool more = (iter < a.ctl.maxIter && !mx.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
+                              iter < a.ctl.minIter;
+            if (!more) active &= ~(1u << k);
         }
-        active = next;
     }
-    // whatever is still in x32 (singular components) goes to psi
-    k_mx_fold<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, a.validMask, x, a.psi);
-    RT_CHECK_LAUNCH();
-    launch_count(ctx);
     return RT_OK;
 }
 
@@ -1355,7 +1347,7 @@ rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf
             SolveArgs t = b;
             t.ctl.tolerance *= ctx->mixedTighten;
             t.ctl.relTol *= ctx->mixedTighten;
-            st = pcg ? run_pcg_mixed(ctx, t, perf) : run_pbicgstab_mixed(ctx, t, perf);
+            st = pcg ? run_pcg_flex32(ctx, t, perf) : run_pbicgstab_mixed(ctx, t, perf);
         }
         else st = pcg ? run_pcg(ctx, b, perf) : run_pbicgstab(ctx, b, perf);
     }

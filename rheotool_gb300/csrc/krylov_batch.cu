@@ -383,14 +383,14 @@ __global__ void k_b_start(int nCases, unsigned vm, Ctl ctl, BSeg S, const double
 }
 
 // PCG scalars; FP32 vectors use the flexible (Polak-Ribiere) beta
-// w.(r - r_old) / w_old.r_old = (w.r - alpha_old w.q_old) / w_old.r_old
+// w.(r - r_old) / w_old.r_old = -alpha_old w.q_old / w_old.r_old
 __global__ void k_b_pcg_a(int nSeg, BSeg S, const double *__restrict__ res, int mixed) {
     for (int sg = threadIdx.x + blockIdx.x * blockDim.x; sg < nSeg; sg += blockDim.x * gridDim.x) {
         if (!S.active[sg]) continue;
         const double aold = S.A[sg];
         S.Aold[sg] = aold;
         S.A[sg] = res[sg];
-        S.beta[sg] = mixed ? (res[sg] - S.alpha[sg] * res[nSeg + sg]) / aold : res[sg] / aold;
+        S.beta[sg] = mixed ? -S.alpha[sg] * res[nSeg + sg] / aold : res[sg] / aold;
     }
 }
 

@@ -136,7 +136,7 @@ template <int P> struct Ring {
 // arrays of P steps x 32 lanes, plus the cells of the backward sweep.
 template <int MODE, int NC> struct Stage { static constexpr int NA = 4 + NC; };
 
-constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per CTA on sm_100-class parts
+constexpr size_t kMaxSmem = 227 * 1024 - 1024;   // dynamic shared memory per CTA (static part kept free)
 constexpr int kPre = 8;                   // L2 prefetch distance (chunks)
 
 template <class Real, int MODE, int NC, int P>
@@ -230,25 +230,35 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
         auto xslot = [&](int b, int t, int q) -> u64 * {
             return xfer + ((((size_t)b * nJB + jb) * T + t) * 32 + lane) * VW + q * W;
         };
-        constexpr int RB = (int)sizeof(Real);
-        // stage the coefficients of the chunk starting at step tc into buffer b
+        // stage the coefficients of the chunk starting at step tc into buffer
+        // b: the chunk's entries of one array are one contiguous block of
+        // P x 32 (the backward sweep walks it mirrored), copied in 16-byte
+        // pieces spread over the lanes; smem layout [buffer][array][P * 32]
+        constexpr int EPC = 16 / (int)sizeof(Real);   // entries per 16-byte piece
+        constexpr int PIECES = P * 32 / EPC;
+        auto copy_block = [&](Real *dst, const Real *src) {
+#pragma unroll
+            for (int i = lane; i < PIECES; i += 32) cp_async<16>(dst + i * EPC, src + i * EPC);
+        };
         auto stage_chunk = [&](int tc, int b) {
+            const long long lo = (MODE == 1) ? (long long)blk * BS + (long long)(T - tc - P) * 32
+                                             : (long long)blk * BS + (long long)tc * 32;
+            Real *dst = myStage + (size_t)b * NA * P * 32;
+            if (MODE == 2) {
+                copy_block(dst + 0 * P * 32, g.D + lo); copy_block(dst + 1 * P * 32, g.Pz + lo);
+                copy_block(dst + 2 * P * 32, g.Py + lo); copy_block(dst + 3 * P * 32, g.Px + lo);
+            } else {
+                copy_block(dst + 0 * P * 32, (MODE == 0 ? g.Az : g.Bz) + lo);
+                copy_block(dst + 1 * P * 32, (MODE == 0 ? g.Ay : g.By) + lo);
+                copy_block(dst + 2 * P * 32, (MODE == 0 ? g.Ax : g.Bx) + lo);
+                if (MODE == 0) copy_block(dst + 3 * P * 32, g.rDinv + lo);
 #pragma unroll
-            for (int s = 0; s < P; ++s) {
-                const long long e = e0 + (tc + s) * st;
-                Real *d = myStage + ((size_t)(b * P + s) * NA) * 32 + lane;
-                if (MODE == 2) {
-                    cp_async<RB>(d + 0 * 32, g.D + e); cp_async<RB>(d + 1 * 32, g.Pz + e);
-                    cp_async<RB>(d + 2 * 32, g.Py + e); cp_async<RB>(d + 3 * 32, g.Px + e);
-                } else {
-                    cp_async<RB>(d + 0 * 32, (MODE == 0 ? g.Az : g.Bz) + e);
-                    cp_async<RB>(d + 1 * 32, (MODE == 0 ? g.Ay : g.By) + e);
-                    cp_async<RB>(d + 2 * 32, (MODE == 0 ? g.Ax : g.Bx) + e);
-                    if (MODE == 0) cp_async<RB>(d + 3 * 32, g.rDinv + e);
+                for (int q = 0; q < NC; ++q)
+                    copy_block(dst + (size_t)(4 + q) * P * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo);
+                if (MODE == 1) {
 #pragma unroll
-                    for (int q = 0; q < NC; ++q)
-                        cp_async<RB>(d + (4 + q) * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + e);
-                    if (MODE == 1) cp_async<4>(myCStage + (b * P + s) * 32 + lane, g.cellOf + e);
+                    for (int i = lane; i < P * 8; i += 32)
+                        cp_async<16>(myCStage + b * P * 32 + i * 4, g.cellOf + lo + i * 4);
                 }
             }
         };
@@ -359,20 +369,23 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
             Real out[P][NC];
             int cell[P];
             Real pre[P][NC], cy[P], cx[P];
+            const Real *db = myStage + (size_t)buf * NA * P * 32;
 #pragma unroll
             for (int s = 0; s < P; ++s) {
-                const Real *d = myStage + ((size_t)(buf * P + s) * NA) * 32 + lane;
-                const Real c0 = d[0], c3 = (MODE == 0) ? d[96] : Real(0);
-                cy[s] = (MODE == 2) ? d[64] : d[32];
-                cx[s] = (MODE == 2) ? d[96] : d[64];
-                cell[s] = (MODE == 1) ? myCStage[(buf * P + s) * 32 + lane] : 0;
+                // entry of (step s, lane) inside the chunk's blocks
+                const int si = (MODE == 1) ? (P - 1 - s) * 32 + (31 - lane) : s * 32 + lane;
+                const Real *d = db + si;
+                const Real c0 = d[0], c3 = (MODE == 0) ? d[3 * P * 32] : Real(0);
+                cy[s] = (MODE == 2) ? d[2 * P * 32] : d[P * 32];
+                cx[s] = (MODE == 2) ? d[3 * P * 32] : d[2 * P * 32];
+                cell[s] = (MODE == 1) ? myCStage[buf * P * 32 + si] : 0;
 #pragma unroll
                 for (int q = 0; q < NC; ++q) {
                     const Real wk = wkv[s][q];
                     if (MODE == 2) {
-                        pre[s][q] = r_sub(c0, r_div(d[32], wk));   // D - Pz / rD(k-1)
+                        pre[s][q] = r_sub(c0, r_div(d[P * 32], wk));   // D - Pz / rD(k-1)
                     } else {
-                        const Real rk = d[(4 + q) * 32];
+                        const Real rk = d[(size_t)(4 + q) * P * 32];
                         const Real v0 = (MODE == 0) ? r_mul(c3, rk) : rk;
                         pre[s][q] = r_fma(-c0, wk, v0);
                     }
@@ -567,7 +580,17 @@ void launch_mode(rt_ctx *ctx, const SkewT<Real> &g, int nc, unsigned mask, Real 
     if (MODE == 2 || nc == 1) launch_fit<Real, MODE, 1>(ctx, g, mask, w, CS);
     else if constexpr (MODE != 2) {
         if (nc <= 3) launch_fit<Real, MODE, 3>(ctx, g, mask, w, CS);
-        else launch_fit<Real, MODE, 6>(ctx, g, mask, w, CS);
+        else if (sweep_smem_bytes<Real, MODE, 6, 1>(g.nJB) <= kMaxSmem) launch_fit<Real, MODE, 6>(ctx, g, mask, w, CS);
+        else {
+            // six components do not fit one CTA's shared memory (many
+            // j-blocks, FP64): two launches of three, on shifted views
+            launch_fit<Real, MODE, 3>(ctx, g, mask & 7u, w, CS);
+            SkewT<Real> h = g;
+            h.rS += 3 * g.nSkew;
+            h.wS += 3 * g.nSkew;
+            RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
+            launch_fit<Real, MODE, 3>(ctx, h, (mask >> 3) & 7u, w ? w + 3 * (size_t)ctx->mesh.N : w, CS);
+        }
     }
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
