@@ -334,6 +334,7 @@ def main():
 
     ctx = Context(local)
     ms, perf, launches, clocks = timed(ctx, prec, True)
+    schedule = ctx.sweep_schedule()
     total_cells = N * args.steps * world
     value = total_cells / (ms * 1e-3)
 
@@ -435,7 +436,8 @@ def main():
                                    + (", mixed-precision form" if mixed else ", FP64 plain form"),
                        "cells": N, "faces": F, "parallelism": f"replicas x{world} (independent cases)",
                        "l2": "inputs larger than L2: the step touches ~2 GB of fields and matrices per step",
-                       "iterations_last_step": iters(perf)},
+                       "iterations_last_step": iters(perf),
+                       "sweep_schedule_autotuned": schedule},
             "clocks": clocks, "gpu_launches": launches, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
         }
         if second is not None:

@@ -194,6 +194,11 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * FP64 solve differs from the exact solution, so the mixed form iterates a
  * little further to keep its fields within 1e-6 of the FP64 form. */
 #define RT_OPT_MIXED_TIGHTEN 5
+/* RT_OPT_SWEEP_TUNE: schedule of the one-component systolic sweeps (chunk of
+ * P steps, NB chunks staged ahead): 0 (default) times the candidates on the
+ * first application per structured mesh and precision and keeps the fastest;
+ * 1 .. 5 forces one (P, NB) of (8,3) (8,5) (16,3) (16,4) (4,6). */
+#define RT_OPT_SWEEP_TUNE 6
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);
@@ -277,6 +282,11 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                               const rt_model_params *models, const rt_case_ctl *ctl,
                               const int32_t *pRefCell, const double *pRefValue);
 rt_status rt_batch_step_perf(rt_ctx *ctx, rt_step_perf *perf);
+
+/* The sweep schedules in use: schedule[0..2] = candidate, P, NB of the FP64
+ * one-component sweeps, schedule[3..5] of the FP32 ones (-1, 0, 0 before the
+ * first application).  No reference counterpart. */
+rt_status rt_sweep_schedule(rt_ctx *ctx, int32_t *schedule);
 
 /* Device memory held by all contexts of this library in the process (bytes):
  * what an admission controller adds a new case's footprint to.  No reference

@@ -29,6 +29,7 @@ RT_OPT_SWEEP_PLANES = 2
 RT_OPT_PRECISION = 3
 RT_OPT_MIXED_PARTS = 4
 RT_OPT_MIXED_TIGHTEN = 5
+RT_OPT_SWEEP_TUNE = 6
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {
@@ -172,6 +173,7 @@ def load_library(path: str = LIBNAME):
         "rt_batch_case_setup": ([vp, P(rt_bc_desc), P(rt_model_params), P(rt_case_ctl), _ip, _dp], C.c_int32),
         "rt_batch_step_perf": ([vp, P(rt_step_perf)], C.c_int32),
         "rt_device_bytes": ([P(C.c_int64)], C.c_int32),
+        "rt_sweep_schedule": ([vp, _ip], C.c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

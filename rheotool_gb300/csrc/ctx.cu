@@ -299,7 +299,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         }
         s.nx = nx; s.ny = ny; s.nz = nz;
         s.nJB = (ny + 31) / 32;
-        s.T = ((nx + 31 + 7) / 8) * 8;   // steps per block, padded to whole chunks
+        s.T = ((nx + 31 + 15) / 16) * 16;   // steps per block, padded to whole chunks (P <= 16)
         s.nSkew = (long long)nz * s.nJB * s.T * 32;
         std::vector<int> cellOf((size_t)s.nSkew, -1);
         for (int k = 0; k < nz; ++k)
@@ -321,6 +321,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         s.data.alloc((size_t)(12 + 6 + 6) * s.nSkew);
         s.data.zero(ctx->stream);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        s.tune[0] = s.tune[1] = -1;
         s.on = true;
         return RT_OK;
     });
@@ -338,8 +339,14 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
             RT_REQUIRE(s.on, RT_ENOTREADY, "mesh is not structured");
             RT_REQUIRE(value >= 1 && value <= 16, RT_EINVAL, "planes per cluster: 1 .. 16");
             s.KC = (int)std::min<int64_t>(value, s.nz);
+            s.tune[0] = s.tune[1] = -1;
             return RT_OK;
         }
+        case RT_OPT_SWEEP_TUNE:
+            RT_REQUIRE(value >= 0 && value <= 5, RT_EINVAL, "RT_OPT_SWEEP_TUNE: 0 autotune, 1 .. 5 a schedule");
+            ctx->sweepTune = (int)value;
+            ctx->mesh.sm.tune[0] = ctx->mesh.sm.tune[1] = -1;
+            return RT_OK;
         case RT_OPT_MIXED_TIGHTEN:
             RT_REQUIRE(value >= 0 && value <= 12, RT_EINVAL, "RT_OPT_MIXED_TIGHTEN: decades 0 .. 12");
             ctx->mixedTighten = std::pow(10.0, -(double)value);
@@ -769,4 +776,19 @@ rt_status rt_device_bytes(int64_t *bytes) {
     if (!bytes) return RT_EINVAL;
     *bytes = (int64_t)device_bytes().load();
     return RT_OK;
+}
+
+rt_status rt_sweep_schedule(rt_ctx *ctx, int32_t *schedule) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(schedule, RT_EINVAL, "null argument");
+        const StructMesh &s = ctx->mesh.sm;
+        static const int P[5] = {8, 8, 16, 16, 4}, NB[5] = {3, 5, 3, 4, 6};
+        for (int i = 0; i < 2; ++i) {
+            const int k = s.tune[i];
+            schedule[3 * i] = k;
+            schedule[3 * i + 1] = k >= 0 ? P[k] : 0;
+            schedule[3 * i + 2] = k >= 0 ? NB[k] : 0;
+        }
+        return RT_OK;
+    });
 }

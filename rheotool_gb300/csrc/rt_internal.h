@@ -116,6 +116,8 @@ struct StructMesh {
     DBuf<int> sync;            // work counter, error flag
     DBuf<unsigned long long> xfer;   // tagged hand-off words between clusters
     unsigned epoch = 0;        // tag of the current launch's hand-off words
+    int tune[2] = {-1, -1};    // schedule of the one-component sweeps (FP64, FP32), -1 until tuned
+    float tuneMs[2] = {0, 0};  // its time per application
     DBuf<double> data;         // 12 + 6 + 6 arrays of nSkew doubles
     bool pendingCheck = false;
 
@@ -292,6 +294,7 @@ struct Prof {
 
 struct rt_ctx {
     int sweepMode = 0;           // 0 auto, 1 level-scheduled, 2 structured systolic
+    int sweepTune = 0;           // 0 autotune the sweep schedule, k > 0: candidate k - 1
     int device = 0;
     int numSMs = 0;
     cudaStream_t stream = nullptr;

@@ -128,7 +128,7 @@ __device__ __forceinline__ int wait_count(const volatile int *c, int need, int *
 
 // Ring depths (steps, powers of two) of the hand-offs for chunk size P.
 template <int P> struct Ring {
-    static constexpr int R = (P >= 4) ? 16 : 8;       // plane ring: at least two chunks
+    static constexpr int R = (P >= 16) ? 32 : (P >= 4) ? 16 : 8;   // plane ring: at least two chunks
     static constexpr int RJ = (P >= 8) ? 128 : 64;    // j-block ring: the consumer lags ~32 + P steps
 };
 
@@ -139,11 +139,11 @@ template <int MODE, int NC> struct Stage { static constexpr int NA = 4 + NC; };
 constexpr size_t kMaxSmem = 227 * 1024 - 1024;   // dynamic shared memory per CTA (static part kept free)
 constexpr int kPre = 8;                   // L2 prefetch distance (chunks)
 
-template <class Real, int MODE, int NC, int P>
+template <class Real, int MODE, int NC, int P, int NB = 3>
 size_t sweep_smem_bytes(int nJB) {
     constexpr int VW = NC * Words<Real>::W;
     const size_t rings = (size_t)nJB * (Ring<P>::R * 32 + Ring<P>::RJ) * VW * sizeof(u64);
-    const size_t stage = (size_t)nJB * 3 * P * 32 * (Stage<MODE, NC>::NA * sizeof(Real) + sizeof(int));
+    const size_t stage = (size_t)nJB * NB * P * 32 * (Stage<MODE, NC>::NA * sizeof(Real) + sizeof(int));
     return rings + stage;
 }
 
@@ -178,7 +178,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // on the dependent chain.  Invalid entries (outside the mesh, padding) have
 // zero coefficients and zero right-hand sides, so every lane runs the same
 // branch-free recurrence.
-template <class Real, int MODE, int NC, int P>
+template <class Real, int MODE, int NC, int P, int NB>
 __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
                                                   int *sync, u64 *__restrict__ xfer, unsigned epoch,
                                                   long long maxSpin) {
@@ -194,9 +194,9 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
     u64 *ringK = reinterpret_cast<u64 *>(smem_raw);                 // [nJB][R][32][VW], written by the k-producer
     u64 *ringJ = ringK + (size_t)nJB * R * 32 * VW;                  // [nJB][RJ][VW]
     Real *stage = reinterpret_cast<Real *>(ringJ + (size_t)nJB * RJ * VW);   // [nJB][3][P][NA][32]
-    int *cstage = (int *)(stage + (size_t)nJB * 3 * P * NA * 32);    // [nJB][3][P][32]
-    Real *myStage = stage + (size_t)jo * 3 * P * NA * 32;
-    int *myCStage = cstage + (size_t)jo * 3 * P * 32;
+    int *cstage = (int *)(stage + (size_t)nJB * NB * P * NA * 32);   // [nJB][NB][P][32]
+    Real *myStage = stage + (size_t)jo * NB * P * NA * 32;
+    int *myCStage = cstage + (size_t)jo * NB * P * 32;
     for (size_t i = threadIdx.x; i < (size_t)nJB * (R * 32 + RJ) * VW; i += blockDim.x) ringK[i] = 0ull;
     if (threadIdx.x < 16) { kBack[threadIdx.x] = 0; jProg[threadIdx.x] = 0; }
     if (r == 0 && threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
@@ -251,7 +251,6 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 copy_block(dst + 0 * P * 32, (MODE == 0 ? g.Az : g.Bz) + lo);
                 copy_block(dst + 1 * P * 32, (MODE == 0 ? g.Ay : g.By) + lo);
                 copy_block(dst + 2 * P * 32, (MODE == 0 ? g.Ax : g.Bx) + lo);
-                if (MODE == 0) copy_block(dst + 3 * P * 32, g.rDinv + lo);
 #pragma unroll
                 for (int q = 0; q < NC; ++q)
                     copy_block(dst + (size_t)(4 + q) * P * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo);
@@ -266,16 +265,17 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
         Real yprev[NC];
 #pragma unroll
         for (int q = 0; q < NC; ++q) yprev[q] = (MODE == 2) ? Real(1) : Real(0);
-        // three staging buffers: chunk c is staged two chunks ahead
-        stage_chunk(0, 0);
-        cp_async_commit();
-        if (P < T) stage_chunk(P, 1);
-        cp_async_commit();
+        // NB staging buffers: chunk c is staged NB - 1 chunks ahead
+#pragma unroll
+        for (int c = 0; c < NB - 1; ++c) {
+            if (c * P < T) stage_chunk(c * P, c);
+            cp_async_commit();
+        }
 
         for (int t0 = 0; t0 < T; t0 += P) {
             const int te = t0 + P;   // T is a multiple of P
-            const int buf = (t0 / P) % 3;
-            cp_async_wait<1>();      // this chunk's group is complete
+            const int buf = (t0 / P) % NB;
+            cp_async_wait<NB - 2>();   // this chunk's group is complete
             // ---- back-pressure: consumers have read what this chunk overwrites
             if (kLocalCons && seenCK < te - R) {
                 int v = 0;
@@ -304,7 +304,6 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                     prefetch_l2((MODE == 0 ? g.Az : g.Bz) + lo, bytes);
                     prefetch_l2((MODE == 0 ? g.Ay : g.By) + lo, bytes);
                     prefetch_l2((MODE == 0 ? g.Ax : g.Bx) + lo, bytes);
-                    if (MODE == 0) prefetch_l2(g.rDinv + lo, bytes);
 #pragma unroll
                     for (int q = 0; q < NC; ++q)
                         prefetch_l2((MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo, bytes);
@@ -375,7 +374,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 // entry of (step s, lane) inside the chunk's blocks
                 const int si = (MODE == 1) ? (P - 1 - s) * 32 + (31 - lane) : s * 32 + lane;
                 const Real *d = db + si;
-                const Real c0 = d[0], c3 = (MODE == 0) ? d[3 * P * 32] : Real(0);
+                const Real c0 = d[0];
                 cy[s] = (MODE == 2) ? d[2 * P * 32] : d[P * 32];
                 cx[s] = (MODE == 2) ? d[3 * P * 32] : d[2 * P * 32];
                 cell[s] = (MODE == 1) ? myCStage[buf * P * 32 + si] : 0;
@@ -385,9 +384,10 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                     if (MODE == 2) {
                         pre[s][q] = r_sub(c0, r_div(d[P * 32], wk));   // D - Pz / rD(k-1)
                     } else {
+                        // MODE 0: rk = rD r (premultiplied by the gather, the
+                        // sequential sweep's first product); MODE 1: rk = w
                         const Real rk = d[(size_t)(4 + q) * P * 32];
-                        const Real v0 = (MODE == 0) ? r_mul(c3, rk) : rk;
-                        pre[s][q] = r_fma(-c0, wk, v0);
+                        pre[s][q] = r_fma(-c0, wk, rk);
                     }
                 }
             }
@@ -408,15 +408,35 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                         v = r_fma(-cy[s], yj, pre[s][q]);
                         v = r_fma(-cx[s], yprev[q], v);
                     }
-                    if (kLocalCons)
-                        put(consRing + (((size_t)jo * R + (t & (R - 1))) * 32 + lane) * VW + q * W, v,
-                            (unsigned)(t + 1));
-                    if (consJ >= 0 && lane == 31)
-                        put(ringJ + ((size_t)jo * RJ + (t & (RJ - 1))) * VW + q * W, v, (unsigned)(t + 1));
-                    if (crossProducer) put(xslot(bOut, t, q), v, epoch);
                     out[s][q] = v;
                     yprev[q] = v;
                 }
+                (void)t;
+            }
+            // ---- publish the chunk's hand-off words (the consumers read whole
+            // chunks, so publishing per chunk costs them no latency and keeps
+            // the addressing off the dependent chain; a chunk never wraps a
+            // ring: R and RJ are multiples of P)
+            if (kLocalCons) {
+                u64 *base = consRing + (((size_t)jo * R + (t0 & (R - 1))) * 32 + lane) * VW;
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) put(base + s * 32 * VW + q * W, out[s][q], (unsigned)(t0 + s + 1));
+            }
+            if (consJ >= 0 && lane == 31) {
+                u64 *base = ringJ + ((size_t)jo * RJ + (t0 & (RJ - 1))) * VW;
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) put(base + s * VW + q * W, out[s][q], (unsigned)(t0 + s + 1));
+            }
+            if (crossProducer) {
+                u64 *base = xslot(bOut, t0, 0);
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) put(base + s * 32 * VW + q * W, out[s][q], epoch);
             }
             // ---- progress for the producers' back-pressure (after every lane
             // has consumed its hand-off values of this chunk)
@@ -426,7 +446,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 if (depJ >= 0) *(volatile int *)(jProg + jo) = te;
             }
             // ---- stage chunk c + 2 (always commit a group, possibly empty)
-            if (te + P < T) stage_chunk(te + P, ((t0 / P) + 2) % 3);
+            if (te + (NB - 2) * P < T) stage_chunk(te + (NB - 2) * P, ((t0 / P) + NB - 1) % NB);
             cp_async_commit();
             // ---- this chunk's results
 #pragma unroll
@@ -455,14 +475,17 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
     cluster.sync();
 }
 
-// rS = r gathered into the skewed layout (0 outside the mesh)
+// rS = rD r gathered into the skewed layout (0 outside the mesh): the first
+// product of the forward recurrence, rounded as the sequential sweep rounds it
 template <class Real>
 __global__ void k_skew_gather(SkewT<Real> g, unsigned mask, int nc, const Real *__restrict__ r, int N) {
     long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= g.nSkew) return;
     int c = g.cellOf[e];
+    const Real rd = g.rDinv[e];
     for (int q = 0; q < nc; ++q)
-        if ((mask >> q) & 1u) g.rS[(long long)q * g.nSkew + e] = c >= 0 ? r[(long long)q * N + c] : Real(0);
+        if ((mask >> q) & 1u)
+            g.rS[(long long)q * g.nSkew + e] = c >= 0 ? r_mul(rd, r[(long long)q * N + c]) : Real(0);
 }
 
 // gather the skewed per-entry coefficients of one matrix
@@ -519,15 +542,15 @@ __global__ void k_skew_to32(SkewView g, SkewView32 h) {
 
 namespace {
 
-template <class Real, int MODE, int NC, int P>
+template <class Real, int MODE, int NC, int P, int NB = 3>
 void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
     StructMesh &s = ctx->mesh.sm;
-    const size_t shm = sweep_smem_bytes<Real, MODE, NC, P>(g.nJB);
+    const size_t shm = sweep_smem_bytes<Real, MODE, NC, P, NB>(g.nJB);
     static size_t attr = 0;   // per instantiation: dynamic shared memory opted in so far
     if (shm > attr) {
-        RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)shm));
-        RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+        RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P, NB>, cudaFuncAttributeNonPortableClusterSizeAllowed,
                                      1));
         attr = shm;
     }
@@ -551,13 +574,54 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<Real, MODE, NC, P>, g, mask, w, ctx->mesh.N, s.sync.p, s.xfer.p,
+    RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<Real, MODE, NC, P, NB>, g, mask, w, ctx->mesh.N, s.sync.p, s.xfer.p,
                                s.epoch, 1ll << 24));
 }
 
+// Schedules of the one-component sweeps (the pressure solve): chunk size P
+// (steps per wait) and staging depth NB (chunks in flight); the autotuner
+// times the candidates that fit on the first application per mesh and
+// precision and keeps the fastest.
+constexpr int kTuneN = 5;
+constexpr int kTuneP[kTuneN] = {8, 8, 16, 16, 4};
+constexpr int kTuneNB[kTuneN] = {3, 5, 3, 4, 6};
+
+template <class Real, int MODE, int K>
+bool tune_fits(int nJB) {
+    return sweep_smem_bytes<Real, MODE, 1, kTuneP[K], kTuneNB[K]>(nJB) <= kMaxSmem;
+}
+template <class Real, int MODE>
+bool tune_fits_any(int k, int nJB) {
+    switch (k) {
+    case 0: return tune_fits<Real, MODE, 0>(nJB);
+    case 1: return tune_fits<Real, MODE, 1>(nJB);
+    case 2: return tune_fits<Real, MODE, 2>(nJB);
+    case 3: return tune_fits<Real, MODE, 3>(nJB);
+    default: return tune_fits<Real, MODE, 4>(nJB);
+    }
+}
+template <class Real, int MODE>
+void launch_tuned(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS, int k) {
+    switch (k) {
+    case 0: launch_one<Real, MODE, 1, kTuneP[0], kTuneNB[0]>(ctx, g, mask, w, CS); break;
+    case 1: launch_one<Real, MODE, 1, kTuneP[1], kTuneNB[1]>(ctx, g, mask, w, CS); break;
+    case 2: launch_one<Real, MODE, 1, kTuneP[2], kTuneNB[2]>(ctx, g, mask, w, CS); break;
+    case 3: launch_one<Real, MODE, 1, kTuneP[3], kTuneNB[3]>(ctx, g, mask, w, CS); break;
+    default: launch_one<Real, MODE, 1, kTuneP[4], kTuneNB[4]>(ctx, g, mask, w, CS); break;
+    }
+}
+
 // chunk size: the largest of 8, 4, 2, 1 steps whose staging and rings fit
+// (one component: the tuned schedule, if any)
 template <class Real, int MODE, int NC>
 void launch_fit(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
+    if constexpr (NC == 1 && MODE != 2) {
+        const int k = ctx->mesh.sm.tune[sizeof(Real) == 4 ? 1 : 0];
+        if (k >= 0 && tune_fits_any<Real, MODE>(k, g.nJB)) {
+            launch_tuned<Real, MODE>(ctx, g, mask, w, CS, k);
+            return;
+        }
+    }
     if constexpr (NC == 1) {
         if (sweep_smem_bytes<Real, MODE, NC, 8>(g.nJB) <= kMaxSmem) {
             launch_one<Real, MODE, NC, 8>(ctx, g, mask, w, CS);
@@ -612,11 +676,55 @@ void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const do
     launch_count(ctx);
 }
 
+namespace {
+
+// time every fitting schedule of the one-component sweeps on the current
+// right-hand side (two applications each, CUDA events) and keep the fastest
+template <class Real>
+void autotune(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w) {
+    StructMesh &s = ctx->mesh.sm;
+    int &choice = s.tune[sizeof(Real) == 4 ? 1 : 0];
+    if (choice >= 0) return;
+    if (ctx->sweepTune > 0) {   // forced (RT_OPT_SWEEP_TUNE)
+        choice = ctx->sweepTune - 1;
+        return;
+    }
+    cudaEvent_t a, b;
+    RT_CUDA(cudaEventCreate(&a));
+    RT_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    int bestK = 0;
+    for (int k = 0; k < kTuneN; ++k) {
+        if (!tune_fits_any<Real, 0>(k, g.nJB) || !tune_fits_any<Real, 1>(k, g.nJB)) continue;
+        choice = k;
+        for (int rep = 0; rep < 3; ++rep) {
+            if (rep == 1) RT_CUDA(cudaEventRecord(a, ctx->stream));
+            launch_mode<Real, 0>(ctx, g, 1, mask, w);
+            launch_mode<Real, 1>(ctx, g, 1, mask, w);
+        }
+        RT_CUDA(cudaEventRecord(b, ctx->stream));
+        RT_CUDA(cudaEventSynchronize(b));
+        float ms = 0.f;
+        RT_CUDA(cudaEventElapsedTime(&ms, a, b));
+        if (ms < best) {
+            best = ms;
+            bestK = k;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    choice = bestK;
+    s.tuneMs[sizeof(Real) == 4 ? 1 : 0] = best / 2;
+}
+
+}  // namespace
+
 void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
     SkewView g = ctx->mesh.sm.view();
     k_skew_gather<double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
+    if (nc == 1) autotune<double>(ctx, g, mask, w);
     launch_mode<double, 0>(ctx, g, nc, mask, w);
     launch_mode<double, 1>(ctx, g, nc, mask, w);
 }
@@ -636,6 +744,7 @@ void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, flo
     k_skew_gather<float><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
+    if (nc == 1) autotune<float>(ctx, g, mask, w);
     launch_mode<float, 0>(ctx, g, nc, mask, w);
     launch_mode<float, 1>(ctx, g, nc, mask, w);
 }

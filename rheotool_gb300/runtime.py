@@ -87,6 +87,13 @@ class Context:
         """abi.SWEEP_AUTO / SWEEP_LEVELS / SWEEP_SYSTOLIC for the DIC/DILU sweeps."""
         self.set_option(abi.RT_OPT_SWEEP, mode)
 
+    def sweep_schedule(self) -> dict:
+        """The tuned schedules of the one-component systolic sweeps."""
+        a = np.zeros(6, np.int32)
+        self._check(self.lib.rt_sweep_schedule(self._ctx, abi.iptr(a)), "rt_sweep_schedule")
+        return {"fp64": {"candidate": int(a[0]), "P": int(a[1]), "NB": int(a[2])},
+                "fp32": {"candidate": int(a[3]), "P": int(a[4]), "NB": int(a[5])}}
+
     def set_precision(self, precision: int):
         """abi.RT_PREC_FP64 / RT_PREC_MIXED for standalone ldu_solve calls
         (the time step takes its precision from the case control)."""
