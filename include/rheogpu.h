@@ -199,6 +199,10 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * first application per structured mesh and precision and keeps the fastest;
  * 1 .. 5 forces one (P, NB) of (8,3) (8,5) (16,3) (16,4) (4,6). */
 #define RT_OPT_SWEEP_TUNE 6
+/* RT_OPT_SWEEP_RING: deepest plane-to-plane ring of the systolic sweeps, in
+ * steps (a power of two, 8 .. 128; 0 = default 128).  Each launch takes the
+ * deepest ring up to this cap that fits the shared memory. */
+#define RT_OPT_SWEEP_RING 7
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);

@@ -30,6 +30,7 @@ RT_OPT_PRECISION = 3
 RT_OPT_MIXED_PARTS = 4
 RT_OPT_MIXED_TIGHTEN = 5
 RT_OPT_SWEEP_TUNE = 6
+RT_OPT_SWEEP_RING = 7
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {

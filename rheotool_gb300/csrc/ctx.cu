@@ -5,6 +5,7 @@
 #include <numeric>
 
 #include "rt_internal.h"
+#include "sweep.h"
 
 using namespace rt;
 
@@ -308,13 +309,14 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
                     for (int l = 0; l < 32; ++l) {
                         int i = t - l, j = jb * 32 + l;
                         if (i < 0 || i >= nx || j >= ny) continue;
-                        long long e = (((long long)k * s.nJB + jb) * s.T + t) * 32 + l;
+                        // quad layout: one lane's four consecutive steps are adjacent
+                        long long e = ((long long)k * s.nJB + jb) * s.T * 32 + (long long)(t >> 2) * 128 + l * 4 + (t & 3);
                         cellOf[(size_t)e] = at[((size_t)k * ny + j) * nx + i];
                     }
         upload_vec(ctx, cellOf, s.cellOf);
         upload_vec(ctx, lo, s.faceLo);
         upload_vec(ctx, hi, s.faceHi);
-        RT_REQUIRE(s.nJB <= 8, RT_EINVAL, "structured sweeps need ny <= 256");
+        RT_REQUIRE(s.nJB <= 8 && skew_fits(s.nJB), RT_EINVAL, "structured sweeps need ny <= 256");
         s.KC = std::max(1, std::min(nz, 8));   // planes (CTAs) per thread-block cluster
         s.sync.alloc(SYNC_PROGRESS + (size_t)nz * s.nJB);
         s.sync.zero(ctx->stream);
@@ -345,6 +347,12 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
         case RT_OPT_SWEEP_TUNE:
             RT_REQUIRE(value >= 0 && value <= 5, RT_EINVAL, "RT_OPT_SWEEP_TUNE: 0 autotune, 1 .. 5 a schedule");
             ctx->sweepTune = (int)value;
+            ctx->mesh.sm.tune[0] = ctx->mesh.sm.tune[1] = -1;
+            return RT_OK;
+        case RT_OPT_SWEEP_RING:
+            RT_REQUIRE(value == 0 || (value >= 8 && value <= 128 && (value & (value - 1)) == 0), RT_EINVAL,
+                       "RT_OPT_SWEEP_RING: 0, or a power of two 8 .. 128");
+            ctx->sweepRing = (int)value;
             ctx->mesh.sm.tune[0] = ctx->mesh.sm.tune[1] = -1;
             return RT_OK;
         case RT_OPT_MIXED_TIGHTEN:

@@ -92,7 +92,7 @@ struct DBuf {
 constexpr int SYNC_WORK = 0, SYNC_ERROR = 1, SYNC_PROGRESS = 2;
 
 // raw view passed to the kernels; every array has nSkew entries in the
-// skewed (block, step, lane) layout, wS has 6 components of nSkew
+// skewed (block, step / 4, lane, step % 4) layout, wS has 6 components of nSkew
 template <class Real>
 struct SkewT {
     int nx, ny, nz, nJB, T;
@@ -295,6 +295,7 @@ struct Prof {
 struct rt_ctx {
     int sweepMode = 0;           // 0 auto, 1 level-scheduled, 2 structured systolic
     int sweepTune = 0;           // 0 autotune the sweep schedule, k > 0: candidate k - 1
+    int sweepRing = 0;           // deepest plane ring of the systolic sweeps (steps; 0: the default cap)
     int device = 0;
     int numSMs = 0;
     cudaStream_t stream = nullptr;

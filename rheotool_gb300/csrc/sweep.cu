@@ -29,9 +29,10 @@
 // error flag, every other wait gives up on seeing it, and the host reports
 // RT_ETIMEOUT.
 //
-// Per-entry data live in a "skewed" layout, entry (block, step, lane), so the
-// 32 lanes of a step touch 32 consecutive values.  The backward sweep walks
-// the same layout in reverse (lanes mirrored).
+// Per-entry data live in a "skewed" layout of (block, step, lane) in which one
+// lane's four consecutive steps are adjacent (a quad), so a lane reads and
+// writes its coefficients, results and hand-off words as 16-byte vectors.
+// The backward sweep walks the same layout in reverse (lanes mirrored).
 #include <algorithm>
 
 #include <cooperative_groups.h>
@@ -59,14 +60,6 @@ template <class Real> struct Words;
 template <> struct Words<float> { static constexpr int W = 1; };
 template <> struct Words<double> { static constexpr int W = 2; };
 
-__device__ __forceinline__ void put_word(volatile u64 *p, unsigned payload, unsigned tag) {
-    *p = ((u64)tag << 32) | (u64)payload;
-}
-__device__ __forceinline__ void put(volatile u64 *p, float v, unsigned tag) { put_word(p, __float_as_uint(v), tag); }
-__device__ __forceinline__ void put(volatile u64 *p, double v, unsigned tag) {
-    put_word(p, (unsigned)__double2hiint(v), tag);
-    put_word(p + 1, (unsigned)__double2loint(v), tag);
-}
 __device__ __forceinline__ bool get(const volatile u64 *p, unsigned tag, float &v) {
     const u64 a = *p;
     if ((unsigned)(a >> 32) != tag) return false;
@@ -89,11 +82,6 @@ __device__ __forceinline__ bool unpack(const u64 *w, unsigned tag, double &v) {
     if ((unsigned)(w[0] >> 32) != tag || (unsigned)(w[1] >> 32) != tag) return false;
     v = __hiloint2double((int)(unsigned)w[0], (int)(unsigned)w[1]);
     return true;
-}
-
-// prefetch bytes (a multiple of 16, 16-byte aligned) into L2
-__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
 // bounded wait of one lane for a tagged value; false after a timeout or when
@@ -126,25 +114,41 @@ __device__ __forceinline__ int wait_count(const volatile int *c, int need, int *
     return v;
 }
 
-// Ring depths (steps, powers of two) of the hand-offs for chunk size P.
+// Ring depths (steps, powers of two) of the hand-offs for chunk size P.  The
+// plane ring is chosen per launch (at least R, at most kMaxRing): a producer
+// may run at most one ring ahead of its consumer, and with a ring of only two
+// chunks it waits one round trip (data forward, progress back) every chunk,
+// so the launch takes the deepest ring that fits the shared memory.
 template <int P> struct Ring {
     static constexpr int R = (P >= 16) ? 32 : (P >= 4) ? 16 : 8;   // plane ring: at least two chunks
     static constexpr int RJ = (P >= 8) ? 128 : 64;    // j-block ring: the consumer lags ~32 + P steps
 };
+constexpr int kMaxRing = 128;
 
-// Per-warp staging of a chunk's coefficients (cp.async, three buffers): NA
-// arrays of P steps x 32 lanes, plus the cells of the backward sweep.
-template <int MODE, int NC> struct Stage { static constexpr int NA = 4 + NC; };
+// Per-warp staging of a chunk's coefficients (cp.async, NB buffers): NA
+// arrays of P steps x 32 lanes (MODE 2: D, Pz, Py, Px; MODE 0/1: the z, y, x
+// coefficients and the NC right-hand sides), plus the cells of the backward
+// sweep.
+template <int MODE, int NC> struct Stage { static constexpr int NA = (MODE == 2) ? 4 : 3 + NC; };
 
 constexpr size_t kMaxSmem = 227 * 1024 - 1024;   // dynamic shared memory per CTA (static part kept free)
-constexpr int kPre = 8;                   // L2 prefetch distance (chunks)
 
 template <class Real, int MODE, int NC, int P, int NB = 3>
-size_t sweep_smem_bytes(int nJB) {
+size_t sweep_smem_bytes(int nJB, int R = Ring<P>::R) {
     constexpr int VW = NC * Words<Real>::W;
-    const size_t rings = (size_t)nJB * (Ring<P>::R * 32 + Ring<P>::RJ) * VW * sizeof(u64);
-    const size_t stage = (size_t)nJB * NB * P * 32 * (Stage<MODE, NC>::NA * sizeof(Real) + sizeof(int));
+    const size_t rings = (size_t)nJB * ((size_t)R * 32 + Ring<P>::RJ) * VW * sizeof(u64);
+    const size_t stage =
+        (size_t)nJB * NB * P * 32 * (Stage<MODE, NC>::NA * sizeof(Real) + (MODE == 1 ? sizeof(int) : 0));
     return rings + stage;
+}
+
+// the deepest plane ring (a power of two from Ring<P>::R up to cap, and no
+// deeper than the sweep) that fits the shared memory
+template <class Real, int MODE, int NC, int P, int NB = 3>
+int ring_depth(int nJB, int T, int cap) {
+    int R = Ring<P>::R;
+    while (2 * R <= cap && R < T && sweep_smem_bytes<Real, MODE, NC, P, NB>(nJB, 2 * R) <= kMaxSmem) R *= 2;
+    return R;
 }
 
 template <int BYTES>
@@ -156,12 +160,68 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// ---- pairs of tagged words (16-byte vector accesses; each 64-bit element is
+// single-copy atomic on its own, which is all the tag protocol needs)
+__device__ __forceinline__ void ld2_shared(unsigned a, u64 &x, u64 &y) {
+    asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(x), "=l"(y) : "r"(a) : "memory");
+}
+__device__ __forceinline__ void st2_shared(unsigned a, u64 x, u64 y) {
+    asm volatile("st.volatile.shared.v2.u64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
+}
+__device__ __forceinline__ void st2_cluster(unsigned a, u64 x, u64 y) {
+    asm volatile("st.volatile.shared::cluster.v2.u64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
+}
+__device__ __forceinline__ void ld2_global(const u64 *p, u64 &x, u64 &y) {
+    asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];" : "=l"(x), "=l"(y) : "l"(p) : "memory");
+}
+__device__ __forceinline__ void st2_global(u64 *p, u64 x, u64 y) {
+    asm volatile("st.volatile.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(x), "l"(y) : "memory");
+}
+__device__ __forceinline__ unsigned map_cluster(unsigned a, unsigned rank) {
+    unsigned m;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(m) : "r"(a), "r"(rank));
+    return m;
+}
+__device__ __forceinline__ void pack(float v, unsigned tag, u64 *w) { w[0] = ((u64)tag << 32) | __float_as_uint(v); }
+__device__ __forceinline__ void pack(double v, unsigned tag, u64 *w) {
+    w[0] = ((u64)tag << 32) | (unsigned)__double2hiint(v);
+    w[1] = ((u64)tag << 32) | (unsigned)__double2loint(v);
+}
+
+// ---- four consecutive steps of one lane (one quad of the skewed layout)
+__device__ __forceinline__ void ld4(const float *p, float *v) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double *v) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void ld4(const int *p, int *v) {
+    const int4 a = *reinterpret_cast<const int4 *>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void st4(float *p, const float *v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double *p, const double *v) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+}
+
 // MODE 0: forward application, 1: backward application, 2: rD recurrence
 // (FP64 only).
 //
-// The producer CTA of a plane writes each step's 32 lanes, tagged, straight
+// Skewed layout: the entry of (block, step t, lane l) is
+// block * 32 T + (t / 4) * 128 + l * 4 + t % 4, so one lane's four
+// consecutive steps are one 16-byte (FP32) or 32-byte (FP64) vector and one
+// chunk of P steps is one contiguous range of P x 32 entries.  The hand-off
+// rings use the same quad order, so a chunk's words are written and read
+// with 16-byte vector accesses.
+//
+// The producer CTA of a plane writes each chunk's 32 lanes, tagged, straight
 // into the consumer CTA's ring (distributed shared memory); each consumer lane
-// waits on its own slot.  The consumer reports its progress back into the
+// waits on its own words.  The consumer reports its progress back into the
 // producer's shared memory after each chunk, which bounds how far the
 // producer may run ahead (so a slot is never overwritten before it is read;
 // the two waits can never close a cycle).  The j-block hand-off stays inside
@@ -173,7 +233,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // of a CTA that has exited.
 //
 // Latency: a chunk's coefficients are staged into shared memory with cp.async
-// two chunks ahead; the terms of a step that do not depend on the previous
+// NB - 1 chunks ahead; the terms of a step that do not depend on the previous
 // step are formed for the whole chunk first, so only the j and i terms stay
 // on the dependent chain.  Invalid entries (outside the mesh, padding) have
 // zero coefficients and zero right-hand sides, so every lane runs the same
@@ -181,9 +241,12 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <class Real, int MODE, int NC, int P, int NB>
 __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
                                                   int *sync, u64 *__restrict__ xfer, unsigned epoch,
-                                                  long long maxSpin) {
-    constexpr int R = Ring<P>::R, RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA, W = Words<Real>::W;
+                                                  long long maxSpin, int R) {
+    static_assert(P % 4 == 0 && P <= 32, "a chunk is whole quads");
+    constexpr int RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA, W = Words<Real>::W;
     constexpr int VW = NC * W;   // words per (step, lane)
+    constexpr int QW = 4 * VW;   // words per (quad, lane)
+    constexpr int PQ = P / 4;    // quads per chunk
     cg::cluster_group cluster = cg::this_cluster();
     const int CS = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -191,10 +254,10 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
     __shared__ int kBack[16], jProg[16];
     const int lane = threadIdx.x & 31, jo = threadIdx.x >> 5;
     const int nJB = g.nJB;
-    u64 *ringK = reinterpret_cast<u64 *>(smem_raw);                 // [nJB][R][32][VW], written by the k-producer
+    u64 *ringK = reinterpret_cast<u64 *>(smem_raw);                 // [nJB][R/4][32][4][VW], written by the k-producer
     u64 *ringJ = ringK + (size_t)nJB * R * 32 * VW;                  // [nJB][RJ][VW]
-    Real *stage = reinterpret_cast<Real *>(ringJ + (size_t)nJB * RJ * VW);   // [nJB][3][P][NA][32]
-    int *cstage = (int *)(stage + (size_t)nJB * NB * P * NA * 32);   // [nJB][NB][P][32]
+    Real *stage = reinterpret_cast<Real *>(ringJ + (size_t)nJB * RJ * VW);   // [nJB][NB][NA][P * 32]
+    int *cstage = (int *)(stage + (size_t)nJB * NB * P * NA * 32);   // [nJB][NB][P * 32] (MODE 1)
     Real *myStage = stage + (size_t)jo * NB * P * NA * 32;
     int *myCStage = cstage + (size_t)jo * NB * P * 32;
     for (size_t i = threadIdx.x; i < (size_t)nJB * (R * 32 + RJ) * VW; i += blockDim.x) ringK[i] = 0ull;
@@ -209,8 +272,10 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
     const bool exists = grp < nGroups && k >= 0 && k < g.nz;
     if (exists) {
         const int jb = (MODE == 1) ? nJB - 1 - jo : jo;
+        const int lf = (MODE == 1) ? 31 - lane : lane;   // the lane's entry column in the forward layout
         const long long BS = (long long)T * 32;
         const int blk = k * nJB + jb;
+        const long long blk0 = (long long)blk * BS;
         const bool hasK = (MODE == 1) ? (k + 1 < g.nz) : (k > 0);
         const bool kLocalProd = hasK && r > 0;
         const bool kGlob = hasK && r == 0;
@@ -221,14 +286,17 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
         const int bIn = (MODE == 1) ? gi : gi - 1, bOut = (MODE == 1) ? gi - 1 : gi;
         const int depJ = (jo > 0) ? jo - 1 : -1;
         const int consJ = (jo + 1 < nJB) ? jo + 1 : -1;
-        u64 *consRing = kLocalCons ? cluster.map_shared_rank(ringK, r + 1) : nullptr;
+        const unsigned ringKs = (unsigned)__cvta_generic_to_shared(ringK);
+        const unsigned ringJs = (unsigned)__cvta_generic_to_shared(ringJ);
+        const unsigned consRing = kLocalCons ? map_cluster(ringKs, (unsigned)(r + 1)) : 0u;
         int *prodBack = kLocalProd ? cluster.map_shared_rank(kBack, r - 1) : nullptr;
-        // entry of step t: e0 + t * st
-        const long long e0 = (MODE == 1) ? (long long)blk * BS + (long long)(T - 1) * 32 + (31 - lane)
-                                         : (long long)blk * BS + lane;
-        const long long st = (MODE == 1) ? -32 : 32;
-        auto xslot = [&](int b, int t, int q) -> u64 * {
-            return xfer + ((((size_t)b * nJB + jb) * T + t) * 32 + lane) * VW + q * W;
+        // word index, in this warp's plane ring, of the quad holding step t of this lane
+        auto kword = [&](int t) -> unsigned {
+            return ((unsigned)(jo * (R >> 2) + ((t & (R - 1)) >> 2)) * 32u + (unsigned)lane) * QW;
+        };
+        // the same in the global hand-off at cluster boundary b
+        auto xword = [&](int b, int t) -> u64 * {
+            return xfer + ((((size_t)b * nJB + jb) * (T >> 2) + (t >> 2)) * 32 + lane) * QW;
         };
         // stage the coefficients of the chunk starting at step tc into buffer
         // b: the chunk's entries of one array are one contiguous block of
@@ -241,8 +309,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
             for (int i = lane; i < PIECES; i += 32) cp_async<16>(dst + i * EPC, src + i * EPC);
         };
         auto stage_chunk = [&](int tc, int b) {
-            const long long lo = (MODE == 1) ? (long long)blk * BS + (long long)(T - tc - P) * 32
-                                             : (long long)blk * BS + (long long)tc * 32;
+            const long long lo = (MODE == 1) ? blk0 + (long long)(T - tc - P) * 32 : blk0 + (long long)tc * 32;
             Real *dst = myStage + (size_t)b * NA * P * 32;
             if (MODE == 2) {
                 copy_block(dst + 0 * P * 32, g.D + lo); copy_block(dst + 1 * P * 32, g.Pz + lo);
@@ -253,7 +320,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 copy_block(dst + 2 * P * 32, (MODE == 0 ? g.Ax : g.Bx) + lo);
 #pragma unroll
                 for (int q = 0; q < NC; ++q)
-                    copy_block(dst + (size_t)(4 + q) * P * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo);
+                    copy_block(dst + (size_t)(3 + q) * P * 32, (MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo);
                 if (MODE == 1) {
 #pragma unroll
                     for (int i = lane; i < P * 8; i += 32)
@@ -291,49 +358,28 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 if (v < 0) { fail = 1; break; }
                 seenCJ = v;
             }
-            // ---- L2 prefetch of the chunk kPre chunks ahead (one lane, one
-            // contiguous range per array)
-            if (lane == 0 && t0 + kPre * P < T) {
-                const int tp = t0 + kPre * P;
-                const long long lo = (MODE == 1) ? e0 - 31 + (long long)(tp + P - 1) * st : e0 + (long long)tp * st;
-                const unsigned bytes = (unsigned)(P * 32 * sizeof(Real));
-                if (MODE == 2) {
-                    prefetch_l2(g.D + lo, bytes); prefetch_l2(g.Pz + lo, bytes);
-                    prefetch_l2(g.Py + lo, bytes); prefetch_l2(g.Px + lo, bytes);
-                } else {
-                    prefetch_l2((MODE == 0 ? g.Az : g.Bz) + lo, bytes);
-                    prefetch_l2((MODE == 0 ? g.Ay : g.By) + lo, bytes);
-                    prefetch_l2((MODE == 0 ? g.Ax : g.Bx) + lo, bytes);
-#pragma unroll
-                    for (int q = 0; q < NC; ++q)
-                        prefetch_l2((MODE == 0 ? g.rS : g.wS) + (long long)q * g.nSkew + lo, bytes);
-                    if (MODE == 1) prefetch_l2(g.cellOf + lo, (unsigned)(P * 32 * sizeof(int)));
-                }
-            }
             // ---- the hand-off values of the chunk: every load is issued
             // first, then the tags are checked (a word not there yet is waited for)
             Real wkv[P][NC], wjv[P][NC];
             bool ok = true;
             const Real zk = (MODE == 2) ? Real(1) : Real(0);
             if (kLocalProd || kGlob) {
-                u64 kw[P][VW];
+                u64 kw[PQ][QW];
 #pragma unroll
-                for (int s = 0; s < P; ++s) {
-                    const volatile u64 *src = kLocalProd
-                        ? ringK + (((size_t)jo * R + ((t0 + s) & (R - 1))) * 32 + lane) * VW
-                        : xslot(bIn, t0 + s, 0);
+                for (int qd = 0; qd < PQ; ++qd)
 #pragma unroll
-                    for (int j = 0; j < VW; ++j) kw[s][j] = src[j];
-                }
+                    for (int h = 0; h < QW / 2; ++h) {
+                        if (kLocalProd) ld2_shared(ringKs + 8u * (kword(t0 + 4 * qd) + 2 * h), kw[qd][2 * h], kw[qd][2 * h + 1]);
+                        else ld2_global(xword(bIn, t0 + 4 * qd) + 2 * h, kw[qd][2 * h], kw[qd][2 * h + 1]);
+                    }
 #pragma unroll
                 for (int s = 0; s < P; ++s)
 #pragma unroll
                     for (int q = 0; q < NC; ++q) {
                         const unsigned tag = kLocalProd ? (unsigned)(t0 + s + 1) : epoch;
-                        if (!unpack(&kw[s][q * W], tag, wkv[s][q])) {
-                            const volatile u64 *src = kLocalProd
-                                ? ringK + (((size_t)jo * R + ((t0 + s) & (R - 1))) * 32 + lane) * VW + q * W
-                                : xslot(bIn, t0 + s, q);
+                        const int wi = (s & 3) * VW + q * W;
+                        if (!unpack(&kw[s >> 2][wi], tag, wkv[s][q])) {
+                            const volatile u64 *src = kLocalProd ? ringK + kword(t0 + s) + wi : xword(bIn, t0 + s) + wi;
                             ok &= wait_get(src, tag, wkv[s][q], sync, kLocalProd ? maxSpin : maxSpin >> 4, kGlob);
                         }
                     }
@@ -364,38 +410,42 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                                 ok &= wait_get(ringJ + ((size_t)depJ * RJ + ((t0 + s + 31) & (RJ - 1))) * VW + q * W,
                                                (unsigned)(t0 + s + 32), wjv[s][q], sync, maxSpin, false);
             }
-            // ---- the terms that do not depend on the previous step
+            // ---- the terms that do not depend on the previous step (the
+            // staged quads of this lane, indexed by forward step offset)
             Real out[P][NC];
-            int cell[P];
+            int cell[P];   // MODE 1: the cells, by forward step offset
             Real pre[P][NC], cy[P], cx[P];
             const Real *db = myStage + (size_t)buf * NA * P * 32;
+            Real va[NA][P];
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int qd = 0; qd < PQ; ++qd) ld4(db + (size_t)a * P * 32 + qd * 128 + lf * 4, &va[a][4 * qd]);
+            if (MODE == 1) {
+#pragma unroll
+                for (int qd = 0; qd < PQ; ++qd) ld4(myCStage + buf * P * 32 + qd * 128 + lf * 4, &cell[4 * qd]);
+            }
 #pragma unroll
             for (int s = 0; s < P; ++s) {
-                // entry of (step s, lane) inside the chunk's blocks
-                const int si = (MODE == 1) ? (P - 1 - s) * 32 + (31 - lane) : s * 32 + lane;
-                const Real *d = db + si;
-                const Real c0 = d[0];
-                cy[s] = (MODE == 2) ? d[2 * P * 32] : d[P * 32];
-                cx[s] = (MODE == 2) ? d[3 * P * 32] : d[2 * P * 32];
-                cell[s] = (MODE == 1) ? myCStage[buf * P * 32 + si] : 0;
+                const int sf = (MODE == 1) ? P - 1 - s : s;
+                if (MODE == 2) {
+                    cy[s] = va[2][sf];
+                    cx[s] = va[3][sf];
+                    pre[s][0] = r_sub(va[0][sf], r_div(va[1][sf], wkv[s][0]));   // D - Pz / rD(k-1)
+                } else {
+                    const Real c0 = va[0][sf];
+                    cy[s] = va[1][sf];
+                    cx[s] = va[2][sf];
+                    // MODE 0: rk = rD r (premultiplied by the gather, the
+                    // sequential sweep's first product); MODE 1: rk = w
 #pragma unroll
-                for (int q = 0; q < NC; ++q) {
-                    const Real wk = wkv[s][q];
-                    if (MODE == 2) {
-                        pre[s][q] = r_sub(c0, r_div(d[P * 32], wk));   // D - Pz / rD(k-1)
-                    } else {
-                        // MODE 0: rk = rD r (premultiplied by the gather, the
-                        // sequential sweep's first product); MODE 1: rk = w
-                        const Real rk = d[(size_t)(4 + q) * P * 32];
-                        pre[s][q] = r_fma(-c0, wk, rk);
-                    }
+                    for (int q = 0; q < NC; ++q) pre[s][q] = r_fma(-c0, wkv[s][q], va[3 + q][sf]);
                 }
             }
             if (__any_sync(0xffffffffu, !ok)) { fail = 1; break; }
             // ---- the recurrence (order of operations of the sequential sweep)
 #pragma unroll
             for (int s = 0; s < P; ++s) {
-                const int t = t0 + s;
 #pragma unroll
                 for (int q = 0; q < NC; ++q) {
                     const Real yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
@@ -411,32 +461,37 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                     out[s][q] = v;
                     yprev[q] = v;
                 }
-                (void)t;
             }
             // ---- publish the chunk's hand-off words (the consumers read whole
             // chunks, so publishing per chunk costs them no latency and keeps
             // the addressing off the dependent chain; a chunk never wraps a
             // ring: R and RJ are multiples of P)
-            if (kLocalCons) {
-                u64 *base = consRing + (((size_t)jo * R + (t0 & (R - 1))) * 32 + lane) * VW;
+            if (kLocalCons || crossProducer) {
 #pragma unroll
-                for (int s = 0; s < P; ++s)
+                for (int qd = 0; qd < PQ; ++qd) {
+                    u64 wd[QW];
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) put(base + s * 32 * VW + q * W, out[s][q], (unsigned)(t0 + s + 1));
+                    for (int e = 0; e < 4; ++e)
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            pack(out[4 * qd + e][q], kLocalCons ? (unsigned)(t0 + 4 * qd + e + 1) : epoch,
+                                 &wd[e * VW + q * W]);
+#pragma unroll
+                    for (int h = 0; h < QW / 2; ++h) {
+                        if (kLocalCons) st2_cluster(consRing + 8u * (kword(t0 + 4 * qd) + 2 * h), wd[2 * h], wd[2 * h + 1]);
+                        else st2_global(xword(bOut, t0 + 4 * qd) + 2 * h, wd[2 * h], wd[2 * h + 1]);
+                    }
+                }
             }
             if (consJ >= 0 && lane == 31) {
-                u64 *base = ringJ + ((size_t)jo * RJ + (t0 & (RJ - 1))) * VW;
+                u64 wd[P * VW];
 #pragma unroll
                 for (int s = 0; s < P; ++s)
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) put(base + s * VW + q * W, out[s][q], (unsigned)(t0 + s + 1));
-            }
-            if (crossProducer) {
-                u64 *base = xslot(bOut, t0, 0);
+                    for (int q = 0; q < NC; ++q) pack(out[s][q], (unsigned)(t0 + s + 1), &wd[s * VW + q * W]);
+                const unsigned base = ringJs + 8u * (unsigned)(((jo * RJ) + (t0 & (RJ - 1))) * VW);
 #pragma unroll
-                for (int s = 0; s < P; ++s)
-#pragma unroll
-                    for (int q = 0; q < NC; ++q) put(base + s * 32 * VW + q * W, out[s][q], epoch);
+                for (int h = 0; h < P * VW / 2; ++h) st2_shared(base + 16u * h, wd[2 * h], wd[2 * h + 1]);
             }
             // ---- progress for the producers' back-pressure (after every lane
             // has consumed its hand-off values of this chunk)
@@ -445,21 +500,29 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 if (kLocalProd) *(volatile int *)(prodBack + jo) = te;
                 if (depJ >= 0) *(volatile int *)(jProg + jo) = te;
             }
-            // ---- stage chunk c + 2 (always commit a group, possibly empty)
+            // ---- stage chunk c + NB - 1 (always commit a group, possibly empty)
             if (te + (NB - 2) * P < T) stage_chunk(te + (NB - 2) * P, ((t0 / P) + NB - 1) % NB);
             cp_async_commit();
-            // ---- this chunk's results
+            // ---- this chunk's results: the forward sweeps write whole quads
+            // of the skewed layout, the backward sweep scatters to the cells
+            if (MODE == 1) {
 #pragma unroll
-            for (int s = 0; s < P; ++s) {
-                const long long e = e0 + (t0 + s) * st;
-                if (MODE == 2) {
-                    g.rDraw[e] = out[s][0];
-                } else {
+                for (int s = 0; s < P; ++s)
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) {
-                        if (!((mask >> q) & 1u)) continue;
-                        g.wS[(long long)q * g.nSkew + e] = out[s][q];
-                        if (MODE == 1 && cell[s] >= 0) w[(long long)q * N + cell[s]] = out[s][q];
+                    for (int q = 0; q < NC; ++q)
+                        if (((mask >> q) & 1u) && cell[P - 1 - s] >= 0) w[(long long)q * N + cell[P - 1 - s]] = out[s][q];
+            } else {
+                const long long e = blk0 + (long long)(t0 >> 2) * 128 + lane * 4;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) {
+                    if (MODE == 0 && !((mask >> q) & 1u)) continue;
+                    Real *dst = (MODE == 2) ? g.rDraw + e : g.wS + (long long)q * g.nSkew + e;
+#pragma unroll
+                    for (int qd = 0; qd < PQ; ++qd) {
+                        Real v4[4];
+#pragma unroll
+                        for (int x = 0; x < 4; ++x) v4[x] = out[4 * qd + x][q];
+                        st4(dst + qd * 128, v4);
                     }
                 }
             }
@@ -545,7 +608,8 @@ namespace {
 template <class Real, int MODE, int NC, int P, int NB = 3>
 void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
     StructMesh &s = ctx->mesh.sm;
-    const size_t shm = sweep_smem_bytes<Real, MODE, NC, P, NB>(g.nJB);
+    const int R = ring_depth<Real, MODE, NC, P, NB>(g.nJB, g.T, ctx->sweepRing > 0 ? ctx->sweepRing : kMaxRing);
+    const size_t shm = sweep_smem_bytes<Real, MODE, NC, P, NB>(g.nJB, R);
     static size_t attr = 0;   // per instantiation: dynamic shared memory opted in so far
     if (shm > attr) {
         RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -575,7 +639,7 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
     cfg.attrs = at;
     cfg.numAttrs = 1;
     RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<Real, MODE, NC, P, NB>, g, mask, w, ctx->mesh.N, s.sync.p, s.xfer.p,
-                               s.epoch, 1ll << 24));
+                               s.epoch, 1ll << 24, R));
 }
 
 // Schedules of the one-component sweeps (the pressure solve): chunk size P
@@ -611,53 +675,72 @@ void launch_tuned(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int
     }
 }
 
-// chunk size: the largest of 8, 4, 2, 1 steps whose staging and rings fit
-// (one component: the tuned schedule, if any)
+// the chunk schedule of an NC-component sweep: the tuned one (one
+// component), else chunks of 8 (one component) or 4 steps with three staging
+// buffers, else 4 steps with two; false when none fits
 template <class Real, int MODE, int NC>
-void launch_fit(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
+bool launch_fit(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
     if constexpr (NC == 1 && MODE != 2) {
         const int k = ctx->mesh.sm.tune[sizeof(Real) == 4 ? 1 : 0];
         if (k >= 0 && tune_fits_any<Real, MODE>(k, g.nJB)) {
             launch_tuned<Real, MODE>(ctx, g, mask, w, CS, k);
-            return;
+            return true;
         }
     }
     if constexpr (NC == 1) {
         if (sweep_smem_bytes<Real, MODE, NC, 8>(g.nJB) <= kMaxSmem) {
             launch_one<Real, MODE, NC, 8>(ctx, g, mask, w, CS);
-            return;
+            return true;
         }
     }
-    // (FP64 six-component chunks of 4 steps would spill registers)
-    if (!(sizeof(Real) == 8 && NC == 6) && sweep_smem_bytes<Real, MODE, NC, 4>(g.nJB) <= kMaxSmem) {
-        if constexpr (!(sizeof(Real) == 8 && NC == 6)) launch_one<Real, MODE, NC, 4>(ctx, g, mask, w, CS);
-    } else if (sweep_smem_bytes<Real, MODE, NC, 2>(g.nJB) <= kMaxSmem) launch_one<Real, MODE, NC, 2>(ctx, g, mask, w, CS);
-    else launch_one<Real, MODE, NC, 1>(ctx, g, mask, w, CS);
+    if (sweep_smem_bytes<Real, MODE, NC, 4>(g.nJB) <= kMaxSmem) {
+        launch_one<Real, MODE, NC, 4>(ctx, g, mask, w, CS);
+        return true;
+    }
+    if (sweep_smem_bytes<Real, MODE, NC, 4, 2>(g.nJB) <= kMaxSmem) {
+        launch_one<Real, MODE, NC, 4, 2>(ctx, g, mask, w, CS);
+        return true;
+    }
+    return false;
 }
 
+// the nc components of one sweep, in launches of as many components as fit
+// one CTA's shared memory (six in FP32, three, or one), on shifted views
 template <class Real, int MODE>
 void launch_mode(rt_ctx *ctx, const SkewT<Real> &g, int nc, unsigned mask, Real *w) {
     StructMesh &s = ctx->mesh.sm;
-    // the group counter restarts; the error flag stays until skew_check reads it
-    RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
     const int CS = s.KC;   // planes (CTAs) per cluster
-    if (MODE == 2 || nc == 1) launch_fit<Real, MODE, 1>(ctx, g, mask, w, CS);
-    else if constexpr (MODE != 2) {
-        if (nc <= 3) launch_fit<Real, MODE, 3>(ctx, g, mask, w, CS);
-        else if (sweep_smem_bytes<Real, MODE, 6, 1>(g.nJB) <= kMaxSmem) launch_fit<Real, MODE, 6>(ctx, g, mask, w, CS);
-        else {
-            // six components do not fit one CTA's shared memory (many
-            // j-blocks, FP64): two launches of three, on shifted views
-            launch_fit<Real, MODE, 3>(ctx, g, mask & 7u, w, CS);
-            SkewT<Real> h = g;
-            h.rS += 3 * g.nSkew;
-            h.wS += 3 * g.nSkew;
-            RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
-            launch_fit<Real, MODE, 3>(ctx, h, (mask >> 3) & 7u, w ? w + 3 * (size_t)ctx->mesh.N : w, CS);
+    // components c0 .. c0 + n - 1 in one launch; false (nothing launched)
+    // when they do not fit
+    auto part = [&](int c0, int n) -> bool {
+        const unsigned mc = (mask >> c0) & ((1u << n) - 1u);
+        if (!mc) return true;
+        SkewT<Real> h = g;
+        h.rS += (size_t)c0 * g.nSkew;
+        h.wS += (size_t)c0 * g.nSkew;
+        Real *wc = w ? w + (size_t)c0 * ctx->mesh.N : w;
+        // the group counter restarts; the error flag stays until skew_check reads it
+        RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
+        bool ok = false;
+        if (n == 1) ok = launch_fit<Real, MODE, 1>(ctx, h, mc, wc, CS);
+        else if constexpr (MODE != 2) {
+            if (n == 3) ok = launch_fit<Real, MODE, 3>(ctx, h, mc, wc, CS);
+            else if constexpr (sizeof(Real) == 4) ok = launch_fit<Real, MODE, 6>(ctx, h, mc, wc, CS);
         }
-    }
+        if (ok) launch_count(ctx, 2);
+        return ok;
+    };
+    auto singles = [&](int c0, int n) -> bool {
+        bool ok = true;
+        for (int c = c0; c < c0 + n && ok; ++c) ok = part(c, 1);
+        return ok;
+    };
+    bool ok;
+    if (MODE == 2 || nc == 1) ok = part(0, 1);
+    else if (nc <= 3) ok = part(0, 3) || singles(0, nc);
+    else ok = part(0, 6) || ((part(0, 3) || singles(0, 3)) && (part(3, 3) || singles(3, nc - 3)));
+    RT_REQUIRE(ok, RT_EINVAL, "the systolic sweep does not fit one CTA's shared memory");
     RT_CHECK_LAUNCH();
-    launch_count(ctx, 2);
     s.pendingCheck = true;
 }
 
@@ -747,6 +830,11 @@ void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, flo
     if (nc == 1) autotune<float>(ctx, g, mask, w);
     launch_mode<float, 0>(ctx, g, nc, mask, w);
     launch_mode<float, 1>(ctx, g, nc, mask, w);
+}
+
+bool skew_fits(int nJB) {
+    return nJB >= 1 && nJB <= 16 && sweep_smem_bytes<double, 2, 1, 4, 2>(nJB) <= kMaxSmem &&
+           sweep_smem_bytes<double, 0, 1, 4, 2>(nJB) <= kMaxSmem && sweep_smem_bytes<double, 1, 1, 4, 2>(nJB) <= kMaxSmem;
 }
 
 rt_status skew_check(rt_ctx *ctx) {

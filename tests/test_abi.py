@@ -25,6 +25,17 @@ def test_library_exports_every_declared_symbol():
             assert hasattr(lib, name), f"{name} declared in {os.path.basename(h)} is not exported"
 
 
+def test_header_constants_match_the_bindings():
+    """Every integer #define of the headers has the same value in abi.py."""
+    seen = 0
+    for h in headers():
+        for name, val in re.findall(r"^#define\s+(RT_\w+)\s+(-?\d+)\s*$", open(h).read(), re.M):
+            assert hasattr(abi, name), f"{name} missing from abi.py"
+            assert getattr(abi, name) == int(val), name
+            seen += 1
+    assert seen > 10
+
+
 def test_struct_layouts_match_the_c_compiler():
     from oracle import pyoracle
     L = pyoracle.lib()

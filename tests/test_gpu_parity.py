@@ -198,6 +198,7 @@ SWEEP_MESHES = {
     "cavity20": lambda: cavity_mesh(20),                              # one j-block, one plane
     "cavity70": lambda: cavity_mesh(70),                              # three j-blocks
     "contraction3d": lambda: contraction_mesh(12, 10, 30, 10, 6, 4.0, 4.0),   # holes, 2 j-blocks, 6 planes
+    "contraction3d_11": lambda: contraction_mesh(12, 10, 30, 10, 11, 4.0, 4.0),   # two clusters (8 + 3 planes)
 }
 
 
@@ -375,3 +376,32 @@ def test_unknown_model_is_rejected(ctx):
     case.model.type = "NoSuchModelLog"
     with pytest.raises(ValueError):
         ConstitutiveEq.New("", case, ctx)
+
+
+@pytest.mark.parametrize("tune,ring", [(1, 0), (2, 0), (3, 0), (4, 0), (5, 0), (5, 8), (3, 8)])
+def test_systolic_schedules_equal_level_sweeps(ctx, tune, ring):
+    """Every chunk schedule (chunk size, staging depth) and ring depth of the
+    one-component sweeps gives the level-scheduled bits, across a cluster
+    boundary (the global hand-off) and with the shallowest plane ring (the
+    producers wait on their consumers)."""
+    mesh = SWEEP_MESHES["contraction3d_11"]()
+    rng = np.random.default_rng(22)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=0.0)
+    b = rng.normal(size=(1, mesh.nCells)) * mesh.V
+    ctl = SolverControl("PCG", "DIC", 1e-12, 0.0, 0, 500)
+    ctx.upload_mesh(mesh)
+    out = {}
+    try:
+        ctx.set_option(abi.RT_OPT_SWEEP_TUNE, tune)
+        ctx.set_option(abi.RT_OPT_SWEEP_RING, ring)
+        for mode in (abi.SWEEP_LEVELS, abi.SWEEP_SYSTOLIC):
+            ctx.set_sweep(mode)
+            x = np.zeros((1, mesh.nCells))
+            perf = ctx.ldu_solve(diag, upper, lower, b, x, ctl)
+            out[mode] = (x, [p.nIterations for p in perf])
+    finally:
+        ctx.set_sweep(abi.SWEEP_AUTO)
+        ctx.set_option(abi.RT_OPT_SWEEP_TUNE, 0)
+        ctx.set_option(abi.RT_OPT_SWEEP_RING, 0)
+    assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
+    assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
