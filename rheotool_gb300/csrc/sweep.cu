@@ -73,17 +73,16 @@ __device__ __forceinline__ bool get(const volatile u64 *p, unsigned tag, double 
     return true;
 }
 
-__device__ __forceinline__ bool unpack(const u64 *w, unsigned tag, float &v) {
-    if ((unsigned)(w[0] >> 32) != tag) return false;
-    v = __uint_as_float((unsigned)w[0]);
-    return true;
-}
-__device__ __forceinline__ bool unpack(const u64 *w, unsigned tag, double &v) {
-    if ((unsigned)(w[0] >> 32) != tag || (unsigned)(w[1] >> 32) != tag) return false;
-    v = __hiloint2double((int)(unsigned)w[0], (int)(unsigned)w[1]);
-    return true;
-}
 
+// the value of a word pair, and whether it carries the tag (no branch)
+__device__ __forceinline__ bool peek(const u64 *w, unsigned tag, float &v) {
+    v = __uint_as_float((unsigned)w[0]);
+    return (unsigned)(w[0] >> 32) == tag;
+}
+__device__ __forceinline__ bool peek(const u64 *w, unsigned tag, double &v) {
+    v = __hiloint2double((int)(unsigned)w[0], (int)(unsigned)w[1]);
+    return ((unsigned)(w[0] >> 32) == tag) & ((unsigned)(w[1] >> 32) == tag);
+}
 // bounded wait of one lane for a tagged value; false after a timeout or when
 // another warp has failed (the error flag is then set)
 template <class Real>
@@ -220,8 +219,9 @@ __device__ __forceinline__ void st4(double *p, const double *v) {
 // with 16-byte vector accesses.
 //
 // The producer CTA of a plane writes each chunk's 32 lanes, tagged, straight
-// into the consumer CTA's ring (distributed shared memory); each consumer lane
-// waits on its own words.  The consumer reports its progress back into the
+// into the consumer CTA's ring (distributed shared memory: remote stores do
+// not wait, and the consumer's local loads are cheap); each consumer lane
+// checks its own words.  The consumer reports its progress back into the
 // producer's shared memory after each chunk, which bounds how far the
 // producer may run ahead (so a slot is never overwritten before it is read;
 // the two waits can never close a cycle).  The j-block hand-off stays inside
@@ -288,6 +288,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
         const int consJ = (jo + 1 < nJB) ? jo + 1 : -1;
         const unsigned ringKs = (unsigned)__cvta_generic_to_shared(ringK);
         const unsigned ringJs = (unsigned)__cvta_generic_to_shared(ringJ);
+        // the consumer plane's ring, written through distributed shared memory
         const unsigned consRing = kLocalCons ? map_cluster(ringKs, (unsigned)(r + 1)) : 0u;
         int *prodBack = kLocalProd ? cluster.map_shared_rank(kBack, r - 1) : nullptr;
         // word index, in this warp's plane ring, of the quad holding step t of this lane
@@ -372,17 +373,26 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                         if (kLocalProd) ld2_shared(ringKs + 8u * (kword(t0 + 4 * qd) + 2 * h), kw[qd][2 * h], kw[qd][2 * h + 1]);
                         else ld2_global(xword(bIn, t0 + 4 * qd) + 2 * h, kw[qd][2 * h], kw[qd][2 * h + 1]);
                     }
+                // every word checked in registers; one warp-uniform branch to
+                // the (rare) waits for words not there yet
+                const unsigned ktag = kLocalProd ? (unsigned)(t0 + 1) : epoch;
+                bool hit = true;
 #pragma unroll
                 for (int s = 0; s < P; ++s)
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) {
-                        const unsigned tag = kLocalProd ? (unsigned)(t0 + s + 1) : epoch;
-                        const int wi = (s & 3) * VW + q * W;
-                        if (!unpack(&kw[s >> 2][wi], tag, wkv[s][q])) {
+                    for (int q = 0; q < NC; ++q)
+                        hit &= peek(&kw[s >> 2][(s & 3) * VW + q * W], kLocalProd ? ktag + s : ktag, wkv[s][q]);
+                if (__any_sync(0xffffffffu, !hit)) {
+#pragma unroll
+                    for (int s = 0; s < P; ++s)
+#pragma unroll
+                        for (int q = 0; q < NC; ++q) {
+                            const int wi = (s & 3) * VW + q * W;
+                            const unsigned tag = kLocalProd ? ktag + s : ktag;
                             const volatile u64 *src = kLocalProd ? ringK + kword(t0 + s) + wi : xword(bIn, t0 + s) + wi;
                             ok &= wait_get(src, tag, wkv[s][q], sync, kLocalProd ? maxSpin : maxSpin >> 4, kGlob);
                         }
-                    }
+                }
             } else {
 #pragma unroll
                 for (int s = 0; s < P; ++s)
@@ -393,22 +403,33 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
             for (int s = 0; s < P; ++s)
 #pragma unroll
                 for (int q = 0; q < NC; ++q) wjv[s][q] = zk;
-            if (depJ >= 0 && lane == 0) {
-                u64 jw[P][VW];
+            if (depJ >= 0) {
+                // lane s < P fetches and checks the words of step t0 + 31 + s
+                // of the block below (in parallel), lane 0 gathers them
+                Real jv[NC];
 #pragma unroll
-                for (int s = 0; s < P; ++s)
+                for (int q = 0; q < NC; ++q) jv[q] = zk;
+                if (lane < P && t0 + lane + 31 < T) {
+                    const volatile u64 *src = ringJ + ((size_t)depJ * RJ + ((t0 + lane + 31) & (RJ - 1))) * VW;
+                    u64 jw[VW];
 #pragma unroll
-                    for (int j = 0; j < VW; ++j)
-                        jw[s][j] = (t0 + s + 31 < T) ? ringJ[((size_t)depJ * RJ + ((t0 + s + 31) & (RJ - 1))) * VW + j]
-                                                     : 0ull;
+                    for (int j = 0; j < VW; ++j) jw[j] = src[j];
+                    bool hit = true;
 #pragma unroll
-                for (int s = 0; s < P; ++s)
-                    if (t0 + s + 31 < T)
+                    for (int q = 0; q < NC; ++q) hit &= peek(&jw[q * W], (unsigned)(t0 + lane + 32), jv[q]);
+                    if (!hit) {
 #pragma unroll
                         for (int q = 0; q < NC; ++q)
-                            if (!unpack(&jw[s][q * W], (unsigned)(t0 + s + 32), wjv[s][q]))
-                                ok &= wait_get(ringJ + ((size_t)depJ * RJ + ((t0 + s + 31) & (RJ - 1))) * VW + q * W,
-                                               (unsigned)(t0 + s + 32), wjv[s][q], sync, maxSpin, false);
+                            ok &= wait_get(src + q * W, (unsigned)(t0 + lane + 32), jv[q], sync, maxSpin, false);
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < P; ++s)
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) {
+                        const Real v = __shfl_sync(0xffffffffu, jv[q], s);
+                        if (lane == 0) wjv[s][q] = v;
+                    }
             }
             // ---- the terms that do not depend on the previous step (the
             // staged quads of this lane, indexed by forward step offset)
