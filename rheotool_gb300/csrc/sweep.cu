@@ -405,24 +405,27 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 for (int q = 0; q < NC; ++q) wjv[s][q] = zk;
             if (depJ >= 0) {
                 // lane s < P fetches and checks the words of step t0 + 31 + s
-                // of the block below (in parallel), lane 0 gathers them
+                // of the block below (lanes past P repeat the last one), all
+                // in parallel; lane 0 gathers them by shuffles
+                const int ts = t0 + 31 + min(lane, P - 1);
+                const bool live = ts < T;   // steps past the row end read as zero
+                const volatile u64 *src = ringJ + ((size_t)depJ * RJ + (ts & (RJ - 1))) * VW;
+                u64 jw[VW];
+#pragma unroll
+                for (int j = 0; j < VW; ++j) jw[j] = src[j];
                 Real jv[NC];
+                bool hit = true;
 #pragma unroll
-                for (int q = 0; q < NC; ++q) jv[q] = zk;
-                if (lane < P && t0 + lane + 31 < T) {
-                    const volatile u64 *src = ringJ + ((size_t)depJ * RJ + ((t0 + lane + 31) & (RJ - 1))) * VW;
-                    u64 jw[VW];
-#pragma unroll
-                    for (int j = 0; j < VW; ++j) jw[j] = src[j];
-                    bool hit = true;
-#pragma unroll
-                    for (int q = 0; q < NC; ++q) hit &= peek(&jw[q * W], (unsigned)(t0 + lane + 32), jv[q]);
-                    if (!hit) {
+                for (int q = 0; q < NC; ++q) hit &= peek(&jw[q * W], (unsigned)(ts + 1), jv[q]);
+                if (__any_sync(0xffffffffu, live && !hit)) {
+                    if (live) {
 #pragma unroll
                         for (int q = 0; q < NC; ++q)
-                            ok &= wait_get(src + q * W, (unsigned)(t0 + lane + 32), jv[q], sync, maxSpin, false);
+                            ok &= wait_get(src + q * W, (unsigned)(ts + 1), jv[q], sync, maxSpin, false);
                     }
                 }
+#pragma unroll
+                for (int q = 0; q < NC; ++q) jv[q] = live ? jv[q] : zk;
 #pragma unroll
                 for (int s = 0; s < P; ++s)
 #pragma unroll
