@@ -1045,6 +1045,22 @@ struct Mixed : Solver {
         }
     }
 
+    // FP64 r -> FP32 preconditioner -> FP64 w (the structured sweeps round on
+    // the way in and out; otherwise through the FP32 vectors r32, w32)
+    void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32) {
+        if (systolic() && a.ctl.preconditioner != RT_PRECOND_NONE && a.ctl.preconditioner != RT_PRECOND_DIAGONAL) {
+            const double fpc = (double)ctx->mesh.F / N;
+            ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 16.0 + 24.0 * pop(mask)));
+            skew_precondition32d(ctx, a.nc, mask, r, w);
+            return;
+        }
+        k_mx_d2f<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, r, r32);
+        precondition32(mask, r32, w32);
+        k_mx_f2d<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, w32, w);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 2);
+    }
+
     void precondition32(unsigned mask, const float *r, float *w) {
         const DevMesh &m = ctx->mesh;
         const int pre = a.ctl.preconditioner;
@@ -1184,9 +1200,7 @@ rt_status run_pcg_flex32(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) 
     }
     int iter = 0;
     while (active) {
-        k_mx_d2f<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, rA, r32);
-        mx.precondition32(active, r32, z32);
-        k_mx_f2d<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, z32, zA);
+        mx.precondition32d(active, rA, zA, r32, z32);
         if (iter == 0) mx.dot(active, zA, rA);
         else mx.dot(active, zA, rA, zA, wA);   // wA = A p of the previous iteration
         k_mx_sc_pcg_a<<<1, 32, 0, mx.st>>>(active, iter == 0, ctx->red.result.p, mx.S);

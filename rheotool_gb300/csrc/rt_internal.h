@@ -102,6 +102,7 @@ struct SkewT {
     Real *rDinv, *Az, *Ay, *Ax, *Bz, *By, *Bx;
     Real *wS;   // 6 components
     Real *rS;   // 6 components
+    double *w64;   // backward sweep of the FP32 coefficients: FP64 output (cell order) instead of w, or null
 };
 using SkewView = SkewT<double>;
 using SkewView32 = SkewT<float>;
@@ -131,6 +132,7 @@ struct StructMesh {
         for (int i = 0; i < 12; ++i) *slots[i] = p + (size_t)i * nSkew;
         v.wS = p + (size_t)12 * nSkew;
         v.rS = p + (size_t)18 * nSkew;
+        v.w64 = nullptr;
         return v;
     }
 
@@ -149,6 +151,7 @@ struct StructMesh {
         for (int i = 0; i < 7; ++i) *slots[i] = p + (size_t)i * nSkew;
         v.wS = p + (size_t)7 * nSkew;
         v.rS = p + (size_t)13 * nSkew;
+        v.w64 = nullptr;
         return v;
     }
 };

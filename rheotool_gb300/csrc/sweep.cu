@@ -478,6 +478,10 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                     if (MODE == 2) {
                         v = r_sub(pre[s][q], r_div(cy[s], yj));
                         v = r_sub(v, r_div(cx[s], yprev[q]));
+                    } else if (sizeof(Real) == 4) {
+                        // FP32: the i term first, so only one product waits on the shuffle
+                        v = r_fma(-cx[s], yprev[q], pre[s][q]);
+                        v = r_fma(-cy[s], yj, v);
                     } else {
                         v = r_fma(-cy[s], yj, pre[s][q]);
                         v = r_fma(-cx[s], yprev[q], v);
@@ -530,11 +534,20 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
             // ---- this chunk's results: the forward sweeps write whole quads
             // of the skewed layout, the backward sweep scatters to the cells
             if (MODE == 1) {
+                if (g.w64) {
 #pragma unroll
-                for (int s = 0; s < P; ++s)
+                    for (int s = 0; s < P; ++s)
 #pragma unroll
-                    for (int q = 0; q < NC; ++q)
-                        if (((mask >> q) & 1u) && cell[P - 1 - s] >= 0) w[(long long)q * N + cell[P - 1 - s]] = out[s][q];
+                        for (int q = 0; q < NC; ++q)
+                            if (((mask >> q) & 1u) && cell[P - 1 - s] >= 0)
+                                g.w64[(long long)q * N + cell[P - 1 - s]] = (double)out[s][q];
+                } else {
+#pragma unroll
+                    for (int s = 0; s < P; ++s)
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            if (((mask >> q) & 1u) && cell[P - 1 - s] >= 0) w[(long long)q * N + cell[P - 1 - s]] = out[s][q];
+                }
             } else {
                 const long long e = blk0 + (long long)(t0 >> 2) * 128 + lane * 4;
 #pragma unroll
@@ -564,15 +577,16 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
 
 // rS = rD r gathered into the skewed layout (0 outside the mesh): the first
 // product of the forward recurrence, rounded as the sequential sweep rounds it
-template <class Real>
-__global__ void k_skew_gather(SkewT<Real> g, unsigned mask, int nc, const Real *__restrict__ r, int N) {
+// (an FP64 right-hand side of the FP32 sweeps is rounded first)
+template <class Real, class In>
+__global__ void k_skew_gather(SkewT<Real> g, unsigned mask, int nc, const In *__restrict__ r, int N) {
     long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= g.nSkew) return;
     int c = g.cellOf[e];
     const Real rd = g.rDinv[e];
     for (int q = 0; q < nc; ++q)
         if ((mask >> q) & 1u)
-            g.rS[(long long)q * g.nSkew + e] = c >= 0 ? r_mul(rd, r[(long long)q * N + c]) : Real(0);
+            g.rS[(long long)q * g.nSkew + e] = c >= 0 ? r_mul(rd, (Real)r[(long long)q * N + c]) : Real(0);
 }
 
 // gather the skewed per-entry coefficients of one matrix
@@ -742,6 +756,7 @@ void launch_mode(rt_ctx *ctx, const SkewT<Real> &g, int nc, unsigned mask, Real 
         SkewT<Real> h = g;
         h.rS += (size_t)c0 * g.nSkew;
         h.wS += (size_t)c0 * g.nSkew;
+        if (h.w64) h.w64 += (size_t)c0 * ctx->mesh.N;
         Real *wc = w ? w + (size_t)c0 * ctx->mesh.N : w;
         // the group counter restarts; the error flag stays until skew_check reads it
         RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
@@ -828,7 +843,7 @@ void autotune(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w) {
 
 void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
     SkewView g = ctx->mesh.sm.view();
-    k_skew_gather<double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
+    k_skew_gather<double, double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
     if (nc == 1) autotune<double>(ctx, g, mask, w);
@@ -848,7 +863,7 @@ void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const 
 
 void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, float *w) {
     SkewView32 g = ctx->mesh.sm.view32();
-    k_skew_gather<float><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
+    k_skew_gather<float, float><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
     if (nc == 1) autotune<float>(ctx, g, mask, w);
@@ -859,6 +874,17 @@ void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, flo
 bool skew_fits(int nJB) {
     return nJB >= 1 && nJB <= 16 && sweep_smem_bytes<double, 2, 1, 4, 2>(nJB) <= kMaxSmem &&
            sweep_smem_bytes<double, 0, 1, 4, 2>(nJB) <= kMaxSmem && sweep_smem_bytes<double, 1, 1, 4, 2>(nJB) <= kMaxSmem;
+}
+
+void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
+    SkewView32 g = ctx->mesh.sm.view32();
+    g.w64 = w;
+    k_skew_gather<float, double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    if (nc == 1) autotune<float>(ctx, g, mask, (float *)nullptr);
+    launch_mode<float, 0>(ctx, g, nc, mask, (float *)nullptr);
+    launch_mode<float, 1>(ctx, g, nc, mask, (float *)nullptr);
 }
 
 rt_status skew_check(rt_ctx *ctx) {

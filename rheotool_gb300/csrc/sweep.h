@@ -13,6 +13,8 @@ void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, doub
 void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
 // FP32 w = M^-1 r with the coefficients of the last skew_prepare32
 void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, float *w);
+// the same with an FP64 right-hand side and result (rounded on the way in and out)
+void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
 // whether the sweeps of a structured mesh with nJB j-blocks fit one CTA's shared memory
 bool skew_fits(int nJB);
 // RT_ETIMEOUT if a bounded wait of the last sweeps ran out

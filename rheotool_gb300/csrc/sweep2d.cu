@@ -129,8 +129,13 @@ __global__ void __launch_bounds__(1024) k_sweep2d(Skew2D<Real> g, unsigned mask,
                     v = r_sub(v, r_div(cx[s], yprev[q]));
                 } else {
                     const Real pre = (MODE == 0) ? r_mul(c0[s], rk[s][q]) : rk[s][q];
-                    v = r_fma(-cy[s], yj, pre);
-                    v = r_fma(-cx[s], yprev[q], v);
+                    if (sizeof(Real) == 4) {   // FP32: the i term first (as the 3-D sweeps)
+                        v = r_fma(-cx[s], yprev[q], pre);
+                        v = r_fma(-cy[s], yj, v);
+                    } else {
+                        v = r_fma(-cy[s], yj, pre);
+                        v = r_fma(-cx[s], yprev[q], v);
+                    }
                 }
                 if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * kRJ + (t & (kRJ - 1))) * NC + q] = v;
                 out[s][q] = v;
