@@ -545,8 +545,10 @@ struct Solver {
             k_diag_apply<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, rD, r, w);
             launch_count(ctx);
         } else if (systolic()) {
+            // per application: rD 8, coefficients 2*(F/N)*8 (premultiplied,
+            // no addressing), r 8 + w 8 + the forward result 16 per component
             const double fpc = (double)m.F / N;
-            ProfScope ps(ctx, "dilu_precondition", (double)N * (16.0 + fpc * 32.0 + 32.0 * pop(mask)));
+            ProfScope ps(ctx, "dilu_precondition", (double)N * (8.0 + fpc * 16.0 + 32.0 * pop(mask)));
             skew_precondition(ctx, a.nc, mask, r, w);
         } else {
             // per application (forward + backward): rD 16, coefficients
@@ -1050,7 +1052,8 @@ struct Mixed : Solver {
     void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32) {
         if (systolic() && a.ctl.preconditioner != RT_PRECOND_NONE && a.ctl.preconditioner != RT_PRECOND_DIAGONAL) {
             const double fpc = (double)ctx->mesh.F / N;
-            ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 16.0 + 24.0 * pop(mask)));
+            // (FP32 coefficients: rD 4, 2*(F/N)*4; FP64 r and w, FP32 forward result)
+            ProfScope ps(ctx, "dilu_precondition32", (double)N * (4.0 + fpc * 8.0 + 24.0 * pop(mask)));
             skew_precondition32d(ctx, a.nc, mask, r, w);
             return;
         }
@@ -1072,7 +1075,7 @@ struct Mixed : Solver {
             k_mx_diag_apply<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, rD32, r, w);
             launch_count(ctx);
         } else if (systolic()) {
-            ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 16.0 + 16.0 * pop(mask)));
+            ProfScope ps(ctx, "dilu_precondition32", (double)N * (4.0 + fpc * 8.0 + 16.0 * pop(mask)));
             skew_precondition32(ctx, a.nc, mask, r, w);
         } else {
             ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 24.0 + 16.0 * pop(mask)));
