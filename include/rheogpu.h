@@ -228,9 +228,9 @@ rt_status rt_residual(rt_ctx *ctx, const double *diag, const double *upper,
                       const double *psi, double *residual);
 
 /* rt_residual for callers that cannot allocate device memory (a solver
- * callback inside another library's Krylov loop, code being captured into a
- * CUDA graph by its owner, a host whose device memory belongs to its own
- * pool).  No reference counterpart: an addition of this library.  diag, upper,
+ * callback inside another library's Krylov loop, where a cudaMalloc would
+ * synchronise the device in the middle of that loop; a host whose device
+ * memory all belongs to its own pool allocator).  No reference counterpart: an addition of this library.  diag, upper,
  * lower, source and psi are DEVICE pointers on the context's device (nCells /
  * nFaces doubles); residual is a host pointer.  The reduction scratch is a
  * static device array inside the library, so the call allocates nothing; it

@@ -3,9 +3,9 @@
 //
 // Some callers cannot allocate device memory at the point where they need a
 // residual: a solver callback running inside another library's Krylov loop
-// (PETSc / Hypre style), code already being captured into a CUDA graph by its
-// owner, or an embedded host that has handed all device memory to a pool it
-// manages.  rt_residual (ctx.cu) copies host arrays into freshly allocated
+// (PETSc / Hypre style), where a cudaMalloc would synchronise the device in the
+// middle of that loop, or an embedded host that has handed all device memory
+// to a pool it manages.  rt_residual (ctx.cu) copies host arrays into freshly allocated
 // device buffers; rt_residual_noalloc takes device pointers and keeps its
 // reduction scratch in the file-scope array below, so it calls no cudaMalloc,
 // cudaFree or allocating library routine.

@@ -1,7 +1,7 @@
 """rt_residual_noalloc: the residual entry point for callers that cannot
-allocate device memory (a callback inside another library's Krylov loop, code
-already being captured into a CUDA graph, a host whose device memory is owned
-by its own pool).  The inputs live in device memory the test allocates; the
+allocate device memory (a callback inside another library's Krylov loop, where
+a cudaMalloc would synchronise the device mid-loop; a host whose device memory
+is all owned by its own pool allocator).  The inputs live in device memory the test allocates; the
 library allocates nothing and keeps its reduction scratch in a static device
 array.  Its result must equal rt_residual's (host arrays) to the round-off of
 a different reduction order, on two calls in a row (the second call reuses
