@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="form timed for `value` (the other is timed beside it unless --no-plain)")
     ap.add_argument("--no-plain", action="store_true", help="skip the second form")
+    ap.add_argument("--no-floor", action="store_true",
+                    help="skip the FP64 run with 100x tighter tolerances (the solver-tolerance floor)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched cavity sweep")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
     ap.add_argument("--batch-cases", type=int, default=512)
@@ -81,6 +83,24 @@ def make_case(small: bool):
     if small:
         return contraction_case(contraction_mesh(**SAMPLE_DIMS))
     return contraction_case()
+
+
+def rank_max(ms: float, pg) -> float:
+    """The slowest rank's time (every rank gets it), then a barrier; `pg` is
+    torch.distributed with a process group, or None for one rank."""
+    if pg is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.barrier()
+    return float(t[0])
+
+
+def whole_job_value(cells: int, steps: int, world: int, ms_max: float) -> float:
+    """Cell-steps/s of the whole job: every rank steps its own replica of the
+    case, so the units are cells x steps x ranks over the slowest rank's time."""
+    return cells * steps * world / (ms_max * 1e-3)
 
 
 def peaks():
@@ -320,12 +340,7 @@ def main():
         ms = ctx.timer_stop()
         launches = ctx.kernel_count() - k0
         clocks = clk.stop() if clk else None
-        if pg:
-            import torch
-            t = torch.tensor([ms], dtype=torch.float64)
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-            ms = float(t[0])
-            pg.barrier()
+        ms = rank_max(ms, pg)
         return ms, perf, launches, clocks
 
     def iters(perf):
@@ -336,25 +351,55 @@ def main():
     ms, perf, launches, clocks = timed(ctx, prec, True)
     schedule = ctx.sweep_schedule()
     total_cells = N * args.steps * world
-    value = total_cells / (ms * 1e-3)
+    value = whole_job_value(N, args.steps, world, ms)
 
     # ---- the other form on the same case, same steps; field differences ---
     second = None
     field_err = None
+    floor = None
+    names = ("U", "p", "phi", "theta", "tau")
+
+    def rel_err(got, ref):
+        return {n: float(np.linalg.norm(getattr(got, n) - getattr(ref, n))
+                         / max(np.linalg.norm(getattr(ref, n)), 1e-300)) for n in names}
+
     if not args.no_plain:
         ctx2 = Context(local)
         ms2, perf2, _, _ = timed(ctx2, other, False)
         a, b = ctx.fields(), ctx2.fields()
         ref, got = (b, a) if prec == abi.RT_PREC_MIXED else (a, b)
-        field_err = {}
-        for name in ("U", "p", "phi", "theta", "tau"):
-            x, y = getattr(got, name), getattr(ref, name)
-            field_err[name] = float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+        field_err = rel_err(got, ref)
         second = {"precision": "fp64" if other == abi.RT_PREC_FP64 else "mixed",
                   "value": total_cells / (ms2 * 1e-3), "ms_per_step": ms2 / args.steps,
                   "iterations_last_step": iters(perf2)}
         ctx2.close()
         case.precision = prec
+        if not args.no_floor:
+            # The FP64 form again with every Krylov tolerance 100x tighter: how far
+            # the FP64 fields at the case's own tolerances are from converged
+            # solves (the floor below which no two tolerance-stopped forms can
+            # agree), and how far each form is from those converged fields.
+            import copy
+            saved = case.solverU, case.solverP, case.solverTheta
+            tight = []
+            for s in saved:
+                t = copy.copy(s)
+                t.tolerance *= 1e-2
+                t.maxIter = max(5 * s.maxIter, 4000)
+                tight.append(t)
+            case.solverU, case.solverP, case.solverTheta = tight
+            ctx3 = Context(local)
+            ms3, perf3, _, _ = timed(ctx3, abi.RT_PREC_FP64, False)
+            c = ctx3.fields()
+            ctx3.close()
+            case.solverU, case.solverP, case.solverTheta = saved
+            case.precision = prec
+            fp64_f, mixed_f = (b, a) if prec == abi.RT_PREC_MIXED else (a, b)
+            floor = {"what": "relative L2 field differences after the same steps from the same state; "
+                             "'tight' = FP64 form with every Krylov tolerance x1e-2",
+                     "fp64_vs_fp64_tight": rel_err(fp64_f, c),
+                     "mixed_vs_fp64_tight": rel_err(mixed_f, c),
+                     "iterations_last_step_tight": iters(perf3), "ms_per_step_tight": ms3 / args.steps}
 
     # ---- roofline of the dominant operation (live CUDA events) ------------
     roof = None
@@ -445,7 +490,19 @@ def main():
             line[key] = second
             line["speedup_vs_" + key] = value / second["value"]
             line["field_error_vs_fp64"] = field_err
+        if floor is not None:
+            line["solver_tolerance_floor"] = floor
         line["profile_ms_2_steps"] = {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+        if prof:
+            peak, _ = peaks()
+            ops = {}
+            for k, (n, tms, by) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+                if k.startswith("solve_") or by <= 0 or n == 0:
+                    continue
+                gbs = (by / n) / (tms / n * 1e-3) / 1e9
+                ops[k] = {"launches": n, "avg_ms": round(tms / n, 5), "bytes_per_launch": by / n,
+                          "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+            line["roofline_per_operation"] = ops
         if batched is not None:
             line["batched"] = batched
         if served is not None:
