@@ -67,6 +67,10 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-steps", type=int, default=10)
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="instead of the throughput line: the precision sweep on the periodic PTT channel")
+    ap.add_argument("--sweep-dims", default="400x100x100", help="periodic channel cells nx x ny x nz")
+    ap.add_argument("--sweep-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -275,6 +279,68 @@ def run_served(args):
             "speedup_throughput": served["cell_steps_per_s"] / plain["cell_steps_per_s"]}
 
 
+def run_precision_sweep(args):
+    """Precision sweep: a channel periodic in x and z (4,000,000 cells by
+    default), linear PTT-Log (epsilon 0.25, zeta 0, beta 1/9), Wi in {0.5, 2,
+    8}, laminar velocity profile and a seeded lognormal initial conformation
+    (theta = Q diag(0.1 z) Q^T, z ~ N(0, 1)^3, Q Haar-random; seed 20261203).
+    For each Wi the same steps run in three forms from the same state: the
+    FP64 plain form, the mixed form (FP32 Krylov iterations and sweeps, FP64
+    residual replacement; FP32 constitutive algebra with FP64 eigen-solve
+    fallback and exp back-transformation), and the FP64 form with every
+    Krylov tolerance 100x tighter.  Reported per field: relative L2 of mixed
+    vs FP64, of FP64 vs the tight FP64 (the solver-tolerance floor) and of
+    mixed vs the tight FP64; and the device-timed cell-steps/s of each form."""
+    import copy
+    import numpy as np
+    from rheotool_gb300 import abi
+    from rheotool_gb300.case import SolverControl, periodic_channel_case, periodic_channel_state
+    from rheotool_gb300.mesh import periodic_channel_mesh
+    from rheotool_gb300.runtime import Context
+    nx, ny, nz = (int(v) for v in args.sweep_dims.lower().split("x"))
+    mesh = periodic_channel_mesh(nx, ny, nz)
+    N = mesh.nCells
+    names = ("U", "p", "phi", "theta", "tau")
+    ctx = Context(0)
+    result = {}
+    for Wi in (0.5, 2.0, 8.0):
+        case = periodic_channel_case(mesh, Wi=Wi)
+        f0 = periodic_channel_state(case, sigma=0.1, seed=20261203)
+        runs = {}
+        for form in ("fp64", "mixed", "fp64_tight"):
+            c = copy.copy(case)
+            c.precision = abi.RT_PREC_MIXED if form == "mixed" else abi.RT_PREC_FP64
+            if form == "fp64_tight":
+                c.solverU, c.solverP, c.solverTheta = [
+                    SolverControl(x.solver, x.preconditioner, x.tolerance * 1e-2, x.relTol, x.minIter,
+                                  max(5 * x.maxIter, 4000)) for x in (case.solverU, case.solverP, case.solverTheta)]
+            ctx.setup_case(c, f0.copy())
+            ctx.sync()
+            ctx.timer_start()
+            perf = ctx.step(args.sweep_steps)
+            ms = ctx.timer_stop()
+            runs[form] = (ctx.fields(), ms, perf)
+        err = lambda a, b: {n: float(np.linalg.norm(getattr(a, n) - getattr(b, n))
+                                     / max(np.linalg.norm(getattr(b, n)), 1e-300)) for n in names}
+        f64, fmx, ftt = runs["fp64"][0], runs["mixed"][0], runs["fp64_tight"][0]
+        result[f"Wi={Wi:g}"] = {
+            "mixed_vs_fp64": err(fmx, f64), "fp64_vs_fp64_tight": err(f64, ftt),
+            "mixed_vs_fp64_tight": err(fmx, ftt),
+            "cell_steps_per_s": {k: N * args.sweep_steps / (v[1] * 1e-3) for k, v in runs.items()},
+            "p_iterations_last_step": {k: v[2].p.nIterations for k, v in runs.items()},
+            "theta_max_abs": float(np.abs(f64.theta).max()),
+        }
+    ctx.close()
+    line = {"metric": "per-field relative L2 error of the mixed form vs the FP64 form (precision sweep)",
+            "config": {"workload": f"3-D channel periodic in x and z, {nx}x{ny}x{nz} = {N:,} cells, walls at y=+-1, "
+                                   "body-force driven (mean velocity 1), PTT-Log linear epsilon=0.25 zeta=0, "
+                                   "beta=1/9, rho=0.01, dt=5e-3, Euler, GaussDefCmpw cubista, p PCG-DIC 1e-8, "
+                                   "U/theta PBiCGStab-DILU 1e-10; theta0 = Q diag(0.1 z) Q^T seeded lognormal",
+                       "steps": args.sweep_steps, "cells": N},
+            "data": "synthetic", "results": result}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -308,6 +374,10 @@ def main():
     rank, world, local = dist()
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.precision_sweep:
+        if rank == 0:
+            run_precision_sweep(args)
         return
     import numpy as np
     from rheotool_gb300 import abi

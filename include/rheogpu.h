@@ -71,6 +71,18 @@ typedef struct {
     const double *bDeltaCoeffs;                 /* nB 1/|Cf - C_P|             */
     const int32_t *patchStart, *patchSize;      /* nPatches                    */
     int32_t solveDir[3];                        /* 0 for an empty direction    */
+    /* Cyclic (periodic) patch pairs.  OpenFOAM keeps a cyclic face pair as
+     * boundary faces whose implicit coefficients act through an lduInterface
+     * (cyclicFvPatch, cyclicLduInterface): they enter A x and the residual,
+     * but not the DIC/DILU factorisation or sweeps.  Here each pair is one
+     * internal face (owner < neighbour, in upper-triangular order like the
+     * others) with coupled[f] = 1: every operator treats it as the internal
+     * face across the periodic boundary, and the preconditioners skip it,
+     * which is the interface treatment.  delta[3f..3f+2] is C_N - C_P across
+     * each face, with the neighbour translated by the period for coupled
+     * faces; NULL means C[N] - C[P].  coupled == NULL: no coupled faces.     */
+    const double *delta;                        /* 3*nFaces or NULL            */
+    const int32_t *coupled;                     /* nFaces flags or NULL        */
 } rt_mesh_desc;
 
 /* ---- boundary conditions (one kind per patch and field) ---------------- */
@@ -144,6 +156,10 @@ typedef struct {
     double pRefValue;
     rt_solver_ctl solverU, solverP, solverTheta;
     int32_t precision, pad_;
+    /* uniform body force per unit mass in the momentum equation (the source
+     * an fvOptions meanVelocityForce / pressure-gradient source adds to UEqn
+     * to drive a periodic channel); zero for the other cases                */
+    double bodyForce[3];
 } rt_case_ctl;
 
 typedef struct {

@@ -42,7 +42,12 @@
  *   - CG (Hestenes & Stiefel 1952), BiCGStab (van der Vorst 1992), D-ILU(0)
  *     with the diagonal chosen so that diag(M) = diag(A) (Pommerell 1992),
  *     applied as a forward and a backward substitution in face order;
- *   - cyclic Jacobi eigenvalue method with Rutishauser's rotation formulas.
+ *   - cyclic Jacobi eigenvalue method with Rutishauser's rotation formulas;
+ *   - cyclic (periodic) patches: each face pair is an internal face whose
+ *     neighbour centre is translated by the period (weights, deltaCoeffs and
+ *     C_N - C_P from the translated geometry); its coefficients act in A x
+ *     and in the residual but not in the DIC/DILU factorisation or sweeps,
+ *     which is how an lduInterface coupling enters OpenFOAM's solvers.
  *
  * Parity status: the reference needs OpenFOAM v9 and Eigen, neither of which
  * exists here, so this restatement is pinned only by closed-form solutions
@@ -233,6 +238,7 @@ static void dilu_rd(const rt_mesh_desc *m, const double *diag, const double *upp
                     const double *lower, double *rD) {
     for (int c = 0; c < m->nCells; ++c) rD[c] = diag[c];
     for (int f = 0; f < m->nFaces; ++f) {
+        if (m->coupled && m->coupled[f]) continue;   /* interface: not factorised */
         int l = m->owner[f], u = m->neighbour[f];
         rD[u] -= upper[f] * lower[f] / rD[l];
     }
@@ -247,10 +253,12 @@ static void precondition(const rt_mesh_desc *m, int type, const double *rD,
     for (int c = 0; c < N; ++c) w[c] = rD[c] * r[c];
     if (type == RT_PRECOND_DIAGONAL) return;
     for (int f = 0; f < m->nFaces; ++f) {
+        if (m->coupled && m->coupled[f]) continue;   /* interfaces stay out of the sweeps */
         int l = m->owner[f], u = m->neighbour[f];
         w[u] -= rD[u] * lower[f] * w[l];
     }
     for (int f = m->nFaces - 1; f >= 0; --f) {
+        if (m->coupled && m->coupled[f]) continue;
         int l = m->owner[f], u = m->neighbour[f];
         w[l] -= rD[l] * upper[f] * w[u];
     }
@@ -543,8 +551,9 @@ static void defcmpw(const rt_mesh_desc *m, int scheme, const double *phi, const 
         gauss_grad(m, x, xb, nc, k, g);
         for (int f = 0; f < nF; ++f) {
             int o = m->owner[f], n = m->neighbour[f];
-            double d[3] = {m->C[3 * n] - m->C[3 * o], m->C[3 * n + 1] - m->C[3 * o + 1],
-                           m->C[3 * n + 2] - m->C[3 * o + 2]};
+            double d[3];
+            for (int i = 0; i < 3; ++i)   /* C_N - C_P; across a cyclic face, the translated one */
+                d[i] = m->delta ? m->delta[3 * f + i] : m->C[3 * n + i] - m->C[3 * o + i];
             double u = upw[f];
             double gu[3];
             for (int i = 0; i < 3; ++i) gu[i] = g[3 * o + i] * u + (1.0 - u) * g[3 * n + i];
@@ -950,8 +959,10 @@ static int step_once(or_case *k, rt_step_perf *perf) {
             }
         }
     }
+    /* explicit divTau terms plus the uniform body force per unit mass (the
+     * pressure-gradient source that drives a periodic channel) */
     for (int c = 0; c < N; ++c)
-        for (int j = 0; j < 3; ++j) UE.source[3 * c + j] += m->V[c] * expl[3 * c + j];
+        for (int j = 0; j < 3; ++j) UE.source[3 * c + j] += m->V[c] * (expl[3 * c + j] + ctl->bodyForce[j]);
 
     /* solve(UEqn == -grad(p)) */
     double *gp = DALLOC(3 * (size_t)N);

@@ -60,6 +60,7 @@ class rt_mesh_desc(C.Structure):
         ("bCell", _ip), ("bSf", _dp), ("bmagSf", _dp), ("bCf", _dp), ("bDeltaCoeffs", _dp),
         ("patchStart", _ip), ("patchSize", _ip),
         ("solveDir", C.c_int32 * 3),
+        ("delta", _dp), ("coupled", _ip),
     ]
 
 
@@ -106,6 +107,7 @@ class rt_case_ctl(C.Structure):
         ("pRefValue", C.c_double),
         ("solverU", rt_solver_ctl), ("solverP", rt_solver_ctl), ("solverTheta", rt_solver_ctl),
         ("precision", C.c_int32), ("pad_", C.c_int32),
+        ("bodyForce", C.c_double * 3),
     ]
 
 

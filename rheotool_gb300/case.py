@@ -19,7 +19,7 @@ from typing import Callable, Dict, Optional, Tuple, Union
 import numpy as np
 
 from . import abi
-from .mesh import Mesh, cavity_mesh, contraction_mesh, channel_mesh
+from .mesh import Mesh, cavity_mesh, contraction_mesh, channel_mesh, periodic_channel_mesh
 
 BC_KINDS = {"fixedValue": abi.RT_BC_FIXED, "zeroGradient": abi.RT_BC_ZEROGRAD,
             "linearExtrapolation": abi.RT_BC_LINEXTRAP}
@@ -85,6 +85,7 @@ class Case:
     pRefValue: float = 0.0
     precision: int = abi.RT_PREC_FP64
     name: str = "case"
+    bodyForce: Tuple[float, float, float] = (0.0, 0.0, 0.0)   # per unit mass, in UEqn
 
     # ------------------------------------------------------------------
     def _field_bc(self, fld: str, ncomp: int):
@@ -134,6 +135,10 @@ class Case:
         md.patchSize = i(np.array([p.size for p in m.patches]))
         for k in range(3):
             md.solveDir[k] = int(m.solveDir[k])
+        if m.delta is not None:
+            md.delta = d(m.delta)
+        if m.coupled is not None:
+            md.coupled = i(m.coupled)
 
         kU, Ub = self._field_bc("U", 3)
         kP, pb = self._field_bc("p", 1)
@@ -152,6 +157,8 @@ class Case:
         ctl.solverP = self.solverP.to_c()
         ctl.solverTheta = self.solverTheta.to_c()
         ctl.precision = self.precision
+        for k in range(3):
+            ctl.bodyForce[k] = float(self.bodyForce[k])
         self._keep = keep
         return md, bd, mp, ctl
 
@@ -217,6 +224,82 @@ def channel_case(mesh: Optional[Mesh] = None, model: str = "Oldroyd-BLog", U_in:
         "walls": dict(WALL_VE),
     }
     return Case(mesh, mdl, bcs, deltaT=dt, name=f"channel_{model}")
+
+
+def periodic_channel_case(mesh: Optional[Mesh] = None, model: str = "PTTLog", Wi: float = 2.0,
+                          beta: float = 1.0 / 9.0, rho: float = 0.01, U_mean: float = 1.0,
+                          H: float = 1.0, dt: float = 5e-3, epsilon: float = 0.25, **model_kw) -> Case:
+    """Channel periodic in x and z between walls at y = +-H, driven by a
+    uniform streamwise body force (the mean pressure gradient).  The force is
+    the one that gives a Newtonian fluid of the same total viscosity the mean
+    velocity U_mean: g = 3 (etaS + etaP) U_mean / (rho H^2).  lambda = Wi H /
+    U_mean.  The default model is the linear PTT (epsilon 0.25, zeta 0).  The
+    walls are the only patch, so p needs a reference cell."""
+    mesh = mesh if mesh is not None else periodic_channel_mesh()
+    eta0 = 1.0
+    kw = dict(model_kw)
+    if model == "PTTLog":
+        kw.setdefault("epsilon", epsilon)
+    mdl = Model(model, rho=rho, etaS=beta * eta0, etaP=(1.0 - beta) * eta0, lambda_=Wi * H / U_mean, **kw)
+    bcs = {"walls": dict(WALL_VE)}
+    g = 3.0 * eta0 * U_mean / (rho * H * H)
+    return Case(mesh, mdl, bcs, deltaT=dt, name=f"periodicChannel{mesh.nCells}_{model}_Wi{Wi:g}",
+                bodyForce=(g, 0.0, 0.0))
+
+
+def lognormal_conformation(n: int, sigma: float = 0.1, seed: int = 20261203):
+    """Per-cell log-conformation theta = Q diag(sigma z) Q^T with z ~ N(0, 1)^3
+    and Q a Haar-random rotation (QR of a Gaussian matrix, signs fixed), so
+    that A = exp(theta) = I + a lognormal perturbation, always SPD.  Returns
+    theta (n, 6; xx xy xz yy yz zz), eigVals = exp(mu) ascending (n, 3) and
+    eigVecs (n, 9; row-major, eigenvectors as columns), the state calcEig
+    leaves behind."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mu = sigma * rng.standard_normal((n, 3))
+    G = rng.standard_normal((n, 3, 3))
+    Q, R = np.linalg.qr(G)
+    Q = Q * np.sign(np.diagonal(R, axis1=1, axis2=2))[:, None, :]
+    order = np.argsort(mu, axis=1)
+    mu = np.take_along_axis(mu, order, axis=1)
+    Q = np.take_along_axis(Q, order[:, None, :], axis=2)
+    T = np.einsum("nij,nj,nkj->nik", Q, mu, Q)
+    theta = np.stack([T[:, 0, 0], T[:, 0, 1], T[:, 0, 2], T[:, 1, 1], T[:, 1, 2], T[:, 2, 2]], axis=1)
+    return np.ascontiguousarray(theta), np.exp(mu), np.ascontiguousarray(Q.reshape(n, 9))
+
+
+def periodic_channel_state(case: "Case", sigma: float = 0.1, seed: int = 20261203) -> "Fields":
+    """Initial state of the periodic channel: the laminar Newtonian profile
+    u = 1.5 U_mean (1 - y^2/H^2) (with its face fluxes), p = 0, and the
+    lognormal log-conformation of `lognormal_conformation` with the matching
+    eigen-decomposition and tau = etaP/(lambda (1 - zeta)) (A - I)
+    (Oldroyd-B, Giesekus and PTT; zeta = 0 but for PTT).  Boundary values of
+    theta and tau are the wall cells' values."""
+    m = case.mesh
+    md = case.model
+    if md.type == "FENE-PLog":
+        raise ValueError("the lognormal initial state is defined for Oldroyd-B, Giesekus and PTT")
+    N = m.nCells
+    f = Fields.zeros(m)
+    H = float(np.abs(m.bCf[:, 1]).max())
+    g = case.bodyForce[0]
+    U_mean = g * md.rho * H * H / (3.0 * (md.etaS + md.etaP))
+    y = m.C[:, 1]
+    f.U[:, 0] = 1.5 * U_mean * (1.0 - (y / H) ** 2)
+    Uf = m.w[:, None] * (f.U[m.owner] - f.U[m.neighbour]) + f.U[m.neighbour]
+    f.phi[:] = (m.Sf * Uf).sum(1)
+    th, ev, vv = lognormal_conformation(N, sigma, seed)
+    f.theta[:] = th
+    f.eigVals[:] = ev
+    f.eigVecs[:] = vv
+    R = vv.reshape(N, 3, 3)
+    A = np.einsum("nij,nj,nkj->nik", R, ev, R)
+    zeta = md.zeta if md.type == "PTTLog" else 0.0
+    c = md.etaP / (md.lambda_ * (1.0 - zeta))
+    T = c * (A - np.eye(3)[None])
+    f.tau[:] = np.stack([T[:, 0, 0], T[:, 0, 1], T[:, 0, 2], T[:, 1, 1], T[:, 1, 2], T[:, 2, 2]], axis=1)
+    f.thetab[:] = f.theta[m.bCell]
+    f.taub[:] = f.tau[m.bCell]
+    return f
 
 
 @dataclass

@@ -186,6 +186,20 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
         m.w.upload(md->weights, F, s);
         m.deltaCoeffs.upload(md->deltaCoeffs, F, s);
         upload_vec(ctx, aos_to_soa_host(md->C, N, 3), m.C);
+        {
+            // face delta vectors C_N - C_P (given, for cyclic faces)
+            std::vector<double> dv((size_t)3 * F);
+            for (int f = 0; f < F; ++f)
+                for (int d = 0; d < 3; ++d)
+                    dv[(size_t)d * F + f] = md->delta ? md->delta[3 * f + d]
+                                                      : md->C[3 * md->neighbour[f] + d] - md->C[3 * md->owner[f] + d];
+            upload_vec(ctx, dv, m.d);
+        }
+        m.coupledH.assign(F, 0);
+        m.hasCoupled = false;
+        if (md->coupled)
+            for (int f = 0; f < F; ++f)
+                if (md->coupled[f]) { m.coupledH[f] = 1; m.hasCoupled = true; }
         m.V.upload(md->V, N, s);
         m.bCell.upload(md->bCell, NB, s);
         upload_vec(ctx, aos_to_soa_host(md->bSf, NB, 3), m.bSf);
@@ -221,6 +235,28 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
         }
         upload_vec(ctx, ef, m.ellFace);
         upload_vec(ctx, en, m.ellNbr);
+        // the preconditioner's ELL: the same slots without the coupled faces
+        m.pellFace.release();
+        m.pellNbr.release();
+        m.pnSlots = ns;
+        if (m.hasCoupled) {
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (int f = 0; f < F; ++f)
+                if (!m.coupledH[f]) { cnt[md->owner[f]]++; cnt[md->neighbour[f]]++; }
+            int pns = 0;
+            for (int c = 0; c < N; ++c) pns = std::max(pns, cnt[c]);
+            m.pnSlots = pns;
+            std::vector<int> pf((size_t)std::max(pns, 1) * N, -1), pn((size_t)std::max(pns, 1) * N, -1);
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (int f = 0; f < F; ++f) {
+                if (m.coupledH[f]) continue;
+                int o = md->owner[f], n = md->neighbour[f];
+                pf[(size_t)cnt[o] * N + o] = f; pn[(size_t)cnt[o] * N + o] = n; cnt[o]++;
+                pf[(size_t)cnt[n] * N + n] = f; pn[(size_t)cnt[n] * N + n] = o; cnt[n]++;
+            }
+            upload_vec(ctx, pf, m.pellFace);
+            upload_vec(ctx, pn, m.pellNbr);
+        }
         // ---- boundary CSR ----------------------------------------------------
         std::vector<int> bs(N + 1, 0), bl(NB);
         for (int b = 0; b < NB; ++b) bs[md->bCell[b] + 1]++;
@@ -289,6 +325,7 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         std::vector<int> lo((size_t)3 * N, -1), hi((size_t)3 * N, -1);
         for (int f = 0; f < F; ++f) {
             int o = own[f], n = nei[f];
+            if (m.hasCoupled && m.coupledH[f]) continue;   // not part of the sweeps
             int di = cellIJK[3 * n] - cellIJK[3 * o], dj = cellIJK[3 * n + 1] - cellIJK[3 * o + 1],
                 dk = cellIJK[3 * n + 2] - cellIJK[3 * o + 2];
             int dir = (di == 0 && dj == 0 && dk == 1) ? 0 : (di == 0 && dj == 1 && dk == 0) ? 1
@@ -594,6 +631,7 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
         DevMesh &m = ctx->mesh;
         Batch &b = m.batch;
         const int N = m.N, F = m.F, NB = m.NB, n = nCases;
+        RT_REQUIRE(!m.hasCoupled, RT_EINVAL, "batches of cases with coupled (cyclic) faces are not supported");
         RT_REQUIRE(cellStart[0] == 0 && cellStart[n] == N && faceStart[0] == 0 && faceStart[n] == F &&
                        bFaceStart[0] == 0 && bFaceStart[n] == NB,
                    RT_EINVAL, "case ranges must cover the cells, faces and boundary faces");

@@ -85,7 +85,7 @@ __global__ void k_defc_face(MeshView m, Lims L, int hr, const double *__restrict
     upper[f] = (1.0 - u) * ph;
     if (!hr) return;
     int o = m.owner[f], n = m.neighbour[f];
-    double d0 = m.C[n] - m.C[o], d1 = m.C[N + n] - m.C[N + o], d2 = m.C[2 * N + n] - m.C[2 * N + o];
+    double d0 = m.d[f], d1 = m.d[m.F + f], d2 = m.d[2 * m.F + f];
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         double go0 = g[((size_t)0 * NC + k) * N + o], go1 = g[((size_t)1 * NC + k) * N + o],

@@ -25,6 +25,7 @@ struct MeshView {
     const double *__restrict__ magSf;
     const double *__restrict__ w;
     const double *__restrict__ delta;
+    const double *__restrict__ d;       // 3F SoA, C_N - C_P across each face
     const double *__restrict__ C;       // 3N SoA
     const double *__restrict__ V;
     const double *__restrict__ bSf;     // 3NB SoA
@@ -42,7 +43,7 @@ inline MeshView view(const DevMesh &m) {
     const bool b = m.batch.n > 1;
     return MeshView{m.N, m.F, m.NB, m.nSlots, m.owner.p, m.neighbour.p, m.ellFace.p, m.ellNbr.p,
                     m.bStart.p, m.bList.p, m.bCell.p, m.Sf.p, m.magSf.p, m.w.p, m.deltaCoeffs.p,
-                    m.C.p, m.V.p, m.bSf.p, m.bmagSf.p, m.bDelta.p, m.bCtoF.p,
+                    m.d.p, m.C.p, m.V.p, m.bSf.p, m.bmagSf.p, m.bDelta.p, m.bCtoF.p,
                     b ? m.batch.caseOf.p : nullptr, b ? m.batch.params.p : nullptr,
                     b ? m.batch.refCell.p : nullptr, b ? m.batch.refValue.p : nullptr};
 }

@@ -456,7 +456,8 @@ namespace {
 
 struct Solver {
     rt_ctx *ctx;
-    Ell e;
+    Ell e;    // the matrix (every internal face)
+    Ell pe;   // the DIC/DILU factorisation and sweeps (coupled faces left out)
     int N;
     cudaStream_t st;
     const SolveArgs &a;
@@ -467,6 +468,7 @@ struct Solver {
         const DevMesh &m = ctx->mesh;
         N = m.N;
         e = Ell{m.N, m.nSlots, m.ellFace.p, m.ellNbr.p};
+        pe = m.hasCoupled ? Ell{m.N, m.pnSlots, m.pellFace.p, m.pellNbr.p} : e;
         st = ctx->stream;
         S = ctx->scal.p;
         nB = ctx->red.nBlocks;
@@ -520,7 +522,7 @@ struct Solver {
             ProfScope ps(ctx, "dilu_rD", (double)N * (16.0 + fpc * 28.0));
             for (int l = 0; l < m.nLevels; ++l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
-                k_rd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, a.diag,
+                k_rd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, a.diag,
                                                                   a.upper, a.lower, rD);
             }
             RT_CHECK_LAUNCH();
@@ -557,12 +559,12 @@ struct Solver {
             ProfScope ps(ctx, "dilu_precondition", (double)N * (16.0 + fpc * 32.0 + 32.0 * pop(mask)));
             for (int l = 0; l < m.nLevels; ++l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
-                k_fwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD,
+                k_fwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, mask, rD,
                                                                    a.lower, r, w);
             }
             for (int l = m.nLevels - 1; l >= 0; --l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
-                k_bwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD,
+                k_bwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, mask, rD,
                                                                    a.upper, w);
             }
             launch_count(ctx, 2 * m.nLevels);
@@ -1081,12 +1083,12 @@ struct Mixed : Solver {
             ProfScope ps(ctx, "dilu_precondition32", (double)N * (8.0 + fpc * 24.0 + 16.0 * pop(mask)));
             for (int l = 0; l < m.nLevels; ++l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
-                k_fwd_level<float><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD32,
+                k_fwd_level<float><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, mask, rD32,
                                                                           l32, r, w);
             }
             for (int l = m.nLevels - 1; l >= 0; --l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
-                k_bwd_level<float><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(e, l0, l1, m.levelCells.p, mask, rD32,
+                k_bwd_level<float><<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, mask, rD32,
                                                                           u32, w);
             }
             launch_count(ctx, 2 * m.nLevels);

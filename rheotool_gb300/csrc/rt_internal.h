@@ -209,6 +209,15 @@ struct DevMesh {
     DBuf<int> owner, neighbour;
     DBuf<double> Sf;         // 3F SoA
     DBuf<double> magSf, w, deltaCoeffs;
+    DBuf<double> d;          // 3F SoA, C_N - C_P (coupled faces: neighbour translated by the period)
+    // coupled (cyclic) faces: internal faces that the DIC/DILU factorisation
+    // and sweeps skip; coupledH[f] != 0 on the host
+    bool hasCoupled = false;
+    std::vector<char> coupledH;
+    // ELL adjacency of the preconditioner (the faces that are not coupled);
+    // empty when the mesh has no coupled faces (the full ELL serves then)
+    DBuf<int> pellFace, pellNbr;
+    int pnSlots = 0;
     // cells (N)
     DBuf<double> C;          // 3N SoA
     DBuf<double> V;

@@ -177,9 +177,11 @@ __global__ void k_sub_lap(MeshView m, double gam0, double *__restrict__ lower, d
 }
 
 // UEqn diag and source
+// (body: the uniform body force per unit mass, added to the explicit divTau
+// terms before they are integrated over the cell)
 __global__ void k_mom_cell(MeshView m, double rDeltaT, double gam0, const double *__restrict__ diagC,
                            const double *__restrict__ srcC, const double *__restrict__ U0,
-                           const double *__restrict__ expl, double *__restrict__ diag,
+                           const double *__restrict__ expl, double3 body, double *__restrict__ diag,
                            double *__restrict__ src) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
@@ -194,10 +196,11 @@ __global__ void k_mom_cell(MeshView m, double rDeltaT, double gam0, const double
     }
     double v = m.V[c];
     diag[c] = ((0.0 + rDeltaT * v) + diagC[c]) - ld;
+    const double bf[3] = {body.x, body.y, body.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k)
         src[(size_t)k * N + c] = ((0.0 + rDeltaT * U0[(size_t)k * N + c] * v) + srcC[(size_t)k * N + c]) +
-                                 v * expl[(size_t)k * N + c];
+                                 v * (expl[(size_t)k * N + c] + bf[k]);
 }
 
 // boundary coefficients of UEqn: convection minus laplacian (fixedValue faces)
@@ -570,7 +573,8 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     ProfScope psMom(ctx, "mom_assembly", (double)N * (48.0 + 72.0 + 24.0 + 24.0 + 8.0 + 24.0 + 24.0 + 24.0 + 8.0 + 24.0) + F * 32.0);
     k_divtau_expl<<<gN, RT_BLOCK, 0, s>>>(m, mc, cs.tau.p, cs.taub.p, G, cs.U.p, cs.Ub.p, expl);
     double *diag = W.take(N), *src = W.take(3 * (size_t)N);
-    k_mom_cell<<<gN, RT_BLOCK, 0, s>>>(m, rDeltaT, gam, diagC, srcC, U0, expl, diag, src);
+    const double3 body = make_double3(ctl.bodyForce[0], ctl.bodyForce[1], ctl.bodyForce[2]);
+    k_mom_cell<<<gN, RT_BLOCK, 0, s>>>(m, rDeltaT, gam, diagC, srcC, U0, expl, body, diag, src);
     if (F) k_sub_lap<<<gF, RT_BLOCK, 0, s>>>(m, gam, lower, upper);
     if (NB) k_mom_bnd<<<gB, RT_BLOCK, 0, s>>>(m, gam, cs.bkU.p, cs.Ub.p, intC, bouC);
     RT_CHECK_LAUNCH();

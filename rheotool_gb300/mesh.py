@@ -90,6 +90,11 @@ class Mesh:
     shape: Tuple[int, int, int]     # (nx, ny, nz) of the bounding grid
     cellIJK: np.ndarray             # (nCells, 3) int32 grid position
     name: str = "mesh"
+    # cyclic (periodic) face pairs, stored as internal faces: C_N - C_P per
+    # face with the neighbour translated by the period (None: C[N] - C[P]),
+    # and a flag per face (None: no coupled faces)
+    delta: Optional[np.ndarray] = None      # (nFaces, 3)
+    coupled: Optional[np.ndarray] = None    # (nFaces,) int32
 
     @property
     def nFaces(self) -> int:
@@ -136,12 +141,22 @@ def structured_mesh(
     active: Optional[np.ndarray] = None,
     empty_z: bool = False,
     name: str = "mesh",
+    periodic: Sequence[bool] = (False, False, False),
 ) -> Mesh:
     """Build an LDU mesh from node coordinates and an active-cell mask.
 
     ``patch_of(direction, i, j, k, Cf)`` returns, for the boundary faces of the
     given direction at cells (i, j, k) with face centres Cf (m, 3), an integer
     array of indices into ``patch_names``, or -1 for an empty face.
+
+    ``periodic[d]`` joins the two ends of direction d (x, y, z) by a cyclic
+    patch pair: each pair of end cells shares one internal face, owned by the
+    lower-numbered cell (the one at index 0) and placed at that cell's end of
+    the box, with the neighbour centre translated by the period for the
+    weights, the deltaCoeffs and the face delta vector.  Such faces are
+    flagged in ``Mesh.coupled`` (they act in the matrix but, like OpenFOAM's
+    cyclic lduInterfaces, not in the DIC/DILU preconditioners).  A periodic
+    direction needs at least 3 cells and no holes at its ends.
     """
     xs, ys, zs = (np.asarray(a, dtype=np.float64) for a in (xs, ys, zs))
     nx, ny, nz = len(xs) - 1, len(ys) - 1, len(zs) - 1
@@ -158,8 +173,20 @@ def structured_mesh(
     C = np.stack([xc[ii], yc[jj], zc[kk]], axis=1)
     V = dx[ii] * dy[jj] * dz[kk]
 
+    periodic = tuple(bool(p) for p in periodic)
+    dims = (nx, ny, nz)
+    for a, per in enumerate(periodic):
+        if not per:
+            continue
+        if dims[a] < 3 or (a == 2 and empty_z):
+            raise ValueError("a periodic direction needs at least 3 cells (and cannot be empty)")
+        ends = np.take(active, [0, dims[a] - 1], axis=2 - a)
+        if not ends.all():
+            raise ValueError("a periodic direction cannot have holes at its ends")
+    period = np.array([xs[-1] - xs[0], ys[-1] - ys[0], zs[-1] - zs[0]])
+
     # ---- internal faces --------------------------------------------------
-    own_l, nei_l, Sf_l, Cf_l = [], [], [], []
+    own_l, nei_l, Sf_l, Cf_l, sh_l, cp_l = [], [], [], [], [], []
     for d, (di, dj, dk) in ((XP, _DIRS[XP]), (YP, _DIRS[YP]), (ZP, _DIRS[ZP])):
         i2, j2, k2 = ii + di, jj + dj, kk + dk
         inside = (i2 < nx) & (j2 < ny) & (k2 < nz)
@@ -184,18 +211,46 @@ def structured_mesh(
             F[:] = np.stack([xc[ii[c]], yc[jj[c]], zs[kk[c] + 1]], axis=1)
         Sf_l.append(S)
         Cf_l.append(F)
+        sh_l.append(np.zeros((c.size, 3)))
+        cp_l.append(np.zeros(c.size, np.int32))
+        a = (XP, YP, ZP).index(d)
+        if periodic[a]:
+            # the cyclic pair: owner at index 0, neighbour at the far end
+            pos = (ii, jj, kk)[a]
+            lo = np.nonzero(pos == 0)[0]
+            far = [ii[lo], jj[lo], kk[lo]]
+            far[a] = np.full(lo.size, dims[a] - 1)
+            nbw = idx[far[2], far[1], far[0]]
+            S = np.zeros((lo.size, 3))
+            F = np.stack([xc[ii[lo]], yc[jj[lo]], zc[kk[lo]]], axis=1)
+            area = (dy[jj[lo]] * dz[kk[lo]], dx[ii[lo]] * dz[kk[lo]], dx[ii[lo]] * dy[jj[lo]])[a]
+            S[:, a] = -area                        # outward from the owner, towards -axis
+            F[:, a] = (xs, ys, zs)[a][0]
+            shift = np.zeros((lo.size, 3))
+            shift[:, a] = -period[a]               # the neighbour's image next to the owner
+            own_l.append(lo)
+            nei_l.append(nbw)
+            Sf_l.append(S)
+            Cf_l.append(F)
+            sh_l.append(shift)
+            cp_l.append(np.ones(lo.size, np.int32))
     owner = np.concatenate(own_l)
     neighbour = np.concatenate(nei_l)
     Sf = np.concatenate(Sf_l)
     Cf = np.concatenate(Cf_l)
+    shift = np.concatenate(sh_l)
+    coupled = np.concatenate(cp_l)
     order = np.lexsort((neighbour, owner))
     owner, neighbour, Sf, Cf = owner[order], neighbour[order], Sf[order], Cf[order]
+    shift, coupled = shift[order], coupled[order]
+    CN = C[neighbour] + shift
     magSf = np.sqrt((Sf * Sf).sum(1))
     sfdOwn = np.abs((Sf * (Cf - C[owner])).sum(1))
-    sfdNei = np.abs((Sf * (C[neighbour] - Cf)).sum(1))
+    sfdNei = np.abs((Sf * (CN - Cf)).sum(1))
     w = sfdNei / (sfdOwn + sfdNei)
-    dvec = C[neighbour] - C[owner]
+    dvec = CN - C[owner]
     deltaCoeffs = 1.0 / np.sqrt((dvec * dvec).sum(1))
+    anyPeriodic = any(periodic)
 
     # ---- boundary faces ------------------------------------------------------
     b_cell, b_dir, b_patch, b_Sf, b_Cf = [], [], [], [], []
@@ -207,6 +262,8 @@ def structured_mesh(
         ins = ~out
         nb[ins] = idx[k2[ins], j2[ins], i2[ins]]
         c = np.nonzero(nb < 0)[0]
+        if periodic[d // 2]:
+            continue          # the ends of a periodic direction are joined
         if c.size == 0:
             continue
         S = np.zeros((c.size, 3))
@@ -255,6 +312,8 @@ def structured_mesh(
         bCf=np.ascontiguousarray(bCf), bDelta=bDelta, bPatch=bPatch.astype(np.int32),
         patches=patches, solveDir=solveDir, shape=(nx, ny, nz),
         cellIJK=np.stack([ii, jj, kk], axis=1).astype(np.int32), name=name,
+        delta=np.ascontiguousarray(dvec) if anyPeriodic else None,
+        coupled=coupled if anyPeriodic else None,
     )
     return m
 
@@ -345,3 +404,21 @@ def channel_mesh(nx: int = 20, ny: int = 16, nz: int = 4, L: float = 4.0,
 
     return structured_mesh(xs, ys, zs, patch_of, ["inlet", "outlet", "walls"],
                            empty_z=two_d, name=f"channel{nx}x{ny}x{nz}")
+
+
+def periodic_channel_mesh(nx: int = 400, ny: int = 100, nz: int = 100, L: float = 8.0,
+                          H: float = 1.0, depth: float = 4.0, wall_ratio: float = 4.0) -> Mesh:
+    """3-D channel, periodic (cyclic) in the streamwise x and spanwise z
+    directions, walls at y = -H and y = +H (patch ``walls``, the only patch).
+    The wall-normal spacing is refined towards both walls (``wall_ratio`` =
+    centre cell height / wall cell height); x and z are uniform.  The
+    defaults give 4,000,000 cells."""
+    xs = graded_nodes(0.0, L, nx)
+    ys = two_sided_nodes(-H, H, ny, wall_ratio) if wall_ratio != 1.0 else graded_nodes(-H, H, ny)
+    zs = graded_nodes(0.0, depth, nz)
+
+    def patch_of(d, i, j, k, Cf):
+        return np.zeros(i.size, np.int64)
+
+    return structured_mesh(xs, ys, zs, patch_of, ["walls"], periodic=(True, False, True),
+                           name=f"periodicChannel{nx}x{ny}x{nz}")

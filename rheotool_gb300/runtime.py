@@ -242,6 +242,10 @@ def _mesh_desc(mesh, keeper) -> abi.rt_mesh_desc:
     md.patchSize = i(np.array([p.size for p in mesh.patches] or [0]))
     for k in range(3):
         md.solveDir[k] = int(mesh.solveDir[k])
+    if getattr(mesh, "delta", None) is not None:
+        md.delta = d(mesh.delta)
+    if getattr(mesh, "coupled", None) is not None:
+        md.coupled = i(mesh.coupled)
     keeper._mesh_keep = keep
     return md
 
