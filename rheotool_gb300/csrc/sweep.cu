@@ -16,7 +16,9 @@
 // (register) and the j-1 value lane l-1's previous result (shuffle).  Lane 0
 // reads j-1 from the j-block below (step t + 31) and every lane reads k-1 from
 // the block of the previous plane (same step).  The steps are taken in chunks
-// of P: a chunk waits once, reads its staged coefficients and publishes once.
+// of P: a chunk stages its coefficients and exchanges the j-block words once,
+// and takes the previous plane's words and publishes its own to the next
+// plane quad by quad (four steps), so the planes lag one another by a quad.
 //
 // One CTA owns one plane (warp = j-block); a thread-block cluster owns CS
 // consecutive planes.  Values handed to another warp (plane to plane through
@@ -239,7 +241,7 @@ __device__ __forceinline__ void st4(double *p, const double *v) {
 // zero coefficients and zero right-hand sides, so every lane runs the same
 // branch-free recurrence.
 template <class Real, int MODE, int NC, int P, int NB>
-__global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
+__global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
                                                   int *sync, u64 *__restrict__ xfer, unsigned epoch,
                                                   long long maxSpin, int R) {
     static_assert(P % 4 == 0 && P <= 32, "a chunk is whole quads");
@@ -359,46 +361,13 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                 if (v < 0) { fail = 1; break; }
                 seenCJ = v;
             }
-            // ---- the hand-off values of the chunk: every load is issued
-            // first, then the tags are checked (a word not there yet is waited for)
+            // ---- the chunk's inputs, in the order of their readiness: the
+            // j-block words (the block below runs ahead) and the staged
+            // coefficients first, then, quad by quad, the previous plane's
+            // words, which the pipeline waits on
             Real wkv[P][NC], wjv[P][NC];
             bool ok = true;
             const Real zk = (MODE == 2) ? Real(1) : Real(0);
-            if (kLocalProd || kGlob) {
-                u64 kw[PQ][QW];
-#pragma unroll
-                for (int qd = 0; qd < PQ; ++qd)
-#pragma unroll
-                    for (int h = 0; h < QW / 2; ++h) {
-                        if (kLocalProd) ld2_shared(ringKs + 8u * (kword(t0 + 4 * qd) + 2 * h), kw[qd][2 * h], kw[qd][2 * h + 1]);
-                        else ld2_global(xword(bIn, t0 + 4 * qd) + 2 * h, kw[qd][2 * h], kw[qd][2 * h + 1]);
-                    }
-                // every word checked in registers; one warp-uniform branch to
-                // the (rare) waits for words not there yet
-                const unsigned ktag = kLocalProd ? (unsigned)(t0 + 1) : epoch;
-                bool hit = true;
-#pragma unroll
-                for (int s = 0; s < P; ++s)
-#pragma unroll
-                    for (int q = 0; q < NC; ++q)
-                        hit &= peek(&kw[s >> 2][(s & 3) * VW + q * W], kLocalProd ? ktag + s : ktag, wkv[s][q]);
-                if (__any_sync(0xffffffffu, !hit)) {
-#pragma unroll
-                    for (int s = 0; s < P; ++s)
-#pragma unroll
-                        for (int q = 0; q < NC; ++q) {
-                            const int wi = (s & 3) * VW + q * W;
-                            const unsigned tag = kLocalProd ? ktag + s : ktag;
-                            const volatile u64 *src = kLocalProd ? ringK + kword(t0 + s) + wi : xword(bIn, t0 + s) + wi;
-                            ok &= wait_get(src, tag, wkv[s][q], sync, kLocalProd ? maxSpin : maxSpin >> 4, kGlob);
-                        }
-                }
-            } else {
-#pragma unroll
-                for (int s = 0; s < P; ++s)
-#pragma unroll
-                    for (int q = 0; q < NC; ++q) wkv[s][q] = zk;
-            }
 #pragma unroll
             for (int s = 0; s < P; ++s)
 #pragma unroll
@@ -423,6 +392,7 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                         for (int q = 0; q < NC; ++q)
                             ok &= wait_get(src + q * W, (unsigned)(ts + 1), jv[q], sync, maxSpin, false);
                     }
+                    if (__any_sync(0xffffffffu, !ok)) { fail = 1; break; }
                 }
 #pragma unroll
                 for (int q = 0; q < NC; ++q) jv[q] = live ? jv[q] : zk;
@@ -449,54 +419,95 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
 #pragma unroll
                 for (int qd = 0; qd < PQ; ++qd) ld4(myCStage + buf * P * 32 + qd * 128 + lf * 4, &cell[4 * qd]);
             }
+            // ---- quad by quad: the previous plane's words of four steps, the
+            // terms that wait on them, the recurrence and the publication of
+            // the quad's results to the next plane.  The next plane starts on a
+            // quad as soon as it is published, so a plane lags the previous
+            // one by about one quad of work plus the hand-off, not a chunk.
+            // (Each word is checked in registers; one warp-uniform branch
+            // leads to the rare bounded waits for words not there yet.  A
+            // ring never wraps inside a chunk: R is a multiple of P.)
+            const unsigned ktag = kLocalProd ? (unsigned)(t0 + 1) : epoch;
+            bool qfail = false;
 #pragma unroll
-            for (int s = 0; s < P; ++s) {
-                const int sf = (MODE == 1) ? P - 1 - s : s;
-                if (MODE == 2) {
-                    cy[s] = va[2][sf];
-                    cx[s] = va[3][sf];
-                    pre[s][0] = r_sub(va[0][sf], r_div(va[1][sf], wkv[s][0]));   // D - Pz / rD(k-1)
-                } else {
-                    const Real c0 = va[0][sf];
-                    cy[s] = va[1][sf];
-                    cx[s] = va[2][sf];
-                    // MODE 0: rk = rD r (premultiplied by the gather, the
-                    // sequential sweep's first product); MODE 1: rk = w
+            for (int qd = 0; qd < PQ; ++qd) {
+                if (kLocalProd || kGlob) {
+                    u64 kw[QW];
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) pre[s][q] = r_fma(-c0, wkv[s][q], va[3 + q][sf]);
-                }
-            }
-            if (__any_sync(0xffffffffu, !ok)) { fail = 1; break; }
-            // ---- the recurrence (order of operations of the sequential sweep)
-#pragma unroll
-            for (int s = 0; s < P; ++s) {
-#pragma unroll
-                for (int q = 0; q < NC; ++q) {
-                    const Real yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
-                    const Real yj = (lane > 0) ? yup : wjv[s][q];
-                    Real v;
-                    if (MODE == 2) {
-                        v = r_sub(pre[s][q], r_div(cy[s], yj));
-                        v = r_sub(v, r_div(cx[s], yprev[q]));
-                    } else if (sizeof(Real) == 4) {
-                        // FP32: the i term first, so only one product waits on the shuffle
-                        v = r_fma(-cx[s], yprev[q], pre[s][q]);
-                        v = r_fma(-cy[s], yj, v);
-                    } else {
-                        v = r_fma(-cy[s], yj, pre[s][q]);
-                        v = r_fma(-cx[s], yprev[q], v);
+                    for (int h = 0; h < QW / 2; ++h) {
+                        if (kLocalProd) ld2_shared(ringKs + 8u * (kword(t0 + 4 * qd) + 2 * h), kw[2 * h], kw[2 * h + 1]);
+                        else ld2_global(xword(bIn, t0 + 4 * qd) + 2 * h, kw[2 * h], kw[2 * h + 1]);
                     }
-                    out[s][q] = v;
-                    yprev[q] = v;
-                }
-            }
-            // ---- publish the chunk's hand-off words (the consumers read whole
-            // chunks, so publishing per chunk costs them no latency and keeps
-            // the addressing off the dependent chain; a chunk never wraps a
-            // ring: R and RJ are multiples of P)
-            if (kLocalCons || crossProducer) {
+                    bool hit = true;
 #pragma unroll
-                for (int qd = 0; qd < PQ; ++qd) {
+                    for (int e = 0; e < 4; ++e)
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            hit &= peek(&kw[e * VW + q * W], kLocalProd ? ktag + 4 * qd + e : ktag, wkv[4 * qd + e][q]);
+                    if (__any_sync(0xffffffffu, !hit)) {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+#pragma unroll
+                            for (int q = 0; q < NC; ++q) {
+                                const int s = 4 * qd + e;
+                                const int wi = e * VW + q * W;
+                                const unsigned tag = kLocalProd ? ktag + s : ktag;
+                                const volatile u64 *src = kLocalProd ? ringK + kword(t0 + s) + wi : xword(bIn, t0 + s) + wi;
+                                ok &= wait_get(src, tag, wkv[s][q], sync, kLocalProd ? maxSpin : maxSpin >> 4, kGlob);
+                            }
+                        if (__any_sync(0xffffffffu, !ok)) { qfail = true; break; }
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+#pragma unroll
+                        for (int q = 0; q < NC; ++q) wkv[4 * qd + e][q] = zk;
+                }
+                // the terms of the quad's steps that do not depend on the previous step
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int s = 4 * qd + e;
+                    const int sf = (MODE == 1) ? P - 1 - s : s;
+                    if (MODE == 2) {
+                        cy[s] = va[2][sf];
+                        cx[s] = va[3][sf];
+                        pre[s][0] = r_sub(va[0][sf], r_div(va[1][sf], wkv[s][0]));   // D - Pz / rD(k-1)
+                    } else {
+                        const Real c0 = va[0][sf];
+                        cy[s] = va[1][sf];
+                        cx[s] = va[2][sf];
+                        // MODE 0: rk = rD r (premultiplied by the gather, the
+                        // sequential sweep's first product); MODE 1: rk = w
+#pragma unroll
+                        for (int q = 0; q < NC; ++q) pre[s][q] = r_fma(-c0, wkv[s][q], va[3 + q][sf]);
+                    }
+                }
+                // the recurrence (order of operations of the sequential sweep)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int s = 4 * qd + e;
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) {
+                        const Real yup = __shfl_up_sync(0xffffffffu, yprev[q], 1);
+                        const Real yj = (lane > 0) ? yup : wjv[s][q];
+                        Real v;
+                        if (MODE == 2) {
+                            v = r_sub(pre[s][q], r_div(cy[s], yj));
+                            v = r_sub(v, r_div(cx[s], yprev[q]));
+                        } else if (sizeof(Real) == 4) {
+                            // FP32: the i term first, so only one product waits on the shuffle
+                            v = r_fma(-cx[s], yprev[q], pre[s][q]);
+                            v = r_fma(-cy[s], yj, v);
+                        } else {
+                            v = r_fma(-cy[s], yj, pre[s][q]);
+                            v = r_fma(-cx[s], yprev[q], v);
+                        }
+                        out[s][q] = v;
+                        yprev[q] = v;
+                    }
+                }
+                // publish the quad to the next plane
+                if (kLocalCons || crossProducer) {
                     u64 wd[QW];
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
@@ -511,6 +522,9 @@ __global__ void __launch_bounds__(512) k_systolic(SkewT<Real> g, unsigned mask, 
                     }
                 }
             }
+            if (qfail) { fail = 1; break; }
+            // ---- the j-block hand-off words of the whole chunk (the block
+            // above lags by more than a chunk)
             if (consJ >= 0 && lane == 31) {
                 u64 wd[P * VW];
 #pragma unroll
