@@ -194,7 +194,8 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
 
 /* Options.  RT_OPT_SWEEP: 0 auto (systolic when structured), 1 level-scheduled
  * sweeps, 2 structured systolic sweeps.  RT_OPT_SWEEP_PLANES: planes per
- * thread-block cluster of the systolic sweeps, one CTA per plane (1 .. 16).
+ * thread-block cluster of the systolic sweeps, one CTA per plane (1 .. 16;
+ * default 16, or 8 where a cluster of 16 cannot be scheduled).
  * RT_OPT_PRECISION: RT_PREC_FP64 or RT_PREC_MIXED for rt_ldu_solve (the time
  * step takes its precision from rt_case_ctl). */
 #define RT_OPT_SWEEP 1

@@ -354,7 +354,9 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         upload_vec(ctx, lo, s.faceLo);
         upload_vec(ctx, hi, s.faceHi);
         RT_REQUIRE(s.nJB <= 8 && skew_fits(s.nJB), RT_EINVAL, "structured sweeps need ny <= 256");
-        s.KC = std::max(1, std::min(nz, 8));   // planes (CTAs) per thread-block cluster
+        // planes (CTAs) per thread-block cluster: 16 (the non-portable maximum;
+        // fewer hand-offs through global memory), 8 where 16 cannot be scheduled
+        s.KC = std::max(1, std::min(nz, 16));
         s.sync.alloc(SYNC_PROGRESS + (size_t)nz * s.nJB);
         s.sync.zero(ctx->stream);
         s.data.alloc((size_t)(12 + 6 + 6) * s.nSkew);

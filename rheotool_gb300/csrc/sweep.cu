@@ -429,6 +429,16 @@ __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mas
             // ring never wraps inside a chunk: R is a multiple of P.)
             const unsigned ktag = kLocalProd ? (unsigned)(t0 + 1) : epoch;
             bool qfail = false;
+            // across a cluster boundary the words come from global memory: the
+            // whole chunk's words are loaded at once (one memory round trip),
+            // and checked quad by quad
+            u64 kwg[PQ][QW];
+            if (kGlob) {
+#pragma unroll
+                for (int qd = 0; qd < PQ; ++qd)
+#pragma unroll
+                    for (int h = 0; h < QW / 2; ++h) ld2_global(xword(bIn, t0 + 4 * qd) + 2 * h, kwg[qd][2 * h], kwg[qd][2 * h + 1]);
+            }
 #pragma unroll
             for (int qd = 0; qd < PQ; ++qd) {
                 if (kLocalProd || kGlob) {
@@ -436,7 +446,7 @@ __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mas
 #pragma unroll
                     for (int h = 0; h < QW / 2; ++h) {
                         if (kLocalProd) ld2_shared(ringKs + 8u * (kword(t0 + 4 * qd) + 2 * h), kw[2 * h], kw[2 * h + 1]);
-                        else ld2_global(xword(bIn, t0 + 4 * qd) + 2 * h, kw[2 * h], kw[2 * h + 1]);
+                        else { kw[2 * h] = kwg[qd][2 * h]; kw[2 * h + 1] = kwg[qd][2 * h + 1]; }
                     }
                     bool hit = true;
 #pragma unroll
@@ -669,6 +679,30 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
         RT_CUDA(cudaFuncSetAttribute(k_systolic<Real, MODE, NC, P, NB>, cudaFuncAttributeNonPortableClusterSizeAllowed,
                                      1));
         attr = shm;
+    }
+    // a cluster of more than 8 CTAs (non-portable) must fit one GPC with this
+    // launch's shared memory; otherwise the portable 8 (checked once per
+    // instantiation and cluster size)
+    static int fits16 = -1;
+    if (CS > 8) {
+        if (fits16 < 0) {
+            cudaLaunchConfig_t q = {};
+            q.gridDim = dim3(CS);
+            q.blockDim = dim3(32 * g.nJB);
+            q.dynamicSmemBytes = shm;
+            cudaLaunchAttribute qa[1];
+            qa[0].id = cudaLaunchAttributeClusterDimension;
+            qa[0].val.clusterDim.x = CS;
+            qa[0].val.clusterDim.y = 1;
+            qa[0].val.clusterDim.z = 1;
+            q.attrs = qa;
+            q.numAttrs = 1;
+            int n = 0;
+            cudaError_t e = cudaOccupancyMaxActiveClusters(&n, k_systolic<Real, MODE, NC, P, NB>, &q);
+            if (e != cudaSuccess) (void)cudaGetLastError();
+            fits16 = (e == cudaSuccess && n >= 1) ? 1 : 0;
+        }
+        if (!fits16) CS = 8;
     }
     const int nGroups = (g.nz + CS - 1) / CS;
     // tagged hand-off between clusters: (boundaries) x blocks x steps x lanes x words

@@ -381,15 +381,16 @@ def test_unknown_model_is_rejected(ctx):
 @pytest.mark.parametrize("tune,ring", [(1, 0), (2, 0), (3, 0), (4, 0), (5, 0), (5, 8), (3, 8)])
 def test_systolic_schedules_equal_level_sweeps(ctx, tune, ring):
     """Every chunk schedule (chunk size, staging depth) and ring depth of the
-    one-component sweeps gives the level-scheduled bits, across a cluster
-    boundary (the global hand-off) and with the shallowest plane ring (the
-    producers wait on their consumers)."""
+    one-component sweeps gives the level-scheduled bits, across cluster
+    boundaries (clusters of 4 planes: the global hand-off twice) and with the
+    shallowest plane ring (the producers wait on their consumers)."""
     mesh = SWEEP_MESHES["contraction3d_11"]()
     rng = np.random.default_rng(22)
     diag, upper, lower = laplacian_system(mesh, rng, asym=0.0)
     b = rng.normal(size=(1, mesh.nCells)) * mesh.V
     ctl = SolverControl("PCG", "DIC", 1e-12, 0.0, 0, 500)
     ctx.upload_mesh(mesh)
+    ctx.set_option(abi.RT_OPT_SWEEP_PLANES, 4)
     out = {}
     try:
         ctx.set_option(abi.RT_OPT_SWEEP_TUNE, tune)
@@ -403,5 +404,32 @@ def test_systolic_schedules_equal_level_sweeps(ctx, tune, ring):
         ctx.set_sweep(abi.SWEEP_AUTO)
         ctx.set_option(abi.RT_OPT_SWEEP_TUNE, 0)
         ctx.set_option(abi.RT_OPT_SWEEP_RING, 0)
+    assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
+    assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
+
+
+@pytest.mark.parametrize("planes", [0, 8])
+@pytest.mark.parametrize("solver,pre,asym,nc", [("PCG", "DIC", 0.0, 1), ("PBiCGStab", "DILU", 3.0, 3)])
+def test_systolic_cluster_sizes_equal_level_sweeps(ctx, planes, solver, pre, asym, nc):
+    """20 planes: the default clusters of 16 planes (or 8 where 16 cannot be
+    scheduled) and clusters of 8 both cross a cluster boundary; same bits as
+    the level-scheduled sweeps."""
+    mesh = contraction_mesh(12, 10, 30, 10, 20, 4.0, 4.0)
+    rng = np.random.default_rng(23)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=asym)
+    b = rng.normal(size=(nc, mesh.nCells)) * mesh.V
+    ctl = SolverControl(solver, pre, 1e-12, 0.0, 0, 500)
+    ctx.upload_mesh(mesh)
+    if planes:
+        ctx.set_option(abi.RT_OPT_SWEEP_PLANES, planes)
+    out = {}
+    try:
+        for mode in (abi.SWEEP_LEVELS, abi.SWEEP_SYSTOLIC):
+            ctx.set_sweep(mode)
+            x = np.zeros((nc, mesh.nCells))
+            perf = ctx.ldu_solve(diag, upper, lower, b, x, ctl)
+            out[mode] = (x, [p.nIterations for p in perf])
+    finally:
+        ctx.set_sweep(abi.SWEEP_AUTO)
     assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
     assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
