@@ -103,6 +103,7 @@ typedef struct {
 #define RT_MODEL_GIESEKUS_LOG 1   /* type GiesekusLog                           */
 #define RT_MODEL_PTT_LOG      2   /* type PTTLog                                */
 #define RT_MODEL_FENEP_LOG    3   /* type FENE-PLog                             */
+#define RT_MODEL_FENECR_LOG   4   /* type FENE-CRLog (FENE-CR/FENE-CRLog/FENE_CRLog.C:127-180) */
 #define RT_PTT_LINEAR 0
 #define RT_PTT_EXP    1
 #define RT_STAB_NONE     0

@@ -18,10 +18,10 @@
  *                                         SelfAdjointEigenSolver is replaced by
  *                                         the cyclic Jacobi method, eigenvalues
  *                                         ascending as Eigen returns them)
- *   - Oldroyd-BLog / GiesekusLog / PTTLog / FENE-PLog correct()
+ *   - Oldroyd-BLog / GiesekusLog / PTTLog / FENE-PLog / FENE-CRLog correct()
  *                                         Oldroyd_BLog.C:127-179, GiesekusLog.C:
  *                                         128-176, PTTLog.C:176-268, FENE_PLog.C:
- *                                         128-182
+ *                                         128-182, FENE_CRLog.C:127-180
  *   - GaussDefCmpw convection ........... libs/gaussDefCmpwConvectionScheme/
  *                                         gaussDefCmpwConvectionScheme.C:72-170,
  *                                         197-328; limiters.H:39-100
@@ -728,6 +728,13 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
                 ? exp((mp->epsilon / (1.0 - zeta)) * (trA - 3.0))
                 : (1.0 + (mp->epsilon / (1.0 - zeta)) * (trA - 3.0));
             for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
+        } else if (mp->model == RT_MODEL_FENECR_LOG) {
+            /* FENE_CRLog.C:140-163 */
+            double f = mp->L2 / (mp->L2 - trA);
+            fP[c] = f;
+            S = t3_mul(t3_mul(R, invm1), Rt);
+            double lf = (1.0 / lambda) * f;
+            for (int i = 0; i < 9; ++i) S.a[i] = lf * S.a[i];
         } else {
             double f = mp->L2 / (mp->L2 - trA);
             double a = mp->L2 / (mp->L2 - 3.0);
@@ -785,7 +792,9 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
         }
         double sy[6];
         t3_symm(T, sy);
-        for (int q = 0; q < 6; ++q) s->tau[6 * (size_t)c + q] = cP * sy[q];
+        /* FENE-CR: (etaP/lambda) f symm(A - I) with the pre-solve f (FENE_CRLog.C:174) */
+        double cPc = (mp->model == RT_MODEL_FENECR_LOG) ? cP * fP[c] : cP;
+        for (int q = 0; q < 6; ++q) s->tau[6 * (size_t)c + q] = cPc * sy[q];
     }
     tau_correct_bc(k);
 

@@ -16,7 +16,7 @@ LIBNAME = os.path.join(HERE, "librheogpu.so")
 
 RT_OK, RT_EINVAL, RT_ENOCONV, RT_ENAN, RT_ETIMEOUT, RT_EOOM, RT_ECUDA, RT_ENOTREADY = range(8)
 RT_BC_FIXED, RT_BC_ZEROGRAD, RT_BC_LINEXTRAP = 0, 1, 2
-RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG = 0, 1, 2, 3
+RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG, RT_MODEL_FENECR_LOG = 0, 1, 2, 3, 4
 RT_PTT_LINEAR, RT_PTT_EXP = 0, 1
 RT_STAB_NONE, RT_STAB_BSD, RT_STAB_COUPLING = 0, 1, 2
 RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB = 0, 1
@@ -38,6 +38,7 @@ MODEL_NAMES = {
     "GiesekusLog": RT_MODEL_GIESEKUS_LOG,
     "PTTLog": RT_MODEL_PTT_LOG,
     "FENE-PLog": RT_MODEL_FENEP_LOG,
+    "FENE-CRLog": RT_MODEL_FENECR_LOG,
 }
 LIMITER_NAMES = {
     "none": RT_LIM_NONE, "upwind": RT_LIM_UPWIND, "cubista": RT_LIM_CUBISTA,

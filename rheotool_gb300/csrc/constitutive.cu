@@ -185,6 +185,16 @@ __device__ __forceinline__ void theta_rhs_cell(int c, int N, const rt_model_para
                                                     : (1.0 + (mp.epsilon / (1.0 - zeta)) * (trA - 3.0));
 #pragma unroll
         for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
+    } else if (mp.model == RT_MODEL_FENECR_LOG) {
+        // FENE_CRLog.C:140-163: (1/lambda) f R (Lambda^-1 - I) R^T, f from the pre-solve A
+        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
+        double trA = A.a[0] + A.a[4] + A.a[8];
+        double f = mp.L2 / (mp.L2 - trA);
+        fP[c] = f;
+        S = mul(mul(R, invm1), Rt);
+        const double lf = (1.0 / lambda) * f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = lf * S.a[i];
     } else {
         T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
         double trA = A.a[0] + A.a[4] + A.a[8];
@@ -253,13 +263,15 @@ __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__res
     for (int k = 0; k < 6; ++k) bSolve[(size_t)k * N + c] = b[k];
 }
 
-// tau = c (R Lambda R^T - I)   (FENE-P: c (f R Lambda R^T - a I))
+// tau = c (R Lambda R^T - I)   (FENE-P: c (f R Lambda R^T - a I); FENE-CR:
+// (c f)(R Lambda R^T - I), FENE_CRLog.C:174, with the pre-solve f)
 __device__ __forceinline__ void tau_cell(int c, int N, const rt_model_params &mp, const double *__restrict__ Rv,
                                          const double *__restrict__ evv, const double *__restrict__ fP,
                                          double *__restrict__ tau) {
     double zeta = (mp.model == RT_MODEL_PTT_LOG) ? mp.zeta : 0.0;
     double cP = mp.etaP / mp.lambda;
     if (mp.model == RT_MODEL_PTT_LOG) cP = mp.etaP / (mp.lambda * (1.0 - zeta));
+    if (mp.model == RT_MODEL_FENECR_LOG) cP = cP * fP[c];
     T3 R = load9(Rv, N, c);
     T3 A = mul(mul(R, dg(evv[c], evv[N + c], evv[2 * N + c])), tr(R));
     T3 T;
@@ -435,6 +447,14 @@ __global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restr
         const F3 T = frdr(R, d0, d1, d2);
 #pragma unroll
         for (int i = 0; i < 9; ++i) S.a[i] = (lambdaInv * T.a[i]) * fac;
+    } else if (mp.model == RT_MODEL_FENECR_LOG) {
+        const double trA = e0 + e1 + e2;
+        const double f = mp.L2 / (mp.L2 - trA);
+        fP[c] = f;
+        const float lf = (float)((1.0 / mp.lambda) * f);
+        S = frdr(R, d0, d1, d2);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = lf * S.a[i];
     } else {
         const double trA = e0 + e1 + e2;
         const double f = mp.L2 / (mp.L2 - trA);
@@ -478,6 +498,7 @@ __global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ 
     }
     double cP = mp.etaP / mp.lambda;
     if (mp.model == RT_MODEL_PTT_LOG) cP = mp.etaP / (mp.lambda * (1.0 - mp.zeta));
+    if (mp.model == RT_MODEL_FENECR_LOG) cP = cP * fP[c];
     const F3 R = fload9(Rv, N, c);
     F3 T;
     if (mp.model == RT_MODEL_FENEP_LOG) {

@@ -418,14 +418,15 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
     return guarded(ctx, [&]() -> rt_status {
         RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
         RT_REQUIRE(bc && mp && ctl, RT_EINVAL, "null argument");
-        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_FENEP_LOG, RT_EINVAL,
+        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_FENECR_LOG, RT_EINVAL,
                    "unknown constitutive model");
         RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
         RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
         RT_REQUIRE(ctl->divU >= RT_LIM_NONE && ctl->divU <= RT_LIM_SUPERBEE &&
                        ctl->divTheta >= RT_LIM_NONE && ctl->divTheta <= RT_LIM_SUPERBEE,
                    RT_EINVAL, "unknown GaussDefCmpw limiter");
-        RT_REQUIRE(mp->model != RT_MODEL_FENEP_LOG || mp->L2 > 3.0, RT_EINVAL, "FENE-P needs L2 > 3");
+        RT_REQUIRE((mp->model != RT_MODEL_FENEP_LOG && mp->model != RT_MODEL_FENECR_LOG) || mp->L2 > 3.0, RT_EINVAL,
+                   "FENE-P and FENE-CR need L2 > 3");
         DevMesh &m = ctx->mesh;
         DevCase &c = ctx->cs;
         RT_REQUIRE(ctl->pRefCell >= 0 && ctl->pRefCell < m.N, RT_EINVAL, "pRefCell out of range");
@@ -778,12 +779,12 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model
             const Batch &b = ctx->mesh.batch;
             for (int c = 0; c < b.n; ++c) {
                 const rt_model_params &mp = models[c];
-                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_FENEP_LOG, RT_EINVAL,
+                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_FENECR_LOG, RT_EINVAL,
                            "case " + std::to_string(c) + ": unknown constitutive model");
                 RT_REQUIRE(mp.lambda > 0 && mp.rho > 0, RT_EINVAL,
                            "case " + std::to_string(c) + ": lambda and rho must be positive");
-                RT_REQUIRE(mp.model != RT_MODEL_FENEP_LOG || mp.L2 > 3.0, RT_EINVAL,
-                           "case " + std::to_string(c) + ": FENE-P needs L2 > 3");
+                RT_REQUIRE((mp.model != RT_MODEL_FENEP_LOG && mp.model != RT_MODEL_FENECR_LOG) || mp.L2 > 3.0, RT_EINVAL,
+                           "case " + std::to_string(c) + ": FENE-P and FENE-CR need L2 > 3");
                 RT_REQUIRE(pRefCell[c] < 0 || (pRefCell[c] >= b.cellStartH[c] && pRefCell[c] < b.cellStartH[c + 1]),
                            RT_EINVAL, "case " + std::to_string(c) + ": pRefCell outside the case");
             }

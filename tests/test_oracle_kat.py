@@ -202,6 +202,8 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
             g = (A - I) + alpha * (A - I) @ (A - I)
         elif model == "PTTLog":
             g = (1.0 + eps * (np.trace(A) - 3.0)) * (A - I)
+        elif model == "FENE-CRLog":
+            g = (L2 / (L2 - np.trace(A))) * (A - I)
         else:
             f = L2 / (L2 - np.trace(A))
             a = L2 / (L2 - 3.0)
@@ -212,6 +214,8 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
     A = sol.y[:, -1].reshape(3, 3)
     if model == "FENE-PLog":
         return (L2 / (L2 - np.trace(A))) * A - (L2 / (L2 - 3.0)) * I
+    if model == "FENE-CRLog":
+        return (L2 / (L2 - np.trace(A))) * (A - I)
     return A - I
 
 
@@ -220,6 +224,7 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
     ("GiesekusLog", {"alpha": 0.3}, {"alpha": 0.3}),
     ("PTTLog", {"epsilon": 0.25}, {"eps": 0.25}),
     ("FENE-PLog", {"L2": 100.0}, {"L2": 100.0}),
+    ("FENE-CRLog", {"L2": 20.0}, {"L2": 20.0}),
 ])
 def test_steady_shear_matches_conformation_form(model, kw, ckw):
     lam, etaP, rate = 1.0, 0.8, 1.5
