@@ -104,6 +104,8 @@ typedef struct {
 #define RT_MODEL_PTT_LOG      2   /* type PTTLog                                */
 #define RT_MODEL_FENEP_LOG    3   /* type FENE-PLog                             */
 #define RT_MODEL_FENECR_LOG   4   /* type FENE-CRLog (FENE-CR/FENE-CRLog/FENE_CRLog.C:127-180) */
+#define RT_MODEL_ROLIEPOLY_LOG 5  /* type Rolie-PolyLog (Rolie-Poly/Rolie-PolyLog/RoliePolyLog.C:125-203);
+                                     lambda carries lambdaD */
 #define RT_PTT_LINEAR 0
 #define RT_PTT_EXP    1
 #define RT_STAB_NONE     0
@@ -116,7 +118,11 @@ typedef struct {
     double alpha;     /* Giesekus mobility                                    */
     double epsilon;   /* PTT extensibility                                    */
     double zeta;      /* PTT slip                                             */
-    double L2;        /* FENE-P squared extensibility                         */
+    double L2;        /* FENE-P / FENE-CR squared extensibility               */
+    double lambdaR;   /* Rolie-Poly stretch relaxation time (lambda = lambdaD) */
+    double beta;      /* Rolie-Poly convective constraint release coefficient */
+    double delta;     /* Rolie-Poly CCR exponent                              */
+    double chiMax;    /* Rolie-Poly maximum stretch (finite extensibility when > 1) */
 } rt_model_params;
 
 /* ---- linear solvers ----------------------------------------------------- */

@@ -18,10 +18,11 @@
  *                                         SelfAdjointEigenSolver is replaced by
  *                                         the cyclic Jacobi method, eigenvalues
  *                                         ascending as Eigen returns them)
- *   - Oldroyd-BLog / GiesekusLog / PTTLog / FENE-PLog / FENE-CRLog correct()
- *                                         Oldroyd_BLog.C:127-179, GiesekusLog.C:
+ *   - Oldroyd-BLog / GiesekusLog / PTTLog / FENE-PLog / FENE-CRLog /
+ *     Rolie-PolyLog correct() ........... Oldroyd_BLog.C:127-179, GiesekusLog.C:
  *                                         128-176, PTTLog.C:176-268, FENE_PLog.C:
- *                                         128-182, FENE_CRLog.C:127-180
+ *                                         128-182, FENE_CRLog.C:127-180,
+ *                                         RoliePolyLog.C:125-203
  *   - GaussDefCmpw convection ........... libs/gaussDefCmpwConvectionScheme/
  *                                         gaussDefCmpwConvectionScheme.C:72-170,
  *                                         197-328; limiters.H:39-100
@@ -674,6 +675,18 @@ static void theta_valid(const rt_mesh_desc *m, int *valid) {
     for (int q = 0; q < 6; ++q) valid[q] = (v[ij[q][0]] * v[ij[q][1]]) > 0;
 }
 
+
+/* Rolie-Poly: finite-extensibility factor and stretch rate M1 (RoliePolyLog.C:143-156) */
+static double rp_chi(const rt_model_params *mp, double trA) {
+    double c2 = mp->chiMax * mp->chiMax;
+    return ((3.0 - (trA / 3.0) / c2) * (1.0 - 1.0 / c2)) / ((1.0 - (trA / 3.0) / c2) * (3.0 - 1.0 / c2));
+}
+static double rp_m1(const rt_model_params *mp, double trA) {
+    double M1 = 2.0 * (1.0 - sqrt(3.0 / trA)) / mp->lambdaR;
+    if (mp->chiMax > 1.0) M1 *= rp_chi(mp, trA);
+    return M1;
+}
+
 static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_perf *perf) {
     const rt_mesh_desc *m = k->m;
     const rt_model_params *mp = k->mp;
@@ -728,6 +741,18 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
                 ? exp((mp->epsilon / (1.0 - zeta)) * (trA - 3.0))
                 : (1.0 + (mp->epsilon / (1.0 - zeta)) * (trA - 3.0));
             for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
+        } else if (mp->model == RT_MODEL_ROLIEPOLY_LOG) {
+            /* RoliePolyLog.C:140-179: -(1/lambdaD) A^-1 ((A - I) + M1 lambdaD (A + beta (trA/3)^delta (A - I))) */
+            t3 Ai = t3_mul(t3_mul(R, t3_diag(1.0 / ev[0], 1.0 / ev[1], 1.0 / ev[2])), Rt);
+            double M1 = rp_m1(mp, trA);
+            double ccr = mp->beta * pow(trA / 3.0, mp->delta);
+            t3 G;
+            for (int i = 0; i < 9; ++i) {
+                double AmI = A.a[i] - ((i % 4 == 0) ? 1.0 : 0.0);
+                G.a[i] = AmI + (M1 * lambda) * (A.a[i] + ccr * AmI);
+            }
+            t3 AG = t3_mul(Ai, G);
+            for (int i = 0; i < 9; ++i) S.a[i] = -((1.0 / lambda) * AG.a[i]);
         } else if (mp->model == RT_MODEL_FENECR_LOG) {
             /* FENE_CRLog.C:140-163 */
             double f = mp->L2 / (mp->L2 - trA);
@@ -792,8 +817,10 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
         }
         double sy[6];
         t3_symm(T, sy);
-        /* FENE-CR: (etaP/lambda) f symm(A - I) with the pre-solve f (FENE_CRLog.C:174) */
+        /* FENE-CR: (etaP/lambda) f symm(A - I) with the pre-solve f (FENE_CRLog.C:174);
+         * Rolie-Poly: times the finite-extensibility factor of the new trA (RoliePolyLog.C:189-199) */
         double cPc = (mp->model == RT_MODEL_FENECR_LOG) ? cP * fP[c] : cP;
+        if (mp->model == RT_MODEL_ROLIEPOLY_LOG && mp->chiMax > 1.0) cPc = cP * rp_chi(mp, A.a[0] + A.a[4] + A.a[8]);
         for (int q = 0; q < 6; ++q) s->tau[6 * (size_t)c + q] = cPc * sy[q];
     }
     tau_correct_bc(k);

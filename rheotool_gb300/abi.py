@@ -16,7 +16,8 @@ LIBNAME = os.path.join(HERE, "librheogpu.so")
 
 RT_OK, RT_EINVAL, RT_ENOCONV, RT_ENAN, RT_ETIMEOUT, RT_EOOM, RT_ECUDA, RT_ENOTREADY = range(8)
 RT_BC_FIXED, RT_BC_ZEROGRAD, RT_BC_LINEXTRAP = 0, 1, 2
-RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG, RT_MODEL_FENECR_LOG = 0, 1, 2, 3, 4
+(RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG, RT_MODEL_FENECR_LOG,
+ RT_MODEL_ROLIEPOLY_LOG) = 0, 1, 2, 3, 4, 5
 RT_PTT_LINEAR, RT_PTT_EXP = 0, 1
 RT_STAB_NONE, RT_STAB_BSD, RT_STAB_COUPLING = 0, 1, 2
 RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB = 0, 1
@@ -39,6 +40,7 @@ MODEL_NAMES = {
     "PTTLog": RT_MODEL_PTT_LOG,
     "FENE-PLog": RT_MODEL_FENEP_LOG,
     "FENE-CRLog": RT_MODEL_FENECR_LOG,
+    "Rolie-PolyLog": RT_MODEL_ROLIEPOLY_LOG,
 }
 LIMITER_NAMES = {
     "none": RT_LIM_NONE, "upwind": RT_LIM_UPWIND, "cubista": RT_LIM_CUBISTA,
@@ -77,6 +79,7 @@ class rt_model_params(C.Structure):
         ("model", C.c_int32), ("pttFunction", C.c_int32), ("stabilization", C.c_int32), ("pad_", C.c_int32),
         ("rho", C.c_double), ("etaS", C.c_double), ("etaP", C.c_double), ("lambda_", C.c_double),
         ("alpha", C.c_double), ("epsilon", C.c_double), ("zeta", C.c_double), ("L2", C.c_double),
+        ("lambdaR", C.c_double), ("beta", C.c_double), ("delta", C.c_double), ("chiMax", C.c_double),
     ]
 
 

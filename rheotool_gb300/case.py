@@ -3,7 +3,8 @@
 
 The keys mirror rheoTool's dictionaries one to one:
 ``constant/constitutiveProperties`` (``type``, ``rho``, ``etaS``, ``etaP``,
-``lambda``, ``alpha``, ``epsilon``, ``zeta``, ``L2``, ``stabilization``,
+``lambda``, ``alpha``, ``epsilon``, ``zeta``, ``L2``, ``lambdaR``/``lambdaD``,
+``beta``, ``delta``, ``chiMax`` (Rolie-Poly), ``stabilization``,
 ``destructionFunctionType``; read in e.g. ``GiesekusLog.C:93-120`` and
 ``constitutiveEq::checkForStab``), ``system/fvSolution`` (``solver``,
 ``preconditioner``, ``tolerance``, ``relTol``, ``minIter``, ``maxIter``,
@@ -54,6 +55,10 @@ class Model:
     epsilon: float = 0.0
     zeta: float = 0.0
     L2: float = 100.0
+    lambdaR: float = 1.0      # Rolie-PolyLog (its lambdaD is lambda_)
+    beta: float = 0.0
+    delta: float = -0.5
+    chiMax: float = 0.0
     stabilization: str = "coupling"
     destructionFunctionType: str = "linear"
 
@@ -64,7 +69,8 @@ class Model:
         ptt = abi.RT_PTT_EXP if self.destructionFunctionType == "exponential" else abi.RT_PTT_LINEAR
         return abi.rt_model_params(abi.MODEL_NAMES[self.type], ptt, STABS[self.stabilization], 0,
                                    self.rho, self.etaS, self.etaP, self.lambda_, self.alpha,
-                                   self.epsilon, self.zeta, self.L2)
+                                   self.epsilon, self.zeta, self.L2, self.lambdaR, self.beta,
+                                   self.delta, self.chiMax)
 
 
 Value = Union[float, Tuple[float, ...], Callable[[np.ndarray], np.ndarray]]

@@ -137,6 +137,18 @@ void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double 
     launch_count(ctx);
 }
 
+// Rolie-Poly stretch rate M1 = 2 (1 - sqrt(3/trA)) / lambdaR, times the
+// finite-extensibility factor when chiMax > 1 (RoliePolyLog.C:143-156)
+__host__ __device__ inline double roliepoly_chi(const rt_model_params &mp, double trA) {
+    const double c2 = mp.chiMax * mp.chiMax;
+    return ((3.0 - (trA / 3.0) / c2) * (1.0 - 1.0 / c2)) / ((1.0 - (trA / 3.0) / c2) * (3.0 - 1.0 / c2));
+}
+__host__ __device__ inline double roliepoly_m1(const rt_model_params &mp, double trA) {
+    double M1 = 2.0 * (1.0 - sqrt(3.0 / trA)) / mp.lambdaR;
+    if (mp.chiMax > 1.0) M1 *= roliepoly_chi(mp, trA);
+    return M1;
+}
+
 // ---------------------------------------------------------------------------
 // theta source: rhs = symm(Omega theta - theta Omega + 2B + S_model)
 // ---------------------------------------------------------------------------
@@ -185,6 +197,23 @@ __device__ __forceinline__ void theta_rhs_cell(int c, int N, const rt_model_para
                                                     : (1.0 + (mp.epsilon / (1.0 - zeta)) * (trA - 3.0));
 #pragma unroll
         for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
+    } else if (mp.model == RT_MODEL_ROLIEPOLY_LOG) {
+        // RoliePolyLog.C:140-179: -(1/lambdaD) A^-1 ((A - I) + M1 lambdaD (A + beta (trA/3)^delta (A - I)))
+        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
+        T3 Ai = mul(mul(R, dg(1.0 / e0, 1.0 / e1, 1.0 / e2)), Rt);
+        const double trA = A.a[0] + A.a[4] + A.a[8];
+        const double lamD = lambda;
+        const double M1 = roliepoly_m1(mp, trA);
+        const double ccr = mp.beta * pow(trA / 3.0, mp.delta);
+        T3 G;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const double AmI = A.a[i] - ((i % 4 == 0) ? 1.0 : 0.0);
+            G.a[i] = AmI + (M1 * lamD) * (A.a[i] + ccr * AmI);
+        }
+        T3 AG = mul(Ai, G);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S.a[i] = -((1.0 / lamD) * AG.a[i]);
     } else if (mp.model == RT_MODEL_FENECR_LOG) {
         // FENE_CRLog.C:140-163: (1/lambda) f R (Lambda^-1 - I) R^T, f from the pre-solve A
         T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
@@ -285,6 +314,8 @@ __device__ __forceinline__ void tau_cell(int c, int N, const rt_model_params &mp
         T = A;
         T.a[0] -= 1.0; T.a[4] -= 1.0; T.a[8] -= 1.0;
     }
+    if (mp.model == RT_MODEL_ROLIEPOLY_LOG && mp.chiMax > 1.0)   // RoliePolyLog.C:189-199
+        cP = cP * roliepoly_chi(mp, A.a[0] + A.a[4] + A.a[8]);
     tau[c] = cP * T.a[0];
     tau[(size_t)N + c] = cP * (0.5 * (T.a[1] + T.a[3]));
     tau[(size_t)2 * N + c] = cP * (0.5 * (T.a[2] + T.a[6]));
@@ -397,7 +428,7 @@ __global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restr
     if (c >= N) return;
     const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    if (!mix_fp32_ok(log(e0), log(e1), log(e2))) {
+    if (mp.model == RT_MODEL_ROLIEPOLY_LOG || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         theta_rhs_cell(c, N, mp, L, Rv, evv, theta, rhs, fP);
         return;
     }
@@ -492,7 +523,7 @@ __global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ 
     if (c >= N) return;
     const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    if (!mix_fp32_ok(log(e0), log(e1), log(e2))) {
+    if (mp.model == RT_MODEL_ROLIEPOLY_LOG || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         tau_cell(c, N, mp, Rv, evv, fP, tau);
         return;
     }

@@ -418,10 +418,12 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
     return guarded(ctx, [&]() -> rt_status {
         RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
         RT_REQUIRE(bc && mp && ctl, RT_EINVAL, "null argument");
-        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_FENECR_LOG, RT_EINVAL,
+        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_ROLIEPOLY_LOG, RT_EINVAL,
                    "unknown constitutive model");
         RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
         RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
+        RT_REQUIRE(mp->model != RT_MODEL_ROLIEPOLY_LOG || mp->lambdaR > 0, RT_EINVAL,
+                   "Rolie-Poly needs lambdaR > 0");
         RT_REQUIRE(ctl->divU >= RT_LIM_NONE && ctl->divU <= RT_LIM_SUPERBEE &&
                        ctl->divTheta >= RT_LIM_NONE && ctl->divTheta <= RT_LIM_SUPERBEE,
                    RT_EINVAL, "unknown GaussDefCmpw limiter");
@@ -779,7 +781,7 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model
             const Batch &b = ctx->mesh.batch;
             for (int c = 0; c < b.n; ++c) {
                 const rt_model_params &mp = models[c];
-                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_FENECR_LOG, RT_EINVAL,
+                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_ROLIEPOLY_LOG, RT_EINVAL,
                            "case " + std::to_string(c) + ": unknown constitutive model");
                 RT_REQUIRE(mp.lambda > 0 && mp.rho > 0, RT_EINVAL,
                            "case " + std::to_string(c) + ": lambda and rho must be positive");

@@ -251,7 +251,8 @@ def test_residual_matches_oracle(ctx):
 
 
 MODELS = [("Oldroyd-BLog", {}), ("GiesekusLog", {"alpha": 0.1}),
-          ("PTTLog", {"epsilon": 0.25}), ("FENE-PLog", {"L2": 100.0}), ("FENE-CRLog", {"L2": 20.0})]
+          ("PTTLog", {"epsilon": 0.25}), ("FENE-PLog", {"L2": 100.0}), ("FENE-CRLog", {"L2": 20.0}),
+          ("Rolie-PolyLog", {"lambdaR": 0.2, "chiMax": 5.0})]
 
 
 def flow_state(case, steps=3):

@@ -158,7 +158,11 @@ def zero_d(model, lam, etaP, dt, **kw):
     diag(1e-8, -1e-8, 0): from exactly theta = 0 with R = I, decomposeGradU
     gives B = 0 and Omega.theta - theta.Omega = 0 under pure shear, so the
     log-conformation update (rheoTool's as well) would stay at rest."""
+    # model keys that the case builder's own arguments shadow (Rolie-Poly's beta)
+    late = {k: kw.pop(k) for k in ("beta",) if k in kw}
     case = cavity_case(2, model=model, Wi=lam, beta=1.0 - etaP, Re=1.0, dt=dt, **kw)
+    for k, v in late.items():
+        setattr(case.model, k, v)
     f = Fields.zeros(case.mesh)
     f.theta[:, 0], f.theta[:, 3] = 1e-8, -1e-8
     f.eigVals[:, 0], f.eigVals[:, 1] = np.exp(1e-8), np.exp(-1e-8)
@@ -186,7 +190,13 @@ def test_oldroydb_startup_shear_closed_form():
     assert abs(txy - exact) < 2e-3 * exact
 
 
-def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
+def rp_chi(trA, chiMax):
+    c2 = chiMax * chiMax
+    return ((3.0 - (trA / 3.0) / c2) * (1.0 - 1.0 / c2)) / ((1.0 - (trA / 3.0) / c2) * (3.0 - 1.0 / c2))
+
+
+def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=1.0, beta=0.0, delta=-0.5,
+                        chiMax=0.0):
     """Steady simple shear of the conformation-tensor form, integrated with
     scipy (an independent formulation of the same model)."""
     from scipy.integrate import solve_ivp
@@ -204,6 +214,12 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
             g = (1.0 + eps * (np.trace(A) - 3.0)) * (A - I)
         elif model == "FENE-CRLog":
             g = (L2 / (L2 - np.trace(A))) * (A - I)
+        elif model == "Rolie-PolyLog":
+            trA = np.trace(A)
+            M1 = 2.0 * (1.0 - np.sqrt(3.0 / trA)) / lambdaR
+            if chiMax > 1.0:
+                M1 *= rp_chi(trA, chiMax)
+            g = (A - I) + lam * M1 * (A + beta * (trA / 3.0) ** delta * (A - I))
         else:
             f = L2 / (L2 - np.trace(A))
             a = L2 / (L2 - 3.0)
@@ -216,6 +232,8 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
         return (L2 / (L2 - np.trace(A))) * A - (L2 / (L2 - 3.0)) * I
     if model == "FENE-CRLog":
         return (L2 / (L2 - np.trace(A))) * (A - I)
+    if model == "Rolie-PolyLog" and chiMax > 1.0:
+        return rp_chi(np.trace(A), chiMax) * (A - I)
     return A - I
 
 
@@ -225,6 +243,10 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0):
     ("PTTLog", {"epsilon": 0.25}, {"eps": 0.25}),
     ("FENE-PLog", {"L2": 100.0}, {"L2": 100.0}),
     ("FENE-CRLog", {"L2": 20.0}, {"L2": 20.0}),
+    ("Rolie-PolyLog", {"lambdaR": 0.2, "beta": 0.5, "delta": -0.5},
+     {"lambdaR": 0.2, "beta": 0.5, "delta": -0.5}),
+    ("Rolie-PolyLog", {"lambdaR": 0.3, "beta": 0.3, "delta": -0.5, "chiMax": 5.0},
+     {"lambdaR": 0.3, "beta": 0.3, "delta": -0.5, "chiMax": 5.0}),
 ])
 def test_steady_shear_matches_conformation_form(model, kw, ckw):
     lam, etaP, rate = 1.0, 0.8, 1.5
