@@ -59,7 +59,31 @@ def build(verbose: bool = False, extra=()) -> str:
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    build_host()
     return OUT
+
+
+HOST = os.path.join(HERE, "host")
+HOST_OUT = os.path.join(HERE, "librheogpu_host.so")
+
+
+def build_host() -> str:
+    """The C++ host mirror (host/rheogpu_host.cpp) as librheogpu_host.so,
+    linked to librheogpu.so beside it."""
+    src = os.path.join(HOST, "rheogpu_host.cpp")
+    deps = [src, os.path.join(HOST, "rheogpu.hpp"), os.path.join(HERE, "..", "include", "rheogpu.h"), OUT]
+    if os.path.exists(HOST_OUT) and all(os.path.getmtime(d) <= os.path.getmtime(HOST_OUT) for d in deps):
+        return HOST_OUT
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("no C++ compiler for the host library")
+    cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-o", HOST_OUT, src, "-L" + HERE, "-lrheogpu",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        raise RuntimeError("host library build failed")
+    return HOST_OUT
 
 
 if __name__ == "__main__":

@@ -1,0 +1,187 @@
+// test_host.cpp — checks of the C++ host mirror (rheotool_gb300/host).
+//   --cpu : dictionary parsing, run-time selection and its errors, and the
+//           error raised when no GPU can be opened (no compute call)
+//   --gpu : LduSolver::New + solve on a chain of cells (PCG-DIC and
+//           PBiCGStab-DILU) against a direct tridiagonal solve
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../rheotool_gb300/host/rheogpu.hpp"
+
+using namespace rheogpu;
+
+static int failures = 0;
+#define CHECK(c)                                                              \
+    do {                                                                      \
+        if (!(c)) {                                                           \
+            std::fprintf(stderr, "FAILED %s:%d: %s\n", __FILE__, __LINE__, #c); \
+            ++failures;                                                       \
+        }                                                                     \
+    } while (0)
+
+template <class F>
+static std::string throws(F f) {
+    try {
+        f();
+    } catch (const FatalError &e) {
+        return e.what();
+    }
+    return "";
+}
+
+static void cpu_checks() {
+    const char *props =
+        "/* constitutiveProperties */\n"
+        "parameters\n{\n    type            GiesekusLog;\n    rho             rho [1 -3 0 0 0 0 0] 0.01;\n"
+        "    etaS 0.111; etaP 0.889;  // comment\n    lambda 0.5;\n    alpha 0.1;\n"
+        "    stabilization   coupling;\n    nested { a 1; b (0 0 1); }\n}\n";
+    Dictionary d = Dictionary::parse(props, "constitutiveProperties");
+    const Dictionary &p = d.subDict("parameters");
+    CHECK(p.lookup("type") == "GiesekusLog");
+    CHECK(p.subDict("nested").lookup("b") == "(0 0 1)");
+    CHECK(std::fabs(p.lookupScalar("alpha") - 0.1) < 1e-15);
+    CHECK(p.lookupOrDefault("missing", 7.0) == 7.0);
+    CHECK(throws([&] { p.lookup("missing"); }).find("keyword missing is undefined") != std::string::npos);
+
+    // rho carries OpenFOAM's dimensioned form in the reference dictionaries:
+    // the plain-number form is what the mirror reads
+    Dictionary q = Dictionary::parse("type GiesekusLog; rho 0.01; etaS 0.111; etaP 0.889; lambda 0.5; alpha 0.1;"
+                                     " stabilization coupling;", "parameters");
+    auto ce = ConstitutiveEq::New("ce", q);
+    CHECK(ce->type() == "GiesekusLog" && ce->params().model == RT_MODEL_GIESEKUS_LOG);
+    CHECK(ce->params().stabilization == RT_STAB_COUPLING && std::fabs(ce->etaP() - 0.889) < 1e-15);
+    CHECK(!ce->isGNF());
+
+    Dictionary rp = Dictionary::parse("type Rolie-PolyLog; rho 1; etaS 0.1; etaP 0.9; lambdaD 1.0; lambdaR 0.2;"
+                                      " beta 0.5; delta -0.5; chiMax 5; stabilization none;");
+    auto r = ConstitutiveEq::New("rp", rp);
+    CHECK(r->params().model == RT_MODEL_ROLIEPOLY_LOG && r->params().lambda == 1.0 && r->params().lambdaR == 0.2);
+
+    Dictionary bad = Dictionary::parse("type BoguerLog; rho 1; etaS 1; etaP 1; lambda 1; stabilization none;");
+    std::string m = throws([&] { ConstitutiveEq::New("x", bad); });
+    CHECK(m.find("Unknown constitutiveEq type BoguerLog") != std::string::npos);
+    CHECK(m.find("Oldroyd-BLog") != std::string::npos && m.find("FENE-PLog") != std::string::npos);
+
+    Dictionary ptt = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
+                                       " destructionFunctionType exponential; stabilization BSD;");
+    auto pt = ConstitutiveEq::New("p", ptt);
+    CHECK(pt->params().pttFunction == RT_PTT_EXP && pt->params().stabilization == RT_STAB_BSD);
+    Dictionary nostab = Dictionary::parse("type Oldroyd-BLog; rho 1; etaS 1; etaP 1; lambda 1;");
+    CHECK(throws([&] { ConstitutiveEq::New("o", nostab); }).find("stabilization") != std::string::npos);
+
+    Dictionary sol = Dictionary::parse("p { solver PCG; preconditioner DIC; tolerance 1e-8; relTol 0; }"
+                                       " U { solver PBiCG; preconditioner DILU; }"
+                                       " T { solver PBiCGStab; preconditioner { preconditioner DILU; } }");
+    rt_solver_ctl cp = LduSolver::readControls(sol.subDict("p"));
+    CHECK(cp.solver == RT_SOLVER_PCG && cp.preconditioner == RT_PRECOND_DIC && cp.tolerance == 1e-8);
+    CHECK(cp.maxIter == 1000 && cp.minIter == 0 && cp.relTol == 0.0);
+    rt_solver_ctl ct = LduSolver::readControls(sol.subDict("T"));
+    CHECK(ct.solver == RT_SOLVER_PBICGSTAB && ct.preconditioner == RT_PRECOND_DILU && ct.tolerance == 1e-6);
+    std::string e1 = throws([&] { LduSolver::readControls(sol.subDict("U")); });
+    CHECK(e1.find("Unknown lduMatrix::solver PBiCG") != std::string::npos);
+
+    std::string e2 = throws([&] { Context ctx(0); });
+    CHECK(e2.find("rt_ctx_create") != std::string::npos);
+}
+
+// chain of n cells (one face between neighbours), no boundary faces
+struct Chain {
+    int n;
+    std::vector<int32_t> own, nei;
+    std::vector<double> Sf, magSf, Cf, w, dc, C, V;
+    rt_mesh_desc desc{};
+    explicit Chain(int n_) : n(n_) {
+        for (int f = 0; f + 1 < n; ++f) {
+            own.push_back(f);
+            nei.push_back(f + 1);
+            Sf.insert(Sf.end(), {1.0, 0.0, 0.0});
+            magSf.push_back(1.0);
+            Cf.insert(Cf.end(), {f + 1.0, 0.0, 0.0});
+            w.push_back(0.5);
+            dc.push_back(1.0);
+        }
+        for (int c = 0; c < n; ++c) {
+            C.insert(C.end(), {c + 0.5, 0.0, 0.0});
+            V.push_back(1.0);
+        }
+        desc.nCells = n;
+        desc.nFaces = n - 1;
+        desc.owner = own.data();
+        desc.neighbour = nei.data();
+        desc.Sf = Sf.data();
+        desc.magSf = magSf.data();
+        desc.Cf = Cf.data();
+        desc.weights = w.data();
+        desc.deltaCoeffs = dc.data();
+        desc.C = C.data();
+        desc.V = V.data();
+        desc.solveDir[0] = desc.solveDir[1] = desc.solveDir[2] = 1;
+    }
+};
+
+// Thomas algorithm for the tridiagonal LDU system
+static std::vector<double> thomas(const std::vector<double> &d, const std::vector<double> &up,
+                                  const std::vector<double> &lo, const std::vector<double> &b) {
+    const int n = (int)d.size();
+    std::vector<double> c(n), x(n), dd(d), bb(b);
+    for (int i = 1; i < n; ++i) {   // row i: lo[i-1] x[i-1] + d[i] x[i] + up[i] x[i+1]
+        double m = lo[i - 1] / dd[i - 1];
+        dd[i] -= m * up[i - 1];
+        bb[i] -= m * bb[i - 1];
+    }
+    x[n - 1] = bb[n - 1] / dd[n - 1];
+    for (int i = n - 2; i >= 0; --i) x[i] = (bb[i] - up[i] * x[i + 1]) / dd[i];
+    return x;
+}
+
+static void gpu_checks() {
+    const int n = 5000;
+    Chain ch(n);
+    Context ctx(0);
+    ctx.uploadMesh(ch.desc);
+    std::vector<double> b(n);
+    unsigned s = 12345u;
+    for (int i = 0; i < n; ++i) {
+        s = s * 1664525u + 1013904223u;
+        b[i] = (double)(s >> 8) / (double)(1u << 24) - 0.5;
+    }
+    Dictionary sol = Dictionary::parse("p { solver PCG; preconditioner DIC; tolerance 1e-12; maxIter 20000; }"
+                                       " T { solver PBiCGStab; preconditioner { preconditioner DILU; }"
+                                       " tolerance 1e-12; maxIter 20000; }");
+    for (const char *field : {"p", "T"}) {
+        const bool sym = std::string(field) == "p";
+        std::vector<double> d(n, sym ? 2.01 : 2.05), up(n - 1, sym ? -1.0 : -1.2), lo(n - 1, sym ? -1.0 : -0.8);
+        LduMatrixView mv{d.data(), up.data(), lo.data()};
+        auto solver = LduSolver::New(field, ctx, mv, sol.subDict(field));
+        std::vector<double> x(n, 0.0);
+        SolverPerformance perf = solver->solve(x.data(), b.data());
+        std::vector<double> ref = thomas(d, up, lo, b);
+        double num = 0, den = 0;
+        for (int i = 0; i < n; ++i) {
+            num += (x[i] - ref[i]) * (x[i] - ref[i]);
+            den += ref[i] * ref[i];
+        }
+        std::printf("%s: %s %d iterations, residual %.3e -> %.3e, rel error %.3e\n", field,
+                    perf.solverName.c_str(), perf.nIterations, perf.initialResidual, perf.finalResidual,
+                    std::sqrt(num / den));
+        CHECK(perf.converged && perf.nIterations > 0);
+        CHECK(std::sqrt(num / den) < 1e-8);
+    }
+}
+
+int main(int argc, char **argv) {
+    const bool gpu = argc > 1 && std::strcmp(argv[1], "--gpu") == 0;
+    try {
+        if (gpu) gpu_checks();
+        else cpu_checks();
+    } catch (const FatalError &e) {
+        std::fprintf(stderr, "FatalError: %s\n", e.what());
+        return 2;
+    }
+    if (failures) return 1;
+    std::printf("host checks passed (%s)\n", gpu ? "gpu" : "cpu");
+    return 0;
+}
