@@ -162,7 +162,10 @@ typedef struct {
     int32_t pRefCell, needReference; /* needReference: p has no fixed patch    */
     double pRefValue;
     rt_solver_ctl solverU, solverP, solverTheta;
-    int32_t precision, pad_;
+    int32_t precision;
+    int32_t nInIter;                 /* inner iterations of a step (UEqn, pEqn,
+                                        constEq.correct() on the step's old-time
+                                        fields; rheoFoam.C:96-150); 0 or 1: one */
     /* uniform body force per unit mass in the momentum equation (the source
      * an fvOptions meanVelocityForce / pressure-gradient source adds to UEqn
      * to drive a periodic channel); zero for the other cases                */

@@ -687,7 +687,10 @@ static double rp_m1(const rt_model_params *mp, double trA) {
     return M1;
 }
 
-static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_perf *perf) {
+/* thetaOld: theta at the start of the time step (the inner iterations of a
+ * step share it); NULL = the current theta */
+static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_perf *perf,
+                                const double *thetaOld) {
     const rt_mesh_desc *m = k->m;
     const rt_model_params *mp = k->mp;
     or_state *s = k->s;
@@ -779,7 +782,7 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
     or_matrix Mx;
     mat_alloc(&Mx, m, 6);
     double *theta0 = DALLOC(6 * (size_t)N);
-    memcpy(theta0, s->theta, sizeof(double) * 6 * N);
+    memcpy(theta0, thetaOld ? thetaOld : s->theta, sizeof(double) * 6 * N);
     or_matrix Md;
     mat_alloc(&Md, m, 6);
     add_ddt(m, 1.0 / k->ctl->deltaT, theta0, 6, &Mx);
@@ -837,7 +840,7 @@ int or_constitutive_correct(const rt_mesh_desc *m, const rt_bc_desc *bc,
                             or_state *s, const double *gradU, rt_solver_perf *perf) {
     or_case k;
     case_init(&k, m, bc, mp, ctl, s);
-    int st = constitutive_correct(&k, gradU, perf);
+    int st = constitutive_correct(&k, gradU, perf, NULL);
     case_free(&k);
     return st;
 }
@@ -926,7 +929,10 @@ static void fvc_laplacian(const rt_mesh_desc *m, const double *U, const double *
 /* ------------------------------------------------------------------------ */
 /* one segregated rheoFoam step                                               */
 /* ------------------------------------------------------------------------ */
-static int step_once(or_case *k, rt_step_perf *perf) {
+/* One inner iteration of a time step: UEqn, pEqn and constEq.correct() with
+ * the old-time fields of the step (U, phi and theta at its start). */
+static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const double *U0bs,
+                      const double *phi0s, const double *phi0bs, const double *theta0s) {
     const rt_mesh_desc *m = k->m;
     const rt_model_params *mp = k->mp;
     const rt_case_ctl *ctl = k->ctl;
@@ -938,8 +944,8 @@ static int step_once(or_case *k, rt_step_perf *perf) {
     /* old-time fields */
     double *U0 = DALLOC(3 * (size_t)N), *U0b = DALLOC(3 * (size_t)nB);
     double *phi0 = DALLOC(nF), *phi0b = DALLOC(nB);
-    memcpy(U0, s->U, sizeof(double) * 3 * N); memcpy(U0b, s->Ub, sizeof(double) * 3 * nB);
-    memcpy(phi0, s->phi, sizeof(double) * nF); memcpy(phi0b, s->phib, sizeof(double) * nB);
+    memcpy(U0, U0s, sizeof(double) * 3 * N); memcpy(U0b, U0bs, sizeof(double) * 3 * nB);
+    memcpy(phi0, phi0s, sizeof(double) * nF); memcpy(phi0b, phi0bs, sizeof(double) * nB);
 
     /* ---------------- UEqn ---------------- */
     double *G = DALLOC(9 * (size_t)N), *Gb = DALLOC(9 * (size_t)nB);
@@ -1181,7 +1187,28 @@ static int step_once(or_case *k, rt_step_perf *perf) {
     free(U0); free(U0b); free(phi0); free(phi0b);
 
     /* ---------------- constEq.correct() ---------------- */
-    return constitutive_correct(k, NULL, perf->theta);
+    return constitutive_correct(k, NULL, perf->theta, theta0s);
+}
+
+/* One time step: nInIter inner iterations (rheoFoam.C:96-150; createControls.H
+ * nInIter, 0 meaning 1) on the old-time fields of the step. */
+static int step_once(or_case *k, rt_step_perf *perf) {
+    const rt_mesh_desc *m = k->m;
+    or_state *s = k->s;
+    const int N = m->nCells, nF = m->nFaces, nB = m->nBFaces;
+    double *U0 = DALLOC(3 * (size_t)N), *U0b = DALLOC(3 * (size_t)nB);
+    double *phi0 = DALLOC(nF), *phi0b = DALLOC(nB), *theta0 = DALLOC(6 * (size_t)N);
+    memcpy(U0, s->U, sizeof(double) * 3 * N); memcpy(U0b, s->Ub, sizeof(double) * 3 * nB);
+    memcpy(phi0, s->phi, sizeof(double) * nF); memcpy(phi0b, s->phib, sizeof(double) * nB);
+    memcpy(theta0, s->theta, sizeof(double) * 6 * N);
+    const int nIn = k->ctl->nInIter > 1 ? k->ctl->nInIter : 1;
+    int st = RT_OK;
+    for (int it = 0; it < nIn && st == RT_OK; ++it) {
+        memset(perf, 0, sizeof *perf);
+        st = step_inner(k, perf, U0, U0b, phi0, phi0b, theta0);
+    }
+    free(U0); free(U0b); free(phi0); free(phi0b); free(theta0);
+    return st;
 }
 
 int or_step(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *mp,

@@ -110,7 +110,7 @@ class rt_case_ctl(C.Structure):
         ("pRefCell", C.c_int32), ("needReference", C.c_int32),
         ("pRefValue", C.c_double),
         ("solverU", rt_solver_ctl), ("solverP", rt_solver_ctl), ("solverTheta", rt_solver_ctl),
-        ("precision", C.c_int32), ("pad_", C.c_int32),
+        ("precision", C.c_int32), ("nInIter", C.c_int32),
         ("bodyForce", C.c_double * 3),
     ]
 

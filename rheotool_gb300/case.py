@@ -92,6 +92,7 @@ class Case:
     precision: int = abi.RT_PREC_FP64
     name: str = "case"
     bodyForce: Tuple[float, float, float] = (0.0, 0.0, 0.0)   # per unit mass, in UEqn
+    nInIter: int = 1          # SIMPLE.nInIter: inner iterations per time step
 
     # ------------------------------------------------------------------
     def _field_bc(self, fld: str, ncomp: int):
@@ -163,6 +164,7 @@ class Case:
         ctl.solverP = self.solverP.to_c()
         ctl.solverTheta = self.solverTheta.to_c()
         ctl.precision = self.precision
+        ctl.nInIter = int(self.nInIter)
         for k in range(3):
             ctl.bodyForce[k] = float(self.bodyForce[k])
         self._keep = keep

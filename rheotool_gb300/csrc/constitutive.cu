@@ -611,7 +611,7 @@ unsigned theta_valid_mask(const DevMesh &m) {
     return mask;
 }
 
-rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf) {
+rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf, const double *thetaOld) {
     DevMesh &mesh = ctx->mesh;
     DevCase &cs = ctx->cs;
     const int N = mesh.N, F = mesh.F, NB = mesh.NB;
@@ -641,7 +641,8 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
                                                         cs.eigVals.p, cs.theta.p, rhs, fP);
         RT_CHECK_LAUNCH();
     }
-    RT_CUDA(cudaMemcpyAsync(theta0, cs.theta.p, sizeof(double) * 6 * N, cudaMemcpyDeviceToDevice, s));
+    RT_CUDA(cudaMemcpyAsync(theta0, thetaOld ? thetaOld : cs.theta.p, sizeof(double) * 6 * N,
+                            cudaMemcpyDeviceToDevice, s));
     const double fpc = (double)F / N;
     {
         ProfScope ps(ctx, "grad", (double)N * (48.0 + fpc * 16.0 + 72.0 + 144.0));

@@ -355,7 +355,10 @@ void launch_count(rt_ctx *ctx, int n = 1);
 
 // constitutive.cu
 void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double *eigVecs);
-rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf);
+// thetaOld: theta at the start of the time step (shared by its inner
+// iterations); null = the current theta
+rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf,
+                               const double *thetaOld = nullptr);
 
 // step.cu
 rt_status step_once(rt_ctx *ctx, rt_step_perf *perf);

@@ -533,7 +533,10 @@ __global__ void k_U_correct(int N, const double *__restrict__ HbyA, const double
 }
 
 // ---------------------------------------------------------------------------
-rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
+// one inner iteration of a time step (UEqn, pEqn, constEq.correct()) on the
+// step's old-time fields U0, U0b, phi0, phi0b and theta0 (null: the current theta)
+static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, const double *U0b,
+                            const double *phi0, const double *phi0b, const double *theta0) {
     DevMesh &mesh = ctx->mesh;
     DevCase &cs = ctx->cs;
     const rt_case_ctl &ctl = cs.ctl;
@@ -545,13 +548,6 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     Work &W = ctx->work;
     WorkMark wmark(W);
     const int gN = nblocks(N), gF = nblocks(F), gB = nblocks(std::max(NB, 1));
-
-    // old-time fields
-    double *U0 = W.take(3 * (size_t)N), *U0b = W.take(3 * (size_t)NB), *phi0 = W.take(F), *phi0b = W.take(NB);
-    RT_CUDA(cudaMemcpyAsync(U0, cs.U.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
-    if (NB) RT_CUDA(cudaMemcpyAsync(U0b, cs.Ub.p, sizeof(double) * 3 * NB, cudaMemcpyDeviceToDevice, s));
-    if (F) RT_CUDA(cudaMemcpyAsync(phi0, cs.phi.p, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
-    if (NB) RT_CUDA(cudaMemcpyAsync(phi0b, cs.phib.p, sizeof(double) * NB, cudaMemcpyDeviceToDevice, s));
 
     // ---------------- UEqn ----------------
     double *G = W.take(9 * (size_t)N);
@@ -663,7 +659,35 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     perf->contErrGlobal = 0.0;
 
     // ---------------- constEq.correct() ----------------
-    return constitutive_correct(ctx, nullptr, perf->theta);
+    return constitutive_correct(ctx, nullptr, perf->theta, theta0);
+}
+
+// one time step: nInIter inner iterations (rheoFoam.C:96-150; 0 means 1)
+// on the old-time fields taken at its start
+rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
+    DevMesh &mesh = ctx->mesh;
+    DevCase &cs = ctx->cs;
+    const int N = mesh.N, F = mesh.F, NB = mesh.NB;
+    cudaStream_t s = ctx->stream;
+    Work &W = ctx->work;
+    WorkMark wmark(W);
+    const int nIn = cs.ctl.nInIter > 1 ? cs.ctl.nInIter : 1;
+    double *U0 = W.take(3 * (size_t)N), *U0b = W.take(3 * (size_t)NB), *phi0 = W.take(F), *phi0b = W.take(NB);
+    RT_CUDA(cudaMemcpyAsync(U0, cs.U.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+    if (NB) RT_CUDA(cudaMemcpyAsync(U0b, cs.Ub.p, sizeof(double) * 3 * NB, cudaMemcpyDeviceToDevice, s));
+    if (F) RT_CUDA(cudaMemcpyAsync(phi0, cs.phi.p, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
+    if (NB) RT_CUDA(cudaMemcpyAsync(phi0b, cs.phib.p, sizeof(double) * NB, cudaMemcpyDeviceToDevice, s));
+    double *theta0 = nullptr;
+    if (nIn > 1) {
+        theta0 = W.take(6 * (size_t)N);
+        RT_CUDA(cudaMemcpyAsync(theta0, cs.theta.p, sizeof(double) * 6 * N, cudaMemcpyDeviceToDevice, s));
+    }
+    rt_status st = RT_OK;
+    for (int it = 0; it < nIn && st == RT_OK; ++it) {
+        *perf = rt_step_perf{};
+        st = step_inner(ctx, perf, U0, U0b, phi0, phi0b, theta0);
+    }
+    return st;
 }
 
 }  // namespace rt

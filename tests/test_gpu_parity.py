@@ -434,3 +434,11 @@ def test_systolic_cluster_sizes_equal_level_sweeps(ctx, planes, solver, pre, asy
         ctx.set_sweep(abi.SWEEP_AUTO)
     assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
     assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
+
+
+def test_step_inner_iterations(ctx):
+    """SIMPLE nInIter = 3: UEqn, pEqn and constEq.correct() three times per
+    step on the step's old-time fields (rheoFoam.C:96-150), against the oracle."""
+    case = cavity_case(16, model="GiesekusLog", alpha=0.1, Wi=0.5, dt=5e-3)
+    case.nInIter = 3
+    assert_step_parity(ctx, case, 4)

@@ -129,3 +129,28 @@ def test_periodic_channel_state_ptt():
     o = Oracle(case, fields=f.copy())
     o.step(1)
     assert np.isfinite(o.f.U).all() and np.isfinite(o.f.theta).all()
+
+
+def test_inner_iterations_steady_profile_and_default():
+    """SIMPLE nInIter: 0 and 1 are the same step (bit for bit); with 2 inner
+    iterations per step the steady Oldroyd-B channel reaches the same laminar
+    profile."""
+    mesh = periodic_channel_mesh(3, 24, 3, L=1.0, depth=1.0, wall_ratio=1.0)
+    a = periodic_channel_case(mesh, model="Oldroyd-BLog", Wi=0.05, beta=0.5, rho=0.01, dt=2e-3)
+    b = periodic_channel_case(mesh, model="Oldroyd-BLog", Wi=0.05, beta=0.5, rho=0.01, dt=2e-3)
+    b.nInIter = 0
+    oa, ob = Oracle(a), Oracle(b)
+    oa.step(3)
+    ob.step(3)
+    assert np.array_equal(oa.f.U, ob.f.U) and np.array_equal(oa.f.theta, ob.f.theta)
+    c = periodic_channel_case(mesh, model="Oldroyd-BLog", Wi=0.05, beta=0.5, rho=0.01, dt=2e-3)
+    c.nInIter = 2
+    c.solverP.tolerance = 1e-10
+    oc = Oracle(c)
+    oc.step(3)
+    assert not np.array_equal(oc.f.U, oa.f.U)       # the inner iteration changes the transient
+    oc.step(297)
+    nx, ny, nz = mesh.shape
+    y = mesh.C[:ny * nx:nx, 1]
+    u = oc.f.U[:ny * nx:nx, 0]
+    assert np.max(np.abs(u - 1.5 * (1.0 - y ** 2))) < 5e-3 * 1.5
