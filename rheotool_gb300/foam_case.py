@@ -1,0 +1,307 @@
+"""Run an OpenFOAM/rheoTool case directory through the library.
+
+``load_case(case_dir)`` reads what rheoFoam reads for the segregated step:
+
+* ``constant/polyMesh`` (``foam_io.read_polymesh``);
+* ``constant/constitutiveProperties``: the ``parameters`` sub-dictionary
+  (``type``, ``rho``, ``etaS``, ``etaP``, ``lambda`` ... ``stabilization``;
+  dimensioned entries ``rho rho [1 -3 0 0 0 0 0] 0.01;`` give their number);
+* ``system/fvSolution``: the ``solvers`` entries for p, U and theta (keys may
+  be quoted regular expressions such as ``"(theta|tau)"``) and ``SIMPLE``
+  (``nInIter``, ``pRefCell``, ``pRefValue``);
+* ``system/fvSchemes``: ``div(phi,U)`` and ``div(phi,theta)`` (GaussDefCmpw
+  with a limiter) and the ddt scheme;
+* ``system/controlDict``: ``deltaT``, ``endTime``, ``writeInterval``;
+* ``0/U``, ``0/p``, ``0/theta``, ``0/tau``: initial internal fields and the
+  boundary conditions (fixedValue, zeroGradient, linearExtrapolation; empty
+  and cyclic patches are part of the mesh).
+
+What the library does not implement is refused with a clear message unless
+``substitute=True`` is given, in which case each substitution is recorded in
+``loaded.substitutions``: PBiCG becomes PBiCGStab (same preconditioner and
+tolerance); Crank-Nicolson ddt becomes Euler; a ``codedFixedValue`` patch
+(its code cannot run here) uses its ``value`` entry unless
+``bc_overrides`` gives the values.  ``run_case`` steps the case on the GPU
+and writes OpenFOAM fields at the write times.
+
+    python -m rheotool_gb300.foam_case CASE_DIR [--steps N] [--substitute] [--mixed]
+"""
+from __future__ import annotations
+
+import argparse
+import fnmatch
+import os
+import re
+from dataclasses import dataclass, field
+from typing import Any, Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import abi, foam_io
+from .case import Case, Fields, Model, SolverControl
+
+# ---------------------------------------------------------------------------
+# dictionaries
+# ---------------------------------------------------------------------------
+
+
+def parse_dict(text: str) -> Dict[str, Any]:
+    """OpenFOAM dictionary text -> nested dict of raw string values (the
+    FoamFile header is skipped; comments removed)."""
+    t = foam_io._strip(text)
+    pos = 0
+
+    def level(i: int) -> Tuple[Dict[str, Any], int]:
+        d: Dict[str, Any] = {}
+        n = len(t)
+        while i < n:
+            while i < n and t[i].isspace():
+                i += 1
+            if i >= n:
+                break
+            if t[i] == "}":
+                return d, i + 1
+            if t[i] == '"':
+                e = t.index('"', i + 1)
+                key = t[i + 1:e]
+                i = e + 1
+            else:
+                s = i
+                while i < n and not t[i].isspace() and t[i] not in "{;":
+                    i += 1
+                key = t[s:i]
+            while i < n and t[i].isspace():
+                i += 1
+            if i < n and t[i] == "{":
+                sub, i = level(i + 1)
+                d[key] = sub
+                continue
+            s, depth = i, 0
+            while i < n and not (t[i] == ";" and depth == 0):
+                if t[i] == "(":
+                    depth += 1
+                elif t[i] == ")":
+                    depth -= 1
+                i += 1
+            d[key] = t[s:i].strip()
+            i += 1
+        return d, i
+
+    d, _ = level(pos)
+    d.pop("FoamFile", None)
+    return d
+
+
+def read_dict(path: str) -> Dict[str, Any]:
+    return parse_dict(foam_io._read_text(path))
+
+
+def scalar(v: str) -> float:
+    """The number of a plain or dimensioned scalar entry."""
+    nums = re.findall(r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?", v.split("]")[-1])
+    if not nums:
+        raise ValueError(f"no number in {v!r}")
+    return float(nums[-1])
+
+
+def lookup_pattern(d: Dict[str, Any], name: str) -> Optional[Any]:
+    """An entry by exact name, else by a key that is a regular expression
+    (OpenFOAM's quoted keys) or a glob matching it."""
+    if name in d:
+        return d[name]
+    for k, v in d.items():
+        try:
+            if re.fullmatch(k, name):
+                return v
+        except re.error:
+            pass
+        if fnmatch.fnmatch(name, k):
+            return v
+    return None
+
+
+# ---------------------------------------------------------------------------
+# the case
+# ---------------------------------------------------------------------------
+LIMITERS = {"upwind", "cubista", "minmod", "smart", "waceb", "superbee"}
+
+
+@dataclass
+class LoadedCase:
+    case: Case
+    fields: Fields
+    endTime: float
+    writeInterval: float
+    substitutions: List[str] = field(default_factory=list)
+
+
+class CaseError(ValueError):
+    pass
+
+
+def _solver(d: Dict[str, Any], name: str, subs: List[str], substitute: bool) -> SolverControl:
+    e = lookup_pattern(d, name)
+    if e is None:
+        raise CaseError(f"fvSolution: no solver entry for {name}")
+    sv = e.get("solver", "")
+    if sv == "PBiCG":
+        if not substitute:
+            raise CaseError(f"fvSolution {name}: solver PBiCG is not implemented (PBiCGStab is); "
+                            "pass substitute=True to use PBiCGStab")
+        subs.append(f"{name}: PBiCG -> PBiCGStab")
+        sv = "PBiCGStab"
+    if sv not in ("PCG", "PBiCGStab"):
+        raise CaseError(f"fvSolution {name}: solver {sv!r} is not implemented (PCG, PBiCGStab)")
+    pre = e.get("preconditioner", "none")
+    if isinstance(pre, dict):
+        pre = pre.get("preconditioner", "none")
+    if pre not in ("DIC", "DILU", "diagonal", "none"):
+        raise CaseError(f"fvSolution {name}: preconditioner {pre!r} is not implemented")
+    return SolverControl(sv, pre, scalar(e.get("tolerance", "1e-6")), scalar(e.get("relTol", "0")),
+                         int(scalar(e.get("minIter", "0"))), int(scalar(e.get("maxIter", "1000"))))
+
+
+def _limiter(schemes: Dict[str, Any], key: str) -> str:
+    v = lookup_pattern(schemes.get("divSchemes", {}), key)
+    if v is None:
+        v = schemes.get("divSchemes", {}).get("default", "none")
+    words = v.split()
+    if len(words) >= 2 and words[0] == "GaussDefCmpw" and words[1] in LIMITERS:
+        return words[1]
+    if words[:2] == ["Gauss", "upwind"]:
+        return "upwind"
+    raise CaseError(f"fvSchemes {key}: {v!r} is not implemented (GaussDefCmpw <limiter> or Gauss upwind)")
+
+
+def load_case(case_dir: str, substitute: bool = False,
+              bc_overrides: Optional[Dict[str, Dict[str, Tuple[str, Any]]]] = None,
+              precision: int = abi.RT_PREC_FP64) -> LoadedCase:
+    subs: List[str] = []
+    mesh = foam_io.read_polymesh(case_dir)
+    cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
+    par = cp.get("parameters", cp)
+    typ = par.get("type", "")
+    if typ not in abi.MODEL_NAMES:
+        raise CaseError(f"Unknown constitutiveEq type {typ}; valid: {sorted(abi.MODEL_NAMES)}")
+    mkw: Dict[str, Any] = dict(type=typ, rho=scalar(par["rho"]), etaS=scalar(par["etaS"]), etaP=scalar(par["etaP"]),
+                               stabilization=par.get("stabilization", "none"))
+    mkw["lambda_"] = scalar(par["lambdaD"] if typ == "Rolie-PolyLog" else par["lambda"])
+    for k in ("alpha", "epsilon", "zeta", "L2", "lambdaR", "beta", "delta", "chiMax"):
+        if k in par:
+            mkw[k] = scalar(par[k])
+    if "destructionFunctionType" in par:
+        mkw["destructionFunctionType"] = par["destructionFunctionType"]
+    model = Model(**mkw)
+
+    sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))
+    solvers = sol.get("solvers", {})
+    simple = sol.get("SIMPLE", {})
+    sch = read_dict(os.path.join(case_dir, "system", "fvSchemes"))
+    ddt = sch.get("ddtSchemes", {}).get("default", "Euler").split()[0]
+    if ddt != "Euler":
+        if not substitute:
+            raise CaseError(f"fvSchemes ddt {ddt} is not implemented (Euler); pass substitute=True for Euler")
+        subs.append(f"ddt: {ddt} -> Euler")
+    ctrl = read_dict(os.path.join(case_dir, "system", "controlDict"))
+
+    # boundary conditions and initial fields
+    ncomp = {"U": 3, "p": 1, "theta": 6, "tau": 6}
+    kinds = {"fixedValue", "zeroGradient", "linearExtrapolation"}
+    bcs: Dict[str, Dict[str, Tuple[str, Any]]] = {p.name: {} for p in mesh.patches}
+    f = Fields.zeros(mesh)
+    for name, nc in ncomp.items():
+        path = os.path.join(case_dir, "0", name)
+        internal, bf = foam_io.read_field(path, n_internal=mesh.nCells)
+        arr = np.asarray(internal, dtype=np.float64).reshape(mesh.nCells, nc) if nc > 1 else np.asarray(internal)
+        getattr(f, name)[:] = arr
+        for p in mesh.patches:
+            e = lookup_pattern(bf, p.name)
+            if e is None:
+                raise CaseError(f"0/{name}: no boundary condition for patch {p.name}")
+            typ_b = e["type"]
+            val = None
+            if e["value"] is not None:
+                v = np.asarray(e["value"], dtype=np.float64)
+                val = np.broadcast_to(v.reshape(-1, nc) if v.size != nc else v.reshape(1, nc), (p.size, nc)).copy()
+            ov = (bc_overrides or {}).get(p.name, {}).get(name)
+            if ov is not None:
+                bcs[p.name][name] = ov
+                continue
+            if typ_b == "codedFixedValue":
+                if not substitute:
+                    raise CaseError(f"0/{name} patch {p.name}: codedFixedValue cannot run here; give bc_overrides "
+                                    "or pass substitute=True to use its value entry")
+                subs.append(f"0/{name} {p.name}: codedFixedValue -> fixedValue (its value entry)")
+                typ_b = "fixedValue"
+            if typ_b not in kinds:
+                raise CaseError(f"0/{name} patch {p.name}: boundary type {typ_b!r} is not implemented "
+                                f"({sorted(kinds)})")
+            if typ_b == "fixedValue":
+                if val is None:
+                    raise CaseError(f"0/{name} patch {p.name}: fixedValue without a value")
+                bcs[p.name][name] = ("fixedValue", val)
+            else:
+                bcs[p.name][name] = (typ_b, None)
+    case = Case(mesh, model, bcs, deltaT=scalar(ctrl.get("deltaT", "1e-3")),
+                divU=_limiter(sch, "div(phi,U)"), divTheta=_limiter(sch, "div(phi,theta)"),
+                solverU=_solver(solvers, "U", subs, substitute), solverP=_solver(solvers, "p", subs, substitute),
+                solverTheta=_solver(solvers, "theta", subs, substitute),
+                pRefCell=int(scalar(simple.get("pRefCell", "0"))), pRefValue=scalar(simple.get("pRefValue", "0")),
+                precision=precision, name=os.path.basename(os.path.abspath(case_dir)),
+                nInIter=int(scalar(simple.get("nInIter", "1"))))
+    # boundary values of the initial state (fixed values; the rest from the cells)
+    for p in mesh.patches:
+        sl = slice(p.start, p.start + p.size)
+        for name, nc in ncomp.items():
+            kind, val = case.bcs[p.name][name]
+            bnd = getattr(f, name + "b")
+            cells = getattr(f, name)[mesh.bCell[sl]]
+            if kind == "fixedValue" and val is not None:
+                v = np.asarray(val(mesh.bCf[sl]) if callable(val) else val, dtype=np.float64)
+                bnd[sl] = np.broadcast_to(v.reshape(-1, nc) if nc > 1 else v.reshape(-1), bnd[sl].shape)
+            else:
+                bnd[sl] = cells
+    # initial face fluxes from U (createPhi)
+    Uf = mesh.w[:, None] * (f.U[mesh.owner] - f.U[mesh.neighbour]) + f.U[mesh.neighbour]
+    f.phi[:] = (mesh.Sf * Uf).sum(1)
+    f.phib[:] = (mesh.bSf * f.Ub).sum(1)
+    return LoadedCase(case, f, scalar(ctrl.get("endTime", "1")), scalar(ctrl.get("writeInterval", "1")), subs)
+
+
+def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, **load_kw) -> LoadedCase:
+    """Load the case, step it on the GPU to endTime (or `steps` steps) and
+    write the fields at every write time and at the end."""
+    from .runtime import Context
+    lc = load_case(case_dir, **load_kw)
+    case = lc.case
+    dt = case.deltaT
+    n = steps if steps is not None else int(round(lc.endTime / dt))
+    every = max(1, int(round(lc.writeInterval / dt)))
+    with Context(device) as ctx:
+        ctx.setup_case(case, lc.fields)
+        done = 0
+        while done < n:
+            k = min(every, n - done)
+            ctx.step(k)
+            done += k
+            t = done * dt
+            foam_io.write_fields(os.path.join(case_dir, f"{t:g}"), case.mesh, ctx.fields())
+    return lc
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("case_dir")
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--substitute", action="store_true")
+    ap.add_argument("--mixed", action="store_true", help="the mixed-precision form")
+    a = ap.parse_args(argv)
+    lc = run_case(a.case_dir, steps=a.steps, device=a.device, substitute=a.substitute,
+                  precision=abi.RT_PREC_MIXED if a.mixed else abi.RT_PREC_FP64)
+    for s in lc.substitutions:
+        print("substituted:", s)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,106 @@
+"""Loading an OpenFOAM case directory (polyMesh, 0/, constant/, system/) into
+the library's Case on the CPU: a lid-driven cavity written as OpenFOAM files
+loads into the same case the builder makes (mesh, model, BCs, solver
+controls, schemes) and the oracle steps both to the same fields; what the
+library does not implement is refused unless substitutions are allowed."""
+import os
+
+import numpy as np
+import pytest
+
+from rheotool_gb300 import foam_io
+from rheotool_gb300.case import cavity_case, lid_profile
+from rheotool_gb300.foam_case import CaseError, load_case, parse_dict, scalar
+from rheotool_gb300.mesh import YP, graded_nodes
+
+HDR = 'FoamFile\n{{\n    version 2.0;\n    format ascii;\n    class {cls};\n    object {obj};\n}}\n'
+
+
+def _write(path, cls, obj, body):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        f.write(HDR.format(cls=cls, obj=obj) + body)
+
+
+def _cavity_dir(root, n=8, solverU="PBiCGStab", ddt="Euler", lid="fixedValue"):
+    xs = graded_nodes(0.0, 1.0, n)
+    foam_io.write_structured_polymesh(os.path.join(root, "constant", "polyMesh"), xs, xs, np.array([-0.5, 0.5]),
+                                      lambda d, i, j, k, Cf: np.zeros(i.size, np.int64) if d == YP
+                                      else np.ones(i.size, np.int64),
+                                      ["movingLid", "fixedWalls"], ["wall", "wall"], empty_z=True)
+    mesh = foam_io.read_polymesh(root)
+    lidU = lid_profile(mesh.bCf[mesh.patch("movingLid").start:][:mesh.patch("movingLid").size])
+    lidv = "nonuniform List<vector> {}\n(\n{}\n)".format(len(lidU), "\n".join(
+        f"({u[0]!r} {u[1]!r} {u[2]!r})" for u in lidU.tolist()))
+    lidbc = (f"movingLid {{ type fixedValue; value {lidv}; }}" if lid == "fixedValue"
+             else "movingLid { type codedFixedValue; value uniform (0 0 0); name movLid; }")
+    _write(os.path.join(root, "0", "U"), "volVectorField", "U",
+           "dimensions [0 1 -1 0 0 0 0];\ninternalField uniform (0 0 0);\nboundaryField\n{\n"
+           f"    {lidbc}\n    fixedWalls {{ type fixedValue; value uniform (0 0 0); }}\n"
+           "    frontAndBack { type empty; }\n}\n")
+    _write(os.path.join(root, "0", "p"), "volScalarField", "p",
+           "dimensions [0 2 -2 0 0 0 0];\ninternalField uniform 0;\nboundaryField\n{\n"
+           "    \"(movingLid|fixedWalls)\" { type zeroGradient; }\n    frontAndBack { type empty; }\n}\n")
+    _write(os.path.join(root, "0", "theta"), "volSymmTensorField", "theta",
+           "dimensions [0 0 0 0 0 0 0];\ninternalField uniform (0 0 0 0 0 0);\nboundaryField\n{\n"
+           "    movingLid { type zeroGradient; }\n    fixedWalls { type zeroGradient; }\n"
+           "    frontAndBack { type empty; }\n}\n")
+    _write(os.path.join(root, "0", "tau"), "volSymmTensorField", "tau",
+           "dimensions [1 -1 -2 0 0 0 0];\ninternalField uniform (0 0 0 0 0 0);\nboundaryField\n{\n"
+           "    movingLid { type linearExtrapolation; value uniform (0 0 0 0 0 0); }\n"
+           "    fixedWalls { type linearExtrapolation; value uniform (0 0 0 0 0 0); }\n"
+           "    frontAndBack { type empty; }\n}\n")
+    _write(os.path.join(root, "constant", "constitutiveProperties"), "dictionary", "constitutiveProperties",
+           "parameters\n{\n    type Oldroyd-BLog;\n    rho rho [1 -3 0 0 0 0 0] 0.01;\n"
+           "    etaS etaS [1 -1 -1 0 0 0 0] 0.5;\n    etaP etaP [1 -1 -1 0 0 0 0] 0.5;\n"
+           "    lambda lambda [0 0 1 0 0 0 0] 0.5;\n    stabilization coupling;\n}\n")
+    _write(os.path.join(root, "system", "fvSolution"), "dictionary", "fvSolution",
+           "solvers\n{\n    p { solver PCG; preconditioner DIC; tolerance 1e-8; relTol 0; maxIter 800; }\n"
+           f"    U {{ solver {solverU}; preconditioner {{ preconditioner DILU; }} tolerance 1e-10; relTol 0; }}\n"
+           "    \"(theta|tau)\" { solver PBiCGStab; preconditioner DILU; tolerance 1e-10; relTol 0; }\n}\n"
+           "SIMPLE\n{\n    nInIter 1;\n    pRefCell 0;\n    pRefValue 0;\n}\n")
+    _write(os.path.join(root, "system", "fvSchemes"), "dictionary", "fvSchemes",
+           f"ddtSchemes {{ default {ddt}; }}\ndivSchemes\n{{\n    default none;\n"
+           "    div(phi,U) GaussDefCmpw cubista;\n    div(phi,theta) GaussDefCmpw cubista;\n}\n")
+    _write(os.path.join(root, "system", "controlDict"), "dictionary", "controlDict",
+           "application rheoFoam;\ndeltaT 1e-3;\nendTime 0.003;\nwriteInterval 0.001;\n")
+    return root
+
+
+def test_parse_dict_and_scalars():
+    d = parse_dict('FoamFile { version 2.0; }\n// c\nsolvers { "(U|theta)" { solver PBiCGStab; '
+                   'preconditioner { preconditioner DILU; } } }\nrho rho [1 -3 0 0 0 0 0] 0.01;\nx 2e-3;')
+    assert d["solvers"]["(U|theta)"]["preconditioner"]["preconditioner"] == "DILU"
+    assert scalar(d["rho"]) == 0.01 and scalar(d["x"]) == 2e-3
+
+
+def test_cavity_case_directory_loads_like_the_builder(tmp_path):
+    from oracle.pyoracle import Oracle
+    root = _cavity_dir(str(tmp_path / "cavity"))
+    lc = load_case(root)
+    ref = cavity_case(8)
+    c = lc.case
+    assert c.model.type == "Oldroyd-BLog" and c.model.rho == 0.01 and c.model.lambda_ == 0.5
+    assert c.model.stabilization == "coupling" and c.divU == "cubista" and c.nInIter == 1
+    assert (c.solverP.solver, c.solverP.preconditioner, c.solverP.tolerance, c.solverP.maxIter) == \
+        ("PCG", "DIC", 1e-8, 800)
+    assert (c.solverU.solver, c.solverU.preconditioner, c.solverTheta.solver) == ("PBiCGStab", "DILU", "PBiCGStab")
+    assert c.deltaT == 1e-3 and lc.endTime == 0.003 and not lc.substitutions
+    a, b = Oracle(ref), Oracle(c, lc.fields.copy())
+    a.step(3)
+    b.step(3)
+    for name in ("U", "p", "phi", "theta", "tau"):
+        x, y = getattr(b.f, name), getattr(a.f, name)
+        assert np.linalg.norm(x - y) <= 1e-11 * max(np.linalg.norm(y), 1e-300), name
+
+
+def test_unimplemented_entries_are_refused_or_substituted(tmp_path):
+    root = _cavity_dir(str(tmp_path / "c1"), solverU="PBiCG", ddt="CrankNicolson 1", lid="coded")
+    with pytest.raises(CaseError, match="PBiCG|CrankNicolson|codedFixedValue"):
+        load_case(root)
+    lc = load_case(root, substitute=True)
+    text = " ".join(lc.substitutions)
+    assert "PBiCG -> PBiCGStab" in text and "CrankNicolson -> Euler" in text and "codedFixedValue" in text
+    assert lc.case.solverU.solver == "PBiCGStab"
+    lc2 = load_case(root, substitute=True, bc_overrides={"movingLid": {"U": ("fixedValue", lid_profile)}})
+    assert callable(lc2.case.bcs["movingLid"]["U"][1])
