@@ -1,7 +1,7 @@
 /*
  * oracle.c — FP64 CPU restatement of rheoFoam's segregated time step.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker the CUDA library is
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the CUDA library is
  * compared against (tests/, __graft_entry__.smoke(), bench.py's CPU baseline).
  * Nothing in the product links or calls it.
  *

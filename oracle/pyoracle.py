@@ -1,8 +1,8 @@
 """ctypes binding of the FP64 CPU oracle (liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
-baseline leg of bench.py as the checker.  The product (rheotool_gb300) never
-imports this module.
+baseline leg of bench.py, as the oracle the library is compared against.  The
+product (rheotool_gb300) never imports this module.
 """
 from __future__ import annotations
 
