@@ -318,6 +318,32 @@ def test_poiseuille_channel_oldroydb():
 # ---------------------------------------------------------------------------
 # golden vectors (frozen oracle output, regenerated by tests/golden/make_golden.py)
 # ---------------------------------------------------------------------------
+def _golden_cases():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.golden_cases()
+
+
+@pytest.mark.parametrize("index", range(4))
+def test_golden_vectors(index):
+    """Every frozen oracle output (the cavity for Oldroyd-B, FENE-CR and
+    Rolie-Poly, the periodic PTT channel with two inner iterations) is
+    reproduced to round-off by the current oracle."""
+    from oracle.pyoracle import Oracle
+    name, case, f0, steps = _golden_cases()[index]
+    path = os.path.join(GOLDEN, name)
+    if not os.path.exists(path):
+        pytest.skip("golden file missing")
+    g = np.load(path)
+    o = Oracle(case, None if f0 is None else f0.copy())
+    o.step(steps)
+    for field in ("U", "p", "theta", "tau", "phi"):
+        ref = g[field]
+        assert np.linalg.norm(getattr(o.f, field) - ref) <= 1e-12 * np.linalg.norm(ref), (name, field)
+
+
 def test_golden_cavity_oracle():
     path = os.path.join(GOLDEN, "cavity16_oldroydb_10steps.npz")
     if not os.path.exists(path):
