@@ -100,8 +100,9 @@ public:
                                           const Dictionary &controls);
     // one component: psi (nCells) is updated in place
     SolverPerformance solve(double *psi, const double *source, int cmpt = 0) const;
-    // nCmpt components sharing the matrix (component-major blocks of nCells)
-    std::vector<SolverPerformance> solve(double *psi, const double *source, int nCmpt, int) const;
+    // nCmpt components sharing the matrix (component-major blocks of nCells),
+    // solved together as fvMatrix::solveSegregated solves a vector or tensor
+    std::vector<SolverPerformance> solveComponents(double *psi, const double *source, int nCmpt) const;
     const std::string &type() const { return type_; }
     static const std::vector<std::string> &solvers();
     static const std::vector<std::string> &preconditioners();

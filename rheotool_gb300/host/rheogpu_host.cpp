@@ -203,7 +203,7 @@ rt_solver_ctl LduSolver::readControls(const Dictionary &c) {
     return ctl;
 }
 
-std::vector<SolverPerformance> LduSolver::solve(double *psi, const double *source, int nCmpt, int) const {
+std::vector<SolverPerformance> LduSolver::solveComponents(double *psi, const double *source, int nCmpt) const {
     std::vector<rt_solver_perf> perf((size_t)nCmpt);
     rt_status s = rt_ldu_solve(ctx_.get(), m_.diag, m_.upper, m_.lower, source, psi, nCmpt, &ctl_, perf.data());
     if (s != RT_ENOCONV) ctx_.check(s, "rt_ldu_solve(" + field_ + ")");
@@ -222,7 +222,7 @@ std::vector<SolverPerformance> LduSolver::solve(double *psi, const double *sourc
 }
 
 SolverPerformance LduSolver::solve(double *psi, const double *source, int cmpt) const {
-    SolverPerformance p = solve(psi, source, 1, 0)[0];
+    SolverPerformance p = solveComponents(psi, source, 1)[0];
     (void)cmpt;   // the component index only names the output, as in OpenFOAM
     return p;
 }
