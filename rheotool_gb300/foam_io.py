@@ -20,7 +20,8 @@ library and the oracle take:
   separation of the two patch faces), in upper-triangular order with the
   other internal faces.  ``Mesh.foamFace`` records, for every LDU face, the
   OpenFOAM face it came from (for a cyclic pair, the face on the owner's
-  patch), which the field writer uses to put ``phi`` back on the patches.
+  patch) and ``Mesh.foamPartner`` the pair's other face, which the field
+  writer uses to put ``phi`` back on both cyclic patches.
 
 The field writer emits ``volScalarField`` / ``volVectorField`` /
 ``volSymmTensorField`` / ``volTensorField`` / ``surfaceScalarField`` files in
@@ -270,6 +271,7 @@ def read_polymesh(case_dir: str, name: Optional[str] = None) -> Mesh:
     shift = np.zeros((nI, 3))
     coupled = np.zeros(nI, np.int32)
     src = np.arange(nI)
+    partner = np.full(nI, -1, dtype=np.int64)   # the other patch face of a cyclic pair
     for fa, fb in cyc_faces:
         ca, cb = own[fa], own[fb]
         sep = Cf[fa] - Cf[fb]                 # translation taking patch b onto patch a
@@ -287,10 +289,12 @@ def read_polymesh(case_dir: str, name: Optional[str] = None) -> Mesh:
         shift = np.concatenate([shift, sh])
         coupled = np.concatenate([coupled, np.ones(fa.size, np.int32)])
         src = np.concatenate([src, np.where(a_low, fa, fb)])
+        partner = np.concatenate([partner, np.where(a_low, fb, fa)])
     if np.any(o == nb):
         raise ValueError("a cyclic face joins a cell to itself")
     order = np.lexsort((nb, o))
-    o, nb, iSf, iCf, shift, coupled, src = (x[order] for x in (o, nb, iSf, iCf, shift, coupled, src))
+    o, nb, iSf, iCf, shift, coupled, src, partner = (x[order] for x in (o, nb, iSf, iCf, shift, coupled, src,
+                                                                        partner))
     CN = C[nb] + shift
     magSf = np.linalg.norm(iSf, axis=1)
     sfdOwn = np.abs((iSf * (iCf - C[o])).sum(1))
@@ -327,6 +331,7 @@ def read_polymesh(case_dir: str, name: Optional[str] = None) -> Mesh:
         coupled=coupled if hasCyc else None,
     )
     m.foamFace = src.astype(np.int64)          # OpenFOAM face of each LDU face
+    m.foamPartner = partner                    # for a cyclic pair, the face on the other patch
     m.foamBFace = bidx.astype(np.int64)        # OpenFOAM face of each boundary face
     m.foamPatches = bnd
     m.foamNFaces = nFaces
@@ -603,7 +608,21 @@ def write_fields(time_dir: str, mesh: Mesh, fields, bc_types: Optional[Dict[str,
         if src is not None:
             internal = np.empty(nI)
             internal[src[keep]] = phi_int[keep]
-        bnd["coupled"] = ("cyclic", phi_int[~keep])
+        patches = getattr(mesh, "foamPatches", None)
+        if src is not None and patches is not None:
+            # each cyclic patch face gets the flux out of its own cell: the
+            # pair's flux on the owner's face, minus it on the partner's face
+            face_phi = {}
+            cf = np.nonzero(~keep)[0]
+            for f in cf:
+                face_phi[int(src[f])] = phi_int[f]
+                face_phi[int(mesh.foamPartner[f])] = -phi_int[f]
+            for pd in patches:
+                if pd.get("type") == "cyclic":
+                    s0, n0 = int(pd["startFace"]), int(pd["nFaces"])
+                    bnd[pd["name"]] = ("cyclic", np.array([face_phi[i] for i in range(s0, s0 + n0)]))
+        else:
+            bnd["coupled"] = ("cyclic", phi_int[~keep])
     else:
         internal = phi_int
         src = getattr(mesh, "foamFace", None)

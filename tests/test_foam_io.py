@@ -139,3 +139,27 @@ def test_oracle_step_on_read_mesh_equals_generated(tmp_path):
     for name in ("U", "p", "theta", "tau", "phi"):
         x, y = getattr(b.f, name), getattr(a.f, name)
         assert np.linalg.norm(x - y) <= 1e-11 * max(np.linalg.norm(y), 1e-300), name
+
+
+def test_cyclic_phi_written_on_both_patches(tmp_path):
+    """A periodic mesh read from polyMesh files writes phi in OpenFOAM's
+    layout: internal faces in their order, each cyclic patch face with the
+    flux out of its own cell (the two halves of a pair opposite)."""
+    xs = graded_nodes(0.0, 2.0, 5)
+    ys = two_sided_nodes(-1.0, 1.0, 4, 2.0)
+    zs = graded_nodes(0.0, 1.0, 3)
+    foam_io.write_structured_polymesh(str(tmp_path / "mesh"), xs, ys, zs,
+                                      lambda d, i, j, k, Cf: np.zeros(i.size, np.int64), ["walls"],
+                                      periodic=(True, False, True))
+    m = foam_io.read_polymesh(str(tmp_path / "mesh"))
+    case = periodic_channel_case(m, Wi=2.0)
+    f = periodic_channel_state(case)
+    foam_io.write_fields(str(tmp_path / "0"), m, f, prec=17)
+    phi, b = foam_io.read_field(str(tmp_path / "0" / "phi"))
+    keep = m.coupled == 0
+    assert phi.size == int(keep.sum())
+    lo, hi = b["cyclic_x_lo"]["value"], b["cyclic_x_hi"]["value"]
+    assert np.allclose(lo, -hi) and np.abs(hi).max() > 0          # the flow leaves at x = L, enters at x = 0
+    assert np.all(hi > 0)
+    zl, zh = b["cyclic_z_lo"]["value"], b["cyclic_z_hi"]["value"]
+    assert np.allclose(zl, 0.0) and np.allclose(zh, 0.0)           # no spanwise flow
