@@ -19,9 +19,12 @@
 What the library does not implement is refused with a clear message unless
 ``substitute=True`` is given, in which case each substitution is recorded in
 ``loaded.substitutions``: PBiCG becomes PBiCGStab (same preconditioner and
-tolerance); Crank-Nicolson ddt becomes Euler; a ``codedFixedValue`` patch
-(its code cannot run here) uses its ``value`` entry unless
-``bc_overrides`` gives the values.  ``run_case`` steps the case on the GPU
+tolerance); rheoTool's external sparse solvers (``solverType eigenSolver``,
+``petscSolver``, ``hypreSolver``) become PCG-DIC for p and PBiCGStab-DILU for
+the others at their tolerance; Crank-Nicolson ddt becomes Euler;
+non-orthogonal correctors and relaxation factors other than 1 are dropped; a
+``codedFixedValue`` patch (its code cannot run here) uses its ``value`` entry
+unless ``bc_overrides`` gives the values.  ``run_case`` steps the case on the GPU
 and writes OpenFOAM fields at the write times.
 
     python -m rheotool_gb300.foam_case CASE_DIR [--steps N] [--substitute] [--mixed]
@@ -144,6 +147,16 @@ def _solver(d: Dict[str, Any], name: str, subs: List[str], substitute: bool) -> 
     if e is None:
         raise CaseError(f"fvSolution: no solver entry for {name}")
     sv = e.get("solver", "")
+    stype = e.get("solverType", "openFoam")
+    if stype != "openFoam":
+        # rheoTool's external sparse solvers (sparseSolver.C:41): Eigen, PETSc, Hypre
+        if not substitute:
+            raise CaseError(f"fvSolution {name}: solverType {stype} ({sv}) is not implemented; pass "
+                            "substitute=True for the library's Krylov solver at the same tolerance")
+        new = ("PCG", "DIC") if name == "p" else ("PBiCGStab", "DILU")
+        subs.append(f"{name}: solverType {stype} {sv} -> {new[0]}-{new[1]}")
+        return SolverControl(new[0], new[1], scalar(e.get("tolerance", "1e-6")), scalar(e.get("relTol", "0")),
+                             int(scalar(e.get("minIter", "0"))), int(scalar(e.get("maxIter", "1000"))))
     if sv == "PBiCG":
         if not substitute:
             raise CaseError(f"fvSolution {name}: solver PBiCG is not implemented (PBiCGStab is); "
@@ -196,6 +209,17 @@ def load_case(case_dir: str, substitute: bool = False,
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))
     solvers = sol.get("solvers", {})
     simple = sol.get("SIMPLE", {})
+    if int(scalar(simple.get("nNonOrthogonalCorrectors", "0"))) > 0:
+        if not substitute:
+            raise CaseError("SIMPLE nNonOrthogonalCorrectors > 0 is not implemented (orthogonal meshes)")
+        subs.append("SIMPLE nNonOrthogonalCorrectors -> 0")
+    relax = sol.get("relaxationFactors", {})
+    for group in ("fields", "equations"):
+        for k, v in (relax.get(group, {}) or {}).items():
+            if isinstance(v, str) and scalar(v) != 1.0:
+                if not substitute:
+                    raise CaseError(f"relaxationFactors {group} {k} {v}: only 1 (no relaxation) is implemented")
+                subs.append(f"relaxationFactors {group} {k}: {v} -> 1")
     sch = read_dict(os.path.join(case_dir, "system", "fvSchemes"))
     ddt = sch.get("ddtSchemes", {}).get("default", "Euler").split()[0]
     if ddt != "Euler":

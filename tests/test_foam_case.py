@@ -104,3 +104,32 @@ def test_unimplemented_entries_are_refused_or_substituted(tmp_path):
     assert lc.case.solverU.solver == "PBiCGStab"
     lc2 = load_case(root, substitute=True, bc_overrides={"movingLid": {"U": ("fixedValue", lid_profile)}})
     assert callable(lc2.case.bcs["movingLid"]["U"][1])
+
+
+def test_rheotool_external_solvers_and_relaxation(tmp_path):
+    """The Cavity tutorial's form: p and U through rheoTool's eigenSolver
+    (Eigen BiCGSTAB + ILUT) and relaxation factors of 1 are accepted as
+    written only with substitutions; factors other than 1 are refused."""
+    root = _cavity_dir(str(tmp_path / "c2"))
+    path = os.path.join(root, "system", "fvSolution")
+    _write(path, "dictionary", "fvSolution",
+           "solvers\n{\n    \"(p|U)\"\n    {\n        solverType eigenSolver;\n        solver BiCGSTAB;\n"
+           "        tolerance 1e-12;\n        maxIter 1000;\n        preconditioner { preconditioner ILUT; }\n    }\n"
+           "    \"(theta|tau)\" { solver PBiCGStab; preconditioner { preconditioner DILU; } tolerance 1e-10; }\n}\n"
+           "SIMPLE { nInIter 1; nNonOrthogonalCorrectors 0; pRefCell 0; pRefValue 0; }\n"
+           "relaxationFactors { fields { p 1; } equations { U 1; } }\n")
+    with pytest.raises(CaseError, match="eigenSolver"):
+        load_case(root)
+    lc = load_case(root, substitute=True)
+    assert (lc.case.solverP.solver, lc.case.solverP.preconditioner, lc.case.solverP.tolerance) == ("PCG", "DIC", 1e-12)
+    assert (lc.case.solverU.solver, lc.case.solverU.preconditioner) == ("PBiCGStab", "DILU")
+    assert any("eigenSolver" in x for x in lc.substitutions)
+    assert not any("relaxation" in x for x in lc.substitutions)
+    with open(path) as f:
+        text = f.read().replace("equations { U 1; }", "equations { U 0.7; }")
+    with open(path, "w") as f:
+        f.write(text)
+    with pytest.raises(CaseError, match="relaxationFactors"):
+        load_case(root)
+    lc2 = load_case(root, substitute=True)
+    assert any("relaxationFactors equations U: 0.7 -> 1" in x for x in lc2.substitutions)
