@@ -220,10 +220,11 @@ __device__ __forceinline__ void st4(double *p, const double *v) {
 // rings use the same quad order, so a chunk's words are written and read
 // with 16-byte vector accesses.
 //
-// The producer CTA of a plane writes each chunk's 32 lanes, tagged, straight
-// into the consumer CTA's ring (distributed shared memory: remote stores do
-// not wait, and the consumer's local loads are cheap); each consumer lane
-// checks its own words.  The consumer reports its progress back into the
+// The producer CTA of a plane writes each quad (four steps) of its 32 lanes,
+// tagged, straight into the consumer CTA's ring as soon as the quad is
+// computed (distributed shared memory: remote stores do not wait, and the
+// consumer's local loads are cheap); each consumer lane checks its own words
+// quad by quad, so a plane lags the previous one by about a quad.  The consumer reports its progress back into the
 // producer's shared memory after each chunk, which bounds how far the
 // producer may run ahead (so a slot is never overwritten before it is read;
 // the two waits can never close a cycle).  The j-block hand-off stays inside
@@ -235,9 +236,10 @@ __device__ __forceinline__ void st4(double *p, const double *v) {
 // of a CTA that has exited.
 //
 // Latency: a chunk's coefficients are staged into shared memory with cp.async
-// NB - 1 chunks ahead; the terms of a step that do not depend on the previous
-// step are formed for the whole chunk first, so only the j and i terms stay
-// on the dependent chain.  Invalid entries (outside the mesh, padding) have
+// NB - 1 chunks ahead and read, with the j-block words, before the wait for
+// the previous plane; the terms of a step that do not depend on the previous
+// step are formed quad by quad ahead of the recurrence, so only the j and i
+// terms stay on the dependent chain.  Invalid entries (outside the mesh, padding) have
 // zero coefficients and zero right-hand sides, so every lane runs the same
 // branch-free recurrence.
 template <class Real, int MODE, int NC, int P, int NB>

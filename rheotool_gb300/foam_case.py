@@ -145,7 +145,8 @@ class CaseError(ValueError):
 def _solver(d: Dict[str, Any], name: str, subs: List[str], substitute: bool) -> SolverControl:
     e = lookup_pattern(d, name)
     if e is None:
-        raise CaseError(f"fvSolution: no solver entry for {name}")
+        raise CaseError(f"fvSolution: no solver entry for {name} (a case that solves U, p and tau coupled "
+                        "through rheoTool's coupledSolvers is not supported)")
     sv = e.get("solver", "")
     stype = e.get("solverType", "openFoam")
     if stype != "openFoam":
