@@ -1,8 +1,8 @@
 """OpenFOAM case I/O: the ``constant/polyMesh`` reader and ASCII field files.
 
 The reader turns an OpenFOAM polyMesh (``points``, ``faces``, ``owner``,
-``neighbour``, ``boundary``; plain or ``.gz``) into the LDU ``Mesh`` the
-library and the oracle take:
+``neighbour``, ``boundary``; ASCII or binary format, plain or ``.gz``) into
+the LDU ``Mesh`` the library and the oracle take:
 
 * geometry as OpenFOAM's ``primitiveMesh`` defines it: a face's centre and
   area vector from the triangles joining each edge to the mean of its points
@@ -111,8 +111,56 @@ def _numbers(s: str) -> np.ndarray:
     return np.array(s.split(), dtype=np.float64) if s.strip() else np.zeros(0)
 
 
+def _read_bytes(path: str) -> bytes:
+    for p in (path, path + ".gz"):
+        if os.path.exists(p):
+            if p.endswith(".gz"):
+                with gzip.open(p, "rb") as f:
+                    return f.read()
+            with open(p, "rb") as f:
+                return f.read()
+    raise FileNotFoundError(path)
+
+
+def _binary_header(raw: bytes) -> Optional[Dict[str, str]]:
+    """The FoamFile header of a binary-format file (None for ASCII)."""
+    head = raw[:4096].decode("latin-1")
+    h = _header(head)
+    return h if h.get("format", "ascii") == "binary" else None
+
+
+def _binary_lists(raw: bytes, dtypes: List[np.dtype], widths: List[int]) -> List[np.ndarray]:
+    """The raw lists ``N ( <N x width items of dtype> )`` that follow the
+    header of a binary-format file, in order."""
+    pos = raw.index(b"}", raw.index(b"FoamFile")) + 1
+    out = []
+    for dt, wdt in zip(dtypes, widths):
+        m = re.compile(rb"(\d+)\s*\(").search(raw, pos)
+        if not m:
+            raise ValueError("binary list not found")
+        n = int(m.group(1))
+        nbytes = n * wdt * dt.itemsize
+        a = m.end()
+        out.append(np.frombuffer(raw[a:a + nbytes], dtype=dt).reshape(n, wdt) if wdt > 1
+                   else np.frombuffer(raw[a:a + nbytes], dtype=dt).copy())
+        pos = a + nbytes + 1      # past ')'
+    return out
+
+
+def _label_dtype(h: Dict[str, str]) -> np.dtype:
+    return np.dtype(np.int64) if "label=64" in h.get("arch", "") else np.dtype(np.int32)
+
+
+def _scalar_dtype(h: Dict[str, str]) -> np.dtype:
+    return np.dtype(np.float32) if "scalar=32" in h.get("arch", "") else np.dtype(np.float64)
+
+
 def read_label_list(path: str) -> np.ndarray:
-    t = _body(_read_text(path))
+    raw = _read_bytes(path)
+    hb = _binary_header(raw)
+    if hb is not None:
+        return _binary_lists(raw, [_label_dtype(hb)], [1])[0].astype(np.int64)
+    t = _body(raw.decode("latin-1"))
     n, a, b = _list_span(t)
     v = np.array(t[a:b].split(), dtype=np.int64)
     if v.size != n:
@@ -121,7 +169,11 @@ def read_label_list(path: str) -> np.ndarray:
 
 
 def read_vector_list(path: str) -> np.ndarray:
-    t = _body(_read_text(path))
+    raw = _read_bytes(path)
+    hb = _binary_header(raw)
+    if hb is not None:
+        return _binary_lists(raw, [_scalar_dtype(hb)], [3])[0].astype(np.float64)
+    t = _body(raw.decode("latin-1"))
     n, a, b = _list_span(t)
     v = _numbers(t[a:b]).reshape(-1, 3)
     if v.shape[0] != n:
@@ -130,8 +182,16 @@ def read_vector_list(path: str) -> np.ndarray:
 
 
 def read_faces(path: str) -> List[np.ndarray]:
-    """faceList: ``N ( k(a b c ...) ... )``; also faceCompactList."""
-    text = _read_text(path)
+    """faceList: ``N ( k(a b c ...) ... )``; also faceCompactList (offsets
+    then labels), which is how binary files store the faces."""
+    raw = _read_bytes(path)
+    hb = _binary_header(raw)
+    if hb is not None:
+        ld = _label_dtype(hb)
+        offs, lab = _binary_lists(raw, [ld, ld], [1, 1])
+        offs, lab = offs.astype(np.int64), lab.astype(np.int64)
+        return [lab[offs[i]:offs[i + 1]] for i in range(len(offs) - 1)]
+    text = raw.decode("latin-1")
     t = _body(text)
     if "faceCompactList" in _header(text).get("class", ""):
         n1, a1, b1 = _list_span(t)

@@ -163,3 +163,40 @@ def test_cyclic_phi_written_on_both_patches(tmp_path):
     assert np.all(hi > 0)
     zl, zh = b["cyclic_z_lo"]["value"], b["cyclic_z_hi"]["value"]
     assert np.allclose(zl, 0.0) and np.allclose(zh, 0.0)           # no spanwise flow
+
+
+def _write_binary(path, cls, obj, arrays):
+    hdr = ('FoamFile\n{\n    version 2.0;\n    format binary;\n    arch "LSB;label=32;scalar=64";\n'
+           f'    class {cls};\n    location "constant/polyMesh";\n    object {obj};\n}}\n\n')
+    with open(path, "wb") as f:
+        f.write(hdr.encode())
+        for a in arrays:
+            f.write(f"{len(a)}\n(".encode())
+            f.write(np.ascontiguousarray(a).tobytes())
+            f.write(b")\n\n")
+
+
+def test_binary_polymesh_reads_like_ascii(tmp_path):
+    """A polyMesh written in OpenFOAM's binary format (labels int32, scalars
+    float64, faces as a faceCompactList) reads into the same mesh as the
+    ASCII files."""
+    ascii_dir, bin_dir = str(tmp_path / "a"), str(tmp_path / "b")
+    xs = graded_nodes(0.0, 1.0, 5, 2.0)
+    foam_io.write_structured_polymesh(ascii_dir, xs, xs, xs, lambda d, i, j, k, Cf: np.zeros(i.size, np.int64),
+                                      ["walls"])
+    ref = foam_io.read_polymesh(ascii_dir)
+    os.makedirs(bin_dir)
+    pts = foam_io.read_vector_list(os.path.join(ascii_dir, "points"))
+    faces = foam_io.read_faces(os.path.join(ascii_dir, "faces"))
+    own = foam_io.read_label_list(os.path.join(ascii_dir, "owner")).astype(np.int32)
+    nei = foam_io.read_label_list(os.path.join(ascii_dir, "neighbour")).astype(np.int32)
+    offs = np.concatenate([[0], np.cumsum([len(f) for f in faces])]).astype(np.int32)
+    lab = np.concatenate(faces).astype(np.int32)
+    _write_binary(os.path.join(bin_dir, "points"), "vectorField", "points", [pts.astype(np.float64)])
+    _write_binary(os.path.join(bin_dir, "faces"), "faceCompactList", "faces", [offs, lab])
+    _write_binary(os.path.join(bin_dir, "owner"), "labelList", "owner", [own])
+    _write_binary(os.path.join(bin_dir, "neighbour"), "labelList", "neighbour", [nei])
+    with open(os.path.join(ascii_dir, "boundary")) as f, open(os.path.join(bin_dir, "boundary"), "w") as g:
+        g.write(f.read())
+    m = foam_io.read_polymesh(bin_dir)
+    _same_mesh(m, ref, tol=0.0 + 1e-15)
