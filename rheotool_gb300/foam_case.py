@@ -22,7 +22,8 @@ What the library does not implement is refused with a clear message unless
 tolerance); rheoTool's external sparse solvers (``solverType eigenSolver``,
 ``petscSolver``, ``hypreSolver``) become PCG-DIC for p and PBiCGStab-DILU for
 the others at their tolerance; Crank-Nicolson ddt becomes Euler;
-non-orthogonal correctors and relaxation factors other than 1 are dropped; a
+non-orthogonal correctors and relaxation factors other than 1 are dropped (a
+non-orthogonal mesh runs with the orthogonal laplacian only on request); a
 ``codedFixedValue`` patch (its code cannot run here) uses its ``value`` entry
 unless ``bc_overrides`` gives the values.  ``run_case`` steps the case on the GPU
 and writes OpenFOAM fields at the write times.
@@ -192,6 +193,14 @@ def load_case(case_dir: str, substitute: bool = False,
               precision: int = abi.RT_PREC_FP64) -> LoadedCase:
     subs: List[str] = []
     mesh = foam_io.read_polymesh(case_dir)
+    q = foam_io.mesh_quality(mesh)
+    if q["nonOrthogonality"] > 1e-6:
+        # the laplacian and face gradients are the orthogonal ones (no
+        # non-orthogonal correction): exact only on orthogonal meshes
+        msg = f"mesh non-orthogonality {q['nonOrthogonality']:.3g} deg: orthogonal laplacian used"
+        if not substitute:
+            raise CaseError(msg + " (pass substitute=True to run it anyway)")
+        subs.append(msg)
     cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
     par = cp.get("parameters", cp)
     typ = par.get("type", "")

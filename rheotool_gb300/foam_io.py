@@ -274,6 +274,26 @@ def cell_geometry(nCells: int, owner: np.ndarray, neighbour: np.ndarray, Cf: np.
     return C, vol / 3.0
 
 
+def mesh_quality(mesh: Mesh) -> Dict[str, float]:
+    """Maximum non-orthogonality (degrees between the face normal and C_N - C_P)
+    and maximum face skewness (distance of the face centre from the line
+    C_P C_N, over |C_N - C_P|) of the internal faces.  The library's
+    laplacian and face gradients are the orthogonal ones, exact only when the
+    non-orthogonality is zero."""
+    if mesh.nFaces == 0:
+        return {"nonOrthogonality": 0.0, "skewness": 0.0}
+    d = mesh.delta if mesh.delta is not None else mesh.C[mesh.neighbour] - mesh.C[mesh.owner]
+    n = mesh.Sf / mesh.magSf[:, None]
+    dl = np.linalg.norm(d, axis=1)
+    cosang = np.clip((n * d).sum(1) / dl, -1.0, 1.0)
+    nonorth = float(np.degrees(np.arccos(cosang)).max())
+    # face centre relative to the owner centre, its part off the line P-N
+    r = mesh.Cf - mesh.C[mesh.owner]
+    t = (r * d).sum(1) / (dl * dl)
+    off = np.linalg.norm(r - t[:, None] * d, axis=1)
+    return {"nonOrthogonality": nonorth, "skewness": float((off / dl).max())}
+
+
 # ---------------------------------------------------------------------------
 # polyMesh -> LDU mesh
 # ---------------------------------------------------------------------------

@@ -200,3 +200,24 @@ def test_binary_polymesh_reads_like_ascii(tmp_path):
         g.write(f.read())
     m = foam_io.read_polymesh(bin_dir)
     _same_mesh(m, ref, tol=0.0 + 1e-15)
+
+
+def test_mesh_quality():
+    m = periodic_channel_mesh(5, 4, 3, L=2.0, depth=1.0)
+    q = foam_io.mesh_quality(m)
+    assert q["nonOrthogonality"] < 1e-9 and q["skewness"] < 1e-9
+
+
+def test_mesh_quality_of_distorted_cells(tmp_path):
+    n = 3
+    xs = graded_nodes(0.0, 1.0, n)
+    foam_io.write_structured_polymesh(str(tmp_path), xs, xs, xs, lambda d, i, j, k, Cf: np.zeros(i.size, np.int64),
+                                      ["walls"])
+    pts = foam_io.read_vector_list(os.path.join(str(tmp_path), "points"))
+    inner = np.all((pts > 1e-9) & (pts < 1 - 1e-9), axis=1)
+    pts[inner] += 0.05
+    with open(os.path.join(str(tmp_path), "points"), "w") as f:
+        f.write(foam_io._header_text("vectorField", "points", "constant/polyMesh"))
+        f.write(f"{len(pts)}\n(\n" + "\n".join("(" + " ".join(f"{float(x):.17g}" for x in p) + ")" for p in pts) + "\n)\n")
+    q = foam_io.mesh_quality(foam_io.read_polymesh(str(tmp_path)))
+    assert q["nonOrthogonality"] > 1.0
