@@ -12,6 +12,8 @@
 //       converged, singular).  Reached in rheoTool through
 //       sparseSolver<Type>::solve (libs/sparseMatrixSolvers/segregated/
 //       sparseSolver.H:200-205, openFoamSolver/openFoamSolver.C:46-53).
+//   SparseSolver::New(fieldName, controls) / solve(matrix, psi, source, nCmpt)
+//       rheoTool's sparseSolver<Type> selection by `solverType`.
 //   ConstitutiveEq::New(name, constitutiveProperties) / correct() / tau()
 //       rheoTool's constitutiveEq run-time selection (constitutiveEq.H:250-262,
 //       newConstitutiveEq.C:32-61) for the log-conformation models the
@@ -117,6 +119,32 @@ private:
     Context &ctx_;
     LduMatrixView m_;
     rt_solver_ctl ctl_;
+};
+
+// rheoTool's sparseSolver<Type> (libs/sparseMatrixSolvers/segregated/
+// sparseSolver.H:134-212): the per-field solver of rheoFoam's U and p,
+// selected by `solverType` (sparseSolver.C:41).  The library serves the
+// `openFoam` type (openFoamSolver.C:46-75: the lduMatrix solver of each
+// component); the external types (eigenSolver, petscSolver, hypreSolver)
+// throw FatalError listing the valid ones.
+class SparseSolver {
+public:
+    static std::unique_ptr<SparseSolver> New(const std::string &fieldName, Context &ctx,
+                                             const Dictionary &controls);
+    static const std::vector<std::string> &types();
+    // the solverType and lduMatrix controls of an entry (FatalError if not served)
+    static rt_solver_ctl readControls(const Dictionary &controls);
+    // every component of the field (component-major blocks of nCells), as
+    // fvMatrix<Type>::solveSegregated does
+    std::vector<SolverPerformance> solve(const LduMatrixView &matrix, double *psi, const double *source,
+                                         int nCmpt) const;
+    bool isExternalSolver() const { return false; }
+
+private:
+    SparseSolver(std::string f, Context &c, Dictionary d) : field_(std::move(f)), ctx_(c), controls_(std::move(d)) {}
+    std::string field_;
+    Context &ctx_;
+    Dictionary controls_;
 };
 
 class ConstitutiveEq {

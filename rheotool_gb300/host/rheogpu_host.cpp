@@ -228,6 +228,30 @@ SolverPerformance LduSolver::solve(double *psi, const double *source, int cmpt) 
 }
 
 // ---------------------------------------------------------------------------
+// SparseSolver (rheoTool sparseSolver<Type>)
+// ---------------------------------------------------------------------------
+const std::vector<std::string> &SparseSolver::types() {
+    static const std::vector<std::string> v{"openFoam"};
+    return v;
+}
+
+rt_solver_ctl SparseSolver::readControls(const Dictionary &c) {
+    const std::string t = c.lookupOrDefault("solverType", std::string("openFoam"));
+    if (t != "openFoam") throw FatalError(valid_list("sparseSolver solverType", t, types()));
+    return LduSolver::readControls(c);
+}
+
+std::unique_ptr<SparseSolver> SparseSolver::New(const std::string &fieldName, Context &ctx, const Dictionary &c) {
+    readControls(c);
+    return std::unique_ptr<SparseSolver>(new SparseSolver(fieldName, ctx, c));
+}
+
+std::vector<SolverPerformance> SparseSolver::solve(const LduMatrixView &m, double *psi, const double *source,
+                                                   int nCmpt) const {
+    return LduSolver::New(field_, ctx_, m, controls_)->solveComponents(psi, source, nCmpt);
+}
+
+// ---------------------------------------------------------------------------
 // ConstitutiveEq (constitutiveEq run-time selection)
 // ---------------------------------------------------------------------------
 const std::vector<std::string> &ConstitutiveEq::types() {

@@ -83,6 +83,13 @@ static void cpu_checks() {
     std::string e1 = throws([&] { LduSolver::readControls(sol.subDict("U")); });
     CHECK(e1.find("Unknown lduMatrix::solver PBiCG") != std::string::npos);
 
+    // sparseSolver selection by solverType: only the openFoam type is served
+    Dictionary ext = Dictionary::parse("solverType eigenSolver; solver BiCGSTAB; tolerance 1e-12;");
+    std::string e3 = throws([&] { SparseSolver::readControls(ext); });
+    CHECK(e3.find("Unknown sparseSolver solverType eigenSolver") != std::string::npos);
+    Dictionary of = Dictionary::parse("solverType openFoam; solver PCG; preconditioner DIC; tolerance 1e-9;");
+    CHECK(SparseSolver::readControls(of).solver == RT_SOLVER_PCG);
+
     std::string e2 = throws([&] { Context ctx(0); });
     CHECK(e2.find("rt_ctx_create") != std::string::npos);
 }
