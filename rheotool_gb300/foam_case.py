@@ -206,8 +206,11 @@ def load_case(case_dir: str, substitute: bool = False,
     typ = par.get("type", "")
     if typ not in abi.MODEL_NAMES:
         raise CaseError(f"Unknown constitutiveEq type {typ}; valid: {sorted(abi.MODEL_NAMES)}")
+    for key in ("rho", "etaS", "etaP", "stabilization", "lambdaD" if typ == "Rolie-PolyLog" else "lambda"):
+        if key not in par:   # constitutiveEq's lookups (constitutiveEq.C:435-438 for stabilization)
+            raise CaseError(f"keyword {key} is undefined in constitutiveProperties")
     mkw: Dict[str, Any] = dict(type=typ, rho=scalar(par["rho"]), etaS=scalar(par["etaS"]), etaP=scalar(par["etaP"]),
-                               stabilization=par.get("stabilization", "none"))
+                               stabilization=par["stabilization"])
     mkw["lambda_"] = scalar(par["lambdaD"] if typ == "Rolie-PolyLog" else par["lambda"])
     for k in ("alpha", "epsilon", "zeta", "L2", "lambdaR", "beta", "delta", "chiMax"):
         if k in par:
