@@ -106,6 +106,12 @@ typedef struct {
 #define RT_MODEL_FENECR_LOG   4   /* type FENE-CRLog (FENE-CR/FENE-CRLog/FENE_CRLog.C:127-180) */
 #define RT_MODEL_ROLIEPOLY_LOG 5  /* type Rolie-PolyLog (Rolie-Poly/Rolie-PolyLog/RoliePolyLog.C:125-203);
                                      lambda carries lambdaD */
+#define RT_MODEL_XPOMPOM_LOG  6   /* type XPomPomLog (XPomPom/XPomPomLog/XPomPomLog.C:133-198);
+                                     lambda carries lambdaB, alpha the anisotropy */
+#define RT_MODEL_WHITEMETZNERCY_LOG 7 /* type WhiteMetznerCYLog (WhiteMetznerCY/WhiteMetznerCYLog/
+                                     WhiteMetznerCYLog.C:145-206); the log form needs m = n,
+                                     L = K and b = a, so n, K and a serve both the
+                                     viscosity and the relaxation time */
 #define RT_PTT_LINEAR 0
 #define RT_PTT_EXP    1
 #define RT_STAB_NONE     0
@@ -123,6 +129,11 @@ typedef struct {
     double beta;      /* Rolie-Poly convective constraint release coefficient */
     double delta;     /* Rolie-Poly CCR exponent                              */
     double chiMax;    /* Rolie-Poly maximum stretch (finite extensibility when > 1) */
+    double lambdaS;   /* XPomPom stretch relaxation time (lambda = lambdaB)   */
+    double q;         /* XPomPom number of arms                               */
+    double n;         /* XPomPom stretch exponent; WhiteMetznerCY power index */
+    double K;         /* WhiteMetznerCY time constant (K = L)                 */
+    double a;         /* WhiteMetznerCY Carreau-Yasuda exponent (a = b)       */
 } rt_model_params;
 
 /* ---- linear solvers ----------------------------------------------------- */

@@ -19,10 +19,12 @@
  *                                         the cyclic Jacobi method, eigenvalues
  *                                         ascending as Eigen returns them)
  *   - Oldroyd-BLog / GiesekusLog / PTTLog / FENE-PLog / FENE-CRLog /
- *     Rolie-PolyLog correct() ........... Oldroyd_BLog.C:127-179, GiesekusLog.C:
+ *     Rolie-PolyLog / XPomPomLog / WhiteMetznerCYLog correct()
+ *                                         Oldroyd_BLog.C:127-179, GiesekusLog.C:
  *                                         128-176, PTTLog.C:176-268, FENE_PLog.C:
  *                                         128-182, FENE_CRLog.C:127-180,
- *                                         RoliePolyLog.C:125-203
+ *                                         RoliePolyLog.C:125-203, XPomPomLog.C:
+ *                                         133-198, WhiteMetznerCYLog.C:145-206
  *   - GaussDefCmpw convection ........... libs/gaussDefCmpwConvectionScheme/
  *                                         gaussDefCmpwConvectionScheme.C:72-170,
  *                                         197-328; limiters.H:39-100
@@ -687,28 +689,40 @@ static double rp_m1(const rt_model_params *mp, double trA) {
     return M1;
 }
 
-/* thetaOld: theta at the start of the time step (the inner iterations of a
- * step share it); NULL = the current theta */
-static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_perf *perf,
-                                const double *thetaOld) {
-    const rt_mesh_desc *m = k->m;
-    const rt_model_params *mp = k->mp;
-    or_state *s = k->s;
-    const int N = m->nCells;
+/* XPomPom: f of the pre-solve conformation (XPomPomLog.C:148-163) */
+static double xpp_f(const rt_model_params *mp, double trA, double trAA) {
+    const double lam = sqrt(trA / 3.0), al = mp->alpha;
+    const double stretch = (mp->n == 0.0) ? (1.0 - 1.0 / lam) : (1.0 - 1.0 / pow(lam, mp->n + 1.0));
+    return ((2.0 * (mp->lambda / mp->lambdaS)) * exp((2.0 / mp->q) * (lam - 1.0))) * stretch +
+           (1.0 / (lam * lam)) * (1.0 - al - (al / 3.0) * (trAA - 2.0 * trA));
+}
+/* WhiteMetznerCY: the Carreau-Yasuda factor of etaP and lambda at the shear
+ * rate sqrt(2) |symm(L)| (WhiteMetznerCYLog.C:152-161, m = n, L = K, b = a) */
+static double wmcy_factor(const rt_model_params *mp, const double *L) {
+    double d2 = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double d = 0.5 * (L[3 * i + j] + L[3 * j + i]);
+            d2 += d * d;
+        }
+    return pow(1.0 + pow((mp->K * sqrt(2.0)) * sqrt(d2), mp->a), (mp->n - 1.0) / mp->a);
+}
+
+/* the cell-local right-hand side of the theta equation,
+ * symm(Omega theta - theta Omega + 2B + S_model), for n cells (AoS: L and
+ * eigVecs 9 a cell, eigVals 3, theta and rhs 6); fP receives the FENE-P/CR f
+ * of the pre-solve conformation and WhiteMetznerCY's etaP/lambda */
+void or_theta_source(const rt_model_params *mp, int N, const double *L, const double *eigVecs,
+                     const double *eigVals, const double *theta, double *rhs, double *fP) {
     const double lambda = mp->lambda, etaP = mp->etaP;
-    double *L = DALLOC(9 * (size_t)N);
-    if (gradUin) memcpy(L, gradUin, sizeof(double) * 9 * N);
-    else grad_vector(m, s->U, s->Ub, L);
-    double *rhs = DALLOC(6 * (size_t)N);
-    double *fP = DALLOC(N);   /* FENE-P f from the pre-solve conformation */
     const double zeta = (mp->model == RT_MODEL_PTT_LOG) ? mp->zeta : 0.0;
 
 #pragma omp parallel for num_threads(nthreads_) schedule(static)
     for (int c = 0; c < N; ++c) {
         t3 Lc, R, Lt, M;
         memcpy(Lc.a, L + 9 * (size_t)c, sizeof Lc.a);
-        memcpy(R.a, s->eigVecs + 9 * (size_t)c, sizeof R.a);
-        const double *ev = s->eigVals + 3 * (size_t)c;
+        memcpy(R.a, eigVecs + 9 * (size_t)c, sizeof R.a);
+        const double *ev = eigVals + 3 * (size_t)c;
         Lt = t3_T(Lc);
         if (mp->model == RT_MODEL_PTT_LOG) {
             /* L^T - zeta symm(L) */
@@ -756,6 +770,25 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
             }
             t3 AG = t3_mul(Ai, G);
             for (int i = 0; i < 9; ++i) S.a[i] = -((1.0 / lambda) * AG.a[i]);
+        } else if (mp->model == RT_MODEL_XPOMPOM_LOG) {
+            /* XPomPomLog.C:165-185: -(1/lambdaB) A^-1 (A (f - 2 alpha) + alpha A.A + (alpha - 1) I) */
+            t3 Ai = t3_mul(t3_mul(R, t3_diag(1.0 / ev[0], 1.0 / ev[1], 1.0 / ev[2])), Rt);
+            t3 AA = t3_mul(A, A);
+            const double al = mp->alpha;
+            const double f = xpp_f(mp, trA, AA.a[0] + AA.a[4] + AA.a[8]);
+            t3 G;
+            for (int i = 0; i < 9; ++i)
+                G.a[i] = (A.a[i] * (f - 2.0 * al) + al * AA.a[i]) + ((i % 4 == 0) ? (al - 1.0) : 0.0);
+            t3 AG = t3_mul(Ai, G);
+            for (int i = 0; i < 9; ++i) S.a[i] = -((1.0 / lambda) * AG.a[i]);
+        } else if (mp->model == RT_MODEL_WHITEMETZNERCY_LOG) {
+            /* WhiteMetznerCYLog.C:170-193, 203: (1/lambda(gd)) R (Lambda^-1 - I) R^T;
+             * tau with etaP(gd)/lambda(gd) of the same pre-solve grad U */
+            const double F = wmcy_factor(mp, Lc.a);
+            const double lamc = lambda * F;
+            fP[c] = (etaP * F) / lamc;
+            S = t3_mul(t3_mul(R, invm1), Rt);
+            for (int i = 0; i < 9; ++i) S.a[i] = (1.0 / lamc) * S.a[i];
         } else if (mp->model == RT_MODEL_FENECR_LOG) {
             /* FENE_CRLog.C:140-163 */
             double f = mp->L2 / (mp->L2 - trA);
@@ -771,12 +804,63 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
             S = t3_mul(t3_mul(R, D), Rt);
             for (int i = 0; i < 9; ++i) S.a[i] = (1.0 / lambda) * S.a[i];
         }
-        t3 Th = t3_from_symm(s->theta + 6 * (size_t)c);
+        t3 Th = t3_from_symm(theta + 6 * (size_t)c);
         t3 OT = t3_mul(Om, Th), TO = t3_mul(Th, Om);
         t3 Tsum;
         for (int i = 0; i < 9; ++i) Tsum.a[i] = OT.a[i] - TO.a[i] + 2.0 * B.a[i] + S.a[i];
         t3_symm(Tsum, rhs + 6 * (size_t)c);
     }
+}
+
+/* tau of n cells from the post-solve eigen-decomposition (AoS) */
+void or_tau_cells(const rt_model_params *mp, int N, const double *eigVecs, const double *eigVals,
+                  const double *fP, double *tau) {
+    const double lambda = mp->lambda, etaP = mp->etaP;
+    const double zeta = (mp->model == RT_MODEL_PTT_LOG) ? mp->zeta : 0.0;
+    double cP = etaP / lambda;
+    if (mp->model == RT_MODEL_PTT_LOG) cP = etaP / (lambda * (1.0 - zeta));
+#pragma omp parallel for num_threads(nthreads_) schedule(static)
+    for (int c = 0; c < N; ++c) {
+        t3 R, Rt;
+        memcpy(R.a, eigVecs + 9 * (size_t)c, sizeof R.a);
+        Rt = t3_T(R);
+        const double *ev = eigVals + 3 * (size_t)c;
+        t3 A = t3_mul(t3_mul(R, t3_diag(ev[0], ev[1], ev[2])), Rt);
+        t3 T;
+        if (mp->model == RT_MODEL_FENEP_LOG) {
+            double a = mp->L2 / (mp->L2 - 3.0);
+            for (int i = 0; i < 9; ++i) T.a[i] = fP[c] * A.a[i];
+            T.a[0] -= a; T.a[4] -= a; T.a[8] -= a;
+        } else {
+            T = A;
+            T.a[0] -= 1.0; T.a[4] -= 1.0; T.a[8] -= 1.0;
+        }
+        double sy[6];
+        t3_symm(T, sy);
+        /* FENE-CR: (etaP/lambda) f symm(A - I) with the pre-solve f (FENE_CRLog.C:174);
+         * Rolie-Poly: times the finite-extensibility factor of the new trA (RoliePolyLog.C:189-199) */
+        double cPc = (mp->model == RT_MODEL_FENECR_LOG) ? cP * fP[c] : cP;
+        if (mp->model == RT_MODEL_WHITEMETZNERCY_LOG) cPc = fP[c];
+        if (mp->model == RT_MODEL_ROLIEPOLY_LOG && mp->chiMax > 1.0) cPc = cP * rp_chi(mp, A.a[0] + A.a[4] + A.a[8]);
+        for (int q = 0; q < 6; ++q) tau[6 * (size_t)c + q] = cPc * sy[q];
+    }
+}
+
+/* thetaOld: theta at the start of the time step (the inner iterations of a
+ * step share it); NULL = the current theta */
+
+static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_perf *perf,
+                                const double *thetaOld) {
+    const rt_mesh_desc *m = k->m;
+    const rt_model_params *mp = k->mp;
+    or_state *s = k->s;
+    const int N = m->nCells;
+    double *L = DALLOC(9 * (size_t)N);
+    if (gradUin) memcpy(L, gradUin, sizeof(double) * 9 * N);
+    else grad_vector(m, s->U, s->Ub, L);
+    double *rhs = DALLOC(6 * (size_t)N);
+    double *fP = DALLOC(N);   /* FENE-P/CR f of the pre-solve conformation; WhiteMetznerCY etaP/lambda */
+    or_theta_source(mp, N, L, s->eigVecs, s->eigVals, s->theta, rhs, fP);
 
     /* theta equation: ddt + GaussDefCmpw == rhs */
     or_matrix Mx;
@@ -800,32 +884,7 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
 
     /* calcEig and tau */
     or_eig(N, s->theta, s->eigVals, s->eigVecs);
-    double cP = etaP / lambda;
-    if (mp->model == RT_MODEL_PTT_LOG) cP = etaP / (lambda * (1.0 - zeta));
-#pragma omp parallel for num_threads(nthreads_) schedule(static)
-    for (int c = 0; c < N; ++c) {
-        t3 R, Rt;
-        memcpy(R.a, s->eigVecs + 9 * (size_t)c, sizeof R.a);
-        Rt = t3_T(R);
-        const double *ev = s->eigVals + 3 * (size_t)c;
-        t3 A = t3_mul(t3_mul(R, t3_diag(ev[0], ev[1], ev[2])), Rt);
-        t3 T;
-        if (mp->model == RT_MODEL_FENEP_LOG) {
-            double a = mp->L2 / (mp->L2 - 3.0);
-            for (int i = 0; i < 9; ++i) T.a[i] = fP[c] * A.a[i];
-            T.a[0] -= a; T.a[4] -= a; T.a[8] -= a;
-        } else {
-            T = A;
-            T.a[0] -= 1.0; T.a[4] -= 1.0; T.a[8] -= 1.0;
-        }
-        double sy[6];
-        t3_symm(T, sy);
-        /* FENE-CR: (etaP/lambda) f symm(A - I) with the pre-solve f (FENE_CRLog.C:174);
-         * Rolie-Poly: times the finite-extensibility factor of the new trA (RoliePolyLog.C:189-199) */
-        double cPc = (mp->model == RT_MODEL_FENECR_LOG) ? cP * fP[c] : cP;
-        if (mp->model == RT_MODEL_ROLIEPOLY_LOG && mp->chiMax > 1.0) cPc = cP * rp_chi(mp, A.a[0] + A.a[4] + A.a[8]);
-        for (int q = 0; q < 6; ++q) s->tau[6 * (size_t)c + q] = cPc * sy[q];
-    }
+    or_tau_cells(mp, N, s->eigVecs, s->eigVals, fP, s->tau);
     tau_correct_bc(k);
 
     int st = RT_OK;

@@ -27,8 +27,8 @@ class or_state(C.Structure):
 
 
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
-            os.path.join(HERE, "oracle.c")):
+    deps = (os.path.join(HERE, "oracle.c"), os.path.join(HERE, "..", "include", "rheogpu.h"))
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(d) for d in deps):
         subprocess.check_call(["make", "-s", "-C", HERE, "-B" if force else "liboracle.so"])
     return LIB
 
@@ -55,6 +55,8 @@ def lib():
                                               P(abi.rt_model_params), P(abi.rt_case_ctl),
                                               P(or_state), _dp, P(abi.rt_solver_perf)]
         L.or_constitutive_correct.restype = C.c_int
+        L.or_theta_source.argtypes = [P(abi.rt_model_params), C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.or_tau_cells.argtypes = [P(abi.rt_model_params), C.c_int, _dp, _dp, _dp, _dp]
         L.or_step.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params),
                               P(abi.rt_case_ctl), P(or_state), C.c_int, P(abi.rt_step_perf)]
         L.or_step.restype = C.c_int
@@ -139,3 +141,23 @@ def eig3(s) -> tuple:
     V = np.zeros(9)
     lib().or_eig3(abi.dptr(s), abi.dptr(mu), abi.dptr(V))
     return mu, V.reshape(3, 3)
+
+
+def theta_source(mp: abi.rt_model_params, L, eigVecs, eigVals, theta):
+    """The cell-local theta right-hand side of n cells (AoS arrays (n,9),
+    (n,9), (n,3), (n,6)) -> (rhs (n,6), fP (n,))."""
+    L, eigVecs, eigVals, theta = (np.ascontiguousarray(a, dtype=np.float64) for a in (L, eigVecs, eigVals, theta))
+    n = theta.shape[0]
+    rhs, fP = np.zeros((n, 6)), np.zeros(n)
+    lib().or_theta_source(C.byref(mp), n, abi.dptr(L), abi.dptr(eigVecs), abi.dptr(eigVals), abi.dptr(theta),
+                          abi.dptr(rhs), abi.dptr(fP))
+    return rhs, fP
+
+
+def tau_cells(mp: abi.rt_model_params, eigVecs, eigVals, fP):
+    """tau (n,6) of n cells from eigVecs (n,9), eigVals (n,3) and fP (n,)."""
+    eigVecs, eigVals, fP = (np.ascontiguousarray(a, dtype=np.float64) for a in (eigVecs, eigVals, fP))
+    n = eigVals.shape[0]
+    tau = np.zeros((n, 6))
+    lib().or_tau_cells(C.byref(mp), n, abi.dptr(eigVecs), abi.dptr(eigVals), abi.dptr(fP), abi.dptr(tau))
+    return tau

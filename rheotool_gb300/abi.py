@@ -17,7 +17,7 @@ LIBNAME = os.path.join(HERE, "librheogpu.so")
 RT_OK, RT_EINVAL, RT_ENOCONV, RT_ENAN, RT_ETIMEOUT, RT_EOOM, RT_ECUDA, RT_ENOTREADY = range(8)
 RT_BC_FIXED, RT_BC_ZEROGRAD, RT_BC_LINEXTRAP = 0, 1, 2
 (RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG, RT_MODEL_FENECR_LOG,
- RT_MODEL_ROLIEPOLY_LOG) = 0, 1, 2, 3, 4, 5
+ RT_MODEL_ROLIEPOLY_LOG, RT_MODEL_XPOMPOM_LOG, RT_MODEL_WHITEMETZNERCY_LOG) = 0, 1, 2, 3, 4, 5, 6, 7
 RT_PTT_LINEAR, RT_PTT_EXP = 0, 1
 RT_STAB_NONE, RT_STAB_BSD, RT_STAB_COUPLING = 0, 1, 2
 RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB = 0, 1
@@ -41,6 +41,8 @@ MODEL_NAMES = {
     "FENE-PLog": RT_MODEL_FENEP_LOG,
     "FENE-CRLog": RT_MODEL_FENECR_LOG,
     "Rolie-PolyLog": RT_MODEL_ROLIEPOLY_LOG,
+    "XPomPomLog": RT_MODEL_XPOMPOM_LOG,
+    "WhiteMetznerCYLog": RT_MODEL_WHITEMETZNERCY_LOG,
 }
 LIMITER_NAMES = {
     "none": RT_LIM_NONE, "upwind": RT_LIM_UPWIND, "cubista": RT_LIM_CUBISTA,
@@ -80,6 +82,7 @@ class rt_model_params(C.Structure):
         ("rho", C.c_double), ("etaS", C.c_double), ("etaP", C.c_double), ("lambda_", C.c_double),
         ("alpha", C.c_double), ("epsilon", C.c_double), ("zeta", C.c_double), ("L2", C.c_double),
         ("lambdaR", C.c_double), ("beta", C.c_double), ("delta", C.c_double), ("chiMax", C.c_double),
+        ("lambdaS", C.c_double), ("q", C.c_double), ("n", C.c_double), ("K", C.c_double), ("a", C.c_double),
     ]
 
 

@@ -1,6 +1,6 @@
 // constitutive.cu — log-conformation constitutive update on the device:
-// boilerLog.H (M = R^T L^T R, decomposeGradU), the Oldroyd-B / Giesekus /
-// PTT / FENE-P sources, the theta equation (Euler + GaussDefCmpw, six
+// the per-cell sources and tau of constitutive_cell.cuh (decomposeGradU and
+// the eight log models), the theta equation (Euler + GaussDefCmpw, six
 // components solved in lock step with PBiCGStab-DILU), calcEig (cyclic Jacobi,
 // eigenvalues ascending, exp of the eigenvalues) and tau with its
 // linearExtrapolation wall values.
@@ -10,48 +10,11 @@
 //             linearExtrapolationFvPatchField.C:102-150.
 #include <cmath>
 
+#include "constitutive_cell.cuh"
 #include "fv_device.cuh"
 #include "fv_ops.h"
 
 namespace rt {
-
-// ---------------------------------------------------------------------------
-// 3x3 tensors in registers (row-major)
-// ---------------------------------------------------------------------------
-struct T3 {
-    double a[9];
-};
-
-__device__ __forceinline__ T3 mul(const T3 &A, const T3 &B) {
-    T3 C;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            C.a[3 * i + j] = A.a[3 * i] * B.a[j] + A.a[3 * i + 1] * B.a[3 + j] + A.a[3 * i + 2] * B.a[6 + j];
-    return C;
-}
-__device__ __forceinline__ T3 tr(const T3 &A) {
-    T3 B;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) B.a[3 * i + j] = A.a[3 * j + i];
-    return B;
-}
-__device__ __forceinline__ T3 dg(double x, double y, double z) {
-    T3 A;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A.a[i] = 0.0;
-    A.a[0] = x; A.a[4] = y; A.a[8] = z;
-    return A;
-}
-__device__ __forceinline__ T3 load9(const double *__restrict__ p, int n, int c) {
-    T3 A;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A.a[i] = p[(size_t)i * n + c];
-    return A;
-}
 
 // ---------------------------------------------------------------------------
 // cyclic Jacobi on a symmetric 3x3 (same sweep order, skip rule and sort as
@@ -137,123 +100,6 @@ void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double 
     launch_count(ctx);
 }
 
-// Rolie-Poly stretch rate M1 = 2 (1 - sqrt(3/trA)) / lambdaR, times the
-// finite-extensibility factor when chiMax > 1 (RoliePolyLog.C:143-156)
-__host__ __device__ inline double roliepoly_chi(const rt_model_params &mp, double trA) {
-    const double c2 = mp.chiMax * mp.chiMax;
-    return ((3.0 - (trA / 3.0) / c2) * (1.0 - 1.0 / c2)) / ((1.0 - (trA / 3.0) / c2) * (3.0 - 1.0 / c2));
-}
-__host__ __device__ inline double roliepoly_m1(const rt_model_params &mp, double trA) {
-    double M1 = 2.0 * (1.0 - sqrt(3.0 / trA)) / mp.lambdaR;
-    if (mp.chiMax > 1.0) M1 *= roliepoly_chi(mp, trA);
-    return M1;
-}
-
-// ---------------------------------------------------------------------------
-// theta source: rhs = symm(Omega theta - theta Omega + 2B + S_model)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void theta_rhs_cell(int c, int N, const rt_model_params &mp,
-                                               const double *__restrict__ L, const double *__restrict__ Rv,
-                                               const double *__restrict__ evv, const double *__restrict__ theta,
-                                               double *__restrict__ rhs, double *__restrict__ fP) {
-    const double lambda = mp.lambda;
-    const double zeta = (mp.model == RT_MODEL_PTT_LOG) ? mp.zeta : 0.0;
-    T3 Lc = load9(L, N, c), R = load9(Rv, N, c);
-    double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    T3 Lt = tr(Lc);
-    if (mp.model == RT_MODEL_PTT_LOG) {
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                Lt.a[3 * i + j] = Lt.a[3 * i + j] - zeta * (0.5 * (Lc.a[3 * i + j] + Lc.a[3 * j + i]));
-    }
-    T3 Rt = tr(R);
-    T3 M = mul(mul(Rt, Lt), R);
-    T3 om = dg(0.0, 0.0, 0.0), Bt = dg(M.a[0], M.a[4], M.a[8]);
-    om.a[1] = (e1 * M.a[1] + e0 * M.a[3]) / (e1 - e0 + 1e-16);
-    om.a[2] = (e2 * M.a[2] + e0 * M.a[6]) / (e2 - e0 + 1e-16);
-    om.a[5] = (e2 * M.a[5] + e1 * M.a[7]) / (e2 - e1 + 1e-16);
-    om.a[3] = -om.a[1]; om.a[6] = -om.a[2]; om.a[7] = -om.a[5];
-    T3 Om = mul(mul(R, om), Rt);
-    T3 B = mul(mul(R, Bt), Rt);
-    T3 invm1 = dg(1.0 / e0 - 1.0, 1.0 / e1 - 1.0, 1.0 / e2 - 1.0);
-    T3 S;
-    if (mp.model == RT_MODEL_OLDROYDB_LOG) {
-        S = mul(mul(R, invm1), Rt);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S.a[i] = (1.0 / lambda) * S.a[i];
-    } else if (mp.model == RT_MODEL_GIESEKUS_LOG) {
-        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
-        T3 T = mul(mul(R, invm1), Rt);
-        T3 ATT = mul(A, mul(T, T));
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S.a[i] = (1.0 / lambda) * (T.a[i] - mp.alpha * ATT.a[i]);
-    } else if (mp.model == RT_MODEL_PTT_LOG) {
-        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
-        double trA = A.a[0] + A.a[4] + A.a[8];
-        T3 T = mul(mul(R, invm1), Rt);
-        double fac = (mp.pttFunction == RT_PTT_EXP) ? exp((mp.epsilon / (1.0 - zeta)) * (trA - 3.0))
-                                                    : (1.0 + (mp.epsilon / (1.0 - zeta)) * (trA - 3.0));
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
-    } else if (mp.model == RT_MODEL_ROLIEPOLY_LOG) {
-        // RoliePolyLog.C:140-179: -(1/lambdaD) A^-1 ((A - I) + M1 lambdaD (A + beta (trA/3)^delta (A - I)))
-        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
-        T3 Ai = mul(mul(R, dg(1.0 / e0, 1.0 / e1, 1.0 / e2)), Rt);
-        const double trA = A.a[0] + A.a[4] + A.a[8];
-        const double lamD = lambda;
-        const double M1 = roliepoly_m1(mp, trA);
-        const double ccr = mp.beta * pow(trA / 3.0, mp.delta);
-        T3 G;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) {
-            const double AmI = A.a[i] - ((i % 4 == 0) ? 1.0 : 0.0);
-            G.a[i] = AmI + (M1 * lamD) * (A.a[i] + ccr * AmI);
-        }
-        T3 AG = mul(Ai, G);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S.a[i] = -((1.0 / lamD) * AG.a[i]);
-    } else if (mp.model == RT_MODEL_FENECR_LOG) {
-        // FENE_CRLog.C:140-163: (1/lambda) f R (Lambda^-1 - I) R^T, f from the pre-solve A
-        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
-        double trA = A.a[0] + A.a[4] + A.a[8];
-        double f = mp.L2 / (mp.L2 - trA);
-        fP[c] = f;
-        S = mul(mul(R, invm1), Rt);
-        const double lf = (1.0 / lambda) * f;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S.a[i] = lf * S.a[i];
-    } else {
-        T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
-        double trA = A.a[0] + A.a[4] + A.a[8];
-        double f = mp.L2 / (mp.L2 - trA);
-        double a = mp.L2 / (mp.L2 - 3.0);
-        fP[c] = f;
-        T3 D = dg(a * (1.0 / e0) - f, a * (1.0 / e1) - f, a * (1.0 / e2) - f);
-        S = mul(mul(R, D), Rt);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S.a[i] = (1.0 / lambda) * S.a[i];
-    }
-    double th[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) th[q] = theta[(size_t)q * N + c];
-    T3 Th;
-    Th.a[0] = th[0]; Th.a[1] = th[1]; Th.a[2] = th[2];
-    Th.a[3] = th[1]; Th.a[4] = th[3]; Th.a[5] = th[4];
-    Th.a[6] = th[2]; Th.a[7] = th[4]; Th.a[8] = th[5];
-    T3 OT = mul(Om, Th), TO = mul(Th, Om);
-    T3 Ts;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) Ts.a[i] = OT.a[i] - TO.a[i] + 2.0 * B.a[i] + S.a[i];
-    rhs[c] = Ts.a[0];
-    rhs[(size_t)N + c] = 0.5 * (Ts.a[1] + Ts.a[3]);
-    rhs[(size_t)2 * N + c] = 0.5 * (Ts.a[2] + Ts.a[6]);
-    rhs[(size_t)3 * N + c] = Ts.a[4];
-    rhs[(size_t)4 * N + c] = 0.5 * (Ts.a[5] + Ts.a[7]);
-    rhs[(size_t)5 * N + c] = Ts.a[8];
-}
-
 __global__ void k_theta_rhs(int N, rt_model_params mp, const int *__restrict__ caseOf,
                             const rt_model_params *__restrict__ cp, const double *__restrict__ L,
                             const double *__restrict__ Rv, const double *__restrict__ evv,
@@ -290,38 +136,6 @@ __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__res
     dSolve[c] = d;
 #pragma unroll
     for (int k = 0; k < 6; ++k) bSolve[(size_t)k * N + c] = b[k];
-}
-
-// tau = c (R Lambda R^T - I)   (FENE-P: c (f R Lambda R^T - a I); FENE-CR:
-// (c f)(R Lambda R^T - I), FENE_CRLog.C:174, with the pre-solve f)
-__device__ __forceinline__ void tau_cell(int c, int N, const rt_model_params &mp, const double *__restrict__ Rv,
-                                         const double *__restrict__ evv, const double *__restrict__ fP,
-                                         double *__restrict__ tau) {
-    double zeta = (mp.model == RT_MODEL_PTT_LOG) ? mp.zeta : 0.0;
-    double cP = mp.etaP / mp.lambda;
-    if (mp.model == RT_MODEL_PTT_LOG) cP = mp.etaP / (mp.lambda * (1.0 - zeta));
-    if (mp.model == RT_MODEL_FENECR_LOG) cP = cP * fP[c];
-    T3 R = load9(Rv, N, c);
-    T3 A = mul(mul(R, dg(evv[c], evv[N + c], evv[2 * N + c])), tr(R));
-    T3 T;
-    if (mp.model == RT_MODEL_FENEP_LOG) {
-        double a = mp.L2 / (mp.L2 - 3.0);
-        double f = fP[c];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) T.a[i] = f * A.a[i];
-        T.a[0] -= a; T.a[4] -= a; T.a[8] -= a;
-    } else {
-        T = A;
-        T.a[0] -= 1.0; T.a[4] -= 1.0; T.a[8] -= 1.0;
-    }
-    if (mp.model == RT_MODEL_ROLIEPOLY_LOG && mp.chiMax > 1.0)   // RoliePolyLog.C:189-199
-        cP = cP * roliepoly_chi(mp, A.a[0] + A.a[4] + A.a[8]);
-    tau[c] = cP * T.a[0];
-    tau[(size_t)N + c] = cP * (0.5 * (T.a[1] + T.a[3]));
-    tau[(size_t)2 * N + c] = cP * (0.5 * (T.a[2] + T.a[6]));
-    tau[(size_t)3 * N + c] = cP * T.a[4];
-    tau[(size_t)4 * N + c] = cP * (0.5 * (T.a[5] + T.a[7]));
-    tau[(size_t)5 * N + c] = cP * T.a[8];
 }
 
 __global__ void k_tau(int N, rt_model_params mp, const int *__restrict__ caseOf,
@@ -394,6 +208,12 @@ __device__ __forceinline__ bool mix_fp32_ok(double m0, double m1, double m2) {
     return scale <= kMixMuHi && gap > kMixGap * scale && isfinite(scale);
 }
 
+// models whose cell algebra has no FP32 form here (Rolie-Poly, XPomPom,
+// WhiteMetznerCY): the mixed kernels run their FP64 code for every cell
+__device__ __forceinline__ bool mixed_fp64_model(int model) {
+    return model == RT_MODEL_ROLIEPOLY_LOG || model == RT_MODEL_XPOMPOM_LOG || model == RT_MODEL_WHITEMETZNERCY_LOG;
+}
+
 __global__ void k_eig_mixed(int n, const double *__restrict__ theta, double *__restrict__ ev,
                             double *__restrict__ vec) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -428,7 +248,7 @@ __global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restr
     if (c >= N) return;
     const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    if (mp.model == RT_MODEL_ROLIEPOLY_LOG || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
+    if (mixed_fp64_model(mp.model) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         theta_rhs_cell(c, N, mp, L, Rv, evv, theta, rhs, fP);
         return;
     }
@@ -523,7 +343,7 @@ __global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ 
     if (c >= N) return;
     const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    if (mp.model == RT_MODEL_ROLIEPOLY_LOG || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
+    if (mixed_fp64_model(mp.model) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         tau_cell(c, N, mp, Rv, evv, fP, tau);
         return;
     }

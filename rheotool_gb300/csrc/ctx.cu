@@ -418,8 +418,12 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
     return guarded(ctx, [&]() -> rt_status {
         RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
         RT_REQUIRE(bc && mp && ctl, RT_EINVAL, "null argument");
-        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_ROLIEPOLY_LOG, RT_EINVAL,
+        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_WHITEMETZNERCY_LOG, RT_EINVAL,
                    "unknown constitutive model");
+        RT_REQUIRE(mp->model != RT_MODEL_XPOMPOM_LOG || (mp->lambdaS > 0 && mp->q > 0), RT_EINVAL,
+                   "XPomPom needs lambdaS > 0 and q > 0");
+        RT_REQUIRE(mp->model != RT_MODEL_WHITEMETZNERCY_LOG || mp->a > 0, RT_EINVAL,
+                   "WhiteMetznerCY needs a > 0");
         RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
         RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
         RT_REQUIRE(mp->model != RT_MODEL_ROLIEPOLY_LOG || mp->lambdaR > 0, RT_EINVAL,
@@ -781,8 +785,14 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model
             const Batch &b = ctx->mesh.batch;
             for (int c = 0; c < b.n; ++c) {
                 const rt_model_params &mp = models[c];
-                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_ROLIEPOLY_LOG, RT_EINVAL,
+                RT_REQUIRE(mp.model >= RT_MODEL_OLDROYDB_LOG && mp.model <= RT_MODEL_WHITEMETZNERCY_LOG, RT_EINVAL,
                            "case " + std::to_string(c) + ": unknown constitutive model");
+                RT_REQUIRE(mp.model != RT_MODEL_ROLIEPOLY_LOG || mp.lambdaR > 0, RT_EINVAL,
+                           "case " + std::to_string(c) + ": Rolie-Poly needs lambdaR > 0");
+                RT_REQUIRE(mp.model != RT_MODEL_XPOMPOM_LOG || (mp.lambdaS > 0 && mp.q > 0), RT_EINVAL,
+                           "case " + std::to_string(c) + ": XPomPom needs lambdaS > 0 and q > 0");
+                RT_REQUIRE(mp.model != RT_MODEL_WHITEMETZNERCY_LOG || mp.a > 0, RT_EINVAL,
+                           "case " + std::to_string(c) + ": WhiteMetznerCY needs a > 0");
                 RT_REQUIRE(mp.lambda > 0 && mp.rho > 0, RT_EINVAL,
                            "case " + std::to_string(c) + ": lambda and rho must be positive");
                 RT_REQUIRE((mp.model != RT_MODEL_FENEP_LOG && mp.model != RT_MODEL_FENECR_LOG) || mp.L2 > 3.0, RT_EINVAL,

@@ -139,6 +139,26 @@ class LoadedCase:
     substitutions: List[str] = field(default_factory=list)
 
 
+# the keywords each model's constructor looks up without a default, beyond
+# rho, etaS, etaP, lambda (lambdaD, lambdaB) and stabilization
+# (GiesekusLog.C, PTTLog.C, FENE_PLog.C, FENE_CRLog.C, RoliePolyLog.C,
+# XPomPomLog.C:114-122, WhiteMetznerCYLog.C:124-133)
+MODEL_KEYS = {
+    "GiesekusLog": ("alpha",),
+    "PTTLog": ("epsilon", "zeta", "destructionFunctionType", "alpha", "beta"),
+    "FENE-PLog": ("L2",),
+    "FENE-CRLog": ("L2",),
+    "Rolie-PolyLog": ("lambdaR", "beta", "delta", "chiMax"),
+    "XPomPomLog": ("lambdaS", "alpha", "q", "n"),
+    "WhiteMetznerCYLog": ("m", "n", "K", "L", "a", "b"),
+}
+# the temperature functions each model builds (thermoFunction::New)
+THERMO_KEYS = {
+    "Rolie-PolyLog": ("thermoEta", "thermoLambdaD", "thermoLambdaR"),
+    "XPomPomLog": ("thermoEta", "thermoLambdaS", "thermoLambdaB"),
+}
+
+
 class CaseError(ValueError):
     pass
 
@@ -206,17 +226,34 @@ def load_case(case_dir: str, substitute: bool = False,
     typ = par.get("type", "")
     if typ not in abi.MODEL_NAMES:
         raise CaseError(f"Unknown constitutiveEq type {typ}; valid: {sorted(abi.MODEL_NAMES)}")
-    for key in ("rho", "etaS", "etaP", "stabilization", "lambdaD" if typ == "Rolie-PolyLog" else "lambda"):
+    lam_key = {"Rolie-PolyLog": "lambdaD", "XPomPomLog": "lambdaB"}.get(typ, "lambda")
+    for key in ("rho", "etaS", "etaP", "stabilization", lam_key) + MODEL_KEYS.get(typ, ()):
         if key not in par:   # constitutiveEq's lookups (constitutiveEq.C:435-438 for stabilization)
             raise CaseError(f"keyword {key} is undefined in constitutiveProperties")
     mkw: Dict[str, Any] = dict(type=typ, rho=scalar(par["rho"]), etaS=scalar(par["etaS"]), etaP=scalar(par["etaP"]),
                                stabilization=par["stabilization"])
-    mkw["lambda_"] = scalar(par["lambdaD"] if typ == "Rolie-PolyLog" else par["lambda"])
-    for k in ("alpha", "epsilon", "zeta", "L2", "lambdaR", "beta", "delta", "chiMax"):
+    mkw["lambda_"] = scalar(par[lam_key])
+    for k in ("alpha", "epsilon", "zeta", "L2", "lambdaR", "beta", "delta", "chiMax", "lambdaS", "q", "n", "K",
+              "a"):
         if k in par:
             mkw[k] = scalar(par[k])
+    if typ == "WhiteMetznerCYLog":
+        # WhiteMetznerCYLog.C:140-149: the log form only when m = n, K = L, a = b
+        for x, y in (("m", "n"), ("K", "L"), ("a", "b")):
+            if scalar(par[x]) != scalar(par[y]):
+                raise CaseError("The Log version of the WhiteMetznerCY model can only be used if m=n and K=L and "
+                                "a=b; use the stress version (WhiteMetznerCY)")
+    for th in THERMO_KEYS.get(typ, ("thermoEta", "thermoLambda")):
+        # thermoFunction::New: no sub-dictionary means the Constant (isothermal) function
+        t = par.get(th)
+        if isinstance(t, dict) and t.get("type", "Constant") != "Constant":
+            raise CaseError(f"{th} type {t.get('type')}: only the Constant thermoFunction is implemented")
     if "destructionFunctionType" in par:
         mkw["destructionFunctionType"] = par["destructionFunctionType"]
+        if typ == "PTTLog" and par["destructionFunctionType"] not in ("linear", "exponential"):
+            # the generalized (Mittag-Leffler) function of PTTLog.C:198-236 is not built
+            raise CaseError(f"PTTLog destructionFunctionType {par['destructionFunctionType']}: implemented are "
+                            "linear and exponential")
     model = Model(**mkw)
 
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))

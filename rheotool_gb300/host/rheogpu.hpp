@@ -151,7 +151,8 @@ class ConstitutiveEq {
 public:
     // `type` selects the model; the other keywords are the model's (rho,
     // etaS, etaP, lambda, alpha, epsilon, zeta, L2, lambdaR/lambdaD, beta,
-    // delta, chiMax, destructionFunctionType, stabilization)
+    // delta, chiMax, lambdaS/lambdaB, q, n, m, K, L, a, b,
+    // destructionFunctionType, stabilization)
     static std::unique_ptr<ConstitutiveEq> New(const std::string &name, const Dictionary &constitutiveProperties);
     static const std::vector<std::string> &types();
 

@@ -255,8 +255,8 @@ std::vector<SolverPerformance> SparseSolver::solve(const LduMatrixView &m, doubl
 // ConstitutiveEq (constitutiveEq run-time selection)
 // ---------------------------------------------------------------------------
 const std::vector<std::string> &ConstitutiveEq::types() {
-    static const std::vector<std::string> v{"FENE-CRLog", "FENE-PLog", "GiesekusLog", "Oldroyd-BLog", "PTTLog",
-                                            "Rolie-PolyLog"};
+    static const std::vector<std::string> v{"FENE-CRLog", "FENE-PLog",         "GiesekusLog",      "Oldroyd-BLog",
+                                            "PTTLog",     "Rolie-PolyLog",     "WhiteMetznerCYLog", "XPomPomLog"};
     return v;
 }
 
@@ -272,6 +272,8 @@ std::unique_ptr<ConstitutiveEq> ConstitutiveEq::New(const std::string &name, con
     else if (type == "FENE-PLog") mp.model = RT_MODEL_FENEP_LOG;
     else if (type == "FENE-CRLog") mp.model = RT_MODEL_FENECR_LOG;
     else if (type == "Rolie-PolyLog") mp.model = RT_MODEL_ROLIEPOLY_LOG;
+    else if (type == "XPomPomLog") mp.model = RT_MODEL_XPOMPOM_LOG;
+    else if (type == "WhiteMetznerCYLog") mp.model = RT_MODEL_WHITEMETZNERCY_LOG;
     else throw FatalError(valid_list("constitutiveEq type", type, types()));
     mp.rho = d.lookupScalar("rho");
     mp.etaS = d.lookupScalar("etaS");
@@ -282,13 +284,32 @@ std::unique_ptr<ConstitutiveEq> ConstitutiveEq::New(const std::string &name, con
         mp.beta = d.lookupScalar("beta");
         mp.delta = d.lookupScalar("delta");
         mp.chiMax = d.lookupScalar("chiMax");
+    } else if (mp.model == RT_MODEL_XPOMPOM_LOG) {
+        // XPomPomLog.C:114-122
+        mp.lambda = d.lookupScalar("lambdaB");
+        mp.lambdaS = d.lookupScalar("lambdaS");
+        mp.q = d.lookupScalar("q");
+        mp.n = d.lookupScalar("n");
     } else {
         mp.lambda = d.lookupScalar("lambda");
     }
-    if (mp.model == RT_MODEL_GIESEKUS_LOG) mp.alpha = d.lookupScalar("alpha");
+    if (mp.model == RT_MODEL_WHITEMETZNERCY_LOG) {
+        // WhiteMetznerCYLog.C:118-141: the log form needs m = n, K = L, a = b
+        mp.n = d.lookupScalar("n");
+        mp.K = d.lookupScalar("K");
+        mp.a = d.lookupScalar("a");
+        if (d.lookupScalar("m") != mp.n || d.lookupScalar("L") != mp.K || d.lookupScalar("b") != mp.a)
+            throw FatalError("The Log version of the WhiteMetznerCY model can only be used if:\n\n   m=n   and   K=L"
+                             "   and   a=b\n\n Check if this is the case, otherwise use the stress version "
+                             "(WhiteMetznerCY).");
+    }
+    if (mp.model == RT_MODEL_GIESEKUS_LOG || mp.model == RT_MODEL_XPOMPOM_LOG) mp.alpha = d.lookupScalar("alpha");
     if (mp.model == RT_MODEL_PTT_LOG) {
         mp.epsilon = d.lookupScalar("epsilon");
         mp.zeta = d.lookupScalar("zeta");
+        // PTTLog.C reads the generalized function's alpha and beta whatever the type
+        mp.alpha = d.lookupScalar("alpha");
+        mp.beta = d.lookupScalar("beta");
         const std::string f = d.lookup("destructionFunctionType");
         if (f == "linear") mp.pttFunction = RT_PTT_LINEAR;
         else if (f == "exponential") mp.pttFunction = RT_PTT_EXP;

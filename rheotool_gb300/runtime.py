@@ -257,7 +257,8 @@ class ConstitutiveEq:
     """GPU constitutive model behind rheoTool's constitutiveEq API.
 
     ``New(name, case)`` selects by ``case.model.type`` (``Oldroyd-BLog``,
-    ``GiesekusLog``, ``PTTLog``, ``FENE-PLog``, ``FENE-CRLog``), exactly as
+    ``GiesekusLog``, ``PTTLog``, ``FENE-PLog``, ``FENE-CRLog``,
+    ``Rolie-PolyLog``, ``XPomPomLog``, ``WhiteMetznerCYLog``), exactly as
     ``constitutiveEq::New`` does from ``constitutiveProperties``; an unknown
     type raises like the reference's FatalError (``newConstitutiveEq.C:47-58``).
     """

@@ -66,9 +66,28 @@ static void cpu_checks() {
     CHECK(m.find("Oldroyd-BLog") != std::string::npos && m.find("FENE-PLog") != std::string::npos);
 
     Dictionary ptt = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
-                                       " destructionFunctionType exponential; stabilization BSD;");
+                                       " alpha 1; beta 1; destructionFunctionType exponential; stabilization BSD;");
     auto pt = ConstitutiveEq::New("p", ptt);
     CHECK(pt->params().pttFunction == RT_PTT_EXP && pt->params().stabilization == RT_STAB_BSD);
+    Dictionary pttg = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
+                                        " alpha 1; beta 1; destructionFunctionType generalized; stabilization BSD;");
+    CHECK(throws([&] { ConstitutiveEq::New("p", pttg); }).find("Unknown destructionFunctionType generalized") !=
+          std::string::npos);
+
+    Dictionary xpp = Dictionary::parse("type XPomPomLog; rho 1; etaS 0.1; etaP 0.9; lambdaB 1.0; lambdaS 0.25;"
+                                       " alpha 0.15; q 2; n 0; stabilization coupling;");
+    auto x = ConstitutiveEq::New("xpp", xpp);
+    CHECK(x->params().model == RT_MODEL_XPOMPOM_LOG && x->params().lambda == 1.0 && x->params().lambdaS == 0.25);
+    CHECK(x->params().alpha == 0.15 && x->params().q == 2.0 && x->params().n == 0.0);
+    Dictionary wm = Dictionary::parse("type WhiteMetznerCYLog; rho 1; etaS 0.1; etaP 0.9; lambda 1; m 0.5; n 0.5;"
+                                      " K 1; L 1; a 2; b 2; stabilization coupling;");
+    auto w = ConstitutiveEq::New("wm", wm);
+    CHECK(w->params().model == RT_MODEL_WHITEMETZNERCY_LOG && w->params().n == 0.5 && w->params().K == 1.0 &&
+          w->params().a == 2.0);
+    Dictionary wmbad = Dictionary::parse("type WhiteMetznerCYLog; rho 1; etaS 0.1; etaP 0.9; lambda 1; m 0.5;"
+                                         " n 0.4; K 1; L 1; a 2; b 2; stabilization coupling;");
+    CHECK(throws([&] { ConstitutiveEq::New("wm", wmbad); }).find("m=n") != std::string::npos);
+
     Dictionary nostab = Dictionary::parse("type Oldroyd-BLog; rho 1; etaS 1; etaP 1; lambda 1;");
     CHECK(throws([&] { ConstitutiveEq::New("o", nostab); }).find("stabilization") != std::string::npos);
 

@@ -133,3 +133,37 @@ def test_rheotool_external_solvers_and_relaxation(tmp_path):
         load_case(root)
     lc2 = load_case(root, substitute=True)
     assert any("relaxationFactors equations U: 0.7 -> 1" in x for x in lc2.substitutions)
+
+
+def _props(root, body):
+    _write(os.path.join(root, "constant", "constitutiveProperties"), "dictionary", "constitutiveProperties",
+           "parameters\n{\n" + body + "\n}\n")
+
+
+def test_model_keywords_as_the_reference_reads_them(tmp_path):
+    """XPomPomLog and WhiteMetznerCYLog read their constructors' keywords
+    (lambdaB for lambda; WhiteMetznerCYLog only with m = n, K = L, a = b);
+    a missing keyword, a temperature function other than Constant and the
+    generalized PTT function are refused as the reference would abort."""
+    root = _cavity_dir(str(tmp_path / "m"))
+    base = "rho 1; etaS 0.1; etaP 0.9; stabilization coupling;"
+    _props(root, "type XPomPomLog; " + base + " lambdaB 0.5; lambdaS 0.2; alpha 0.15; q 2; n 0;")
+    m = load_case(root).case.model
+    assert (m.type, m.lambda_, m.lambdaS, m.alpha, m.q, m.n) == ("XPomPomLog", 0.5, 0.2, 0.15, 2.0, 0.0)
+    _props(root, "type WhiteMetznerCYLog; " + base + " lambda 0.5; m 0.4; n 0.4; K 1; L 1; a 2; b 2;")
+    m = load_case(root).case.model
+    assert (m.type, m.lambda_, m.n, m.K, m.a) == ("WhiteMetznerCYLog", 0.5, 0.4, 1.0, 2.0)
+    _props(root, "type WhiteMetznerCYLog; " + base + " lambda 0.5; m 0.5; n 0.4; K 1; L 1; a 2; b 2;")
+    with pytest.raises(CaseError, match="m=n"):
+        load_case(root)
+    _props(root, "type XPomPomLog; " + base + " lambdaB 0.5; lambdaS 0.2; alpha 0.15; q 2;")
+    with pytest.raises(CaseError, match="keyword n is undefined"):
+        load_case(root)
+    _props(root, "type GiesekusLog; " + base + " lambda 0.5; alpha 0.1;"
+           " thermoLambda { type Arrhenius; }")
+    with pytest.raises(CaseError, match="thermoLambda type Arrhenius"):
+        load_case(root)
+    _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; alpha 1; beta 1;"
+           " destructionFunctionType generalized;")
+    with pytest.raises(CaseError, match="generalized"):
+        load_case(root)

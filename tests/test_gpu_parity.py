@@ -252,7 +252,9 @@ def test_residual_matches_oracle(ctx):
 
 MODELS = [("Oldroyd-BLog", {}), ("GiesekusLog", {"alpha": 0.1}),
           ("PTTLog", {"epsilon": 0.25}), ("FENE-PLog", {"L2": 100.0}), ("FENE-CRLog", {"L2": 20.0}),
-          ("Rolie-PolyLog", {"lambdaR": 0.2, "chiMax": 5.0})]
+          ("Rolie-PolyLog", {"lambdaR": 0.2, "chiMax": 5.0}),
+          ("XPomPomLog", {"lambdaS": 0.2, "q": 2.0, "alpha": 0.15}),
+          ("WhiteMetznerCYLog", {"K": 1.0, "a": 2.0})]
 
 
 def flow_state(case, steps=3):

@@ -158,8 +158,9 @@ def zero_d(model, lam, etaP, dt, **kw):
     diag(1e-8, -1e-8, 0): from exactly theta = 0 with R = I, decomposeGradU
     gives B = 0 and Omega.theta - theta.Omega = 0 under pure shear, so the
     log-conformation update (rheoTool's as well) would stay at rest."""
-    # model keys that the case builder's own arguments shadow (Rolie-Poly's beta)
-    late = {k: kw.pop(k) for k in ("beta",) if k in kw}
+    # model keys that the case builder's own arguments shadow (Rolie-Poly's
+    # beta, XPomPom's and WhiteMetznerCY's n)
+    late = {k: kw.pop(k) for k in ("beta", "n") if k in kw}
     case = cavity_case(2, model=model, Wi=lam, beta=1.0 - etaP, Re=1.0, dt=dt, **kw)
     for k, v in late.items():
         setattr(case.model, k, v)
@@ -196,7 +197,7 @@ def rp_chi(trA, chiMax):
 
 
 def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=1.0, beta=0.0, delta=-0.5,
-                        chiMax=0.0):
+                        chiMax=0.0, lambdaS=1.0, q=1.0, n=0.0, K=0.0, a=1.0):
     """Steady simple shear of the conformation-tensor form, integrated with
     scipy (an independent formulation of the same model)."""
     from scipy.integrate import solve_ivp
@@ -220,10 +221,19 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=
             if chiMax > 1.0:
                 M1 *= rp_chi(trA, chiMax)
             g = (A - I) + lam * M1 * (A + beta * (trA / 3.0) ** delta * (A - I))
+        elif model == "XPomPomLog":
+            trA = np.trace(A)
+            Lb = np.sqrt(trA / 3.0)
+            f = (2.0 * (lam / lambdaS) * np.exp((2.0 / q) * (Lb - 1.0)) * (1.0 - Lb ** -(n + 1.0))
+                 + (1.0 - alpha - (alpha / 3.0) * (np.trace(A @ A) - 2.0 * trA)) / Lb ** 2)
+            g = A * (f - 2.0 * alpha) + alpha * A @ A + (alpha - 1.0) * I
+        elif model == "WhiteMetznerCYLog":
+            # Oldroyd-B with the Carreau-Yasuda relaxation time at the shear rate
+            g = (A - I) / (1.0 + (K * rate) ** a) ** ((n - 1.0) / a)
         else:
             f = L2 / (L2 - np.trace(A))
-            a = L2 / (L2 - 3.0)
-            g = f * A - a * I
+            a2 = L2 / (L2 - 3.0)
+            g = f * A - a2 * I
         return (kap @ A + A @ kap.T - g / lam).reshape(-1)
 
     sol = solve_ivp(rhs, (0, 60 * lam), I.reshape(-1), rtol=1e-12, atol=1e-14, method="LSODA")
@@ -247,6 +257,11 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=
      {"lambdaR": 0.2, "beta": 0.5, "delta": -0.5}),
     ("Rolie-PolyLog", {"lambdaR": 0.3, "beta": 0.3, "delta": -0.5, "chiMax": 5.0},
      {"lambdaR": 0.3, "beta": 0.3, "delta": -0.5, "chiMax": 5.0}),
+    ("XPomPomLog", {"lambdaS": 0.4, "q": 2.0, "alpha": 0.15, "n": 0.0},
+     {"lambdaS": 0.4, "q": 2.0, "alpha": 0.15, "n": 0.0}),
+    ("XPomPomLog", {"lambdaS": 0.25, "q": 5.0, "alpha": 0.1, "n": 1.5},
+     {"lambdaS": 0.25, "q": 5.0, "alpha": 0.1, "n": 1.5}),
+    ("WhiteMetznerCYLog", {"K": 0.5, "a": 2.0, "n": 0.6}, {"K": 0.5, "a": 2.0, "n": 0.6}),
 ])
 def test_steady_shear_matches_conformation_form(model, kw, ckw):
     lam, etaP, rate = 1.0, 0.8, 1.5
@@ -263,6 +278,11 @@ def test_steady_shear_matches_conformation_form(model, kw, ckw):
     if model == "Oldroyd-BLog":
         assert abs(tau[1] - etaP * rate) < 1e-8
         assert abs((tau[0] - tau[3]) - 2 * etaP * lam * rate ** 2) < 1e-7
+    if model == "WhiteMetznerCYLog":
+        # closed form: tau_xy = etaP(gd) gd, N1 = 2 etaP(gd) lambda(gd) gd^2
+        F = (1.0 + (kw["K"] * rate) ** kw["a"]) ** ((kw["n"] - 1.0) / kw["a"])
+        assert abs(tau[1] - etaP * F * rate) < 1e-8
+        assert abs((tau[0] - tau[3]) - 2 * etaP * F * lam * F * rate ** 2) < 1e-7
 
 
 # ---------------------------------------------------------------------------
@@ -326,10 +346,11 @@ def _golden_cases():
     return mod.golden_cases()
 
 
-@pytest.mark.parametrize("index", range(4))
+@pytest.mark.parametrize("index", range(6))
 def test_golden_vectors(index):
-    """Every frozen oracle output (the cavity for Oldroyd-B, FENE-CR and
-    Rolie-Poly, the periodic PTT channel with two inner iterations) is
+    """Every frozen oracle output (the cavity for Oldroyd-B, FENE-CR,
+    Rolie-Poly, XPomPom and WhiteMetznerCY, the periodic PTT channel with two
+    inner iterations) is
     reproduced to round-off by the current oracle."""
     from oracle.pyoracle import Oracle
     name, case, f0, steps = _golden_cases()[index]
