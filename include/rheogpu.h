@@ -114,6 +114,8 @@ typedef struct {
                                      viscosity and the relaxation time */
 #define RT_PTT_LINEAR 0
 #define RT_PTT_EXP    1
+#define RT_PTT_GENERALIZED 2   /* Gamma(beta) E_{alpha,beta}(z), the Mittag-Leffler function
+                                  summed as in PTTLog.C:201-236 (alpha, beta > 0) */
 #define RT_STAB_NONE     0
 #define RT_STAB_BSD      1
 #define RT_STAB_COUPLING 2
@@ -121,12 +123,13 @@ typedef struct {
 typedef struct {
     int32_t model, pttFunction, stabilization, pad_;
     double rho, etaS, etaP, lambda;
-    double alpha;     /* Giesekus mobility                                    */
+    double alpha;     /* Giesekus mobility; XPomPom anisotropy; PTT generalized: Mittag-Leffler alpha */
     double epsilon;   /* PTT extensibility                                    */
     double zeta;      /* PTT slip                                             */
     double L2;        /* FENE-P / FENE-CR squared extensibility               */
     double lambdaR;   /* Rolie-Poly stretch relaxation time (lambda = lambdaD) */
-    double beta;      /* Rolie-Poly convective constraint release coefficient */
+    double beta;      /* Rolie-Poly convective constraint release coefficient;
+                         PTT generalized: Mittag-Leffler beta                  */
     double delta;     /* Rolie-Poly CCR exponent                              */
     double chiMax;    /* Rolie-Poly maximum stretch (finite extensibility when > 1) */
     double lambdaS;   /* XPomPom stretch relaxation time (lambda = lambdaB)   */
@@ -134,6 +137,9 @@ typedef struct {
     double n;         /* XPomPom stretch exponent; WhiteMetznerCY power index */
     double K;         /* WhiteMetznerCY time constant (K = L)                 */
     double a;         /* WhiteMetznerCY Carreau-Yasuda exponent (a = b)       */
+    double rTolMittagLeffler;       /* PTT generalized: series tolerance (1e-12)  */
+    int32_t maxIterMittagLeffler;   /* PTT generalized: series terms at most (200) */
+    int32_t pad2_;
 } rt_model_params;
 
 /* ---- linear solvers ----------------------------------------------------- */

@@ -689,6 +689,33 @@ static double rp_m1(const rt_model_params *mp, double trA) {
     return M1;
 }
 
+/* generalized PTT (PTTLog.C:143-169): g[0] = Gamma(beta), then
+ * Gamma(alpha k + beta) while k < maxIterMittagLeffler and the last value is
+ * below 1e100; returns the number of series terms available (g holds one
+ * more value) */
+static int ml_table(const rt_model_params *mp, double *g) {
+    g[0] = tgamma(mp->beta);
+    int k = 0;
+    while (k < mp->maxIterMittagLeffler && g[k] < 1e+100) {
+        g[k + 1] = tgamma(mp->alpha * k + mp->beta);
+        ++k;
+    }
+    return k;
+}
+/* E_{alpha,beta}(z) summed term by term (PTTLog.C:205-222) */
+static double ml_sum(const rt_model_params *mp, const double *g, int K, double z) {
+    double sum = 0.0, sumOld = 0.0, err = 1.0;
+    int k = 0;
+    while (k < K && err > mp->rTolMittagLeffler) {
+        double t = pow(z, (double)k) / g[k + 1];
+        sumOld = sum;
+        sum += t;
+        err = fabs((sumOld - sum) / (sumOld + 1e-12));
+        ++k;
+    }
+    return sum;
+}
+
 /* XPomPom: f of the pre-solve conformation (XPomPomLog.C:148-163) */
 static double xpp_f(const rt_model_params *mp, double trA, double trAA) {
     const double lam = sqrt(trA / 3.0), al = mp->alpha;
@@ -716,6 +743,9 @@ void or_theta_source(const rt_model_params *mp, int N, const double *L, const do
                      const double *eigVals, const double *theta, double *rhs, double *fP) {
     const double lambda = mp->lambda, etaP = mp->etaP;
     const double zeta = (mp->model == RT_MODEL_PTT_LOG) ? mp->zeta : 0.0;
+    const int gen = mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED;
+    double *mlg = gen ? DALLOC((size_t)mp->maxIterMittagLeffler + 1) : NULL;
+    const int mlK = gen ? ml_table(mp, mlg) : 0;
 
 #pragma omp parallel for num_threads(nthreads_) schedule(static)
     for (int c = 0; c < N; ++c) {
@@ -754,9 +784,11 @@ void or_theta_source(const rt_model_params *mp, int N, const double *L, const do
             for (int i = 0; i < 9; ++i) S.a[i] = (1.0 / lambda) * (T.a[i] - mp->alpha * ATT.a[i]);
         } else if (mp->model == RT_MODEL_PTT_LOG) {
             t3 T = t3_mul(t3_mul(R, invm1), Rt);
-            double fac = (mp->pttFunction == RT_PTT_EXP)
-                ? exp((mp->epsilon / (1.0 - zeta)) * (trA - 3.0))
-                : (1.0 + (mp->epsilon / (1.0 - zeta)) * (trA - 3.0));
+            const double z = (mp->epsilon / (1.0 - zeta)) * (trA - 3.0);
+            double fac;
+            if (mp->pttFunction == RT_PTT_EXP) fac = exp(z);
+            else if (gen) fac = mlg[0] * ml_sum(mp, mlg, mlK, z);   /* PTTLog.C:201-236 */
+            else fac = 1.0 + z;
             for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
         } else if (mp->model == RT_MODEL_ROLIEPOLY_LOG) {
             /* RoliePolyLog.C:140-179: -(1/lambdaD) A^-1 ((A - I) + M1 lambdaD (A + beta (trA/3)^delta (A - I))) */
@@ -810,6 +842,7 @@ void or_theta_source(const rt_model_params *mp, int N, const double *L, const do
         for (int i = 0; i < 9; ++i) Tsum.a[i] = OT.a[i] - TO.a[i] + 2.0 * B.a[i] + S.a[i];
         t3_symm(Tsum, rhs + 6 * (size_t)c);
     }
+    free(mlg);
 }
 
 /* tau of n cells from the post-solve eigen-decomposition (AoS) */

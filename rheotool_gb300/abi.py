@@ -18,7 +18,7 @@ RT_OK, RT_EINVAL, RT_ENOCONV, RT_ENAN, RT_ETIMEOUT, RT_EOOM, RT_ECUDA, RT_ENOTRE
 RT_BC_FIXED, RT_BC_ZEROGRAD, RT_BC_LINEXTRAP = 0, 1, 2
 (RT_MODEL_OLDROYDB_LOG, RT_MODEL_GIESEKUS_LOG, RT_MODEL_PTT_LOG, RT_MODEL_FENEP_LOG, RT_MODEL_FENECR_LOG,
  RT_MODEL_ROLIEPOLY_LOG, RT_MODEL_XPOMPOM_LOG, RT_MODEL_WHITEMETZNERCY_LOG) = 0, 1, 2, 3, 4, 5, 6, 7
-RT_PTT_LINEAR, RT_PTT_EXP = 0, 1
+RT_PTT_LINEAR, RT_PTT_EXP, RT_PTT_GENERALIZED = 0, 1, 2
 RT_STAB_NONE, RT_STAB_BSD, RT_STAB_COUPLING = 0, 1, 2
 RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB = 0, 1
 RT_PRECOND_NONE, RT_PRECOND_DIC, RT_PRECOND_DILU, RT_PRECOND_DIAGONAL = 0, 1, 2, 3
@@ -83,6 +83,7 @@ class rt_model_params(C.Structure):
         ("alpha", C.c_double), ("epsilon", C.c_double), ("zeta", C.c_double), ("L2", C.c_double),
         ("lambdaR", C.c_double), ("beta", C.c_double), ("delta", C.c_double), ("chiMax", C.c_double),
         ("lambdaS", C.c_double), ("q", C.c_double), ("n", C.c_double), ("K", C.c_double), ("a", C.c_double),
+        ("rTolMittagLeffler", C.c_double), ("maxIterMittagLeffler", C.c_int32), ("pad2_", C.c_int32),
     ]
 
 

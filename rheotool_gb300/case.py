@@ -5,7 +5,8 @@ The keys mirror rheoTool's dictionaries one to one:
 ``constant/constitutiveProperties`` (``type``, ``rho``, ``etaS``, ``etaP``,
 ``lambda``, ``alpha``, ``epsilon``, ``zeta``, ``L2``, ``lambdaR``/``lambdaD``,
 ``beta``, ``delta``, ``chiMax`` (Rolie-Poly), ``lambdaS``/``lambdaB``, ``q``,
-``n`` (XPomPom), ``n``/``m``, ``K``/``L``, ``a``/``b`` (WhiteMetznerCY), ``stabilization``,
+``n`` (XPomPom), ``n``/``m``, ``K``/``L``, ``a``/``b`` (WhiteMetznerCY),
+``rTolMittagLeffler``, ``maxIterMittagLeffler`` (generalized PTT), ``stabilization``,
 ``destructionFunctionType``; read in e.g. ``GiesekusLog.C:93-120`` and
 ``constitutiveEq::checkForStab``), ``system/fvSolution`` (``solver``,
 ``preconditioner``, ``tolerance``, ``relTol``, ``minIter``, ``maxIter``,
@@ -65,6 +66,8 @@ class Model:
     n: float = 0.0            # XPomPomLog stretch exponent, WhiteMetznerCYLog power index
     K: float = 0.0            # WhiteMetznerCYLog (the log form has L = K, b = a, m = n)
     a: float = 1.0
+    rTolMittagLeffler: float = 1e-12   # PTTLog generalized (its alpha and beta are alpha, beta)
+    maxIterMittagLeffler: int = 200
     stabilization: str = "coupling"
     destructionFunctionType: str = "linear"
 
@@ -72,14 +75,16 @@ class Model:
         if self.type not in abi.MODEL_NAMES:
             raise ValueError(f"Unknown constitutiveEq type {self.type}; valid: "
                              f"{sorted(abi.MODEL_NAMES)}")
-        if self.type == "PTTLog" and self.destructionFunctionType not in ("linear", "exponential"):
-            raise ValueError(f"PTTLog destructionFunctionType {self.destructionFunctionType}: implemented are "
-                             "linear and exponential")
-        ptt = abi.RT_PTT_EXP if self.destructionFunctionType == "exponential" else abi.RT_PTT_LINEAR
+        ptts = {"linear": abi.RT_PTT_LINEAR, "exponential": abi.RT_PTT_EXP, "generalized": abi.RT_PTT_GENERALIZED}
+        if self.type == "PTTLog" and self.destructionFunctionType not in ptts:
+            raise ValueError(f"PTTLog destructionFunctionType {self.destructionFunctionType}; valid: "
+                             f"{sorted(ptts)}")
+        ptt = ptts.get(self.destructionFunctionType, abi.RT_PTT_LINEAR)
         return abi.rt_model_params(abi.MODEL_NAMES[self.type], ptt, STABS[self.stabilization], 0,
                                    self.rho, self.etaS, self.etaP, self.lambda_, self.alpha,
                                    self.epsilon, self.zeta, self.L2, self.lambdaR, self.beta,
-                                   self.delta, self.chiMax, self.lambdaS, self.q, self.n, self.K, self.a)
+                                   self.delta, self.chiMax, self.lambdaS, self.q, self.n, self.K, self.a,
+                                   self.rTolMittagLeffler, int(self.maxIterMittagLeffler), 0)
 
 
 Value = Union[float, Tuple[float, ...], Callable[[np.ndarray], np.ndarray]]

@@ -104,10 +104,10 @@ __global__ void k_theta_rhs(int N, rt_model_params mp, const int *__restrict__ c
                             const rt_model_params *__restrict__ cp, const double *__restrict__ L,
                             const double *__restrict__ Rv, const double *__restrict__ evv,
                             const double *__restrict__ theta, double *__restrict__ rhs,
-                            double *__restrict__ fP) {
+                            double *__restrict__ fP, const double *__restrict__ mlg, int mlK) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
-    theta_rhs_cell(c, N, caseOf ? cp[caseOf[c]] : mp, L, Rv, evv, theta, rhs, fP);
+    theta_rhs_cell(c, N, caseOf ? cp[caseOf[c]] : mp, L, Rv, evv, theta, rhs, fP, mlg, mlK);
 }
 
 // theta matrix: diag = rDeltaT V + diagC; source = rDeltaT theta0 V + srcC + V rhs;
@@ -209,9 +209,12 @@ __device__ __forceinline__ bool mix_fp32_ok(double m0, double m1, double m2) {
 }
 
 // models whose cell algebra has no FP32 form here (Rolie-Poly, XPomPom,
-// WhiteMetznerCY): the mixed kernels run their FP64 code for every cell
-__device__ __forceinline__ bool mixed_fp64_model(int model) {
-    return model == RT_MODEL_ROLIEPOLY_LOG || model == RT_MODEL_XPOMPOM_LOG || model == RT_MODEL_WHITEMETZNERCY_LOG;
+// WhiteMetznerCY, the generalized PTT function): the mixed kernels run their
+// FP64 code for every cell
+__device__ __forceinline__ bool mixed_fp64_model(const rt_model_params &mp) {
+    return mp.model == RT_MODEL_ROLIEPOLY_LOG || mp.model == RT_MODEL_XPOMPOM_LOG ||
+           mp.model == RT_MODEL_WHITEMETZNERCY_LOG ||
+           (mp.model == RT_MODEL_PTT_LOG && mp.pttFunction == RT_PTT_GENERALIZED);
 }
 
 __global__ void k_eig_mixed(int n, const double *__restrict__ theta, double *__restrict__ ev,
@@ -243,13 +246,13 @@ __global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restr
                                   const rt_model_params *__restrict__ cp, const double *__restrict__ L,
                                   const double *__restrict__ Rv, const double *__restrict__ evv,
                                   const double *__restrict__ theta, double *__restrict__ rhs,
-                                  double *__restrict__ fP) {
+                                  double *__restrict__ fP, const double *__restrict__ mlg, int mlK) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
     const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    if (mixed_fp64_model(mp.model) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
-        theta_rhs_cell(c, N, mp, L, Rv, evv, theta, rhs, fP);
+    if (mixed_fp64_model(mp) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
+        theta_rhs_cell(c, N, mp, L, Rv, evv, theta, rhs, fP, mlg, mlK);
         return;
     }
     const float lambdaInv = (float)(1.0 / mp.lambda);
@@ -343,7 +346,7 @@ __global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ 
     if (c >= N) return;
     const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
-    if (mixed_fp64_model(mp.model) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
+    if (mixed_fp64_model(mp) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         tau_cell(c, N, mp, Rv, evv, fP, tau);
         return;
     }
@@ -455,10 +458,11 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
         ProfScope ps(ctx, "theta_rhs", (double)N * (72.0 + 72.0 + 24.0 + 48.0 + 48.0));
         if (cs.ctl.precision == RT_PREC_MIXED && (ctx->mixedParts & 2))
             k_theta_rhs_mixed<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, G, cs.eigVecs.p,
-                                                              cs.eigVals.p, cs.theta.p, rhs, fP);
+                                                              cs.eigVals.p, cs.theta.p, rhs, fP, cs.mlGamma.p,
+                                                              cs.mlK);
         else
             k_theta_rhs<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, G, cs.eigVecs.p,
-                                                        cs.eigVals.p, cs.theta.p, rhs, fP);
+                                                        cs.eigVals.p, cs.theta.p, rhs, fP, cs.mlGamma.p, cs.mlK);
         RT_CHECK_LAUNCH();
     }
     RT_CUDA(cudaMemcpyAsync(theta0, thetaOld ? thetaOld : cs.theta.p, sizeof(double) * 6 * N,

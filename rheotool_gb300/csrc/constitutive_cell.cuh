@@ -10,6 +10,7 @@
 
 #include <cmath>
 #include <cstddef>
+#include <vector>
 
 #include "../../include/rheogpu.h"
 
@@ -75,6 +76,34 @@ RT_HDI double roliepoly_m1(const rt_model_params &mp, double trA) {
     return M1;
 }
 
+// Generalized PTT (PTTLog.C:143-169): Gamma(beta) first, then
+// Gamma(alpha k + beta) for k = 0, 1, ... while fewer than maxIterMittagLeffler
+// and the last below 1e100.  Host only: computed once per case setup.
+inline std::vector<double> ml_gamma_table(const rt_model_params &mp) {
+    std::vector<double> g{std::tgamma(mp.beta)};
+    int k = 0;
+    while (k < mp.maxIterMittagLeffler && g.back() < 1e+100) {
+        g.push_back(std::tgamma(mp.alpha * k + mp.beta));
+        ++k;
+    }
+    return g;
+}
+
+// E_{alpha,beta}(z) = sum_k z^k / Gamma(alpha k + beta), summed term by term
+// until the relative change of the sum is at most rTolMittagLeffler or mlK
+// terms are taken (PTTLog.C:205-222); g is ml_gamma_table's table, mlK its
+// size less one
+RT_HDI double mittag_leffler(const rt_model_params &mp, const double *__restrict__ g, int mlK, double z) {
+    double sum = 0.0, sumOld = 0.0, err = 1.0;
+    for (int k = 0; k < mlK && err > mp.rTolMittagLeffler; ++k) {
+        const double t = pow(z, (double)k) / g[k + 1];
+        sumOld = sum;
+        sum += t;
+        err = fabs((sumOld - sum) / (sumOld + 1e-12));
+    }
+    return sum;
+}
+
 // XPomPom: f of the pre-solve conformation (XPomPomLog.C:148-163); the
 // backbone stretch is sqrt(tr A / 3)
 RT_HDI double xpompom_f(const rt_model_params &mp, double trA, double trAA) {
@@ -102,10 +131,12 @@ RT_HDI double whitemetznercy_factor(const rt_model_params &mp, const double L[9]
 // ---------------------------------------------------------------------------
 // theta source: rhs = symm(Omega theta - theta Omega + 2B + S_model)
 // ---------------------------------------------------------------------------
-RT_HD void theta_rhs_cell(int c, int N, const rt_model_params &mp,
-                                               const double *__restrict__ L, const double *__restrict__ Rv,
-                                               const double *__restrict__ evv, const double *__restrict__ theta,
-                                               double *__restrict__ rhs, double *__restrict__ fP) {
+// mlg: the Gamma-function table of the generalized PTT function (mlK + 1
+// values, ml_gamma_table), null for the other models
+RT_HD void theta_rhs_cell(int c, int N, const rt_model_params &mp, const double *__restrict__ L,
+                          const double *__restrict__ Rv, const double *__restrict__ evv,
+                          const double *__restrict__ theta, double *__restrict__ rhs, double *__restrict__ fP,
+                          const double *__restrict__ mlg = nullptr, int mlK = 0) {
     const double lambda = mp.lambda;
     const double zeta = (mp.model == RT_MODEL_PTT_LOG) ? mp.zeta : 0.0;
     T3 Lc = load9(L, N, c), R = load9(Rv, N, c);
@@ -145,8 +176,11 @@ RT_HD void theta_rhs_cell(int c, int N, const rt_model_params &mp,
         T3 A = mul(mul(R, dg(e0, e1, e2)), Rt);
         double trA = A.a[0] + A.a[4] + A.a[8];
         T3 T = mul(mul(R, invm1), Rt);
-        double fac = (mp.pttFunction == RT_PTT_EXP) ? exp((mp.epsilon / (1.0 - zeta)) * (trA - 3.0))
-                                                    : (1.0 + (mp.epsilon / (1.0 - zeta)) * (trA - 3.0));
+        const double z = (mp.epsilon / (1.0 - zeta)) * (trA - 3.0);
+        double fac;
+        if (mp.pttFunction == RT_PTT_EXP) fac = exp(z);
+        else if (mp.pttFunction == RT_PTT_GENERALIZED) fac = (mlK > 0) ? mlg[0] * mittag_leffler(mp, mlg, mlK, z) : 0.0;
+        else fac = 1.0 + z;
 #pragma unroll
         for (int i = 0; i < 9; ++i) S.a[i] = ((1.0 / lambda) * T.a[i]) * fac;
     } else if (mp.model == RT_MODEL_ROLIEPOLY_LOG) {

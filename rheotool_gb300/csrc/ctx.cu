@@ -4,6 +4,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "constitutive_cell.cuh"
 #include "rt_internal.h"
 #include "sweep.h"
 
@@ -424,6 +425,14 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
                    "XPomPom needs lambdaS > 0 and q > 0");
         RT_REQUIRE(mp->model != RT_MODEL_WHITEMETZNERCY_LOG || mp->a > 0, RT_EINVAL,
                    "WhiteMetznerCY needs a > 0");
+        const bool pttGen = mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED;
+        RT_REQUIRE(mp->model != RT_MODEL_PTT_LOG || (mp->pttFunction >= RT_PTT_LINEAR &&
+                                                     mp->pttFunction <= RT_PTT_GENERALIZED),
+                   RT_EINVAL, "unknown PTT destruction function");
+        // PTTLog.C:147-152
+        RT_REQUIRE(!pttGen || (mp->alpha > 0 && mp->beta > 0), RT_EINVAL,
+                   "Both alpha and beta should be positive values for the Mittag-Leffler function to converge.");
+        RT_REQUIRE(!pttGen || mp->maxIterMittagLeffler >= 1, RT_EINVAL, "maxIterMittagLeffler must be positive");
         RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
         RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
         RT_REQUIRE(mp->model != RT_MODEL_ROLIEPOLY_LOG || mp->lambdaR > 0, RT_EINVAL,
@@ -438,6 +447,15 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
         RT_REQUIRE(ctl->pRefCell >= 0 && ctl->pRefCell < m.N, RT_EINVAL, "pRefCell out of range");
         c.mp = *mp;
         c.ctl = *ctl;
+        if (pttGen) {
+            std::vector<double> g = ml_gamma_table(*mp);
+            c.mlK = (int)g.size() - 1;
+            RT_REQUIRE(c.mlK >= 1, RT_EINVAL, "Gamma(beta) overflows: no Mittag-Leffler term");
+            upload_vec(ctx, g, c.mlGamma);
+        } else {
+            c.mlGamma.release();
+            c.mlK = 0;
+        }
         const int P = m.nPatches, NB = m.NB, N = m.N;
         c.kindU.assign(bc->U, bc->U + P);
         c.kindP.assign(bc->p, bc->p + P);
@@ -793,6 +811,10 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model
                            "case " + std::to_string(c) + ": XPomPom needs lambdaS > 0 and q > 0");
                 RT_REQUIRE(mp.model != RT_MODEL_WHITEMETZNERCY_LOG || mp.a > 0, RT_EINVAL,
                            "case " + std::to_string(c) + ": WhiteMetznerCY needs a > 0");
+                RT_REQUIRE(mp.model != RT_MODEL_PTT_LOG || mp.pttFunction == RT_PTT_LINEAR ||
+                               mp.pttFunction == RT_PTT_EXP,
+                           RT_EINVAL, "case " + std::to_string(c) + ": the batched form runs the linear and "
+                                      "exponential PTT functions");
                 RT_REQUIRE(mp.lambda > 0 && mp.rho > 0, RT_EINVAL,
                            "case " + std::to_string(c) + ": lambda and rho must be positive");
                 RT_REQUIRE((mp.model != RT_MODEL_FENEP_LOG && mp.model != RT_MODEL_FENECR_LOG) || mp.L2 > 3.0, RT_EINVAL,

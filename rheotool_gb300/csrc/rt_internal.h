@@ -257,6 +257,9 @@ struct DevCase {
     DBuf<double> UbFixed, pbFixed, thetabFixed, taubFixed;
     // state (SoA)
     DBuf<double> U, Ub, p, pb, phi, phib, theta, thetab, tau, taub, eigVals, eigVecs;
+    // generalized PTT: Gamma(beta), Gamma(alpha k + beta) for k < mlK (else empty, mlK = 0)
+    DBuf<double> mlGamma;
+    int mlK = 0;
 };
 
 // scratch arrays of the step, allocated once per mesh

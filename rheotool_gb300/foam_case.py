@@ -145,7 +145,7 @@ class LoadedCase:
 # XPomPomLog.C:114-122, WhiteMetznerCYLog.C:124-133)
 MODEL_KEYS = {
     "GiesekusLog": ("alpha",),
-    "PTTLog": ("epsilon", "zeta", "destructionFunctionType", "alpha", "beta"),
+    "PTTLog": ("epsilon", "zeta", "destructionFunctionType"),
     "FENE-PLog": ("L2",),
     "FENE-CRLog": ("L2",),
     "Rolie-PolyLog": ("lambdaR", "beta", "delta", "chiMax"),
@@ -250,10 +250,20 @@ def load_case(case_dir: str, substitute: bool = False,
             raise CaseError(f"{th} type {t.get('type')}: only the Constant thermoFunction is implemented")
     if "destructionFunctionType" in par:
         mkw["destructionFunctionType"] = par["destructionFunctionType"]
-        if typ == "PTTLog" and par["destructionFunctionType"] not in ("linear", "exponential"):
-            # the generalized (Mittag-Leffler) function of PTTLog.C:198-236 is not built
-            raise CaseError(f"PTTLog destructionFunctionType {par['destructionFunctionType']}: implemented are "
-                            "linear and exponential")
+        dft = par["destructionFunctionType"]
+        if typ == "PTTLog" and dft not in ("linear", "exponential", "generalized"):
+            raise CaseError(f"PTTLog destructionFunctionType {dft}; valid: exponential, generalized, linear")
+        if typ == "PTTLog" and dft == "generalized":
+            # PTTLog.C:143-152: the Mittag-Leffler alpha and beta, both positive
+            for key in ("alpha", "beta"):
+                if key not in par:
+                    raise CaseError(f"keyword {key} is undefined in constitutiveProperties")
+            if scalar(par["alpha"]) <= 0 or scalar(par["beta"]) <= 0:
+                raise CaseError("Both alpha and beta should be positive values for the Mittag-Leffler function "
+                                "to converge.")
+            for key, cast in (("rTolMittagLeffler", float), ("maxIterMittagLeffler", int)):
+                if key in par:
+                    mkw[key] = cast(scalar(par[key]))
     model = Model(**mkw)
 
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))

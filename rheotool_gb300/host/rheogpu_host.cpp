@@ -307,13 +307,21 @@ std::unique_ptr<ConstitutiveEq> ConstitutiveEq::New(const std::string &name, con
     if (mp.model == RT_MODEL_PTT_LOG) {
         mp.epsilon = d.lookupScalar("epsilon");
         mp.zeta = d.lookupScalar("zeta");
-        // PTTLog.C reads the generalized function's alpha and beta whatever the type
-        mp.alpha = d.lookupScalar("alpha");
-        mp.beta = d.lookupScalar("beta");
+        mp.rTolMittagLeffler = d.lookupOrDefault("rTolMittagLeffler", 1e-12);
+        mp.maxIterMittagLeffler = d.lookupOrDefault("maxIterMittagLeffler", 200);
         const std::string f = d.lookup("destructionFunctionType");
         if (f == "linear") mp.pttFunction = RT_PTT_LINEAR;
         else if (f == "exponential") mp.pttFunction = RT_PTT_EXP;
-        else throw FatalError(valid_list("destructionFunctionType", f, {"linear", "exponential"}));
+        else if (f == "generalized") mp.pttFunction = RT_PTT_GENERALIZED;
+        else throw FatalError(valid_list("destructionFunctionType", f, {"exponential", "generalized", "linear"}));
+        if (mp.pttFunction == RT_PTT_GENERALIZED) {
+            // PTTLog.C:143-152
+            mp.alpha = d.lookupScalar("alpha");
+            mp.beta = d.lookupScalar("beta");
+            if (mp.alpha <= 0 || mp.beta <= 0)
+                throw FatalError("Both alpha and beta should be positive values for the Mittag-Leffler function "
+                                 "to converge.");
+        }
     }
     if (mp.model == RT_MODEL_FENEP_LOG || mp.model == RT_MODEL_FENECR_LOG) mp.L2 = d.lookupScalar("L2");
     // constitutiveEq::checkForStab

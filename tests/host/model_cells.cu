@@ -8,7 +8,12 @@
 
 extern "C" void mc_theta_source(const rt_model_params *mp, int n, const double *L, const double *eigVecs,
                                 const double *eigVals, const double *theta, double *rhs, double *fP) {
-    for (int c = 0; c < n; ++c) rt::theta_rhs_cell(c, n, *mp, L, eigVecs, eigVals, theta, rhs, fP);
+    // the generalized PTT function's Gamma table, as the case setup makes it
+    std::vector<double> g;
+    if (mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED) g = rt::ml_gamma_table(*mp);
+    const int K = g.empty() ? 0 : (int)g.size() - 1;
+    for (int c = 0; c < n; ++c)
+        rt::theta_rhs_cell(c, n, *mp, L, eigVecs, eigVals, theta, rhs, fP, g.empty() ? nullptr : g.data(), K);
 }
 
 extern "C" void mc_tau(const rt_model_params *mp, int n, const double *eigVecs, const double *eigVals,

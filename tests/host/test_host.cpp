@@ -66,12 +66,20 @@ static void cpu_checks() {
     CHECK(m.find("Oldroyd-BLog") != std::string::npos && m.find("FENE-PLog") != std::string::npos);
 
     Dictionary ptt = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
-                                       " alpha 1; beta 1; destructionFunctionType exponential; stabilization BSD;");
+                                       " destructionFunctionType exponential; stabilization BSD;");
     auto pt = ConstitutiveEq::New("p", ptt);
     CHECK(pt->params().pttFunction == RT_PTT_EXP && pt->params().stabilization == RT_STAB_BSD);
     Dictionary pttg = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
-                                        " alpha 1; beta 1; destructionFunctionType generalized; stabilization BSD;");
-    CHECK(throws([&] { ConstitutiveEq::New("p", pttg); }).find("Unknown destructionFunctionType generalized") !=
+                                        " alpha 0.8; beta 1.2; destructionFunctionType generalized; stabilization BSD;");
+    auto pg = ConstitutiveEq::New("p", pttg);
+    CHECK(pg->params().pttFunction == RT_PTT_GENERALIZED && pg->params().alpha == 0.8 && pg->params().beta == 1.2);
+    CHECK(pg->params().maxIterMittagLeffler == 200 && pg->params().rTolMittagLeffler == 1e-12);
+    Dictionary pttb = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
+                                        " alpha 0.8; beta 0; destructionFunctionType generalized; stabilization BSD;");
+    CHECK(throws([&] { ConstitutiveEq::New("p", pttb); }).find("should be positive") != std::string::npos);
+    Dictionary pttu = Dictionary::parse("type PTTLog; rho 1; etaS 1; etaP 1; lambda 1; epsilon 0.25; zeta 0;"
+                                        " destructionFunctionType quadratic; stabilization BSD;");
+    CHECK(throws([&] { ConstitutiveEq::New("p", pttu); }).find("Unknown destructionFunctionType quadratic") !=
           std::string::npos);
 
     Dictionary xpp = Dictionary::parse("type XPomPomLog; rho 1; etaS 0.1; etaP 0.9; lambdaB 1.0; lambdaS 0.25;"

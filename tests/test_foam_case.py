@@ -143,8 +143,9 @@ def _props(root, body):
 def test_model_keywords_as_the_reference_reads_them(tmp_path):
     """XPomPomLog and WhiteMetznerCYLog read their constructors' keywords
     (lambdaB for lambda; WhiteMetznerCYLog only with m = n, K = L, a = b);
-    a missing keyword, a temperature function other than Constant and the
-    generalized PTT function are refused as the reference would abort."""
+    a missing keyword, a temperature function other than Constant, a
+    generalized PTT function without positive alpha and beta and an unknown
+    destruction function are refused as the reference would abort."""
     root = _cavity_dir(str(tmp_path / "m"))
     base = "rho 1; etaS 0.1; etaP 0.9; stabilization coupling;"
     _props(root, "type XPomPomLog; " + base + " lambdaB 0.5; lambdaS 0.2; alpha 0.15; q 2; n 0;")
@@ -163,7 +164,14 @@ def test_model_keywords_as_the_reference_reads_them(tmp_path):
            " thermoLambda { type Arrhenius; }")
     with pytest.raises(CaseError, match="thermoLambda type Arrhenius"):
         load_case(root)
-    _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; alpha 1; beta 1;"
+    _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; alpha 0.8; beta 1.2;"
+           " destructionFunctionType generalized; maxIterMittagLeffler 150;")
+    m = load_case(root).case.model
+    assert (m.destructionFunctionType, m.alpha, m.beta, m.maxIterMittagLeffler) == ("generalized", 0.8, 1.2, 150)
+    _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; alpha 0.8; beta 0;"
            " destructionFunctionType generalized;")
-    with pytest.raises(CaseError, match="generalized"):
+    with pytest.raises(CaseError, match="should be positive"):
+        load_case(root)
+    _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; destructionFunctionType quadratic;")
+    with pytest.raises(CaseError, match="quadratic"):
         load_case(root)

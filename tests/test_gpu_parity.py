@@ -251,10 +251,25 @@ def test_residual_matches_oracle(ctx):
 
 
 MODELS = [("Oldroyd-BLog", {}), ("GiesekusLog", {"alpha": 0.1}),
-          ("PTTLog", {"epsilon": 0.25}), ("FENE-PLog", {"L2": 100.0}), ("FENE-CRLog", {"L2": 20.0}),
+          ("PTTLog", {"epsilon": 0.25}),
+          ("PTTLog", {"epsilon": 0.25, "destructionFunctionType": "generalized", "alpha": 0.8, "beta": 1.2}),
+          ("FENE-PLog", {"L2": 100.0}), ("FENE-CRLog", {"L2": 20.0}),
           ("Rolie-PolyLog", {"lambdaR": 0.2, "chiMax": 5.0}),
           ("XPomPomLog", {"lambdaS": 0.2, "q": 2.0, "alpha": 0.15}),
           ("WhiteMetznerCYLog", {"K": 1.0, "a": 2.0})]
+
+
+def model_cavity(model, kw):
+    """The 16x16 cavity with the model's keywords; beta (Rolie-Poly, the
+    generalized PTT function) and n (XPomPom, WhiteMetznerCY) are set on the
+    model after the case is built, since cavity_case's own beta and n are the
+    viscosity ratio and the mesh size."""
+    kw = dict(kw)
+    late = {k: kw.pop(k) for k in ("beta", "n") if k in kw}
+    case = cavity_case(16, model=model, **kw)
+    for k, v in late.items():
+        setattr(case.model, k, v)
+    return case
 
 
 def flow_state(case, steps=3):
@@ -269,7 +284,7 @@ def flow_state(case, steps=3):
 @pytest.mark.parametrize("model,kw", MODELS)
 def test_constitutive_correct_matches_oracle(ctx, model, kw):
     from oracle.pyoracle import Oracle
-    case = cavity_case(16, model=model, **kw)
+    case = model_cavity(model, kw)
     f0 = flow_state(case)
     ctx.setup_case(case, f0)
     perf_g = ctx.constitutive_correct()
@@ -301,7 +316,7 @@ def test_constitutive_correct_with_imposed_gradU(ctx):
 
 @pytest.mark.parametrize("model,kw", MODELS)
 def test_step_cavity_matches_oracle(ctx, model, kw):
-    case = cavity_case(16, model=model, **kw)
+    case = model_cavity(model, kw)
     assert_step_parity(ctx, case, 5)
 
 

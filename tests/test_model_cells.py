@@ -32,6 +32,9 @@ MODELS = [
     ("GiesekusLog", {"alpha": 0.3}),
     ("PTTLog", {"epsilon": 0.25, "zeta": 0.1}),
     ("PTTLog", {"epsilon": 0.25, "destructionFunctionType": "exponential"}),
+    ("PTTLog", {"epsilon": 0.25, "zeta": 0.1, "destructionFunctionType": "generalized", "alpha": 0.8, "beta": 1.2}),
+    ("PTTLog", {"epsilon": 0.5, "destructionFunctionType": "generalized", "alpha": 1.5, "beta": 0.7,
+                "maxIterMittagLeffler": 12}),
     ("FENE-PLog", {"L2": 100.0}),
     ("FENE-CRLog", {"L2": 20.0}),
     ("Rolie-PolyLog", {"lambdaR": 0.2, "beta": 0.5, "delta": -0.5}),
@@ -94,6 +97,18 @@ def test_cell_algebra_matches_oracle(cells, model, kw):
     tau_s = np.zeros((6, n))
     cells.mc_tau(C.byref(mp), n, abi.dptr(Rs), abi.dptr(es), abi.dptr(fP_o), abi.dptr(tau_s))
     assert np.max(np.abs(tau_s.T - tau_o)) <= 1e-14 * np.max(np.abs(tau_o))
+
+
+def test_generalized_ptt_with_unit_alpha_beta_is_the_exponential(cells):
+    """Gamma(1) E_{1,1}(z) = exp(z): the generalized function with alpha =
+    beta = 1 gives the exponential PTT source to the series tolerance."""
+    L, eigVecs, eigVals, theta = random_cells(256, 11)
+    kw = dict(rho=1.0, etaS=0.3, etaP=0.7, lambda_=0.8, epsilon=0.3)
+    gen = Model("PTTLog", destructionFunctionType="generalized", alpha=1.0, beta=1.0, **kw).to_c()
+    exp_ = Model("PTTLog", destructionFunctionType="exponential", **kw).to_c()
+    rg, _ = pyoracle.theta_source(gen, L, eigVecs, eigVals, theta)
+    re, _ = pyoracle.theta_source(exp_, L, eigVecs, eigVals, theta)
+    assert np.max(np.abs(rg - re)) <= 1e-11 * np.max(np.abs(re))
 
 
 def test_whitemetznercy_factor_is_the_carreau_yasuda_law(cells):

@@ -197,7 +197,7 @@ def rp_chi(trA, chiMax):
 
 
 def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=1.0, beta=0.0, delta=-0.5,
-                        chiMax=0.0, lambdaS=1.0, q=1.0, n=0.0, K=0.0, a=1.0):
+                        chiMax=0.0, lambdaS=1.0, q=1.0, n=0.0, K=0.0, a=1.0, mlab=None):
     """Steady simple shear of the conformation-tensor form, integrated with
     scipy (an independent formulation of the same model)."""
     from scipy.integrate import solve_ivp
@@ -211,6 +211,12 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=
             g = A - I
         elif model == "GiesekusLog":
             g = (A - I) + alpha * (A - I) @ (A - I)
+        elif model == "PTTLog" and mlab is not None:
+            # Gamma(beta) E_{alpha,beta}(z) by its series, with scipy's Gamma
+            from scipy.special import gamma
+            z = eps * (np.trace(A) - 3.0)
+            k = np.arange(60)
+            g = gamma(mlab[1]) * np.sum(z ** k / gamma(mlab[0] * k + mlab[1])) * (A - I)
         elif model == "PTTLog":
             g = (1.0 + eps * (np.trace(A) - 3.0)) * (A - I)
         elif model == "FENE-CRLog":
@@ -251,6 +257,8 @@ def conformation_steady(model, lam, rate, alpha=0.0, eps=0.0, L2=100.0, lambdaR=
     ("Oldroyd-BLog", {}, {}),
     ("GiesekusLog", {"alpha": 0.3}, {"alpha": 0.3}),
     ("PTTLog", {"epsilon": 0.25}, {"eps": 0.25}),
+    ("PTTLog", {"epsilon": 0.25, "destructionFunctionType": "generalized", "alpha": 0.8, "beta": 1.2},
+     {"eps": 0.25, "mlab": (0.8, 1.2)}),
     ("FENE-PLog", {"L2": 100.0}, {"L2": 100.0}),
     ("FENE-CRLog", {"L2": 20.0}, {"L2": 20.0}),
     ("Rolie-PolyLog", {"lambdaR": 0.2, "beta": 0.5, "delta": -0.5},
