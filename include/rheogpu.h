@@ -15,7 +15,14 @@
  *                            Oldroyd-B/Oldroyd-BLog/Oldroyd_BLog.C:127-179,
  *                            Giesekus/GiesekusLog/GiesekusLog.C:128-176,
  *                            PTT/PTTLog/PTTLog.C:176-268,
- *                            FENE-P/FENE-PLog/FENE_PLog.C:128-182
+ *                            FENE-P/FENE-PLog/FENE_PLog.C:128-182,
+ *                            FENE-CR/FENE-CRLog/FENE_CRLog.C:127-180,
+ *                            Rolie-Poly/Rolie-PolyLog/RoliePolyLog.C:125-203,
+ *                            XPomPom/XPomPomLog/XPomPomLog.C:133-198,
+ *                            WhiteMetznerCY/WhiteMetznerCYLog/
+ *                            WhiteMetznerCYLog.C:145-206
+ *   rt_constitutive_correct_iter  the same, called nInIter times in one time
+ *                            step (solvers/rheoFoam/rheoFoam.C:149-153)
  *   rt_ldu_solve             lduMatrix::solver::solve(psi, source, cmpt) of
  *                            OpenFOAM's PCG/DIC and PBiCGStab/DILU, reached
  *                            through sparseSolver<Type>::solve
@@ -291,6 +298,17 @@ rt_status rt_residual_noalloc(rt_ctx *ctx, const double *diag, const double *upp
  * thetaPerf gets 6 entries (components not solved have nIterations = -1). */
 rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU,
                                   rt_solver_perf *thetaPerf);
+
+/* constitutiveEq::correct() as rheoFoam's inner iterations call it
+ * (rheoFoam.C:149-153 with nInIter > 1): newTimeStep != 0 first keeps the
+ * current theta as the time step's old-time field, OpenFOAM's
+ * theta.oldTime() after the time increment; every call then solves fvm::ddt
+ * against that field, so nInIter calls in one step iterate the update rather
+ * than advance nInIter steps.  rt_constitutive_correct is the call with
+ * newTimeStep = 1.  A call with newTimeStep = 0 before any with 1 since the
+ * case setup returns RT_ENOTREADY. */
+rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t newTimeStep,
+                                       rt_solver_perf *thetaPerf);
 
 /* nSteps segregated rheoFoam time steps; perf (may be NULL) gets the last. */
 rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf);

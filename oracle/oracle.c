@@ -937,6 +937,19 @@ int or_constitutive_correct(const rt_mesh_desc *m, const rt_bc_desc *bc,
     return st;
 }
 
+/* the same with the theta equation's old-time field given (AoS 6 nCells):
+ * an inner iteration of a time step that started from thetaOld */
+int or_constitutive_correct_old(const rt_mesh_desc *m, const rt_bc_desc *bc,
+                                const rt_model_params *mp, const rt_case_ctl *ctl,
+                                or_state *s, const double *gradU, const double *thetaOld,
+                                rt_solver_perf *perf) {
+    or_case k;
+    case_init(&k, m, bc, mp, ctl, s);
+    int st = constitutive_correct(&k, gradU, perf, thetaOld);
+    case_free(&k);
+    return st;
+}
+
 /* ------------------------------------------------------------------------ */
 /* explicit divergences used by divTau                                        */
 /* ------------------------------------------------------------------------ */

@@ -55,6 +55,10 @@ def lib():
                                               P(abi.rt_model_params), P(abi.rt_case_ctl),
                                               P(or_state), _dp, P(abi.rt_solver_perf)]
         L.or_constitutive_correct.restype = C.c_int
+        L.or_constitutive_correct_old.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc),
+                                                  P(abi.rt_model_params), P(abi.rt_case_ctl),
+                                                  P(or_state), _dp, _dp, P(abi.rt_solver_perf)]
+        L.or_constitutive_correct_old.restype = C.c_int
         L.or_theta_source.argtypes = [P(abi.rt_model_params), C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.or_tau_cells.argtypes = [P(abi.rt_model_params), C.c_int, _dp, _dp, _dp, _dp]
         L.or_step.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params),
@@ -96,12 +100,21 @@ class Oracle:
             raise RuntimeError(f"oracle step failed: {abi.STATUS_NAMES.get(st, st)}")
         return perf
 
-    def constitutive_correct(self, gradU: np.ndarray = None):
+    def constitutive_correct(self, gradU: np.ndarray = None, thetaOld: np.ndarray = None):
+        """One correct(); thetaOld (nCells, 6): the old-time theta of the
+        theta equation (an inner iteration of a step that started there),
+        default the current theta."""
         perf = (abi.rt_solver_perf * 6)()
         g = None if gradU is None else np.ascontiguousarray(gradU, dtype=np.float64)
-        st = lib().or_constitutive_correct(C.byref(self.md), C.byref(self.bd), C.byref(self.mp),
-                                           C.byref(self.ctl), C.byref(_state(self.f)),
-                                           None if g is None else g.ctypes.data_as(_dp), perf)
+        gp = None if g is None else g.ctypes.data_as(_dp)
+        if thetaOld is None:
+            st = lib().or_constitutive_correct(C.byref(self.md), C.byref(self.bd), C.byref(self.mp),
+                                               C.byref(self.ctl), C.byref(_state(self.f)), gp, perf)
+        else:
+            t0 = np.ascontiguousarray(thetaOld, dtype=np.float64)
+            st = lib().or_constitutive_correct_old(C.byref(self.md), C.byref(self.bd), C.byref(self.mp),
+                                                   C.byref(self.ctl), C.byref(_state(self.f)), gp,
+                                                   t0.ctypes.data_as(_dp), perf)
         if st != 0:
             raise RuntimeError(f"oracle constitutive correct failed: {st}")
         return list(perf)

@@ -169,6 +169,7 @@ def load_library(path: str = LIBNAME):
         "rt_residual": ([vp, _dp, _dp, _dp, _dp, _dp, _dp], C.c_int32),
         "rt_residual_noalloc": ([vp, vp, vp, vp, vp, vp, _dp], C.c_int32),
         "rt_constitutive_correct": ([vp, _dp, P(rt_solver_perf)], C.c_int32),
+        "rt_constitutive_correct_iter": ([vp, _dp, C.c_int32, P(rt_solver_perf)], C.c_int32),
         "rt_step": ([vp, C.c_int32, P(rt_step_perf)], C.c_int32),
         "rt_op_grad": ([vp, _dp, _dp, _dp], C.c_int32),
         "rt_op_eig": ([vp, C.c_int32, _dp, _dp, _dp], C.c_int32),

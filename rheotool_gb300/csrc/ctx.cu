@@ -447,6 +447,7 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
         RT_REQUIRE(ctl->pRefCell >= 0 && ctl->pRefCell < m.N, RT_EINVAL, "pRefCell out of range");
         c.mp = *mp;
         c.ctl = *ctl;
+        c.thetaOldSaved = false;
         if (pttGen) {
             std::vector<double> g = ml_gamma_table(*mp);
             c.mlK = (int)g.size() - 1;
@@ -624,6 +625,29 @@ rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_pe
         DBuf<double> g;
         if (gradU) upload_soa(ctx, gradU, ctx->mesh.N, 9, g);
         rt_status st = constitutive_correct(ctx, gradU ? g.p : nullptr, thetaPerf);
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return st;
+    });
+}
+
+rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t newTimeStep,
+                                       rt_solver_perf *thetaPerf) {
+    return guarded(ctx, [&]() -> rt_status {
+        DevCase &c = ctx->cs;
+        RT_REQUIRE(c.ready, RT_ENOTREADY, "case not set up");
+        RT_REQUIRE(thetaPerf, RT_EINVAL, "null perf");
+        const size_t n6 = 6 * (size_t)ctx->mesh.N;
+        if (newTimeStep) {
+            c.thetaOld.alloc(n6);
+            RT_CUDA(cudaMemcpyAsync(c.thetaOld.p, c.theta.p, sizeof(double) * n6, cudaMemcpyDeviceToDevice,
+                                    ctx->stream));
+            c.thetaOldSaved = true;
+        }
+        RT_REQUIRE(c.thetaOldSaved && c.thetaOld.p && c.thetaOld.n == n6, RT_ENOTREADY,
+                   "no old-time theta: the first call of a time step needs newTimeStep = 1");
+        DBuf<double> g;
+        if (gradU) upload_soa(ctx, gradU, ctx->mesh.N, 9, g);
+        rt_status st = constitutive_correct(ctx, gradU ? g.p : nullptr, thetaPerf, c.thetaOld.p);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
         return st;
     });

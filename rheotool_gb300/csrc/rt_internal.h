@@ -257,6 +257,9 @@ struct DevCase {
     DBuf<double> UbFixed, pbFixed, thetabFixed, taubFixed;
     // state (SoA)
     DBuf<double> U, Ub, p, pb, phi, phib, theta, thetab, tau, taub, eigVals, eigVecs;
+    // the theta of the start of the time step, kept by rt_constitutive_correct_iter
+    DBuf<double> thetaOld;
+    bool thetaOldSaved = false;
     // generalized PTT: Gamma(beta), Gamma(alpha k + beta) for k < mlK (else empty, mlK = 0)
     DBuf<double> mlGamma;
     int mlK = 0;

@@ -166,6 +166,10 @@ public:
     // one constitutiveEq::correct() on the device-resident case of ctx
     // (set up with these params); gradU (9 nCells, AoS) may be null
     std::vector<SolverPerformance> correct(Context &ctx, const double *gradU = nullptr) const;
+    // the same as one of rheoFoam's nInIter calls in a time step: newTimeStep
+    // keeps the current theta as the step's old-time field, later calls of the
+    // step solve against it (rt_constitutive_correct_iter)
+    std::vector<SolverPerformance> correctIter(Context &ctx, bool newTimeStep, const double *gradU = nullptr) const;
     // tau (6 nCells AoS) and its boundary values (6 nBFaces, may be null)
     void tau(Context &ctx, double *internal, double *boundary = nullptr) const;
 

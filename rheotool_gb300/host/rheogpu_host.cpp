@@ -333,9 +333,8 @@ std::unique_ptr<ConstitutiveEq> ConstitutiveEq::New(const std::string &name, con
     return ce;
 }
 
-std::vector<SolverPerformance> ConstitutiveEq::correct(Context &ctx, const double *gradU) const {
-    rt_solver_perf perf[6];
-    ctx.check(rt_constitutive_correct(ctx.get(), gradU, perf), "constitutiveEq::correct (" + type_ + ")");
+namespace {
+std::vector<SolverPerformance> theta_performance(const rt_solver_perf perf[6]) {
     static const char *cmpt[6] = {"xx", "xy", "xz", "yy", "yz", "zz"};
     std::vector<SolverPerformance> out;
     for (int k = 0; k < 6; ++k) {
@@ -351,6 +350,20 @@ std::vector<SolverPerformance> ConstitutiveEq::correct(Context &ctx, const doubl
         out.push_back(p);
     }
     return out;
+}
+}  // namespace
+
+std::vector<SolverPerformance> ConstitutiveEq::correct(Context &ctx, const double *gradU) const {
+    rt_solver_perf perf[6];
+    ctx.check(rt_constitutive_correct(ctx.get(), gradU, perf), "constitutiveEq::correct (" + type_ + ")");
+    return theta_performance(perf);
+}
+
+std::vector<SolverPerformance> ConstitutiveEq::correctIter(Context &ctx, bool newTimeStep, const double *gradU) const {
+    rt_solver_perf perf[6];
+    ctx.check(rt_constitutive_correct_iter(ctx.get(), gradU, newTimeStep ? 1 : 0, perf),
+              "constitutiveEq::correct (" + type_ + ")");
+    return theta_performance(perf);
 }
 
 void ConstitutiveEq::tau(Context &ctx, double *internal, double *boundary) const {

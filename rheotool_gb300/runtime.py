@@ -146,10 +146,18 @@ class Context:
         self._check(self.lib.rt_step(self._ctx, int(n), C.byref(perf)), "rt_step")
         return perf
 
-    def constitutive_correct(self, gradU=None) -> List[abi.rt_solver_perf]:
+    def constitutive_correct(self, gradU=None, newTimeStep: Optional[bool] = None) -> List[abi.rt_solver_perf]:
+        """One constitutiveEq::correct().  newTimeStep None: a step of its own
+        (rt_constitutive_correct); True / False: the first / a further inner
+        iteration of a time step, solved against the theta kept by the first
+        (rt_constitutive_correct_iter)."""
         perf = (abi.rt_solver_perf * 6)()
         g = None if gradU is None else _c(gradU)
-        self._check(self.lib.rt_constitutive_correct(self._ctx, abi.optr(g), perf), "rt_constitutive_correct")
+        if newTimeStep is None:
+            self._check(self.lib.rt_constitutive_correct(self._ctx, abi.optr(g), perf), "rt_constitutive_correct")
+        else:
+            self._check(self.lib.rt_constitutive_correct_iter(self._ctx, abi.optr(g), int(bool(newTimeStep)), perf),
+                        "rt_constitutive_correct_iter")
         return list(perf)
 
     def ldu_solve(self, diag, upper, lower, source, psi, ctl) -> List[abi.rt_solver_perf]:

@@ -459,3 +459,31 @@ def test_step_inner_iterations(ctx):
     case = cavity_case(16, model="GiesekusLog", alpha=0.1, Wi=0.5, dt=5e-3)
     case.nInIter = 3
     assert_step_parity(ctx, case, 4)
+
+
+def test_constitutive_correct_inner_iterations(ctx):
+    """rt_constitutive_correct_iter: three correct() calls of one time step
+    solve fvm::ddt against the step's starting theta (OpenFOAM's
+    theta.oldTime()), as rheoFoam's nInIter loop calls constEq.correct();
+    the oracle does the same from the same fields."""
+    from oracle.pyoracle import Oracle
+    from rheotool_gb300.runtime import RheoGpuError
+    case = model_cavity("GiesekusLog", {"alpha": 0.1})
+    f0 = flow_state(case)
+    ctx.setup_case(case, f0)
+    with pytest.raises(RheoGpuError) as e:
+        ctx.constitutive_correct(newTimeStep=False)
+    assert e.value.status == abi.RT_ENOTREADY
+    perf_g = [ctx.constitutive_correct(newTimeStep=(i == 0)) for i in range(3)]
+    got = ctx.fields()
+    o = Oracle(case, f0.copy())
+    perf_o = [o.constitutive_correct(thetaOld=f0.theta.copy()) for _ in range(3)]
+    for pg, po in zip(perf_g, perf_o):
+        assert [p.nIterations for p in pg] == [p.nIterations for p in po]
+    for name in ("theta", "tau", "eigVals"):
+        assert rel(getattr(got, name), getattr(o.f, name)) < 1e-11, name
+    # three plain calls advance three steps instead
+    o3 = Oracle(case, f0.copy())
+    for _ in range(3):
+        o3.constitutive_correct()
+    assert rel(o3.f.theta, o.f.theta) > 1e-6
