@@ -208,21 +208,10 @@ def _limiter(schemes: Dict[str, Any], key: str) -> str:
     raise CaseError(f"fvSchemes {key}: {v!r} is not implemented (GaussDefCmpw <limiter> or Gauss upwind)")
 
 
-def load_case(case_dir: str, substitute: bool = False,
-              bc_overrides: Optional[Dict[str, Dict[str, Tuple[str, Any]]]] = None,
-              precision: int = abi.RT_PREC_FP64) -> LoadedCase:
-    subs: List[str] = []
-    mesh = foam_io.read_polymesh(case_dir)
-    q = foam_io.mesh_quality(mesh)
-    if q["nonOrthogonality"] > 1e-6:
-        # the laplacian and face gradients are the orthogonal ones (no
-        # non-orthogonal correction): exact only on orthogonal meshes
-        msg = f"mesh non-orthogonality {q['nonOrthogonality']:.3g} deg: orthogonal laplacian used"
-        if not substitute:
-            raise CaseError(msg + " (pass substitute=True to run it anyway)")
-        subs.append(msg)
-    cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
-    par = cp.get("parameters", cp)
+def read_model(par: Dict[str, Any]) -> Model:
+    """The Model of a constitutiveProperties ``parameters`` dictionary, with
+    the keywords each model's constructor reads and its FatalErrors as
+    CaseError (newConstitutiveEq.C:32-61 and the models' constructors)."""
     typ = par.get("type", "")
     if typ not in abi.MODEL_NAMES:
         raise CaseError(f"Unknown constitutiveEq type {typ}; valid: {sorted(abi.MODEL_NAMES)}")
@@ -264,7 +253,24 @@ def load_case(case_dir: str, substitute: bool = False,
             for key, cast in (("rTolMittagLeffler", float), ("maxIterMittagLeffler", int)):
                 if key in par:
                     mkw[key] = cast(scalar(par[key]))
-    model = Model(**mkw)
+    return Model(**mkw)
+
+
+def load_case(case_dir: str, substitute: bool = False,
+              bc_overrides: Optional[Dict[str, Dict[str, Tuple[str, Any]]]] = None,
+              precision: int = abi.RT_PREC_FP64) -> LoadedCase:
+    subs: List[str] = []
+    mesh = foam_io.read_polymesh(case_dir)
+    q = foam_io.mesh_quality(mesh)
+    if q["nonOrthogonality"] > 1e-6:
+        # the laplacian and face gradients are the orthogonal ones (no
+        # non-orthogonal correction): exact only on orthogonal meshes
+        msg = f"mesh non-orthogonality {q['nonOrthogonality']:.3g} deg: orthogonal laplacian used"
+        if not substitute:
+            raise CaseError(msg + " (pass substitute=True to run it anyway)")
+        subs.append(msg)
+    cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
+    model = read_model(cp.get("parameters", cp))
 
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))
     solvers = sol.get("solvers", {})

@@ -487,3 +487,34 @@ def test_constitutive_correct_inner_iterations(ctx):
     for _ in range(3):
         o3.constitutive_correct()
     assert rel(o3.f.theta, o.f.theta) > 1e-6
+
+
+def test_rheotest_driver_on_the_gpu(ctx):
+    """rheoTestFoam's transient mode (uniaxial extension, Giesekus, nInIter 2)
+    through the library equals the same driver stepped by the oracle."""
+    from oracle.pyoracle import Oracle
+    from rheotool_gb300.case import Model
+    from rheotool_gb300.rheotest import GpuBackend, RheoTestParameters, run_rheotest
+
+    class OracleBackend:
+        def setup(self, case, fields):
+            self.o = Oracle(case, fields.copy())
+
+        def fields(self):
+            return self.o.f.copy()
+
+        def correct(self, L, newTimeStep):
+            if newTimeStep:
+                self.theta0 = self.o.f.theta.copy()
+            self.o.constitutive_correct(L, thetaOld=self.theta0)
+
+        def tau(self):
+            return self.o.f.tau[0].copy()
+
+    model = Model("GiesekusLog", etaS=0.2, etaP=0.8, lambda_=1.0, alpha=0.3)
+    params = RheoTestParameters(np.diag([1.0, -0.5, -0.5]), [0.3])
+    got = run_rheotest(model, params, 0.01, 0.2, nInIter=2, backend=GpuBackend(ctx=ctx))
+    want = run_rheotest(model, params, 0.01, 0.2, nInIter=2, backend=OracleBackend())
+    assert len(got) == len(want) == 20
+    for g, w in zip(got, want):
+        assert np.max(np.abs(g.extraStress - w.extraStress)) <= 1e-11 * np.max(np.abs(w.extraStress))
