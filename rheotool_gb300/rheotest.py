@@ -24,15 +24,21 @@ values give fvc::grad(U) in the reference.  From theta = 0 exactly, a pure
 shear leaves the log-conformation update at rest (the reference's as well):
 give a small initial theta for shear flows.
 
-The backend (``GpuBackend`` by default) is what steps the cell: ``setup``
-(case and fields), ``fields``, ``correct`` (grad U, new time step or not) and
-``tau`` (the first cell's tau).
+A multiMode model (multiMode.C: a list of models) runs each mode on its own
+box; extraStress sums the modes' tau and etaS, and lambdaMin / lambdaMax of
+the ramp's time step range over the modes (createFields.H:185-200).  In a
+homogeneous flow the modes do not interact, so this is the reference's
+multi-mode update; the flow solver takes single-mode models only.
+
+A backend is what steps the cell of one mode: ``setup`` (case and fields),
+``fields``, ``correct`` (grad U, new time step or not) and ``tau`` (the
+first cell's tau).  ``GpuBackend`` (one library context) is the default.
 """
 from __future__ import annotations
 
 import os
 from dataclasses import dataclass
-from typing import Any, Dict, List, Optional, Sequence
+from typing import Any, Dict, List, Optional, Sequence, Union
 
 import numpy as np
 
@@ -113,35 +119,54 @@ def homogeneous_case(model: Model, deltaT: float, solverTheta: Optional[SolverCo
     return case, f
 
 
-def run_rheotest(model: Model, params: RheoTestParameters, deltaT: float, endTime: float, nInIter: int = 0,
-                 solverTheta: Optional[SolverControl] = None, theta0: Optional[np.ndarray] = None,
-                 backend=None) -> List[RheoTestRow]:
-    """The rows rheoTestFoam writes to its Report (see the module docstring)."""
+def run_rheotest(model: Union[Model, Sequence[Model]], params: RheoTestParameters, deltaT: float,
+                 endTime: float, nInIter: int = 0, solverTheta: Optional[SolverControl] = None,
+                 theta0: Optional[np.ndarray] = None, backend=None) -> List[RheoTestRow]:
+    """The rows rheoTestFoam writes to its Report (see the module docstring).
+    model: one Model or the modes of a multiMode model; backend: one per
+    mode (a list, or a single backend for a single mode), default a
+    GpuBackend each."""
+    modes = [model] if isinstance(model, Model) else list(model)
+    if not modes:
+        raise ValueError("multiMode: no models")
     own = backend is None
-    backend = GpuBackend() if own else backend
+    backends = [GpuBackend() for _ in modes] if own else (list(backend) if isinstance(backend, (list, tuple))
+                                                         else [backend])
+    if len(backends) != len(modes):
+        raise ValueError(f"{len(modes)} modes need as many backends, got {len(backends)}")
     try:
         G = np.asarray(params.gradU, dtype=np.float64).reshape(3, 3)
         rates = [float(r) for r in params.rates]
         if not rates:
             raise ValueError("gammaEpsilonDotL is empty")
-        lam = model.lambda_           # lambdaMin = lambdaMax for a single-mode model
-        dt = (lam + lam) * 0.5 / rates[0] if params.ramp else float(deltaT)
-        case, f = homogeneous_case(model, dt, solverTheta, theta0)
-        backend.setup(case, f)
-        n = case.mesh.nCells
+        lamMax, lamMin = max(m.lambda_ for m in modes), min(m.lambda_ for m in modes)
+        etaS = sum(m.etaS for m in modes)
+        dt = (lamMin + lamMax) * 0.5 / rates[0] if params.ramp else float(deltaT)
+        cases = []
+        for m, be in zip(modes, backends):
+            case, f = homogeneous_case(m, dt, solverTheta, theta0)
+            be.setup(case, f)
+            cases.append(case)
+        n = cases[0].mesh.nCells
         rows: List[RheoTestRow] = []
         L = G * rates[0]
+
+        def tau_total():
+            return sum(be.tau() for be in backends)
+
         if not params.ramp:
             nsteps = int(round(float(endTime) / dt))
             for s in range(1, nsteps + 1):
-                for i in range(int(nInIter)):
-                    backend.correct(np.tile(L.reshape(9), (n, 1)), i == 0)
-                rows.append(RheoTestRow(s * dt, extra_stress(backend.tau(), L, model.etaS)))
+                for be in backends:
+                    for i in range(int(nInIter)):
+                        be.correct(np.tile(L.reshape(9), (n, 1)), i == 0)
+                rows.append(RheoTestRow(s * dt, extra_stress(tau_total(), L, etaS)))
             return rows
         idx, cnt, old = 0, 0, np.zeros((3, 3))
         while True:
-            backend.correct(np.tile(L.reshape(9), (n, 1)), True)
-            es = extra_stress(backend.tau(), L, model.etaS)
+            for be in backends:
+                be.correct(np.tile(L.reshape(9), (n, 1)), True)
+            es = extra_stress(tau_total(), L, etaS)
             T = _full(es)
             relError = float(np.linalg.norm(T - old) / (np.linalg.norm(T) + SMALL))
             if relError < params.relTol or cnt > params.maxIter:
@@ -150,14 +175,16 @@ def run_rheotest(model: Model, params: RheoTestParameters, deltaT: float, endTim
                 idx, cnt = idx + 1, 0
                 if idx == len(rates):
                     return rows
-                case.deltaT = (lam + lam) * 0.5 / rates[idx]
-                backend.setup(case, backend.fields())
+                for case, be in zip(cases, backends):
+                    case.deltaT = (lamMin + lamMax) * 0.5 / rates[idx]
+                    be.setup(case, be.fields())
                 L = G * rates[idx]
             old = T
             cnt += 1
     finally:
         if own:
-            backend.close()
+            for be in backends:
+                be.close()
 
 
 def report_text(rows: List[RheoTestRow], params: RheoTestParameters) -> str:
@@ -185,6 +212,22 @@ def _switch(v: Any) -> bool:
     return str(v).strip().lower() in ("true", "on", "yes", "y", "1")
 
 
+def read_modes(par: Dict[str, Any]) -> Union[Model, List[Model]]:
+    """The Model of a ``parameters`` dictionary, or the modes of a
+    multiMode one (``models ( M1 { ... } M2 { ... } );``, multiMode.C:69-91)."""
+    from .foam_case import CaseError, parse_dict, read_model
+    if par.get("type") != "multiMode":
+        return read_model(par)
+    raw = par.get("models")
+    if not isinstance(raw, str) or not raw.strip().startswith("("):
+        raise CaseError("keyword models is undefined in the multiMode parameters")
+    entries = parse_dict(raw.strip()[1:-1])
+    modes = [read_model(d) for d in entries.values() if isinstance(d, dict)]
+    if not modes:
+        raise CaseError("multiMode: the models list is empty")
+    return modes
+
+
 def load_rheotest_case(case_dir: str, substitute: bool = True) -> Dict[str, Any]:
     """The inputs of a rheoTestFoam case directory: the model
     (constant/constitutiveProperties ``parameters``), rheoTestFoamParameters,
@@ -194,7 +237,7 @@ def load_rheotest_case(case_dir: str, substitute: bool = True) -> Dict[str, Any]
     from . import foam_io
     from .foam_case import CaseError, _solver, read_dict, read_model, scalar
     cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
-    model = read_model(cp.get("parameters", cp))
+    model = read_modes(cp.get("parameters", cp))
     rp = cp.get("rheoTestFoamParameters")
     if not isinstance(rp, dict):
         raise CaseError("sub-dictionary rheoTestFoamParameters is undefined in constitutiveProperties")
@@ -238,11 +281,13 @@ def main(argv=None):
     ap.add_argument("case_dir")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
-    be = GpuBackend(a.device)
+    modes = load_rheotest_case(a.case_dir)["model"]
+    bes = [GpuBackend(a.device) for _ in (modes if isinstance(modes, list) else [modes])]
     try:
-        rows = run_rheotest_case(a.case_dir, backend=be)
+        rows = run_rheotest_case(a.case_dir, backend=bes)
     finally:
-        be.ctx.close()
+        for be in bes:
+            be.close()
     print(f"{len(rows)} rows written to {os.path.join(a.case_dir, 'Report')}")
 
 

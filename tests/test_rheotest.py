@@ -158,3 +158,38 @@ def test_case_directory_and_report(tmp_path):
     assert float(text[3].split("\t")[1]) == pytest.approx(rows[1].extraStress[0], rel=1e-5)
     t = report_text(rows[:1], RheoTestParameters(UNIAXIAL, [0.05], ramp=False)).splitlines()
     assert t[0] == "******* Transient mode: fixed ε̇|γ̇ = 0.05 **********"
+
+
+def test_multimode_sums_the_modes():
+    """Two Oldroyd-B modes in steady shear: tau_xy = (etaS1 + etaS2 + etaP1 +
+    etaP2) rate, N1 = 2 (etaP1 lambda1 + etaP2 lambda2) rate^2; the ramp's
+    time step uses lambdaMin and lambdaMax of the modes."""
+    m1 = Model("Oldroyd-BLog", etaS=0.1, etaP=0.5, lambda_=0.8)
+    m2 = Model("Oldroyd-BLog", etaS=0.05, etaP=0.3, lambda_=1.2)
+    params = RheoTestParameters(SHEAR, [2.0, 3.0], ramp=True, relTol=1e-10)
+    bes = [OracleBackend(), OracleBackend()]
+    rows = run_rheotest([m1, m2], params, None, None, theta0=SEED, backend=bes)
+    assert bes[0].o.case.deltaT == pytest.approx((0.8 + 1.2) * 0.5 / 3.0)
+    for r in rows:
+        es = r.extraStress
+        assert r.status == "Converged"
+        assert abs(es[1] - (0.1 + 0.05 + 0.5 + 0.3) * r.x) < 1e-7 * r.x
+        assert abs((es[0] - es[3]) - 2 * (0.5 * 0.8 + 0.3 * 1.2) * r.x ** 2) < 1e-6 * r.x ** 2
+    with pytest.raises(ValueError, match="backends"):
+        run_rheotest([m1, m2], params, None, None, backend=OracleBackend())
+
+
+def test_multimode_case_directory(tmp_path):
+    from rheotool_gb300.foam_case import parse_dict
+    from rheotool_gb300.rheotest import read_modes
+    par = parse_dict("parameters\n{\n    type multiMode;\n    models\n    (\n"
+                     "        M1 { type XPomPomLog; rho 1; etaS 0; etaP 280.4; lambdaB 0.0039; lambdaS 0.00056;"
+                     " alpha 0.3; q 1; n 0; stabilization coupling; }\n"
+                     "        M2 { type GiesekusLog; rho 1; etaS 0.1; etaP 810.4; lambda 0.051; alpha 0.3;"
+                     " stabilization coupling; }\n    );\n}\n")["parameters"]
+    modes = read_modes(par)
+    assert [m.type for m in modes] == ["XPomPomLog", "GiesekusLog"]
+    assert modes[0].lambda_ == 0.0039 and modes[0].lambdaS == 0.00056 and modes[1].alpha == 0.3
+    from rheotool_gb300.foam_case import CaseError
+    with pytest.raises(CaseError, match="models"):
+        read_modes({"type": "multiMode"})
