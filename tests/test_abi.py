@@ -26,10 +26,11 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_header_constants_match_the_bindings():
-    """Every integer #define of the headers has the same value in abi.py."""
+    """Every integer #define of the headers (with or without a trailing
+    comment) has the same value in abi.py."""
     seen = 0
     for h in headers():
-        for name, val in re.findall(r"^#define\s+(RT_\w+)\s+(-?\d+)\s*$", open(h).read(), re.M):
+        for name, val in re.findall(r"^#define\s+(RT_\w+)\s+(-?\d+)\s*(?:/\*.*)?$", open(h).read(), re.M):
             assert hasattr(abi, name), f"{name} missing from abi.py"
             assert getattr(abi, name) == int(val), name
             seen += 1
