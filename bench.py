@@ -8,22 +8,25 @@ Giesekus-Log alpha = 0.1, Wi = 2, beta = 1/9, synthetic mesh and inputs (no
 dataset exists for it).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--precision mixed|fp64]
+                    [--precision fp64|mixed]
 
 Prints one JSON line.  `value` is device-timed (CUDA events on the library's
 stream) whole-job cell-steps/s of the selected form with all fields resident
-in HBM: by default the mixed-precision form (FP32 Krylov iterations and
-sweeps, FP64 residual replacement, FP64 assembly and constitutive update).
-The FP64 plain path is timed in the same run on the same case (`plain_fp64`)
-and `field_error_vs_fp64` gives each field's relative L2 difference between
-the two forms after the same number of steps from the same initial state.
-`e2e` is the same metric through the C ABI with host buffers (each step
-uploads U, p, phi and downloads U, p, phi, tau); `roofline` is for the
-operation with the largest device time, measured live with CUDA events;
-`cpu_baseline` is the FP64 CPU oracle on a bounded sample of the same
-workload.  `--impl reference` times the reference algorithm on the host
-cores: the reference itself (rheoTool on OpenFOAM v9) cannot be built here,
-so its FP64 CPU restatement (oracle/) runs instead, with all host threads.
+in HBM: by default the FP64 plain form, the reference's own precision.  The
+mixed-precision form (FP32 Krylov iterations and sweeps, FP64 residual
+replacement; FP32 constitutive algebra with FP64 fallbacks) is timed in the
+same run on the same case and steps (`mixed_precision`), with each field's
+relative L2 difference from the FP64 form (`field_error_vs_fp64`).  `e2e` is
+the same metric over the same steps from the same state, through the C ABI
+with pinned host buffers (each step uploads U, p, phi and downloads U, p,
+phi, tau; theta stays resident, as it does between rheoFoam time steps).
+`roofline` is for the operation with the largest device time, measured live
+with CUDA events; `cpu_baseline` is the FP64 CPU oracle on a bounded sample
+of the same workload.  `--impl reference` times the reference algorithm on
+the host cores over the same mesh and steps: the reference itself (rheoTool
+on OpenFOAM v9) cannot be built here, so its FP64 CPU restatement (oracle/)
+runs instead; its Krylov iterations, sweeps and face loops are sequential, as
+one OpenFOAM process runs them, so it runs on one core.
 """
 from __future__ import annotations
 
@@ -56,7 +59,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="form timed for `value` (the other is timed beside it unless --no-plain)")
     ap.add_argument("--no-plain", action="store_true", help="skip the second form")
     ap.add_argument("--no-floor", action="store_true",
@@ -70,7 +73,8 @@ def parse():
     ap.add_argument("--precision-sweep", action="store_true",
                     help="instead of the throughput line: the precision sweep on the periodic PTT channel")
     ap.add_argument("--sweep-dims", default="400x100x100", help="periodic channel cells nx x ny x nz")
-    ap.add_argument("--sweep-steps", type=int, default=5)
+    ap.add_argument("--sweep-steps", type=int, default=3)
+    ap.add_argument("--no-sweep", action="store_true", help="skip the precision sweep key of the default line")
     return ap.parse_args()
 
 
@@ -162,10 +166,10 @@ class Clocks:
 
 
 def cpu_baseline(seconds: float, warm: int = 1):
-    """FP64 CPU oracle on the 126,675-cell sample, all host threads."""
+    """FP64 CPU oracle on the 126,675-cell sample, one core (its Krylov
+    sweeps, face loops and cell loops all run on one thread)."""
     from oracle import pyoracle
-    threads = os.cpu_count() or 1
-    pyoracle.set_threads(threads)
+    pyoracle.set_threads(1)
     case = make_case(True)
     o = pyoracle.Oracle(case)
     if warm:
@@ -178,10 +182,9 @@ def cpu_baseline(seconds: float, warm: int = 1):
             break
     dt = time.perf_counter() - t0
     cells = case.mesh.nCells
-    return {"value": cells * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    return {"value": cells * n / dt, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"same contraction/Giesekus case at {cells:,} cells (1/8 of the 1M mesh), "
-                      f"{n} time steps after {warm} warm-up step(s), FP64 oracle (serial face loops and "
-                      f"Krylov sweeps, OpenMP over cell-local loops), {dt:.1f} s"}
+                      f"{n} time steps after {warm} warm-up step(s), FP64 oracle on one core, {dt:.1f} s"}
 
 
 def run_batched(args):
@@ -331,23 +334,24 @@ def run_precision_sweep(args):
             "theta_max_abs": float(np.abs(f64.theta).max()),
         }
     ctx.close()
-    line = {"metric": "per-field relative L2 error of the mixed form vs the FP64 form (precision sweep)",
+    return {"metric": "per-field relative L2 error of the mixed form vs the FP64 form (precision sweep)",
             "config": {"workload": f"3-D channel periodic in x and z, {nx}x{ny}x{nz} = {N:,} cells, walls at y=+-1, "
                                    "body-force driven (mean velocity 1), PTT-Log linear epsilon=0.25 zeta=0, "
                                    "beta=1/9, rho=0.01, dt=5e-3, Euler, GaussDefCmpw cubista, p PCG-DIC 1e-8, "
                                    "U/theta PBiCGStab-DILU 1e-10; theta0 = Q diag(0.1 z) Q^T seeded lognormal",
                        "steps": args.sweep_steps, "cells": N},
             "data": "synthetic", "results": result}
-    print(json.dumps(line), flush=True)
 
 
 def run_reference(args, rank):
+    """The reference algorithm on the host: the FP64 oracle on the same mesh
+    (1,000,000 cells unless --small) and the same steps as the GPU arm's
+    `value` (W untimed warm-up steps, then K timed), on one core."""
     if rank != 0:
         return
     from oracle import pyoracle
-    threads = os.cpu_count() or 1
-    pyoracle.set_threads(threads)
-    case = make_case(True)
+    pyoracle.set_threads(1)
+    case = make_case(args.small)
     o = pyoracle.Oracle(case)
     if args.warmup:
         o.step(args.warmup)
@@ -356,14 +360,17 @@ def run_reference(args, rank):
     dt = time.perf_counter() - t0
     cells = case.mesh.nCells
     v = cells * args.steps / dt
+    workload = (WORKLOAD if not args.small else WORKLOAD.replace("1,000,000", f"{cells:,}")) + ", FP64 plain form"
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "sample_cells": cells},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{cells:,}-cell sample of the contraction case, {args.steps} steps; "
-                                   "rheoTool/OpenFOAM v9 is not buildable here, its FP64 restatement runs"},
+        "data": "synthetic", "config": {"workload": workload, "cells": cells},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"the whole {cells:,}-cell case, steps {args.warmup + 1}..{args.warmup + args.steps} "
+                                   "(the GPU arm's timed steps); rheoTool/OpenFOAM v9 is not buildable here, its FP64 "
+                                   "restatement runs on one core (sequential Krylov sweeps and face loops, as one "
+                                   "OpenFOAM process runs them)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -377,7 +384,7 @@ def main():
         return
     if args.precision_sweep:
         if rank == 0:
-            run_precision_sweep(args)
+            print(json.dumps(run_precision_sweep(args)), flush=True)
         return
     import numpy as np
     from rheotool_gb300 import abi
@@ -435,13 +442,13 @@ def main():
 
     if not args.no_plain:
         ctx2 = Context(local)
-        ms2, perf2, _, _ = timed(ctx2, other, False)
+        ms2, perf2, launches2, _ = timed(ctx2, other, False)
         a, b = ctx.fields(), ctx2.fields()
         ref, got = (b, a) if prec == abi.RT_PREC_MIXED else (a, b)
         field_err = rel_err(got, ref)
         second = {"precision": "fp64" if other == abi.RT_PREC_FP64 else "mixed",
                   "value": total_cells / (ms2 * 1e-3), "ms_per_step": ms2 / args.steps,
-                  "iterations_last_step": iters(perf2)}
+                  "gpu_launches": launches2, "iterations_last_step": iters(perf2)}
         ctx2.close()
         case.precision = prec
         if not args.no_floor:
@@ -452,10 +459,10 @@ def main():
             import copy
             saved = case.solverU, case.solverP, case.solverTheta
             tight = []
-            for s in saved:
-                t = copy.copy(s)
+            for s_ in saved:
+                t = copy.copy(s_)
                 t.tolerance *= 1e-2
-                t.maxIter = max(5 * s.maxIter, 4000)
+                t.maxIter = max(5 * s_.maxIter, 4000)
                 tight.append(t)
             case.solverU, case.solverP, case.solverTheta = tight
             ctx3 = Context(local)
@@ -502,6 +509,9 @@ def main():
                                                             if not k.startswith("solve_")), 1e-30)}
 
     # ---- end to end through the C ABI with host buffers -------------------
+    # The same steps as `value` from the same state: a fresh case setup, W
+    # warm-up steps, then K timed steps, each uploading U, p and phi from
+    # pinned host memory, stepping once and downloading U, p, phi and tau.
     e2e = None
     if not args.no_e2e:
         try:
@@ -511,28 +521,43 @@ def main():
             pin = lambda shape: np.zeros(shape)
         U, Ub, p, pb = pin((N, 3)), pin((NB, 3)), pin(N), pin(NB)
         phi, phib, tau = pin(F), pin(NB), pin((N, 6))
-        # start from the current device state
-        for fid, a, b in ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib)):
-            ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a), abi.dptr(b))
-        ke = max(2, min(args.steps, 5))
-        ctx.sync()
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            for fid, a, b in ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib)):
-                ctx.lib.rt_field_set(ctx._ctx, fid, abi.dptr(a), abi.dptr(b))
+        up = ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib))
+        case.precision = prec
+        ctx.setup_case(case)
+        for fid, a_, b_ in up:
+            ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a_), abi.dptr(b_))
+        for _ in range(args.warmup):
+            for fid, a_, b_ in up:
+                ctx.lib.rt_field_set(ctx._ctx, fid, abi.dptr(a_), abi.dptr(b_))
             ctx.step(1)
-            for fid, a, b in ((abi.RT_FIELD_U, U, Ub), (abi.RT_FIELD_P, p, pb), (abi.RT_FIELD_PHI, phi, phib)):
-                ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a), abi.dptr(b))
+            for fid, a_, b_ in up:
+                ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a_), abi.dptr(b_))
+        ctx.sync()
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for fid, a_, b_ in up:
+                st = ctx.lib.rt_field_set(ctx._ctx, fid, abi.dptr(a_), abi.dptr(b_))
+                assert st == 0
+            ctx.step(1)
+            for fid, a_, b_ in up:
+                st = ctx.lib.rt_field_get(ctx._ctx, fid, abi.dptr(a_), abi.dptr(b_))
+                assert st == 0
             ctx.lib.rt_field_get(ctx._ctx, abi.RT_FIELD_TAU, abi.dptr(tau), None)
-        dt = time.perf_counter() - t0
+        dt = rank_max((time.perf_counter() - t0) * 1e3, pg) * 1e-3
         h2d = 8 * (3 * N + 3 * NB + N + NB + F + NB)
         d2h = h2d + 8 * 6 * N
-        e2e = {"value": N * ke * world / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "steps": ke, "path": "rt_field_set(U,p,phi) + rt_step(1) + rt_field_get(U,p,phi,tau), pinned host"}
+        e2e = {"value": N * args.steps * world / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": args.steps, "warmup": args.warmup,
+               "path": "rt_field_set(U,p,phi) + rt_step(1) + rt_field_get(U,p,phi,tau) per step, pinned host "
+                       "buffers, host wall clock; the same steps as value from the same initial state "
+                       "(theta stays resident between steps, as between rheoFoam time steps)"}
 
     ctx.close()
     batched = None if (args.no_batch or args.small) else run_batched(args)
     served = None if (args.no_serve or args.small) else run_served(args)
+    sweep = None if (args.no_sweep or args.small or rank != 0) else run_precision_sweep(args)
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -557,9 +582,9 @@ def main():
         }
         if second is not None:
             key = "plain_fp64" if mixed else "mixed_precision"
+            second["speedup_mixed_vs_fp64"] = (value / second["value"]) if mixed else (second["value"] / value)
+            second["field_error_vs_fp64"] = field_err
             line[key] = second
-            line["speedup_vs_" + key] = value / second["value"]
-            line["field_error_vs_fp64"] = field_err
         if floor is not None:
             line["solver_tolerance_floor"] = floor
         line["profile_ms_2_steps"] = {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
@@ -577,6 +602,8 @@ def main():
             line["batched"] = batched
         if served is not None:
             line["served"] = served
+        if sweep is not None:
+            line["precision_sweep"] = sweep
         print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()

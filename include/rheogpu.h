@@ -254,6 +254,19 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * steps (a power of two, 8 .. 128; 0 = default 128).  Each launch takes the
  * deepest ring up to this cap that fits the shared memory. */
 #define RT_OPT_SWEEP_RING 7
+/* RT_OPT_WAIT_LIMIT: spins a bounded device-side wait of the systolic sweeps
+ * makes before it gives up (sets the sweep's error flag; the call returns
+ * RT_ETIMEOUT and the context stays usable).  Default 2^24 (about a second
+ * for a wait between thread-block clusters, which polls 16x less often);
+ * 64 .. 2^40. */
+#define RT_OPT_WAIT_LIMIT 8
+/* RT_OPT_STALL_TEST: failure-detection tests only.  value > 0: in the next
+ * `value` systolic sweep launches, the first plane of every thread-block
+ * cluster after the first waits for a hand-off word that no plane writes, so
+ * its bounded wait runs out and the call returns RT_ETIMEOUT (meshes with
+ * more planes than one cluster holds; see RT_OPT_SWEEP_PLANES).  0 (default)
+ * clears it. */
+#define RT_OPT_STALL_TEST 9
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);
@@ -281,14 +294,20 @@ rt_status rt_residual(rt_ctx *ctx, const double *diag, const double *upper,
 /* rt_residual for callers that cannot allocate device memory (a solver
  * callback inside another library's Krylov loop, where a cudaMalloc would
  * synchronise the device in the middle of that loop; a host whose device
- * memory all belongs to its own pool allocator).  No reference counterpart: an addition of this library.  diag, upper,
- * lower, source and psi are DEVICE pointers on the context's device (nCells /
- * nFaces doubles); residual is a host pointer.  The reduction scratch is a
- * static device array inside the library, so the call allocates nothing; it
- * limits meshes to 2,097,152 cells (RT_EINVAL beyond).  The first call on a
- * device resolves that array's address, so make it before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * memory all belongs to its own pool allocator).  No reference counterpart:
+ * an addition of this library.  diag, upper, lower, source and psi are
+ * DEVICE pointers (device or managed memory) on the context's device
+ * (nCells / nFaces doubles); anything else is refused with RT_EINVAL before
+ * any kernel runs.  residual is a host pointer.  The kernels run on the
+ * context's stream, which is not ordered after the caller's streams: the
+ * caller finishes the work that writes the inputs first (synchronises its
+ * stream, or has that work complete before the call by other means).  The
+ * reduction scratch is a static device array inside the library, so the call
+ * allocates nothing; it limits meshes to 2,097,152 cells (RT_EINVAL beyond).
+ * The first call on each context resolves that array's address on the
+ * context's device, so make it before any stream capture.  All calls share
+ * the one array: calls that overlap on the GPU race and must be serialised by
+ * the caller. */
 rt_status rt_residual_noalloc(rt_ctx *ctx, const double *diag, const double *upper,
                               const double *lower, const double *source,
                               const double *psi, double *residual);
@@ -305,8 +324,10 @@ rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU,
  * theta.oldTime() after the time increment; every call then solves fvm::ddt
  * against that field, so nInIter calls in one step iterate the update rather
  * than advance nInIter steps.  rt_constitutive_correct is the call with
- * newTimeStep = 1.  A call with newTimeStep = 0 before any with 1 since the
- * case setup returns RT_ENOTREADY. */
+ * newTimeStep = 1.  A call with newTimeStep = 0 returns RT_ENOTREADY unless
+ * a call with 1 came after the last rt_case_setup, rt_step,
+ * rt_constitutive_correct or rt_field_set of theta (each of those starts
+ * another time step, or replaces theta). */
 rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t newTimeStep,
                                        rt_solver_perf *thetaPerf);
 

@@ -32,6 +32,8 @@ RT_OPT_MIXED_PARTS = 4
 RT_OPT_MIXED_TIGHTEN = 5
 RT_OPT_SWEEP_TUNE = 6
 RT_OPT_SWEEP_RING = 7
+RT_OPT_WAIT_LIMIT = 8
+RT_OPT_STALL_TEST = 9
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {

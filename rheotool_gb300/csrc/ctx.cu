@@ -395,6 +395,14 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
             ctx->sweepRing = (int)value;
             ctx->mesh.sm.tune[0] = ctx->mesh.sm.tune[1] = -1;
             return RT_OK;
+        case RT_OPT_WAIT_LIMIT:
+            RT_REQUIRE(value >= 64 && value <= (1ll << 40), RT_EINVAL, "RT_OPT_WAIT_LIMIT: 64 .. 2^40 spins");
+            ctx->waitLimit = value;
+            return RT_OK;
+        case RT_OPT_STALL_TEST:
+            RT_REQUIRE(value >= 0 && value <= 1000, RT_EINVAL, "RT_OPT_STALL_TEST: 0 .. 1000 launches");
+            ctx->stallTest = (int)value;
+            return RT_OK;
         case RT_OPT_MIXED_TIGHTEN:
             RT_REQUIRE(value >= 0 && value <= 12, RT_EINVAL, "RT_OPT_MIXED_TIGHTEN: decades 0 .. 12");
             ctx->mixedTighten = std::pow(10.0, -(double)value);
@@ -520,6 +528,8 @@ rt_status rt_field_set(rt_ctx *ctx, int32_t field, const double *internal, const
         int nc, nIn;
         field_info(ctx, field, &in, &bd, &nc, &nIn);
         if (internal) upload_soa(ctx, internal, nIn, nc, *in);
+        // a new theta starts a new time step for rt_constitutive_correct_iter
+        if (field == RT_FIELD_THETA && internal) ctx->cs.thetaOldSaved = false;
         if (boundary) {
             RT_REQUIRE(bd != nullptr, RT_EINVAL, "field has no boundary values");
             upload_soa(ctx, boundary, ctx->mesh.NB, nc, *bd);
@@ -624,6 +634,9 @@ rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_pe
         RT_REQUIRE(thetaPerf, RT_EINVAL, "null perf");
         DBuf<double> g;
         if (gradU) upload_soa(ctx, gradU, ctx->mesh.N, 9, g);
+        // a completed time step: the old-time theta kept by
+        // rt_constitutive_correct_iter belongs to an earlier step now
+        ctx->cs.thetaOldSaved = false;
         rt_status st = constitutive_correct(ctx, gradU ? g.p : nullptr, thetaPerf);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
         return st;
@@ -659,6 +672,9 @@ rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf) {
         RT_REQUIRE(nSteps >= 0, RT_EINVAL, "nSteps must be >= 0");
         rt_step_perf local{};
         rt_status st = RT_OK;
+        // the steps advance theta: an old-time theta kept by
+        // rt_constitutive_correct_iter no longer belongs to the current step
+        if (nSteps > 0) ctx->cs.thetaOldSaved = false;
         for (int i = 0; i < nSteps && st == RT_OK; ++i) {
             local = rt_step_perf{};
             st = step_once(ctx, &local);

@@ -645,7 +645,8 @@ rt_status run_pcg(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
             perf[k].nIterations = iter;
             bool more = (iter < a.ctl.maxIter && !sv.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
                         iter < a.ctl.minIter;
-            if (!more) active &= ~(1u << k);
+            // a NaN/Inf residual never converges: stop (RT_ENAN follows)
+            if (!more || !std::isfinite(perf[k].finalResidual)) active &= ~(1u << k);
         }
     }
     (void)h;
@@ -708,6 +709,8 @@ rt_status run_pbicgstab(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
             if (sv.conv(perf[k].finalResidual, perf[k].initialResidual)) {
                 finish |= 1u << k;
                 perf[k].nIterations = iter + 1;
+            } else if (!std::isfinite(perf[k].finalResidual)) {
+                perf[k].nIterations = iter + 1;   // stops (RT_ENAN follows)
             } else {
                 cont |= 1u << k;
             }
@@ -741,7 +744,7 @@ rt_status run_pbicgstab(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
             perf[k].nIterations = iter;
             bool more = (iter < a.ctl.maxIter && !sv.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
                         iter < a.ctl.minIter;
-            if (!more) active &= ~(1u << k);
+            if (!more || !std::isfinite(perf[k].finalResidual)) active &= ~(1u << k);
         }
     }
     return RT_OK;
@@ -1233,7 +1236,7 @@ rt_status run_pcg_flex32(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) 
             perf[k].nIterations = iter;
             const bool more = (iter < a.ctl.maxIter && !mx.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
                               iter < a.ctl.minIter;
-            if (!more) active &= ~(1u << k);
+            if (!more || !std::isfinite(perf[k].finalResidual)) active &= ~(1u << k);
         }
     }
     return RT_OK;

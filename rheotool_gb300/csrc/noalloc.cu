@@ -19,34 +19,49 @@
 // reads, so nothing has to be cleared between calls; but all calls share the
 // one array, so calls that overlap on the GPU (two host threads, two streams)
 // race and must be serialised by the caller.
-#include <mutex>
-
+//
+// The kernels run on the context's stream.  Nothing orders that stream after
+// the streams on which the caller wrote its inputs, so the caller completes
+// that work before the call.  The five input pointers are checked with
+// cudaPointerGetAttributes (which allocates nothing): host memory, or memory
+// of another device, is refused with RT_EINVAL before any kernel runs.
 #include "rt_internal.h"
 
 namespace {
 
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = 8192;
-constexpr int kMaxDevices = 128;
-
 static __device__ __align__(256) double g_rt_noalloc_scratch[3 * kMaxBlocks + 8];
 
-std::mutex g_mutex;
-double *g_scratch[kMaxDevices] = {};
-
-// device address of the scratch array on the current device (first call per
-// device resolves it; the symbol name in host code is only a host stand-in)
-rt::Error scratch_on_device(int device, double **out) {
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (device < 0 || device >= kMaxDevices) return rt::Error{RT_EINVAL, "device index out of range"};
-    if (!g_scratch[device]) {
+// Device address of the scratch array on the context's device (current when
+// this runs).  In host code the symbol's name is only a host-side stand-in;
+// the address is resolved on the first call of each context and kept in it,
+// so a context created after a device reset resolves it again.
+rt::Error scratch_on_device(rt_ctx *ctx, double **out) {
+    if (!ctx->noallocScratch) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_rt_noalloc_scratch);
         if (e != cudaSuccess)
             return rt::Error{RT_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)};
-        g_scratch[device] = static_cast<double *>(p);
+        ctx->noallocScratch = p;
     }
-    *out = g_scratch[device];
+    *out = static_cast<double *>(ctx->noallocScratch);
+    return rt::Error{RT_OK, ""};
+}
+
+// a caller's array must be device (or managed) memory of the context's device
+rt::Error check_device_pointer(const rt_ctx *ctx, const void *p, const char *name) {
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return rt::Error{RT_EINVAL, std::string(name) + ": not a CUDA pointer (" + cudaGetErrorString(e) + ")"};
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+        return rt::Error{RT_EINVAL, std::string(name) + ": not device memory (host or unregistered pointer)"};
+    if (at.device != ctx->device)
+        return rt::Error{RT_EINVAL, std::string(name) + ": memory of device " + std::to_string(at.device) +
+                                        ", the context is on device " + std::to_string(ctx->device)};
     return rt::Error{RT_OK, ""};
 }
 
@@ -143,6 +158,10 @@ extern "C" rt_status rt_residual_noalloc(rt_ctx *ctx, const double *diag, const 
         return RT_EINVAL;
     }
     const int N = ctx->mesh.N;
+    if (N <= 0) {   // rt_mesh_upload refuses empty meshes; nothing to reduce
+        *residual = 0.0;
+        return RT_OK;
+    }
     const int nb = (N + kThreads - 1) / kThreads;
     if (nb > kMaxBlocks) {
         ctx->lastError = "rt_residual_noalloc: " + std::to_string(N) + " cells exceed the maximum of " +
@@ -155,8 +174,17 @@ extern "C" rt_status rt_residual_noalloc(rt_ctx *ctx, const double *diag, const 
         ctx->lastError = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
         return RT_ECUDA;
     }
+    const void *args[5] = {diag, upper, lower, source, psi};
+    const char *names[5] = {"diag", "upper", "lower", "source", "psi"};
+    for (int i = 0; i < 5; ++i) {
+        rt::Error pe = check_device_pointer(ctx, args[i], names[i]);
+        if (pe.status != RT_OK) {
+            ctx->lastError = "rt_residual_noalloc: " + pe.msg;
+            return pe.status;
+        }
+    }
     double *scr = nullptr;
-    rt::Error se = scratch_on_device(ctx->device, &scr);
+    rt::Error se = scratch_on_device(ctx, &scr);
     if (se.status != RT_OK) {
         ctx->lastError = "rt_residual_noalloc: " + se.msg;
         return se.status;

@@ -334,6 +334,15 @@ struct rt_ctx {
     cudaEvent_t tStart = nullptr, tStop = nullptr;
     bool meshReady = false;
     long long kernelLaunches = 0;
+    // rt_residual_noalloc: device address of its static scratch array on this
+    // context's device, resolved on the context's first call
+    void *noallocScratch = nullptr;
+    // bounded waits of the systolic sweeps: spins before a wait gives up
+    // (RT_OPT_WAIT_LIMIT); stallTest > 0: the next sweep launch's
+    // cluster-to-cluster consumers expect a tag no producer writes
+    // (RT_OPT_STALL_TEST, failure-detection tests)
+    long long waitLimit = 1ll << 24;
+    int stallTest = 0;
 };
 
 namespace rt {

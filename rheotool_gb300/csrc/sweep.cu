@@ -245,7 +245,7 @@ __device__ __forceinline__ void st4(double *p, const double *v) {
 template <class Real, int MODE, int NC, int P, int NB>
 __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
                                                   int *sync, u64 *__restrict__ xfer, unsigned epoch,
-                                                  long long maxSpin, int R) {
+                                                  unsigned cepoch, long long maxSpin, int R) {
     static_assert(P % 4 == 0 && P <= 32, "a chunk is whole quads");
     constexpr int RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA, W = Words<Real>::W;
     constexpr int VW = NC * W;   // words per (step, lane)
@@ -429,7 +429,10 @@ __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mas
             // (Each word is checked in registers; one warp-uniform branch
             // leads to the rare bounded waits for words not there yet.  A
             // ring never wraps inside a chunk: R is a multiple of P.)
-            const unsigned ktag = kLocalProd ? (unsigned)(t0 + 1) : epoch;
+            // (cepoch, the tag a cluster's first plane expects from the
+            // previous cluster, is the launch's epoch except in a
+            // failure-detection test, where no producer writes it)
+            const unsigned ktag = kLocalProd ? (unsigned)(t0 + 1) : cepoch;
             bool qfail = false;
             // across a cluster boundary the words come from global memory: the
             // whole chunk's words are loaded at once (one memory round trip),
@@ -714,6 +717,14 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
         s.xfer.zero(ctx->stream);
     }
     if (++s.epoch == 0) s.epoch = 1;   // 0 marks a cleared word
+    // failure-detection test (RT_OPT_STALL_TEST): this launch's consumers of
+    // the cluster-to-cluster hand-off wait for a tag that no launch writes
+    // (epochs stay far below 2^31), so their bounded waits run out
+    unsigned cepoch = s.epoch;
+    if (ctx->stallTest > 0) {
+        cepoch = s.epoch ^ 0x80000000u;
+        --ctx->stallTest;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nGroups * CS);
     cfg.blockDim = dim3(32 * g.nJB);
@@ -727,7 +738,7 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
     cfg.attrs = at;
     cfg.numAttrs = 1;
     RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<Real, MODE, NC, P, NB>, g, mask, w, ctx->mesh.N, s.sync.p, s.xfer.p,
-                               s.epoch, 1ll << 24, R));
+                               s.epoch, cepoch, ctx->waitLimit, R));
 }
 
 // Schedules of the one-component sweeps (the pressure solve): chunk size P

@@ -19,3 +19,15 @@ def ctx():
     c = Context(0)
     yield c
     c.close()
+
+
+def pytest_terminal_summary(terminalreporter):
+    """The bar each full-step GPU parity case passed at (plain 1e-9, or the
+    round-off sensitivity bar of ill-conditioned cases), with its errors."""
+    for name, mod in list(sys.modules.items()):
+        if name.endswith("test_gpu_parity") and getattr(mod, "BAR_LOG", None):
+            terminalreporter.write_sep("-", "step parity bars")
+            for label, kind, errs, bar in mod.BAR_LOG:
+                e = " ".join(f"{n}={v:.1e}" for n, v in errs.items())
+                b = "" if bar is None else " bar " + " ".join(f"{n}={v:.1e}" for n, v in bar.items())
+                terminalreporter.write_line(f"{label}: {kind}: {e}{b}")

@@ -51,15 +51,24 @@ def step_bar(case, steps, ref, names):
     return {n: max(TOL_STEP, 100.0 * sens[n]) for n in names}
 
 
-def assert_step_parity(ctx, case, steps, names=("U", "p", "theta", "tau", "phi")):
+# which bar each full-step case passed at: printed at the end of the run
+# (tests/conftest.py), so a green run shows which cases met the plain 1e-9 bar
+# and which only the round-off sensitivity bar
+BAR_LOG = []
+
+
+def assert_step_parity(ctx, case, steps, names=("U", "p", "theta", "tau", "phi"), label=None):
     ref = oracle_run(case, steps)
     ctx.setup_case(case)
     pg = ctx.step(steps)
     got = ctx.fields()
     errs = {n: rel(getattr(got, n), getattr(ref, n)) for n in names}
+    label = label or f"{case.name} ({steps} steps)"
     if all(e < TOL_STEP for e in errs.values()):
+        BAR_LOG.append((label, "plain 1e-9", errs, None))
         return pg, ref
     bar = step_bar(case, steps, ref, names)
+    BAR_LOG.append((label, "sensitivity", errs, bar))
     for n in names:
         assert errs[n] < bar[n], (n, errs[n], bar[n])
     return pg, ref
@@ -341,6 +350,50 @@ def test_step_contraction3d_giesekus(ctx):
     from oracle.pyoracle import Oracle
     case = contraction_case(small_contraction(), dt=0.02)
     assert_step_parity(ctx, case, 6)
+
+
+def test_step_contraction_headline_sample_fp64(ctx):
+    """The headline case's kernel configuration at a size the oracle steps in
+    seconds: the 126,675-cell sample of the 1M-cell contraction (133 x 51 x
+    25 bounding grid, graded; two j-blocks per plane, two clusters of planes
+    with a cluster-to-cluster hand-off, the autotuned chunk schedule),
+    GiesekusLog Wi = 2, FP64 plain form, 3 steps: 1e-9 from the oracle."""
+    dims = dict(nx_up=67, nx_down=66, ny_in=25, ny_out=13, nz=25)
+    case = contraction_case(contraction_mesh(**dims))
+    assert case.mesh.nCells == 126675
+    pg, ref = assert_step_parity(ctx, case, 3, label="contraction 126,675-cell headline sample (3 steps)")
+    assert pg.p.nIterations > 100       # a real pressure solve, through the systolic sweeps
+
+
+@pytest.mark.parametrize("solver,pre,asym,nc,tune", [("PCG", "DIC", 0.0, 1, 3), ("PCG", "DIC", 0.0, 1, 2),
+                                                     ("PBiCGStab", "DILU", 3.0, 3, 0)])
+def test_systolic_sweeps_headline_structure(ctx, solver, pre, asym, nc, tune):
+    """The 1M-cell headline's sweep structure: 100 rows (four j-blocks per
+    plane), 34 planes (clusters of 16, 16 and 2: two cluster-to-cluster
+    hand-offs), the chunk of 16 steps the autotuner picks there (forced);
+    same bits and iteration counts as the level-scheduled sweeps."""
+    mesh = contraction_mesh(nx_up=20, nx_down=20, ny_in=50, ny_out=25, nz=34, L_up=4.0, L_down=4.0)
+    assert mesh.shape[1] == 100 and mesh.shape[2] == 34
+    rng = np.random.default_rng(24)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=asym)
+    b = rng.normal(size=(nc, mesh.nCells)) * mesh.V
+    ctl = SolverControl(solver, pre, 1e-10, 0.0, 0, 300)
+    ctx.upload_mesh(mesh)
+    out = {}
+    try:
+        ctx.set_option(abi.RT_OPT_SWEEP_TUNE, tune)
+        for mode in (abi.SWEEP_LEVELS, abi.SWEEP_SYSTOLIC):
+            ctx.set_sweep(mode)
+            x = np.zeros((nc, mesh.nCells))
+            perf = ctx.ldu_solve(diag, upper, lower, b, x, ctl)
+            out[mode] = (x, [p.nIterations for p in perf])
+        if tune:
+            assert ctx.sweep_schedule()["fp64"]["P"] == 16
+    finally:
+        ctx.set_sweep(abi.SWEEP_AUTO)
+        ctx.set_option(abi.RT_OPT_SWEEP_TUNE, 0)
+    assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
+    assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
 
 
 def test_step_channel_fixed_outlet(ctx):
