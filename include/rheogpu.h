@@ -24,7 +24,7 @@
  *   rt_constitutive_correct_iter  the same, called nInIter times in one time
  *                            step (solvers/rheoFoam/rheoFoam.C:149-153)
  *   rt_ldu_solve             lduMatrix::solver::solve(psi, source, cmpt) of
- *                            OpenFOAM's PCG/DIC and PBiCGStab/DILU, reached
+ *                            OpenFOAM's PCG/DIC, PBiCGStab/DILU and PBiCG/DILU, reached
  *                            through sparseSolver<Type>::solve
  *                            (libs/sparseMatrixSolvers/segregated/sparseSolver.H:
  *                            200-205, openFoamSolver/openFoamSolver.C:46-53)
@@ -152,6 +152,10 @@ typedef struct {
 /* ---- linear solvers ----------------------------------------------------- */
 #define RT_SOLVER_PCG       0
 #define RT_SOLVER_PBICGSTAB 1
+#define RT_SOLVER_PBICG     2   /* OpenFOAM PBiCG (the Contraction41 tutorials' U and theta
+                                   solver, of90/tutorials/rheoFoam/Contraction41/Oldroyd-BLog/
+                                   system/fvSolution:32,47); FP64 in both precision forms;
+                                   not in the batched form */
 #define RT_PRECOND_NONE     0
 #define RT_PRECOND_DIC      1
 #define RT_PRECOND_DILU     2
@@ -311,6 +315,30 @@ rt_status rt_residual(rt_ctx *ctx, const double *diag, const double *upper,
 rt_status rt_residual_noalloc(rt_ctx *ctx, const double *diag, const double *upper,
                               const double *lower, const double *source,
                               const double *psi, double *residual);
+
+/* ---- multiMode models (multiMode.C:69-91, 144-156, 222, 247-256) -------
+ * A multiMode constitutive model is a list of modes, each a constitutive
+ * model of its own with its own theta, tau and eigen fields on the common U
+ * and phi.  rt_case_setup_modes sets up such a case: models[nModes] (every
+ * mode with the same rho and stabilization, so that the momentum equation's
+ * sum of the modes' divTau is one divTau with the summed tau and the summed
+ * etaS and etaP); all modes take the theta and tau conditions of bcs.
+ * rt_step and rt_constitutive_correct then correct every mode in turn
+ * (rt_step_perf.theta holds the last mode's solves, rt_mode_perf every
+ * mode's: 6 records per mode).  rt_field_get(RT_FIELD_TAU) gives the summed
+ * tau (multiMode::tau()); RT_FIELD_THETA, EIGVALS and EIGVECS without a mode
+ * are mode 0's; rt_field_set_mode / rt_field_get_mode address one mode's
+ * theta, tau, eigVals or eigVecs (the summed tau is formed at the next
+ * correct()).  nModes = 1 is rt_case_setup.  Not in the batched form;
+ * rt_constitutive_correct_iter runs single-mode models. */
+#define RT_MAX_MODES 16
+rt_status rt_case_setup_modes(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model_params *models,
+                              int32_t nModes, const rt_case_ctl *ctl);
+rt_status rt_field_set_mode(rt_ctx *ctx, int32_t field, int32_t mode, const double *internal,
+                            const double *boundary);
+rt_status rt_field_get_mode(rt_ctx *ctx, int32_t field, int32_t mode, double *internal,
+                            double *boundary);
+rt_status rt_mode_perf(rt_ctx *ctx, rt_solver_perf *thetaPerf);
 
 /* One constitutiveEq::correct() on the device-resident U, phi, theta, eig
  * fields; gradU (9*nCells AoS) may be NULL (then fvc::grad(U) is used).

@@ -378,11 +378,82 @@ static void pbicgstab(const rt_mesh_desc *m, const double *diag, const double *u
     free(yA); free(rA); free(rD);
 }
 
+/* Preconditioned bi-conjugate gradients (Fletcher 1976; the preconditioned
+ * form of Barrett et al. 1994, "Templates", fig. 2.7) in OpenFOAM's lduMatrix
+ * conventions, as the PBiCG solver of the Contraction41 tutorials' U and
+ * theta equations runs it (of90/tutorials/rheoFoam/Contraction41/
+ * Oldroyd-BLog/system/fvSolution:32,47): the shadow system is the transposed
+ * one with the same right-hand side (rT = b - A^T psi), preconditioned by the
+ * transpose of the DILU factorisation (the same rD, the lower and upper
+ * coefficients exchanged).  Per iteration: w = M^-1 r, wT = M^-T rT, rho =
+ * w.rT, p = w (+ beta p), pT = wT (+ beta pT), q = A p, qT = A^T pT, alpha =
+ * rho / (q.pT); the singularity test and the stopping rules are those of
+ * pcg() above. */
+static void pbicg(const rt_mesh_desc *m, const double *diag, const double *upper,
+                  const double *lower, const double *b, double *x,
+                  const rt_solver_ctl *ctl, rt_solver_perf *perf) {
+    const int N = m->nCells;
+    double *wA = DALLOC(N), *rA = DALLOC(N), *pA = DALLOC(N), *rD = DALLOC(N);
+    double *wT = DALLOC(N), *rT = DALLOC(N), *pT = DALLOC(N);
+    int pre = ctl->preconditioner;
+    if (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU) dilu_rd(m, diag, upper, lower, rD);
+    else if (pre == RT_PRECOND_DIAGONAL) for (int c = 0; c < N; ++c) rD[c] = 1.0 / diag[c];
+    amul(m, diag, upper, lower, x, wA);
+    amul(m, diag, lower, upper, x, wT);           /* A^T x: the coefficients exchanged */
+    for (int c = 0; c < N; ++c) {
+        rA[c] = b[c] - wA[c];
+        rT[c] = b[c] - wT[c];
+    }
+    double nf = norm_factor(m, diag, upper, lower, b, x, wA);
+    perf->initialResidual = sum_mag(rA, N) / nf;
+    perf->finalResidual = perf->initialResidual;
+    perf->nIterations = 0;
+    perf->singular = 0;
+    if (ctl->minIter > 0 || !conv_check(perf->finalResidual, perf->initialResidual, ctl)) {
+        double wArT = 1e20, wArTold;
+        do {
+            wArTold = wArT;
+            precondition(m, pre, rD, upper, lower, rA, wA);
+            precondition(m, pre, rD, lower, upper, rT, wT);   /* M^-T */
+            wArT = sum_prod(wA, rT, N);
+            if (perf->nIterations == 0) {
+                for (int c = 0; c < N; ++c) {
+                    pA[c] = wA[c];
+                    pT[c] = wT[c];
+                }
+            } else {
+                double beta = wArT / wArTold;
+                for (int c = 0; c < N; ++c) {
+                    pA[c] = wA[c] + beta * pA[c];
+                    pT[c] = wT[c] + beta * pT[c];
+                }
+            }
+            amul(m, diag, upper, lower, pA, wA);
+            amul(m, diag, lower, upper, pT, wT);
+            double wApT = sum_prod(wA, pT, N);
+            if (fabs(wApT) / nf < OR_VSMALL) { perf->singular = 1; break; }
+            double alpha = wArT / wApT;
+            for (int c = 0; c < N; ++c) {
+                x[c] += alpha * pA[c];
+                rA[c] -= alpha * wA[c];
+                rT[c] -= alpha * wT[c];
+            }
+            perf->finalResidual = sum_mag(rA, N) / nf;
+        } while ((++perf->nIterations < ctl->maxIter &&
+                  !conv_check(perf->finalResidual, perf->initialResidual, ctl) &&
+                  isfinite(perf->finalResidual)) ||
+                 perf->nIterations < ctl->minIter);
+    }
+    perf->converged = conv_check(perf->finalResidual, perf->initialResidual, ctl);
+    free(wA); free(rA); free(pA); free(rD); free(wT); free(rT); free(pT);
+}
+
 /* One component solve, lduMatrix::solver semantics. */
 int or_ldu_solve(const rt_mesh_desc *m, const double *diag, const double *upper,
                  const double *lower, const double *b, double *x,
                  const rt_solver_ctl *ctl, rt_solver_perf *perf) {
     if (ctl->solver == RT_SOLVER_PCG) pcg(m, diag, upper, lower, b, x, ctl, perf);
+    else if (ctl->solver == RT_SOLVER_PBICG) pbicg(m, diag, upper, lower, b, x, ctl, perf);
     else pbicgstab(m, diag, upper, lower, b, x, ctl, perf);
     return (isfinite(perf->finalResidual)) ? RT_OK : RT_ENAN;
 }
@@ -621,11 +692,21 @@ typedef struct {
     const rt_case_ctl *ctl;
     or_state *s;
     int *kU, *kP, *kTh, *kTau;
+    /* multiMode (nModes > 1): the modes' models and states (theta, tau and
+     * the eigen fields of each; U, p and phi are s's), and where each mode's
+     * theta solve records go (6 per mode, or NULL); s->tau is then the sum
+     * of the modes' tau and mp the summed-viscosity model of the momentum
+     * equation */
+    int nModes;
+    const rt_model_params *models;
+    or_state *modes;
+    rt_solver_perf *modePerf;
 } or_case;
 
 static void case_init(or_case *k, const rt_mesh_desc *m, const rt_bc_desc *bc,
                       const rt_model_params *mp, const rt_case_ctl *ctl, or_state *s) {
     k->m = m; k->bc = bc; k->mp = mp; k->ctl = ctl; k->s = s;
+    k->nModes = 1; k->models = NULL; k->modes = NULL; k->modePerf = NULL;
     int nB = m->nBFaces;
     k->kU = (int *)xcalloc(nB, sizeof(int)); k->kP = (int *)xcalloc(nB, sizeof(int));
     k->kTh = (int *)xcalloc(nB, sizeof(int)); k->kTau = (int *)xcalloc(nB, sizeof(int));
@@ -1032,6 +1113,54 @@ static void fvc_laplacian(const rt_mesh_desc *m, const double *U, const double *
 }
 
 /* ------------------------------------------------------------------------ */
+/* multiMode (multiMode.C:69-91, 144-156, 222, 247-256)                       */
+/* ------------------------------------------------------------------------ */
+/* correct() of every mode in turn, each with its own model and its own
+ * theta, tau and eigen fields on the common U and phi; then tau() = the sum
+ * of the modes' tau (internal and boundary values).  theta0s: the modes'
+ * old-time theta, mode after mode (NULL: their current theta).  perf gets the
+ * last mode's records, k->modePerf (if set) every mode's. */
+static int modes_correct(or_case *k, const double *gradU, rt_solver_perf *perf, const double *theta0s) {
+    const rt_mesh_desc *m = k->m;
+    or_state *s = k->s;
+    const size_t n6 = 6 * (size_t)m->nCells, b6 = 6 * (size_t)m->nBFaces;
+    int st = RT_OK;
+    for (int i = 0; i < k->nModes && st == RT_OK; ++i) {
+        or_state si = k->modes[i];
+        si.U = s->U; si.Ub = s->Ub; si.p = s->p; si.pb = s->pb; si.phi = s->phi; si.phib = s->phib;
+        or_case ki = *k;
+        ki.mp = &k->models[i];
+        ki.s = &si;
+        ki.nModes = 1;
+        rt_solver_perf *pi = k->modePerf ? k->modePerf + 6 * i : perf;
+        st = constitutive_correct(&ki, gradU, pi, theta0s ? theta0s + n6 * i : NULL);
+        if (pi != perf) memcpy(perf, pi, 6 * sizeof *perf);
+    }
+    memset(s->tau, 0, sizeof(double) * n6);
+    memset(s->taub, 0, sizeof(double) * b6);
+    for (int i = 0; i < k->nModes; ++i) {
+        for (size_t j = 0; j < n6; ++j) s->tau[j] += k->modes[i].tau[j];
+        for (size_t j = 0; j < b6; ++j) s->taub[j] += k->modes[i].taub[j];
+    }
+    return st;
+}
+
+/* The momentum equation of a multiMode model: the sum of the modes' divTau
+ * (multiMode.C:144-156).  With a common rho and stabilization it is one
+ * divTau with the summed tau (s->tau) and the summed etaS and etaP; mode 0's
+ * model carries the rest. */
+static rt_model_params modes_momentum_model(const rt_model_params *models, int nModes) {
+    rt_model_params e = models[0];
+    e.etaS = 0.0;
+    e.etaP = 0.0;
+    for (int i = 0; i < nModes; ++i) {
+        e.etaS += models[i].etaS;
+        e.etaP += models[i].etaP;
+    }
+    return e;
+}
+
+/* ------------------------------------------------------------------------ */
 /* one segregated rheoFoam step                                               */
 /* ------------------------------------------------------------------------ */
 /* One inner iteration of a time step: UEqn, pEqn and constEq.correct() with
@@ -1292,7 +1421,8 @@ static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const d
     free(U0); free(U0b); free(phi0); free(phi0b);
 
     /* ---------------- constEq.correct() ---------------- */
-    return constitutive_correct(k, NULL, perf->theta, theta0s);
+    if (k->nModes <= 1) return constitutive_correct(k, NULL, perf->theta, theta0s);
+    return modes_correct(k, NULL, perf->theta, theta0s);
 }
 
 /* One time step: nInIter inner iterations (rheoFoam.C:96-150; createControls.H
@@ -1301,11 +1431,15 @@ static int step_once(or_case *k, rt_step_perf *perf) {
     const rt_mesh_desc *m = k->m;
     or_state *s = k->s;
     const int N = m->nCells, nF = m->nFaces, nB = m->nBFaces;
+    const int nM = k->nModes > 1 ? k->nModes : 1;
     double *U0 = DALLOC(3 * (size_t)N), *U0b = DALLOC(3 * (size_t)nB);
-    double *phi0 = DALLOC(nF), *phi0b = DALLOC(nB), *theta0 = DALLOC(6 * (size_t)N);
+    double *phi0 = DALLOC(nF), *phi0b = DALLOC(nB), *theta0 = DALLOC(6 * (size_t)N * nM);
     memcpy(U0, s->U, sizeof(double) * 3 * N); memcpy(U0b, s->Ub, sizeof(double) * 3 * nB);
     memcpy(phi0, s->phi, sizeof(double) * nF); memcpy(phi0b, s->phib, sizeof(double) * nB);
-    memcpy(theta0, s->theta, sizeof(double) * 6 * N);
+    if (k->nModes > 1)
+        for (int i = 0; i < nM; ++i) memcpy(theta0 + 6 * (size_t)N * i, k->modes[i].theta, sizeof(double) * 6 * N);
+    else
+        memcpy(theta0, s->theta, sizeof(double) * 6 * N);
     const int nIn = k->ctl->nInIter > 1 ? k->ctl->nInIter : 1;
     int st = RT_OK;
     for (int it = 0; it < nIn && st == RT_OK; ++it) {
@@ -1331,6 +1465,50 @@ int or_step(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *
         }
     }
     if (perf) *perf = local;
+    case_free(&k);
+    return st;
+}
+
+/* nSteps rheoFoam steps of a multiMode model: models[nModes] (a common rho
+ * and stabilization), s the common fields (U, p, phi; tau and taub get the
+ * summed tau), modes[i] each mode's theta, tau and eigen fields; modePerf
+ * (6 per mode, or NULL) each mode's theta solve records of the last step. */
+int or_step_modes(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models, int nModes,
+                  const rt_case_ctl *ctl, or_state *s, or_state *modes, int nSteps, rt_step_perf *perf,
+                  rt_solver_perf *modePerf) {
+    if (nModes < 1) return RT_EINVAL;
+    for (int i = 1; i < nModes; ++i)
+        if (models[i].rho != models[0].rho || models[i].stabilization != models[0].stabilization) return RT_EINVAL;
+    rt_model_params eff = modes_momentum_model(models, nModes);
+    or_case k;
+    case_init(&k, m, bc, &eff, ctl, s);
+    k.nModes = nModes; k.models = models; k.modes = modes; k.modePerf = modePerf;
+    rt_step_perf local;
+    int st = RT_OK;
+    for (int i = 0; i < nSteps && st == RT_OK; ++i) {
+        memset(&local, 0, sizeof local);
+        st = step_once(&k, &local);
+        if (st == RT_OK) {
+            if (!isfinite(local.p.finalResidual)) st = RT_ENAN;
+            for (int j = 0; j < 3; ++j) if (local.U[j].nIterations >= 0 && !isfinite(local.U[j].finalResidual)) st = RT_ENAN;
+        }
+    }
+    if (perf) *perf = local;
+    case_free(&k);
+    return st;
+}
+
+/* correct() of a multiMode model on the common fields of s (the modes'
+ * fields in modes[]); s->tau gets the summed tau. */
+int or_constitutive_correct_modes(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models,
+                                  int nModes, const rt_case_ctl *ctl, or_state *s, or_state *modes,
+                                  const double *gradU, rt_solver_perf *modePerf) {
+    if (nModes < 1) return RT_EINVAL;
+    or_case k;
+    case_init(&k, m, bc, &models[0], ctl, s);
+    k.nModes = nModes; k.models = models; k.modes = modes; k.modePerf = modePerf;
+    rt_solver_perf last[6];
+    int st = modes_correct(&k, gradU, last, NULL);
     case_free(&k);
     return st;
 }

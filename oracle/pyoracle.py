@@ -65,6 +65,14 @@ def lib():
                               P(abi.rt_case_ctl), P(or_state), C.c_int, P(abi.rt_step_perf)]
         L.or_step.restype = C.c_int
         L.or_init_fields.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(or_state)]
+        L.or_step_modes.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params), C.c_int,
+                                    P(abi.rt_case_ctl), P(or_state), P(or_state), C.c_int, P(abi.rt_step_perf),
+                                    P(abi.rt_solver_perf)]
+        L.or_step_modes.restype = C.c_int
+        L.or_constitutive_correct_modes.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params),
+                                                    C.c_int, P(abi.rt_case_ctl), P(or_state), P(or_state), _dp,
+                                                    P(abi.rt_solver_perf)]
+        L.or_constitutive_correct_modes.restype = C.c_int
         _lib = L
     return _lib
 
@@ -82,23 +90,65 @@ def _state(f: Fields) -> or_state:
     return s
 
 
+def _mode_states(f: Fields):
+    """or_state array of a multiMode state's modes (their U, p and phi
+    pointers are the common fields')."""
+    arr = (or_state * len(f.modes))()
+    base = _state(f)
+    for i, m in enumerate(f.modes):
+        st = or_state()
+        for name, _ in or_state._fields_:
+            a = getattr(m, name, None)
+            if a is None:
+                setattr(st, name, getattr(base, name))
+            else:
+                assert a.dtype == np.float64 and a.flags.c_contiguous, name
+                setattr(st, name, a.ctypes.data_as(_dp))
+        arr[i] = st
+    return arr
+
+
 class Oracle:
     """FP64 CPU restatement of one case (same Case object as the GPU path)."""
 
     def __init__(self, case: Case, fields: Fields = None):
         self.case = case
         self.md, self.bd, self.mp, self.ctl = case.descriptors()
-        self.f = fields if fields is not None else Fields.zeros(case.mesh)
+        self.nModes = len(case.models)
+        self.models = case.mode_params()
+        self.f = fields if fields is not None else Fields.zeros(case.mesh, self.nModes)
         if fields is None:
             lib().or_init_fields(C.byref(self.md), C.byref(self.bd), C.byref(_state(self.f)))
+            if self.nModes > 1:
+                # every mode starts from the boundary values of theta and tau;
+                # the summed tau's boundary values are the modes' sum
+                for m in self.f.modes:
+                    m.thetab[...] = self.f.thetab
+                    m.taub[...] = self.f.taub
+                self.f.taub[...] = sum(m.taub for m in self.f.modes)
+        self.modePerf = (abi.rt_solver_perf * (6 * self.nModes))()
 
     def step(self, n: int = 1) -> abi.rt_step_perf:
         perf = abi.rt_step_perf()
-        st = lib().or_step(C.byref(self.md), C.byref(self.bd), C.byref(self.mp), C.byref(self.ctl),
-                           C.byref(_state(self.f)), int(n), C.byref(perf))
+        if self.nModes > 1:
+            st = lib().or_step_modes(C.byref(self.md), C.byref(self.bd), self.models, self.nModes,
+                                     C.byref(self.ctl), C.byref(_state(self.f)), _mode_states(self.f), int(n),
+                                     C.byref(perf), self.modePerf)
+        else:
+            st = lib().or_step(C.byref(self.md), C.byref(self.bd), C.byref(self.mp), C.byref(self.ctl),
+                               C.byref(_state(self.f)), int(n), C.byref(perf))
         if st != 0:
             raise RuntimeError(f"oracle step failed: {abi.STATUS_NAMES.get(st, st)}")
+        self._mode0_view()
         return perf
+
+    def _mode0_view(self):
+        """A multiMode state shows mode 0's theta and eigen fields at the top
+        level (tau there is the modes' sum)."""
+        if self.nModes > 1:
+            m0 = self.f.modes[0]
+            for name in ("theta", "thetab", "eigVals", "eigVecs"):
+                getattr(self.f, name)[...] = getattr(m0, name)
 
     def constitutive_correct(self, gradU: np.ndarray = None, thetaOld: np.ndarray = None):
         """One correct(); thetaOld (nCells, 6): the old-time theta of the
@@ -107,6 +157,16 @@ class Oracle:
         perf = (abi.rt_solver_perf * 6)()
         g = None if gradU is None else np.ascontiguousarray(gradU, dtype=np.float64)
         gp = None if g is None else g.ctypes.data_as(_dp)
+        if self.nModes > 1:
+            if thetaOld is not None:
+                raise ValueError("multiMode: inner iterations run inside step()")
+            st = lib().or_constitutive_correct_modes(C.byref(self.md), C.byref(self.bd), self.models, self.nModes,
+                                                     C.byref(self.ctl), C.byref(_state(self.f)),
+                                                     _mode_states(self.f), gp, self.modePerf)
+            if st != 0:
+                raise RuntimeError(f"oracle constitutive correct failed: {st}")
+            self._mode0_view()
+            return list(self.modePerf[6 * (self.nModes - 1):])
         if thetaOld is None:
             st = lib().or_constitutive_correct(C.byref(self.md), C.byref(self.bd), C.byref(self.mp),
                                                C.byref(self.ctl), C.byref(_state(self.f)), gp, perf)

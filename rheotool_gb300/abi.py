@@ -20,7 +20,7 @@ RT_BC_FIXED, RT_BC_ZEROGRAD, RT_BC_LINEXTRAP = 0, 1, 2
  RT_MODEL_ROLIEPOLY_LOG, RT_MODEL_XPOMPOM_LOG, RT_MODEL_WHITEMETZNERCY_LOG) = 0, 1, 2, 3, 4, 5, 6, 7
 RT_PTT_LINEAR, RT_PTT_EXP, RT_PTT_GENERALIZED = 0, 1, 2
 RT_STAB_NONE, RT_STAB_BSD, RT_STAB_COUPLING = 0, 1, 2
-RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB = 0, 1
+RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB, RT_SOLVER_PBICG = 0, 1, 2
 RT_PRECOND_NONE, RT_PRECOND_DIC, RT_PRECOND_DILU, RT_PRECOND_DIAGONAL = 0, 1, 2, 3
 RT_LIM_NONE, RT_LIM_UPWIND, RT_LIM_CUBISTA, RT_LIM_MINMOD, RT_LIM_SMART, RT_LIM_WACEB, RT_LIM_SUPERBEE = -1, 0, 1, 2, 3, 4, 5
 RT_PREC_FP64, RT_PREC_MIXED = 0, 1
@@ -34,6 +34,7 @@ RT_OPT_SWEEP_TUNE = 6
 RT_OPT_SWEEP_RING = 7
 RT_OPT_WAIT_LIMIT = 8
 RT_OPT_STALL_TEST = 9
+RT_MAX_MODES = 16
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 
 MODEL_NAMES = {
@@ -165,6 +166,10 @@ def load_library(path: str = LIBNAME):
         "rt_status_string": ([C.c_int32], C.c_char_p),
         "rt_mesh_upload": ([vp, P(rt_mesh_desc)], C.c_int32),
         "rt_case_setup": ([vp, P(rt_bc_desc), P(rt_model_params), P(rt_case_ctl)], C.c_int32),
+        "rt_case_setup_modes": ([vp, P(rt_bc_desc), P(rt_model_params), C.c_int32, P(rt_case_ctl)], C.c_int32),
+        "rt_field_set_mode": ([vp, C.c_int32, C.c_int32, _dp, _dp], C.c_int32),
+        "rt_field_get_mode": ([vp, C.c_int32, C.c_int32, _dp, _dp], C.c_int32),
+        "rt_mode_perf": ([vp, P(rt_solver_perf)], C.c_int32),
         "rt_field_set": ([vp, C.c_int32, _dp, _dp], C.c_int32),
         "rt_field_get": ([vp, C.c_int32, _dp, _dp], C.c_int32),
         "rt_ldu_solve": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int32, P(rt_solver_ctl), P(rt_solver_perf)], C.c_int32),

@@ -17,7 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
-from typing import Callable, Dict, Optional, Tuple, Union
+from typing import Callable, Dict, List, Optional, Tuple, Union
 
 import numpy as np
 
@@ -26,7 +26,7 @@ from .mesh import Mesh, cavity_mesh, contraction_mesh, channel_mesh, periodic_ch
 
 BC_KINDS = {"fixedValue": abi.RT_BC_FIXED, "zeroGradient": abi.RT_BC_ZEROGRAD,
             "linearExtrapolation": abi.RT_BC_LINEXTRAP}
-SOLVERS = {"PCG": abi.RT_SOLVER_PCG, "PBiCGStab": abi.RT_SOLVER_PBICGSTAB}
+SOLVERS = {"PCG": abi.RT_SOLVER_PCG, "PBiCGStab": abi.RT_SOLVER_PBICGSTAB, "PBiCG": abi.RT_SOLVER_PBICG}
 PRECONDS = {"none": abi.RT_PRECOND_NONE, "DIC": abi.RT_PRECOND_DIC,
             "DILU": abi.RT_PRECOND_DILU, "diagonal": abi.RT_PRECOND_DIAGONAL}
 STABS = {"none": abi.RT_STAB_NONE, "BSD": abi.RT_STAB_BSD, "coupling": abi.RT_STAB_COUPLING}
@@ -107,6 +107,22 @@ class Case:
     name: str = "case"
     bodyForce: Tuple[float, float, float] = (0.0, 0.0, 0.0)   # per unit mass, in UEqn
     nInIter: int = 1          # SIMPLE.nInIter: inner iterations per time step
+    # multiMode (multiMode.C:69-91): the modes after the first (``model``);
+    # every mode has its own theta, tau and eigen fields, tau is their sum
+    moreModes: List[Model] = field(default_factory=list)
+
+    @property
+    def models(self) -> List[Model]:
+        """The modes of the constitutive model (one for a single-mode model)."""
+        return [self.model] + list(self.moreModes)
+
+    def mode_params(self):
+        """ctypes array of every mode's rt_model_params."""
+        ms = self.models
+        arr = (abi.rt_model_params * len(ms))()
+        for i, m in enumerate(ms):
+            arr[i] = m.to_c()
+        return arr
 
     # ------------------------------------------------------------------
     def _field_bc(self, fld: str, ncomp: int):
@@ -339,14 +355,42 @@ class Fields:
     taub: np.ndarray
     eigVals: np.ndarray
     eigVecs: np.ndarray
+    # multiMode: every mode's constitutive fields (empty for a single-mode
+    # model); theta, eigVals and eigVecs above are then mode 0's and tau,
+    # taub the modes' sum (multiMode::tau())
+    modes: List["ModeFields"] = field(default_factory=list)
 
     @staticmethod
-    def zeros(mesh: Mesh) -> "Fields":
+    def zeros(mesh: Mesh, nModes: int = 1) -> "Fields":
         N, nF, nB = mesh.nCells, mesh.nFaces, mesh.nBFaces
         z = lambda *s: np.zeros(s)
-        return Fields(U=z(N, 3), Ub=z(nB, 3), p=z(N), pb=z(nB), phi=z(nF), phib=z(nB),
-                      theta=z(N, 6), thetab=z(nB, 6), tau=z(N, 6), taub=z(nB, 6),
-                      eigVals=np.ones((N, 3)), eigVecs=np.tile(np.eye(3).reshape(9), (N, 1)))
+        f = Fields(U=z(N, 3), Ub=z(nB, 3), p=z(N), pb=z(nB), phi=z(nF), phib=z(nB),
+                   theta=z(N, 6), thetab=z(nB, 6), tau=z(N, 6), taub=z(nB, 6),
+                   eigVals=np.ones((N, 3)), eigVecs=np.tile(np.eye(3).reshape(9), (N, 1)))
+        if nModes > 1:
+            f.modes = [ModeFields.zeros(mesh) for _ in range(nModes)]
+        return f
 
     def copy(self) -> "Fields":
-        return Fields(**{k: v.copy() for k, v in self.__dict__.items()})
+        return Fields(**{k: (v.copy() if isinstance(v, np.ndarray) else [m.copy() for m in v])
+                         for k, v in self.__dict__.items()})
+
+
+@dataclass
+class ModeFields:
+    """One mode's constitutive fields of a multiMode model."""
+    theta: np.ndarray
+    thetab: np.ndarray
+    tau: np.ndarray
+    taub: np.ndarray
+    eigVals: np.ndarray
+    eigVecs: np.ndarray
+
+    @staticmethod
+    def zeros(mesh: Mesh) -> "ModeFields":
+        N, nB = mesh.nCells, mesh.nBFaces
+        return ModeFields(np.zeros((N, 6)), np.zeros((nB, 6)), np.zeros((N, 6)), np.zeros((nB, 6)),
+                          np.ones((N, 3)), np.tile(np.eye(3).reshape(9), (N, 1)))
+
+    def copy(self) -> "ModeFields":
+        return ModeFields(**{k: v.copy() for k, v in self.__dict__.items()})

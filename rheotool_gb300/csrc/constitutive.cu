@@ -515,4 +515,36 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
     return st;
 }
 
+// tauTot = sum over the modes of tau (internal and boundary values)
+__global__ void k_add_into(size_t n, const double *__restrict__ a, double *__restrict__ acc, int first) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) acc[i] = first ? a[i] : acc[i] + a[i];
+}
+
+// multiMode correct() (multiMode.C:247-256): every mode's correct() in
+// turn on the common U and phi, each with its own model, theta, tau and eigen
+// fields; then tau() = the sum of the modes' tau (multiMode.C:222)
+rt_status modes_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf, const double *theta0s) {
+    DevCase &cs = ctx->cs;
+    if (cs.nModes <= 1) return constitutive_correct(ctx, gradU, perf, theta0s);
+    const int N = ctx->mesh.N, NB = ctx->mesh.NB;
+    const size_t n6 = 6 * (size_t)N, b6 = 6 * (size_t)NB;
+    cs.modePerf.assign(6 * (size_t)cs.nModes, rt_solver_perf{});
+    rt_status st = RT_OK;
+    for (int i = 0; i < cs.nModes && st == RT_OK; ++i) {
+        ModeSwap sw(cs, i > 0 ? cs.modes[i - 1].get() : nullptr);
+        st = constitutive_correct(ctx, gradU, &cs.modePerf[6 * (size_t)i], theta0s ? theta0s + n6 * i : nullptr);
+    }
+    for (int k = 0; k < 6; ++k) perf[k] = cs.modePerf[6 * (size_t)(cs.nModes - 1) + k];
+    cudaStream_t s = ctx->stream;
+    for (int i = 0; i < cs.nModes; ++i) {
+        const double *t = i ? cs.modes[i - 1]->tau.p : cs.tau.p, *tb = i ? cs.modes[i - 1]->taub.p : cs.taub.p;
+        k_add_into<<<nblocks((long long)n6), RT_BLOCK, 0, s>>>(n6, t, cs.tauTot.p, i == 0);
+        if (b6) k_add_into<<<nblocks((long long)b6), RT_BLOCK, 0, s>>>(b6, tb, cs.taubTot.p, i == 0);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, b6 ? 2 : 1);
+    }
+    return st;
+}
+
 }  // namespace rt

@@ -82,6 +82,27 @@ std::vector<double> aos_to_soa_host(const double *a, int n, int nc) {
     return o;
 }
 
+// the parameter checks of one constitutive model (each mode of a multiMode one)
+void validate_model(const rt_model_params *mp) {
+    RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_WHITEMETZNERCY_LOG, RT_EINVAL,
+               "unknown constitutive model");
+    RT_REQUIRE(mp->model != RT_MODEL_XPOMPOM_LOG || (mp->lambdaS > 0 && mp->q > 0), RT_EINVAL,
+               "XPomPom needs lambdaS > 0 and q > 0");
+    RT_REQUIRE(mp->model != RT_MODEL_WHITEMETZNERCY_LOG || mp->a > 0, RT_EINVAL, "WhiteMetznerCY needs a > 0");
+    const bool pttGen = mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED;
+    RT_REQUIRE(mp->model != RT_MODEL_PTT_LOG || (mp->pttFunction >= RT_PTT_LINEAR &&
+                                                 mp->pttFunction <= RT_PTT_GENERALIZED),
+               RT_EINVAL, "unknown PTT destruction function");
+    // PTTLog.C:147-152
+    RT_REQUIRE(!pttGen || (mp->alpha > 0 && mp->beta > 0), RT_EINVAL,
+               "Both alpha and beta should be positive values for the Mittag-Leffler function to converge.");
+    RT_REQUIRE(!pttGen || mp->maxIterMittagLeffler >= 1, RT_EINVAL, "maxIterMittagLeffler must be positive");
+    RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
+    RT_REQUIRE(mp->model != RT_MODEL_ROLIEPOLY_LOG || mp->lambdaR > 0, RT_EINVAL, "Rolie-Poly needs lambdaR > 0");
+    RT_REQUIRE((mp->model != RT_MODEL_FENEP_LOG && mp->model != RT_MODEL_FENECR_LOG) || mp->L2 > 3.0, RT_EINVAL,
+               "FENE-P and FENE-CR need L2 > 3");
+}
+
 }  // namespace
 
 namespace rt {
@@ -427,35 +448,30 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
     return guarded(ctx, [&]() -> rt_status {
         RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
         RT_REQUIRE(bc && mp && ctl, RT_EINVAL, "null argument");
-        RT_REQUIRE(mp->model >= RT_MODEL_OLDROYDB_LOG && mp->model <= RT_MODEL_WHITEMETZNERCY_LOG, RT_EINVAL,
-                   "unknown constitutive model");
-        RT_REQUIRE(mp->model != RT_MODEL_XPOMPOM_LOG || (mp->lambdaS > 0 && mp->q > 0), RT_EINVAL,
-                   "XPomPom needs lambdaS > 0 and q > 0");
-        RT_REQUIRE(mp->model != RT_MODEL_WHITEMETZNERCY_LOG || mp->a > 0, RT_EINVAL,
-                   "WhiteMetznerCY needs a > 0");
+        validate_model(mp);
         const bool pttGen = mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED;
-        RT_REQUIRE(mp->model != RT_MODEL_PTT_LOG || (mp->pttFunction >= RT_PTT_LINEAR &&
-                                                     mp->pttFunction <= RT_PTT_GENERALIZED),
-                   RT_EINVAL, "unknown PTT destruction function");
-        // PTTLog.C:147-152
-        RT_REQUIRE(!pttGen || (mp->alpha > 0 && mp->beta > 0), RT_EINVAL,
-                   "Both alpha and beta should be positive values for the Mittag-Leffler function to converge.");
-        RT_REQUIRE(!pttGen || mp->maxIterMittagLeffler >= 1, RT_EINVAL, "maxIterMittagLeffler must be positive");
         RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
-        RT_REQUIRE(mp->lambda > 0 && mp->rho > 0, RT_EINVAL, "lambda and rho must be positive");
-        RT_REQUIRE(mp->model != RT_MODEL_ROLIEPOLY_LOG || mp->lambdaR > 0, RT_EINVAL,
-                   "Rolie-Poly needs lambdaR > 0");
+        for (const rt_solver_ctl *sc : {&ctl->solverU, &ctl->solverP, &ctl->solverTheta}) {
+            RT_REQUIRE(sc->solver >= RT_SOLVER_PCG && sc->solver <= RT_SOLVER_PBICG, RT_EINVAL, "unknown solver");
+            RT_REQUIRE(sc->preconditioner >= RT_PRECOND_NONE && sc->preconditioner <= RT_PRECOND_DIAGONAL, RT_EINVAL,
+                       "unknown preconditioner");
+        }
         RT_REQUIRE(ctl->divU >= RT_LIM_NONE && ctl->divU <= RT_LIM_SUPERBEE &&
                        ctl->divTheta >= RT_LIM_NONE && ctl->divTheta <= RT_LIM_SUPERBEE,
                    RT_EINVAL, "unknown GaussDefCmpw limiter");
-        RT_REQUIRE((mp->model != RT_MODEL_FENEP_LOG && mp->model != RT_MODEL_FENECR_LOG) || mp->L2 > 3.0, RT_EINVAL,
-                   "FENE-P and FENE-CR need L2 > 3");
         DevMesh &m = ctx->mesh;
         DevCase &c = ctx->cs;
         RT_REQUIRE(ctl->pRefCell >= 0 && ctl->pRefCell < m.N, RT_EINVAL, "pRefCell out of range");
         c.mp = *mp;
         c.ctl = *ctl;
         c.thetaOldSaved = false;
+        c.nModes = 1;            // rt_case_setup_modes adds the further modes
+        c.modes.clear();
+        c.tauTot.release();
+        c.taubTot.release();
+        c.thetaStep0.release();
+        c.modePerf.clear();
+        c.mpMom = *mp;
         if (pttGen) {
             std::vector<double> g = ml_gamma_table(*mp);
             c.mlK = (int)g.size() - 1;
@@ -514,7 +530,11 @@ static void field_info(rt_ctx *ctx, int field, DBuf<double> **in, DBuf<double> *
     case RT_FIELD_P: *in = &c.p; *bd = &c.pb; *nc = 1; break;
     case RT_FIELD_PHI: *in = &c.phi; *bd = &c.phib; *nc = 1; *nIn = ctx->mesh.F; break;
     case RT_FIELD_THETA: *in = &c.theta; *bd = &c.thetab; *nc = 6; break;
-    case RT_FIELD_TAU: *in = &c.tau; *bd = &c.taub; *nc = 6; break;
+    case RT_FIELD_TAU:   // multiMode: the modes' summed tau (multiMode::tau())
+        *in = c.nModes > 1 ? &c.tauTot : &c.tau;
+        *bd = c.nModes > 1 ? &c.taubTot : &c.taub;
+        *nc = 6;
+        break;
     case RT_FIELD_EIGVALS: *in = &c.eigVals; *bd = nullptr; *nc = 3; break;
     case RT_FIELD_EIGVECS: *in = &c.eigVecs; *bd = nullptr; *nc = 9; break;
     default: throw Error{RT_EINVAL, "unknown field id"};
@@ -535,6 +555,158 @@ rt_status rt_field_set(rt_ctx *ctx, int32_t field, const double *internal, const
             upload_soa(ctx, boundary, ctx->mesh.NB, nc, *bd);
         }
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return RT_OK;
+    });
+}
+
+// one mode's theta / tau / eigVals / eigVecs of a multiMode case
+static void mode_field_info(rt_ctx *ctx, int field, int mode, DBuf<double> **in, DBuf<double> **bd, int *nc) {
+    DevCase &c = ctx->cs;
+    RT_REQUIRE(mode >= 0 && mode < c.nModes, RT_EINVAL, "mode out of range");
+    RT_REQUIRE(field == RT_FIELD_THETA || field == RT_FIELD_TAU || field == RT_FIELD_EIGVALS ||
+                   field == RT_FIELD_EIGVECS,
+               RT_EINVAL, "per-mode fields: theta, tau, eigVals, eigVecs");
+    if (mode == 0 || c.nModes == 1) {
+        switch (field) {
+        case RT_FIELD_THETA: *in = &c.theta; *bd = &c.thetab; *nc = 6; return;
+        case RT_FIELD_TAU: *in = &c.tau; *bd = &c.taub; *nc = 6; return;
+        case RT_FIELD_EIGVALS: *in = &c.eigVals; *bd = nullptr; *nc = 3; return;
+        default: *in = &c.eigVecs; *bd = nullptr; *nc = 9; return;
+        }
+    }
+    ModeState &m = *c.modes[mode - 1];
+    switch (field) {
+    case RT_FIELD_THETA: *in = &m.theta; *bd = &m.thetab; *nc = 6; return;
+    case RT_FIELD_TAU: *in = &m.tau; *bd = &m.taub; *nc = 6; return;
+    case RT_FIELD_EIGVALS: *in = &m.eigVals; *bd = nullptr; *nc = 3; return;
+    default: *in = &m.eigVecs; *bd = nullptr; *nc = 9; return;
+    }
+}
+
+rt_status rt_field_set_mode(rt_ctx *ctx, int32_t field, int32_t mode, const double *internal,
+                            const double *boundary) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
+        DBuf<double> *in, *bd;
+        int nc;
+        mode_field_info(ctx, field, mode, &in, &bd, &nc);
+        if (internal) upload_soa(ctx, internal, ctx->mesh.N, nc, *in);
+        if (field == RT_FIELD_THETA && internal) {
+            if (mode == 0) ctx->cs.thetaOldSaved = false;
+            else ctx->cs.modes[mode - 1]->thetaOldSaved = false;
+        }
+        if (boundary) {
+            RT_REQUIRE(bd != nullptr, RT_EINVAL, "field has no boundary values");
+            upload_soa(ctx, boundary, ctx->mesh.NB, nc, *bd);
+        }
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        return RT_OK;
+    });
+}
+
+rt_status rt_field_get_mode(rt_ctx *ctx, int32_t field, int32_t mode, double *internal, double *boundary) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
+        DBuf<double> *in, *bd;
+        int nc;
+        mode_field_info(ctx, field, mode, &in, &bd, &nc);
+        if (internal) download_aos(ctx, *in, ctx->mesh.N, nc, internal);
+        if (boundary) {
+            RT_REQUIRE(bd != nullptr, RT_EINVAL, "field has no boundary values");
+            download_aos(ctx, *bd, ctx->mesh.NB, nc, boundary);
+        }
+        return RT_OK;
+    });
+}
+
+rt_status rt_mode_perf(rt_ctx *ctx, rt_solver_perf *thetaPerf) {
+    return guarded(ctx, [&]() -> rt_status {
+        RT_REQUIRE(thetaPerf, RT_EINVAL, "null argument");
+        DevCase &c = ctx->cs;
+        RT_REQUIRE(c.ready, RT_ENOTREADY, "case not set up");
+        RT_REQUIRE(c.nModes > 1 && c.modePerf.size() == 6 * (size_t)c.nModes, RT_ENOTREADY,
+                   "no multiMode correct() has run");
+        for (size_t i = 0; i < c.modePerf.size(); ++i) thetaPerf[i] = c.modePerf[i];
+        return RT_OK;
+    });
+}
+
+rt_status rt_case_setup_modes(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params *models, int32_t nModes,
+                              const rt_case_ctl *ctl) {
+    {
+        rt_status v = guarded(ctx, [&]() -> rt_status {
+            RT_REQUIRE(models && nModes >= 1 && nModes <= RT_MAX_MODES, RT_EINVAL,
+                       "multiMode: 1 .. " + std::to_string(RT_MAX_MODES) + " modes");
+            RT_REQUIRE(ctx->mesh.batch.n <= 1, RT_EINVAL, "the batched form runs single-mode models");
+            for (int i = 0; i < nModes; ++i) {
+                validate_model(&models[i]);
+                // one divTau with the summed tau and viscosities (multiMode.C:144-156)
+                RT_REQUIRE(models[i].rho == models[0].rho && models[i].stabilization == models[0].stabilization,
+                           RT_EINVAL, "multiMode: every mode needs the same rho and stabilization");
+            }
+            return RT_OK;
+        });
+        if (v != RT_OK) return v;
+    }
+    rt_status st = rt_case_setup(ctx, bc, &models[0], ctl);
+    if (st != RT_OK || nModes == 1) return st;
+    return guarded(ctx, [&]() -> rt_status {
+        DevCase &c = ctx->cs;
+        const int N = ctx->mesh.N, NB = ctx->mesh.NB;
+        const size_t n6 = 6 * (size_t)N, b6 = 6 * (size_t)NB;
+        cudaStream_t s = ctx->stream;
+        c.ready = false;
+        for (int i = 1; i < nModes; ++i) {
+            std::unique_ptr<ModeState> m(new ModeState());
+            m->mp = models[i];
+            // every mode starts as mode 0 did: theta = tau = 0, A = I, the
+            // boundary values of the theta and tau conditions
+            m->theta.alloc(n6); m->theta.zero(s);
+            m->tau.alloc(n6); m->tau.zero(s);
+            m->thetab.alloc(b6); m->taub.alloc(b6);
+            if (b6) {
+                RT_CUDA(cudaMemcpyAsync(m->thetab.p, c.thetab.p, sizeof(double) * b6, cudaMemcpyDeviceToDevice, s));
+                RT_CUDA(cudaMemcpyAsync(m->taub.p, c.taub.p, sizeof(double) * b6, cudaMemcpyDeviceToDevice, s));
+            }
+            m->eigVals.alloc(3 * (size_t)N);
+            m->eigVecs.alloc(9 * (size_t)N);
+            RT_CUDA(cudaMemcpyAsync(m->eigVals.p, c.eigVals.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+            RT_CUDA(cudaMemcpyAsync(m->eigVecs.p, c.eigVecs.p, sizeof(double) * 9 * N, cudaMemcpyDeviceToDevice, s));
+            if (models[i].model == RT_MODEL_PTT_LOG && models[i].pttFunction == RT_PTT_GENERALIZED) {
+                std::vector<double> g = ml_gamma_table(models[i]);
+                m->mlK = (int)g.size() - 1;
+                RT_REQUIRE(m->mlK >= 1, RT_EINVAL, "Gamma(beta) overflows: no Mittag-Leffler term");
+                upload_vec(ctx, g, m->mlGamma);
+            }
+            c.modes.push_back(std::move(m));
+        }
+        c.nModes = nModes;
+        rt_model_params e = models[0];
+        e.etaS = 0.0;
+        e.etaP = 0.0;
+        for (int i = 0; i < nModes; ++i) {
+            e.etaS += models[i].etaS;
+            e.etaP += models[i].etaP;
+        }
+        c.mpMom = e;
+        // tau() of the initial state: the modes' sum
+        c.tauTot.alloc(n6);
+        c.tauTot.zero(s);
+        c.taubTot.alloc(b6);
+        c.taubTot.zero(s);
+        for (int i = 0; i < nModes && b6; ++i) {
+            const double *tb = i ? c.modes[i - 1]->taub.p : c.taub.p;
+            // taubTot += taub_i (through the host: setup only)
+            std::vector<double> h(b6), acc(b6);
+            RT_CUDA(cudaMemcpyAsync(h.data(), tb, sizeof(double) * b6, cudaMemcpyDeviceToHost, s));
+            RT_CUDA(cudaMemcpyAsync(acc.data(), c.taubTot.p, sizeof(double) * b6, cudaMemcpyDeviceToHost, s));
+            RT_CUDA(cudaStreamSynchronize(s));
+            for (size_t j = 0; j < b6; ++j) acc[j] += h[j];
+            RT_CUDA(cudaMemcpyAsync(c.taubTot.p, acc.data(), sizeof(double) * b6, cudaMemcpyHostToDevice, s));
+            RT_CUDA(cudaStreamSynchronize(s));
+        }
+        RT_CUDA(cudaStreamSynchronize(s));
+        c.ready = true;
         return RT_OK;
     });
 }
@@ -561,7 +733,7 @@ rt_status rt_ldu_solve(rt_ctx *ctx, const double *diag, const double *upper, con
         RT_REQUIRE(ctx->meshReady, RT_ENOTREADY, "mesh not uploaded");
         RT_REQUIRE(ncmpt >= 1 && ncmpt <= 6, RT_EINVAL, "ncmpt must be 1..6");
         RT_REQUIRE(diag && upper && lower && source && psi && ctl && perf, RT_EINVAL, "null argument");
-        RT_REQUIRE(ctl->solver == RT_SOLVER_PCG || ctl->solver == RT_SOLVER_PBICGSTAB, RT_EINVAL, "unknown solver");
+        RT_REQUIRE(ctl->solver >= RT_SOLVER_PCG && ctl->solver <= RT_SOLVER_PBICG, RT_EINVAL, "unknown solver");
         RT_REQUIRE(ctl->preconditioner >= RT_PRECOND_NONE && ctl->preconditioner <= RT_PRECOND_DIAGONAL,
                    RT_EINVAL, "unknown preconditioner");
         const int N = ctx->mesh.N, F = ctx->mesh.F;
@@ -637,7 +809,7 @@ rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_pe
         // a completed time step: the old-time theta kept by
         // rt_constitutive_correct_iter belongs to an earlier step now
         ctx->cs.thetaOldSaved = false;
-        rt_status st = constitutive_correct(ctx, gradU ? g.p : nullptr, thetaPerf);
+        rt_status st = modes_correct(ctx, gradU ? g.p : nullptr, thetaPerf);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
         return st;
     });
@@ -649,6 +821,9 @@ rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t
         DevCase &c = ctx->cs;
         RT_REQUIRE(c.ready, RT_ENOTREADY, "case not set up");
         RT_REQUIRE(thetaPerf, RT_EINVAL, "null perf");
+        RT_REQUIRE(c.nModes == 1, RT_EINVAL,
+                   "rt_constitutive_correct_iter runs single-mode models (a multiMode step's inner iterations "
+                   "run inside rt_step)");
         const size_t n6 = 6 * (size_t)ctx->mesh.N;
         if (newTimeStep) {
             c.thetaOld.alloc(n6);

@@ -486,12 +486,13 @@ struct Solver {
 
     static int pop(unsigned m) { return __builtin_popcount(m); }
 
-    void amul(unsigned mask, const double *x, double *y) {
+    // y = A x, or with T the transposed product A^T x (coefficients exchanged)
+    void amul(unsigned mask, const double *x, double *y, bool T = false) {
         // algorithmic bytes per cell: diag 8, lower+upper 2*(F/N)*8, face
         // addressing 2*(F/N)*4, x and y 16 per component
         const double fpc = (double)ctx->mesh.F / N;
         ProfScope ps(ctx, "amul", (double)N * (8.0 + fpc * 24.0 + 16.0 * pop(mask)));
-        k_amul<<<nblocks(N), RT_BLOCK, 0, st>>>(e, mask, a.diag, a.upper, a.lower, x, y);
+        k_amul<<<nblocks(N), RT_BLOCK, 0, st>>>(e, mask, a.diag, T ? a.lower : a.upper, T ? a.upper : a.lower, x, y);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
     }
@@ -537,9 +538,12 @@ struct Solver {
         }
     }
 
-    void precondition(unsigned mask, const double *rD, const double *r, double *w) {
+    // w = M^-1 r, or with T the transposed preconditioner M^-T r (the same rD,
+    // the lower and upper coefficients exchanged; PBiCG's shadow system)
+    void precondition(unsigned mask, const double *rD, const double *r, double *w, bool T = false) {
         const DevMesh &m = ctx->mesh;
         int pre = a.ctl.preconditioner;
+        const double *lower = T ? a.upper : a.lower, *upper = T ? a.lower : a.upper;
         if (pre == RT_PRECOND_NONE) {
             k_copy<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, r, w);
             launch_count(ctx);
@@ -551,7 +555,8 @@ struct Solver {
             // no addressing), r 8 + w 8 + the forward result 16 per component
             const double fpc = (double)m.F / N;
             ProfScope ps(ctx, "dilu_precondition", (double)N * (8.0 + fpc * 16.0 + 32.0 * pop(mask)));
-            skew_precondition(ctx, a.nc, mask, r, w);
+            if (T) skew_precondition_T(ctx, a.nc, mask, r, w);
+            else skew_precondition(ctx, a.nc, mask, r, w);
         } else {
             // per application (forward + backward): rD 16, coefficients
             // 2*(F/N)*8, addressing 2*(F/N)*8, r 8 + w 8 + w 16 per component
@@ -560,12 +565,12 @@ struct Solver {
             for (int l = 0; l < m.nLevels; ++l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
                 k_fwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, mask, rD,
-                                                                   a.lower, r, w);
+                                                                   lower, r, w);
             }
             for (int l = m.nLevels - 1; l >= 0; --l) {
                 int l0 = m.levelStartH[l], l1 = m.levelStartH[l + 1];
                 k_bwd_level<<<nblocks(l1 - l0), RT_BLOCK, 0, st>>>(pe, l0, l1, m.levelCells.p, mask, rD,
-                                                                   a.upper, w);
+                                                                   upper, w);
             }
             launch_count(ctx, 2 * m.nLevels);
         }
@@ -650,6 +655,133 @@ rt_status run_pcg(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         }
     }
     (void)h;
+    return RT_OK;
+}
+
+// rT = b - A^T psi on the masked components
+__global__ void k_sub(int N, unsigned mask, const double *__restrict__ b, const double *__restrict__ y,
+                      double *__restrict__ r) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k)
+        if ((mask >> k) & 1u) r[(size_t)k * N + c] = b[(size_t)k * N + c] - y[(size_t)k * N + c];
+}
+
+// PBiCG: pA = wA (+ beta pA), pT = wT (+ beta pT), beta = wArT / wArTold
+__global__ void k_pbicg_p(int N, unsigned mask, int first, const double *__restrict__ S,
+                          const double *__restrict__ wA, const double *__restrict__ wT, double *__restrict__ pA,
+                          double *__restrict__ pT) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        size_t i = (size_t)k * N + c;
+        if (first) {
+            pA[i] = wA[i];
+            pT[i] = wT[i];
+        } else {
+            double beta = S[S_A * 8 + k] / S[S_AOLD * 8 + k];
+            pA[i] = wA[i] + beta * pA[i];
+            pT[i] = wT[i] + beta * pT[i];
+        }
+    }
+}
+
+// PBiCG: psi += alpha pA; rA -= alpha wA; rT -= alpha wT; partial |rA|
+__global__ void k_pbicg_update(int N, unsigned mask, const double *__restrict__ S, const double *__restrict__ pA,
+                               const double *__restrict__ wA, const double *__restrict__ wT,
+                               double *__restrict__ psi, double *__restrict__ rA, double *__restrict__ rT,
+                               double *partial, int nB) {
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const bool sing = S[S_SING * 8 + k] != 0.0;
+        const double alpha = S[S_ALPHA * 8 + k];
+        double v = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            if (!sing) {
+                psi[o + c] += alpha * pA[o + c];
+                rA[o + c] -= alpha * wA[o + c];
+                rT[o + c] -= alpha * wT[o + c];
+            }
+            v += fabs(rA[o + c]);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+}
+
+// Preconditioned bi-conjugate gradients, OpenFOAM's PBiCG (the U and theta
+// solver of rheoTool's Contraction41 tutorials, fvSolution:32,47): the
+// shadow system is the transposed one with the same source (rT = b - A^T
+// psi), preconditioned by the transposed DILU factorisation; per iteration
+// wA = M^-1 rA, wT = M^-T rT, wArT = wA.rT, pA/pT updates with beta =
+// wArT/wArTold, wA = A pA, wT = A^T pT, alpha = wArT / (wA.pT).  Stopping
+// and singularity rules as run_pcg.
+rt_status run_pbicg(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    Solver sv(ctx, a);
+    const int N = sv.N;
+    const size_t V6 = 6 * (size_t)N;
+    double *ws = ctx->kws.p;
+    double *wA = ws, *rA = ws + V6, *pA = ws + 2 * V6, *wT = ws + 3 * V6, *rT = ws + 4 * V6, *pT = ws + 5 * V6,
+           *rD = ws + 48 * (size_t)N;
+    const unsigned mask = a.validMask;
+    sv.compute_rd(rD);
+    if (sv.systolic()) skew_prepare_T(ctx, a.upper, a.lower);
+    sv.prologue(mask, wA, rA);
+    sv.amul(mask, a.psi, wT, true);
+    k_sub<<<nblocks(N), RT_BLOCK, 0, sv.st>>>(N, mask, a.source, wT, rT);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, sv.S, sizeof(double) * 3 * 8, cudaMemcpyDeviceToHost, sv.st));
+    RT_CUDA(cudaStreamSynchronize(sv.st));
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        perf[k].initialResidual = ctx->red.hostResult[S_INIT * 8 + k];
+        perf[k].finalResidual = ctx->red.hostResult[S_FIN * 8 + k];
+        perf[k].nIterations = 0;
+        perf[k].singular = 0;
+    }
+    unsigned active = 0;
+    for (int k = 0; k < 6; ++k)
+        if (((mask >> k) & 1u) && (a.ctl.minIter > 0 || !sv.conv(perf[k].finalResidual, perf[k].initialResidual)))
+            active |= 1u << k;
+    int iter = 0;
+    while (active) {
+        sv.precondition(active, rD, rA, wA);
+        sv.precondition(active, rD, rT, wT, true);
+        sv.dot(active, wA, rT);
+        k_sc_pcg_a<<<1, 32, 0, sv.st>>>(active, ctx->red.result.p, sv.S);   // wArTold, wArT
+        k_pbicg_p<<<nblocks(N), RT_BLOCK, 0, sv.st>>>(N, active, iter == 0, sv.S, wA, wT, pA, pT);
+        sv.amul(active, pA, wA);
+        sv.amul(active, pT, wT, true);
+        sv.dot(active, wA, pT);
+        k_sc_pcg_alpha<<<1, 32, 0, sv.st>>>(active, ctx->red.result.p, sv.S);   // singularity, alpha
+        k_pbicg_update<<<sv.nB, RT_BLOCK, 0, sv.st>>>(N, active, sv.S, pA, wA, wT, a.psi, rA, rT,
+                                                      ctx->red.partial.p, sv.nB);
+        RT_CHECK_LAUNCH();
+        sv.finalize(1, active);
+        k_sc_fin<<<1, 32, 0, sv.st>>>(active, ctx->red.result.p, sv.S);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 4);
+        RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, sv.S, sizeof(double) * (S_SING + 1) * 8,
+                                cudaMemcpyDeviceToHost, sv.st));
+        RT_CUDA(cudaStreamSynchronize(sv.st));
+        const double *H = ctx->red.hostResult;
+        ++iter;
+        for (int k = 0; k < 6; ++k) {
+            if (!((active >> k) & 1u)) continue;
+            if (H[S_SING * 8 + k] != 0.0) {
+                perf[k].singular = 1;
+                active &= ~(1u << k);
+                continue;
+            }
+            perf[k].finalResidual = H[S_FIN * 8 + k];
+            perf[k].nIterations = iter;
+            bool more = (iter < a.ctl.maxIter && !sv.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
+                        iter < a.ctl.minIter;
+            if (!more || !std::isfinite(perf[k].finalResidual)) active &= ~(1u << k);
+        }
+    }
     return RT_OK;
 }
 
@@ -1362,10 +1494,15 @@ rt_status ldu_solve_device(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf
     b.validMask = mask;
     rt_status st = RT_OK;
     if (mask && ctx->mesh.batch.n > 1) {
+        RT_REQUIRE(a.ctl.solver != RT_SOLVER_PBICG, RT_EINVAL, "the batched form runs PCG and PBiCGStab, not PBiCG");
         st = batch_solve(ctx, b, perf);
     } else if (mask) {
         const bool pcg = a.ctl.solver == RT_SOLVER_PCG;
-        if (a.precision == RT_PREC_MIXED && (ctx->mixedParts & 1)) {
+        if (a.ctl.solver == RT_SOLVER_PBICG) {
+            // (FP64 in both forms: the mixed form's FP32 iterations are built
+            // for PCG and PBiCGStab)
+            st = run_pbicg(ctx, b, perf);
+        } else if (a.precision == RT_PREC_MIXED && (ctx->mixedParts & 1)) {
             SolveArgs t = b;
             t.ctl.tolerance *= ctx->mixedTighten;
             t.ctl.relTol *= ctx->mixedTighten;

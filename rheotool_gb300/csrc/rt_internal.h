@@ -9,7 +9,9 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/rheogpu.h"
@@ -133,6 +135,18 @@ struct StructMesh {
         v.wS = p + (size_t)12 * nSkew;
         v.rS = p + (size_t)18 * nSkew;
         v.w64 = nullptr;
+        return v;
+    }
+
+    // the premultiplied coefficients of the transposed factorisation (the
+    // lower and upper coefficients exchanged, the same rD): PBiCG's M^-T,
+    // allocated on first use
+    DBuf<double> dataT;
+    SkewView viewT() {
+        if (dataT.n != (size_t)6 * nSkew) dataT.alloc((size_t)6 * nSkew);
+        SkewView v = view();
+        double **slots[] = {&v.Az, &v.Ay, &v.Ax, &v.Bz, &v.By, &v.Bx};
+        for (int i = 0; i < 6; ++i) *slots[i] = dataT.p + (size_t)i * nSkew;
         return v;
     }
 
@@ -263,6 +277,56 @@ struct DevCase {
     // generalized PTT: Gamma(beta), Gamma(alpha k + beta) for k < mlK (else empty, mlK = 0)
     DBuf<double> mlGamma;
     int mlK = 0;
+    // multiMode (nModes > 1): mode 0 lives in the fields above, modes 1 ..
+    // nModes - 1 in `modes`; a mode's correct() swaps its state in (ModeSwap).
+    // The momentum equation reads the summed tau (tauTot, taubTot) and the
+    // summed-viscosity model mpMom; thetaStep0 keeps every mode's theta at
+    // the start of a step with inner iterations.
+    int nModes = 1;
+    std::vector<std::unique_ptr<struct ModeState>> modes;
+    DBuf<double> tauTot, taubTot, thetaStep0;
+    rt_model_params mpMom{};
+    std::vector<rt_solver_perf> modePerf;   // 6 per mode: the last correct()'s theta solves
+};
+
+// one further mode of a multiMode model: the DevCase's per-mode members
+struct ModeState {
+    rt_model_params mp{};
+    DBuf<double> theta, thetab, tau, taub, eigVals, eigVecs, thetaOld, mlGamma;
+    bool thetaOldSaved = false;
+    int mlK = 0;
+};
+
+template <class T>
+void swap_buf(DBuf<T> &a, DBuf<T> &b) {
+    std::swap(a.p, b.p);
+    std::swap(a.n, b.n);
+}
+
+// exchanges a mode's state with the DevCase's own per-mode members for the
+// guard's lifetime (constitutive_correct then works on that mode)
+struct ModeSwap {
+    DevCase &cs;
+    ModeState *ms;
+    static void swap_all(DevCase &c, ModeState &m) {
+        std::swap(c.mp, m.mp);
+        swap_buf(c.theta, m.theta);
+        swap_buf(c.thetab, m.thetab);
+        swap_buf(c.tau, m.tau);
+        swap_buf(c.taub, m.taub);
+        swap_buf(c.eigVals, m.eigVals);
+        swap_buf(c.eigVecs, m.eigVecs);
+        swap_buf(c.thetaOld, m.thetaOld);
+        swap_buf(c.mlGamma, m.mlGamma);
+        std::swap(c.thetaOldSaved, m.thetaOldSaved);
+        std::swap(c.mlK, m.mlK);
+    }
+    ModeSwap(DevCase &c, ModeState *m) : cs(c), ms(m) {
+        if (ms) swap_all(cs, *ms);
+    }
+    ~ModeSwap() {
+        if (ms) swap_all(cs, *ms);
+    }
 };
 
 // scratch arrays of the step, allocated once per mesh
@@ -374,6 +438,10 @@ void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double 
 // iterations); null = the current theta
 rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf,
                                const double *thetaOld = nullptr);
+
+// correct() of every mode of a multiMode model (or the one mode), then the
+// summed tau; theta0s: the modes' old-time theta, mode after mode (or null)
+rt_status modes_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf, const double *theta0s = nullptr);
 
 // step.cu
 rt_status step_once(rt_ctx *ctx, rt_step_perf *perf);

@@ -563,11 +563,15 @@ static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, c
         convection(ctx, ctl.divU, 3, cs.phi.p, cs.phib.p, cs.U.p, cs.Ub.p, cs.bkU.p, G, lower, upper, diagC, srcC,
                    intC, bouC, flux);
     }
-    const MomCoef mc = mom_coef(mp);
+    // (multiMode: the summed divTau of the modes, one divTau with the summed
+    // tau and viscosities, multiMode.C:144-156)
+    const bool multi = cs.nModes > 1;
+    const MomCoef mc = mom_coef(multi ? cs.mpMom : mp);
     const double gam = mc.gam;
     double *expl = W.take(3 * (size_t)N);
     ProfScope psMom(ctx, "mom_assembly", (double)N * (48.0 + 72.0 + 24.0 + 24.0 + 8.0 + 24.0 + 24.0 + 24.0 + 8.0 + 24.0) + F * 32.0);
-    k_divtau_expl<<<gN, RT_BLOCK, 0, s>>>(m, mc, cs.tau.p, cs.taub.p, G, cs.U.p, cs.Ub.p, expl);
+    k_divtau_expl<<<gN, RT_BLOCK, 0, s>>>(m, mc, multi ? cs.tauTot.p : cs.tau.p, multi ? cs.taubTot.p : cs.taub.p, G,
+                                          cs.U.p, cs.Ub.p, expl);
     double *diag = W.take(N), *src = W.take(3 * (size_t)N);
     const double3 body = make_double3(ctl.bodyForce[0], ctl.bodyForce[1], ctl.bodyForce[2]);
     k_mom_cell<<<gN, RT_BLOCK, 0, s>>>(m, rDeltaT, gam, diagC, srcC, U0, expl, body, diag, src);
@@ -659,7 +663,7 @@ static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, c
     perf->contErrGlobal = 0.0;
 
     // ---------------- constEq.correct() ----------------
-    return constitutive_correct(ctx, nullptr, perf->theta, theta0);
+    return modes_correct(ctx, nullptr, perf->theta, theta0);
 }
 
 // one time step: nInIter inner iterations (rheoFoam.C:96-150; 0 means 1)
@@ -678,7 +682,15 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     if (F) RT_CUDA(cudaMemcpyAsync(phi0, cs.phi.p, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
     if (NB) RT_CUDA(cudaMemcpyAsync(phi0b, cs.phib.p, sizeof(double) * NB, cudaMemcpyDeviceToDevice, s));
     double *theta0 = nullptr;
-    if (nIn > 1) {
+    if (nIn > 1 && cs.nModes > 1) {
+        // every mode's theta at the start of the step
+        const size_t n6 = 6 * (size_t)N;
+        cs.thetaStep0.alloc(n6 * cs.nModes);
+        theta0 = cs.thetaStep0.p;
+        for (int i = 0; i < cs.nModes; ++i)
+            RT_CUDA(cudaMemcpyAsync(theta0 + n6 * i, i ? cs.modes[i - 1]->theta.p : cs.theta.p, sizeof(double) * n6,
+                                    cudaMemcpyDeviceToDevice, s));
+    } else if (nIn > 1) {
         theta0 = W.take(6 * (size_t)N);
         RT_CUDA(cudaMemcpyAsync(theta0, cs.theta.p, sizeof(double) * 6 * N, cudaMemcpyDeviceToDevice, s));
     }

@@ -912,6 +912,27 @@ void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, doub
     launch_mode<double, 1>(ctx, g, nc, mask, w);
 }
 
+void skew_prepare_T(rt_ctx *ctx, const double *upper, const double *lower) {
+    StructMesh &s = ctx->mesh.sm;
+    SkewView g = s.viewT();
+    // the lower and upper coefficients exchanged: forward sweep rD_c a_fc,
+    // backward rD_c a_cf (rDinv is rewritten with the same values)
+    k_skew_premul<<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, s.faceLo.p, s.faceHi.p, ctx->mesh.N, lower,
+                                                                  upper);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+}
+
+void skew_precondition_T(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
+    SkewView g = ctx->mesh.sm.viewT();
+    k_skew_gather<double, double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    if (nc == 1) autotune<double>(ctx, g, mask, w);
+    launch_mode<double, 0>(ctx, g, nc, mask, w);
+    launch_mode<double, 1>(ctx, g, nc, mask, w);
+}
+
 void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const double *lower) {
     skew_prepare(ctx, diag, upper, lower);
     StructMesh &s = ctx->mesh.sm;

@@ -9,6 +9,10 @@ namespace rt {
 void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
 // w = M^-1 r for the masked components (nc <= 6), forward then backward
 void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
+// the transposed factorisation's coefficients (after skew_prepare of the
+// same matrix) and w = M^-T r with them (PBiCG)
+void skew_prepare_T(rt_ctx *ctx, const double *upper, const double *lower);
+void skew_precondition_T(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
 // mixed precision: skew_prepare, then FP32 copies of the sweep coefficients
 void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
 // FP32 w = M^-1 r with the coefficients of the last skew_prepare32

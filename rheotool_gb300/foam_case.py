@@ -18,8 +18,7 @@
 
 What the library does not implement is refused with a clear message unless
 ``substitute=True`` is given, in which case each substitution is recorded in
-``loaded.substitutions``: PBiCG becomes PBiCGStab (same preconditioner and
-tolerance); rheoTool's external sparse solvers (``solverType eigenSolver``,
+``loaded.substitutions``: rheoTool's external sparse solvers (``solverType eigenSolver``,
 ``petscSolver``, ``hypreSolver``) become PCG-DIC for p and PBiCGStab-DILU for
 the others at their tolerance; Crank-Nicolson ddt becomes Euler;
 non-orthogonal correctors and relaxation factors other than 1 are dropped (a
@@ -179,14 +178,8 @@ def _solver(d: Dict[str, Any], name: str, subs: List[str], substitute: bool) -> 
         subs.append(f"{name}: solverType {stype} {sv} -> {new[0]}-{new[1]}")
         return SolverControl(new[0], new[1], scalar(e.get("tolerance", "1e-6")), scalar(e.get("relTol", "0")),
                              int(scalar(e.get("minIter", "0"))), int(scalar(e.get("maxIter", "1000"))))
-    if sv == "PBiCG":
-        if not substitute:
-            raise CaseError(f"fvSolution {name}: solver PBiCG is not implemented (PBiCGStab is); "
-                            "pass substitute=True to use PBiCGStab")
-        subs.append(f"{name}: PBiCG -> PBiCGStab")
-        sv = "PBiCGStab"
-    if sv not in ("PCG", "PBiCGStab"):
-        raise CaseError(f"fvSolution {name}: solver {sv!r} is not implemented (PCG, PBiCGStab)")
+    if sv not in ("PCG", "PBiCGStab", "PBiCG"):
+        raise CaseError(f"fvSolution {name}: solver {sv!r} is not implemented (PCG, PBiCGStab, PBiCG)")
     pre = e.get("preconditioner", "none")
     if isinstance(pre, dict):
         pre = pre.get("preconditioner", "none")

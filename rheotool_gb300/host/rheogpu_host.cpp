@@ -156,7 +156,7 @@ void Context::setupCase(const rt_bc_desc &bcs, const rt_model_params &model, con
 // LduSolver (lduMatrix::solver)
 // ---------------------------------------------------------------------------
 const std::vector<std::string> &LduSolver::solvers() {
-    static const std::vector<std::string> v{"PCG", "PBiCGStab"};
+    static const std::vector<std::string> v{"PBiCG", "PBiCGStab", "PCG"};
     return v;
 }
 const std::vector<std::string> &LduSolver::preconditioners() {
@@ -186,6 +186,7 @@ rt_solver_ctl LduSolver::readControls(const Dictionary &c) {
     rt_solver_ctl ctl{};
     if (solver == "PCG") ctl.solver = RT_SOLVER_PCG;
     else if (solver == "PBiCGStab") ctl.solver = RT_SOLVER_PBICGSTAB;
+    else if (solver == "PBiCG") ctl.solver = RT_SOLVER_PBICG;
     else throw FatalError(valid_list("lduMatrix::solver", solver, solvers()));
     // "preconditioner DIC;" or "preconditioner { preconditioner DIC; }"
     std::string pre = c.isDict("preconditioner") ? c.subDict("preconditioner").lookup("preconditioner")

@@ -104,9 +104,17 @@ class Context:
             self.upload_mesh(case.mesh)
         self.case = case
         _, bd, mp, ctl = case.descriptors()
-        self._check(self.lib.rt_case_setup(self._ctx, C.byref(bd), C.byref(mp), C.byref(ctl)), "rt_case_setup")
+        if len(case.models) > 1:
+            self._check(self.lib.rt_case_setup_modes(self._ctx, C.byref(bd), case.mode_params(), len(case.models),
+                                                     C.byref(ctl)), "rt_case_setup_modes")
+        else:
+            self._check(self.lib.rt_case_setup(self._ctx, C.byref(bd), C.byref(mp), C.byref(ctl)), "rt_case_setup")
         if fields is not None:
             self.set_fields(fields)
+
+    @property
+    def nModes(self) -> int:
+        return len(self.case.models) if self.case is not None else 1
 
     def set_field(self, fid: int, internal=None, boundary=None):
         i = None if internal is None else _c(internal)
@@ -123,6 +131,15 @@ class Context:
         self.set_field(abi.RT_FIELD_U, f.U, f.Ub)
         self.set_field(abi.RT_FIELD_P, f.p, f.pb)
         self.set_field(abi.RT_FIELD_PHI, f.phi, f.phib)
+        if f.modes:
+            for i, m in enumerate(f.modes):
+                for fid, a, b in ((abi.RT_FIELD_THETA, m.theta, m.thetab), (abi.RT_FIELD_TAU, m.tau, m.taub),
+                                  (abi.RT_FIELD_EIGVALS, m.eigVals, None), (abi.RT_FIELD_EIGVECS, m.eigVecs, None)):
+                    self._check(self.lib.rt_field_set_mode(self._ctx, fid, i, abi.optr(_c(a)),
+                                                           abi.optr(None if b is None else _c(b))),
+                                "rt_field_set_mode")
+            self.set_field(abi.RT_FIELD_TAU, f.tau, f.taub)     # the summed tau
+            return
         self.set_field(abi.RT_FIELD_THETA, f.theta, f.thetab)
         self.set_field(abi.RT_FIELD_TAU, f.tau, f.taub)
         self.set_field(abi.RT_FIELD_EIGVALS, f.eigVals)
@@ -138,7 +155,24 @@ class Context:
         ta, tab = self.get_field(abi.RT_FIELD_TAU, (N, 6), (nB, 6))
         ev, _ = self.get_field(abi.RT_FIELD_EIGVALS, (N, 3))
         vv, _ = self.get_field(abi.RT_FIELD_EIGVECS, (N, 9))
-        return Fields(U, Ub, p, pb, phi, phib, th, thb, ta, tab, ev, vv)
+        f = Fields(U, Ub, p, pb, phi, phib, th, thb, ta, tab, ev, vv)
+        if self.nModes > 1:
+            from .case import ModeFields
+            for i in range(self.nModes):
+                m = ModeFields.zeros(self.mesh)
+                for fid, a, b in ((abi.RT_FIELD_THETA, m.theta, m.thetab), (abi.RT_FIELD_TAU, m.tau, m.taub),
+                                  (abi.RT_FIELD_EIGVALS, m.eigVals, None), (abi.RT_FIELD_EIGVECS, m.eigVecs, None)):
+                    self._check(self.lib.rt_field_get_mode(self._ctx, fid, i, abi.dptr(a), abi.optr(b)),
+                                "rt_field_get_mode")
+                f.modes.append(m)
+        return f
+
+    def mode_perf(self) -> List[List[abi.rt_solver_perf]]:
+        """Every mode's theta solve records of the last correct() (multiMode)."""
+        n = self.nModes
+        perf = (abi.rt_solver_perf * (6 * n))()
+        self._check(self.lib.rt_mode_perf(self._ctx, perf), "rt_mode_perf")
+        return [list(perf[6 * i:6 * i + 6]) for i in range(n)]
 
     # ------------------------------------------------------------------
     def step(self, n: int = 1) -> abi.rt_step_perf:
@@ -310,8 +344,8 @@ class SolverPerformance:
 
 
 class LduSolver:
-    """lduMatrix::solver stand-in: PCG (+DIC/diagonal/none) and PBiCGStab
-    (+DILU/diagonal/none) on the context's mesh addressing."""
+    """lduMatrix::solver stand-in: PCG (+DIC/diagonal/none), PBiCGStab and
+    PBiCG (+DILU/diagonal/none) on the context's mesh addressing."""
 
     def __init__(self, fieldName: str, ctl: SolverControl, ctx: Context):
         self.fieldName = fieldName
@@ -320,7 +354,7 @@ class LduSolver:
 
     @staticmethod
     def New(fieldName: str, ctl: SolverControl, ctx: Context) -> "LduSolver":
-        if ctl.solver not in ("PCG", "PBiCGStab"):
+        if ctl.solver not in ("PCG", "PBiCGStab", "PBiCG"):
             raise ValueError(f"Unknown asymmetric matrix solver {ctl.solver}")
         return LduSolver(fieldName, ctl, ctx)
 

@@ -101,14 +101,18 @@ static void cpu_checks() {
 
     Dictionary sol = Dictionary::parse("p { solver PCG; preconditioner DIC; tolerance 1e-8; relTol 0; }"
                                        " U { solver PBiCG; preconditioner DILU; }"
-                                       " T { solver PBiCGStab; preconditioner { preconditioner DILU; } }");
+                                       " T { solver PBiCGStab; preconditioner { preconditioner DILU; } }"
+                                       " V { solver GAMG; smoother GaussSeidel; }");
     rt_solver_ctl cp = LduSolver::readControls(sol.subDict("p"));
     CHECK(cp.solver == RT_SOLVER_PCG && cp.preconditioner == RT_PRECOND_DIC && cp.tolerance == 1e-8);
     CHECK(cp.maxIter == 1000 && cp.minIter == 0 && cp.relTol == 0.0);
     rt_solver_ctl ct = LduSolver::readControls(sol.subDict("T"));
     CHECK(ct.solver == RT_SOLVER_PBICGSTAB && ct.preconditioner == RT_PRECOND_DILU && ct.tolerance == 1e-6);
-    std::string e1 = throws([&] { LduSolver::readControls(sol.subDict("U")); });
-    CHECK(e1.find("Unknown lduMatrix::solver PBiCG") != std::string::npos);
+    rt_solver_ctl cu = LduSolver::readControls(sol.subDict("U"));
+    CHECK(cu.solver == RT_SOLVER_PBICG && cu.preconditioner == RT_PRECOND_DILU);
+    std::string e1 = throws([&] { LduSolver::readControls(sol.subDict("V")); });
+    CHECK(e1.find("Unknown lduMatrix::solver GAMG") != std::string::npos);
+    CHECK(e1.find("PBiCG\nPBiCGStab\nPCG") != std::string::npos);
 
     // sparseSolver selection by solverType: only the openFoam type is served
     Dictionary ext = Dictionary::parse("solverType eigenSolver; solver BiCGSTAB; tolerance 1e-12;");

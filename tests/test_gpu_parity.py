@@ -203,6 +203,45 @@ def test_pbicgstab_multi_rhs_matches_oracle(ctx, precond):
         assert rel(xg[k], xo) < 1e-9 or np.abs(xo).max() == 0
 
 
+@pytest.mark.parametrize("precond", ["DILU", "diagonal"])
+@pytest.mark.parametrize("mesh_fn", [small_contraction, lambda: cavity_mesh(14)])
+def test_pbicg_multi_rhs_matches_oracle(ctx, precond, mesh_fn):
+    """PBiCG (the Contraction41 tutorials' U and theta solver): the transposed
+    DILU sweeps and A^T products of the shadow system, per component against
+    the oracle's solve (same iteration counts, 1e-9)."""
+    from oracle.pyoracle import Oracle
+    mesh = mesh_fn()
+    case = contraction_case(mesh) if mesh.name.startswith("contraction") else cavity_case(mesh=mesh)
+    rng = np.random.default_rng(15)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=5.0)
+    nc = 3
+    b = rng.normal(size=(nc, mesh.nCells)) * mesh.V
+    b[1] = 0.0
+    x0 = rng.normal(size=(nc, mesh.nCells)) * 0.01
+    ctl = SolverControl("PBiCG", precond, 1e-10, 0.0, 0, 1000)
+    ctx.upload_mesh(mesh)
+    xg = x0.copy()
+    perf = ctx.ldu_solve(diag, upper, lower, b, xg, ctl)
+    orc = Oracle(case)
+    for k in range(nc):
+        xo = x0[k].copy()
+        po = orc.ldu_solve(diag, upper, lower, b[k].copy(), xo, ctl)
+        assert perf[k].nIterations == po.nIterations, (k, perf[k].nIterations, po.nIterations)
+        assert bool(perf[k].converged) == bool(po.converged) and po.converged
+        assert rel(xg[k], xo) < 1e-9
+
+
+def test_step_contraction_pbicg_tutorial_solvers(ctx):
+    """The Contraction41 tutorial's solver choice (fvSolution:18-51): p
+    PCG-DIC, U and theta PBiCG-DILU; full steps against the oracle."""
+    case = contraction_case(small_contraction(), dt=0.02)
+    case.solverU = SolverControl("PBiCG", "DILU", 1e-8, 0.0, 1, 1000)
+    case.solverTheta = SolverControl("PBiCG", "DILU", 1e-12, 0.0, 0, 1000)
+    case.solverP = SolverControl("PCG", "DIC", 1e-10, 0.0, 0, 800)
+    pg, _ = assert_step_parity(ctx, case, 4, label="contraction 460 cells, PBiCG U/theta (4 steps)")
+    assert pg.U[0].nIterations >= 1
+
+
 SWEEP_MESHES = {
     "cavity20": lambda: cavity_mesh(20),                              # one j-block, one plane
     "cavity70": lambda: cavity_mesh(70),                              # three j-blocks
@@ -212,7 +251,8 @@ SWEEP_MESHES = {
 
 
 @pytest.mark.parametrize("mesh_name", sorted(SWEEP_MESHES))
-@pytest.mark.parametrize("solver,pre,asym,nc", [("PCG", "DIC", 0.0, 1), ("PBiCGStab", "DILU", 3.0, 3)])
+@pytest.mark.parametrize("solver,pre,asym,nc", [("PCG", "DIC", 0.0, 1), ("PBiCGStab", "DILU", 3.0, 3),
+                                                ("PBiCG", "DILU", 3.0, 3)])
 def test_systolic_sweeps_equal_level_sweeps(ctx, mesh_name, solver, pre, asym, nc):
     """The structured systolic DIC/DILU sweeps evaluate the recurrences in the
     level-scheduled (and sequential) order of operations: same bits."""
@@ -365,7 +405,66 @@ def test_step_contraction_headline_sample_fp64(ctx):
     assert pg.p.nIterations > 100       # a real pressure solve, through the systolic sweeps
 
 
-@pytest.mark.parametrize("solver,pre,asym,nc,tune", [("PCG", "DIC", 0.0, 1, 3), ("PCG", "DIC", 0.0, 1, 2),
+def lognormal_state(case, sigma=0.1, seed=20261203):
+    """The case's initial fields (createPhi, boundary values) with the seeded
+    lognormal log-conformation of the precision sweep (A = I + a lognormal
+    perturbation, eigenvalues apart): tau = etaP/lambda (A - I), zero-gradient
+    theta boundaries at their cells' values."""
+    from oracle.pyoracle import Oracle
+    from rheotool_gb300.case import lognormal_conformation
+    m, md = case.mesh, case.model
+    f0 = Oracle(case).f.copy()
+    th, ev, vv = lognormal_conformation(m.nCells, sigma, seed)
+    f0.theta[:], f0.eigVals[:], f0.eigVecs[:] = th, ev, vv
+    R = vv.reshape(-1, 3, 3)
+    T = md.etaP / md.lambda_ * (np.einsum("nij,nj,nkj->nik", R, ev, R) - np.eye(3))
+    f0.tau[:] = np.stack([T[:, 0, 0], T[:, 0, 1], T[:, 0, 2], T[:, 1, 1], T[:, 1, 2], T[:, 2, 2]], axis=1)
+    for p in m.patches:
+        sl = slice(p.start, p.start + p.size)
+        if case.bcs[p.name]["theta"][0] == "zeroGradient":
+            f0.thetab[sl] = f0.theta[m.bCell[sl]]
+    return f0
+
+
+def test_step_contraction_headline_sample_lognormal(ctx):
+    """The headline sample again, from the seeded lognormal conformation
+    instead of theta = 0: no cell starts with degenerate eigenvalues, so the
+    case is well conditioned (the oracle's own fields move by 2e-9 in phi
+    and 2e-10 in theta under a 1e-16 inlet perturbation over 3 steps, against
+    7e-3 in theta from theta = 0); the FP64 step against the oracle."""
+    from oracle.pyoracle import Oracle
+    dims = dict(nx_up=67, nx_down=66, ny_in=25, ny_out=13, nz=25)
+    case = contraction_case(contraction_mesh(**dims))
+    f0 = lognormal_state(case)
+    ref = Oracle(case, f0.copy())
+    ref.step(3)
+    ctx.setup_case(case, f0)
+    ctx.step(3)
+    got = ctx.fields()
+    names = ("U", "p", "theta", "tau", "phi")
+    errs = {n: rel(getattr(got, n), getattr(ref.f, n)) for n in names}
+    label = "contraction 126,675-cell headline sample, lognormal theta0 (3 steps)"
+    if all(e < TOL_STEP for e in errs.values()):
+        BAR_LOG.append((label, "plain 1e-9", errs, None))
+        return
+    # the sensitivity bar, measured from the same state
+    sens = {n: 0.0 for n in names}
+    for seed in (1, 2):
+        g0 = f0.copy()
+        rng = np.random.default_rng(seed)
+        g0.Ub[:] *= 1.0 + 1e-16 * rng.standard_normal(g0.Ub.shape)
+        g0.phib[:] = (case.mesh.bSf * g0.Ub).sum(1)
+        o = Oracle(case, g0)
+        o.step(3)
+        for n in names:
+            sens[n] = max(sens[n], rel(getattr(o.f, n), getattr(ref.f, n)))
+    bar = {n: max(TOL_STEP, 100.0 * sens[n]) for n in names}
+    BAR_LOG.append((label, "sensitivity", errs, bar))
+    for n in names:
+        assert errs[n] < bar[n], (n, errs[n], bar[n])
+
+
+@pytest.mark.parametrize("solver,pre,asym,nc,tune", [("PCG", "DIC", 0.0, 1, 3), ("PCG", "DIC", 0.0, 1, 4),
                                                      ("PBiCGStab", "DILU", 3.0, 3, 0)])
 def test_systolic_sweeps_headline_structure(ctx, solver, pre, asym, nc, tune):
     """The 1M-cell headline's sweep structure: 100 rows (four j-blocks per
@@ -394,6 +493,94 @@ def test_systolic_sweeps_headline_structure(ctx, solver, pre, asym, nc, tune):
         ctx.set_option(abi.RT_OPT_SWEEP_TUNE, 0)
     assert out[abi.SWEEP_LEVELS][1] == out[abi.SWEEP_SYSTOLIC][1]
     assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
+
+
+def multimode_case(base, n_extra=2):
+    """A multiMode model of three different modes on the base case:
+    Oldroyd-B (the base model), Giesekus lambda 0.2 alpha 0.15 and linear PTT
+    lambda 0.05 epsilon 0.3 (common rho and stabilization)."""
+    import copy
+    m0 = base.model
+    m1 = copy.copy(m0)
+    m1.type, m1.lambda_, m1.alpha, m1.etaP, m1.etaS = "GiesekusLog", 0.2, 0.15, 0.3, 0.0
+    m2 = copy.copy(m0)
+    m2.type, m2.lambda_, m2.epsilon, m2.etaP, m2.etaS = "PTTLog", 0.05, 0.3, 0.2, 0.1
+    base.moreModes = [m1, m2][:n_extra]
+    base.name += "_multiMode"
+    return base
+
+
+def assert_modes_parity(got, ref, tol=TOL_STEP):
+    for name in ("U", "p", "phi", "tau"):
+        e = rel(getattr(got, name), getattr(ref, name))
+        assert e < tol, (name, e)
+    assert len(got.modes) == len(ref.modes)
+    for i, (g, r) in enumerate(zip(got.modes, ref.modes)):
+        for name in ("theta", "tau", "eigVals", "taub"):
+            e = rel(getattr(g, name), getattr(r, name))
+            assert e < tol, (i, name, e)
+
+
+@pytest.mark.parametrize("nInIter", [1, 2])
+def test_step_multimode_cavity(ctx, nInIter):
+    """multiMode in the flow step (multiMode.C:144-156, 222, 247-256): three
+    different modes, each with its own theta, tau and eigen fields; the
+    momentum equation takes the summed tau and viscosities; every mode is
+    corrected each step (with inner iterations, against the step's old-time
+    theta of each mode)."""
+    from oracle.pyoracle import Oracle
+    case = multimode_case(cavity_case(12, model="Oldroyd-BLog", Wi=0.5, dt=2e-3))
+    case.nInIter = nInIter
+    ref = Oracle(case)
+    ref.step(4)
+    ctx.setup_case(case)
+    ctx.step(4)
+    got = ctx.fields()
+    assert_modes_parity(got, ref.f)
+    perf = ctx.mode_perf()
+    for i in range(3):
+        assert [p.nIterations for p in perf[i]] == [ref.modePerf[6 * i + k].nIterations for k in range(6)]
+    BAR_LOG.append((f"{case.name} nInIter {nInIter} (4 steps)", "plain 1e-9",
+                    {n: rel(getattr(got, n), getattr(ref.f, n)) for n in ("U", "p", "tau")}, None))
+
+
+def test_step_multimode_contraction3d(ctx):
+    from oracle.pyoracle import Oracle
+    case = multimode_case(contraction_case(small_contraction(), model="Oldroyd-BLog", dt=0.02), n_extra=1)
+    ref = Oracle(case)
+    ref.step(4)
+    ctx.setup_case(case)
+    ctx.step(4)
+    assert_modes_parity(ctx.fields(), ref.f)
+
+
+def test_constitutive_correct_multimode(ctx):
+    from oracle.pyoracle import Oracle
+    from rheotool_gb300.runtime import RheoGpuError
+    case = multimode_case(cavity_case(10, model="Oldroyd-BLog"))
+    o = Oracle(case)
+    o.step(2)
+    f0 = o.f.copy()
+    o.constitutive_correct()
+    ctx.setup_case(case, f0)
+    ctx.constitutive_correct()
+    got = ctx.fields()
+    for i in range(3):
+        for name in ("theta", "tau"):
+            assert rel(getattr(got.modes[i], name), getattr(o.f.modes[i], name)) < 1e-11
+    assert rel(got.tau, o.f.tau) < 1e-11
+    with pytest.raises(RheoGpuError) as e:
+        ctx.constitutive_correct(newTimeStep=True)
+    assert e.value.status == abi.RT_EINVAL
+
+
+def test_multimode_needs_a_common_rho_and_stabilization(ctx):
+    from rheotool_gb300.runtime import RheoGpuError
+    case = multimode_case(cavity_case(6), n_extra=1)
+    case.moreModes[0].rho = 2 * case.model.rho
+    with pytest.raises(RheoGpuError) as e:
+        ctx.setup_case(case)
+    assert e.value.status == abi.RT_EINVAL
 
 
 def test_step_channel_fixed_outlet(ctx):

@@ -102,6 +102,50 @@ def test_pbicgstab_matches_dense_solve(pre):
     assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
 
 
+@pytest.mark.parametrize("pre", ["DILU", "diagonal", "none"])
+def test_pbicg_matches_dense_solve(pre):
+    """PBiCG (OpenFOAM's bi-conjugate gradients, the Contraction41 tutorials'
+    U and theta solver) on an upwinded convection-diffusion matrix."""
+    mesh = contraction_mesh(6, 5, 4, 2, 3, 2.0, 2.0)
+    rng = np.random.default_rng(6)
+    phi = rng.normal(size=mesh.nFaces)
+    u = (phi >= 0).astype(float)
+    lower = -u * phi - 1.0
+    upper = (1 - u) * phi - 1.0
+    diag = np.zeros(mesh.nCells)
+    np.subtract.at(diag, mesh.owner, lower)
+    np.subtract.at(diag, mesh.neighbour, upper)
+    diag += 0.5
+    b = rng.normal(size=mesh.nCells)
+    x = np.zeros(mesh.nCells)
+    o = Oracle(contraction_case(mesh))
+    p = o.ldu_solve(diag, upper, lower, b, x, SolverControl("PBiCG", pre, 1e-13, 0, 0, 2000))
+    xd = np.linalg.solve(dense(mesh, diag, upper, lower), b)
+    assert p.converged and not p.singular
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+    assert o.residual(diag, upper, lower, b, x) < 1e-13
+
+
+def test_pbicg_on_a_symmetric_matrix_is_pcg():
+    """With a symmetric matrix, a symmetric preconditioner and rT = r, the
+    shadow recurrences of BiCG repeat the primal ones: PBiCG takes PCG's
+    iterations (same counts, the same solution to round-off)."""
+    mesh = cavity_mesh(9)
+    rng = np.random.default_rng(7)
+    g = 1.0 + rng.random(mesh.nFaces)
+    diag = np.zeros(mesh.nCells)
+    np.subtract.at(diag, mesh.owner, g)
+    np.subtract.at(diag, mesh.neighbour, g)
+    diag -= 0.1
+    b = rng.normal(size=mesh.nCells)
+    o = Oracle(cavity_case(9))
+    x1, x2 = np.zeros(mesh.nCells), np.zeros(mesh.nCells)
+    p1 = o.ldu_solve(diag, g, g, b, x1, SolverControl("PCG", "DIC", 1e-12, 0, 0, 1000))
+    p2 = o.ldu_solve(diag, g, g, b, x2, SolverControl("PBiCG", "DIC", 1e-12, 0, 0, 1000))
+    assert p1.nIterations == p2.nIterations
+    assert np.linalg.norm(x1 - x2) <= 1e-12 * np.linalg.norm(x1)
+
+
 def test_dilu_preconditioner_is_exact_for_tridiagonal():
     # D-ILU of a tridiagonal matrix has no fill-in: one application solves it
     mesh = cavity_mesh(1, ny=12)       # a 1 x 12 column: tridiagonal LDU
@@ -384,3 +428,45 @@ def test_golden_cavity_oracle():
     for name in ("U", "p", "theta", "tau", "phi"):
         ref = g[name]
         assert np.linalg.norm(getattr(o.f, name) - ref) <= 1e-12 * np.linalg.norm(ref), name
+
+
+# ---------------------------------------------------------------------------
+# multiMode (multiMode.C): modes summed
+# ---------------------------------------------------------------------------
+def test_multimode_of_two_half_modes_is_the_single_mode():
+    """Oldroyd-B's conformation does not depend on etaP, so two identical
+    modes with etaP/2 each carry half the stress each: their multiMode model
+    steps exactly as the single mode (summed tau, summed viscosities)."""
+    import copy
+    one = cavity_case(10, model="Oldroyd-BLog", Wi=0.5)
+    two = copy.copy(one)
+    half = copy.copy(one.model)
+    half.etaP = one.model.etaP / 2
+    half.etaS = one.model.etaS / 2
+    two.model = half
+    two.moreModes = [copy.copy(half)]
+    a, b = Oracle(one), Oracle(two)
+    a.step(4)
+    b.step(4)
+    for name in ("U", "p", "phi", "tau", "theta"):
+        x, y = getattr(b.f, name), getattr(a.f, name)
+        assert np.linalg.norm(x - y) <= 1e-12 * np.linalg.norm(y), name
+    for m in b.f.modes:
+        assert np.linalg.norm(2 * m.tau - a.f.tau) <= 1e-12 * np.linalg.norm(a.f.tau)
+        assert np.linalg.norm(m.theta - a.f.theta) <= 1e-12 * np.linalg.norm(a.f.theta)
+
+
+def test_multimode_modes_differ_and_sum():
+    """Two different modes (Oldroyd-B lambda 0.5, Giesekus lambda 0.1): each
+    mode keeps its own conformation, and tau is their sum."""
+    import copy
+    case = cavity_case(10, model="Oldroyd-BLog", Wi=0.5)
+    m2 = copy.copy(case.model)
+    m2.type, m2.lambda_, m2.alpha, m2.etaP, m2.etaS = "GiesekusLog", 0.1, 0.2, 0.3, 0.0
+    case.moreModes = [m2]
+    o = Oracle(case)
+    o.step(3)
+    t0, t1 = o.f.modes[0].tau, o.f.modes[1].tau
+    assert np.linalg.norm(t0 - t1) > 1e-3 * np.linalg.norm(t0)
+    assert np.array_equal(o.f.tau, t0 + t1)
+    assert np.array_equal(o.f.theta, o.f.modes[0].theta)
