@@ -198,7 +198,22 @@ typedef struct {
      * an fvOptions meanVelocityForce / pressure-gradient source adds to UEqn
      * to drive a periodic channel); zero for the other cases                */
     double bodyForce[3];
+    /* SIMPLE nNonOrthogonalCorrectors (pEqn.H:31-50): the pressure equation
+     * is solved 1 + nNonOrthCorr times, each from the last solution, and the
+     * flux is updated after the last solve.  The library's laplacian is the
+     * orthogonal one ("Gauss linear orthogonal", the tutorials' choice), whose
+     * explicit non-orthogonal correction is zero. */
+    int32_t nNonOrthCorr;
+    /* ddtSchemes default: RT_DDT_EULER, or RT_DDT_CRANKNICOLSON with the
+     * off-centering coefficient ddtPsi ("CrankNicolson 1" is ddtPsi = 1;
+     * 0 is Euler) for every ddt of the step: fvm::ddt(U), fvm::ddt(theta)
+     * and the ddtCorr of the face flux */
+    int32_t ddtScheme;
+    double ddtPsi;
 } rt_case_ctl;
+
+#define RT_DDT_EULER          0
+#define RT_DDT_CRANKNICOLSON  1
 
 typedef struct {
     rt_solver_perf U[3], p, theta[6];

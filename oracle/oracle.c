@@ -80,6 +80,31 @@ typedef struct {
     double *eigVecs;         /* 9N */
 } or_state;
 
+/* Crank-Nicolson state kept between time steps (NULL or scheme Euler: the
+ * implicit Euler ddt).  The scheme is the trapezoidal rule written with the
+ * stored time derivative of the old time level D: the step from n to n+1
+ * solves (c/dt)(x - x_n) - psi D_n = f(x), c = 1 + psi, psi the off-centering
+ * coefficient (1: Crank-Nicolson, 0: Euler), with D_n = c_{n-1}(x_n -
+ * x_{n-1})/dt - psi D_{n-1}; the first step is an implicit Euler step (c = 1,
+ * D_0 = 0), so D_1 = (x_1 - x_0)/dt is the derivative that step implies.  D
+ * is formed at the start of a step from the fields there and the fields at
+ * the start of the previous step (xs), then xs takes the current fields.  The
+ * flux correction ddtCorr takes the same old-time parts:
+ * ddtCorr = coef (c/dt phi_n + psi D_phi - Sf.interp(c/dt U_n + psi D_U)). */
+typedef struct {
+    int scheme;          /* RT_DDT_EULER / RT_DDT_CRANKNICOLSON */
+    double psi;
+    int nSteps;          /* time steps of the flow (U, phi) started so far */
+    int nThSteps;        /* time steps of the theta equations started so far */
+    double *DU, *DUb;    /* 3N, 3nB */
+    double *Dphi, *Dphib;/* nF, nB */
+    double *Dth;         /* 6N per mode */
+    double *Us, *Ubs, *phis, *phibs, *ths;   /* the fields at the start of the last step */
+} or_ddt;
+
+/* coefficient c of the step with index j (0-based) */
+static double ddt_coef(const or_ddt *d, int j) { return j == 0 ? 1.0 : 1.0 + d->psi; }
+
 static void *xcalloc(size_t n, size_t sz) {
     void *p = calloc(n ? n : 1, sz);
     if (!p) { fprintf(stderr, "oracle: out of memory\n"); abort(); }
@@ -664,6 +689,19 @@ static void add_ddt(const rt_mesh_desc *m, double rDeltaT, const double *x0, int
     }
 }
 
+/* Crank-Nicolson ddt (see or_ddt): diag += (c/dt) V, source += ((c/dt) x0
+ * + psi D) V; D == NULL is add_ddt */
+static void add_ddt_cn(const rt_mesh_desc *m, double rDeltaT, double c, double psi, const double *x0,
+                       const double *D, int nc, or_matrix *M) {
+    if (!D) { add_ddt(m, rDeltaT, x0, nc, M); return; }
+    const double rDtCoef = c * rDeltaT;
+    for (int cl = 0; cl < m->nCells; ++cl) {
+        M->diag[cl] += rDtCoef * m->V[cl];
+        for (int k = 0; k < nc; ++k)
+            M->source[nc * cl + k] += (rDtCoef * x0[nc * cl + k] + psi * D[nc * cl + k]) * m->V[cl];
+    }
+}
+
 /* Solve all valid components of an nc-component matrix, fvMatrix::solveSegregated. */
 static void solve_segregated(const rt_mesh_desc *m, or_matrix *M, double *x,
                              const int *valid, const rt_solver_ctl *ctl, rt_solver_perf *perf) {
@@ -701,12 +739,18 @@ typedef struct {
     const rt_model_params *models;
     or_state *modes;
     rt_solver_perf *modePerf;
+    /* Crank-Nicolson: the state (NULL for Euler), the coefficient c of the
+     * current step and, for the theta equation of each mode, its D */
+    or_ddt *ddt;
+    double ddtC, ddtCth;
+    const double *Dth;
 } or_case;
 
 static void case_init(or_case *k, const rt_mesh_desc *m, const rt_bc_desc *bc,
                       const rt_model_params *mp, const rt_case_ctl *ctl, or_state *s) {
     k->m = m; k->bc = bc; k->mp = mp; k->ctl = ctl; k->s = s;
     k->nModes = 1; k->models = NULL; k->modes = NULL; k->modePerf = NULL;
+    k->ddt = NULL; k->ddtC = 1.0; k->ddtCth = 1.0; k->Dth = NULL;
     int nB = m->nBFaces;
     k->kU = (int *)xcalloc(nB, sizeof(int)); k->kP = (int *)xcalloc(nB, sizeof(int));
     k->kTh = (int *)xcalloc(nB, sizeof(int)); k->kTau = (int *)xcalloc(nB, sizeof(int));
@@ -983,7 +1027,7 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
     memcpy(theta0, thetaOld ? thetaOld : s->theta, sizeof(double) * 6 * N);
     or_matrix Md;
     mat_alloc(&Md, m, 6);
-    add_ddt(m, 1.0 / k->ctl->deltaT, theta0, 6, &Mx);
+    add_ddt_cn(m, 1.0 / k->ctl->deltaT, k->ddtCth, k->ddt ? k->ddt->psi : 0.0, theta0, k->Dth, 6, &Mx);
     defcmpw(m, k->ctl->divTheta, s->phi, s->phib, s->theta, s->thetab, k->kTh, 6, &Md);
     for (int c = 0; c < N; ++c) Mx.diag[c] += Md.diag[c];
     for (int f = 0; f < m->nFaces; ++f) { Mx.lower[f] = Md.lower[f]; Mx.upper[f] = Md.upper[f]; }
@@ -1132,6 +1176,7 @@ static int modes_correct(or_case *k, const double *gradU, rt_solver_perf *perf, 
         ki.mp = &k->models[i];
         ki.s = &si;
         ki.nModes = 1;
+        ki.Dth = k->Dth ? k->Dth + n6 * i : NULL;
         rt_solver_perf *pi = k->modePerf ? k->modePerf + 6 * i : perf;
         st = constitutive_correct(&ki, gradU, pi, theta0s ? theta0s + n6 * i : NULL);
         if (pi != perf) memcpy(perf, pi, 6 * sizeof *perf);
@@ -1186,7 +1231,7 @@ static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const d
     grad_vector(m, s->U, s->Ub, G);
     or_matrix UE;
     mat_alloc(&UE, m, 3);
-    add_ddt(m, rDeltaT, U0, 3, &UE);
+    add_ddt_cn(m, rDeltaT, k->ddtC, k->ddt ? k->ddt->psi : 0.0, U0, k->ddt ? k->ddt->DU : NULL, 3, &UE);
     or_matrix Cv;
     mat_alloc(&Cv, m, 3);
     defcmpw(m, ctl->divU, s->phi, s->phib, s->U, s->Ub, k->kU, 3, &Cv);
@@ -1304,6 +1349,16 @@ static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const d
         double phiCorr = phi0[f] - u0f;
         double cc = 1.0 - fmin(fabs(phiCorr) / (fabs(phi0[f]) + OR_SMALL), 1.0);
         double ddtCorr = cc * rDeltaT * phiCorr;
+        if (k->ddt) {
+            /* Crank-Nicolson: the old-time parts c/dt x0 + psi D of phi and U */
+            const or_ddt *d = k->ddt;
+            const double rc = k->ddtC * rDeltaT;
+            double uf = 0.0;
+            for (int j = 0; j < 3; ++j)
+                uf += S[j] * lin_interp(w, rc * U0[3 * o + j] + d->psi * d->DU[3 * o + j],
+                                        rc * U0[3 * n + j] + d->psi * d->DU[3 * n + j]);
+            ddtCorr = cc * ((rc * phi0[f] + d->psi * d->Dphi[f]) - uf);
+        }
         phiHbyA[f] = hf + lin_interp(w, rAU[o], rAU[n]) * ddtCorr;
     }
     for (int b = 0; b < nB; ++b) {
@@ -1314,7 +1369,15 @@ static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const d
         double phiCorr = phi0b[b] - u0f;
         double cc = (k->kU[b] == RT_BC_FIXED) ? 0.0
                   : 1.0 - fmin(fabs(phiCorr) / (fabs(phi0b[b]) + OR_SMALL), 1.0);
-        phiHbyAb[b] = hf + rAU[c] * (cc * rDeltaT * phiCorr);
+        double ddtCorr = cc * rDeltaT * phiCorr;
+        if (k->ddt) {
+            const or_ddt *d = k->ddt;
+            const double rc = k->ddtC * rDeltaT;
+            double uf = 0.0;
+            for (int j = 0; j < 3; ++j) uf += S[j] * (rc * U0b[3 * b + j] + d->psi * d->DUb[3 * b + j]);
+            ddtCorr = cc * ((rc * phi0b[b] + d->psi * d->Dphib[b]) - uf);
+        }
+        phiHbyAb[b] = hf + rAU[c] * ddtCorr;
     }
     /* adjustCorrPhi when p needs a reference */
     if (ctl->needReference) {
@@ -1384,10 +1447,16 @@ static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const d
         memcpy(d2, pd, sizeof(double) * N);
         memcpy(b2, ps, sizeof(double) * N);
         for (int b = 0; b < nB; ++b) { d2[m->bCell[b]] += pIntC[b]; b2[m->bCell[b]] += pBouC[b]; }
-        or_ldu_solve(m, d2, pu, pu, b2, s->p, &ctl->solverP, &perf->p);
+        /* the non-orthogonal corrector loop (pEqn.H:31-50): with the orthogonal
+         * laplacian the equation is the same each time; every solve starts
+         * from the last one's p, the flux follows the last */
+        const int nCorr = ctl->nNonOrthCorr > 0 ? ctl->nNonOrthCorr : 0;
+        for (int corr = 0; corr <= nCorr; ++corr) {
+            or_ldu_solve(m, d2, pu, pu, b2, s->p, &ctl->solverP, &perf->p);
+            correct_bc(m, k->kP, s->p, s->pb, 1);
+        }
         free(d2); free(b2);
     }
-    correct_bc(m, k->kP, s->p, s->pb, 1);
     /* phi = phiHbyA - pEqn.flux() */
     for (int f = 0; f < nF; ++f) {
         int o = m->owner[f], n = m->neighbour[f];
@@ -1427,11 +1496,53 @@ static int step_inner(or_case *k, rt_step_perf *perf, const double *U0s, const d
 
 /* One time step: nInIter inner iterations (rheoFoam.C:96-150; createControls.H
  * nInIter, 0 meaning 1) on the old-time fields of the step. */
+/* Start of a Crank-Nicolson time step (see or_ddt): the old-time
+ * derivatives D of the step that ended, from the fields now and at that
+ * step's start; then the start fields become the current ones.  flow: U and
+ * phi too (rt_step), else the theta equations only (a correct() of its own). */
+static void ddt_begin_step(or_case *k, int flow) {
+    or_ddt *d = k->ddt;
+    if (!d || d->scheme != RT_DDT_CRANKNICOLSON) return;
+    const rt_mesh_desc *m = k->m;
+    or_state *s = k->s;
+    const size_t N = m->nCells, nF = m->nFaces, nB = m->nBFaces;
+    const int nM = k->nModes > 1 ? k->nModes : 1;
+    const double rDt = 1.0 / k->ctl->deltaT, psi = d->psi;
+    if (flow) {
+        if (d->nSteps >= 1) {
+            const double r = ddt_coef(d, d->nSteps - 1) * rDt;
+            for (size_t i = 0; i < 3 * N; ++i) d->DU[i] = r * (s->U[i] - d->Us[i]) - psi * d->DU[i];
+            for (size_t i = 0; i < 3 * nB; ++i) d->DUb[i] = r * (s->Ub[i] - d->Ubs[i]) - psi * d->DUb[i];
+            for (size_t i = 0; i < nF; ++i) d->Dphi[i] = r * (s->phi[i] - d->phis[i]) - psi * d->Dphi[i];
+            for (size_t i = 0; i < nB; ++i) d->Dphib[i] = r * (s->phib[i] - d->phibs[i]) - psi * d->Dphib[i];
+        }
+        memcpy(d->Us, s->U, sizeof(double) * 3 * N);
+        memcpy(d->Ubs, s->Ub, sizeof(double) * 3 * nB);
+        memcpy(d->phis, s->phi, sizeof(double) * nF);
+        memcpy(d->phibs, s->phib, sizeof(double) * nB);
+        d->nSteps++;
+        k->ddtC = ddt_coef(d, d->nSteps - 1);
+    }
+    for (int i = 0; i < nM; ++i) {
+        const double *th = k->nModes > 1 ? k->modes[i].theta : s->theta;
+        double *D = d->Dth + 6 * N * i, *ts = d->ths + 6 * N * i;
+        if (d->nThSteps >= 1) {
+            const double r = ddt_coef(d, d->nThSteps - 1) * rDt;
+            for (size_t j = 0; j < 6 * N; ++j) D[j] = r * (th[j] - ts[j]) - psi * D[j];
+        }
+        memcpy(ts, th, sizeof(double) * 6 * N);
+    }
+    d->nThSteps++;
+    k->ddtCth = ddt_coef(d, d->nThSteps - 1);
+    k->Dth = d->Dth;
+}
+
 static int step_once(or_case *k, rt_step_perf *perf) {
     const rt_mesh_desc *m = k->m;
     or_state *s = k->s;
     const int N = m->nCells, nF = m->nFaces, nB = m->nBFaces;
     const int nM = k->nModes > 1 ? k->nModes : 1;
+    ddt_begin_step(k, 1);
     double *U0 = DALLOC(3 * (size_t)N), *U0b = DALLOC(3 * (size_t)nB);
     double *phi0 = DALLOC(nF), *phi0b = DALLOC(nB), *theta0 = DALLOC(6 * (size_t)N * nM);
     memcpy(U0, s->U, sizeof(double) * 3 * N); memcpy(U0b, s->Ub, sizeof(double) * 3 * nB);
@@ -1452,6 +1563,7 @@ static int step_once(or_case *k, rt_step_perf *perf) {
 
 int or_step(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *mp,
             const rt_case_ctl *ctl, or_state *s, int nSteps, rt_step_perf *perf) {
+    if (ctl->ddtScheme != RT_DDT_EULER) return RT_EINVAL;   /* Crank-Nicolson keeps state: or_step_ddt */
     or_case k;
     case_init(&k, m, bc, mp, ctl, s);
     rt_step_perf local;
@@ -1473,16 +1585,31 @@ int or_step(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *
  * and stabilization), s the common fields (U, p, phi; tau and taub get the
  * summed tau), modes[i] each mode's theta, tau and eigen fields; modePerf
  * (6 per mode, or NULL) each mode's theta solve records of the last step. */
+int or_step_ddt(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models, int nModes,
+                const rt_case_ctl *ctl, or_state *s, or_state *modes, int nSteps, rt_step_perf *perf,
+                rt_solver_perf *modePerf, or_ddt *ddt);
+
 int or_step_modes(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models, int nModes,
                   const rt_case_ctl *ctl, or_state *s, or_state *modes, int nSteps, rt_step_perf *perf,
                   rt_solver_perf *modePerf) {
-    if (nModes < 1) return RT_EINVAL;
+    if (ctl->ddtScheme != RT_DDT_EULER) return RT_EINVAL;
+    return or_step_ddt(m, bc, models, nModes, ctl, s, modes, nSteps, perf, modePerf, NULL);
+}
+
+/* nSteps steps of a single- (nModes 1, modes NULL) or multiMode case with the
+ * ddt scheme of ctl; ddt: the Crank-Nicolson state (required for it). */
+int or_step_ddt(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models, int nModes,
+                const rt_case_ctl *ctl, or_state *s, or_state *modes, int nSteps, rt_step_perf *perf,
+                rt_solver_perf *modePerf, or_ddt *ddt) {
+    if (nModes < 1 || (nModes > 1 && !modes)) return RT_EINVAL;
+    if (ctl->ddtScheme == RT_DDT_CRANKNICOLSON && !ddt) return RT_EINVAL;
     for (int i = 1; i < nModes; ++i)
         if (models[i].rho != models[0].rho || models[i].stabilization != models[0].stabilization) return RT_EINVAL;
     rt_model_params eff = modes_momentum_model(models, nModes);
     or_case k;
     case_init(&k, m, bc, &eff, ctl, s);
-    k.nModes = nModes; k.models = models; k.modes = modes; k.modePerf = modePerf;
+    if (nModes > 1) { k.nModes = nModes; k.models = models; k.modes = modes; k.modePerf = modePerf; }
+    if (ctl->ddtScheme == RT_DDT_CRANKNICOLSON) { ddt->scheme = RT_DDT_CRANKNICOLSON; ddt->psi = ctl->ddtPsi; k.ddt = ddt; }
     rt_step_perf local;
     int st = RT_OK;
     for (int i = 0; i < nSteps && st == RT_OK; ++i) {
@@ -1494,6 +1621,34 @@ int or_step_modes(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_pa
         }
     }
     if (perf) *perf = local;
+    case_free(&k);
+    return st;
+}
+
+/* correct() of a single- or multiMode model as a time step of its own
+ * (newTimeStep != 0) or as a further inner iteration of the current one, with
+ * the ddt scheme of ctl (ddt: the Crank-Nicolson state, required for it; the
+ * old-time theta is then the one kept at the start of the time step). */
+int or_constitutive_correct_ddt(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models,
+                                int nModes, const rt_case_ctl *ctl, or_state *s, or_state *modes,
+                                const double *gradU, int newTimeStep, rt_solver_perf *modePerf, or_ddt *ddt) {
+    if (nModes < 1 || (nModes > 1 && !modes) || !ddt || ctl->ddtScheme != RT_DDT_CRANKNICOLSON) return RT_EINVAL;
+    or_case k;
+    case_init(&k, m, bc, &models[0], ctl, s);
+    if (nModes > 1) { k.nModes = nModes; k.models = models; k.modes = modes; k.modePerf = modePerf; }
+    ddt->scheme = RT_DDT_CRANKNICOLSON;
+    ddt->psi = ctl->ddtPsi;
+    k.ddt = ddt;
+    if (newTimeStep || ddt->nThSteps == 0) ddt_begin_step(&k, 0);
+    k.ddtCth = ddt_coef(ddt, ddt->nThSteps - 1);
+    k.Dth = ddt->Dth;
+    int st;
+    if (nModes > 1) {
+        rt_solver_perf last[6];
+        st = modes_correct(&k, gradU, last, ddt->ths);
+    } else {
+        st = constitutive_correct(&k, gradU, modePerf, ddt->ths);
+    }
     case_free(&k);
     return st;
 }

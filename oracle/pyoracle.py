@@ -26,6 +26,11 @@ class or_state(C.Structure):
                                    "tau", "taub", "eigVals", "eigVecs")]
 
 
+class or_ddt(C.Structure):
+    _fields_ = [("scheme", C.c_int), ("psi", C.c_double), ("nSteps", C.c_int), ("nThSteps", C.c_int)] + \
+               [(n, _dp) for n in ("DU", "DUb", "Dphi", "Dphib", "Dth", "Us", "Ubs", "phis", "phibs", "ths")]
+
+
 def build(force: bool = False) -> str:
     deps = (os.path.join(HERE, "oracle.c"), os.path.join(HERE, "..", "include", "rheogpu.h"))
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(d) for d in deps):
@@ -73,6 +78,14 @@ def lib():
                                                     C.c_int, P(abi.rt_case_ctl), P(or_state), P(or_state), _dp,
                                                     P(abi.rt_solver_perf)]
         L.or_constitutive_correct_modes.restype = C.c_int
+        L.or_step_ddt.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params), C.c_int,
+                                  P(abi.rt_case_ctl), P(or_state), P(or_state), C.c_int, P(abi.rt_step_perf),
+                                  P(abi.rt_solver_perf), P(or_ddt)]
+        L.or_step_ddt.restype = C.c_int
+        L.or_constitutive_correct_ddt.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params),
+                                                  C.c_int, P(abi.rt_case_ctl), P(or_state), P(or_state), _dp, C.c_int,
+                                                  P(abi.rt_solver_perf), P(or_ddt)]
+        L.or_constitutive_correct_ddt.restype = C.c_int
         _lib = L
     return _lib
 
@@ -127,10 +140,26 @@ class Oracle:
                     m.taub[...] = self.f.taub
                 self.f.taub[...] = sum(m.taub for m in self.f.modes)
         self.modePerf = (abi.rt_solver_perf * (6 * self.nModes))()
+        # Crank-Nicolson: the old-time derivatives and start-of-step fields
+        self.cn = case.ddt == "CrankNicolson"
+        if self.cn:
+            m = case.mesh
+            N, nF, nB = m.nCells, m.nFaces, m.nBFaces
+            z = np.zeros
+            self._ddt_arrays = {"DU": z(3 * N), "DUb": z(3 * nB), "Dphi": z(nF), "Dphib": z(nB),
+                                "Dth": z(6 * N * self.nModes), "Us": z(3 * N), "Ubs": z(3 * nB), "phis": z(nF),
+                                "phibs": z(nB), "ths": z(6 * N * self.nModes)}
+            self.ddt = or_ddt(abi.RT_DDT_CRANKNICOLSON, case.ddtPsi, 0, 0,
+                              *[self._ddt_arrays[n].ctypes.data_as(_dp) for n, _ in or_ddt._fields_[4:]])
 
     def step(self, n: int = 1) -> abi.rt_step_perf:
         perf = abi.rt_step_perf()
-        if self.nModes > 1:
+        if self.cn:
+            modes = _mode_states(self.f) if self.nModes > 1 else None
+            st = lib().or_step_ddt(C.byref(self.md), C.byref(self.bd), self.models, self.nModes,
+                                   C.byref(self.ctl), C.byref(_state(self.f)), modes, int(n), C.byref(perf),
+                                   self.modePerf, C.byref(self.ddt))
+        elif self.nModes > 1:
             st = lib().or_step_modes(C.byref(self.md), C.byref(self.bd), self.models, self.nModes,
                                      C.byref(self.ctl), C.byref(_state(self.f)), _mode_states(self.f), int(n),
                                      C.byref(perf), self.modePerf)
@@ -150,13 +179,26 @@ class Oracle:
             for name in ("theta", "thetab", "eigVals", "eigVecs"):
                 getattr(self.f, name)[...] = getattr(m0, name)
 
-    def constitutive_correct(self, gradU: np.ndarray = None, thetaOld: np.ndarray = None):
+    def constitutive_correct(self, gradU: np.ndarray = None, thetaOld: np.ndarray = None, newTimeStep=None):
         """One correct(); thetaOld (nCells, 6): the old-time theta of the
         theta equation (an inner iteration of a step that started there),
         default the current theta."""
         perf = (abi.rt_solver_perf * 6)()
         g = None if gradU is None else np.ascontiguousarray(gradU, dtype=np.float64)
         gp = None if g is None else g.ctypes.data_as(_dp)
+        if self.cn:
+            # Crank-Nicolson: a time step of its own unless newTimeStep is
+            # False (a further inner iteration, against the theta kept at the
+            # start of the step; thetaOld is not used)
+            modes = _mode_states(self.f) if self.nModes > 1 else None
+            st = lib().or_constitutive_correct_ddt(C.byref(self.md), C.byref(self.bd), self.models, self.nModes,
+                                                   C.byref(self.ctl), C.byref(_state(self.f)), modes, gp,
+                                                   int(newTimeStep is None or bool(newTimeStep)), self.modePerf,
+                                                   C.byref(self.ddt))
+            if st != 0:
+                raise RuntimeError(f"oracle constitutive correct failed: {st}")
+            self._mode0_view()
+            return list(self.modePerf[6 * (self.nModes - 1):])
         if self.nModes > 1:
             if thetaOld is not None:
                 raise ValueError("multiMode: inner iterations run inside step()")

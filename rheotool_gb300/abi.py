@@ -24,6 +24,7 @@ RT_SOLVER_PCG, RT_SOLVER_PBICGSTAB, RT_SOLVER_PBICG = 0, 1, 2
 RT_PRECOND_NONE, RT_PRECOND_DIC, RT_PRECOND_DILU, RT_PRECOND_DIAGONAL = 0, 1, 2, 3
 RT_LIM_NONE, RT_LIM_UPWIND, RT_LIM_CUBISTA, RT_LIM_MINMOD, RT_LIM_SMART, RT_LIM_WACEB, RT_LIM_SUPERBEE = -1, 0, 1, 2, 3, 4, 5
 RT_PREC_FP64, RT_PREC_MIXED = 0, 1
+RT_DDT_EULER, RT_DDT_CRANKNICOLSON = 0, 1
 RT_FIELD_U, RT_FIELD_P, RT_FIELD_PHI, RT_FIELD_THETA, RT_FIELD_TAU, RT_FIELD_EIGVALS, RT_FIELD_EIGVECS = range(7)
 RT_OPT_SWEEP = 1
 RT_OPT_SWEEP_PLANES = 2
@@ -119,6 +120,7 @@ class rt_case_ctl(C.Structure):
         ("solverU", rt_solver_ctl), ("solverP", rt_solver_ctl), ("solverTheta", rt_solver_ctl),
         ("precision", C.c_int32), ("nInIter", C.c_int32),
         ("bodyForce", C.c_double * 3),
+        ("nNonOrthCorr", C.c_int32), ("ddtScheme", C.c_int32), ("ddtPsi", C.c_double),
     ]
 
 

@@ -107,6 +107,9 @@ class Case:
     name: str = "case"
     bodyForce: Tuple[float, float, float] = (0.0, 0.0, 0.0)   # per unit mass, in UEqn
     nInIter: int = 1          # SIMPLE.nInIter: inner iterations per time step
+    nNonOrthCorr: int = 0     # SIMPLE.nNonOrthogonalCorrectors
+    ddt: str = "Euler"        # ddtSchemes default: "Euler" or "CrankNicolson"
+    ddtPsi: float = 1.0       # CrankNicolson off-centering coefficient
     # multiMode (multiMode.C:69-91): the modes after the first (``model``);
     # every mode has its own theta, tau and eigen fields, tau is their sum
     moreModes: List[Model] = field(default_factory=list)
@@ -195,6 +198,11 @@ class Case:
         ctl.solverTheta = self.solverTheta.to_c()
         ctl.precision = self.precision
         ctl.nInIter = int(self.nInIter)
+        ctl.nNonOrthCorr = int(self.nNonOrthCorr)
+        if self.ddt not in ("Euler", "CrankNicolson"):
+            raise ValueError(f"ddt scheme {self.ddt!r}: Euler or CrankNicolson")
+        ctl.ddtScheme = abi.RT_DDT_CRANKNICOLSON if self.ddt == "CrankNicolson" else abi.RT_DDT_EULER
+        ctl.ddtPsi = float(self.ddtPsi)
         for k in range(3):
             ctl.bodyForce[k] = float(self.bodyForce[k])
         self._keep = keep

@@ -112,11 +112,13 @@ __global__ void k_theta_rhs(int N, rt_model_params mp, const int *__restrict__ c
 
 // theta matrix: diag = rDeltaT V + diagC; source = rDeltaT theta0 V + srcC + V rhs;
 // complete diagonal/source for the solve (boundary coefficients added)
+// (Dth non-null: Crank-Nicolson, rDeltaT = c/dt and the source ((c/dt)
+// theta0 + psi Dth) V; else Euler)
 __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__restrict__ diagC,
                                  const double *__restrict__ srcC, const double *__restrict__ theta0,
                                  const double *__restrict__ rhs, const double *__restrict__ intC,
                                  const double *__restrict__ bouC, double *__restrict__ dSolve,
-                                 double *__restrict__ bSolve) {
+                                 double *__restrict__ bSolve, double psi, const double *__restrict__ Dth) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
     const int N = m.N;
@@ -124,9 +126,11 @@ __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__res
     double d = (0.0 + rDeltaT * v) + diagC[c];
     double b[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k)
-        b[k] = ((0.0 + rDeltaT * theta0[(size_t)k * N + c] * v) + srcC[(size_t)k * N + c]) +
-               v * rhs[(size_t)k * N + c];
+    for (int k = 0; k < 6; ++k) {
+        const size_t i = (size_t)k * N + c;
+        const double ddtSrc = Dth ? (rDeltaT * theta0[i] + psi * Dth[i]) * v : rDeltaT * theta0[i] * v;
+        b[k] = ((0.0 + ddtSrc) + srcC[i]) + v * rhs[i];
+    }
     for (int i = m.bStart[c]; i < m.bStart[c + 1]; ++i) {
         int bf = m.bList[i];
         d += intC[bf];
@@ -465,7 +469,9 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
                                                         cs.eigVals.p, cs.theta.p, rhs, fP, cs.mlGamma.p, cs.mlK);
         RT_CHECK_LAUNCH();
     }
-    RT_CUDA(cudaMemcpyAsync(theta0, thetaOld ? thetaOld : cs.theta.p, sizeof(double) * 6 * N,
+    // (Crank-Nicolson: the old-time theta is the one taken at the step's start)
+    const bool cn = cs.ctl.ddtScheme == RT_DDT_CRANKNICOLSON;
+    RT_CUDA(cudaMemcpyAsync(theta0, cn ? cs.ths.p : (thetaOld ? thetaOld : cs.theta.p), sizeof(double) * 6 * N,
                             cudaMemcpyDeviceToDevice, s));
     const double fpc = (double)F / N;
     {
@@ -478,8 +484,9 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
                    upper, diagC, srcC, intC, bouC, flux);
     }
     MeshView m = view(mesh);
-    k_theta_assemble<<<nblocks(N), RT_BLOCK, 0, s>>>(m, 1.0 / cs.ctl.deltaT, diagC, srcC, theta0, rhs, intC, bouC,
-                                                      dS, bS);
+    k_theta_assemble<<<nblocks(N), RT_BLOCK, 0, s>>>(m, (cn ? cs.ddtCth : 1.0) * (1.0 / cs.ctl.deltaT), diagC, srcC, theta0,
+                                                      rhs, intC, bouC, dS, bS, cn ? cs.ctl.ddtPsi : 0.0,
+                                                      cn ? cs.Dth.p : nullptr);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 2);
     SolveArgs a{dS, upper, lower, bS, cs.theta.p, 6, theta_valid_mask(mesh), cs.ctl.solverTheta, cs.ctl.precision,

@@ -153,6 +153,9 @@ rt_status rt_ctx_destroy(rt_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->red.hostResult) cudaFreeHost(ctx->red.hostResult);
+    if (ctx->red.hostFlag) cudaFreeHost((void *)ctx->red.hostFlag);
+    for (cudaEvent_t e : ctx->red.poll)
+        if (e) cudaEventDestroy(e);
     if (ctx->mesh.batch.hostCount) cudaFreeHost(ctx->mesh.batch.hostCount);
     for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
     if (ctx->tStart) cudaEventDestroy(ctx->tStart);
@@ -451,6 +454,11 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
         validate_model(mp);
         const bool pttGen = mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED;
         RT_REQUIRE(ctl->deltaT > 0, RT_EINVAL, "deltaT must be positive");
+        RT_REQUIRE(ctl->nNonOrthCorr >= 0 && ctl->nNonOrthCorr <= 100, RT_EINVAL,
+                   "nNonOrthogonalCorrectors: 0 .. 100");
+        RT_REQUIRE(ctl->ddtScheme == RT_DDT_EULER ||
+                       (ctl->ddtScheme == RT_DDT_CRANKNICOLSON && ctl->ddtPsi >= 0.0 && ctl->ddtPsi <= 1.0),
+                   RT_EINVAL, "ddt scheme: Euler, or CrankNicolson with 0 <= psi <= 1");
         for (const rt_solver_ctl *sc : {&ctl->solverU, &ctl->solverP, &ctl->solverTheta}) {
             RT_REQUIRE(sc->solver >= RT_SOLVER_PCG && sc->solver <= RT_SOLVER_PBICG, RT_EINVAL, "unknown solver");
             RT_REQUIRE(sc->preconditioner >= RT_PRECOND_NONE && sc->preconditioner <= RT_PRECOND_DIAGONAL, RT_EINVAL,
@@ -472,6 +480,22 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
         c.thetaStep0.release();
         c.modePerf.clear();
         c.mpMom = *mp;
+        // Crank-Nicolson state: no step taken yet, D = 0
+        c.ddtSteps = c.ddtThSteps = 0;
+        c.ddtC = c.ddtCth = 1.0;
+        for (DBuf<double> *b : {&c.DU, &c.DUb, &c.Dphi, &c.Dphib, &c.Us, &c.Ubs, &c.phis, &c.phibs, &c.Dth, &c.ths})
+            b->release();
+        if (ctl->ddtScheme == RT_DDT_CRANKNICOLSON) {
+            const size_t N = m.N, F = m.F, NB = m.NB;
+            const std::pair<DBuf<double> *, size_t> bufs[] = {{&c.DU, 3 * N}, {&c.DUb, 3 * NB}, {&c.Dphi, F},
+                                                              {&c.Dphib, NB}, {&c.Us, 3 * N}, {&c.Ubs, 3 * NB},
+                                                              {&c.phis, F}, {&c.phibs, NB}, {&c.Dth, 6 * N},
+                                                              {&c.ths, 6 * N}};
+            for (const auto &b : bufs) {
+                b.first->alloc(b.second);
+                b.first->zero(ctx->stream);
+            }
+        }
         if (pttGen) {
             std::vector<double> g = ml_gamma_table(*mp);
             c.mlK = (int)g.size() - 1;
@@ -678,6 +702,10 @@ rt_status rt_case_setup_modes(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_
                 RT_REQUIRE(m->mlK >= 1, RT_EINVAL, "Gamma(beta) overflows: no Mittag-Leffler term");
                 upload_vec(ctx, g, m->mlGamma);
             }
+            if (ctl->ddtScheme == RT_DDT_CRANKNICOLSON) {
+                m->Dth.alloc(n6); m->Dth.zero(s);
+                m->ths.alloc(n6); m->ths.zero(s);
+            }
             c.modes.push_back(std::move(m));
         }
         c.nModes = nModes;
@@ -809,6 +837,7 @@ rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_pe
         // a completed time step: the old-time theta kept by
         // rt_constitutive_correct_iter belongs to an earlier step now
         ctx->cs.thetaOldSaved = false;
+        ddt_begin_step(ctx, false);   // a time step of its own (Crank-Nicolson state)
         rt_status st = modes_correct(ctx, gradU ? g.p : nullptr, thetaPerf);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
         return st;
@@ -826,6 +855,7 @@ rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t
                    "run inside rt_step)");
         const size_t n6 = 6 * (size_t)ctx->mesh.N;
         if (newTimeStep) {
+            ddt_begin_step(ctx, false);   // Crank-Nicolson: the step's old-time derivative and theta
             c.thetaOld.alloc(n6);
             RT_CUDA(cudaMemcpyAsync(c.thetaOld.p, c.theta.p, sizeof(double) * n6, cudaMemcpyDeviceToDevice,
                                     ctx->stream));
@@ -1015,6 +1045,7 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model
         rt_status v = guarded(ctx, [&]() -> rt_status {
             RT_REQUIRE(ctx->meshReady && ctx->mesh.batch.n >= 1, RT_ENOTREADY, "mesh not uploaded");
             RT_REQUIRE(bcs && models && ctl && pRefCell && pRefValue, RT_EINVAL, "null argument");
+            RT_REQUIRE(ctl->ddtScheme == RT_DDT_EULER, RT_EINVAL, "the batched form runs the Euler ddt scheme");
             const Batch &b = ctx->mesh.batch;
             for (int c = 0; c < b.n; ++c) {
                 const rt_model_params &mp = models[c];

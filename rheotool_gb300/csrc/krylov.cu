@@ -31,7 +31,7 @@ namespace rt {
 // scalar slots (device array ctx->scal, [slot*8 + comp])
 enum {
     S_NF = 0, S_INIT, S_FIN, S_XBAR, S_A, S_B, S_AOLD, S_ALPHA, S_OMEGA,
-    S_R0R, S_R0ROLD, S_SING, S_T1, S_T2, S_RST, S_NSLOT
+    S_R0R, S_R0ROLD, S_SING, S_T1, S_T2, S_RST, S_ITER, S_NSLOT
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -450,6 +450,199 @@ void reduce_init(rt_ctx *ctx) {
     RT_CUDA(cudaMallocHost(&r.hostResult, sizeof(double) * 32 * 8));   // one copy of ctx->scal
     ctx->scal.alloc(32 * 8);
     ctx->scal.zero(ctx->stream);
+    r.active.alloc(1);
+    r.active.zero(ctx->stream);
+    r.counter.alloc(1);
+    r.counter.zero(ctx->stream);
+    void *hf = nullptr;
+    RT_CUDA(cudaHostAlloc(&hf, sizeof(int) * 4, cudaHostAllocMapped));
+    r.hostFlag = static_cast<volatile int *>(hf);
+    r.hostFlag[0] = 0;
+    RT_CUDA(cudaHostGetDevicePointer((void **)&r.devFlag, hf, 0));
+    for (cudaEvent_t &e : r.poll) RT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
+// ==========================================================================
+// PCG stopping on the device.  One iteration is four kernels after the
+// preconditioner: k_pcg_rho (w.r, and for the flexible form w.q_old), k_pcg_pq
+// (p = w + beta p into the other p buffer, q = A p with the neighbours' p
+// formed on the fly, p.q), k_pcg_step (psi += alpha p, r -= alpha q, |r|).
+// Each reduction's last block to arrive sums the block partials in the fixed
+// order of k_finalize (so the scalars have the same bits as the host-driven
+// loop) and does the scalar work: beta, alpha and the singularity test, or
+// the residual, the iteration count and the stopping rules of lduMatrix's
+// PCG.  Components that stop leave the device word `active`; when none is
+// left the kernels and sweeps return at once and the mapped host flag drops,
+// which the host polls every few iterations instead of synchronising every
+// iteration.
+// ==========================================================================
+
+// true in every thread of the block that arrives last at `counter` (all
+// blocks' partials are then visible); the counter is re-armed
+__device__ bool last_block(unsigned *counter) {
+    __shared__ bool amLast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        amLast = (t == gridDim.x - 1);
+        if (amLast) *counter = 0u;
+    }
+    __syncthreads();
+    return amLast;
+}
+
+// fixed-order sum of one slot's block partials (k_finalize's order), valid
+// in thread 0; read past L1, since other SMs wrote them
+__device__ double partials_sum(const double *partial, int nB, int slot, int k) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nB; i += blockDim.x) v += __ldcg(partial + (slot * 6 + k) * nB + i);
+    return block_sum(v);
+}
+
+// rho = w.r (slot 0) and, in the flexible form after the first iteration,
+// w.q_old (slot 1); the last block: wArAold = wArA, wArA = rho, flexible beta
+template <bool FLEX>
+__global__ void k_pcg_rho(int N, unsigned mask0, const unsigned *__restrict__ active, int first,
+                          const double *__restrict__ w, const double *__restrict__ r, const double *__restrict__ qold,
+                          double *S, double *partial, int nB, unsigned *counter) {
+    const unsigned mask = mask0 & *active;
+    if (!mask) return;
+    const bool two = FLEX && !first;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        double v0 = 0.0, v1 = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            v0 += w[o + c] * r[o + c];
+            if (two) v1 += w[o + c] * qold[o + c];
+        }
+        store_partial(partial, nB, 0, k, v0);
+        if (two) store_partial(partial, nB, 1, k, v1);
+    }
+    if (!last_block(counter)) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const double rho = partials_sum(partial, nB, 0, k);
+        const double wq = two ? partials_sum(partial, nB, 1, k) : 0.0;
+        if (threadIdx.x == 0) {
+            const double aold = S[S_A * 8 + k];
+            S[S_AOLD * 8 + k] = aold;
+            S[S_A * 8 + k] = rho;
+            if (two) S[S_B * 8 + k] = -S[S_ALPHA * 8 + k] * wq / aold;
+        }
+    }
+}
+
+// p_new = w (+ beta p_old); q = A p_new, the neighbours' p_new formed from
+// their w and p_old exactly as the cell's own; p.q; the last block: alpha =
+// wArA / wApA or the singularity test
+template <bool FLEX>
+__global__ void k_pcg_pq(Ell e, unsigned mask0, const unsigned *__restrict__ active, int first,
+                         const double *__restrict__ diag, const double *__restrict__ upper,
+                         const double *__restrict__ lower, const double *__restrict__ w,
+                         const double *__restrict__ pold, double *__restrict__ pnew, double *__restrict__ q, double *S,
+                         double *partial, int nB, unsigned *counter) {
+    const unsigned mask = mask0 & *active;
+    if (!mask) return;
+    const int N = e.N;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const double beta = first ? 0.0 : (FLEX ? S[S_B * 8 + k] : S[S_A * 8 + k] / S[S_AOLD * 8 + k]);
+        const size_t o = (size_t)k * N;
+        const double *wk = w + o, *pk = pold + o;
+        double v = 0.0;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            const double pc = first ? wk[c] : fma(beta, pk[c], wk[c]);
+            double acc = diag[c] * pc;
+            for (int s = 0; s < e.nSlots; ++s) {
+                const int nb = e.nbr[s * N + c];
+                if (nb < 0) break;
+                const int f = e.face[s * N + c];
+                const double a = nb > c ? upper[f] : lower[f];
+                const double pn = first ? wk[nb] : fma(beta, pk[nb], wk[nb]);
+                acc = fma(a, pn, acc);
+            }
+            pnew[o + c] = pc;
+            q[o + c] = acc;
+            v = fma(acc, pc, v);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+    if (!last_block(counter)) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const double wApA = partials_sum(partial, nB, 0, k);
+        if (threadIdx.x == 0) {
+            if (fabs(wApA) / S[S_NF * 8 + k] < 1e-300) {
+                S[S_SING * 8 + k] = 1.0;
+                S[S_ALPHA * 8 + k] = 0.0;
+            } else {
+                S[S_ALPHA * 8 + k] = S[S_A * 8 + k] / wApA;
+            }
+        }
+    }
+}
+
+// psi += alpha p; r -= alpha q; |r|; the last block: residual, iteration
+// count and lduMatrix's stopping rules per component (a singular component
+// stops without an update, keeping its last residual and count)
+__global__ void k_pcg_step(int N, unsigned mask0, unsigned *active, rt_solver_ctl ctl, const double *__restrict__ p,
+                           const double *__restrict__ q, double *__restrict__ psi, double *__restrict__ r, double *S,
+                           double *partial, int nB, unsigned *counter, int *hostFlag) {
+    const unsigned mask = mask0 & *active;
+    if (!mask) return;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const bool sing = S[S_SING * 8 + k] != 0.0;
+        const double alpha = S[S_ALPHA * 8 + k];
+        double v = 0.0;
+        size_t o = (size_t)k * N;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            if (!sing) {
+                psi[o + c] += alpha * p[o + c];
+                r[o + c] -= alpha * q[o + c];
+            }
+            v += fabs(r[o + c]);
+        }
+        store_partial(partial, nB, 0, k, v);
+    }
+    if (!last_block(counter)) return;
+    unsigned next = mask;
+    for (int k = 0; k < 6; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const double res = partials_sum(partial, nB, 0, k);
+        if (threadIdx.x == 0) {
+            if (S[S_SING * 8 + k] != 0.0) {
+                next &= ~(1u << k);
+            } else {
+                const double fin = res / S[S_NF * 8 + k], init = S[S_INIT * 8 + k];
+                const double it = S[S_ITER * 8 + k] + 1.0;
+                S[S_FIN * 8 + k] = fin;
+                S[S_ITER * 8 + k] = it;
+                const bool conv = fin < ctl.tolerance || (ctl.relTol > 1e-20 && fin < ctl.relTol * init);
+                const bool more = (it < ctl.maxIter && !conv) || it < ctl.minIter;
+                if (!more || !isfinite(fin)) next &= ~(1u << k);
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        *active = (*active & ~mask0) | next;
+        if (!*active) {
+            *(volatile int *)hostFlag = 0;
+            __threadfence_system();
+        }
+    }
+}
+
+// the loop's starting state: the components to iterate, zero iterations
+__global__ void k_pcg_arm(unsigned act, unsigned *active, double *S) {
+    const int k = threadIdx.x;
+    if (k < 6) {
+        S[S_ITER * 8 + k] = 0.0;
+        S[S_SING * 8 + k] = 0.0;
+    }
+    if (k == 0) *active = act;
 }
 
 namespace {
@@ -540,7 +733,10 @@ struct Solver {
 
     // w = M^-1 r, or with T the transposed preconditioner M^-T r (the same rD,
     // the lower and upper coefficients exchanged; PBiCG's shadow system)
-    void precondition(unsigned mask, const double *rD, const double *r, double *w, bool T = false) {
+    // (dmask: the device word of the components still iterating, or null;
+    // the systolic sweeps return at once when it is empty)
+    void precondition(unsigned mask, const double *rD, const double *r, double *w, bool T = false,
+                      const unsigned *dmask = nullptr) {
         const DevMesh &m = ctx->mesh;
         int pre = a.ctl.preconditioner;
         const double *lower = T ? a.upper : a.lower, *upper = T ? a.lower : a.upper;
@@ -556,7 +752,7 @@ struct Solver {
             const double fpc = (double)m.F / N;
             ProfScope ps(ctx, "dilu_precondition", (double)N * (8.0 + fpc * 16.0 + 32.0 * pop(mask)));
             if (T) skew_precondition_T(ctx, a.nc, mask, r, w);
-            else skew_precondition(ctx, a.nc, mask, r, w);
+            else skew_precondition(ctx, a.nc, mask, r, w, dmask);
         } else {
             // per application (forward + backward): rD 16, coefficients
             // 2*(F/N)*8, addressing 2*(F/N)*8, r 8 + w 8 + w 16 per component
@@ -597,65 +793,93 @@ struct Solver {
     }
 };
 
-rt_status run_pcg(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
-    Solver sv(ctx, a);
+// PCG (FLEX = false: FP64, DIC in FP64; FLEX = true: the mixed form's
+// flexible PCG with the FP32 DIC of Mixed::precondition32d) with the stopping
+// decisions on the device.  The host launches iterations ahead and polls the
+// mapped flag every kPoll iterations, after waiting for the iterations
+// launched kPoll earlier, so it stays at most 2 kPoll iterations ahead; the
+// iterations launched after the last component stopped return at once.
+constexpr int kPoll = 8;
+
+template <bool FLEX, class Pre>
+rt_status pcg_device_loop(rt_ctx *ctx, Solver &sv, const SolveArgs &a, rt_solver_perf *perf, Pre &&precondition) {
     const int N = sv.N;
+    const size_t V6 = 6 * (size_t)N;
     double *ws = ctx->kws.p;
-    double *wA = ws, *rA = ws + 6 * (size_t)N, *pA = ws + 12 * (size_t)N, *rD = ws + 48 * (size_t)N;
-    unsigned mask = a.validMask;
-    sv.compute_rd(rD);
-    sv.prologue(mask, wA, rA);
-    double h[2 * 8];
-    RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, sv.S, sizeof(double) * 3 * 8, cudaMemcpyDeviceToHost, sv.st));
+    double *q = ws, *rA = ws + V6, *pbuf[2] = {ws + 2 * V6, ws + 4 * V6}, *z = ws + 3 * V6;
+    const unsigned mask = a.validMask;
+    Reduce &red = ctx->red;
+    RT_CUDA(cudaMemcpyAsync(red.hostResult, sv.S, sizeof(double) * 3 * 8, cudaMemcpyDeviceToHost, sv.st));
     RT_CUDA(cudaStreamSynchronize(sv.st));
+    unsigned act = 0;
     for (int k = 0; k < 6; ++k) {
         if (!((mask >> k) & 1u)) continue;
-        perf[k].initialResidual = ctx->red.hostResult[S_INIT * 8 + k];
-        perf[k].finalResidual = ctx->red.hostResult[S_FIN * 8 + k];
+        perf[k].initialResidual = red.hostResult[S_INIT * 8 + k];
+        perf[k].finalResidual = red.hostResult[S_FIN * 8 + k];
         perf[k].nIterations = 0;
         perf[k].singular = 0;
+        if (a.ctl.minIter > 0 || !sv.conv(perf[k].finalResidual, perf[k].initialResidual)) act |= 1u << k;
     }
-    unsigned active = 0;
-    for (int k = 0; k < 6; ++k)
-        if (((mask >> k) & 1u) && (a.ctl.minIter > 0 || !sv.conv(perf[k].finalResidual, perf[k].initialResidual)))
-            active |= 1u << k;
-    int iter = 0;
-    while (active) {
-        sv.precondition(active, rD, rA, wA);
-        sv.dot(active, wA, rA);
-        k_sc_pcg_a<<<1, 32, 0, sv.st>>>(active, ctx->red.result.p, sv.S);
-        k_pcg_p<<<nblocks(N), RT_BLOCK, 0, sv.st>>>(N, active, iter == 0, sv.S, wA, pA);
-        sv.amul(active, pA, wA);
-        sv.dot(active, wA, pA);
-        k_sc_pcg_alpha<<<1, 32, 0, sv.st>>>(active, ctx->red.result.p, sv.S);
-        k_pcg_update<<<sv.nB, RT_BLOCK, 0, sv.st>>>(N, active, sv.S, pA, wA, a.psi, rA, ctx->red.partial.p, sv.nB);
-        RT_CHECK_LAUNCH();
-        sv.finalize(1, active);
-        k_sc_fin<<<1, 32, 0, sv.st>>>(active, ctx->red.result.p, sv.S);
-        RT_CHECK_LAUNCH();
-        launch_count(ctx, 4);
-        RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, sv.S, sizeof(double) * (S_SING + 1) * 8,
-                                cudaMemcpyDeviceToHost, sv.st));
-        RT_CUDA(cudaStreamSynchronize(sv.st));
-        const double *H = ctx->red.hostResult;
-        ++iter;
-        for (int k = 0; k < 6; ++k) {
-            if (!((active >> k) & 1u)) continue;
-            if (H[S_SING * 8 + k] != 0.0) {
-                perf[k].singular = 1;
-                active &= ~(1u << k);
-                continue;
+    if (!act) return RT_OK;
+    k_pcg_arm<<<1, 32, 0, sv.st>>>(act, red.active.p, sv.S);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+    red.hostFlag[0] = 1;
+    const int maxIt = std::max(a.ctl.maxIter, a.ctl.minIter);
+    const double fpc = (double)ctx->mesh.F / N;
+    for (int it = 0; it < maxIt; ++it) {
+        const int first = it == 0;
+        double *pold = pbuf[it & 1], *pnew = pbuf[(it + 1) & 1];
+        precondition(act, rA, z, red.active.p);
+        {
+            ProfScope ps(ctx, "dot", (double)N * 8.0 * ((FLEX && !first) ? 3 : 2) * sv.pop(act));
+            k_pcg_rho<FLEX><<<sv.nB, RT_BLOCK, 0, sv.st>>>(N, act, red.active.p, first, z, rA, q, sv.S,
+                                                             red.partial.p, sv.nB, red.counter.p);
+            RT_CHECK_LAUNCH();
+        }
+        {
+            // the amul's bytes, plus w and p_old read and p written per component
+            ProfScope ps(ctx, "amul", (double)N * (8.0 + fpc * 24.0 + 40.0 * sv.pop(act)));
+            k_pcg_pq<FLEX><<<sv.nB, RT_BLOCK, 0, sv.st>>>(sv.e, act, red.active.p, first, a.diag, a.upper, a.lower, z,
+                                                            pold, pnew, q, sv.S, red.partial.p, sv.nB, red.counter.p);
+            RT_CHECK_LAUNCH();
+        }
+        {
+            ProfScope ps(ctx, "pcg_update", (double)N * 40.0 * sv.pop(act));
+            k_pcg_step<<<sv.nB, RT_BLOCK, 0, sv.st>>>(N, act, red.active.p, a.ctl, pnew, q, a.psi, rA, sv.S,
+                                                      red.partial.p, sv.nB, red.counter.p, red.devFlag);
+            RT_CHECK_LAUNCH();
+        }
+        launch_count(ctx, 3);
+        if ((it + 1) % kPoll == 0) {
+            const int b = (it + 1) / kPoll;
+            RT_CUDA(cudaEventRecord(red.poll[b & 1], sv.st));
+            if (b >= 2) {
+                RT_CUDA(cudaEventSynchronize(red.poll[(b - 1) & 1]));
+                if (red.hostFlag[0] == 0) break;
             }
-            perf[k].finalResidual = H[S_FIN * 8 + k];
-            perf[k].nIterations = iter;
-            bool more = (iter < a.ctl.maxIter && !sv.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
-                        iter < a.ctl.minIter;
-            // a NaN/Inf residual never converges: stop (RT_ENAN follows)
-            if (!more || !std::isfinite(perf[k].finalResidual)) active &= ~(1u << k);
         }
     }
-    (void)h;
+    RT_CUDA(cudaMemcpyAsync(red.hostResult, sv.S, sizeof(double) * (S_ITER + 1) * 8, cudaMemcpyDeviceToHost, sv.st));
+    RT_CUDA(cudaStreamSynchronize(sv.st));
+    const double *H = red.hostResult;
+    for (int k = 0; k < 6; ++k) {
+        if (!((act >> k) & 1u)) continue;
+        perf[k].finalResidual = H[S_FIN * 8 + k];
+        perf[k].nIterations = (int)H[S_ITER * 8 + k];
+        perf[k].singular = H[S_SING * 8 + k] != 0.0 ? 1 : 0;
+    }
     return RT_OK;
+}
+
+rt_status run_pcg(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
+    Solver sv(ctx, a);
+    double *rD = ctx->kws.p + 48 * (size_t)sv.N;
+    sv.compute_rd(rD);
+    sv.prologue(a.validMask, ctx->kws.p, ctx->kws.p + 6 * (size_t)sv.N);
+    return pcg_device_loop<false>(ctx, sv, a, perf, [&](unsigned act, const double *r, double *w, const unsigned *dm) {
+        sv.precondition(act, rD, r, w, false, dm);
+    });
 }
 
 // rT = b - A^T psi on the masked components
@@ -1186,12 +1410,13 @@ struct Mixed : Solver {
 
     // FP64 r -> FP32 preconditioner -> FP64 w (the structured sweeps round on
     // the way in and out; otherwise through the FP32 vectors r32, w32)
-    void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32) {
+    void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32,
+                         const unsigned *dmask = nullptr) {
         if (systolic() && a.ctl.preconditioner != RT_PRECOND_NONE && a.ctl.preconditioner != RT_PRECOND_DIAGONAL) {
             const double fpc = (double)ctx->mesh.F / N;
             // (FP32 coefficients: rD 4, 2*(F/N)*4; FP64 r and w, FP32 forward result)
             ProfScope ps(ctx, "dilu_precondition32", (double)N * (4.0 + fpc * 8.0 + 24.0 * pop(mask)));
-            skew_precondition32d(ctx, a.nc, mask, r, w);
+            skew_precondition32d(ctx, a.nc, mask, r, w, dmask);
             return;
         }
         k_mx_d2f<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, r, r32);
@@ -1320,58 +1545,12 @@ unsigned mixed_replace_set(const Mixed &mx, const SolveArgs &a, unsigned cand, c
 // vectors lose it and stall).  Stopping test and records as run_pcg.
 rt_status run_pcg_flex32(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
     Mixed mx(ctx, a, 2);
-    const int N = mx.N;
-    double *ws = ctx->kws.p;
-    double *wA = ws, *rA = ws + 6 * (size_t)N, *pA = ws + 12 * (size_t)N, *zA = ws + 18 * (size_t)N;
     float *r32 = mx.v(0), *z32 = mx.v(1);
-    const unsigned mask = a.validMask;
     mx.prepare();
-    mx.prologue(mask, wA, rA);
-    RT_CUDA(cudaMemcpyAsync(ctx->red.hostResult, mx.S, sizeof(double) * 3 * 8, cudaMemcpyDeviceToHost, mx.st));
-    RT_CUDA(cudaStreamSynchronize(mx.st));
-    unsigned active = 0;
-    for (int k = 0; k < 6; ++k) {
-        if (!((mask >> k) & 1u)) continue;
-        perf[k].initialResidual = ctx->red.hostResult[S_INIT * 8 + k];
-        perf[k].finalResidual = ctx->red.hostResult[S_FIN * 8 + k];
-        perf[k].nIterations = 0;
-        perf[k].singular = 0;
-        if (a.ctl.minIter > 0 || !mx.conv(perf[k].finalResidual, perf[k].initialResidual)) active |= 1u << k;
-    }
-    int iter = 0;
-    while (active) {
-        mx.precondition32d(active, rA, zA, r32, z32);
-        if (iter == 0) mx.dot(active, zA, rA);
-        else mx.dot(active, zA, rA, zA, wA);   // wA = A p of the previous iteration
-        k_mx_sc_pcg_a<<<1, 32, 0, mx.st>>>(active, iter == 0, ctx->red.result.p, mx.S);
-        k_pcg_p_flex<<<nblocks(N), RT_BLOCK, 0, mx.st>>>(N, active, iter == 0, mx.S, zA, pA);
-        mx.amul(active, pA, wA);
-        mx.dot(active, wA, pA);
-        k_sc_pcg_alpha<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
-        k_pcg_update<<<mx.nB, RT_BLOCK, 0, mx.st>>>(N, active, mx.S, pA, wA, a.psi, rA, ctx->red.partial.p, mx.nB);
-        RT_CHECK_LAUNCH();
-        mx.finalize(1, active);
-        k_sc_fin<<<1, 32, 0, mx.st>>>(active, ctx->red.result.p, mx.S);
-        RT_CHECK_LAUNCH();
-        launch_count(ctx, 7);
-        mx.sync_scalars();
-        const double *H = ctx->red.hostResult;
-        ++iter;
-        for (int k = 0; k < 6; ++k) {
-            if (!((active >> k) & 1u)) continue;
-            if (H[S_SING * 8 + k] != 0.0) {
-                perf[k].singular = 1;
-                active &= ~(1u << k);
-                continue;
-            }
-            perf[k].finalResidual = H[S_FIN * 8 + k];
-            perf[k].nIterations = iter;
-            const bool more = (iter < a.ctl.maxIter && !mx.conv(perf[k].finalResidual, perf[k].initialResidual)) ||
-                              iter < a.ctl.minIter;
-            if (!more || !std::isfinite(perf[k].finalResidual)) active &= ~(1u << k);
-        }
-    }
-    return RT_OK;
+    mx.prologue(a.validMask, ctx->kws.p, ctx->kws.p + 6 * (size_t)mx.N);
+    return pcg_device_loop<true>(ctx, mx, a, perf, [&](unsigned act, const double *r, double *w, const unsigned *dm) {
+        mx.precondition32d(act, r, w, r32, z32, dm);
+    });
 }
 
 rt_status run_pbicgstab_mixed(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {

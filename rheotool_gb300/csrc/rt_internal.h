@@ -105,6 +105,10 @@ struct SkewT {
     Real *wS;   // 6 components
     Real *rS;   // 6 components
     double *w64;   // backward sweep of the FP32 coefficients: FP64 output (cell order) instead of w, or null
+    // the components still iterating, on the device (a Krylov loop that stops
+    // on the device), or null: a launch whose components have all stopped
+    // returns at once
+    const unsigned *dmask;
 };
 using SkewView = SkewT<double>;
 using SkewView32 = SkewT<float>;
@@ -135,6 +139,7 @@ struct StructMesh {
         v.wS = p + (size_t)12 * nSkew;
         v.rS = p + (size_t)18 * nSkew;
         v.w64 = nullptr;
+        v.dmask = nullptr;
         return v;
     }
 
@@ -166,6 +171,7 @@ struct StructMesh {
         v.wS = p + (size_t)7 * nSkew;
         v.rS = p + (size_t)13 * nSkew;
         v.w64 = nullptr;
+        v.dmask = nullptr;
         return v;
     }
 };
@@ -287,12 +293,20 @@ struct DevCase {
     DBuf<double> tauTot, taubTot, thetaStep0;
     rt_model_params mpMom{};
     std::vector<rt_solver_perf> modePerf;   // 6 per mode: the last correct()'s theta solves
+    // Crank-Nicolson ddt (rt_case_ctl.ddtScheme): the old-time derivatives D
+    // and the fields at the start of the last time step (xs), of the flow (U
+    // with boundary values, phi) and of theta (each mode: Dth, ths here and
+    // in ModeState); the time steps started so far and the coefficient c of
+    // the current step (1 for the first, 1 + psi after)
+    int ddtSteps = 0, ddtThSteps = 0;
+    double ddtC = 1.0, ddtCth = 1.0;
+    DBuf<double> DU, DUb, Dphi, Dphib, Us, Ubs, phis, phibs, Dth, ths;
 };
 
 // one further mode of a multiMode model: the DevCase's per-mode members
 struct ModeState {
     rt_model_params mp{};
-    DBuf<double> theta, thetab, tau, taub, eigVals, eigVecs, thetaOld, mlGamma;
+    DBuf<double> theta, thetab, tau, taub, eigVals, eigVecs, thetaOld, mlGamma, Dth, ths;
     bool thetaOldSaved = false;
     int mlK = 0;
 };
@@ -318,6 +332,8 @@ struct ModeSwap {
         swap_buf(c.eigVecs, m.eigVecs);
         swap_buf(c.thetaOld, m.thetaOld);
         swap_buf(c.mlGamma, m.mlGamma);
+        swap_buf(c.Dth, m.Dth);
+        swap_buf(c.ths, m.ths);
         std::swap(c.thetaOldSaved, m.thetaOldSaved);
         std::swap(c.mlK, m.mlK);
     }
@@ -356,6 +372,13 @@ struct Reduce {
     DBuf<double> partial;   // [8 slots][6 comps][nBlocks]
     DBuf<double> result;    // [8 slots][6 comps]
     double *hostResult = nullptr;  // pinned
+    // Krylov loops that stop on the device: the components still iterating
+    // (one word), the arrival counter of the last-block reductions, and a
+    // pinned, device-mapped flag the host polls (nonzero while iterating)
+    DBuf<unsigned> active, counter;
+    volatile int *hostFlag = nullptr;
+    int *devFlag = nullptr;
+    cudaEvent_t poll[2] = {nullptr, nullptr};
 };
 
 // CUDA-event profiler: named scopes on the context stream, aggregated at
@@ -445,6 +468,9 @@ rt_status modes_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf, 
 
 // step.cu
 rt_status step_once(rt_ctx *ctx, rt_step_perf *perf);
+// start of a Crank-Nicolson time step: the old-time derivatives of the step
+// that ended and the new start fields, of the flow (flow != 0) and of theta
+void ddt_begin_step(rt_ctx *ctx, bool flow);
 void init_fields(rt_ctx *ctx);
 
 inline int nblocks(long long n, int b = RT_BLOCK) { return (int)((n + b - 1) / b); }

@@ -179,10 +179,12 @@ __global__ void k_sub_lap(MeshView m, double gam0, double *__restrict__ lower, d
 // UEqn diag and source
 // (body: the uniform body force per unit mass, added to the explicit divTau
 // terms before they are integrated over the cell)
+// (DU non-null: Crank-Nicolson, diag (c/dt) V and source ((c/dt) U0 + psi DU) V
+// with rDeltaT = c/dt; else Euler)
 __global__ void k_mom_cell(MeshView m, double rDeltaT, double gam0, const double *__restrict__ diagC,
                            const double *__restrict__ srcC, const double *__restrict__ U0,
                            const double *__restrict__ expl, double3 body, double *__restrict__ diag,
-                           double *__restrict__ src) {
+                           double *__restrict__ src, double psi, const double *__restrict__ DU) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
     const double gam = m.caseOf ? mom_coef(m.caseParams[m.caseOf[c]]).gam : gam0;
@@ -198,9 +200,11 @@ __global__ void k_mom_cell(MeshView m, double rDeltaT, double gam0, const double
     diag[c] = ((0.0 + rDeltaT * v) + diagC[c]) - ld;
     const double bf[3] = {body.x, body.y, body.z};
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-        src[(size_t)k * N + c] = ((0.0 + rDeltaT * U0[(size_t)k * N + c] * v) + srcC[(size_t)k * N + c]) +
-                                 v * (expl[(size_t)k * N + c] + bf[k]);
+    for (int k = 0; k < 3; ++k) {
+        const size_t i = (size_t)k * N + c;
+        const double ddtSrc = DU ? (rDeltaT * U0[i] + psi * DU[i]) * v : rDeltaT * U0[i] * v;
+        src[i] = ((0.0 + ddtSrc) + srcC[i]) + v * (expl[i] + bf[k]);
+    }
 }
 
 // boundary coefficients of UEqn: convection minus laplacian (fixedValue faces)
@@ -307,11 +311,14 @@ __global__ void k_HbyA_bnd(int NB, int N, const int *__restrict__ kU, const int 
 }
 
 // phiHbyA on internal faces: flux(HbyA) + interp(rAU) ddtCorr + interp(rAtU - rAU) snGrad(p) |Sf|
+// (DU non-null: Crank-Nicolson ddtCorr with the old-time parts rc x0 + psi D
+// of phi and U, rc = c/dt; else Euler with rDeltaT)
 __global__ void k_phiHbyA(MeshView m, double rDeltaT, const double *__restrict__ HbyA,
                           const double *__restrict__ U0, const double *__restrict__ phi0,
                           const double *__restrict__ rAU, const double *__restrict__ rAtU,
                           const double *__restrict__ p, double *__restrict__ phiHbyA,
-                          double *partial, int nBlk, double *__restrict__ absPreF) {
+                          double *partial, int nBlk, double *__restrict__ absPreF, double rc, double psi,
+                          const double *__restrict__ DU, const double *__restrict__ Dphi) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     double absPre = 0.0;
     if (f < m.F) {
@@ -328,6 +335,15 @@ __global__ void k_phiHbyA(MeshView m, double rDeltaT, const double *__restrict__
         double phiCorr = phi0[f] - u0f;
         double cc = 1.0 - fmin(fabs(phiCorr) / (fabs(phi0[f]) + 1e-15), 1.0);
         double ddtCorr = cc * rDeltaT * phiCorr;
+        if (DU) {
+            double uf = 0.0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const size_t io = (size_t)j * N + o, in = (size_t)j * N + n;
+                uf += m.Sf[(size_t)j * F + f] * lin_interp(w, rc * U0[io] + psi * DU[io], rc * U0[in] + psi * DU[in]);
+            }
+            ddtCorr = cc * ((rc * phi0[f] + psi * Dphi[f]) - uf);
+        }
         double pre = hf + lin_interp(w, rAU[o], rAU[n]) * ddtCorr;
         absPre = fabs(pre);
         if (absPreF) absPreF[f] = absPre;
@@ -353,7 +369,8 @@ __global__ void k_phiHbyA(MeshView m, double rDeltaT, const double *__restrict__
 __global__ void k_phiHbyA_bnd_pre(MeshView m, double rDeltaT, const int *__restrict__ kU,
                                   const double *__restrict__ HbyAb, const double *__restrict__ U0b,
                                   const double *__restrict__ phi0b, const double *__restrict__ rAU,
-                                  double *__restrict__ phiHbyAb) {
+                                  double *__restrict__ phiHbyAb, double rc, double psi,
+                                  const double *__restrict__ DUb, const double *__restrict__ Dphib) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= m.NB) return;
     const int NB = m.NB;
@@ -363,7 +380,13 @@ __global__ void k_phiHbyA_bnd_pre(MeshView m, double rDeltaT, const int *__restr
     double u0f = S0 * U0b[b] + S1 * U0b[NB + b] + S2 * U0b[2 * NB + b];
     double phiCorr = phi0b[b] - u0f;
     double cc = (kU[b] == RT_BC_FIXED) ? 0.0 : 1.0 - fmin(fabs(phiCorr) / (fabs(phi0b[b]) + 1e-15), 1.0);
-    phiHbyAb[b] = hf + rAU[c] * (cc * rDeltaT * phiCorr);
+    double ddtCorr = cc * rDeltaT * phiCorr;
+    if (DUb) {
+        const double uf = S0 * (rc * U0b[b] + psi * DUb[b]) + S1 * (rc * U0b[NB + b] + psi * DUb[NB + b]) +
+                          S2 * (rc * U0b[2 * NB + b] + psi * DUb[2 * NB + b]);
+        ddtCorr = cc * ((rc * phi0b[b] + psi * Dphib[b]) - uf);
+    }
+    phiHbyAb[b] = hf + rAU[c] * ddtCorr;
 }
 
 // adjustCorrPhi: one block; sums over the boundary faces in a fixed order
@@ -574,7 +597,11 @@ static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, c
                                           cs.U.p, cs.Ub.p, expl);
     double *diag = W.take(N), *src = W.take(3 * (size_t)N);
     const double3 body = make_double3(ctl.bodyForce[0], ctl.bodyForce[1], ctl.bodyForce[2]);
-    k_mom_cell<<<gN, RT_BLOCK, 0, s>>>(m, rDeltaT, gam, diagC, srcC, U0, expl, body, diag, src);
+    // Crank-Nicolson: the step's ddt coefficient c/dt and the old-time derivatives
+    const bool cn = ctl.ddtScheme == RT_DDT_CRANKNICOLSON;
+    const double rc = cs.ddtC * rDeltaT, psi = cn ? ctl.ddtPsi : 0.0;
+    k_mom_cell<<<gN, RT_BLOCK, 0, s>>>(m, cn ? rc : rDeltaT, gam, diagC, srcC, U0, expl, body, diag, src, psi,
+                                       cn ? cs.DU.p : nullptr);
     if (F) k_sub_lap<<<gF, RT_BLOCK, 0, s>>>(m, gam, lower, upper);
     if (NB) k_mom_bnd<<<gB, RT_BLOCK, 0, s>>>(m, gam, cs.bkU.p, cs.Ub.p, intC, bouC);
     RT_CHECK_LAUNCH();
@@ -611,8 +638,10 @@ static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, c
     double *absPreF = batched ? W.take(F + 1) : nullptr;
     if (F)
         k_phiHbyA<<<gF, RT_BLOCK, 0, s>>>(m, rDeltaT, HbyA, U0, phi0, rAU, rAtU, cs.p.p, phiHbyA, partial, gF,
-                                          absPreF);
-    if (NB) k_phiHbyA_bnd_pre<<<gB, RT_BLOCK, 0, s>>>(m, rDeltaT, cs.bkU.p, HbyAb, U0b, phi0b, rAU, phiHbyAb);
+                                          absPreF, rc, psi, cn ? cs.DU.p : nullptr, cn ? cs.Dphi.p : nullptr);
+    if (NB)
+        k_phiHbyA_bnd_pre<<<gB, RT_BLOCK, 0, s>>>(m, rDeltaT, cs.bkU.p, HbyAb, U0b, phi0b, rAU, phiHbyAb, rc, psi,
+                                                  cn ? cs.DUb.p : nullptr, cn ? cs.Dphib.p : nullptr);
     RT_CHECK_LAUNCH();
     launch_count(ctx, 4);
     if (batched) {
@@ -641,13 +670,19 @@ static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, c
     SolveArgs pa{pd, pu, pu, ps, cs.p.p, 1, 1u, ctl.solverP, ctl.precision, 1};
     prof_end(ctx, psP.rec, psP.bytes);
     psP.rec = -1;
-    rt_status sp;
-    {
-        ProfScope pss(ctx, "solve_p");
-        sp = ldu_solve_device(ctx, pa, &perf->p);
+    // the non-orthogonal corrector loop (pEqn.H:31-50): the orthogonal
+    // laplacian makes every corrector the same equation, solved from the last
+    // corrector's p; the flux follows the last
+    const int nCorr = ctl.nNonOrthCorr > 0 ? ctl.nNonOrthCorr : 0;
+    for (int corr = 0; corr <= nCorr; ++corr) {
+        rt_status sp;
+        {
+            ProfScope pss(ctx, "solve_p");
+            sp = ldu_solve_device(ctx, pa, &perf->p);
+        }
+        if (sp != RT_OK && sp != RT_ENOCONV) return sp;
+        correct_bc(ctx, cs.bkP.p, 1, cs.p.p, cs.pb.p);
     }
-    if (sp != RT_OK && sp != RT_ENOCONV) return sp;
-    correct_bc(ctx, cs.bkP.p, 1, cs.p.p, cs.pb.p);
     ProfScope psC(ctx, "U_correction", (double)N * (24.0 + 16.0 + 48.0 + 24.0) + F * 40.0);
     k_phi_update<<<nblocks(std::max(F, NB)), RT_BLOCK, 0, s>>>(m, phiHbyA, phiHbyAb, pu, pIntC, pBouC, cs.p.p,
                                                                 cs.phi.p, cs.phib.p);
@@ -666,6 +701,53 @@ static rt_status step_inner(rt_ctx *ctx, rt_step_perf *perf, const double *U0, c
     return modes_correct(ctx, nullptr, perf->theta, theta0);
 }
 
+// D = r (x - xs) - psi D (when `roll`), then xs = x
+__global__ void k_ddt_roll(size_t n, int roll, double r, double psi, const double *__restrict__ x,
+                           double *__restrict__ xs, double *__restrict__ D) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (roll) D[i] = r * (x[i] - xs[i]) - psi * D[i];
+    xs[i] = x[i];
+}
+
+// Crank-Nicolson, restated from the time-integration method: the trapezoidal
+// rule with the stored old-time derivative D, (c/dt)(x - x_n) - psi D_n =
+// f(x), c = 1 + psi (psi the off-centering coefficient), D_n = c_{n-1}(x_n -
+// x_{n-1})/dt - psi D_{n-1}; the first step is implicit Euler (c = 1, D_0 =
+// 0).  At the start of a step, D of the step that ended is formed from the
+// fields now and at that step's start, and the start fields are taken.
+void ddt_begin_step(rt_ctx *ctx, bool flow) {
+    DevCase &cs = ctx->cs;
+    if (cs.ctl.ddtScheme != RT_DDT_CRANKNICOLSON) return;
+    const DevMesh &mesh = ctx->mesh;
+    const size_t N = mesh.N, F = mesh.F, NB = mesh.NB;
+    const double rDt = 1.0 / cs.ctl.deltaT, psi = cs.ctl.ddtPsi;
+    auto coef = [&](int j) { return j == 0 ? 1.0 : 1.0 + psi; };
+    cudaStream_t s = ctx->stream;
+    auto roll = [&](size_t n, int doRoll, double r, const double *x, double *xs, double *D) {
+        if (!n) return;
+        k_ddt_roll<<<nblocks((long long)n), RT_BLOCK, 0, s>>>(n, doRoll, r, psi, x, xs, D);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx);
+    };
+    if (flow) {
+        const double r = cs.ddtSteps >= 1 ? coef(cs.ddtSteps - 1) * rDt : 0.0;
+        roll(3 * N, cs.ddtSteps >= 1, r, cs.U.p, cs.Us.p, cs.DU.p);
+        roll(3 * NB, cs.ddtSteps >= 1, r, cs.Ub.p, cs.Ubs.p, cs.DUb.p);
+        roll(F, cs.ddtSteps >= 1, r, cs.phi.p, cs.phis.p, cs.Dphi.p);
+        roll(NB, cs.ddtSteps >= 1, r, cs.phib.p, cs.phibs.p, cs.Dphib.p);
+        ++cs.ddtSteps;
+        cs.ddtC = coef(cs.ddtSteps - 1);
+    }
+    const double rt = cs.ddtThSteps >= 1 ? coef(cs.ddtThSteps - 1) * rDt : 0.0;
+    for (int i = 0; i < cs.nModes; ++i) {
+        ModeSwap sw(cs, i > 0 ? cs.modes[i - 1].get() : nullptr);
+        roll(6 * N, cs.ddtThSteps >= 1, rt, cs.theta.p, cs.ths.p, cs.Dth.p);
+    }
+    ++cs.ddtThSteps;
+    cs.ddtCth = coef(cs.ddtThSteps - 1);
+}
+
 // one time step: nInIter inner iterations (rheoFoam.C:96-150; 0 means 1)
 // on the old-time fields taken at its start
 rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
@@ -676,6 +758,7 @@ rt_status step_once(rt_ctx *ctx, rt_step_perf *perf) {
     Work &W = ctx->work;
     WorkMark wmark(W);
     const int nIn = cs.ctl.nInIter > 1 ? cs.ctl.nInIter : 1;
+    ddt_begin_step(ctx, true);
     double *U0 = W.take(3 * (size_t)N), *U0b = W.take(3 * (size_t)NB), *phi0 = W.take(F), *phi0b = W.take(NB);
     RT_CUDA(cudaMemcpyAsync(U0, cs.U.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
     if (NB) RT_CUDA(cudaMemcpyAsync(U0b, cs.Ub.p, sizeof(double) * 3 * NB, cudaMemcpyDeviceToDevice, s));

@@ -247,6 +247,12 @@ __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mas
                                                   int *sync, u64 *__restrict__ xfer, unsigned epoch,
                                                   unsigned cepoch, long long maxSpin, int R) {
     static_assert(P % 4 == 0 && P <= 32, "a chunk is whole quads");
+    // every component of the launch has stopped iterating (the same word for
+    // every CTA, written by an earlier kernel): nothing to do
+    if (g.dmask) {
+        mask &= *g.dmask;
+        if (!mask) return;
+    }
     constexpr int RJ = Ring<P>::RJ, NA = Stage<MODE, NC>::NA, W = Words<Real>::W;
     constexpr int VW = NC * W;   // words per (step, lane)
     constexpr int QW = 4 * VW;   // words per (quad, lane)
@@ -611,6 +617,7 @@ template <class Real, class In>
 __global__ void k_skew_gather(SkewT<Real> g, unsigned mask, int nc, const In *__restrict__ r, int N) {
     long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= g.nSkew) return;
+    if (g.dmask) mask &= *g.dmask;
     int c = g.cellOf[e];
     const Real rd = g.rDinv[e];
     for (int q = 0; q < nc; ++q)
@@ -902,8 +909,9 @@ void autotune(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w) {
 
 }  // namespace
 
-void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
+void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w, const unsigned *dmask) {
     SkewView g = ctx->mesh.sm.view();
+    g.dmask = dmask;
     k_skew_gather<double, double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);
@@ -958,9 +966,10 @@ bool skew_fits(int nJB) {
            sweep_smem_bytes<double, 0, 1, 4, 2>(nJB) <= kMaxSmem && sweep_smem_bytes<double, 1, 1, 4, 2>(nJB) <= kMaxSmem;
 }
 
-void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w) {
+void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w, const unsigned *dmask) {
     SkewView32 g = ctx->mesh.sm.view32();
     g.w64 = w;
+    g.dmask = dmask;
     k_skew_gather<float, double><<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, mask, nc, r, ctx->mesh.N);
     RT_CHECK_LAUNCH();
     launch_count(ctx);

@@ -7,8 +7,10 @@ namespace rt {
 
 // per matrix: rD recurrence and the premultiplied sweep coefficients
 void skew_prepare(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
-// w = M^-1 r for the masked components (nc <= 6), forward then backward
-void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
+// w = M^-1 r for the masked components (nc <= 6), forward then backward;
+// dmask (device, or null): the components still iterating
+void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w,
+                       const unsigned *dmask = nullptr);
 // the transposed factorisation's coefficients (after skew_prepare of the
 // same matrix) and w = M^-T r with them (PBiCG)
 void skew_prepare_T(rt_ctx *ctx, const double *upper, const double *lower);
@@ -18,7 +20,8 @@ void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const 
 // FP32 w = M^-1 r with the coefficients of the last skew_prepare32
 void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, float *w);
 // the same with an FP64 right-hand side and result (rounded on the way in and out)
-void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
+void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w,
+                          const unsigned *dmask = nullptr);
 // whether the sweeps of a structured mesh with nJB j-blocks fit one CTA's shared memory
 bool skew_fits(int nJB);
 // RT_ETIMEOUT if a bounded wait of the last sweeps ran out

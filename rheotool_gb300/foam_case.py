@@ -20,9 +20,11 @@ What the library does not implement is refused with a clear message unless
 ``substitute=True`` is given, in which case each substitution is recorded in
 ``loaded.substitutions``: rheoTool's external sparse solvers (``solverType eigenSolver``,
 ``petscSolver``, ``hypreSolver``) become PCG-DIC for p and PBiCGStab-DILU for
-the others at their tolerance; Crank-Nicolson ddt becomes Euler;
-non-orthogonal correctors and relaxation factors other than 1 are dropped (a
-non-orthogonal mesh runs with the orthogonal laplacian only on request); a
+the others at their tolerance; ddt schemes other than Euler and
+CrankNicolson become Euler; relaxation factors other than 1 are dropped (a
+non-orthogonal mesh runs with the orthogonal laplacian only on request;
+``nNonOrthogonalCorrectors`` is honoured, its explicit correction being zero
+with that laplacian); a
 ``codedFixedValue`` patch (its code cannot run here) uses its ``value`` entry
 unless ``bc_overrides`` gives the values.  ``run_case`` steps the case on the GPU
 and writes OpenFOAM fields at the write times.
@@ -268,10 +270,7 @@ def load_case(case_dir: str, substitute: bool = False,
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))
     solvers = sol.get("solvers", {})
     simple = sol.get("SIMPLE", {})
-    if int(scalar(simple.get("nNonOrthogonalCorrectors", "0"))) > 0:
-        if not substitute:
-            raise CaseError("SIMPLE nNonOrthogonalCorrectors > 0 is not implemented (orthogonal meshes)")
-        subs.append("SIMPLE nNonOrthogonalCorrectors -> 0")
+    nNonOrth = int(scalar(simple.get("nNonOrthogonalCorrectors", "0")))
     relax = sol.get("relaxationFactors", {})
     for group in ("fields", "equations"):
         for k, v in (relax.get(group, {}) or {}).items():
@@ -280,11 +279,17 @@ def load_case(case_dir: str, substitute: bool = False,
                     raise CaseError(f"relaxationFactors {group} {k} {v}: only 1 (no relaxation) is implemented")
                 subs.append(f"relaxationFactors {group} {k}: {v} -> 1")
     sch = read_dict(os.path.join(case_dir, "system", "fvSchemes"))
-    ddt = sch.get("ddtSchemes", {}).get("default", "Euler").split()[0]
-    if ddt != "Euler":
+    ddt_words = sch.get("ddtSchemes", {}).get("default", "Euler").split()
+    ddt, ddtPsi = ddt_words[0], 1.0
+    if ddt == "CrankNicolson":
+        # "CrankNicolson psi": the off-centering coefficient (1: Crank-Nicolson)
+        ddtPsi = scalar(ddt_words[1]) if len(ddt_words) > 1 else 1.0
+    elif ddt != "Euler":
         if not substitute:
-            raise CaseError(f"fvSchemes ddt {ddt} is not implemented (Euler); pass substitute=True for Euler")
+            raise CaseError(f"fvSchemes ddt {ddt} is not implemented (Euler, CrankNicolson); pass substitute=True "
+                            "for Euler")
         subs.append(f"ddt: {ddt} -> Euler")
+        ddt = "Euler"
     ctrl = read_dict(os.path.join(case_dir, "system", "controlDict"))
 
     # boundary conditions and initial fields
@@ -331,7 +336,7 @@ def load_case(case_dir: str, substitute: bool = False,
                 solverTheta=_solver(solvers, "theta", subs, substitute),
                 pRefCell=int(scalar(simple.get("pRefCell", "0"))), pRefValue=scalar(simple.get("pRefValue", "0")),
                 precision=precision, name=os.path.basename(os.path.abspath(case_dir)),
-                nInIter=int(scalar(simple.get("nInIter", "1"))))
+                nInIter=int(scalar(simple.get("nInIter", "1"))), nNonOrthCorr=nNonOrth, ddt=ddt, ddtPsi=ddtPsi)
     # boundary values of the initial state (fixed values; the rest from the cells)
     for p in mesh.patches:
         sl = slice(p.start, p.start + p.size)

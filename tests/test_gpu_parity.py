@@ -208,7 +208,11 @@ def test_pbicgstab_multi_rhs_matches_oracle(ctx, precond):
 def test_pbicg_multi_rhs_matches_oracle(ctx, precond, mesh_fn):
     """PBiCG (the Contraction41 tutorials' U and theta solver): the transposed
     DILU sweeps and A^T products of the shadow system, per component against
-    the oracle's solve (same iteration counts, 1e-9)."""
+    the oracle's solve.  BiCG's residuals are erratic on this strongly
+    convective matrix, so two solves that differ only in round-off and stop at
+    the same iteration on a 1e-10 residual agree to about 1e-6; at 1e-13 both
+    are the exact solution to 1e-9 (the iteration counts may then differ by
+    one near the threshold)."""
     from oracle.pyoracle import Oracle
     mesh = mesh_fn()
     case = contraction_case(mesh) if mesh.name.startswith("contraction") else cavity_case(mesh=mesh)
@@ -218,17 +222,22 @@ def test_pbicg_multi_rhs_matches_oracle(ctx, precond, mesh_fn):
     b = rng.normal(size=(nc, mesh.nCells)) * mesh.V
     b[1] = 0.0
     x0 = rng.normal(size=(nc, mesh.nCells)) * 0.01
-    ctl = SolverControl("PBiCG", precond, 1e-10, 0.0, 0, 1000)
     ctx.upload_mesh(mesh)
-    xg = x0.copy()
-    perf = ctx.ldu_solve(diag, upper, lower, b, xg, ctl)
     orc = Oracle(case)
-    for k in range(nc):
-        xo = x0[k].copy()
-        po = orc.ldu_solve(diag, upper, lower, b[k].copy(), xo, ctl)
-        assert perf[k].nIterations == po.nIterations, (k, perf[k].nIterations, po.nIterations)
-        assert bool(perf[k].converged) == bool(po.converged) and po.converged
-        assert rel(xg[k], xo) < 1e-9
+    for tol in (1e-10, 1e-13):
+        ctl = SolverControl("PBiCG", precond, tol, 0.0, 0, 2000)
+        xg = x0.copy()
+        perf = ctx.ldu_solve(diag, upper, lower, b, xg, ctl)
+        for k in range(nc):
+            xo = x0[k].copy()
+            po = orc.ldu_solve(diag, upper, lower, b[k].copy(), xo, ctl)
+            assert bool(perf[k].converged) and po.converged
+            assert orc.residual(diag, upper, lower, b[k], xg[k]) < max(10 * tol, 1e-12)
+            if tol == 1e-10:
+                assert perf[k].nIterations == po.nIterations, (k, perf[k].nIterations, po.nIterations)
+            else:
+                assert abs(perf[k].nIterations - po.nIterations) <= 1
+                assert rel(xg[k], xo) < 1e-9
 
 
 def test_step_contraction_pbicg_tutorial_solvers(ctx):
@@ -583,6 +592,46 @@ def test_multimode_needs_a_common_rho_and_stabilization(ctx):
     assert e.value.status == abi.RT_EINVAL
 
 
+@pytest.mark.parametrize("psi,nInIter", [(1.0, 1), (0.5, 1), (1.0, 2)])
+def test_step_crank_nicolson(ctx, psi, nInIter):
+    """Crank-Nicolson ddt (the Cavity tutorial's ddtSchemes default
+    CrankNicolson 1): fvm::ddt(U), fvm::ddt(theta) and the flux's ddtCorr
+    with the stored old-time derivatives, an implicit Euler first step;
+    against the oracle."""
+    case = cavity_case(12, model="GiesekusLog", alpha=0.1, dt=2e-3)
+    case.ddt, case.ddtPsi, case.nInIter = "CrankNicolson", psi, nInIter
+    assert_step_parity(ctx, case, 5, label=f"cavity12 Giesekus CrankNicolson {psi:g} nInIter {nInIter} (5 steps)")
+
+
+def test_step_crank_nicolson_contraction_multimode(ctx):
+    from oracle.pyoracle import Oracle
+    case = multimode_case(contraction_case(small_contraction(), model="Oldroyd-BLog", dt=0.02), n_extra=1)
+    case.ddt = "CrankNicolson"
+    ref = Oracle(case)
+    ref.step(4)
+    ctx.setup_case(case)
+    ctx.step(4)
+    assert_modes_parity(ctx.fields(), ref.f)
+
+
+def test_constitutive_correct_crank_nicolson(ctx):
+    """correct() as time steps of their own under Crank-Nicolson: each call
+    forms the old-time derivative of theta from the previous one."""
+    from oracle.pyoracle import Oracle
+    case = cavity_case(10, model="GiesekusLog", alpha=0.2)
+    f0 = flow_state(case)
+    case.ddt = "CrankNicolson"
+    o = Oracle(case, f0.copy())
+    ctx.setup_case(case, f0)
+    for _ in range(3):
+        pg = ctx.constitutive_correct()
+        po = o.constitutive_correct()
+        assert [p.nIterations for p in pg] == [p.nIterations for p in po]
+    got = ctx.fields()
+    for name in ("theta", "tau"):
+        assert rel(getattr(got, name), getattr(o.f, name)) < 1e-11, name
+
+
 def test_step_channel_fixed_outlet(ctx):
     from oracle.pyoracle import Oracle
     case = channel_case(model="FENE-PLog", L2=50.0)
@@ -610,11 +659,12 @@ def test_field_roundtrip(ctx):
     ctx.setup_case(case)
     rng = np.random.default_rng(5)
     f = Fields.zeros(case.mesh)
-    for name, a in f.__dict__.items():
-        a[...] = rng.normal(size=a.shape)
+    names = [n for n, a in f.__dict__.items() if isinstance(a, np.ndarray)]
+    for name in names:
+        getattr(f, name)[...] = rng.normal(size=getattr(f, name).shape)
     ctx.set_fields(f)
     g = ctx.fields()
-    for name in f.__dict__:
+    for name in names:
         assert np.array_equal(getattr(g, name), getattr(f, name)), name
 
 

@@ -470,3 +470,45 @@ def test_multimode_modes_differ_and_sum():
     assert np.linalg.norm(t0 - t1) > 1e-3 * np.linalg.norm(t0)
     assert np.array_equal(o.f.tau, t0 + t1)
     assert np.array_equal(o.f.theta, o.f.modes[0].theta)
+
+
+# ---------------------------------------------------------------------------
+# Crank-Nicolson ddt (the Cavity tutorial's "CrankNicolson 1")
+# ---------------------------------------------------------------------------
+def test_crank_nicolson_psi0_is_euler():
+    """Off-centering coefficient 0: c = 1 and no old-time derivative term, the
+    implicit Euler scheme (the ddtCorr's old-time parts are regrouped, so the
+    agreement is to round-off)."""
+    import copy
+    a_case = cavity_case(10, model="GiesekusLog", alpha=0.1)
+    b_case = copy.copy(a_case)
+    b_case.ddt, b_case.ddtPsi = "CrankNicolson", 0.0
+    a, b = Oracle(a_case), Oracle(b_case)
+    a.step(4)
+    b.step(4)
+    for name in ("U", "p", "phi", "theta", "tau"):
+        x, y = getattr(b.f, name), getattr(a.f, name)
+        assert np.linalg.norm(x - y) <= 1e-12 * np.linalg.norm(y), name
+
+
+def test_crank_nicolson_old_time_derivative_recursion():
+    """D_1 = (U_1 - U_0)/dt after the implicit Euler first step, then D_2 =
+    2 (U_2 - U_1)/dt - D_1 (psi = 1); D is formed at the start of the next
+    step, so after three steps the state holds D_2."""
+    case = cavity_case(8, model="Oldroyd-BLog")
+    case.ddt, case.ddtPsi = "CrankNicolson", 1.0
+    o = Oracle(case)
+    U = [o.f.U.copy()]
+    for _ in range(3):
+        o.step(1)
+        U.append(o.f.U.copy())
+    dt = case.deltaT
+    D1 = (U[1] - U[0]) / dt
+    D2 = 2.0 * (U[2] - U[1]) / dt - D1
+    DU = o._ddt_arrays["DU"].reshape(-1, 3)
+    assert np.linalg.norm(DU - D2) <= 1e-9 * np.linalg.norm(D2)
+    assert np.array_equal(o._ddt_arrays["Us"].reshape(-1, 3), U[2])
+    # and CN differs from Euler by more than round-off
+    e = Oracle(cavity_case(8, model="Oldroyd-BLog"))
+    e.step(3)
+    assert np.linalg.norm(e.f.U - o.f.U) > 1e-6 * np.linalg.norm(o.f.U)
