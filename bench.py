@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-steps", type=int, default=10)
+    ap.add_argument("--serve3d-requests", type=int, default=8)
+    ap.add_argument("--serve3d-steps", type=int, default=100)
     ap.add_argument("--precision-sweep", action="store_true",
                     help="instead of the throughput line: the precision sweep on the periodic PTT channel")
     ap.add_argument("--sweep-dims", default="400x100x100", help="periodic channel cells nx x ny x nz")
@@ -274,12 +276,45 @@ def run_served(args):
     plain = poisson_run(plain_cases, args.serve_steps, rate=50.0, slots=1, batch_cells=0, quantum=5,
                         hbm_budget=64 << 30)
     strip = lambda d: {k: v for k, v in d.items() if k != "requests_list"}
-    return {"workload": f"{len(cases)} requests, Poisson 50/s, 2-D cavity (128..256 side) and 2-D contraction "
-                        f"(7k..29k cells) Giesekus cases, {args.serve_steps} steps each; mixed form, 4 slots, "
-                        "small cases batched",
-            "served": strip(served), "plain_fp64_one_request_at_a_time": strip(plain),
-            "speedup_p50": plain["p50_s"] / served["p50_s"] if served["p50_s"] else None,
-            "speedup_throughput": served["cell_steps_per_s"] / plain["cell_steps_per_s"]}
+    out = {"workload": f"{len(cases)} requests, Poisson 50/s, 2-D cavity (128..256 side) and 2-D contraction "
+                       f"(7k..29k cells) Giesekus cases, {args.serve_steps} steps each; mixed form, 4 slots, "
+                       "small cases batched (requests join and leave running batches)",
+           "served": strip(served), "plain_fp64_one_request_at_a_time": strip(plain),
+           "speedup_p50": plain["p50_s"] / served["p50_s"] if served["p50_s"] else None,
+           "speedup_throughput": served["cell_steps_per_s"] / plain["cell_steps_per_s"]}
+    if args.serve3d_requests > 0:
+        out["served_3d"] = run_served_3d(args)
+    return out
+
+
+def run_served_3d(args):
+    """Served form on the serving config's sizes: a Poisson stream (50
+    requests/s) of 3-D 4:1 contraction Giesekus cases of 16k..1M cells (size
+    log-uniform, seeded), each a fixed number of steps (100 by default), in
+    the mixed form on 4 slots; p50/p99 time to solution and aggregate
+    cell-steps/s."""
+    import numpy as np
+    from rheotool_gb300 import abi
+    from rheotool_gb300.case import contraction_case
+    from rheotool_gb300.mesh import contraction_mesh
+    from rheotool_gb300.serve import poisson_run
+    rng = np.random.default_rng(20261204)
+    cases = []
+    for i in range(args.serve3d_requests):
+        target = float(np.exp(rng.uniform(np.log(16e3), np.log(1e6))))
+        f = (target / 1e6) ** (1.0 / 3.0)
+        dims = dict(nx_up=max(4, round(134 * f)), nx_down=max(4, round(132 * f)), ny_in=max(4, round(50 * f)),
+                    ny_out=max(2, round(25 * f)), nz=max(2, round(50 * f)))
+        c = contraction_case(contraction_mesh(**dims))
+        c.precision = abi.RT_PREC_MIXED
+        cases.append(c)
+    served = poisson_run(cases, args.serve3d_steps, rate=50.0, slots=4, batch_cells=0, quantum=10,
+                         hbm_budget=96 << 30)
+    cells = [c.mesh.nCells for c in cases]
+    return {"workload": f"{len(cases)} requests, Poisson 50/s, 3-D planar 4:1 contraction GiesekusLog Wi 2, "
+                        f"{min(cells):,}..{max(cells):,} cells (log-uniform in 16k..1M, seeded), "
+                        f"{args.serve3d_steps} steps each; mixed form, 4 slots",
+            "cells": cells, **{k: v for k, v in served.items() if k != "requests_list"}}
 
 
 def run_precision_sweep(args):

@@ -136,6 +136,23 @@ class BatchContext:
         self.ctx._check(self.ctx.lib.rt_batch_step_perf(self.ctx._ctx, perf), "rt_batch_step_perf")
         return list(perf)
 
+    def set_case_fields(self, states: dict):
+        """Give some cases their fields (case index -> Fields): the others keep
+        the state they have (after setup: their initial state).  The serving
+        loop carries running cases into a new layout this way."""
+        if not states:
+            return
+        f = self.ctx.fields()
+        for i, g in states.items():
+            c0, c1 = self.cellStart[i], self.cellStart[i + 1]
+            f0, f1 = self.faceStart[i], self.faceStart[i + 1]
+            b0, b1 = self.bStart[i], self.bStart[i + 1]
+            for name, lo, hi in (("U", c0, c1), ("Ub", b0, b1), ("p", c0, c1), ("pb", b0, b1), ("phi", f0, f1),
+                                 ("phib", b0, b1), ("theta", c0, c1), ("thetab", b0, b1), ("tau", c0, c1),
+                                 ("taub", b0, b1), ("eigVals", c0, c1), ("eigVecs", c0, c1)):
+                getattr(f, name)[lo:hi] = getattr(g, name)
+        self.ctx.set_fields(f)
+
     def fields(self) -> List[Fields]:
         """Each case's fields."""
         f = self.ctx.fields()

@@ -2,19 +2,23 @@
 
 Requests (a case and a number of time steps) arrive at any time.  The loop
 keeps a set of slots, each driven by its own worker thread on its own CUDA
-stream: a slot holds either one case in its own context or several small
-cases admitted together as one batch (one device mesh, every stage of the
-step one launch for all of them).  A waiting request is admitted as soon as
-a slot is free and its predicted device-memory footprint (bytes per cell
-times its cells, plus a fixed per-slot part) fits in what the budget leaves
-after the footprints of the requests already on the device; the measured
-footprint of each admission is recorded from the library's own allocation
-counter.  Fields stay on the device between steps;
-a slot steps its cases in quanta of a few steps, so the work of all admitted
-requests overlaps on the GPU, and each finished request returns its fields
-and its time to solution.  A case gives the same result alone as in the mix:
-a slot is an independent context, and a batch solves every case with its own
-Krylov scalars and stopping points.
+stream.  A large request runs in a slot of its own; small compatible requests
+share a batch slot (one device mesh, every stage of the step one launch for
+all of them).  A batch slot steps its cases in quanta of a few steps and, at
+every quantum boundary, retires the requests that have taken all their steps
+(their fields go back to the client) and admits waiting compatible requests
+into the running batch: the batch is laid out again with the new membership
+and the running cases carry their fields into it, so a request joins while
+others are mid-flight and leaves as soon as it is done, whatever their step
+counts.  A request is admitted when a slot (or a running batch) has room and
+its predicted device-memory footprint fits what the budget leaves after the
+requests already on the device; the prediction is bytes per cell times cells
+plus a per-slot part, the bytes per cell being the mean of what the library's
+allocation counter measured at the earlier admissions (a default before the
+first).  Fields stay on the device between steps, and a case gives the same
+result alone as in the mix: a slot is an independent context, a batch solves
+every case with its own Krylov scalars and stopping points, and a relayout
+carries each running case's fields unchanged.
 
 No reference counterpart: rheoFoam runs one case per process.
 """
@@ -54,6 +58,7 @@ class Request:
     finished: float = 0.0
     fields: Optional[Fields] = None
     error: Optional[str] = None
+    joined: bool = False          # admitted into a batch that was already running
     done: threading.Event = field(default_factory=threading.Event)
 
     @property
@@ -67,9 +72,11 @@ class Server:
     slots: concurrent slots (worker threads, CUDA streams);
     hbm_budget: device bytes the admitted cases may hold (default: 90 % of
     the free device memory at start);
-    batch_cells: requests at most this many cells are admitted in groups of
-    up to batch_max as one batch slot;
-    quantum: steps a slot takes between two looks at its requests."""
+    batch_cells: requests of at most this many cells share batch slots, up to
+    batch_max requests in one;
+    quantum: steps a slot takes between two looks at its requests;
+    bytes_per_cell: the footprint prediction before any admission has been
+    measured."""
 
     def __init__(self, slots: int = 4, hbm_budget: Optional[int] = None, batch_cells: int = 40000,
                  batch_max: int = 16, quantum: int = 10, device: int = 0, bytes_per_cell: float = 4000.0,
@@ -84,9 +91,9 @@ class Server:
             free, _ = torch.cuda.mem_get_info(device)
             hbm_budget = int(0.9 * free)
         self.budget = hbm_budget - device_bytes()   # what the admitted cases may add
-        self.bytes_per_cell = bytes_per_cell
+        self.default_bytes_per_cell = bytes_per_cell
         self.slot_bytes = slot_bytes
-        self.measured: List[float] = []              # bytes per cell of each admission
+        self.measured: List[float] = []              # bytes per cell of each layout
         self.pending: "queue.Queue[Request]" = queue.Queue()
         self._waiting: List[Request] = []
         self._lock = threading.Lock()
@@ -95,6 +102,7 @@ class Server:
         self._workers = [threading.Thread(target=self._worker, daemon=True) for _ in range(slots)]
         self._next = 0
         self.finished: List[Request] = []
+        self.relayouts = 0                           # batch layouts rebuilt for joins and departures
         for w in self._workers:
             w.start()
 
@@ -118,14 +126,24 @@ class Server:
             w.join()
 
     # ---- admission ---------------------------------------------------------
-    def _footprint(self, cells: int) -> int:
-        return int(self.bytes_per_cell * cells) + self.slot_bytes
-
-    def _take(self) -> Optional[List[Request]]:
-        """The next group to admit (FIFO; small requests grouped), or None."""
+    @property
+    def bytes_per_cell(self) -> float:
+        """The footprint per cell: the mean measured so far, else the default."""
         with self._lock:
-            while not self.pending.empty():
-                self._waiting.append(self.pending.get_nowait())
+            return float(np.mean(self.measured)) if self.measured else self.default_bytes_per_cell
+
+    def _cells_bytes(self, cells: int) -> int:
+        return int((float(np.mean(self.measured)) if self.measured else self.default_bytes_per_cell) * cells)
+
+    def _drain(self):
+        while not self.pending.empty():
+            self._waiting.append(self.pending.get_nowait())
+
+    def _take(self) -> Optional[List]:
+        """The next group to admit into a new slot (FIFO; small compatible
+        requests grouped) with its reservation as the last item, or None."""
+        with self._lock:
+            self._drain()
             if not self._waiting:
                 return None
             head = self._waiting[0]
@@ -134,29 +152,57 @@ class Server:
                 for r in self._waiting[1:]:
                     if len(group) >= self.batch_max:
                         break
-                    if r.case.mesh.nCells <= self.batch_cells and self._batchable(head.case, r.case) \
-                            and r.steps == head.steps:
+                    if r.case.mesh.nCells <= self.batch_cells and self._batchable(head.case, r.case):
                         group.append(r)
-            cells = sum(r.case.mesh.nCells for r in group)
-            need = self._footprint(cells)
+            shares = {r.rid: self._cells_bytes(r.case.mesh.nCells) for r in group}
+            need = sum(shares.values()) + self.slot_bytes
             if self._reserved + need > self.budget:
                 if len(group) > 1:
                     group = [head]
-                    need = self._footprint(head.case.mesh.nCells)
+                    shares = {head.rid: shares[head.rid]}
+                    need = shares[head.rid] + self.slot_bytes
                 if self._reserved + need > self.budget:
                     return None
             for r in group:
                 self._waiting.remove(r)
             self._reserved += need
+            now = time.perf_counter()
             for r in group:
+                r.admitted = now
+            return [group, shares, need]
+
+    def _join(self, like: Case, room: int) -> List:
+        """Waiting requests compatible with a running batch (up to `room`),
+        each with its reservation: [(request, bytes), ...]."""
+        out = []
+        if room <= 0:
+            return out
+        with self._lock:
+            self._drain()
+            for r in list(self._waiting):
+                if len(out) >= room:
+                    break
+                if r.case.mesh.nCells > self.batch_cells or not self._batchable(like, r.case):
+                    continue
+                need = self._cells_bytes(r.case.mesh.nCells)
+                if self._reserved + need > self.budget:
+                    break                     # first come first served: no overtaking past the budget
+                self._waiting.remove(r)
+                self._reserved += need
                 r.admitted = time.perf_counter()
-            return group + [need]
+                r.joined = True
+                out.append((r, need))
+        return out
+
+    def _release(self, nbytes: int):
+        with self._lock:
+            self._reserved -= nbytes
 
     @staticmethod
     def _batchable(a: Case, b: Case) -> bool:
         return all(getattr(a, k) == getattr(b, k) for k in ("deltaT", "divU", "divTheta", "solverU", "solverP",
-                                                            "solverTheta", "precision")) and \
-            np.array_equal(a.mesh.solveDir, b.mesh.solveDir)
+                                                            "solverTheta", "precision", "ddt")) and \
+            np.array_equal(a.mesh.solveDir, b.mesh.solveDir) and len(a.models) == 1 and len(b.models) == 1
 
     # ---- slots ---------------------------------------------------------------
     def _worker(self):
@@ -165,61 +211,110 @@ class Server:
             if got is None:
                 time.sleep(0.002)
                 continue
-            need = [got.pop()]
-
-            def release():
-                with self._lock:
-                    self._reserved -= need[0]
-                    need[0] = 0
-
-            # a context per admission: closing it gives the slot's device
-            # memory back before the next admission is sized
-            ctx = None
+            group, shares, need = got
+            held = {"bytes": need}
             try:
-                before = device_bytes()
-                ctx = Context(self.device)
-                self._run(ctx, got, before, release)
-            except Exception as e:   # the request fails, the loop goes on
-                for r in got:
-                    r.error = f"{type(e).__name__}: {e}"
-                    r.finished = time.perf_counter()
-                    r.done.set()
+                if len(group) == 1 and group[0].case.mesh.nCells > self.batch_cells:
+                    self._run_solo(group[0])
+                else:
+                    self._run_batch(group, held, shares)
+            except Exception as e:   # the slot's requests fail, the loop goes on
+                for r in group:
+                    if not r.done.is_set():
+                        r.error = f"{type(e).__name__}: {e}"
+                        r.finished = time.perf_counter()
+                        r.done.set()
             finally:
-                if ctx is not None:
-                    ctx.close()
-                release()
+                self._release(held["bytes"])
 
-    def _run(self, ctx: Context, group: List[Request], before: int, release):
-        """Set up the slot, step it to the end, hand back the fields; the
-        footprint reservation is held until the worker closes the context."""
-        if len(group) == 1:
-            r = group[0]
-            ctx.setup_case(r.case)
-            slot = None
-        else:
-            slot = BatchContext([r.case for r in group], ctx=ctx)
-        cells = sum(r.case.mesh.nCells for r in group)
-        used = device_bytes() - before    # (other slots may allocate meanwhile: an upper bound)
-        with self._lock:
-            self.measured.append(used / cells)
-        steps = group[0].steps
-        done = 0
-        while done < steps:
-            n = min(self.quantum, steps - done)
-            ctx.step(n)
-            done += n
-        ctx.sync()
-        if slot is None:
-            group[0].fields = ctx.fields()
-        else:
-            for r, f in zip(group, slot.fields()):
-                r.fields = f
+    def _finish(self, reqs: List[Request], fields: List[Fields]):
         now = time.perf_counter()
-        for r in group:
+        for r, f in zip(reqs, fields):
+            r.fields = f
             r.finished = now
             r.done.set()
         with self._lock:
-            self.finished.extend(group)
+            self.finished.extend(reqs)
+
+    def _run_solo(self, r: Request):
+        """A large request in a slot of its own (its own context)."""
+        ctx = None
+        try:
+            before = device_bytes()
+            ctx = Context(self.device)
+            ctx.setup_case(r.case)
+            used = device_bytes() - before    # (other slots may allocate meanwhile: an upper bound)
+            if used > 0:
+                with self._lock:
+                    self.measured.append(used / r.case.mesh.nCells)
+            done = 0
+            while done < r.steps:
+                n = min(self.quantum, r.steps - done)
+                ctx.step(n)
+                done += n
+            ctx.sync()
+            self._finish([r], [ctx.fields()])
+        finally:
+            if ctx is not None:
+                ctx.close()
+
+    def _run_batch(self, group: List[Request], held: Dict[str, int], shares: Dict[int, int]):
+        """A batch slot: step the running requests in quanta; at every
+        quantum boundary retire the finished ones and admit waiting compatible
+        ones into the running batch (a new layout that carries the running
+        cases' fields)."""
+        running = list(group)
+        done = {r.rid: 0 for r in running}
+        states: Dict[int, Fields] = {}       # rid -> fields carried into the next layout
+        ctx = slot = None
+        try:
+            while running:
+                if slot is None:
+                    if ctx is not None:
+                        ctx.close()
+                    before = device_bytes()
+                    ctx = Context(self.device)
+                    slot = BatchContext([r.case for r in running], ctx=ctx)
+                    slot.set_case_fields({i: states[r.rid] for i, r in enumerate(running) if r.rid in states})
+                    states.clear()
+                    used = device_bytes() - before
+                    if used > 0:
+                        with self._lock:
+                            self.measured.append(used / sum(r.case.mesh.nCells for r in running))
+                q = min([self.quantum] + [r.steps - done[r.rid] for r in running])
+                ctx.step(q)
+                for r in running:
+                    done[r.rid] += q
+                leaving = [r for r in running if done[r.rid] >= r.steps]
+                staying = [r for r in running if done[r.rid] < r.steps]
+                joiners = self._join(running[0].case, self.batch_max - len(staying))
+                if not leaving and not joiners:
+                    continue
+                ctx.sync()
+                per_case = slot.fields()
+                fin = []
+                for r, f in zip(running, per_case):
+                    if r in leaving:
+                        fin.append((r, f.copy()))
+                    else:
+                        states[r.rid] = f.copy()
+                self._finish([r for r, _ in fin], [f for _, f in fin])
+                for r, _ in fin:                      # a finished request's share of the reservation
+                    nb = shares.pop(r.rid)
+                    held["bytes"] -= nb
+                    self._release(nb)
+                for r, nb in joiners:
+                    shares[r.rid] = nb
+                    held["bytes"] += nb
+                    done[r.rid] = 0
+                running = staying + [r for r, _ in joiners]
+                slot = None
+                if running:
+                    with self._lock:
+                        self.relayouts += 1
+        finally:
+            if ctx is not None:
+                ctx.close()
 
 
 def percentile(xs: List[float], q: float) -> float:
@@ -246,4 +341,6 @@ def poisson_run(cases: List[Case], steps: int, rate: float, seed: int = 20261203
     cell_steps = sum(r.case.mesh.nCells * r.steps for r in ok)
     return {"requests": len(reqs), "completed": len(ok), "errors": [r.error for r in reqs if r.error][:3],
             "p50_s": percentile(tts, 50), "p99_s": percentile(tts, 99), "mean_s": float(np.mean(tts)) if tts else None,
-            "wall_s": t1 - t0, "cell_steps_per_s": cell_steps / (t1 - t0), "requests_list": reqs}
+            "wall_s": t1 - t0, "cell_steps_per_s": cell_steps / (t1 - t0),
+            "joined_running_batch": sum(1 for r in reqs if r.joined), "relayouts": srv.relayouts,
+            "bytes_per_cell_measured": srv.bytes_per_cell, "requests_list": reqs}

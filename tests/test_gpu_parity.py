@@ -232,7 +232,8 @@ def test_pbicg_multi_rhs_matches_oracle(ctx, precond, mesh_fn):
             xo = x0[k].copy()
             po = orc.ldu_solve(diag, upper, lower, b[k].copy(), xo, ctl)
             assert bool(perf[k].converged) and po.converged
-            assert orc.residual(diag, upper, lower, b[k], xg[k]) < max(10 * tol, 1e-12)
+            if np.any(b[k]):    # (a zero source's normalised residual is 0/0-like at x -> 0)
+                assert orc.residual(diag, upper, lower, b[k], xg[k]) < max(10 * tol, 1e-12)
             if tol == 1e-10:
                 assert perf[k].nIterations == po.nIterations, (k, perf[k].nIterations, po.nIterations)
             else:

@@ -90,3 +90,35 @@ def test_admission_waits_for_memory():
     assert all(r.error is None for r in reqs)
     spans = sorted((r.admitted, r.finished) for r in reqs)
     assert all(spans[i + 1][0] >= spans[i][1] - 1e-3 for i in range(len(spans) - 1))
+
+
+@pytest.mark.parametrize("precision", [abi.RT_PREC_FP64, abi.RT_PREC_MIXED])
+def test_request_joining_a_running_batch_equals_alone(precision):
+    """Continuous batching on the device: requests submitted while a batch is
+    running join it at a quantum boundary (the batch is laid out again and the
+    running case carries its fields into the new layout) and leave when their
+    own steps are done; every result equals the case run alone (1e-8 FP64,
+    1e-6 mixed), the long-running case's included."""
+    cases = mix(precision)
+    long_case, joiners = cases[1], [cases[0], cases[3], cases[4]]
+    srv = Server(slots=1, hbm_budget=8 << 30, batch_cells=2000, batch_max=4, quantum=2)
+    try:
+        first = srv.submit(long_case, 40)
+        t0 = time.time()
+        while first.admitted == 0.0 and time.time() - t0 < 60:
+            time.sleep(0.005)
+        time.sleep(0.05)
+        later = [srv.submit(c, 4 + 2 * i) for i, c in enumerate(joiners)]
+        for r in [first] + later:
+            assert r.done.wait(300), "request not served"
+    finally:
+        srv.close()
+    assert first.error is None and all(r.error is None for r in later)
+    assert any(r.joined for r in later), "no request joined the running batch"
+    assert srv.relayouts >= 1
+    bar = 1e-8 if precision == abi.RT_PREC_FP64 else 1e-6
+    for r in [first] + later:
+        ref = alone(r.case, r.steps)
+        for n in NAMES:
+            e = rel(getattr(r.fields, n), getattr(ref, n))
+            assert e < bar, (r.rid, r.joined, n, e)

@@ -20,6 +20,7 @@ class _Stand:
     peak = 0
     order = []
     batches = []
+    carried = []
     fail_cells = None
 
 
@@ -58,6 +59,10 @@ class FakeBatch:
             _Stand.batches.append(len(cases))
             _Stand.order.extend(c.name for c in cases)
 
+    def set_case_fields(self, states):
+        with _Stand.lock:
+            _Stand.carried.extend(states)
+
     def fields(self):
         return [Fields.zeros(c.mesh) for c in self.cases]
 
@@ -68,7 +73,7 @@ def stand(monkeypatch):
     monkeypatch.setattr(serve, "BatchContext", FakeBatch)
     monkeypatch.setattr(serve, "device_bytes", lambda: 0)
     _Stand.active = _Stand.peak = 0
-    _Stand.order, _Stand.batches, _Stand.fail_cells = [], [], None
+    _Stand.order, _Stand.batches, _Stand.carried, _Stand.fail_cells = [], [], [], None
     return _Stand
 
 
@@ -128,3 +133,36 @@ def test_failing_slot_reports_and_loop_continues(stand):
     reqs = _serve(cases, 3, slots=2, hbm_budget=1 << 40, batch_cells=0)
     assert reqs[-1].error is not None and "stand-in failure" in reqs[-1].error
     assert all(r.error is None for r in reqs[:2])
+
+
+def test_requests_join_and_leave_a_running_batch(stand):
+    """Continuous batching: requests that arrive while a batch runs join it at
+    a quantum boundary (a new layout carrying the running cases' fields), and
+    a request leaves as soon as its own steps are done, whatever the others'."""
+    cases = _cases(6)
+    srv = serve.Server(slots=1, hbm_budget=1 << 40, batch_cells=10 ** 6, batch_max=8, quantum=2)
+    first = [srv.submit(cases[0], 40), srv.submit(cases[1], 4)]
+    time.sleep(0.05)                        # the first two are running
+    later = [srv.submit(c, 6) for c in cases[2:]]
+    reqs = first + later
+    for r in reqs:
+        assert r.done.wait(30)
+    srv.close()
+    assert all(r.error is None and r.fields is not None for r in reqs)
+    assert any(r.joined for r in later)                 # joined a running batch
+    assert srv.relayouts >= 1 and stand.carried          # running cases carried into the new layout
+    assert first[1].finished < first[0].finished        # the short request left first
+    assert len(stand.batches) >= 2
+
+
+def test_measured_footprint_sizes_admission(stand, monkeypatch):
+    """After the first admission the prediction is the measured bytes per
+    cell, not the default."""
+    calls = iter(range(0, 10 ** 9, 64 * 1000))
+    monkeypatch.setattr(serve, "device_bytes", lambda: next(calls))
+    cases = _cases(2)
+    srv = serve.Server(slots=1, hbm_budget=1 << 40, batch_cells=0, bytes_per_cell=1e6, quantum=2)
+    for r in [srv.submit(c, 2) for c in cases]:
+        assert r.done.wait(30)
+    srv.close()
+    assert srv.measured and srv.bytes_per_cell != 1e6
