@@ -286,6 +286,15 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * more planes than one cluster holds; see RT_OPT_SWEEP_PLANES).  0 (default)
  * clears it. */
 #define RT_OPT_STALL_TEST 9
+/* RT_OPT_MIXED_PRECOND: how the mixed form's pressure solve applies its DIC
+ * preconditioner.  0: the exact triangular sweeps (FP32 systolic sweeps on
+ * structured meshes).  k = 1 .. 64: k Jacobi sweeps per triangular factor
+ * (a truncated Neumann series of the same DIC factorisation, the same rD;
+ * Anzt, Chow and Dongarra 2015), each a bandwidth-bound pass over the mesh;
+ * the operator stays symmetric positive definite, the solve takes more
+ * iterations, each far cheaper.  Default 0; the FP64 plain form always uses
+ * the exact sweeps. */
+#define RT_OPT_MIXED_PRECOND 10
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);

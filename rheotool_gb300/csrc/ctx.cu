@@ -282,6 +282,33 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
             upload_vec(ctx, pf, m.pellFace);
             upload_vec(ctx, pn, m.pellNbr);
         }
+        // the preconditioner adjacency split into lower and upper neighbours
+        {
+            std::vector<int> nlo(N, 0), nup(N, 0);
+            for (int f = 0; f < F; ++f) {
+                if (m.hasCoupled && m.coupledH[f]) continue;
+                nlo[md->neighbour[f]]++;
+                nup[md->owner[f]]++;
+            }
+            int mlo = 0, mup = 0;
+            for (int c = 0; c < N; ++c) { mlo = std::max(mlo, nlo[c]); mup = std::max(mup, nup[c]); }
+            m.pnLo = mlo;
+            m.pnUp = mup;
+            std::vector<int> ln((size_t)std::max(mlo, 1) * N, -1), lf((size_t)std::max(mlo, 1) * N, -1);
+            std::vector<int> un((size_t)std::max(mup, 1) * N, -1), uf((size_t)std::max(mup, 1) * N, -1);
+            std::fill(nlo.begin(), nlo.end(), 0);
+            std::fill(nup.begin(), nup.end(), 0);
+            for (int f = 0; f < F; ++f) {   // faces ascending: each cell's slots in face order
+                if (m.hasCoupled && m.coupledH[f]) continue;
+                const int o = md->owner[f], n = md->neighbour[f];
+                ln[(size_t)nlo[n] * N + n] = o; lf[(size_t)nlo[n] * N + n] = f; nlo[n]++;
+                un[(size_t)nup[o] * N + o] = n; uf[(size_t)nup[o] * N + o] = f; nup[o]++;
+            }
+            upload_vec(ctx, ln, m.plNbr);
+            upload_vec(ctx, lf, m.plFace);
+            upload_vec(ctx, un, m.puNbr);
+            upload_vec(ctx, uf, m.puFace);
+        }
         // ---- boundary CSR ----------------------------------------------------
         std::vector<int> bs(N + 1, 0), bl(NB);
         for (int b = 0; b < NB; ++b) bs[md->bCell[b] + 1]++;
@@ -430,6 +457,11 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
         case RT_OPT_MIXED_TIGHTEN:
             RT_REQUIRE(value >= 0 && value <= 12, RT_EINVAL, "RT_OPT_MIXED_TIGHTEN: decades 0 .. 12");
             ctx->mixedTighten = std::pow(10.0, -(double)value);
+            return RT_OK;
+        case RT_OPT_MIXED_PRECOND:
+            RT_REQUIRE(value >= 0 && value <= 64, RT_EINVAL,
+                       "RT_OPT_MIXED_PRECOND: 0 exact sweeps, 1 .. 64 Jacobi sweeps per triangular factor");
+            ctx->mixedJacobi = (int)value;
             return RT_OK;
         case RT_OPT_MIXED_PARTS:
             RT_REQUIRE(value >= 0 && value <= 3, RT_EINVAL, "RT_OPT_MIXED_PARTS: bit 1 Krylov, bit 2 constitutive");

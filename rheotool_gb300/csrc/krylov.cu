@@ -1366,6 +1366,74 @@ __global__ void k_mx_bicg_update(int N, unsigned mask, const double *__restrict_
     }
 }
 
+// --------------------------------------------------------------------------
+// DIC/DILU applied by Jacobi sweeps (RT_OPT_MIXED_PRECOND = m): the forward
+// solve (I + rD L) y = rD r by m sweeps y <- rD r - rD L y from y = rD r,
+// then the backward (I + rD U) z = y by m sweeps z <- y - rD U z from z = y;
+// the truncated Neumann series of the same factorisation (Anzt, Chow and
+// Dongarra 2015), symmetric positive definite for DIC.  FP32 vectors and
+// premultiplied FP32 coefficients over the split lower / upper adjacency;
+// one component (the pressure solve).
+// --------------------------------------------------------------------------
+// lo[j][c] = rD_c a (lower neighbour j), up[j][c] = rD_c a (upper neighbour j)
+__global__ void k_jac_coef(int N, int nLo, int nUp, const int *__restrict__ plFace, const int *__restrict__ puFace,
+                           const double *__restrict__ rDc, const double *__restrict__ upper,
+                           const double *__restrict__ lower, float *__restrict__ rD32, float *__restrict__ lo,
+                           float *__restrict__ up) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const double rd = rDc[c];
+    rD32[c] = (float)rd;
+    for (int j = 0; j < nLo; ++j) {
+        const int f = plFace[(size_t)j * N + c];
+        lo[(size_t)j * N + c] = f >= 0 ? (float)(rd * lower[f]) : 0.0f;
+    }
+    for (int j = 0; j < nUp; ++j) {
+        const int f = puFace[(size_t)j * N + c];
+        up[(size_t)j * N + c] = f >= 0 ? (float)(rd * upper[f]) : 0.0f;
+    }
+}
+
+// the first forward sweep: y0 = rD r (kept) and y1 = y0 - rD L y0, the
+// neighbours' y0 formed on the fly; m = 0: w = y0 (FP64 out)
+__global__ void k_jac_first(int N, int nLo, const int *__restrict__ nbr, const float *__restrict__ lo,
+                            const float *__restrict__ rD32, const double *__restrict__ r, float *__restrict__ y0,
+                            float *__restrict__ y1, double *__restrict__ w, const unsigned *__restrict__ dmask) {
+    if (dmask && !*dmask) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const float b = rD32[c] * (float)r[c];
+    if (!y1) {
+        w[c] = (double)b;
+        return;
+    }
+    float acc = b;
+    for (int j = 0; j < nLo; ++j) {
+        const int nb = nbr[(size_t)j * N + c];
+        if (nb < 0) break;
+        acc = fmaf(-lo[(size_t)j * N + c], rD32[nb] * (float)r[nb], acc);
+    }
+    y0[c] = b;
+    y1[c] = acc;
+}
+
+// one sweep: out = base - sum_j coef_j y_in(nb_j); FP64 out when w is set
+__global__ void k_jac_sweep(int N, int nS, const int *__restrict__ nbr, const float *__restrict__ coef,
+                            const float *__restrict__ base, const float *__restrict__ yin, float *__restrict__ yout,
+                            double *__restrict__ w, const unsigned *__restrict__ dmask) {
+    if (dmask && !*dmask) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    float acc = base[c];
+    for (int j = 0; j < nS; ++j) {
+        const int nb = nbr[(size_t)j * N + c];
+        if (nb < 0) break;
+        acc = fmaf(-coef[(size_t)j * N + c], yin[nb], acc);
+    }
+    if (w) w[c] = (double)acc;
+    else yout[c] = acc;
+}
+
 // FP32 state of one mixed solve
 struct Mixed : Solver {
     float *d32, *u32, *l32, *rD32;   // matrix copy, preconditioner diagonal
@@ -1396,7 +1464,27 @@ struct Mixed : Solver {
             launch_count(ctx);
         }
         const int pre = a.ctl.preconditioner;
-        if (systolic()) {
+        if (jacobi()) {
+            // the exact factorisation's 1/rD in cell order, then the FP32
+            // premultiplied coefficients of the Jacobi sweeps
+            const DevMesh &m = ctx->mesh;
+            const double fpc = (double)m.F / N;
+            {
+                ProfScope ps(ctx, "dilu_rD", (double)N * (16.0 + fpc * 28.0));
+                if (systolic()) {
+                    skew_prepare(ctx, a.diag, a.upper, a.lower);
+                    skew_rdinv_cells(ctx, rD64);
+                } else {
+                    compute_rd(rD64);
+                }
+            }
+            const size_t need = (size_t)(m.pnLo + m.pnUp + 4) * N;
+            if (ctx->jac.n < need) ctx->jac.alloc(need);
+            k_jac_coef<<<nblocks(N), RT_BLOCK, 0, st>>>(N, m.pnLo, m.pnUp, m.plFace.p, m.puFace.p, rD64, a.upper,
+                                                        a.lower, jrD(), jlo(), jup());
+            RT_CHECK_LAUNCH();
+            launch_count(ctx);
+        } else if (systolic()) {
             const double fpc = (double)ctx->mesh.F / N;
             ProfScope ps(ctx, "dilu_rD", (double)N * (16.0 + fpc * 28.0));
             skew_prepare32(ctx, a.diag, a.upper, a.lower);
@@ -1410,8 +1498,50 @@ struct Mixed : Solver {
 
     // FP64 r -> FP32 preconditioner -> FP64 w (the structured sweeps round on
     // the way in and out; otherwise through the FP32 vectors r32, w32)
+    // the Jacobi-swept DIC/DILU of the pressure solve (one component)
+    bool jacobi() const {
+        const int pre = a.ctl.preconditioner;
+        return ctx->mixedJacobi > 0 && a.nc == 1 && (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU);
+    }
+    float *jrD() const { return ctx->jac.p; }
+    float *jlo() const { return ctx->jac.p + N; }
+    float *jup() const { return ctx->jac.p + (size_t)(1 + ctx->mesh.pnLo) * N; }
+    float *jvec(int i) const { return ctx->jac.p + (size_t)(1 + ctx->mesh.pnLo + ctx->mesh.pnUp + i) * N; }
+
+    void jacobi_apply(const double *r, double *w, const unsigned *dmask) {
+        const DevMesh &m = ctx->mesh;
+        const int sweeps = ctx->mixedJacobi;
+        // per sweep: coefficients 4 and addressing 4 per neighbour, base 4, y 4 read, 4 written
+        ProfScope ps(ctx, "dilu_jacobi32", (double)N * (12.0 + 2.0 * sweeps * (12.0 + 4.0 * m.F / N)));
+        float *y0 = jvec(0), *ya = jvec(1), *yb = jvec(2);
+        k_jac_first<<<nblocks(N), RT_BLOCK, 0, st>>>(N, m.pnLo, m.plNbr.p, jlo(), jrD(), r, y0, ya, nullptr, dmask);
+        // forward: y_k = y0 - rD L y_{k-1}
+        float *cur = ya, *spare = yb;
+        for (int k = 1; k < sweeps; ++k) {
+            k_jac_sweep<<<nblocks(N), RT_BLOCK, 0, st>>>(N, m.pnLo, m.plNbr.p, jlo(), y0, cur, spare, nullptr, dmask);
+            std::swap(cur, spare);
+        }
+        // backward from z = y_m: z_k = y_m - rD U z_{k-1}; the last writes FP64 w
+        float *base = cur, *zin = cur, *zout = (cur == ya) ? y0 : ya;
+        float *zalt = (cur == yb) ? y0 : yb;
+        if (cur == y0) zalt = yb;
+        for (int k = 0; k < sweeps; ++k) {
+            const bool last = k == sweeps - 1;
+            k_jac_sweep<<<nblocks(N), RT_BLOCK, 0, st>>>(N, m.pnUp, m.puNbr.p, jup(), base, zin, last ? nullptr : zout,
+                                                         last ? w : nullptr, dmask);
+            zin = zout;
+            std::swap(zout, zalt);
+        }
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 2 * sweeps);
+    }
+
     void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32,
                          const unsigned *dmask = nullptr) {
+        if (jacobi()) {
+            jacobi_apply(r, w, dmask);
+            return;
+        }
         if (systolic() && a.ctl.preconditioner != RT_PRECOND_NONE && a.ctl.preconditioner != RT_PRECOND_DIAGONAL) {
             const double fpc = (double)ctx->mesh.F / N;
             // (FP32 coefficients: rD 4, 2*(F/N)*4; FP64 r and w, FP32 forward result)

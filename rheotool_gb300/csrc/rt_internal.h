@@ -238,6 +238,11 @@ struct DevMesh {
     // empty when the mesh has no coupled faces (the full ELL serves then)
     DBuf<int> pellFace, pellNbr;
     int pnSlots = 0;
+    // the preconditioner's adjacency split by direction: each cell's lower
+    // neighbours (nb < c) in slots 0 .. pnLo - 1 and its upper ones in
+    // 0 .. pnUp - 1, face order, padding -1 (the Jacobi-iterated DIC/DILU)
+    DBuf<int> plNbr, plFace, puNbr, puFace;
+    int pnLo = 0, pnUp = 0;
     // cells (N)
     DBuf<double> C;          // 3N SoA
     DBuf<double> V;
@@ -414,6 +419,11 @@ struct rt_ctx {
     int precision = RT_PREC_FP64;   // of standalone rt_ldu_solve calls
     int mixedParts = 3;             // RT_PREC_MIXED: 1 FP32 Krylov, 2 FP32 constitutive
     double mixedTighten = 1e-2;     // RT_PREC_MIXED: solves stop at tolerance x this factor
+    // RT_PREC_MIXED pressure solve: DIC applied by this many Jacobi sweeps per
+    // triangular factor (0: the exact sweeps); FP32 premultiplied split-ELL
+    // coefficients and three FP32 vectors
+    int mixedJacobi = 0;
+    rt::DBuf<float> jac;
     std::vector<rt_step_perf> batchPerf;   // per case: the last step's solver records
     rt::DBuf<double> scal;       // device scalars of the Krylov loops [32 slots][8]
     rt::DBuf<double> stage;      // staging for AoS <-> SoA field transfers

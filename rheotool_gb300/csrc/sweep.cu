@@ -920,6 +920,21 @@ void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, doub
     launch_mode<double, 1>(ctx, g, nc, mask, w);
 }
 
+// 1/rD of the last skew_prepare, in cell order
+__global__ void k_skew_rdinv_cells(SkewView g, double *__restrict__ rDc) {
+    long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= g.nSkew) return;
+    const int c = g.cellOf[e];
+    if (c >= 0) rDc[c] = g.rDinv[e];
+}
+
+void skew_rdinv_cells(rt_ctx *ctx, double *rDc) {
+    SkewView g = ctx->mesh.sm.view();
+    k_skew_rdinv_cells<<<nblocks(g.nSkew), RT_BLOCK, 0, ctx->stream>>>(g, rDc);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+}
+
 void skew_prepare_T(rt_ctx *ctx, const double *upper, const double *lower) {
     StructMesh &s = ctx->mesh.sm;
     SkewView g = s.viewT();

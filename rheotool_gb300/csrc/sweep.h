@@ -15,6 +15,8 @@ void skew_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, doub
 // same matrix) and w = M^-T r with them (PBiCG)
 void skew_prepare_T(rt_ctx *ctx, const double *upper, const double *lower);
 void skew_precondition_T(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
+// 1/rD of the last skew_prepare in cell order (N doubles)
+void skew_rdinv_cells(rt_ctx *ctx, double *rDc);
 // mixed precision: skew_prepare, then FP32 copies of the sweep coefficients
 void skew_prepare32(rt_ctx *ctx, const double *diag, const double *upper, const double *lower);
 // FP32 w = M^-1 r with the coefficients of the last skew_prepare32

@@ -212,3 +212,42 @@ def test_mixed_constitutive_correct(ctx, model, kw):
     for name in ("theta", "tau", "eigVals"):
         assert rel(getattr(got, name), getattr(ref.f, name)) < TOL_MIXED, (name, rel(getattr(got, name), getattr(ref.f, name)))
     assert rel(recon(got.eigVals, got.eigVecs), recon(ref.f.eigVals, ref.f.eigVecs)) < TOL_MIXED
+
+
+@pytest.mark.parametrize("mesh_name", sorted(MESHES))
+@pytest.mark.parametrize("sweeps", [1, 4, 8])
+def test_mixed_pcg_jacobi_dic(ctx, mesh_name, sweeps):
+    """RT_OPT_MIXED_PRECOND: the mixed pressure solve with its DIC applied by
+    Jacobi sweeps (a truncated Neumann series of the same factorisation) stops
+    on the same FP64 residual test and gives the FP64 solution within the
+    mixed bar; more sweeps, fewer iterations."""
+    from oracle.pyoracle import Oracle
+    mesh = MESHES[mesh_name]()
+    rng = np.random.default_rng(34)
+    diag, upper, lower = laplacian_system(mesh, rng)
+    b = rng.normal(size=mesh.nCells) * mesh.V
+    x0 = rng.normal(size=mesh.nCells) * 0.1
+    ctl = SolverControl("PCG", "DIC", 1e-10, 0.0, 0, 5000)
+    ctx.upload_mesh(mesh)
+    try:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, sweeps)
+        xg, perf = _solve(ctx, mesh, diag, upper, lower, b[None], x0, ctl, abi.RT_PREC_MIXED, abi.SWEEP_AUTO)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 0)
+    pg = perf[0]
+    xo = x0.copy()
+    po = Oracle(_case_for(mesh)).ldu_solve(diag, upper, lower, b, xo, ctl)
+    assert pg.converged and po.converged
+    assert foam_residual(mesh, diag, upper, lower, b, xg, x0) < ctl.tolerance
+    assert rel(xg, xo) < TOL_MIXED
+    # the approximate factorisation costs iterations, fewer with more sweeps
+    assert po.nIterations <= pg.nIterations <= 8 * po.nIterations + 50
+
+
+def test_mixed_step_contraction3d_jacobi_dic(ctx):
+    """Full mixed steps with the Jacobi-swept DIC in the pressure solve."""
+    try:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 6)
+        _mixed_step_check(ctx, contraction_case(small_contraction()), 5)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 0)
