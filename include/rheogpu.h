@@ -295,6 +295,12 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * iterations, each far cheaper.  Default 0; the FP64 plain form always uses
  * the exact sweeps. */
 #define RT_OPT_MIXED_PRECOND 10
+/* RT_OPT_BATCH_PERSISTENT: the batched form's pressure solve on structured
+ * 2-D cases (up to 256 rows) as one persistent CTA per case, each running
+ * all the iterations of its case in one launch (1, default), or as a
+ * per-iteration launch sequence replayed for all cases (0).  Both give every
+ * case the same iterates bit for bit. */
+#define RT_OPT_BATCH_PERSISTENT 11
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);

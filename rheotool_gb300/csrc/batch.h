@@ -44,5 +44,8 @@ void sweep2d_prepare(rt_ctx *ctx, const double *diag, const double *upper, const
 void sweep2d_precondition(rt_ctx *ctx, int nc, unsigned mask, const float *r, float *w);
 void sweep2d_precondition(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w);
 rt_status sweep2d_check(rt_ctx *ctx);
+// the skewed layout of the batch (for the per-case persistent solver)
+Skew2D<float> sweep2d_view32(rt_ctx *ctx);
+Skew2D<double> sweep2d_view64(rt_ctx *ctx);
 
 }  // namespace rt

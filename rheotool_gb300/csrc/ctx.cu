@@ -463,6 +463,10 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
                        "RT_OPT_MIXED_PRECOND: 0 exact sweeps, 1 .. 64 Jacobi sweeps per triangular factor");
             ctx->mixedJacobi = (int)value;
             return RT_OK;
+        case RT_OPT_BATCH_PERSISTENT:
+            RT_REQUIRE(value == 0 || value == 1, RT_EINVAL, "RT_OPT_BATCH_PERSISTENT: 0 or 1");
+            ctx->batchPersistent = (int)value;
+            return RT_OK;
         case RT_OPT_MIXED_PARTS:
             RT_REQUIRE(value >= 0 && value <= 3, RT_EINVAL, "RT_OPT_MIXED_PARTS: bit 1 Krylov, bit 2 constitutive");
             ctx->mixedParts = (int)value;

@@ -25,6 +25,7 @@
 
 #include "batch.h"
 #include "real_ops.cuh"
+#include "sweep2d_cta.cuh"
 
 namespace rt {
 
@@ -620,6 +621,188 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
         if ((vm >> k) & 1u) w[(size_t)k * N + c] = rD ? rD[c] * r[(size_t)k * N + c] : r[(size_t)k * N + c];
 }
 
+// ---- the persistent per-case PCG -------------------------------------------
+// One CTA per case runs the case's whole pressure solve (one component,
+// structured 2-D cases with at most 8 j-blocks): the same operations, in the
+// same order and with the same per-case reduction tree, as one iteration of
+// BSolver::pcg_iteration replayed until the case stops, with __syncthreads
+// between the phases instead of kernel boundaries.  The block partials of a
+// reduction are the launch path's (one per 256-cell block of the case, summed
+// by bsum), and their sum is k_b_fin's (32 lanes over the case's blocks,
+// then a shuffle tree), so a case's iterates have the launch path's bits.
+
+// sum of one slot's partials of case cb in k_b_fin's order; every thread gets it
+__device__ double case_sum(const double *partial, int nBlk, int slot, int b0, int b1) {
+    __shared__ double sv;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = 0.0;
+        for (int i = b0 + (int)threadIdx.x; i < b1; i += 32) v += partial[(slot * 6 + 0) * nBlk + i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) sv = v;
+    }
+    __syncthreads();
+    return sv;
+}
+
+template <class V>
+__global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<V> g, BSeg S, Ctl ctl, int mixed,
+                                                          const V *__restrict__ d32, const V *__restrict__ u32,
+                                                          const V *__restrict__ l32, const double *__restrict__ diag,
+                                                          const double *__restrict__ upper,
+                                                          const double *__restrict__ lower,
+                                                          const double *__restrict__ b, double *__restrict__ psi,
+                                                          V *r, V *w, V *p, V *q, V *x, double *partial, int *err,
+                                                          long long maxSpin, int cap) {
+    __shared__ __align__(16) V ring[8 * s2d::kRJ];
+    __shared__ int sProg[32];
+    const int cb = blockIdx.x, sg = cb * 8, tid = threadIdx.x, N = t.N;
+    const int b0 = t.caseBlk[cb], b1 = t.caseBlk[cb + 1];
+    const int c0 = t.blkCell0[b0], c1 = t.blkCell1[b1 - 1];
+    const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
+    // block partial of the launch path's 256-cell block blk: bsum over its cells
+    auto block_partial = [&](int slot, int blk, double v) {
+        const double sm = bsum(v);
+        if (tid == 0) partial[(slot * 6 + 0) * t.nBlk + blk] = sm;
+    };
+    for (int it = 0; it < cap; ++it) {
+        __syncthreads();
+        if (!S.active[sg]) break;
+        // ---- w = M^-1 r: gather, forward and backward sweeps of this case
+        for (long long i = e0 + tid; i < e1; i += blockDim.x) {
+            const int c = g.cellOf[i];
+            g.rS[i] = c >= 0 ? r[c] : V(0);
+        }
+        for (int mode = 0; mode < 2; ++mode) {
+            if (tid < 32) sProg[tid] = 0;
+            __syncthreads();
+            if (mode == 0) sweep2d_cta<V, 0, 1, 8>(g, cb, 1u, nullptr, N, err, maxSpin, ring, sProg);
+            else sweep2d_cta<V, 1, 1, 8>(g, cb, 1u, w, N, err, maxSpin, ring, sProg);
+            __syncthreads();
+        }
+        if (*(volatile int *)err) break;
+        // ---- rho = w.r (and w.q_old in the flexible form)
+        for (int blk = b0; blk < b1; ++blk) {
+            const int c = t.blkCell0[blk] + tid;
+            const bool in = c < t.blkCell1[blk];
+            block_partial(0, blk, in ? (double)w[c] * (double)r[c] : 0.0);
+            if (mixed) block_partial(1, blk, in ? (double)w[c] * (double)q[c] : 0.0);
+        }
+        const double rho = case_sum(partial, t.nBlk, 0, b0, b1);
+        const double wq = mixed ? case_sum(partial, t.nBlk, 1, b0, b1) : 0.0;
+        if (tid == 0) {   // k_b_pcg_a
+            const double aold = S.A[sg];
+            S.Aold[sg] = aold;
+            S.A[sg] = rho;
+            S.beta[sg] = mixed ? -S.alpha[sg] * wq / aold : rho / aold;
+        }
+        __syncthreads();
+        // ---- p = w (+ beta p)
+        {
+            const bool first = S.iter[sg] == 0;
+            const V beta = V(S.beta[sg]);
+            for (int c = c0 + tid; c < c1; c += blockDim.x) p[c] = first ? w[c] : fma(beta, p[c], w[c]);
+        }
+        __syncthreads();
+        // ---- q = A p (the vector type's matrix copy; FP32: differences form)
+        for (int c = c0 + tid; c < c1; c += blockDim.x) {
+            const V pc = p[c];
+            V acc = V(d32[c]) * pc;
+            for (int s = 0; s < e.nSlots; ++s) {
+                const int nb = e.nbr[s * N + c];
+                if (nb < 0) break;
+                const int f = e.face[s * N + c];
+                acc = fma(V(nb > c ? u32[f] : l32[f]), sizeof(V) == 4 ? p[nb] - pc : p[nb], acc);
+            }
+            q[c] = acc;
+        }
+        __syncthreads();
+        // ---- alpha = rho / q.p, or the singularity stop
+        for (int blk = b0; blk < b1; ++blk) {
+            const int c = t.blkCell0[blk] + tid;
+            block_partial(0, blk, c < t.blkCell1[blk] ? (double)q[c] * (double)p[c] : 0.0);
+        }
+        const double wApA = case_sum(partial, t.nBlk, 0, b0, b1);
+        if (tid == 0) {   // k_b_pcg_alpha
+            if (fabs(wApA) / S.nf[sg] < 1e-300) {
+                S.sing[sg] = 1;
+                S.alpha[sg] = 0.0;
+            } else {
+                S.alpha[sg] = S.A[sg] / wApA;
+            }
+        }
+        __syncthreads();
+        // ---- x += alpha p; r -= alpha q; |r|
+        {
+            const bool sing = S.sing[sg] != 0;
+            const V alpha = V(S.alpha[sg]);
+            for (int blk = b0; blk < b1; ++blk) {
+                const int c = t.blkCell0[blk] + tid;
+                double v = 0.0;
+                if (c < t.blkCell1[blk]) {
+                    V rr = r[c];
+                    if (!sing) {
+                        x[c] = fma(alpha, p[c], x[c]);
+                        rr = fma(-alpha, q[c], rr);
+                        r[c] = rr;
+                    }
+                    v = fabs((double)rr);
+                }
+                block_partial(0, blk, v);
+            }
+        }
+        const double rs = case_sum(partial, t.nBlk, 0, b0, b1);
+        if (tid == 0) {   // k_b_iter_fin
+            if (S.sing[sg]) {
+                S.active[sg] = 0;
+            } else {
+                const double fin = rs / S.nf[sg];
+                S.fin[sg] = fin;
+                S.iter[sg] += 1;
+                if (mixed) {
+                    S.repl[sg] = (fin < kReplaceB * S.last[sg] || bconv(ctl, fin, S.init[sg]) ||
+                                  S.iter[sg] >= ctl.maxIter || !isfinite(fin)) ? 1 : 0;
+                } else {
+                    const bool c = bconv(ctl, fin, S.init[sg]);
+                    const bool more = (S.iter[sg] < ctl.maxIter && !c) || S.iter[sg] < ctl.minIter;
+                    S.conv[sg] = c ? 1 : 0;
+                    if (!more || !isfinite(fin)) S.active[sg] = 0;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- residual replacement (mixed): psi += x, x = 0, r = b - A psi
+        if (S.repl[sg]) {
+            for (int c = c0 + tid; c < c1; c += blockDim.x) {
+                psi[c] += (double)x[c];
+                x[c] = V(0);
+            }
+            __syncthreads();
+            for (int blk = b0; blk < b1; ++blk) {
+                const int c = t.blkCell0[blk] + tid;
+                double v = 0.0;
+                if (c < t.blkCell1[blk]) {
+                    const double rr = b[c] - brow_mul(e, c, diag, upper, lower, psi);
+                    r[c] = (V)rr;
+                    v = fabs(rr);
+                }
+                block_partial(0, blk, v);
+            }
+            const double rt = case_sum(partial, t.nBlk, 0, b0, b1);
+            if (tid == 0 && S.active[sg]) {   // k_b_after
+                const double fin = rt / S.nf[sg];
+                S.fin[sg] = fin;
+                S.last[sg] = fin;
+                const bool c = bconv(ctl, fin, S.init[sg]);
+                const bool more = (S.iter[sg] < ctl.maxIter && !c) || S.iter[sg] < ctl.minIter;
+                S.conv[sg] = c ? 1 : 0;
+                if (!more || !isfinite(fin)) S.active[sg] = 0;
+            }
+        }
+        if (tid == 0) S.repl[sg] = 0;
+    }
+}
+
 // ---- host side --------------------------------------------------------------
 template <class V>
 struct BSolver {
@@ -840,6 +1023,27 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
     };
     int done = 0;
     const int cap = a.ctl.maxIter + 2;
+    // the pressure solve of structured 2-D cases: one persistent CTA per case
+    // runs every iteration of its case (RT_OPT_BATCH_PERSISTENT)
+    const int pre = a.ctl.preconditioner;
+    Batch &bt = ctx->mesh.batch;
+    if (active && pcg && ctx->batchPersistent && bt.sweep2d && a.nc == 1 && bt.maxJB <= 8 &&
+        (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU)) {
+        Skew2D<V> g;
+        if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);
+        else g = sweep2d_view64(ctx);
+        {
+            ProfScope ps(ctx, "batch_pcg_persistent");
+            k_b_pcg_case<V><<<bt.n, RT_BLOCK, 0, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
+                                                          sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
+                                                          sv.v(1), sv.v(2), sv.v(3), x, sv.partial, bt.sErr.p,
+                                                          1ll << 22, cap);
+            RT_CHECK_LAUNCH();
+        }
+        launch_count(ctx);
+        bt.sPending = true;
+        active = 0;
+    }
     if (active) {
         body();   // first iteration eagerly (sets kernel attributes outside any capture)
         ++done;
@@ -874,7 +1078,6 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
     RT_CHECK_LAUNCH();
     launch_count(ctx);
     // records of every segment
-    Batch &bt = ctx->mesh.batch;
     const int nSeg = sv.nSeg;
     bt.hostSegD.resize((size_t)12 * nSeg);
     bt.hostSegI.resize((size_t)6 * nSeg + 8);

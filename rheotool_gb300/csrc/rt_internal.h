@@ -424,6 +424,10 @@ struct rt_ctx {
     // coefficients and three FP32 vectors
     int mixedJacobi = 0;
     rt::DBuf<float> jac;
+    // batched form: the pressure solve of structured 2-D cases as one
+    // persistent CTA per case (RT_OPT_BATCH_PERSISTENT; 0: the per-iteration
+    // launch sequence)
+    int batchPersistent = 1;
     std::vector<rt_step_perf> batchPerf;   // per case: the last step's solver records
     rt::DBuf<double> scal;       // device scalars of the Krylov loops [32 slots][8]
     rt::DBuf<double> stage;      // staging for AoS <-> SoA field transfers

@@ -122,3 +122,25 @@ def test_batch_layout_rejects_a_face_across_cases(ctx):
     st = ctx.lib.rt_batch_layout(ctx._ctx, 2, abi.iptr(bad), abi.iptr(fs), abi.iptr(bs), None, None)
     assert st == abi.RT_EINVAL
     ctx.mesh = None
+
+
+@pytest.mark.parametrize("precision", [abi.RT_PREC_FP64, abi.RT_PREC_MIXED])
+def test_batch_persistent_pressure_solve_equals_launch_sequence(precision):
+    """The batched pressure solve as one persistent CTA per case (all its
+    iterations in one launch) repeats the per-iteration launch sequence's
+    arithmetic: the same fields, bit for bit, and the same iteration counts."""
+    cases = cavity_sweep(n_cases=10, n_min=16, n_max=96, seed=9, dt=2e-3, precision=precision)
+    out = {}
+    for persistent in (0, 1):
+        bt = BatchContext(cases)
+        try:
+            bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, persistent)
+            bt.step(3)
+            out[persistent] = (bt.fields(), [p.p.nIterations for p in bt.case_perf()])
+        finally:
+            bt.ctx.close()
+    assert out[0][1] == out[1][1]
+    assert max(out[1][1]) > 20
+    for i in range(len(cases)):
+        for n in NAMES:
+            assert np.array_equal(getattr(out[0][0][i], n), getattr(out[1][0][i], n)), (i, n)
