@@ -77,6 +77,10 @@ def parse():
     ap.add_argument("--sweep-dims", default="400x100x100", help="periodic channel cells nx x ny x nz")
     ap.add_argument("--sweep-steps", type=int, default=3)
     ap.add_argument("--no-sweep", action="store_true", help="skip the precision sweep key of the default line")
+    ap.add_argument("--no-check", action="store_true", help="skip the mixed-vs-converged-FP64 check on the headline")
+    ap.add_argument("--check-steps", type=int, default=4)
+    ap.add_argument("--mixed-precond", type=int, default=None,
+                    help="RT_OPT_MIXED_PRECOND of the mixed form (Jacobi sweeps of its pressure DIC; 0 exact)")
     return ap.parse_args()
 
 
@@ -378,6 +382,78 @@ def run_precision_sweep(args):
             "data": "synthetic", "results": result}
 
 
+def lognormal_contraction_state(case, sigma=0.1, seed=20261203):
+    """The contraction's initial fields with the seeded lognormal
+    log-conformation of the precision sweep (theta = Q diag(sigma z) Q^T, z ~
+    N(0, 1)^3, Q Haar-random): every cell's conformation eigenvalues apart,
+    tau = etaP/lambda (A - I); U = 0, phi from the inlet."""
+    import numpy as np
+    from rheotool_gb300.case import Fields, lognormal_conformation
+    m, md = case.mesh, case.model
+    f = Fields.zeros(m)
+    for p in m.patches:   # boundary values: fixed values from the BCs, the rest from the cells
+        sl = slice(p.start, p.start + p.size)
+        for name, nc in (("U", 3), ("p", 1), ("theta", 6), ("tau", 6)):
+            kind, val = case.bcs[p.name][name]
+            if kind == "fixedValue" and val is not None:
+                getattr(f, name + "b")[sl] = np.broadcast_to(np.asarray(val, dtype=np.float64),
+                                                             getattr(f, name + "b")[sl].shape)
+    f.phib[:] = (m.bSf * f.Ub).sum(1)
+    th, ev, vv = lognormal_conformation(m.nCells, sigma, seed)
+    f.theta[:], f.eigVals[:], f.eigVecs[:] = th, ev, vv
+    R = vv.reshape(-1, 3, 3)
+    T = md.etaP / md.lambda_ * (np.einsum("nij,nj,nkj->nik", R, ev, R) - np.eye(3))
+    f.tau[:] = np.stack([T[:, 0, 0], T[:, 0, 1], T[:, 0, 2], T[:, 1, 1], T[:, 1, 2], T[:, 2, 2]], axis=1)
+    for p in m.patches:
+        sl = slice(p.start, p.start + p.size)
+        if case.bcs[p.name]["theta"][0] == "zeroGradient":
+            f.thetab[sl] = f.theta[m.bCell[sl]]
+    return f
+
+
+def run_precision_check(args, case):
+    """The mixed form against converged FP64 fields on the headline case
+    itself.  From theta = 0 the contraction is ill-conditioned at round-off
+    level (degenerate conformation eigenvalues: a 1e-16 inlet perturbation
+    moves the FP64 theta by ~1e-2 within a few steps), so the comparison
+    starts from the seeded lognormal conformation, where every cell's
+    eigenvalues are apart.  Three runs of `steps` steps from that state: FP64
+    with every Krylov tolerance x1e-2 ('tight'), FP64 with x1e-4 ('tighter';
+    tight vs tighter is the floor: how converged the tight FP64 fields are)
+    and the mixed form with every tolerance x1e-2 and no further tightening."""
+    import copy
+    import numpy as np
+    from rheotool_gb300 import abi
+    from rheotool_gb300.runtime import Context
+    steps = args.check_steps
+    f0 = lognormal_contraction_state(case)
+    names = ("U", "p", "phi", "theta", "tau")
+    runs = {}
+    for key, prec, fac in (("fp64_tight", abi.RT_PREC_FP64, 1e-2), ("fp64_tighter", abi.RT_PREC_FP64, 1e-4),
+                           ("mixed_tight", abi.RT_PREC_MIXED, 1e-2)):
+        c = copy.copy(case)
+        c.precision = prec
+        c.solverU, c.solverP, c.solverTheta = [copy.copy(x) for x in (case.solverU, case.solverP, case.solverTheta)]
+        for sctl in (c.solverU, c.solverP, c.solverTheta):
+            sctl.tolerance *= fac
+            sctl.maxIter = max(5 * sctl.maxIter, 5000)
+        ctx = Context(0)
+        ctx.set_option(abi.RT_OPT_MIXED_TIGHTEN, 0)
+        ctx.setup_case(c, f0.copy())
+        perf = ctx.step(steps)
+        runs[key] = (ctx.fields(), {"p": perf.p.nIterations, "U": [perf.U[k].nIterations for k in range(3)],
+                                    "p_converged": bool(perf.p.converged)})
+        ctx.close()
+    err = lambda a, b: {n: float(np.linalg.norm(getattr(a, n) - getattr(b, n))
+                                 / max(np.linalg.norm(getattr(b, n)), 1e-300)) for n in names}
+    return {"what": f"relative L2 after {steps} steps of the headline case from the seeded lognormal conformation "
+                    "(sigma 0.1, seed 20261203)",
+            "floor_fp64_tight_vs_tighter": err(runs["fp64_tight"][0], runs["fp64_tighter"][0]),
+            "mixed_tight_vs_fp64_tighter": err(runs["mixed_tight"][0], runs["fp64_tighter"][0]),
+            "mixed_tight_vs_fp64_tight": err(runs["mixed_tight"][0], runs["fp64_tight"][0]),
+            "iterations_last_step": {k: v[1] for k, v in runs.items()}}
+
+
 def run_reference(args, rank):
     """The reference algorithm on the host: the FP64 oracle on the same mesh
     (1,000,000 cells unless --small) and the same steps as the GPU arm's
@@ -439,6 +515,8 @@ def main():
 
     def timed(ctx, precision, clocks):
         case.precision = precision
+        if precision == abi.RT_PREC_MIXED and args.mixed_precond is not None:
+            ctx.set_option(abi.RT_OPT_MIXED_PRECOND, args.mixed_precond)
         ctx.setup_case(case)
         if args.warmup:
             ctx.step(args.warmup)
@@ -593,6 +671,7 @@ def main():
     batched = None if (args.no_batch or args.small) else run_batched(args)
     served = None if (args.no_serve or args.small) else run_served(args)
     sweep = None if (args.no_sweep or args.small or rank != 0) else run_precision_sweep(args)
+    check = None if (args.no_check or rank != 0) else run_precision_check(args, case)
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -639,6 +718,8 @@ def main():
             line["served"] = served
         if sweep is not None:
             line["precision_sweep"] = sweep
+        if check is not None:
+            line["precision_check_headline"] = check
         print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()

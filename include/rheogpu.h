@@ -286,14 +286,14 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * more planes than one cluster holds; see RT_OPT_SWEEP_PLANES).  0 (default)
  * clears it. */
 #define RT_OPT_STALL_TEST 9
-/* RT_OPT_MIXED_PRECOND: how the mixed form's pressure solve applies its DIC
- * preconditioner.  0: the exact triangular sweeps (FP32 systolic sweeps on
- * structured meshes).  k = 1 .. 64: k Jacobi sweeps per triangular factor
- * (a truncated Neumann series of the same DIC factorisation, the same rD;
- * Anzt, Chow and Dongarra 2015), each a bandwidth-bound pass over the mesh;
- * the operator stays symmetric positive definite, the solve takes more
- * iterations, each far cheaper.  Default 0; the FP64 plain form always uses
- * the exact sweeps. */
+/* RT_OPT_MIXED_PRECOND: the preconditioner of the mixed form's pressure
+ * solve (DIC selected).  0: DIC with the exact triangular sweeps (FP32
+ * systolic sweeps on structured meshes).  -1: DIC of the two-colour
+ * (red-black) ordering of a structured mesh, applied in two parallel,
+ * bandwidth-bound passes (more iterations, each far cheaper).  k = 1 .. 64:
+ * DIC applied by k Jacobi sweeps per triangular factor (a truncated Neumann
+ * series of the same factorisation; Anzt, Chow and Dongarra 2015).  The FP64
+ * plain form always uses the exact sweeps. */
 #define RT_OPT_MIXED_PRECOND 10
 /* RT_OPT_BATCH_PERSISTENT: the batched form's pressure solve on structured
  * 2-D cases (up to 256 rows) as one persistent CTA per case, each running

@@ -201,6 +201,8 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
 
         DevMesh &m = ctx->mesh;
         m.sm.on = false;
+        m.colour.release();
+        m.nRed = 0;
         m.N = N; m.F = F; m.NB = NB; m.nPatches = md->nPatches;
         for (int k = 0; k < 3; ++k) m.solveDir[k] = md->solveDir[k];
         cudaStream_t s = ctx->stream;
@@ -413,6 +415,17 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         s.sync.zero(ctx->stream);
         s.data.alloc((size_t)(12 + 6 + 6) * s.nSkew);
         s.data.zero(ctx->stream);
+        // the two colours of the box (red: i + j + k even)
+        {
+            std::vector<unsigned char> col(N);
+            int red = 0;
+            for (int c = 0; c < N; ++c) {
+                col[c] = (unsigned char)((cellIJK[3 * c] + cellIJK[3 * c + 1] + cellIJK[3 * c + 2]) & 1);
+                red += col[c] == 0;
+            }
+            upload_vec(ctx, col, m.colour);
+            m.nRed = red;
+        }
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
         s.tune[0] = s.tune[1] = -1;
         s.on = true;
@@ -459,8 +472,9 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
             ctx->mixedTighten = std::pow(10.0, -(double)value);
             return RT_OK;
         case RT_OPT_MIXED_PRECOND:
-            RT_REQUIRE(value >= 0 && value <= 64, RT_EINVAL,
-                       "RT_OPT_MIXED_PRECOND: 0 exact sweeps, 1 .. 64 Jacobi sweeps per triangular factor");
+            RT_REQUIRE(value >= -1 && value <= 64, RT_EINVAL,
+                       "RT_OPT_MIXED_PRECOND: 0 exact sweeps, -1 red-black DIC, 1 .. 64 Jacobi sweeps per "
+                       "triangular factor");
             ctx->mixedJacobi = (int)value;
             return RT_OK;
         case RT_OPT_BATCH_PERSISTENT:
@@ -1111,6 +1125,13 @@ rt_status rt_batch_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs, const rt_model
     rt_case_ctl c1 = *ctl;
     c1.needReference = 0;
     c1.pRefCell = 0;
+    if (ctx->mesh.batch.n == 1) {
+        // a batch of one case runs the single-case path: its own pressure
+        // reference goes through the case control
+        c1.needReference = pRefCell[0] >= 0 ? 1 : 0;
+        c1.pRefCell = pRefCell[0] >= 0 ? pRefCell[0] : 0;
+        c1.pRefValue = pRefValue[0];
+    }
     st = rt_case_setup(ctx, bcs, &models[0], &c1);
     if (st != RT_OK) return st;
     return guarded(ctx, [&]() -> rt_status {

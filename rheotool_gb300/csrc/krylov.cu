@@ -1434,6 +1434,70 @@ __global__ void k_jac_sweep(int N, int nS, const int *__restrict__ nbr, const fl
     else yout[c] = acc;
 }
 
+// --------------------------------------------------------------------------
+// DIC of the two-colour (red-black) ordering of a structured mesh
+// (RT_OPT_MIXED_PRECOND = -1).  Every neighbour of a red cell is black and
+// comes after it, every neighbour of a black cell is red and comes before:
+// rD is a_cc on red cells and a_cc - sum a_cn a_nc / a_nn on black ones, and
+// an application is two parallel passes, FP32 arithmetic with an FP64 right-
+// hand side and result: black cells w = (r - sum a w_red) / rD with w_red =
+// r / rD formed on the fly, then red cells w = (r - sum a w_black) / rD.
+// --------------------------------------------------------------------------
+__global__ void k_rb_rd(Ell e, const unsigned char *__restrict__ colour, const double *__restrict__ diag,
+                        const double *__restrict__ upper, const double *__restrict__ lower,
+                        float *__restrict__ rDinv) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= e.N) return;
+    double rd = diag[c];
+    if (colour[c]) {
+        for (int s = 0; s < e.nSlots; ++s) {
+            const int nb = e.nbr[s * e.N + c];
+            if (nb < 0) break;
+            const int f = e.face[s * e.N + c];
+            rd -= upper[f] * lower[f] / diag[nb];
+        }
+    }
+    rDinv[c] = (float)(1.0 / rd);
+}
+
+// pass 1: the black cells (FP32 copy kept for pass 2, FP64 result)
+__global__ void k_rb_black(Ell e, const unsigned char *__restrict__ colour, const float *__restrict__ rDinv,
+                           const float *__restrict__ upper, const float *__restrict__ lower,
+                           const double *__restrict__ r, float *__restrict__ wb, double *__restrict__ w,
+                           const unsigned *__restrict__ dmask) {
+    if (dmask && !*dmask) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= e.N || !colour[c]) return;
+    float acc = (float)r[c];
+    for (int s = 0; s < e.nSlots; ++s) {
+        const int nb = e.nbr[s * e.N + c];
+        if (nb < 0) break;
+        const int f = e.face[s * e.N + c];
+        acc = fmaf(-(nb > c ? upper[f] : lower[f]), rDinv[nb] * (float)r[nb], acc);
+    }
+    const float v = rDinv[c] * acc;
+    wb[c] = v;
+    w[c] = (double)v;
+}
+
+// pass 2: the red cells
+__global__ void k_rb_red(Ell e, const unsigned char *__restrict__ colour, const float *__restrict__ rDinv,
+                         const float *__restrict__ upper, const float *__restrict__ lower,
+                         const double *__restrict__ r, const float *__restrict__ wb, double *__restrict__ w,
+                         const unsigned *__restrict__ dmask) {
+    if (dmask && !*dmask) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= e.N || colour[c]) return;
+    float acc = (float)r[c];
+    for (int s = 0; s < e.nSlots; ++s) {
+        const int nb = e.nbr[s * e.N + c];
+        if (nb < 0) break;
+        const int f = e.face[s * e.N + c];
+        acc = fmaf(-(nb > c ? upper[f] : lower[f]), wb[nb], acc);
+    }
+    w[c] = (double)(rDinv[c] * acc);
+}
+
 // FP32 state of one mixed solve
 struct Mixed : Solver {
     float *d32, *u32, *l32, *rD32;   // matrix copy, preconditioner diagonal
@@ -1464,7 +1528,13 @@ struct Mixed : Solver {
             launch_count(ctx);
         }
         const int pre = a.ctl.preconditioner;
-        if (jacobi()) {
+        if (redblack()) {
+            if (ctx->jac.n < 2 * (size_t)N) ctx->jac.alloc(2 * (size_t)N);
+            ProfScope ps(ctx, "dilu_rD", (double)N * (8.0 + 8.0 + 4.0) + (double)ctx->mesh.F * 16.0);
+            k_rb_rd<<<nblocks(N), RT_BLOCK, 0, st>>>(pe, ctx->mesh.colour.p, a.diag, a.upper, a.lower, ctx->jac.p);
+            RT_CHECK_LAUNCH();
+            launch_count(ctx);
+        } else if (jacobi()) {
             // the exact factorisation's 1/rD in cell order, then the FP32
             // premultiplied coefficients of the Jacobi sweeps
             const DevMesh &m = ctx->mesh;
@@ -1498,6 +1568,23 @@ struct Mixed : Solver {
 
     // FP64 r -> FP32 preconditioner -> FP64 w (the structured sweeps round on
     // the way in and out; otherwise through the FP32 vectors r32, w32)
+    // the red-black DIC of the pressure solve (one component, structured mesh)
+    bool redblack() const {
+        return ctx->mixedJacobi < 0 && a.nc == 1 && a.ctl.preconditioner == RT_PRECOND_DIC &&
+               ctx->mesh.colour.p != nullptr && !ctx->mesh.hasCoupled;
+    }
+    void redblack_apply(const double *r, double *w, const unsigned *dmask) {
+        const double fpc = (double)ctx->mesh.F / N;
+        // rDinv 4 + colour 1 + coefficients 2*(F/N)*4 + addressing 2*(F/N)*8 (both passes),
+        // r 8 read twice, the black copy 4 + 4, w 8
+        ProfScope ps(ctx, "dilu_redblack32", (double)N * (5.0 + fpc * 24.0 + 16.0 + 8.0 + 8.0));
+        float *rDi = ctx->jac.p, *wb = ctx->jac.p + N;
+        k_rb_black<<<nblocks(N), RT_BLOCK, 0, st>>>(pe, ctx->mesh.colour.p, rDi, u32, l32, r, wb, w, dmask);
+        k_rb_red<<<nblocks(N), RT_BLOCK, 0, st>>>(pe, ctx->mesh.colour.p, rDi, u32, l32, r, wb, w, dmask);
+        RT_CHECK_LAUNCH();
+        launch_count(ctx, 2);
+    }
+
     // the Jacobi-swept DIC/DILU of the pressure solve (one component)
     bool jacobi() const {
         const int pre = a.ctl.preconditioner;
@@ -1538,6 +1625,10 @@ struct Mixed : Solver {
 
     void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32,
                          const unsigned *dmask = nullptr) {
+        if (redblack()) {
+            redblack_apply(r, w, dmask);
+            return;
+        }
         if (jacobi()) {
             jacobi_apply(r, w, dmask);
             return;

@@ -243,6 +243,11 @@ struct DevMesh {
     // 0 .. pnUp - 1, face order, padding -1 (the Jacobi-iterated DIC/DILU)
     DBuf<int> plNbr, plFace, puNbr, puFace;
     int pnLo = 0, pnUp = 0;
+    // two-colour (red-black) ordering of a structured mesh: colour of each
+    // cell (i + j + k) % 2, and its cells listed red first (N, set by
+    // rt_mesh_set_ijk; empty otherwise)
+    DBuf<unsigned char> colour;
+    int nRed = 0;
     // cells (N)
     DBuf<double> C;          // 3N SoA
     DBuf<double> V;

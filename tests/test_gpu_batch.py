@@ -144,3 +144,21 @@ def test_batch_persistent_pressure_solve_equals_launch_sequence(precision):
     for i in range(len(cases)):
         for n in NAMES:
             assert np.array_equal(getattr(out[0][0][i], n), getattr(out[1][0][i], n)), (i, n)
+
+
+def test_batch_of_one_case_equals_the_case_alone(ctx):
+    """A batch layout holding a single case (what a serving batch shrinks to
+    when its other requests have left) runs the single-case path with the
+    case's own pressure reference: the same bits as the case alone."""
+    case = cavity_case(12, model="GiesekusLog", Wi=2.0, dt=5e-3, alpha=0.1)
+    bt = BatchContext([case])
+    try:
+        bt.step(6)
+        got = bt.fields()[0]
+    finally:
+        bt.ctx.close()
+    ctx.setup_case(case)
+    ctx.step(6)
+    alone = ctx.fields()
+    for n in NAMES:
+        assert np.array_equal(getattr(got, n), getattr(alone, n)), n

@@ -236,7 +236,7 @@ def test_pbicg_multi_rhs_matches_oracle(ctx, precond, mesh_fn):
                 assert orc.residual(diag, upper, lower, b[k], xg[k]) < max(10 * tol, 1e-12)
             if tol == 1e-10:
                 assert perf[k].nIterations == po.nIterations, (k, perf[k].nIterations, po.nIterations)
-            else:
+            elif np.any(b[k]):   # (a zero source's solution is round-off noise around 0 in both)
                 assert abs(perf[k].nIterations - po.nIterations) <= 1
                 assert rel(xg[k], xo) < 1e-9
 

@@ -21,12 +21,14 @@ class _Stand:
     order = []
     batches = []
     carried = []
+    steps = {}
     fail_cells = None
 
 
 class FakeContext:
     def __init__(self, device=0):
         self.case = None
+        self.batch_cases = None
         with _Stand.lock:
             _Stand.active += 1
             _Stand.peak = max(_Stand.peak, _Stand.active)
@@ -40,6 +42,9 @@ class FakeContext:
 
     def step(self, n):
         time.sleep(0.002 * n)
+        with _Stand.lock:
+            for c in (self.batch_cases or [self.case]):
+                _Stand.steps[id(c)] = _Stand.steps.get(id(c), 0) + n
 
     def sync(self):
         pass
@@ -55,6 +60,7 @@ class FakeContext:
 class FakeBatch:
     def __init__(self, cases, ctx=None):
         self.cases = cases
+        ctx.batch_cases = list(cases)
         with _Stand.lock:
             _Stand.batches.append(len(cases))
             _Stand.order.extend(c.name for c in cases)
@@ -74,6 +80,7 @@ def stand(monkeypatch):
     monkeypatch.setattr(serve, "device_bytes", lambda: 0)
     _Stand.active = _Stand.peak = 0
     _Stand.order, _Stand.batches, _Stand.carried, _Stand.fail_cells = [], [], [], None
+    _Stand.steps = {}
     return _Stand
 
 
@@ -150,6 +157,8 @@ def test_requests_join_and_leave_a_running_batch(stand):
     srv.close()
     assert all(r.error is None and r.fields is not None for r in reqs)
     assert any(r.joined for r in later)                 # joined a running batch
+    for r in reqs:                                      # every request took exactly its steps
+        assert stand.steps[id(r.case)] == r.steps, (r.rid, stand.steps[id(r.case)], r.steps)
     assert srv.relayouts >= 1 and stand.carried          # running cases carried into the new layout
     assert first[1].finished < first[0].finished        # the short request left first
     assert len(stand.batches) >= 2
