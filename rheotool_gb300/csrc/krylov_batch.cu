@@ -623,53 +623,45 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
 
 // ---- the persistent per-case PCG -------------------------------------------
 // One CTA per case runs the case's whole pressure solve (one component,
-// structured 2-D cases with at most 8 j-blocks): the same operations, in the
-// same order and with the same per-case reduction tree, as one iteration of
-// BSolver::pcg_iteration replayed until the case stops, with __syncthreads
-// between the phases instead of kernel boundaries.  The block partials of a
-// reduction are the launch path's (one per 256-cell block of the case, summed
-// by bsum), and their sum is k_b_fin's (32 lanes over the case's blocks,
-// then a shuffle tree), so a case's iterates have the launch path's bits.
+// structured 2-D cases with at most 8 j-blocks): the operations of
+// BSolver::pcg_iteration, replayed until the case stops, with __syncthreads
+// between the phases instead of kernel boundaries, and every reduction of the
+// case as one pass of the CTA (each thread sums its cells, then one block
+// tree; the launch path sums 256-cell blocks first, so the two differ in the
+// last bits).  Every scalar decision is the launch path's.
+constexpr int kCaseThreads = 512;
 
-// sum of one slot's partials of case cb in k_b_fin's order; every thread gets it
-__device__ double case_sum(const double *partial, int nBlk, int slot, int b0, int b1) {
+// the CTA's sum, valid in every thread
+__device__ double case_total(double v) {
     __shared__ double sv;
+    const double t = bsum(v);
+    if (threadIdx.x == 0) sv = t;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        double v = 0.0;
-        for (int i = b0 + (int)threadIdx.x; i < b1; i += 32) v += partial[(slot * 6 + 0) * nBlk + i];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) sv = v;
-    }
+    const double r = sv;
     __syncthreads();
-    return sv;
+    return r;
 }
 
 template <class V>
-__global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<V> g, BSeg S, Ctl ctl, int mixed,
-                                                          const V *__restrict__ d32, const V *__restrict__ u32,
-                                                          const V *__restrict__ l32, const double *__restrict__ diag,
-                                                          const double *__restrict__ upper,
-                                                          const double *__restrict__ lower,
-                                                          const double *__restrict__ b, double *__restrict__ psi,
-                                                          V *r, V *w, V *p, V *q, V *x, double *partial, int *err,
-                                                          long long maxSpin, int cap) {
+__global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Skew2D<V> g, BSeg S, Ctl ctl, int mixed,
+                                                              const V *__restrict__ d32, const V *__restrict__ u32,
+                                                              const V *__restrict__ l32,
+                                                              const double *__restrict__ diag,
+                                                              const double *__restrict__ upper,
+                                                              const double *__restrict__ lower,
+                                                              const double *__restrict__ b, double *__restrict__ psi,
+                                                              V *r, V *w, V *p, V *q, V *x, int *err, long long maxSpin,
+                                                              int cap) {
     __shared__ __align__(16) V ring[8 * s2d::kRJ];
     __shared__ int sProg[32];
-    const int cb = blockIdx.x, sg = cb * 8, tid = threadIdx.x, N = t.N;
-    const int b0 = t.caseBlk[cb], b1 = t.caseBlk[cb + 1];
-    const int c0 = t.blkCell0[b0], c1 = t.blkCell1[b1 - 1];
+    const int cb = blockIdx.x, sg = cb * 8, tid = threadIdx.x, nt = blockDim.x, N = t.N;
+    const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
-    // block partial of the launch path's 256-cell block blk: bsum over its cells
-    auto block_partial = [&](int slot, int blk, double v) {
-        const double sm = bsum(v);
-        if (tid == 0) partial[(slot * 6 + 0) * t.nBlk + blk] = sm;
-    };
     for (int it = 0; it < cap; ++it) {
         __syncthreads();
         if (!S.active[sg]) break;
         // ---- w = M^-1 r: gather, forward and backward sweeps of this case
-        for (long long i = e0 + tid; i < e1; i += blockDim.x) {
+        for (long long i = e0 + tid; i < e1; i += nt) {
             const int c = g.cellOf[i];
             g.rS[i] = c >= 0 ? r[c] : V(0);
         }
@@ -682,14 +674,13 @@ __global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<
         }
         if (*(volatile int *)err) break;
         // ---- rho = w.r (and w.q_old in the flexible form)
-        for (int blk = b0; blk < b1; ++blk) {
-            const int c = t.blkCell0[blk] + tid;
-            const bool in = c < t.blkCell1[blk];
-            block_partial(0, blk, in ? (double)w[c] * (double)r[c] : 0.0);
-            if (mixed) block_partial(1, blk, in ? (double)w[c] * (double)q[c] : 0.0);
+        double v0 = 0.0, v1 = 0.0;
+        for (int c = c0 + tid; c < c1; c += nt) {
+            v0 += (double)w[c] * (double)r[c];
+            if (mixed) v1 += (double)w[c] * (double)q[c];
         }
-        const double rho = case_sum(partial, t.nBlk, 0, b0, b1);
-        const double wq = mixed ? case_sum(partial, t.nBlk, 1, b0, b1) : 0.0;
+        const double rho = case_total(v0);
+        const double wq = mixed ? case_total(v1) : 0.0;
         if (tid == 0) {   // k_b_pcg_a
             const double aold = S.A[sg];
             S.Aold[sg] = aold;
@@ -701,11 +692,12 @@ __global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<
         {
             const bool first = S.iter[sg] == 0;
             const V beta = V(S.beta[sg]);
-            for (int c = c0 + tid; c < c1; c += blockDim.x) p[c] = first ? w[c] : fma(beta, p[c], w[c]);
+            for (int c = c0 + tid; c < c1; c += nt) p[c] = first ? w[c] : fma(beta, p[c], w[c]);
         }
         __syncthreads();
-        // ---- q = A p (the vector type's matrix copy; FP32: differences form)
-        for (int c = c0 + tid; c < c1; c += blockDim.x) {
+        // ---- q = A p (the vector type's matrix copy; FP32: differences form); p.q
+        double vq = 0.0;
+        for (int c = c0 + tid; c < c1; c += nt) {
             const V pc = p[c];
             V acc = V(d32[c]) * pc;
             for (int s = 0; s < e.nSlots; ++s) {
@@ -715,14 +707,9 @@ __global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<
                 acc = fma(V(nb > c ? u32[f] : l32[f]), sizeof(V) == 4 ? p[nb] - pc : p[nb], acc);
             }
             q[c] = acc;
+            vq += (double)acc * (double)pc;
         }
-        __syncthreads();
-        // ---- alpha = rho / q.p, or the singularity stop
-        for (int blk = b0; blk < b1; ++blk) {
-            const int c = t.blkCell0[blk] + tid;
-            block_partial(0, blk, c < t.blkCell1[blk] ? (double)q[c] * (double)p[c] : 0.0);
-        }
-        const double wApA = case_sum(partial, t.nBlk, 0, b0, b1);
+        const double wApA = case_total(vq);
         if (tid == 0) {   // k_b_pcg_alpha
             if (fabs(wApA) / S.nf[sg] < 1e-300) {
                 S.sing[sg] = 1;
@@ -733,25 +720,21 @@ __global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<
         }
         __syncthreads();
         // ---- x += alpha p; r -= alpha q; |r|
+        double vr = 0.0;
         {
             const bool sing = S.sing[sg] != 0;
             const V alpha = V(S.alpha[sg]);
-            for (int blk = b0; blk < b1; ++blk) {
-                const int c = t.blkCell0[blk] + tid;
-                double v = 0.0;
-                if (c < t.blkCell1[blk]) {
-                    V rr = r[c];
-                    if (!sing) {
-                        x[c] = fma(alpha, p[c], x[c]);
-                        rr = fma(-alpha, q[c], rr);
-                        r[c] = rr;
-                    }
-                    v = fabs((double)rr);
+            for (int c = c0 + tid; c < c1; c += nt) {
+                V rr = r[c];
+                if (!sing) {
+                    x[c] = fma(alpha, p[c], x[c]);
+                    rr = fma(-alpha, q[c], rr);
+                    r[c] = rr;
                 }
-                block_partial(0, blk, v);
+                vr += fabs((double)rr);
             }
         }
-        const double rs = case_sum(partial, t.nBlk, 0, b0, b1);
+        const double rs = case_total(vr);
         if (tid == 0) {   // k_b_iter_fin
             if (S.sing[sg]) {
                 S.active[sg] = 0;
@@ -773,22 +756,18 @@ __global__ void __launch_bounds__(RT_BLOCK) k_b_pcg_case(BTab t, BEll e, Skew2D<
         __syncthreads();
         // ---- residual replacement (mixed): psi += x, x = 0, r = b - A psi
         if (S.repl[sg]) {
-            for (int c = c0 + tid; c < c1; c += blockDim.x) {
+            for (int c = c0 + tid; c < c1; c += nt) {
                 psi[c] += (double)x[c];
                 x[c] = V(0);
             }
             __syncthreads();
-            for (int blk = b0; blk < b1; ++blk) {
-                const int c = t.blkCell0[blk] + tid;
-                double v = 0.0;
-                if (c < t.blkCell1[blk]) {
-                    const double rr = b[c] - brow_mul(e, c, diag, upper, lower, psi);
-                    r[c] = (V)rr;
-                    v = fabs(rr);
-                }
-                block_partial(0, blk, v);
+            double vt = 0.0;
+            for (int c = c0 + tid; c < c1; c += nt) {
+                const double rr = b[c] - brow_mul(e, c, diag, upper, lower, psi);
+                r[c] = (V)rr;
+                vt += fabs(rr);
             }
-            const double rt = case_sum(partial, t.nBlk, 0, b0, b1);
+            const double rt = case_total(vt);
             if (tid == 0 && S.active[sg]) {   // k_b_after
                 const double fin = rt / S.nf[sg];
                 S.fin[sg] = fin;
@@ -1034,10 +1013,10 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         else g = sweep2d_view64(ctx);
         {
             ProfScope ps(ctx, "batch_pcg_persistent");
-            k_b_pcg_case<V><<<bt.n, RT_BLOCK, 0, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
-                                                          sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
-                                                          sv.v(1), sv.v(2), sv.v(3), x, sv.partial, bt.sErr.p,
-                                                          1ll << 22, cap);
+            k_b_pcg_case<V><<<bt.n, kCaseThreads, 0, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
+                                                              sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
+                                                              sv.v(1), sv.v(2), sv.v(3), x, bt.sErr.p, 1ll << 22,
+                                                              cap);
             RT_CHECK_LAUNCH();
         }
         launch_count(ctx);

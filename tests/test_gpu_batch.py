@@ -127,8 +127,11 @@ def test_batch_layout_rejects_a_face_across_cases(ctx):
 @pytest.mark.parametrize("precision", [abi.RT_PREC_FP64, abi.RT_PREC_MIXED])
 def test_batch_persistent_pressure_solve_equals_launch_sequence(precision):
     """The batched pressure solve as one persistent CTA per case (all its
-    iterations in one launch) repeats the per-iteration launch sequence's
-    arithmetic: the same fields, bit for bit, and the same iteration counts."""
+    iterations in one launch) takes the per-iteration launch sequence's
+    scalar decisions with one-pass reductions per case (the launch path sums
+    256-cell blocks first): iteration counts within one, fields equal within
+    the parity bars (1e-9 FP64, 1e-6 mixed, or the case's round-off
+    sensitivity bar where it is larger)."""
     cases = cavity_sweep(n_cases=10, n_min=16, n_max=96, seed=9, dt=2e-3, precision=precision)
     out = {}
     for persistent in (0, 1):
@@ -139,11 +142,18 @@ def test_batch_persistent_pressure_solve_equals_launch_sequence(precision):
             out[persistent] = (bt.fields(), [p.p.nIterations for p in bt.case_perf()])
         finally:
             bt.ctx.close()
-    assert out[0][1] == out[1][1]
+    assert all(abs(a - b) <= 1 for a, b in zip(out[0][1], out[1][1])), (out[0][1], out[1][1])
     assert max(out[1][1]) > 20
-    for i in range(len(cases)):
+    plain = TOL_STEP if precision == abi.RT_PREC_FP64 else 1e-6
+    for i, c in enumerate(cases):
+        errs = {n: rel(getattr(out[1][0][i], n), getattr(out[0][0][i], n)) for n in NAMES}
+        if all(e < plain for e in errs.values()):
+            continue
+        # round-off amplified by the case itself (conformation eigenvalues
+        # degenerate at rest): the oracle's own sensitivity bar
+        bar = step_bar(c, 3, oracle_run(c, 3), NAMES)
         for n in NAMES:
-            assert np.array_equal(getattr(out[0][0][i], n), getattr(out[1][0][i], n)), (i, n)
+            assert errs[n] < max(plain, bar[n]), (i, n, errs[n], bar[n])
 
 
 def test_batch_of_one_case_equals_the_case_alone(ctx):
