@@ -408,10 +408,51 @@ __global__ void k_patch_zerograd(int N, int NB, int st, int sz, int nc, const in
     for (int q = 0; q < nc; ++q) xb[(size_t)q * NB + b] = x[(size_t)q * N + c];
 }
 
+// one wave of a batch: the faces' new values from the current boundary values
+// (every face of a wave belongs to another patch than the wave's other faces
+// of its case), then stored
+__global__ void k_tau_wave(MeshView m, const int *__restrict__ faces, int nf, const int *__restrict__ bk,
+                           const double *__restrict__ tau, const double *__restrict__ taub, double *__restrict__ val) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    int b = faces[i];
+    int c = m.bCell[b];
+    if (bk[b] == RT_BC_ZEROGRAD) {
+        for (int q = 0; q < 6; ++q) val[(size_t)q * nf + i] = tau[(size_t)q * m.N + c];
+        return;
+    }
+    double ct0 = m.bCtoF[b], ct1 = m.bCtoF[m.NB + b], ct2 = m.bCtoF[2 * m.NB + b];
+    for (int q = 0; q < 6; ++q) {
+        double g[3];
+        cell_grad(m, c, tau + (size_t)q * m.N, taub + (size_t)q * m.NB, g);
+        val[(size_t)q * nf + i] = tau[(size_t)q * m.N + c] + (g[0] * ct0 + g[1] * ct1 + g[2] * ct2);
+    }
+}
+
+__global__ void k_tau_wave_store(int NB, const int *__restrict__ faces, int nf, const double *__restrict__ val,
+                                 double *__restrict__ xb) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    for (int q = 0; q < 6; ++q) xb[(size_t)q * NB + faces[i]] = val[(size_t)q * nf + i];
+}
+
 void tau_correct_bc(rt_ctx *ctx, double *valTmp) {
     DevMesh &mesh = ctx->mesh;
     DevCase &cs = ctx->cs;
     MeshView m = view(mesh);
+    if (!cs.tauWaveH.empty()) {   // a batch: the cases' patches wave by wave
+        for (size_t wv = 0; wv + 1 < cs.tauWaveH.size(); ++wv) {
+            const int f0 = cs.tauWaveH[wv], nf = cs.tauWaveH[wv + 1] - f0;
+            if (nf == 0) continue;
+            const int *faces = cs.tauWaveFace.p + f0;
+            k_tau_wave<<<nblocks(nf), RT_BLOCK, 0, ctx->stream>>>(m, faces, nf, cs.bkTau.p, cs.tau.p, cs.taub.p,
+                                                                 valTmp);
+            k_tau_wave_store<<<nblocks(nf), RT_BLOCK, 0, ctx->stream>>>(m.NB, faces, nf, valTmp, cs.taub.p);
+            launch_count(ctx, 2);
+            RT_CHECK_LAUNCH();
+        }
+        return;
+    }
     for (int p = 0; p < mesh.nPatches; ++p) {
         int st = mesh.patchStartH[p], sz = mesh.patchSizeH[p];
         if (sz == 0) continue;

@@ -576,6 +576,30 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
         per_face(c.kindP, c.bkP);
         per_face(c.kindTheta, c.bkTh);
         per_face(c.kindTau, c.bkTau);
+        c.tauWaveH.clear();
+        c.tauWaveFace.release();
+        if (m.batch.n > 1) {
+            // patch order within each case: the k-th updating patch of a case
+            // sees the values its earlier patches wrote (corner cells)
+            const std::vector<int> &bs = m.batch.bStartH;
+            std::vector<std::vector<int>> waves;
+            std::vector<int> rank(m.batch.n, 0);
+            for (int p = 0; p < P; ++p) {
+                if (m.patchSizeH[p] == 0 || (c.kindTau[p] != RT_BC_ZEROGRAD && c.kindTau[p] != RT_BC_LINEXTRAP))
+                    continue;
+                const int k = (int)(std::upper_bound(bs.begin(), bs.end(), m.patchStartH[p]) - bs.begin()) - 1;
+                const int wv = rank[k]++;
+                if ((int)waves.size() <= wv) waves.resize(wv + 1);
+                for (int i = 0; i < m.patchSizeH[p]; ++i) waves[wv].push_back(m.patchStartH[p] + i);
+            }
+            std::vector<int> faces;
+            c.tauWaveH.push_back(0);
+            for (auto &w : waves) {
+                faces.insert(faces.end(), w.begin(), w.end());
+                c.tauWaveH.push_back((int)faces.size());
+            }
+            if (!faces.empty()) upload_vec(ctx, faces, c.tauWaveFace);
+        }
         upload_soa(ctx, bc->Ub, NB, 3, c.UbFixed);
         upload_soa(ctx, bc->pb, NB, 1, c.pbFixed);
         upload_soa(ctx, bc->thetab, NB, 6, c.thetabFixed);
@@ -1003,6 +1027,14 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
         upload_vec(ctx, bc0, b.blkCell0);
         upload_vec(ctx, bc1, b.blkCell1);
         upload_vec(ctx, cblk, b.caseBlk);
+        {   // the order one-CTA-per-case launches take the cases in: largest first
+            std::vector<int> order(n);
+            std::iota(order.begin(), order.end(), 0);
+            std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+                return cellStart[a + 1] - cellStart[a] > cellStart[c + 1] - cellStart[c];
+            });
+            upload_vec(ctx, order, b.caseOrder);
+        }
         // structured 2-D cases: the skewed layout of the batched sweeps
         b.sweep2d = false;
         bool structured = dims && cellIJK;

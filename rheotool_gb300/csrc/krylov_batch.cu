@@ -630,6 +630,11 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
 // tree; the launch path sums 256-cell blocks first, so the two differ in the
 // last bits).  Every scalar decision is the launch path's.
 constexpr int kCaseThreads = 512;
+template <class V>
+constexpr int kCaseP = sizeof(V) == 4 ? 8 : 4;   // sweep chunk (registers for the prefetched chunk)
+constexpr int kU = 4;                            // cells per thread whose loads are issued together
+constexpr int kUA = 2;                           // the same for q = A p
+constexpr int kSlots = 4;                        // ELL width of the 2-D cases
 
 // the CTA's sum, valid in every thread
 __device__ double case_total(double v) {
@@ -650,37 +655,52 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
                                                               const double *__restrict__ upper,
                                                               const double *__restrict__ lower,
                                                               const double *__restrict__ b, double *__restrict__ psi,
-                                                              V *r, V *w, V *p, V *q, V *x, int *err, long long maxSpin,
-                                                              int cap) {
+                                                              V *__restrict__ r, V *__restrict__ w,
+                                                              V *__restrict__ p, V *__restrict__ q,
+                                                              V *__restrict__ x, const int *__restrict__ order,
+                                                              int *err, long long maxSpin, int cap) {
+    using Acc = typename AccOf<V>::type;
     __shared__ __align__(16) V ring[8 * s2d::kRJ];
     __shared__ int sProg[32];
-    const int cb = blockIdx.x, sg = cb * 8, tid = threadIdx.x, nt = blockDim.x, N = t.N;
+    const int cb = order[blockIdx.x], sg = cb * 8, tid = threadIdx.x, nt = blockDim.x, N = t.N;
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
     for (int it = 0; it < cap; ++it) {
         __syncthreads();
         if (!S.active[sg]) break;
         // ---- w = M^-1 r: gather, forward and backward sweeps of this case
-        for (long long i = e0 + tid; i < e1; i += nt) {
-            const int c = g.cellOf[i];
-            g.rS[i] = c >= 0 ? r[c] : V(0);
+        for (long long i0 = e0 + tid; i0 < e1; i0 += (long long)kU * nt) {
+            int cc[kU];
+            V v[kU];
+#pragma unroll
+            for (int k = 0; k < kU; ++k) {
+                const long long i = i0 + (long long)k * nt;
+                cc[k] = i < e1 ? __ldg(g.cellOf + i) : -1;
+            }
+#pragma unroll
+            for (int k = 0; k < kU; ++k) v[k] = cc[k] >= 0 ? r[cc[k]] : V(0);
+#pragma unroll
+            for (int k = 0; k < kU; ++k)
+                if (i0 + (long long)k * nt < e1) g.rS[i0 + (long long)k * nt] = v[k];
         }
         for (int mode = 0; mode < 2; ++mode) {
             if (tid < 32) sProg[tid] = 0;
             __syncthreads();
-            if (mode == 0) sweep2d_cta<V, 0, 1, 8>(g, cb, 1u, nullptr, N, err, maxSpin, ring, sProg);
-            else sweep2d_cta<V, 1, 1, 8>(g, cb, 1u, w, N, err, maxSpin, ring, sProg);
+            if (mode == 0) sweep2d_cta<V, 0, 1, kCaseP<V>>(g, cb, 1u, nullptr, N, err, maxSpin, ring, sProg);
+            else sweep2d_cta<V, 1, 1, kCaseP<V>>(g, cb, 1u, w, N, err, maxSpin, ring, sProg);
             __syncthreads();
         }
         if (*(volatile int *)err) break;
         // ---- rho = w.r (and w.q_old in the flexible form)
-        double v0 = 0.0, v1 = 0.0;
+        Acc a0, a1;
+#pragma unroll 4
         for (int c = c0 + tid; c < c1; c += nt) {
-            v0 += (double)w[c] * (double)r[c];
-            if (mixed) v1 += (double)w[c] * (double)q[c];
+            const V wc = w[c];
+            acc_dot(a0, wc, r[c]);
+            if (mixed) acc_dot(a1, wc, q[c]);
         }
-        const double rho = case_total(v0);
-        const double wq = mixed ? case_total(v1) : 0.0;
+        const double rho = case_total(acc_value(a0));
+        const double wq = mixed ? case_total(acc_value(a1)) : 0.0;
         if (tid == 0) {   // k_b_pcg_a
             const double aold = S.A[sg];
             S.Aold[sg] = aold;
@@ -692,24 +712,68 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
         {
             const bool first = S.iter[sg] == 0;
             const V beta = V(S.beta[sg]);
-            for (int c = c0 + tid; c < c1; c += nt) p[c] = first ? w[c] : fma(beta, p[c], w[c]);
+            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
+                V wv[kU], pv[kU];
+#pragma unroll
+                for (int k = 0; k < kU; ++k) {
+                    const int c = ci + k * nt;
+                    wv[k] = c < c1 ? w[c] : V(0);
+                    pv[k] = (c < c1 && !first) ? p[c] : V(0);
+                }
+#pragma unroll
+                for (int k = 0; k < kU; ++k)
+                    if (ci + k * nt < c1) p[ci + k * nt] = first ? wv[k] : fma(beta, pv[k], wv[k]);
+            }
         }
         __syncthreads();
         // ---- q = A p (the vector type's matrix copy; FP32: differences form); p.q
-        double vq = 0.0;
-        for (int c = c0 + tid; c < c1; c += nt) {
-            const V pc = p[c];
-            V acc = V(d32[c]) * pc;
-            for (int s = 0; s < e.nSlots; ++s) {
-                const int nb = e.nbr[s * N + c];
-                if (nb < 0) break;
-                const int f = e.face[s * N + c];
-                acc = fma(V(nb > c ? u32[f] : l32[f]), sizeof(V) == 4 ? p[nb] - pc : p[nb], acc);
+        // two rounds of independent loads per kUA cells: the ELL slots (the
+        // rows end in -1 padding, which adds nothing) with the cells' own
+        // values, then the neighbours' values and the face coefficients
+        Acc aq;
+        for (int ci = c0 + tid; ci < c1; ci += kUA * nt) {
+            int nb[kUA][kSlots], fc[kUA][kSlots];
+            V pc[kUA], dc[kUA];
+#pragma unroll
+            for (int k = 0; k < kUA; ++k) {
+                const int c = ci + k * nt;
+                const bool in = c < c1;
+#pragma unroll
+                for (int s = 0; s < kSlots; ++s) {
+                    const bool sl = in && s < e.nSlots;
+                    nb[k][s] = sl ? __ldg(e.nbr + (size_t)s * N + c) : -1;
+                    fc[k][s] = sl ? __ldg(e.face + (size_t)s * N + c) : -1;
+                }
+                pc[k] = in ? p[c] : V(0);
+                dc[k] = in ? V(d32[c]) : V(0);
             }
-            q[c] = acc;
-            vq += (double)acc * (double)pc;
+            V cf[kUA][kSlots], pn[kUA][kSlots];
+#pragma unroll
+            for (int k = 0; k < kUA; ++k) {
+                const int c = ci + k * nt;
+#pragma unroll
+                for (int s = 0; s < kSlots; ++s) {
+                    cf[k][s] = V(0);
+                    pn[k][s] = V(0);
+                    if (nb[k][s] >= 0) {
+                        cf[k][s] = V(nb[k][s] > c ? u32[fc[k][s]] : l32[fc[k][s]]);
+                        pn[k][s] = p[nb[k][s]];
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kUA; ++k) {
+                const int c = ci + k * nt;
+                if (c >= c1) continue;
+                V acc = dc[k] * pc[k];
+#pragma unroll
+                for (int s = 0; s < kSlots; ++s)
+                    if (nb[k][s] >= 0) acc = fma(cf[k][s], sizeof(V) == 4 ? pn[k][s] - pc[k] : pn[k][s], acc);
+                q[c] = acc;
+                acc_dot(aq, acc, pc[k]);
+            }
         }
-        const double wApA = case_total(vq);
+        const double wApA = case_total(acc_value(aq));
         if (tid == 0) {   // k_b_pcg_alpha
             if (fabs(wApA) / S.nf[sg] < 1e-300) {
                 S.sing[sg] = 1;
@@ -720,21 +784,35 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
         }
         __syncthreads();
         // ---- x += alpha p; r -= alpha q; |r|
-        double vr = 0.0;
+        Acc ar;
         {
             const bool sing = S.sing[sg] != 0;
             const V alpha = V(S.alpha[sg]);
-            for (int c = c0 + tid; c < c1; c += nt) {
-                V rr = r[c];
-                if (!sing) {
-                    x[c] = fma(alpha, p[c], x[c]);
-                    rr = fma(-alpha, q[c], rr);
-                    r[c] = rr;
+            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
+                V rv[kU], xv[kU], pv[kU], qv[kU];
+#pragma unroll
+                for (int k = 0; k < kU; ++k) {
+                    const int c = ci + k * nt;
+                    const bool in = c < c1;
+                    rv[k] = in ? r[c] : V(0);
+                    xv[k] = (in && !sing) ? x[c] : V(0);
+                    pv[k] = (in && !sing) ? p[c] : V(0);
+                    qv[k] = (in && !sing) ? q[c] : V(0);
                 }
-                vr += fabs((double)rr);
+#pragma unroll
+                for (int k = 0; k < kU; ++k) {
+                    const int c = ci + k * nt;
+                    if (c >= c1) continue;
+                    if (!sing) {
+                        x[c] = fma(alpha, pv[k], xv[k]);
+                        rv[k] = fma(-alpha, qv[k], rv[k]);
+                        r[c] = rv[k];
+                    }
+                    acc_add(ar, fabs(rv[k]));
+                }
             }
         }
-        const double rs = case_total(vr);
+        const double rs = case_total(acc_value(ar));
         if (tid == 0) {   // k_b_iter_fin
             if (S.sing[sg]) {
                 S.active[sg] = 0;
@@ -779,6 +857,387 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
             }
         }
         if (tid == 0) S.repl[sg] = 0;
+    }
+}
+
+// ---- the persistent per-case BiCGStab -------------------------------------
+// One CTA per case runs the momentum solve of its components (up to three,
+// the valid ones of vm) through every iteration: the operations and scalar
+// decisions of BSolver::bicg_iteration for each segment (case, component),
+// including the half-step exit and the residual replacements of the mixed
+// form, with one-pass reductions per case.
+
+// the CTA's sums of n values, valid in every thread (each warp reduces the
+// warp totals itself, so all warps agree)
+template <int n>
+__device__ void case_totals(double (&v)[n]) {
+    __shared__ double sh[n][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < n; ++i) sh[i][wid] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+        double t = lane < nw ? sh[i][lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        v[i] = t;
+    }
+    __syncthreads();
+}
+
+// y = A x for the components in m (FP32: differences form over the row sums)
+template <class V>
+__device__ void case_amul(const BEll &e, int N, int c0, int c1, unsigned m, const V *__restrict__ d32,
+                          const V *__restrict__ u32, const V *__restrict__ l32, const V *__restrict__ x,
+                          V *__restrict__ y) {
+    const int nt = blockDim.x;
+    for (int c = c0 + (int)threadIdx.x; c < c1; c += nt) {
+        int nb[kSlots], fc[kSlots];
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s) {
+            const bool sl = s < e.nSlots;
+            nb[s] = sl ? __ldg(e.nbr + (size_t)s * N + c) : -1;
+            fc[s] = sl ? __ldg(e.face + (size_t)s * N + c) : -1;
+        }
+        const V dc = d32[c];
+        V cf[kSlots];
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s) cf[s] = nb[s] >= 0 ? V(nb[s] > c ? u32[fc[s]] : l32[fc[s]]) : V(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (!((m >> k) & 1u)) continue;
+            const size_t o = (size_t)k * N;
+            const V xc = x[o + c];
+            V xn[kSlots];
+#pragma unroll
+            for (int s = 0; s < kSlots; ++s) xn[s] = nb[s] >= 0 ? x[o + nb[s]] : V(0);
+            V acc = dc * xc;
+#pragma unroll
+            for (int s = 0; s < kSlots; ++s)
+                if (nb[s] >= 0) acc = fma(cf[s], sizeof(V) == 4 ? xn[s] - xc : xn[s], acc);
+            y[o + c] = acc;
+        }
+    }
+}
+
+// w = M^-1 r for the components in m (gather, forward and backward sweeps)
+template <class V>
+__device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m, const V *__restrict__ r,
+                                  V *__restrict__ w, int *err, long long maxSpin, V *ring, int *sProg) {
+    const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
+    for (long long i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        const int c = __ldg(g.cellOf + i);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if ((m >> k) & 1u) g.rS[(long long)k * g.nSkew + i] = c >= 0 ? r[(size_t)k * N + c] : V(0);
+    }
+    for (int mode = 0; mode < 2; ++mode) {
+        if (threadIdx.x < 32) sProg[threadIdx.x] = 0;
+        __syncthreads();
+        if (mode == 0) sweep2d_cta<V, 0, 3, 4>(g, cb, m, nullptr, N, err, maxSpin, ring, sProg);
+        else sweep2d_cta<V, 1, 3, 4>(g, cb, m, w, N, err, maxSpin, ring, sProg);
+        __syncthreads();
+    }
+}
+
+template <class V>
+__global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e, Skew2D<V> g, BSeg S, Ctl ctl,
+                                                              unsigned vm, int mixed, const V *__restrict__ d32,
+                                                              const V *__restrict__ u32, const V *__restrict__ l32,
+                                                              const double *__restrict__ diag,
+                                                              const double *__restrict__ upper,
+                                                              const double *__restrict__ lower,
+                                                              const double *__restrict__ b, double *__restrict__ psi,
+                                                              V *__restrict__ r, const V *__restrict__ r0,
+                                                              V *__restrict__ p, V *__restrict__ y,
+                                                              V *__restrict__ Ay, V *__restrict__ sv,
+                                                              V *__restrict__ z, V *__restrict__ tt,
+                                                              V *__restrict__ x, const int *__restrict__ order,
+                                                              int *err, long long maxSpin, int cap) {
+    using Acc = typename AccOf<V>::type;
+    __shared__ __align__(16) V ring[8 * s2d::kRJ * 3];
+    __shared__ int sProg[32];
+    __shared__ unsigned sMask[2];   // [0] active & !sing, [1] replacement flags
+    const int cb = order[blockIdx.x], tid = threadIdx.x, nt = blockDim.x, N = t.N;
+    const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
+    const int s0 = cb * 8;
+    // the segments (components) selected by a predicate on their state
+    auto seg_mask = [&](auto pred) {
+        unsigned mm = 0;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (((vm >> k) & 1u) && pred(s0 + k)) mm |= 1u << k;
+        return mm;
+    };
+    // psi += x, x = 0, r = b - A psi (FP64) on the segments in mr; |r| per segment
+    auto replace = [&](unsigned mr, double (&tot)[3]) {
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) tot[k] = 0.0;
+        if (!mr) return;
+        for (int c = c0 + tid; c < c1; c += nt)
+            #pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (!((mr >> k) & 1u)) continue;
+                const size_t i = (size_t)k * N + c;
+                psi[i] += (double)x[i];
+                x[i] = V(0);
+            }
+        __syncthreads();
+        for (int c = c0 + tid; c < c1; c += nt)
+            #pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (!((mr >> k) & 1u)) continue;
+                const size_t o = (size_t)k * N;
+                const double rr = b[o + c] - brow_mul(e, c, diag, upper, lower, psi + o);
+                r[o + c] = (V)rr;
+                tot[k] += fabs(rr);
+            }
+        case_totals(tot);
+    };
+    for (int it = 0; it < cap; ++it) {
+        __syncthreads();
+        const unsigned act = seg_mask([&](int sg) { return S.active[sg] != 0; });
+        if (!act) break;
+        // ---- r0r = r0.r; beta, singular stops
+        {
+            Acc a[3];
+            for (int c = c0 + tid; c < c1; c += nt)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if ((act >> k) & 1u) acc_dot(a[k], r0[(size_t)k * N + c], r[(size_t)k * N + c]);
+            double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
+            case_totals(v);
+            if (tid == 0) {   // k_b_bicg_r0r
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!((act >> k) & 1u)) continue;
+                    const int sg = s0 + k;
+                    const double old = S.r0r[sg], r0r = v[k];
+                    S.r0rOld[sg] = old;
+                    S.r0r[sg] = r0r;
+                    if (fabs(r0r) < 1e-300) { S.sing[sg] = 1; continue; }
+                    if (S.iter[sg] > 0 && !S.rst[sg]) {
+                        const double om = S.omega[sg];
+                        if (fabs(om) < 1e-300) { S.sing[sg] = 1; continue; }
+                        S.beta[sg] = (r0r / old) * (S.alpha[sg] / om);
+                    }
+                }
+                sMask[0] = seg_mask([&](int sg) { return S.active[sg] && !S.sing[sg]; });
+            }
+            __syncthreads();
+        }
+        const unsigned live = sMask[0];
+        // ---- p = r + beta (p - omega Ay)
+        for (int c = c0 + tid; c < c1; c += nt)
+            #pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (!((live >> k) & 1u)) continue;
+                const int sg = s0 + k;
+                const size_t i = (size_t)k * N + c;
+                if (S.iter[sg] == 0 || S.rst[sg]) p[i] = r[i];
+                else p[i] = fma(V(S.beta[sg]), fma(-V(S.omega[sg]), Ay[i], p[i]), r[i]);
+            }
+        __syncthreads();
+        // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
+        case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg);
+        if (*(volatile int *)err) break;
+        case_amul(e, N, c0, c1, vm, d32, u32, l32, y, Ay);
+        __syncthreads();
+        {
+            Acc a[3];
+            for (int c = c0 + tid; c < c1; c += nt)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if ((live >> k) & 1u) acc_dot(a[k], r0[(size_t)k * N + c], Ay[(size_t)k * N + c]);
+            double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
+            case_totals(v);
+            if (tid == 0)   // k_b_bicg_alpha
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!((live >> k) & 1u)) continue;
+                    S.alpha[s0 + k] = S.r0r[s0 + k] / v[k];
+                    S.rst[s0 + k] = 0;
+                }
+            __syncthreads();
+        }
+        // ---- s = r - alpha Ay; the half-step test on |s|
+        {
+            Acc a[3];
+            for (int c = c0 + tid; c < c1; c += nt)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!((live >> k) & 1u)) continue;
+                    const size_t i = (size_t)k * N + c;
+                    const V sk = fma(-V(S.alpha[s0 + k]), Ay[i], r[i]);
+                    sv[i] = sk;
+                    acc_add(a[k], fabs(sk));
+                }
+            double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
+            case_totals(v);
+            if (tid == 0) {   // k_b_bicg_half
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int sg = s0 + k;
+                    if (!((vm >> k) & 1u) || !S.active[sg]) continue;
+                    if (S.sing[sg]) {
+                        S.active[sg] = 0;
+                        continue;
+                    }
+                    const double fs = v[k] / S.nf[sg];
+                    if (bconv(ctl, fs, S.init[sg])) {
+                        S.conv[sg] = 2;
+                        S.repl[sg] = mixed ? 1 : 0;
+                        if (!mixed) S.fin[sg] = fs;
+                    }
+                }
+                sMask[0] = seg_mask([&](int sg) { return S.conv[sg] == 2; });
+                sMask[1] = seg_mask([&](int sg) { return S.repl[sg] != 0; });
+            }
+            __syncthreads();
+        }
+        // ---- half-step exit: x += alpha y; replacement; stop or restart
+        {
+            const unsigned half = sMask[0], mr = sMask[1];
+            if (half) {
+                for (int c = c0 + tid; c < c1; c += nt)
+                    #pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        if (!((half >> k) & 1u)) continue;
+                        const size_t i = (size_t)k * N + c;
+                        x[i] = fma(V(S.alpha[s0 + k]), y[i], x[i]);
+                    }
+                __syncthreads();
+            }
+            double tot[3];
+            replace(mr, tot);
+            if (tid == 0) {   // k_b_half_after
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int sg = s0 + k;
+                    if (!((vm >> k) & 1u) || !S.active[sg] || S.conv[sg] != 2) continue;
+                    if (!mixed) {
+                        S.iter[sg] += 1;
+                        S.conv[sg] = 1;
+                        S.active[sg] = 0;
+                        continue;
+                    }
+                    const double fin = tot[k] / S.nf[sg];
+                    S.fin[sg] = fin;
+                    S.last[sg] = fin;
+                    S.repl[sg] = 0;
+                    const int itn = S.iter[sg] + 1;
+                    const bool c = bconv(ctl, fin, S.init[sg]);
+                    if ((c && itn >= ctl.minIter) || itn >= ctl.maxIter || !isfinite(fin)) {
+                        S.iter[sg] = itn;
+                        S.conv[sg] = c ? 1 : 0;
+                        S.active[sg] = 0;
+                    } else {
+                        S.rst[sg] = 1;
+                    }
+                }
+                sMask[0] = seg_mask([&](int sg) { return S.active[sg] && !S.sing[sg] && S.conv[sg] != 2; });
+            }
+            __syncthreads();
+        }
+        const unsigned full = sMask[0];
+        // ---- z = M^-1 s, tt = A z, omega = tt.s / tt.tt
+        case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg);
+        if (*(volatile int *)err) break;
+        case_amul(e, N, c0, c1, vm, d32, u32, l32, z, tt);
+        __syncthreads();
+        {
+            Acc a[6];
+            for (int c = c0 + tid; c < c1; c += nt)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!((vm >> k) & 1u) || !S.active[s0 + k]) continue;
+                    const V tk = tt[(size_t)k * N + c];
+                    acc_dot(a[k], tk, tk);
+                    acc_dot(a[3 + k], tk, sv[(size_t)k * N + c]);
+                }
+            double v[6];
+            #pragma unroll
+            for (int i = 0; i < 6; ++i) v[i] = acc_value(a[i]);
+            case_totals(v);
+            if (tid == 0)   // k_b_bicg_omega
+                #pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if ((full >> k) & 1u) S.omega[s0 + k] = v[3 + k] / v[k];
+            __syncthreads();
+        }
+        // ---- x += alpha y + omega z; r = s - omega tt; |r|; the stopping test
+        {
+            Acc a[3];
+            for (int c = c0 + tid; c < c1; c += nt)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!((full >> k) & 1u)) continue;
+                    const size_t i = (size_t)k * N + c;
+                    const V alpha = V(S.alpha[s0 + k]), omega = V(S.omega[s0 + k]);
+                    x[i] = fma(alpha, y[i], fma(omega, z[i], x[i]));
+                    const V rv = fma(-omega, tt[i], sv[i]);
+                    r[i] = rv;
+                    acc_add(a[k], fabs(rv));
+                }
+            double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
+            case_totals(v);
+            if (tid == 0) {   // k_b_iter_fin (skipHalf)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int sg = s0 + k;
+                    if (!((vm >> k) & 1u) || !S.active[sg]) continue;
+                    if (S.conv[sg] == 2) {
+                        S.iter[sg] += 1;
+                        S.conv[sg] = 0;
+                        continue;
+                    }
+                    if (S.sing[sg]) {
+                        S.active[sg] = 0;
+                        continue;
+                    }
+                    const double fin = v[k] / S.nf[sg];
+                    S.fin[sg] = fin;
+                    S.iter[sg] += 1;
+                    if (mixed) {
+                        S.repl[sg] = (fin < kReplaceB * S.last[sg] || bconv(ctl, fin, S.init[sg]) ||
+                                      S.iter[sg] >= ctl.maxIter || !isfinite(fin)) ? 1 : 0;
+                    } else {
+                        const bool c = bconv(ctl, fin, S.init[sg]);
+                        const bool more = (S.iter[sg] < ctl.maxIter && !c) || S.iter[sg] < ctl.minIter;
+                        S.conv[sg] = c ? 1 : 0;
+                        if (!more || !isfinite(fin)) S.active[sg] = 0;
+                    }
+                }
+                sMask[1] = seg_mask([&](int sg) { return S.repl[sg] != 0; });
+            }
+            __syncthreads();
+        }
+        // ---- replacement; k_b_after
+        {
+            double tot[3];
+            const unsigned mr = sMask[1];
+            replace(mr, tot);
+            if (tid == 0)
+                #pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int sg = s0 + k;
+                    if (!((vm >> k) & 1u)) continue;
+                    if (S.active[sg] && S.repl[sg]) {
+                        const double fin = tot[k] / S.nf[sg];
+                        S.fin[sg] = fin;
+                        S.last[sg] = fin;
+                        const bool c = bconv(ctl, fin, S.init[sg]);
+                        const bool more = (S.iter[sg] < ctl.maxIter && !c) || S.iter[sg] < ctl.minIter;
+                        S.conv[sg] = c ? 1 : 0;
+                        if (!more || !isfinite(fin)) S.active[sg] = 0;
+                    }
+                    S.repl[sg] = 0;
+                }
+        }
     }
 }
 
@@ -1006,7 +1465,7 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
     // runs every iteration of its case (RT_OPT_BATCH_PERSISTENT)
     const int pre = a.ctl.preconditioner;
     Batch &bt = ctx->mesh.batch;
-    if (active && pcg && ctx->batchPersistent && bt.sweep2d && a.nc == 1 && bt.maxJB <= 8 &&
+    if (active && pcg && ctx->batchPersistent && bt.sweep2d && a.nc == 1 && bt.maxJB <= 8 && sv.e.nSlots <= kSlots &&
         (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU)) {
         Skew2D<V> g;
         if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);
@@ -1015,8 +1474,26 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
             ProfScope ps(ctx, "batch_pcg_persistent");
             k_b_pcg_case<V><<<bt.n, kCaseThreads, 0, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
                                                               sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
-                                                              sv.v(1), sv.v(2), sv.v(3), x, bt.sErr.p, 1ll << 22,
-                                                              cap);
+                                                              sv.v(1), sv.v(2), sv.v(3), x, bt.caseOrder.p,
+                                                              bt.sErr.p, 1ll << 22, cap);
+            RT_CHECK_LAUNCH();
+        }
+        launch_count(ctx);
+        bt.sPending = true;
+        active = 0;
+    }
+    // the momentum solve of the same cases (up to three components)
+    if (active && !pcg && ctx->batchPersistent && bt.sweep2d && a.nc <= 3 && (sv.vm & ~7u) == 0 &&
+        bt.maxJB <= 8 && sv.e.nSlots <= kSlots && (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU)) {
+        Skew2D<V> g;
+        if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);
+        else g = sweep2d_view64(ctx);
+        {
+            ProfScope ps(ctx, "batch_bicgstab_persistent");
+            k_b_bicg_case<V><<<bt.n, kCaseThreads, 0, sv.st>>>(
+                sv.t, sv.e, g, sv.S, sv.ctl, sv.vm, sv.mixed, sv.d32, sv.u32, sv.l32, a.diag, a.upper, a.lower,
+                a.source, a.psi, r, sv.v(1), sv.v(2), sv.v(3), sv.v(4), sv.v(5), sv.v(6), sv.v(7), x,
+                bt.caseOrder.p, bt.sErr.p, 1ll << 22, cap);
             RT_CHECK_LAUNCH();
         }
         launch_count(ctx);

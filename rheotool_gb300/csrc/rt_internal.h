@@ -207,6 +207,7 @@ struct Batch {
     DBuf<double> sData64;             // D, Py, Px, rDraw, rDinv, Ay, Ax, By, Bx, wS(6), rS(6)
     DBuf<float> sData32;              // rDinv, Ay, Ax, By, Bx, wS(6), rS(6)
     DBuf<int> sErr;                   // bounded-wait error flag of the batched sweeps
+    DBuf<int> caseOrder;              // n: cases by decreasing cell count (the CTA order of one-CTA-per-case launches)
     bool sPending = false;
     // batched Krylov state: per-segment scalars (segment = case * 8 + component),
     // case-aligned reduction partials and results
@@ -284,6 +285,11 @@ struct DevCase {
     rt_case_ctl ctl{};
     std::vector<int> kindU, kindP, kindTheta, kindTau;   // per patch
     DBuf<int> bkU, bkP, bkTh, bkTau;                      // per boundary face
+    // batches: the boundary faces whose tau values follow the field (zero
+    // gradient, linear extrapolation) in waves, wave k holding the k-th such
+    // patch of every case (empty for a single case)
+    std::vector<int> tauWaveH;                            // nWaves + 1 starts
+    DBuf<int> tauWaveFace;
     DBuf<double> UbFixed, pbFixed, thetabFixed, taubFixed;
     // state (SoA)
     DBuf<double> U, Ub, p, pb, phi, phib, theta, thetab, tau, taub, eigVals, eigVecs;

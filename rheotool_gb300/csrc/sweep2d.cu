@@ -26,14 +26,16 @@ namespace rt {
 
 namespace {
 
-template <class Real, int MODE, int NC, int P>
-__global__ void __launch_bounds__(1024) k_sweep2d(Skew2D<Real> g, unsigned mask, Real *__restrict__ w, int N,
-                                                  int *err, long long maxSpin) {
+// MAXT: 256 threads (up to 8 j-blocks, the register room for the prefetched
+// chunk) or 1024 (up to 32)
+template <class Real, int MODE, int NC, int P, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_sweep2d(Skew2D<Real> g, const int *__restrict__ order, unsigned mask,
+                                                  Real *__restrict__ w, int N, int *err, long long maxSpin) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int sProg[32];
     if (threadIdx.x < 32) sProg[threadIdx.x] = 0;
     __syncthreads();
-    sweep2d_cta<Real, MODE, NC, P>(g, blockIdx.x, mask, w, N, err, maxSpin, reinterpret_cast<Real *>(smem_raw),
+    sweep2d_cta<Real, MODE, NC, P, (MAXT <= 256)>(g, order[blockIdx.x], mask, w, N, err, maxSpin, reinterpret_cast<Real *>(smem_raw),
                                    sProg);
 }
 
@@ -126,19 +128,26 @@ Skew2D<float> view2d<float>(Batch &b) {
     return g;
 }
 
-template <class Real, int MODE, int NC, int P>
-void launch2d(rt_ctx *ctx, const Skew2D<Real> &g, unsigned mask, Real *w) {
+template <class Real, int MODE, int NC, int P, int MAXT>
+void launch2d_t(rt_ctx *ctx, const Skew2D<Real> &g, unsigned mask, Real *w) {
     Batch &b = ctx->mesh.batch;
     const size_t shm = (size_t)b.maxJB * s2d::kRJ * NC * sizeof(Real);
     static size_t attr = 0;
     if (shm > attr && shm > 48 * 1024) {
-        RT_CUDA(cudaFuncSetAttribute(k_sweep2d<Real, MODE, NC, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        RT_CUDA(cudaFuncSetAttribute(k_sweep2d<Real, MODE, NC, P, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)shm));
         attr = shm;
     }
-    k_sweep2d<Real, MODE, NC, P><<<b.n, 32 * b.maxJB, shm, ctx->stream>>>(g, mask, w, ctx->mesh.N, b.sErr.p,
-                                                                          1ll << 22);
+    k_sweep2d<Real, MODE, NC, P, MAXT><<<b.n, 32 * b.maxJB, shm, ctx->stream>>>(g, b.caseOrder.p, mask, w,
+                                                                                ctx->mesh.N, b.sErr.p, 1ll << 22);
     RT_CHECK_LAUNCH();
+}
+
+template <class Real, int MODE, int NC, int P>
+void launch2d(rt_ctx *ctx, const Skew2D<Real> &g, unsigned mask, Real *w) {
+    Batch &b = ctx->mesh.batch;
+    if (b.maxJB <= 8) launch2d_t<Real, MODE, NC, P, 256>(ctx, g, mask, w);
+    else launch2d_t<Real, MODE, NC, P, 1024>(ctx, g, mask, w);
     launch_count(ctx);
     b.sPending = true;
 }

@@ -38,12 +38,45 @@ __device__ __forceinline__ int spin_cta(const int *c, int need, int *err, long l
 
 }  // namespace s2d
 
+// the coefficients and inputs of one chunk of P steps of a lane
+template <class Real, int NC, int P>
+struct S2Chunk {
+    Real c0[P], cy[P], cx[P];
+    Real rk[P][NC];
+    int cell[P];
+};
+
+// loads of the chunk starting at step t0 (independent of the recurrence):
+// coefficients and cell numbers through the read-only path, the sweep input
+// (written earlier in the same kernel by the persistent solver) plainly
+template <class Real, int MODE, int NC, int P>
+__device__ __forceinline__ void s2_load(const Skew2D<Real> &g, long long e0, long long st, int t0,
+                                        S2Chunk<Real, NC, P> &k) {
+#pragma unroll
+    for (int s = 0; s < P; ++s) {
+        const long long e = e0 + (long long)(t0 + s) * st;
+        if (MODE == 2) {
+            k.c0[s] = __ldg(g.D + e); k.cy[s] = __ldg(g.Py + e); k.cx[s] = __ldg(g.Px + e);
+        } else {
+            k.c0[s] = (MODE == 0) ? __ldg(g.rDinv + e) : Real(0);
+            k.cy[s] = __ldg(((MODE == 0) ? g.Ay : g.By) + e);
+            k.cx[s] = __ldg(((MODE == 0) ? g.Ax : g.Bx) + e);
+#pragma unroll
+            for (int q = 0; q < NC; ++q) k.rk[s][q] = ((MODE == 0) ? g.rS : g.wS)[(long long)q * g.nSkew + e];
+        }
+        k.cell[s] = (MODE == 1) ? __ldg(g.cellOf + e) : 0;
+    }
+}
+
 // One case's sweep by the CTA that owns it (case cb; warps past the case's
 // j-blocks do nothing).  MODE 0: forward application (rS -> wS), 1: backward
 // application (wS -> w), 2: rD recurrence (D, Py, Px -> rDraw).  ringJ: the
 // j-block ring in shared memory ([maxJB][kRJ][NC]), sProg: 32 progress
-// counters, zero on entry (the caller clears them and synchronises).
-template <class Real, int MODE, int NC, int P>
+// counters, zero on entry (the caller clears them and synchronises).  The
+// loads of chunk k + 1 are issued before the waits and the recurrence of
+// chunk k, so their latency hides behind the dependent chain (PF; without
+// it, for launches of up to 1024 threads, each chunk loads just before use).
+template <class Real, int MODE, int NC, int P, bool PF = true>
 __device__ void sweep2d_cta(const Skew2D<Real> &g, int cb, unsigned mask, Real *__restrict__ w, int N, int *err,
                             long long maxSpin, Real *ringJ, int *sProg) {
     const int lane = threadIdx.x & 31, jo = threadIdx.x >> 5;
@@ -61,8 +94,11 @@ __device__ void sweep2d_cta(const Skew2D<Real> &g, int cb, unsigned mask, Real *
 #pragma unroll
     for (int q = 0; q < NC; ++q) yprev[q] = zk;
     int seenJ = 0, seenCJ = 0;
+    S2Chunk<Real, NC, P> cur, nxt;
+    if (PF) s2_load<Real, MODE, NC, P>(g, e0, st, 0, cur);
     for (int t0 = 0; t0 < T; t0 += P) {
         const int te = t0 + P;   // T is a multiple of P
+        if (PF && te < T) s2_load<Real, MODE, NC, P>(g, e0, st, te, nxt);
         // the consumer has read the ring slots this chunk overwrites
         if (consJ >= 0 && seenCJ < te - s2d::kRJ - 31) {
             int v = 0;
@@ -80,23 +116,7 @@ __device__ void sweep2d_cta(const Skew2D<Real> &g, int cb, unsigned mask, Real *
             seenJ = v;
         }
         __syncwarp();
-        // loads of the chunk (independent of the recurrence)
-        Real c0[P], cy[P], cx[P], rk[P][NC];
-        int cell[P];
-#pragma unroll
-        for (int s = 0; s < P; ++s) {
-            const long long e = e0 + (long long)(t0 + s) * st;
-            if (MODE == 2) {
-                c0[s] = g.D[e]; cy[s] = g.Py[e]; cx[s] = g.Px[e];
-            } else {
-                c0[s] = (MODE == 0) ? g.rDinv[e] : Real(0);
-                cy[s] = (MODE == 0) ? g.Ay[e] : g.By[e];
-                cx[s] = (MODE == 0) ? g.Ax[e] : g.Bx[e];
-#pragma unroll
-                for (int q = 0; q < NC; ++q) rk[s][q] = ((MODE == 0) ? g.rS : g.wS)[(long long)q * g.nSkew + e];
-            }
-            cell[s] = (MODE == 1) ? g.cellOf[e] : 0;
-        }
+        if (!PF) s2_load<Real, MODE, NC, P>(g, e0, st, t0, cur);
         Real out[P][NC];
 #pragma unroll
         for (int s = 0; s < P; ++s) {
@@ -109,16 +129,16 @@ __device__ void sweep2d_cta(const Skew2D<Real> &g, int cb, unsigned mask, Real *
                                                                          : zk);
                 Real v;
                 if (MODE == 2) {
-                    v = r_sub(c0[s], r_div(cy[s], yj));
-                    v = r_sub(v, r_div(cx[s], yprev[q]));
+                    v = r_sub(cur.c0[s], r_div(cur.cy[s], yj));
+                    v = r_sub(v, r_div(cur.cx[s], yprev[q]));
                 } else {
-                    const Real pre = (MODE == 0) ? r_mul(c0[s], rk[s][q]) : rk[s][q];
+                    const Real pre = (MODE == 0) ? r_mul(cur.c0[s], cur.rk[s][q]) : cur.rk[s][q];
                     if (sizeof(Real) == 4) {   // FP32: the i term first (as the 3-D sweeps)
-                        v = r_fma(-cx[s], yprev[q], pre);
-                        v = r_fma(-cy[s], yj, v);
+                        v = r_fma(-cur.cx[s], yprev[q], pre);
+                        v = r_fma(-cur.cy[s], yj, v);
                     } else {
-                        v = r_fma(-cy[s], yj, pre);
-                        v = r_fma(-cx[s], yprev[q], v);
+                        v = r_fma(-cur.cy[s], yj, pre);
+                        v = r_fma(-cur.cx[s], yprev[q], v);
                     }
                 }
                 if (consJ >= 0 && lane == 31) ringJ[((size_t)jo * s2d::kRJ + (t & (s2d::kRJ - 1))) * NC + q] = v;
@@ -138,10 +158,11 @@ __device__ void sweep2d_cta(const Skew2D<Real> &g, int cb, unsigned mask, Real *
                 for (int q = 0; q < NC; ++q) {
                     if (!((mask >> q) & 1u)) continue;
                     if (MODE == 0) g.wS[(long long)q * g.nSkew + e] = out[s][q];
-                    else if (cell[s] >= 0) w[(long long)q * N + cell[s]] = out[s][q];
+                    else if (cur.cell[s] >= 0) w[(long long)q * N + cur.cell[s]] = out[s][q];
                 }
             }
         }
+        if (PF) cur = nxt;
     }
     // a warp that gave up releases everything it owes
     if (*(volatile int *)err && lane == 0) s2d::st_release_cta(sProg + jo, T);

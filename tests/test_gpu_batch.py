@@ -125,12 +125,12 @@ def test_batch_layout_rejects_a_face_across_cases(ctx):
 
 
 @pytest.mark.parametrize("precision", [abi.RT_PREC_FP64, abi.RT_PREC_MIXED])
-def test_batch_persistent_pressure_solve_equals_launch_sequence(precision):
-    """The batched pressure solve as one persistent CTA per case (all its
-    iterations in one launch) takes the per-iteration launch sequence's
-    scalar decisions with one-pass reductions per case (the launch path sums
-    256-cell blocks first): iteration counts within one, fields equal within
-    the parity bars (1e-9 FP64, 1e-6 mixed, or the case's round-off
+def test_batch_persistent_solves_equal_launch_sequence(precision):
+    """The batched pressure and momentum solves as one persistent CTA per
+    case (all its iterations in one launch) take the per-iteration launch
+    sequence's scalar decisions with one-pass reductions per case (the launch
+    path sums 256-cell blocks first): iteration counts close, fields equal
+    within the parity bars (1e-9 FP64, 1e-6 mixed, or the case's round-off
     sensitivity bar where it is larger)."""
     cases = cavity_sweep(n_cases=10, n_min=16, n_max=96, seed=9, dt=2e-3, precision=precision)
     out = {}
@@ -139,11 +139,16 @@ def test_batch_persistent_pressure_solve_equals_launch_sequence(precision):
         try:
             bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, persistent)
             bt.step(3)
-            out[persistent] = (bt.fields(), [p.p.nIterations for p in bt.case_perf()])
+            out[persistent] = (bt.fields(), [(p.p.nIterations, p.U[0].nIterations, p.U[1].nIterations)
+                                             for p in bt.case_perf()])
         finally:
             bt.ctx.close()
-    assert all(abs(a - b) <= 1 for a, b in zip(out[0][1], out[1][1])), (out[0][1], out[1][1])
-    assert max(out[1][1]) > 20
+    # PCG within one iteration; BiCGStab's residual is not monotone, so a
+    # round-off change moves its crossing of the tolerance by a few
+    for a, b in zip(out[0][1], out[1][1]):
+        assert abs(a[0] - b[0]) <= 1, (out[0][1], out[1][1])
+        assert all(abs(i - j) <= max(3, 0.1 * i) for i, j in zip(a[1:], b[1:])), (out[0][1], out[1][1])
+    assert max(i[0] for i in out[1][1]) > 20 and max(i[1] for i in out[1][1]) > 2
     plain = TOL_STEP if precision == abi.RT_PREC_FP64 else 1e-6
     for i, c in enumerate(cases):
         errs = {n: rel(getattr(out[1][0][i], n), getattr(out[0][0][i], n)) for n in NAMES}
