@@ -636,6 +636,16 @@ constexpr int kU = 4;                            // cells per thread whose loads
 constexpr int kUA = 2;                           // the same for q = A p
 constexpr int kSlots = 4;                        // ELL width of the 2-D cases
 
+// the bounded-wait error flag as one value for the whole CTA (another CTA
+// may set it at any time: every thread must take the same branch)
+__device__ bool case_error(const int *err) {
+    __shared__ int sv;
+    __syncthreads();
+    if (threadIdx.x == 0) sv = *(volatile const int *)err;
+    __syncthreads();
+    return sv != 0;
+}
+
 // the CTA's sum, valid in every thread
 __device__ double case_total(double v) {
     __shared__ double sv;
@@ -690,7 +700,7 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
             else sweep2d_cta<V, 1, 1, kCaseP<V>>(g, cb, 1u, w, N, err, maxSpin, ring, sProg);
             __syncthreads();
         }
-        if (*(volatile int *)err) break;
+        if (case_error(err)) break;
         // ---- rho = w.r (and w.q_old in the flexible form)
         Acc a0, a1;
 #pragma unroll 4
@@ -895,6 +905,7 @@ __device__ void case_amul(const BEll &e, int N, int c0, int c1, unsigned m, cons
                           const V *__restrict__ u32, const V *__restrict__ l32, const V *__restrict__ x,
                           V *__restrict__ y) {
     const int nt = blockDim.x;
+#pragma unroll 2
     for (int c = c0 + (int)threadIdx.x; c < c1; c += nt) {
         int nb[kSlots], fc[kSlots];
 #pragma unroll
@@ -924,7 +935,9 @@ __device__ void case_amul(const BEll &e, int N, int c0, int c1, unsigned m, cons
     }
 }
 
-// w = M^-1 r for the components in m (gather, forward and backward sweeps)
+// w = M^-1 r for the components in m (gather, forward and backward sweeps):
+// the sweeps of two components at a time, each by its own half of the CTA
+// (warps 0-7 and 8-15, one per j-block) with its own ring and counters
 template <class V>
 __device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m, const V *__restrict__ r,
                                   V *__restrict__ w, int *err, long long maxSpin, V *ring, int *sProg) {
@@ -935,12 +948,30 @@ __device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m,
         for (int k = 0; k < 3; ++k)
             if ((m >> k) & 1u) g.rS[(long long)k * g.nSkew + i] = c >= 0 ? r[(size_t)k * N + c] : V(0);
     }
-    for (int mode = 0; mode < 2; ++mode) {
-        if (threadIdx.x < 32) sProg[threadIdx.x] = 0;
-        __syncthreads();
-        if (mode == 0) sweep2d_cta<V, 0, 3, 4>(g, cb, m, nullptr, N, err, maxSpin, ring, sProg);
-        else sweep2d_cta<V, 1, 3, 4>(g, cb, m, w, N, err, maxSpin, ring, sProg);
-        __syncthreads();
+    int comps[3], nComp = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if ((m >> k) & 1u) comps[nComp++] = k;
+    for (int c0 = 0; c0 < nComp; c0 += 2) {
+        const int grp = threadIdx.x >= 256 ? 1 : 0;   // the half of the CTA
+        const int k = grp == 0 ? comps[c0] : (c0 + 1 < nComp ? comps[c0 + 1] : -1);
+        Skew2D<V> gk = g;
+        if (k >= 0) {
+            gk.rS += (long long)k * g.nSkew;
+            gk.wS += (long long)k * g.nSkew;
+        }
+        for (int mode = 0; mode < 2; ++mode) {
+            if (threadIdx.x < 32) sProg[threadIdx.x] = 0;
+            __syncthreads();
+            if (k >= 0) {
+                V *rg = ring + grp * 8 * s2d::kRJ;
+                if (mode == 0) sweep2d_cta<V, 0, 1, kCaseP<V>>(gk, cb, 1u, nullptr, N, err, maxSpin, rg,
+                                                               sProg + 8 * grp, 8 * grp);
+                else sweep2d_cta<V, 1, 1, kCaseP<V>>(gk, cb, 1u, w + (size_t)k * N, N, err, maxSpin, rg,
+                                                     sProg + 8 * grp, 8 * grp);
+            }
+            __syncthreads();
+        }
     }
 }
 
@@ -961,25 +992,30 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
     using Acc = typename AccOf<V>::type;
     __shared__ __align__(16) V ring[8 * s2d::kRJ * 3];
     __shared__ int sProg[32];
-    __shared__ unsigned sMask[2];   // [0] active & !sing, [1] replacement flags
+    // segment masks that thread 0 publishes, one slot per use, so that no
+    // slot is rewritten in an iteration after threads have read it without a
+    // barrier in between: [0] iterating, [1] half-step exits, [2] their
+    // replacements, [3] full steps, [4] end-of-iteration replacements
+    __shared__ unsigned sMask[5];
     const int cb = order[blockIdx.x], tid = threadIdx.x, nt = blockDim.x, N = t.N;
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const int s0 = cb * 8;
     // the segments (components) selected by a predicate on their state
     auto seg_mask = [&](auto pred) {
         unsigned mm = 0;
-        #pragma unroll
+#pragma unroll
         for (int k = 0; k < 3; ++k)
             if (((vm >> k) & 1u) && pred(s0 + k)) mm |= 1u << k;
         return mm;
     };
     // psi += x, x = 0, r = b - A psi (FP64) on the segments in mr; |r| per segment
     auto replace = [&](unsigned mr, double (&tot)[3]) {
-        #pragma unroll
+#pragma unroll
         for (int k = 0; k < 3; ++k) tot[k] = 0.0;
         if (!mr) return;
+#pragma unroll 4
         for (int c = c0 + tid; c < c1; c += nt)
-            #pragma unroll
+#pragma unroll
             for (int k = 0; k < 3; ++k) {
                 if (!((mr >> k) & 1u)) continue;
                 const size_t i = (size_t)k * N + c;
@@ -987,8 +1023,9 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                 x[i] = V(0);
             }
         __syncthreads();
+#pragma unroll 4
         for (int c = c0 + tid; c < c1; c += nt)
-            #pragma unroll
+#pragma unroll
             for (int k = 0; k < 3; ++k) {
                 if (!((mr >> k) & 1u)) continue;
                 const size_t o = (size_t)k * N;
@@ -1005,14 +1042,15 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- r0r = r0.r; beta, singular stops
         {
             Acc a[3];
+#pragma unroll 4
             for (int c = c0 + tid; c < c1; c += nt)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k)
                     if ((act >> k) & 1u) acc_dot(a[k], r0[(size_t)k * N + c], r[(size_t)k * N + c]);
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_bicg_r0r
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     if (!((act >> k) & 1u)) continue;
                     const int sg = s0 + k;
@@ -1032,31 +1070,43 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         }
         const unsigned live = sMask[0];
         // ---- p = r + beta (p - omega Ay)
-        for (int c = c0 + tid; c < c1; c += nt)
-            #pragma unroll
+        {
+            bool restart[3];
+            V beta[3], omega[3];
+#pragma unroll
             for (int k = 0; k < 3; ++k) {
-                if (!((live >> k) & 1u)) continue;
                 const int sg = s0 + k;
-                const size_t i = (size_t)k * N + c;
-                if (S.iter[sg] == 0 || S.rst[sg]) p[i] = r[i];
-                else p[i] = fma(V(S.beta[sg]), fma(-V(S.omega[sg]), Ay[i], p[i]), r[i]);
+                restart[k] = ((live >> k) & 1u) && (S.iter[sg] == 0 || S.rst[sg]);
+                beta[k] = V(S.beta[sg]);
+                omega[k] = V(S.omega[sg]);
             }
+#pragma unroll 4
+            for (int c = c0 + tid; c < c1; c += nt)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (!((live >> k) & 1u)) continue;
+                    const size_t i = (size_t)k * N + c;
+                    if (restart[k]) p[i] = r[i];
+                    else p[i] = fma(beta[k], fma(-omega[k], Ay[i], p[i]), r[i]);
+                }
+        }
         __syncthreads();
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
         case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg);
-        if (*(volatile int *)err) break;
+        if (case_error(err)) break;
         case_amul(e, N, c0, c1, vm, d32, u32, l32, y, Ay);
         __syncthreads();
         {
             Acc a[3];
+#pragma unroll 4
             for (int c = c0 + tid; c < c1; c += nt)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k)
                     if ((live >> k) & 1u) acc_dot(a[k], r0[(size_t)k * N + c], Ay[(size_t)k * N + c]);
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0)   // k_b_bicg_alpha
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     if (!((live >> k) & 1u)) continue;
                     S.alpha[s0 + k] = S.r0r[s0 + k] / v[k];
@@ -1067,19 +1117,23 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- s = r - alpha Ay; the half-step test on |s|
         {
             Acc a[3];
+            V alpha[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) alpha[k] = V(S.alpha[s0 + k]);
+#pragma unroll 4
             for (int c = c0 + tid; c < c1; c += nt)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     if (!((live >> k) & 1u)) continue;
                     const size_t i = (size_t)k * N + c;
-                    const V sk = fma(-V(S.alpha[s0 + k]), Ay[i], r[i]);
+                    const V sk = fma(-alpha[k], Ay[i], r[i]);
                     sv[i] = sk;
                     acc_add(a[k], fabs(sk));
                 }
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_bicg_half
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int sg = s0 + k;
                     if (!((vm >> k) & 1u) || !S.active[sg]) continue;
@@ -1094,17 +1148,18 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                         if (!mixed) S.fin[sg] = fs;
                     }
                 }
-                sMask[0] = seg_mask([&](int sg) { return S.conv[sg] == 2; });
-                sMask[1] = seg_mask([&](int sg) { return S.repl[sg] != 0; });
+                sMask[1] = seg_mask([&](int sg) { return S.conv[sg] == 2; });
+                sMask[2] = seg_mask([&](int sg) { return S.repl[sg] != 0; });
             }
             __syncthreads();
         }
         // ---- half-step exit: x += alpha y; replacement; stop or restart
         {
-            const unsigned half = sMask[0], mr = sMask[1];
+            const unsigned half = sMask[1], mr = sMask[2];
             if (half) {
+#pragma unroll 4
                 for (int c = c0 + tid; c < c1; c += nt)
-                    #pragma unroll
+#pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         if (!((half >> k) & 1u)) continue;
                         const size_t i = (size_t)k * N + c;
@@ -1115,7 +1170,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
             double tot[3];
             replace(mr, tot);
             if (tid == 0) {   // k_b_half_after
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int sg = s0 + k;
                     if (!((vm >> k) & 1u) || !S.active[sg] || S.conv[sg] != 2) continue;
@@ -1139,32 +1194,34 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                         S.rst[sg] = 1;
                     }
                 }
-                sMask[0] = seg_mask([&](int sg) { return S.active[sg] && !S.sing[sg] && S.conv[sg] != 2; });
+                sMask[3] = seg_mask([&](int sg) { return S.active[sg] && !S.sing[sg] && S.conv[sg] != 2; });
             }
             __syncthreads();
         }
-        const unsigned full = sMask[0];
+        const unsigned full = sMask[3];
         // ---- z = M^-1 s, tt = A z, omega = tt.s / tt.tt
         case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg);
-        if (*(volatile int *)err) break;
+        if (case_error(err)) break;
         case_amul(e, N, c0, c1, vm, d32, u32, l32, z, tt);
         __syncthreads();
         {
             Acc a[6];
+            const unsigned on = seg_mask([&](int sg) { return S.active[sg] != 0; });
+#pragma unroll 4
             for (int c = c0 + tid; c < c1; c += nt)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    if (!((vm >> k) & 1u) || !S.active[s0 + k]) continue;
+                    if (!((on >> k) & 1u)) continue;
                     const V tk = tt[(size_t)k * N + c];
                     acc_dot(a[k], tk, tk);
                     acc_dot(a[3 + k], tk, sv[(size_t)k * N + c]);
                 }
             double v[6];
-            #pragma unroll
+#pragma unroll
             for (int i = 0; i < 6; ++i) v[i] = acc_value(a[i]);
             case_totals(v);
             if (tid == 0)   // k_b_bicg_omega
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k)
                     if ((full >> k) & 1u) S.omega[s0 + k] = v[3 + k] / v[k];
             __syncthreads();
@@ -1172,21 +1229,27 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- x += alpha y + omega z; r = s - omega tt; |r|; the stopping test
         {
             Acc a[3];
+            V alpha[3], omega[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                alpha[k] = V(S.alpha[s0 + k]);
+                omega[k] = V(S.omega[s0 + k]);
+            }
+#pragma unroll 4
             for (int c = c0 + tid; c < c1; c += nt)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     if (!((full >> k) & 1u)) continue;
                     const size_t i = (size_t)k * N + c;
-                    const V alpha = V(S.alpha[s0 + k]), omega = V(S.omega[s0 + k]);
-                    x[i] = fma(alpha, y[i], fma(omega, z[i], x[i]));
-                    const V rv = fma(-omega, tt[i], sv[i]);
+                    x[i] = fma(alpha[k], y[i], fma(omega[k], z[i], x[i]));
+                    const V rv = fma(-omega[k], tt[i], sv[i]);
                     r[i] = rv;
                     acc_add(a[k], fabs(rv));
                 }
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_iter_fin (skipHalf)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int sg = s0 + k;
                     if (!((vm >> k) & 1u) || !S.active[sg]) continue;
@@ -1212,17 +1275,17 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                         if (!more || !isfinite(fin)) S.active[sg] = 0;
                     }
                 }
-                sMask[1] = seg_mask([&](int sg) { return S.repl[sg] != 0; });
+                sMask[4] = seg_mask([&](int sg) { return S.repl[sg] != 0; });
             }
             __syncthreads();
         }
         // ---- replacement; k_b_after
         {
             double tot[3];
-            const unsigned mr = sMask[1];
+            const unsigned mr = sMask[4];
             replace(mr, tot);
             if (tid == 0)
-                #pragma unroll
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int sg = s0 + k;
                     if (!((vm >> k) & 1u)) continue;

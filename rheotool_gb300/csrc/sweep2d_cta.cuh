@@ -68,8 +68,8 @@ __device__ __forceinline__ void s2_load(const Skew2D<Real> &g, long long e0, lon
     }
 }
 
-// One case's sweep by the CTA that owns it (case cb; warps past the case's
-// j-blocks do nothing).  MODE 0: forward application (rS -> wS), 1: backward
+// One case's sweep by the CTA that owns it (case cb; warps wbase .. wbase +
+// nJB - 1 take the j-blocks, the others do nothing).  MODE 0: forward application (rS -> wS), 1: backward
 // application (wS -> w), 2: rD recurrence (D, Py, Px -> rDraw).  ringJ: the
 // j-block ring in shared memory ([maxJB][kRJ][NC]), sProg: 32 progress
 // counters, zero on entry (the caller clears them and synchronises).  The
@@ -78,11 +78,11 @@ __device__ __forceinline__ void s2_load(const Skew2D<Real> &g, long long e0, lon
 // it, for launches of up to 1024 threads, each chunk loads just before use).
 template <class Real, int MODE, int NC, int P, bool PF = true>
 __device__ void sweep2d_cta(const Skew2D<Real> &g, int cb, unsigned mask, Real *__restrict__ w, int N, int *err,
-                            long long maxSpin, Real *ringJ, int *sProg) {
-    const int lane = threadIdx.x & 31, jo = threadIdx.x >> 5;
+                            long long maxSpin, Real *ringJ, int *sProg, int wbase = 0) {
+    const int lane = threadIdx.x & 31, jo = (int)(threadIdx.x >> 5) - wbase;
     const int nJB = g.JB[cb], T = g.T[cb];
     const long long off = g.off[cb];
-    if (jo >= nJB) return;
+    if (jo < 0 || jo >= nJB) return;
     const int jb = (MODE == 1) ? nJB - 1 - jo : jo;
     const long long e0 = (MODE == 1) ? off + ((long long)jb * T + (T - 1)) * 32 + (31 - lane)
                                      : off + (long long)jb * T * 32 + lane;
