@@ -631,7 +631,20 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
 // last bits).  Every scalar decision is the launch path's.
 constexpr int kCaseThreads = 512;
 template <class V>
-constexpr int kCaseP = sizeof(V) == 4 ? 8 : 4;   // sweep chunk (registers for the prefetched chunk)
+constexpr int kCaseP = sizeof(V) == 4 ? 8 : 4;   // sweep chunk of the pressure solve
+// the sweeps of the persistent solvers stage their chunks in shared memory
+// (cp.async) NB - 1 chunks ahead; the momentum solve runs two components'
+// sweeps side by side (16 warps), with shorter chunks
+constexpr int kCaseNB = 4;
+constexpr int kBicgP = 4;
+template <class V>
+constexpr int kBicgNB = sizeof(V) == 4 ? 4 : 2;
+template <class V, int NC, int P, int NB>
+__host__ __device__ constexpr int case_stage_bytes() {   // one warp's staging area, the larger of the two sweeps
+    return s2d::stage_bytes<V, 0, NC, P, NB>() > s2d::stage_bytes<V, 1, NC, P, NB>()
+               ? s2d::stage_bytes<V, 0, NC, P, NB>()
+               : s2d::stage_bytes<V, 1, NC, P, NB>();
+}
 constexpr int kU = 4;                            // cells per thread whose loads are issued together
 constexpr int kUA = 2;                           // the same for q = A p
 constexpr int kSlots = 4;                        // ELL width of the 2-D cases
@@ -658,7 +671,7 @@ __device__ double case_total(double v) {
 }
 
 template <class V>
-__global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Skew2D<V> g, BSeg S, Ctl ctl, int mixed,
+__global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, Skew2D<V> g, BSeg S, Ctl ctl, int mixed,
                                                               const V *__restrict__ d32, const V *__restrict__ u32,
                                                               const V *__restrict__ l32,
                                                               const double *__restrict__ diag,
@@ -670,8 +683,9 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
                                                               V *__restrict__ x, const int *__restrict__ order,
                                                               int *err, long long maxSpin, int cap) {
     using Acc = typename AccOf<V>::type;
-    __shared__ __align__(16) V ring[8 * s2d::kRJ];
+    __shared__ s2d::u64 ring[8 * s2d::kRJ * s2d::W<V>::n];
     __shared__ int sProg[32];
+    extern __shared__ __align__(16) unsigned char stageSmem[];   // 8 warps' sweep staging
     const int cb = order[blockIdx.x], sg = cb * 8, tid = threadIdx.x, nt = blockDim.x, N = t.N;
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
@@ -694,10 +708,14 @@ __global__ void __launch_bounds__(kCaseThreads) k_b_pcg_case(BTab t, BEll e, Ske
                 if (i0 + (long long)k * nt < e1) g.rS[i0 + (long long)k * nt] = v[k];
         }
         for (int mode = 0; mode < 2; ++mode) {
-            if (tid < 32) sProg[tid] = 0;
+            s2d::reset<V, 1>(ring, 8, sProg);
             __syncthreads();
-            if (mode == 0) sweep2d_cta<V, 0, 1, kCaseP<V>>(g, cb, 1u, nullptr, N, err, maxSpin, ring, sProg);
-            else sweep2d_cta<V, 1, 1, kCaseP<V>>(g, cb, 1u, w, N, err, maxSpin, ring, sProg);
+            if (mode == 0)
+                sweep2d_cta<V, 0, 1, kCaseP<V>, true, s2d::kRJ, kCaseNB>(g, cb, 1u, nullptr, N, err, maxSpin, ring,
+                                                                         sProg, 0, stageSmem);
+            else
+                sweep2d_cta<V, 1, 1, kCaseP<V>, true, s2d::kRJ, kCaseNB>(g, cb, 1u, w, N, err, maxSpin, ring, sProg,
+                                                                         0, stageSmem);
             __syncthreads();
         }
         if (case_error(err)) break;
@@ -940,7 +958,8 @@ __device__ void case_amul(const BEll &e, int N, int c0, int c1, unsigned m, cons
 // (warps 0-7 and 8-15, one per j-block) with its own ring and counters
 template <class V>
 __device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m, const V *__restrict__ r,
-                                  V *__restrict__ w, int *err, long long maxSpin, V *ring, int *sProg) {
+                                  V *__restrict__ w, int *err, long long maxSpin, s2d::u64 *ring, int *sProg,
+                                  unsigned char *stage) {
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
     for (long long i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
         const int c = __ldg(g.cellOf + i);
@@ -961,14 +980,17 @@ __device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m,
             gk.wS += (long long)k * g.nSkew;
         }
         for (int mode = 0; mode < 2; ++mode) {
-            if (threadIdx.x < 32) sProg[threadIdx.x] = 0;
+            s2d::reset<V, 1>(ring, 16, sProg);
             __syncthreads();
             if (k >= 0) {
-                V *rg = ring + grp * 8 * s2d::kRJ;
-                if (mode == 0) sweep2d_cta<V, 0, 1, kCaseP<V>>(gk, cb, 1u, nullptr, N, err, maxSpin, rg,
-                                                               sProg + 8 * grp, 8 * grp);
-                else sweep2d_cta<V, 1, 1, kCaseP<V>>(gk, cb, 1u, w + (size_t)k * N, N, err, maxSpin, rg,
-                                                     sProg + 8 * grp, 8 * grp);
+                s2d::u64 *rg = ring + grp * 8 * s2d::kRJ * s2d::W<V>::n;
+                unsigned char *sg = stage + (size_t)grp * 8 * case_stage_bytes<V, 1, kBicgP, kBicgNB<V>>();
+                if (mode == 0)
+                    sweep2d_cta<V, 0, 1, kBicgP, true, s2d::kRJ, kBicgNB<V>>(gk, cb, 1u, nullptr, N, err, maxSpin, rg,
+                                                                             sProg + 8 * grp, 8 * grp, sg);
+                else
+                    sweep2d_cta<V, 1, 1, kBicgP, true, s2d::kRJ, kBicgNB<V>>(gk, cb, 1u, w + (size_t)k * N, N, err,
+                                                                             maxSpin, rg, sProg + 8 * grp, 8 * grp, sg);
             }
             __syncthreads();
         }
@@ -990,7 +1012,8 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                                                               V *__restrict__ x, const int *__restrict__ order,
                                                               int *err, long long maxSpin, int cap) {
     using Acc = typename AccOf<V>::type;
-    __shared__ __align__(16) V ring[8 * s2d::kRJ * 3];
+    __shared__ s2d::u64 ring[16 * s2d::kRJ * s2d::W<V>::n];   // two halves of the CTA, 8 j-blocks each
+    extern __shared__ __align__(16) unsigned char stageSmem[];   // 16 warps' sweep staging
     __shared__ int sProg[32];
     // segment masks that thread 0 publishes, one slot per use, so that no
     // slot is rewritten in an iteration after threads have read it without a
@@ -1092,7 +1115,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         }
         __syncthreads();
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
-        case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg);
+        case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg, stageSmem);
         if (case_error(err)) break;
         case_amul(e, N, c0, c1, vm, d32, u32, l32, y, Ay);
         __syncthreads();
@@ -1200,7 +1223,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         }
         const unsigned full = sMask[3];
         // ---- z = M^-1 s, tt = A z, omega = tt.s / tt.tt
-        case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg);
+        case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg, stageSmem);
         if (case_error(err)) break;
         case_amul(e, N, c0, c1, vm, d32, u32, l32, z, tt);
         __syncthreads();
@@ -1535,7 +1558,9 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         else g = sweep2d_view64(ctx);
         {
             ProfScope ps(ctx, "batch_pcg_persistent");
-            k_b_pcg_case<V><<<bt.n, kCaseThreads, 0, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
+            const int shm = 8 * case_stage_bytes<V, 1, kCaseP<V>, kCaseNB>();
+            RT_CUDA(cudaFuncSetAttribute(k_b_pcg_case<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+            k_b_pcg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
                                                               sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
                                                               sv.v(1), sv.v(2), sv.v(3), x, bt.caseOrder.p,
                                                               bt.sErr.p, 1ll << 22, cap);
@@ -1553,7 +1578,9 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         else g = sweep2d_view64(ctx);
         {
             ProfScope ps(ctx, "batch_bicgstab_persistent");
-            k_b_bicg_case<V><<<bt.n, kCaseThreads, 0, sv.st>>>(
+            const int shm = 16 * case_stage_bytes<V, 1, kBicgP, kBicgNB<V>>();
+            RT_CUDA(cudaFuncSetAttribute(k_b_bicg_case<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+            k_b_bicg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(
                 sv.t, sv.e, g, sv.S, sv.ctl, sv.vm, sv.mixed, sv.d32, sv.u32, sv.l32, a.diag, a.upper, a.lower,
                 a.source, a.psi, r, sv.v(1), sv.v(2), sv.v(3), sv.v(4), sv.v(5), sv.v(6), sv.v(7), x,
                 bt.caseOrder.p, bt.sErr.p, 1ll << 22, cap);

@@ -8,7 +8,9 @@
 // consecutive rows (a j-block), lane l updating cell i = t - l of row
 // 32 jb + l at step t: the i-1 value is the lane's own previous result, the
 // j-1 value lane l-1's (shuffle), and lane 0 reads row 32 jb - 1 from the
-// j-block below through a shared-memory ring behind a progress counter.  The
+// j-block below through a shared-memory ring of tagged words (the value
+// with its step, so the reader waits on the data itself; the reader's
+// progress counter only bounds how far the writer runs ahead).  The
 // recurrences are evaluated in the order of operations of the sequential
 // sweep (y face, then x face), so an FP64 application equals the
 // level-scheduled one bit for bit; the FP32 applications of the mixed
@@ -16,8 +18,8 @@
 //
 // A case with nJB j-blocks runs nx + 31 + 32 (nJB - 1) steps; cases are
 // independent, so the CTAs of a launch never wait on one another.  Every wait
-// is bounded: a timeout sets the error flag, publishes the warp's progress as
-// complete (so no other warp waits on it) and the host reports RT_ETIMEOUT.
+// is bounded: a timeout sets the error flag, every other wait gives up on
+// seeing it, and the host reports RT_ETIMEOUT.
 #include "batch.h"
 #include "real_ops.cuh"
 #include "sweep2d_cta.cuh"
@@ -27,16 +29,21 @@ namespace rt {
 namespace {
 
 // MAXT: 256 threads (up to 8 j-blocks, the register room for the prefetched
-// chunk) or 1024 (up to 32)
+// chunk) or 1024 (up to 32, with a shallower j-block ring to fit the shared
+// memory)
+template <int MAXT>
+__host__ __device__ constexpr int ring2d() { return MAXT <= 256 ? s2d::kRJ : 64; }
 template <class Real, int MODE, int NC, int P, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_sweep2d(Skew2D<Real> g, const int *__restrict__ order, unsigned mask,
                                                   Real *__restrict__ w, int N, int *err, long long maxSpin) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int sProg[32];
-    if (threadIdx.x < 32) sProg[threadIdx.x] = 0;
+    constexpr int RJ = ring2d<MAXT>();
+    s2d::u64 *ring = reinterpret_cast<s2d::u64 *>(smem_raw);
+    const int cb = order[blockIdx.x];
+    s2d::reset<Real, NC, RJ>(ring, g.JB[cb], sProg);
     __syncthreads();
-    sweep2d_cta<Real, MODE, NC, P, (MAXT <= 256)>(g, order[blockIdx.x], mask, w, N, err, maxSpin, reinterpret_cast<Real *>(smem_raw),
-                                   sProg);
+    sweep2d_cta<Real, MODE, NC, P, (MAXT <= 256), RJ>(g, cb, mask, w, N, err, maxSpin, ring, sProg);
 }
 
 }  // namespace
@@ -131,7 +138,7 @@ Skew2D<float> view2d<float>(Batch &b) {
 template <class Real, int MODE, int NC, int P, int MAXT>
 void launch2d_t(rt_ctx *ctx, const Skew2D<Real> &g, unsigned mask, Real *w) {
     Batch &b = ctx->mesh.batch;
-    const size_t shm = (size_t)b.maxJB * s2d::kRJ * NC * sizeof(Real);
+    const size_t shm = (size_t)b.maxJB * ring2d<MAXT>() * NC * s2d::W<Real>::n * sizeof(s2d::u64);
     static size_t attr = 0;
     if (shm > attr && shm > 48 * 1024) {
         RT_CUDA(cudaFuncSetAttribute(k_sweep2d<Real, MODE, NC, P, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
