@@ -79,17 +79,39 @@ struct Ell {
     const int *__restrict__ nbr;
 };
 
+// The ELL slots of a row are read in groups of kSG: the neighbour and face
+// indices of the group first (one round of independent loads), then the
+// coefficients and neighbour values (a second), then the accumulation in slot
+// order.  A row ends in -1 padding, which adds nothing (the same sum as
+// stopping at the row's end).
+constexpr int kSG = 6;
+
+__device__ __forceinline__ void slot_group(const Ell &e, int c, int s0, int (&nb)[kSG], int (&f)[kSG]) {
+#pragma unroll
+    for (int j = 0; j < kSG; ++j) {
+        const bool in = s0 + j < e.nSlots;
+        nb[j] = in ? e.nbr[(s0 + j) * e.N + c] : -1;
+        f[j] = in ? e.face[(s0 + j) * e.N + c] : -1;
+    }
+}
+
 __device__ __forceinline__ double row_mul(const Ell &e, int c, const double *__restrict__ diag,
                                           const double *__restrict__ upper,
                                           const double *__restrict__ lower,
                                           const double *__restrict__ x) {
     double acc = diag[c] * x[c];
-    for (int s = 0; s < e.nSlots; ++s) {
-        int nb = e.nbr[s * e.N + c];
-        if (nb < 0) break;
-        int f = e.face[s * e.N + c];
-        double a = nb > c ? upper[f] : lower[f];
-        acc += a * x[nb];
+    for (int s0 = 0; s0 < e.nSlots; s0 += kSG) {
+        int nb[kSG], f[kSG];
+        slot_group(e, c, s0, nb, f);
+        double a[kSG], xn[kSG];
+#pragma unroll
+        for (int j = 0; j < kSG; ++j) {
+            a[j] = nb[j] >= 0 ? (nb[j] > c ? upper[f[j]] : lower[f[j]]) : 0.0;
+            xn[j] = nb[j] >= 0 ? x[nb[j]] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < kSG; ++j)
+            if (nb[j] >= 0) acc += a[j] * xn[j];
     }
     return acc;
 }
@@ -98,11 +120,15 @@ __device__ __forceinline__ double row_sum(const Ell &e, int c, const double *__r
                                           const double *__restrict__ upper,
                                           const double *__restrict__ lower) {
     double acc = diag[c];
-    for (int s = 0; s < e.nSlots; ++s) {
-        int nb = e.nbr[s * e.N + c];
-        if (nb < 0) break;
-        int f = e.face[s * e.N + c];
-        acc += nb > c ? upper[f] : lower[f];
+    for (int s0 = 0; s0 < e.nSlots; s0 += kSG) {
+        int nb[kSG], f[kSG];
+        slot_group(e, c, s0, nb, f);
+        double a[kSG];
+#pragma unroll
+        for (int j = 0; j < kSG; ++j) a[j] = nb[j] >= 0 ? (nb[j] > c ? upper[f[j]] : lower[f[j]]) : 0.0;
+#pragma unroll
+        for (int j = 0; j < kSG; ++j)
+            if (nb[j] >= 0) acc += a[j];
     }
     return acc;
 }
@@ -165,6 +191,7 @@ __global__ void k_dot(int N, unsigned mask, const double *__restrict__ a, const 
         if (!((mask >> k) & 1u)) continue;
         double v0 = 0.0, v1 = 0.0;
         size_t o = (size_t)k * N;
+        #pragma unroll 4
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             v0 += a[o + c] * b[o + c];
             if (c2) v1 += c2[o + c] * d2[o + c];
@@ -370,6 +397,7 @@ __global__ void k_pcg_update(int N, unsigned mask, const double *__restrict__ S,
         const double alpha = S[S_ALPHA * 8 + k];
         double v = 0.0;
         size_t o = (size_t)k * N;
+        #pragma unroll 4
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             if (!sing) {
                 psi[o + c] += alpha * pA[o + c];
@@ -403,6 +431,7 @@ __global__ void k_bicg_s(int N, unsigned mask, const double *__restrict__ S,
         const double alpha = S[S_ALPHA * 8 + k];
         double v = 0.0;
         size_t o = (size_t)k * N;
+        #pragma unroll 4
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             double s = rA[o + c] - alpha * AyA[o + c];
             sA[o + c] = s;
@@ -429,6 +458,7 @@ __global__ void k_bicg_update(int N, unsigned mask, const double *__restrict__ S
         const double alpha = S[S_ALPHA * 8 + k], omega = S[S_OMEGA * 8 + k];
         double v = 0.0;
         size_t o = (size_t)k * N;
+        #pragma unroll 4
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             psi[o + c] += alpha * yA[o + c] + omega * zA[o + c];
             double r = sA[o + c] - omega * tA[o + c];
@@ -513,6 +543,7 @@ __global__ void k_pcg_rho(int N, unsigned mask0, const unsigned *__restrict__ ac
         if (!((mask >> k) & 1u)) continue;
         double v0 = 0.0, v1 = 0.0;
         size_t o = (size_t)k * N;
+        #pragma unroll 4
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             v0 += w[o + c] * r[o + c];
             if (two) v1 += w[o + c] * qold[o + c];
@@ -552,16 +583,23 @@ __global__ void k_pcg_pq(Ell e, unsigned mask0, const unsigned *__restrict__ act
         const size_t o = (size_t)k * N;
         const double *wk = w + o, *pk = pold + o;
         double v = 0.0;
+#pragma unroll 2
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             const double pc = first ? wk[c] : fma(beta, pk[c], wk[c]);
             double acc = diag[c] * pc;
-            for (int s = 0; s < e.nSlots; ++s) {
-                const int nb = e.nbr[s * N + c];
-                if (nb < 0) break;
-                const int f = e.face[s * N + c];
-                const double a = nb > c ? upper[f] : lower[f];
-                const double pn = first ? wk[nb] : fma(beta, pk[nb], wk[nb]);
-                acc = fma(a, pn, acc);
+            for (int s0 = 0; s0 < e.nSlots; s0 += kSG) {
+                int nb[kSG], f[kSG];
+                slot_group(e, c, s0, nb, f);
+                double a[kSG], wn[kSG], pn[kSG];
+#pragma unroll
+                for (int j = 0; j < kSG; ++j) {
+                    a[j] = nb[j] >= 0 ? (nb[j] > c ? upper[f[j]] : lower[f[j]]) : 0.0;
+                    wn[j] = nb[j] >= 0 ? wk[nb[j]] : 0.0;
+                    pn[j] = (nb[j] >= 0 && !first) ? pk[nb[j]] : 0.0;
+                }
+#pragma unroll
+                for (int j = 0; j < kSG; ++j)
+                    if (nb[j] >= 0) acc = fma(a[j], first ? wn[j] : fma(beta, pn[j], wn[j]), acc);
             }
             pnew[o + c] = pc;
             q[o + c] = acc;
@@ -598,6 +636,7 @@ __global__ void k_pcg_step(int N, unsigned mask0, unsigned *active, rt_solver_ct
         const double alpha = S[S_ALPHA * 8 + k];
         double v = 0.0;
         size_t o = (size_t)k * N;
+        #pragma unroll 4
         for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
             if (!sing) {
                 psi[o + c] += alpha * p[o + c];
