@@ -295,12 +295,15 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * series of the same factorisation; Anzt, Chow and Dongarra 2015).  The FP64
  * plain form always uses the exact sweeps. */
 #define RT_OPT_MIXED_PRECOND 10
-/* RT_OPT_BATCH_PERSISTENT: the batched form's pressure solve on structured
- * 2-D cases (up to 256 rows) as one persistent CTA per case, each running
- * all the iterations of its case in one launch (1, default), or as a
- * per-iteration launch sequence replayed for all cases (0).  Both take the
- * same scalar decisions; the persistent form sums each case's reductions in
- * one pass of its CTA, so the iterates agree to round-off, not bit for bit. */
+/* RT_OPT_BATCH_PERSISTENT: the batched form's pressure and momentum solves
+ * on structured 2-D cases (up to 256 rows) as one persistent CTA per case,
+ * each running all the iterations of its case in one launch, or as a
+ * per-iteration launch sequence replayed for all cases.  0: the launch
+ * sequence; 1 (default): persistent when the batch holds at least half as
+ * many cases as the GPU has SMs (a CTA per case leaves a small batch's SMs
+ * idle); 2: persistent whatever the batch.  Both take the same scalar
+ * decisions; the persistent form sums each case's reductions in one pass of
+ * its CTA, so the iterates agree to round-off, not bit for bit. */
 #define RT_OPT_BATCH_PERSISTENT 11
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,

@@ -85,6 +85,13 @@ class BatchContext:
         md = _mesh_desc(self.mesh, self)
         self.ctx._check(lib.rt_mesh_upload(h, C.byref(md)), "rt_mesh_upload")
         self.ctx.mesh = self.mesh
+        one = self.cases[0].mesh
+        if len(self.cases) == 1 and one.shape is not None and getattr(one, "cellIJK", None) is not None:
+            # a batch of one case runs the single-case path: give it the case's
+            # structured description, so that its sweeps are the systolic ones
+            nx, ny, nz = one.shape
+            a = np.ascontiguousarray(one.cellIJK, dtype=np.int32)
+            self.ctx._check(lib.rt_mesh_set_ijk(h, nx, ny, nz, abi.iptr(a)), "rt_mesh_set_ijk")
         dims = np.array([c.mesh.shape if c.mesh.shape is not None else (0, 0, 0) for c in self.cases],
                         dtype=np.int32).reshape(-1)
         ijk = np.ascontiguousarray(self.mesh.cellIJK, dtype=np.int32)

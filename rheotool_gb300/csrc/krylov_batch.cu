@@ -1551,7 +1551,10 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
     // runs every iteration of its case (RT_OPT_BATCH_PERSISTENT)
     const int pre = a.ctl.preconditioner;
     Batch &bt = ctx->mesh.batch;
-    if (active && pcg && ctx->batchPersistent && bt.sweep2d && a.nc == 1 && bt.maxJB <= 8 && sv.e.nSlots <= kSlots &&
+    // one SM per case: worth it once the cases fill the GPU (a few large
+    // cases iterate faster with their vector work spread over every SM)
+    const bool persistent = ctx->batchPersistent == 2 || (ctx->batchPersistent == 1 && 2 * bt.n >= ctx->numSMs);
+    if (active && pcg && persistent && bt.sweep2d && a.nc == 1 && bt.maxJB <= 8 && sv.e.nSlots <= kSlots &&
         (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU)) {
         Skew2D<V> g;
         if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);
@@ -1571,7 +1574,7 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         active = 0;
     }
     // the momentum solve of the same cases (up to three components)
-    if (active && !pcg && ctx->batchPersistent && bt.sweep2d && a.nc <= 3 && (sv.vm & ~7u) == 0 &&
+    if (active && !pcg && persistent && bt.sweep2d && a.nc <= 3 && (sv.vm & ~7u) == 0 &&
         bt.maxJB <= 8 && sv.e.nSlots <= kSlots && (pre == RT_PRECOND_DIC || pre == RT_PRECOND_DILU)) {
         Skew2D<V> g;
         if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);

@@ -139,8 +139,8 @@ template <class Real, int MODE, int NC, int P, int MAXT>
 void launch2d_t(rt_ctx *ctx, const Skew2D<Real> &g, unsigned mask, Real *w) {
     Batch &b = ctx->mesh.batch;
     const size_t shm = (size_t)b.maxJB * ring2d<MAXT>() * NC * s2d::W<Real>::n * sizeof(s2d::u64);
-    static size_t attr = 0;
-    if (shm > attr && shm > 48 * 1024) {
+    static size_t attr = 0;   // the dynamic shared memory this kernel was opened to
+    if (shm > attr && shm + 1024 > 48 * 1024) {   // (beside its static counters)
         RT_CUDA(cudaFuncSetAttribute(k_sweep2d<Real, MODE, NC, P, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)shm));
         attr = shm;

@@ -137,7 +137,7 @@ def test_batch_persistent_solves_equal_launch_sequence(precision):
     for persistent in (0, 1):
         bt = BatchContext(cases)
         try:
-            bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, persistent)
+            bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, 2 if persistent else 0)
             bt.step(3)
             out[persistent] = (bt.fields(), [(p.p.nIterations, p.U[0].nIterations, p.U[1].nIterations)
                                              for p in bt.case_perf()])
@@ -177,3 +177,25 @@ def test_batch_of_one_case_equals_the_case_alone(ctx):
     alone = ctx.fields()
     for n in NAMES:
         assert np.array_equal(getattr(got, n), getattr(alone, n)), n
+
+
+def test_batch_of_256_row_cases_on_both_paths():
+    """Cases of 256 rows (eight j-blocks: the largest per-case sweep, whose
+    rings take the most shared memory) step through the launch sequence and
+    through the persistent solvers, and the two agree."""
+    cases = [cavity_case(256, model="GiesekusLog", Wi=1.0, dt=1e-3, alpha=0.1), cavity_case(40, dt=1e-3)]
+    for c in cases:
+        c.precision = abi.RT_PREC_MIXED
+    out = []
+    for mode in (0, 2):
+        bt = BatchContext(cases)
+        try:
+            bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, mode)
+            bt.step(2)
+            out.append((bt.fields(), [p.p.nIterations for p in bt.case_perf()]))
+        finally:
+            bt.ctx.close()
+    assert min(out[0][1]) > 0 and min(out[1][1]) > 0
+    for i in range(len(cases)):
+        for n in NAMES:
+            assert rel(getattr(out[1][0][i], n), getattr(out[0][0][i], n)) < 1e-6, (i, n)
