@@ -35,14 +35,23 @@
  *                                         sparseSolver.C:129-180
  *   - adjustCorrPhi ..................... solvers/shared/singlePhase/
  *                                         adjustCorrPhi.H:32-158
- * and OpenFOAM v9 behaviour that is not vendored in rheoTool (fvm::ddt Euler,
- * Gauss linear grad/div, orthogonal laplacian, fvMatrix A/H/H1/flux,
- * ddtCorr, setReference, PCG, PBiCGStab, DIC, DILU), restated from the
- * published methods:
+ *   - multiMode ......................... libs/constitutiveEquations/
+ *                                         constitutiveEqs/multiMode/multiMode.C:
+ *                                         144-156 (divTau), 222 (tau), 247-256
+ *                                         (correct)
+ *   - nNonOrthogonalCorrectors .......... solvers/rheoFoam/pEqn.H:31-50
+ * and OpenFOAM v9 behaviour that is not vendored in rheoTool (fvm::ddt Euler
+ * and Crank-Nicolson, Gauss linear grad/div, orthogonal laplacian, fvMatrix
+ * A/H/H1/flux, ddtCorr, setReference, PCG, PBiCGStab, PBiCG, DIC, DILU),
+ * restated from the published methods:
  *   - Gauss gradient, linear interpolation, orthogonal snGrad, Euler implicit
  *     ddt, SIMPLEC with Rhie-Chow/ddtCorr flux (Jasak 1996 thesis; Van
  *     Doormaal & Raithby 1984 for SIMPLEC);
- *   - CG (Hestenes & Stiefel 1952), BiCGStab (van der Vorst 1992), D-ILU(0)
+ *   - Crank-Nicolson ddt with off-centering psi as the trapezoidal rule on a
+ *     stored old-time derivative (psi = 1: the trapezoidal rule, psi = 0:
+ *     Euler implicit), the first step of a run Euler implicit;
+ *   - CG (Hestenes & Stiefel 1952), BiCGStab (van der Vorst 1992), BiCG
+ *     (Fletcher 1976) with the transposed preconditioner, D-ILU(0)
  *     with the diagonal chosen so that diag(M) = diag(A) (Pommerell 1992),
  *     applied as a forward and a backward substitution in face order;
  *   - cyclic Jacobi eigenvalue method with Rutishauser's rotation formulas;
