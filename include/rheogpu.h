@@ -305,6 +305,12 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * decisions; the persistent form sums each case's reductions in one pass of
  * its CTA, so the iterates agree to round-off, not bit for bit. */
 #define RT_OPT_BATCH_PERSISTENT 11
+/* RT_OPT_SWEEP_COMPONENTS: the systolic sweeps of a solve of two or three
+ * components (the momentum solve).  1 (default): the components side by
+ * side, one one-component sweep each in a single launch (each thread-block
+ * cluster takes a plane group of one component); 0: one sweep carrying all
+ * the components lane by lane.  Both give the same bits. */
+#define RT_OPT_SWEEP_COMPONENTS 12
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
                         const rt_model_params *model, const rt_case_ctl *ctl);

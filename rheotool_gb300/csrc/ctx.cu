@@ -477,6 +477,10 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
                        "triangular factor");
             ctx->mixedJacobi = (int)value;
             return RT_OK;
+        case RT_OPT_SWEEP_COMPONENTS:
+            RT_REQUIRE(value == 0 || value == 1, RT_EINVAL, "RT_OPT_SWEEP_COMPONENTS: 0 or 1");
+            ctx->sweepComponents = (int)value;
+            return RT_OK;
         case RT_OPT_BATCH_PERSISTENT:
             RT_REQUIRE(value >= 0 && value <= 2, RT_EINVAL, "RT_OPT_BATCH_PERSISTENT: 0 never, 1 auto, 2 always");
             ctx->batchPersistent = (int)value;

@@ -439,6 +439,7 @@ struct rt_ctx {
     // persistent CTA per case (RT_OPT_BATCH_PERSISTENT; 0: the per-iteration
     // launch sequence)
     int batchPersistent = 1;
+    int sweepComponents = 1;   // RT_OPT_SWEEP_COMPONENTS
     std::vector<rt_step_perf> batchPerf;   // per case: the last step's solver records
     rt::DBuf<double> scal;       // device scalars of the Krylov loops [32 slots][8]
     rt::DBuf<double> stage;      // staging for AoS <-> SoA field transfers

@@ -245,7 +245,8 @@ __device__ __forceinline__ void st4(double *p, const double *v) {
 template <class Real, int MODE, int NC, int P, int NB>
 __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mask, Real *__restrict__ w, int N,
                                                   int *sync, u64 *__restrict__ xfer, unsigned epoch,
-                                                  unsigned cepoch, long long maxSpin, int R) {
+                                                  unsigned cepoch, long long maxSpin, int R, int ncc,
+                                                  long long xstride) {
     static_assert(P % 4 == 0 && P <= 32, "a chunk is whole quads");
     // every component of the launch has stopped iterating (the same word for
     // every CTA, written by an earlier kernel): nothing to do
@@ -274,12 +275,25 @@ __global__ void __launch_bounds__(256, 1) k_systolic(SkewT<Real> g, unsigned mas
     if (threadIdx.x < 16) { kBack[threadIdx.x] = 0; jProg[threadIdx.x] = 0; }
     if (r == 0 && threadIdx.x == 0) s_grp = atomicAdd(sync + SYNC_WORK, 1);
     cluster.sync();
-    const int grp = *cluster.map_shared_rank(&s_grp, 0);
+    // ncc > 1 (one-component kernels only): the launch sweeps ncc components
+    // side by side; ticket t is plane group t / ncc of component t % ncc, so
+    // every component's groups are taken in dependency order
+    const int ticket = *cluster.map_shared_rank(&s_grp, 0);
+    const int comp = ticket % ncc;
+    const int grp = ticket / ncc;
+    if (ncc > 1) {
+        g.rS += (long long)comp * g.nSkew;
+        g.wS += (long long)comp * g.nSkew;
+        if (w) w += (long long)comp * N;
+        if (g.w64) g.w64 += (long long)comp * N;
+        xfer += (long long)comp * xstride;
+        mask = (mask >> comp) & 1u;
+    }
     const int nGroups = (g.nz + CS - 1) / CS;
     const int T = g.T;
     const int gi = (MODE == 1) ? nGroups - 1 - grp : grp;
     const int k = (MODE == 1) ? gi * CS + (CS - 1 - r) : gi * CS + r;
-    const bool exists = grp < nGroups && k >= 0 && k < g.nz;
+    const bool exists = grp < nGroups && k >= 0 && k < g.nz && mask != 0u;
     if (exists) {
         const int jb = (MODE == 1) ? nJB - 1 - jo : jo;
         const int lf = (MODE == 1) ? 31 - lane : lane;   // the lane's entry column in the forward layout
@@ -680,7 +694,7 @@ __global__ void k_skew_to32(SkewView g, SkewView32 h) {
 namespace {
 
 template <class Real, int MODE, int NC, int P, int NB = 3>
-void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
+void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS, int ncc = 1) {
     StructMesh &s = ctx->mesh.sm;
     const int R = ring_depth<Real, MODE, NC, P, NB>(g.nJB, g.T, ctx->sweepRing > 0 ? ctx->sweepRing : kMaxRing);
     const size_t shm = sweep_smem_bytes<Real, MODE, NC, P, NB>(g.nJB, R);
@@ -719,8 +733,8 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
     const int nGroups = (g.nz + CS - 1) / CS;
     // tagged hand-off between clusters: (boundaries) x blocks x steps x lanes x words
     const size_t words = (size_t)std::max(1, nGroups - 1) * g.nJB * g.T * 32 * NC * Words<Real>::W;
-    if (s.xfer.n < words) {
-        s.xfer.alloc(words);
+    if (s.xfer.n < words * ncc) {
+        s.xfer.alloc(words * ncc);
         s.xfer.zero(ctx->stream);
     }
     if (++s.epoch == 0) s.epoch = 1;   // 0 marks a cleared word
@@ -733,7 +747,7 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
         --ctx->stallTest;
     }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(nGroups * CS);
+    cfg.gridDim = dim3(nGroups * CS * ncc);
     cfg.blockDim = dim3(32 * g.nJB);
     cfg.dynamicSmemBytes = shm;
     cfg.stream = ctx->stream;
@@ -745,7 +759,7 @@ void launch_one(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int C
     cfg.attrs = at;
     cfg.numAttrs = 1;
     RT_CUDA(cudaLaunchKernelEx(&cfg, k_systolic<Real, MODE, NC, P, NB>, g, mask, w, ctx->mesh.N, s.sync.p, s.xfer.p,
-                               s.epoch, cepoch, ctx->waitLimit, R));
+                               s.epoch, cepoch, ctx->waitLimit, R, ncc, (long long)words));
 }
 
 // Schedules of the one-component sweeps (the pressure solve): chunk size P
@@ -771,13 +785,13 @@ bool tune_fits_any(int k, int nJB) {
     }
 }
 template <class Real, int MODE>
-void launch_tuned(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS, int k) {
+void launch_tuned(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS, int k, int ncc = 1) {
     switch (k) {
-    case 0: launch_one<Real, MODE, 1, kTuneP[0], kTuneNB[0]>(ctx, g, mask, w, CS); break;
-    case 1: launch_one<Real, MODE, 1, kTuneP[1], kTuneNB[1]>(ctx, g, mask, w, CS); break;
-    case 2: launch_one<Real, MODE, 1, kTuneP[2], kTuneNB[2]>(ctx, g, mask, w, CS); break;
-    case 3: launch_one<Real, MODE, 1, kTuneP[3], kTuneNB[3]>(ctx, g, mask, w, CS); break;
-    default: launch_one<Real, MODE, 1, kTuneP[4], kTuneNB[4]>(ctx, g, mask, w, CS); break;
+    case 0: launch_one<Real, MODE, 1, kTuneP[0], kTuneNB[0]>(ctx, g, mask, w, CS, ncc); break;
+    case 1: launch_one<Real, MODE, 1, kTuneP[1], kTuneNB[1]>(ctx, g, mask, w, CS, ncc); break;
+    case 2: launch_one<Real, MODE, 1, kTuneP[2], kTuneNB[2]>(ctx, g, mask, w, CS, ncc); break;
+    case 3: launch_one<Real, MODE, 1, kTuneP[3], kTuneNB[3]>(ctx, g, mask, w, CS, ncc); break;
+    default: launch_one<Real, MODE, 1, kTuneP[4], kTuneNB[4]>(ctx, g, mask, w, CS, ncc); break;
     }
 }
 
@@ -785,19 +799,20 @@ void launch_tuned(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int
 // component), else chunks of 8 (one component) or 4 steps with three staging
 // buffers, else 4 steps with two; false when none fits
 template <class Real, int MODE, int NC>
-bool launch_fit(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS) {
+bool launch_fit(rt_ctx *ctx, const SkewT<Real> &g, unsigned mask, Real *w, int CS, int ncc = 1) {
     if constexpr (NC == 1 && MODE != 2) {
         const int k = ctx->mesh.sm.tune[sizeof(Real) == 4 ? 1 : 0];
         if (k >= 0 && tune_fits_any<Real, MODE>(k, g.nJB)) {
-            launch_tuned<Real, MODE>(ctx, g, mask, w, CS, k);
+            launch_tuned<Real, MODE>(ctx, g, mask, w, CS, k, ncc);
             return true;
         }
     }
     if constexpr (NC == 1) {
         if (sweep_smem_bytes<Real, MODE, NC, 8>(g.nJB) <= kMaxSmem) {
-            launch_one<Real, MODE, NC, 8>(ctx, g, mask, w, CS);
+            launch_one<Real, MODE, NC, 8>(ctx, g, mask, w, CS, ncc);
             return true;
         }
+        if (ncc > 1) return false;
     }
     if (sweep_smem_bytes<Real, MODE, NC, 4>(g.nJB) <= kMaxSmem) {
         launch_one<Real, MODE, NC, 4>(ctx, g, mask, w, CS);
@@ -829,10 +844,18 @@ void launch_mode(rt_ctx *ctx, const SkewT<Real> &g, int nc, unsigned mask, Real 
         // the group counter restarts; the error flag stays until skew_check reads it
         RT_CUDA(cudaMemsetAsync(s.sync.p + SYNC_WORK, 0, sizeof(int), ctx->stream));
         bool ok = false;
-        if (n == 1) ok = launch_fit<Real, MODE, 1>(ctx, h, mc, wc, CS);
-        else if constexpr (MODE != 2) {
-            if (n == 3) ok = launch_fit<Real, MODE, 3>(ctx, h, mc, wc, CS);
-            else if constexpr (sizeof(Real) == 4) ok = launch_fit<Real, MODE, 6>(ctx, h, mc, wc, CS);
+        if (n == 1) {
+            ok = launch_fit<Real, MODE, 1>(ctx, h, mc, wc, CS);
+        } else if (n <= 3 && ctx->sweepComponents == 1) {
+            // the components side by side: one-component sweeps, one launch
+            const int ncc = 32 - __builtin_clz(mc);
+            ok = launch_fit<Real, MODE, 1>(ctx, h, mc, wc, CS, ncc);
+        }
+        if constexpr (MODE != 2) {
+            if (!ok && n == 3) ok = launch_fit<Real, MODE, 3>(ctx, h, mc, wc, CS);
+            else if (!ok && n == 6) {
+                if constexpr (sizeof(Real) == 4) ok = launch_fit<Real, MODE, 6>(ctx, h, mc, wc, CS);
+            }
         }
         if (ok) launch_count(ctx, 2);
         return ok;

@@ -505,6 +505,34 @@ def test_systolic_sweeps_headline_structure(ctx, solver, pre, asym, nc, tune):
     assert np.array_equal(out[abi.SWEEP_LEVELS][0], out[abi.SWEEP_SYSTOLIC][0])
 
 
+@pytest.mark.parametrize("nc,asym", [(3, 3.0), (2, 1.0)])
+def test_sweep_components_side_by_side_equal_lane_by_lane(ctx, nc, asym):
+    """A multi-component solve's sweeps with the components side by side
+    (one one-component sweep each, in one launch: RT_OPT_SWEEP_COMPONENTS 1)
+    and carried lane by lane in one sweep (0): the same bits and iteration
+    counts, on the headline's sweep structure (four j-blocks, three clusters
+    of planes)."""
+    mesh = contraction_mesh(nx_up=20, nx_down=20, ny_in=50, ny_out=25, nz=34, L_up=4.0, L_down=4.0)
+    rng = np.random.default_rng(25)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=asym)
+    b = rng.normal(size=(nc, mesh.nCells)) * mesh.V
+    ctl = SolverControl("PBiCGStab", "DILU", 1e-10, 0.0, 0, 300)
+    ctx.upload_mesh(mesh)
+    out = {}
+    try:
+        ctx.set_sweep(abi.SWEEP_SYSTOLIC)
+        for mode in (0, 1):
+            ctx.set_option(abi.RT_OPT_SWEEP_COMPONENTS, mode)
+            x = np.zeros((nc, mesh.nCells))
+            perf = ctx.ldu_solve(diag, upper, lower, b, x, ctl)
+            out[mode] = (x, [p.nIterations for p in perf])
+    finally:
+        ctx.set_option(abi.RT_OPT_SWEEP_COMPONENTS, 1)
+        ctx.set_sweep(abi.SWEEP_AUTO)
+    assert out[0][1] == out[1][1] and min(out[1][1]) > 3
+    assert np.array_equal(out[0][0], out[1][0])
+
+
 def multimode_case(base, n_extra=2):
     """A multiMode model of three different modes on the base case:
     Oldroyd-B (the base model), Giesekus lambda 0.2 alpha 0.15 and linear PTT
