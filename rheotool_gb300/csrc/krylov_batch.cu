@@ -646,7 +646,7 @@ __host__ __device__ constexpr int case_stage_bytes() {   // one warp's staging a
                : s2d::stage_bytes<V, 1, NC, P, NB>();
 }
 constexpr int kU = 4;                            // cells per thread whose loads are issued together
-constexpr int kUA = 2;                           // the same for q = A p
+constexpr int kUA = 4;                           // the same for q = A p
 constexpr int kSlots = 4;                        // ELL width of the 2-D cases
 
 // the bounded-wait error flag as one value for the whole CTA (another CTA
@@ -657,6 +657,23 @@ __device__ bool case_error(const int *err) {
     if (threadIdx.x == 0) sv = *(volatile const int *)err;
     __syncthreads();
     return sv != 0;
+}
+
+// the matrix coefficient of each ELL slot of the case's cells, in the
+// vector type (0 past a row's end), so that A x reads it beside the slot's
+// neighbour instead of through the face; ends with a barrier
+template <class V>
+__device__ void case_ell_coefficients(const BEll &e, int N, int c0, int c1, const V *__restrict__ u32,
+                                      const V *__restrict__ l32, V *__restrict__ aEll) {
+    for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) {
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s) {
+            const int nb = s < e.nSlots ? __ldg(e.nbr + (size_t)s * N + c) : -1;
+            const int f = s < e.nSlots ? __ldg(e.face + (size_t)s * N + c) : -1;
+            aEll[(size_t)s * N + c] = nb >= 0 ? V(nb > c ? u32[f] : l32[f]) : V(0);
+        }
+    }
+    __syncthreads();
 }
 
 // the CTA's sum, valid in every thread
@@ -681,7 +698,8 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
                                                               V *__restrict__ r, V *__restrict__ w,
                                                               V *__restrict__ p, V *__restrict__ q,
                                                               V *__restrict__ x, const int *__restrict__ order,
-                                                              int *err, long long maxSpin, int cap) {
+                                                              V *__restrict__ aEll, int *err, long long maxSpin,
+                                                              int cap) {
     using Acc = typename AccOf<V>::type;
     __shared__ s2d::u64 ring[8 * s2d::kRJ * s2d::W<V>::n];
     __shared__ int sProg[32];
@@ -689,6 +707,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
     const int cb = order[blockIdx.x], sg = cb * 8, tid = threadIdx.x, nt = blockDim.x, N = t.N;
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
+    case_ell_coefficients(e, N, c0, c1, u32, l32, aEll);
     for (int it = 0; it < cap; ++it) {
         __syncthreads();
         if (!S.active[sg]) break;
@@ -756,12 +775,12 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
         __syncthreads();
         // ---- q = A p (the vector type's matrix copy; FP32: differences form); p.q
         // two rounds of independent loads per kUA cells: the ELL slots (the
-        // rows end in -1 padding, which adds nothing) with the cells' own
-        // values, then the neighbours' values and the face coefficients
+        // rows end in -1 padding, which adds nothing) with their coefficients
+        // and the cells' own values, then the neighbours' values
         Acc aq;
         for (int ci = c0 + tid; ci < c1; ci += kUA * nt) {
-            int nb[kUA][kSlots], fc[kUA][kSlots];
-            V pc[kUA], dc[kUA];
+            int nb[kUA][kSlots];
+            V cf[kUA][kSlots], pc[kUA], dc[kUA];
 #pragma unroll
             for (int k = 0; k < kUA; ++k) {
                 const int c = ci + k * nt;
@@ -770,25 +789,16 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
                 for (int s = 0; s < kSlots; ++s) {
                     const bool sl = in && s < e.nSlots;
                     nb[k][s] = sl ? __ldg(e.nbr + (size_t)s * N + c) : -1;
-                    fc[k][s] = sl ? __ldg(e.face + (size_t)s * N + c) : -1;
+                    cf[k][s] = sl ? aEll[(size_t)s * N + c] : V(0);
                 }
                 pc[k] = in ? p[c] : V(0);
                 dc[k] = in ? V(d32[c]) : V(0);
             }
-            V cf[kUA][kSlots], pn[kUA][kSlots];
+            V pn[kUA][kSlots];
 #pragma unroll
-            for (int k = 0; k < kUA; ++k) {
-                const int c = ci + k * nt;
+            for (int k = 0; k < kUA; ++k)
 #pragma unroll
-                for (int s = 0; s < kSlots; ++s) {
-                    cf[k][s] = V(0);
-                    pn[k][s] = V(0);
-                    if (nb[k][s] >= 0) {
-                        cf[k][s] = V(nb[k][s] > c ? u32[fc[k][s]] : l32[fc[k][s]]);
-                        pn[k][s] = p[nb[k][s]];
-                    }
-                }
-            }
+                for (int s = 0; s < kSlots; ++s) pn[k][s] = nb[k][s] >= 0 ? p[nb[k][s]] : V(0);
 #pragma unroll
             for (int k = 0; k < kUA; ++k) {
                 const int c = ci + k * nt;
@@ -920,22 +930,19 @@ __device__ void case_totals(double (&v)[n]) {
 // y = A x for the components in m (FP32: differences form over the row sums)
 template <class V>
 __device__ void case_amul(const BEll &e, int N, int c0, int c1, unsigned m, const V *__restrict__ d32,
-                          const V *__restrict__ u32, const V *__restrict__ l32, const V *__restrict__ x,
-                          V *__restrict__ y) {
+                          const V *__restrict__ aEll, const V *__restrict__ x, V *__restrict__ y) {
     const int nt = blockDim.x;
 #pragma unroll 2
     for (int c = c0 + (int)threadIdx.x; c < c1; c += nt) {
-        int nb[kSlots], fc[kSlots];
+        int nb[kSlots];
+        V cf[kSlots];
 #pragma unroll
         for (int s = 0; s < kSlots; ++s) {
             const bool sl = s < e.nSlots;
             nb[s] = sl ? __ldg(e.nbr + (size_t)s * N + c) : -1;
-            fc[s] = sl ? __ldg(e.face + (size_t)s * N + c) : -1;
+            cf[s] = sl ? aEll[(size_t)s * N + c] : V(0);
         }
         const V dc = d32[c];
-        V cf[kSlots];
-#pragma unroll
-        for (int s = 0; s < kSlots; ++s) cf[s] = nb[s] >= 0 ? V(nb[s] > c ? u32[fc[s]] : l32[fc[s]]) : V(0);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             if (!((m >> k) & 1u)) continue;
@@ -1010,7 +1017,8 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                                                               V *__restrict__ Ay, V *__restrict__ sv,
                                                               V *__restrict__ z, V *__restrict__ tt,
                                                               V *__restrict__ x, const int *__restrict__ order,
-                                                              int *err, long long maxSpin, int cap) {
+                                                              V *__restrict__ aEll, int *err, long long maxSpin,
+                                                              int cap) {
     using Acc = typename AccOf<V>::type;
     __shared__ s2d::u64 ring[16 * s2d::kRJ * s2d::W<V>::n];   // two halves of the CTA, 8 j-blocks each
     extern __shared__ __align__(16) unsigned char stageSmem[];   // 16 warps' sweep staging
@@ -1023,6 +1031,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
     const int cb = order[blockIdx.x], tid = threadIdx.x, nt = blockDim.x, N = t.N;
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const int s0 = cb * 8;
+    case_ell_coefficients(e, N, c0, c1, u32, l32, aEll);
     // the segments (components) selected by a predicate on their state
     auto seg_mask = [&](auto pred) {
         unsigned mm = 0;
@@ -1117,7 +1126,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
         case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg, stageSmem);
         if (case_error(err)) break;
-        case_amul(e, N, c0, c1, vm, d32, u32, l32, y, Ay);
+        case_amul(e, N, c0, c1, vm, d32, aEll, y, Ay);
         __syncthreads();
         {
             Acc a[3];
@@ -1225,7 +1234,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- z = M^-1 s, tt = A z, omega = tt.s / tt.tt
         case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg, stageSmem);
         if (case_error(err)) break;
-        case_amul(e, N, c0, c1, vm, d32, u32, l32, z, tt);
+        case_amul(e, N, c0, c1, vm, d32, aEll, z, tt);
         __syncthreads();
         {
             Acc a[6];
@@ -1341,7 +1350,7 @@ struct BSolver {
     int N, F, nSeg;
     int mixed = sizeof(V) == 4;   // FP32 vectors: residual replacement
     unsigned vm;
-    V *vec, *d32, *u32, *l32, *rD;
+    V *vec, *d32, *u32, *l32, *rD, *aEll;
     double *rD64, *partial, *res;
 
     BSolver(rt_ctx *c, const SolveArgs &args) : ctx(c), a(args), bt(c->mesh.batch) {
@@ -1364,13 +1373,14 @@ struct BSolver {
         S.count = si + (size_t)6 * nSeg;
         // vectors: 9 x 6N of V, then the matrix copy and rD
         const size_t V6 = 6 * (size_t)N;
-        const size_t bytes = sizeof(V) * (9 * V6 + 2 * (size_t)N + 2 * (size_t)F + 64);
+        const size_t bytes = sizeof(V) * (9 * V6 + 2 * (size_t)N + 2 * (size_t)F + (size_t)kSlots * N + 64);
         ctx->kws32.alloc((bytes + sizeof(float) - 1) / sizeof(float));
         vec = reinterpret_cast<V *>(ctx->kws32.p);
         d32 = vec + 9 * V6;
         rD = d32 + N;
         u32 = rD + N;
         l32 = u32 + F;
+        aEll = l32 + F;   // kSlots x N: the persistent solvers' per-slot coefficients
         ctx->kws.alloc(48 * (size_t)N + 2 * (size_t)N + 64);
         rD64 = ctx->kws.p + 48 * (size_t)N;
         partial = bt.bPartial.p;
@@ -1566,7 +1576,7 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
             k_b_pcg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
                                                               sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
                                                               sv.v(1), sv.v(2), sv.v(3), x, bt.caseOrder.p,
-                                                              bt.sErr.p, 1ll << 22, cap);
+                                                              sv.aEll, bt.sErr.p, 1ll << 22, cap);
             RT_CHECK_LAUNCH();
         }
         launch_count(ctx);
@@ -1586,7 +1596,7 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
             k_b_bicg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(
                 sv.t, sv.e, g, sv.S, sv.ctl, sv.vm, sv.mixed, sv.d32, sv.u32, sv.l32, a.diag, a.upper, a.lower,
                 a.source, a.psi, r, sv.v(1), sv.v(2), sv.v(3), sv.v(4), sv.v(5), sv.v(6), sv.v(7), x,
-                bt.caseOrder.p, bt.sErr.p, 1ll << 22, cap);
+                bt.caseOrder.p, sv.aEll, bt.sErr.p, 1ll << 22, cap);
             RT_CHECK_LAUNCH();
         }
         launch_count(ctx);
