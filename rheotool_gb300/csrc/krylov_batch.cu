@@ -927,6 +927,32 @@ __device__ void case_totals(double (&v)[n]) {
     __syncthreads();
 }
 
+// per component in m, the sum over the case's cells of a b (kU cells a
+// round, their loads issued together)
+template <class V, class Acc>
+__device__ void case_dots(int c0, int c1, int N, unsigned m, const V *__restrict__ a, const V *__restrict__ b,
+                          Acc (&acc)[3]) {
+    const int nt = blockDim.x;
+    for (int ci = c0 + (int)threadIdx.x; ci < c1; ci += kU * nt) {
+        V av[kU][3], bv[kU][3];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            const int c = ci + j * nt;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const bool in = c < c1 && ((m >> q) & 1u);
+                av[j][q] = in ? a[(size_t)q * N + c] : V(0);
+                bv[j][q] = in ? b[(size_t)q * N + c] : V(0);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j)
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                if (ci + j * nt < c1 && ((m >> q) & 1u)) acc_dot(acc[q], av[j][q], bv[j][q]);
+    }
+}
+
 // y = A x for the components in m (FP32: differences form over the row sums)
 template <class V>
 __device__ void case_amul(const BEll &e, int N, int c0, int c1, unsigned m, const V *__restrict__ d32,
@@ -1074,11 +1100,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- r0r = r0.r; beta, singular stops
         {
             Acc a[3];
-#pragma unroll 4
-            for (int c = c0 + tid; c < c1; c += nt)
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-                    if ((act >> k) & 1u) acc_dot(a[k], r0[(size_t)k * N + c], r[(size_t)k * N + c]);
+            case_dots(c0, c1, N, act, r0, r, a);
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_bicg_r0r
@@ -1112,15 +1134,31 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                 beta[k] = V(S.beta[sg]);
                 omega[k] = V(S.omega[sg]);
             }
-#pragma unroll 4
-            for (int c = c0 + tid; c < c1; c += nt)
+            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
+                V rv[kU][3], av[kU][3], pv[kU][3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (!((live >> k) & 1u)) continue;
-                    const size_t i = (size_t)k * N + c;
-                    if (restart[k]) p[i] = r[i];
-                    else p[i] = fma(beta[k], fma(-omega[k], Ay[i], p[i]), r[i]);
+                for (int j = 0; j < kU; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const bool in = c < c1 && ((live >> k) & 1u);
+                        const size_t i = (size_t)k * N + c;
+                        rv[j][k] = in ? r[i] : V(0);
+                        av[j][k] = (in && !restart[k]) ? Ay[i] : V(0);
+                        pv[j][k] = (in && !restart[k]) ? p[i] : V(0);
+                    }
                 }
+#pragma unroll
+                for (int j = 0; j < kU; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        if (c >= c1 || !((live >> k) & 1u)) continue;
+                        p[(size_t)k * N + c] =
+                            restart[k] ? rv[j][k] : fma(beta[k], fma(-omega[k], av[j][k], pv[j][k]), rv[j][k]);
+                    }
+                }
+            }
         }
         __syncthreads();
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
@@ -1130,11 +1168,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         __syncthreads();
         {
             Acc a[3];
-#pragma unroll 4
-            for (int c = c0 + tid; c < c1; c += nt)
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-                    if ((live >> k) & 1u) acc_dot(a[k], r0[(size_t)k * N + c], Ay[(size_t)k * N + c]);
+            case_dots(c0, c1, N, live, r0, Ay, a);
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0)   // k_b_bicg_alpha
@@ -1152,16 +1186,30 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
             V alpha[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) alpha[k] = V(S.alpha[s0 + k]);
-#pragma unroll 4
-            for (int c = c0 + tid; c < c1; c += nt)
+            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
+                V av[kU][3], rv[kU][3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (!((live >> k) & 1u)) continue;
-                    const size_t i = (size_t)k * N + c;
-                    const V sk = fma(-alpha[k], Ay[i], r[i]);
-                    sv[i] = sk;
-                    acc_add(a[k], fabs(sk));
+                for (int j = 0; j < kU; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const bool in = c < c1 && ((live >> k) & 1u);
+                        av[j][k] = in ? Ay[(size_t)k * N + c] : V(0);
+                        rv[j][k] = in ? r[(size_t)k * N + c] : V(0);
+                    }
                 }
+#pragma unroll
+                for (int j = 0; j < kU; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        if (c >= c1 || !((live >> k) & 1u)) continue;
+                        const V sk = fma(-alpha[k], av[j][k], rv[j][k]);
+                        sv[(size_t)k * N + c] = sk;
+                        acc_add(a[k], fabs(sk));
+                    }
+                }
+            }
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_bicg_half
@@ -1239,15 +1287,27 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         {
             Acc a[6];
             const unsigned on = seg_mask([&](int sg) { return S.active[sg] != 0; });
-#pragma unroll 4
-            for (int c = c0 + tid; c < c1; c += nt)
+            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
+                V tv[kU][3], svv[kU][3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (!((on >> k) & 1u)) continue;
-                    const V tk = tt[(size_t)k * N + c];
-                    acc_dot(a[k], tk, tk);
-                    acc_dot(a[3 + k], tk, sv[(size_t)k * N + c]);
+                for (int j = 0; j < kU; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const bool in = c < c1 && ((on >> k) & 1u);
+                        tv[j][k] = in ? tt[(size_t)k * N + c] : V(0);
+                        svv[j][k] = in ? sv[(size_t)k * N + c] : V(0);
+                    }
                 }
+#pragma unroll
+                for (int j = 0; j < kU; ++j)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        if (ci + j * nt >= c1 || !((on >> k) & 1u)) continue;
+                        acc_dot(a[k], tv[j][k], tv[j][k]);
+                        acc_dot(a[3 + k], tv[j][k], svv[j][k]);
+                    }
+            }
             double v[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) v[i] = acc_value(a[i]);
@@ -1267,17 +1327,37 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                 alpha[k] = V(S.alpha[s0 + k]);
                 omega[k] = V(S.omega[s0 + k]);
             }
-#pragma unroll 4
-            for (int c = c0 + tid; c < c1; c += nt)
+            constexpr int kU2 = 2;
+            for (int ci = c0 + tid; ci < c1; ci += kU2 * nt) {
+                V yv[kU2][3], zv[kU2][3], xv[kU2][3], tv[kU2][3], svv[kU2][3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (!((full >> k) & 1u)) continue;
-                    const size_t i = (size_t)k * N + c;
-                    x[i] = fma(alpha[k], y[i], fma(omega[k], z[i], x[i]));
-                    const V rv = fma(-omega[k], tt[i], sv[i]);
-                    r[i] = rv;
-                    acc_add(a[k], fabs(rv));
+                for (int j = 0; j < kU2; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const bool in = c < c1 && ((full >> k) & 1u);
+                        const size_t i = (size_t)k * N + c;
+                        yv[j][k] = in ? y[i] : V(0);
+                        zv[j][k] = in ? z[i] : V(0);
+                        xv[j][k] = in ? x[i] : V(0);
+                        tv[j][k] = in ? tt[i] : V(0);
+                        svv[j][k] = in ? sv[i] : V(0);
+                    }
                 }
+#pragma unroll
+                for (int j = 0; j < kU2; ++j) {
+                    const int c = ci + j * nt;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        if (c >= c1 || !((full >> k) & 1u)) continue;
+                        const size_t i = (size_t)k * N + c;
+                        x[i] = fma(alpha[k], yv[j][k], fma(omega[k], zv[j][k], xv[j][k]));
+                        const V rv = fma(-omega[k], tv[j][k], svv[j][k]);
+                        r[i] = rv;
+                        acc_add(a[k], fabs(rv));
+                    }
+                }
+            }
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_iter_fin (skipHalf)
