@@ -636,9 +636,10 @@ constexpr int kCaseP = sizeof(V) == 4 ? 8 : 4;   // sweep chunk of the pressure 
 // (cp.async) NB - 1 chunks ahead; the momentum solve runs two components'
 // sweeps side by side (16 warps), with shorter chunks
 constexpr int kCaseNB = 4;
-constexpr int kBicgP = 4;
 template <class V>
-constexpr int kBicgNB = sizeof(V) == 4 ? 4 : 2;
+constexpr int kBicgP = sizeof(V) == 4 ? 8 : 4;
+template <class V>
+constexpr int kBicgNB = sizeof(V) == 4 ? 3 : 2;
 template <class V, int NC, int P, int NB>
 __host__ __device__ constexpr int case_stage_bytes() {   // one warp's staging area, the larger of the two sweeps
     return s2d::stage_bytes<V, 0, NC, P, NB>() > s2d::stage_bytes<V, 1, NC, P, NB>()
@@ -994,11 +995,27 @@ __device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m,
                                   V *__restrict__ w, int *err, long long maxSpin, s2d::u64 *ring, int *sProg,
                                   unsigned char *stage) {
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
-    for (long long i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
-        const int c = __ldg(g.cellOf + i);
+    const int nt = blockDim.x;
+    for (long long i0 = e0 + threadIdx.x; i0 < e1; i0 += (long long)kU * nt) {
+        int cc[kU];
+        V v[kU][3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-            if ((m >> k) & 1u) g.rS[(long long)k * g.nSkew + i] = c >= 0 ? r[(size_t)k * N + c] : V(0);
+        for (int j = 0; j < kU; ++j) {
+            const long long i = i0 + (long long)j * nt;
+            cc[j] = i < e1 ? __ldg(g.cellOf + i) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) v[j][k] = (cc[j] >= 0 && ((m >> k) & 1u)) ? r[(size_t)k * N + cc[j]] : V(0);
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            const long long i = i0 + (long long)j * nt;
+            if (i >= e1) continue;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if ((m >> k) & 1u) g.rS[(long long)k * g.nSkew + i] = v[j][k];
+        }
     }
     int comps[3], nComp = 0;
 #pragma unroll
@@ -1017,12 +1034,12 @@ __device__ void case_precondition(const Skew2D<V> &g, int cb, int N, unsigned m,
             __syncthreads();
             if (k >= 0) {
                 s2d::u64 *rg = ring + grp * 8 * s2d::kRJ * s2d::W<V>::n;
-                unsigned char *sg = stage + (size_t)grp * 8 * case_stage_bytes<V, 1, kBicgP, kBicgNB<V>>();
+                unsigned char *sg = stage + (size_t)grp * 8 * case_stage_bytes<V, 1, kBicgP<V>, kBicgNB<V>>();
                 if (mode == 0)
-                    sweep2d_cta<V, 0, 1, kBicgP, true, s2d::kRJ, kBicgNB<V>>(gk, cb, 1u, nullptr, N, err, maxSpin, rg,
+                    sweep2d_cta<V, 0, 1, kBicgP<V>, true, s2d::kRJ, kBicgNB<V>>(gk, cb, 1u, nullptr, N, err, maxSpin, rg,
                                                                              sProg + 8 * grp, 8 * grp, sg);
                 else
-                    sweep2d_cta<V, 1, 1, kBicgP, true, s2d::kRJ, kBicgNB<V>>(gk, cb, 1u, w + (size_t)k * N, N, err,
+                    sweep2d_cta<V, 1, 1, kBicgP<V>, true, s2d::kRJ, kBicgNB<V>>(gk, cb, 1u, w + (size_t)k * N, N, err,
                                                                              maxSpin, rg, sProg + 8 * grp, 8 * grp, sg);
             }
             __syncthreads();
@@ -1671,7 +1688,7 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         else g = sweep2d_view64(ctx);
         {
             ProfScope ps(ctx, "batch_bicgstab_persistent");
-            const int shm = 16 * case_stage_bytes<V, 1, kBicgP, kBicgNB<V>>();
+            const int shm = 16 * case_stage_bytes<V, 1, kBicgP<V>, kBicgNB<V>>();
             RT_CUDA(cudaFuncSetAttribute(k_b_bicg_case<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
             k_b_bicg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(
                 sv.t, sv.e, g, sv.S, sv.ctl, sv.vm, sv.mixed, sv.d32, sv.u32, sv.l32, a.diag, a.upper, a.lower,
