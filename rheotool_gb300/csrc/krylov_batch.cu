@@ -650,6 +650,31 @@ constexpr int kU = 4;                            // cells per thread whose loads
 constexpr int kUA = 4;                           // the same for q = A p
 constexpr int kSlots = 4;                        // ELL width of the 2-D cases
 
+// 16-byte packs of a vector: four FP32 or two FP64 values, one load or store
+template <class V> struct Pack;
+template <> struct Pack<float> { using T = float4; static constexpr int n = 4; };
+template <> struct Pack<double> { using T = double2; static constexpr int n = 2; };
+__device__ __forceinline__ void ldp(const float *p, float (&v)[4]) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ldp(const double *p, double (&v)[2]) {
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    v[0] = a.x; v[1] = a.y;
+}
+__device__ __forceinline__ void stp(float *p, const float (&v)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void stp(double *p, const double (&v)[2]) {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+}
+// the pack-aligned part [a, b) of the cell range [c0, c1) (the vectors are
+// 128-byte aligned); the rest, at most a pack at each end, goes cell by cell
+__device__ __forceinline__ void pack_bounds(int c0, int c1, int n, int &a, int &b) {
+    a = min(c1, (c0 + n - 1) / n * n);
+    b = max(a, c1 / n * n);
+}
+
 // the bounded-wait error flag as one value for the whole CTA (another CTA
 // may set it at any time: every thread must take the same branch)
 __device__ bool case_error(const int *err) {
@@ -740,12 +765,30 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
         }
         if (case_error(err)) break;
         // ---- rho = w.r (and w.q_old in the flexible form)
+        constexpr int PN = Pack<V>::n;
+        int pa, pb;
+        pack_bounds(c0, c1, PN, pa, pb);
         Acc a0, a1;
-#pragma unroll 4
-        for (int c = c0 + tid; c < c1; c += nt) {
-            const V wc = w[c];
-            acc_dot(a0, wc, r[c]);
-            if (mixed) acc_dot(a1, wc, q[c]);
+        {
+            auto one = [&](int c) {
+                const V wc = w[c];
+                acc_dot(a0, wc, r[c]);
+                if (mixed) acc_dot(a1, wc, q[c]);
+            };
+            for (int c = c0 + tid; c < pa; c += nt) one(c);
+            for (int c = pb + tid; c < c1; c += nt) one(c);
+#pragma unroll 2
+            for (int g = pa + tid * PN; g < pb; g += nt * PN) {
+                V wv[PN], rv[PN], qv[PN];
+                ldp(w + g, wv);
+                ldp(r + g, rv);
+                if (mixed) ldp(q + g, qv);
+#pragma unroll
+                for (int j = 0; j < PN; ++j) {
+                    acc_dot(a0, wv[j], rv[j]);
+                    if (mixed) acc_dot(a1, wv[j], qv[j]);
+                }
+            }
         }
         const double rho = case_total(acc_value(a0));
         const double wq = mixed ? case_total(acc_value(a1)) : 0.0;
@@ -760,17 +803,17 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
         {
             const bool first = S.iter[sg] == 0;
             const V beta = V(S.beta[sg]);
-            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
-                V wv[kU], pv[kU];
+            auto one = [&](int c) { p[c] = first ? w[c] : fma(beta, p[c], w[c]); };
+            for (int c = c0 + tid; c < pa; c += nt) one(c);
+            for (int c = pb + tid; c < c1; c += nt) one(c);
+#pragma unroll 2
+            for (int g = pa + tid * PN; g < pb; g += nt * PN) {
+                V wv[PN], pv[PN];
+                ldp(w + g, wv);
+                if (!first) ldp(p + g, pv);
 #pragma unroll
-                for (int k = 0; k < kU; ++k) {
-                    const int c = ci + k * nt;
-                    wv[k] = c < c1 ? w[c] : V(0);
-                    pv[k] = (c < c1 && !first) ? p[c] : V(0);
-                }
-#pragma unroll
-                for (int k = 0; k < kU; ++k)
-                    if (ci + k * nt < c1) p[ci + k * nt] = first ? wv[k] : fma(beta, pv[k], wv[k]);
+                for (int j = 0; j < PN; ++j) pv[j] = first ? wv[j] : fma(beta, pv[j], wv[j]);
+                stp(p + g, pv);
             }
         }
         __syncthreads();
@@ -827,28 +870,35 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
         {
             const bool sing = S.sing[sg] != 0;
             const V alpha = V(S.alpha[sg]);
-            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
-                V rv[kU], xv[kU], pv[kU], qv[kU];
-#pragma unroll
-                for (int k = 0; k < kU; ++k) {
-                    const int c = ci + k * nt;
-                    const bool in = c < c1;
-                    rv[k] = in ? r[c] : V(0);
-                    xv[k] = (in && !sing) ? x[c] : V(0);
-                    pv[k] = (in && !sing) ? p[c] : V(0);
-                    qv[k] = (in && !sing) ? q[c] : V(0);
+            auto one = [&](int c) {
+                V rr = r[c];
+                if (!sing) {
+                    x[c] = fma(alpha, p[c], x[c]);
+                    rr = fma(-alpha, q[c], rr);
+                    r[c] = rr;
                 }
+                acc_add(ar, fabs(rr));
+            };
+            for (int c = c0 + tid; c < pa; c += nt) one(c);
+            for (int c = pb + tid; c < c1; c += nt) one(c);
+#pragma unroll 2
+            for (int g = pa + tid * PN; g < pb; g += nt * PN) {
+                V rv[PN], xv[PN], pv[PN], qv[PN];
+                ldp(r + g, rv);
+                if (!sing) {
+                    ldp(x + g, xv);
+                    ldp(p + g, pv);
+                    ldp(q + g, qv);
 #pragma unroll
-                for (int k = 0; k < kU; ++k) {
-                    const int c = ci + k * nt;
-                    if (c >= c1) continue;
-                    if (!sing) {
-                        x[c] = fma(alpha, pv[k], xv[k]);
-                        rv[k] = fma(-alpha, qv[k], rv[k]);
-                        r[c] = rv[k];
+                    for (int j = 0; j < PN; ++j) {
+                        xv[j] = fma(alpha, pv[j], xv[j]);
+                        rv[j] = fma(-alpha, qv[j], rv[j]);
                     }
-                    acc_add(ar, fabs(rv[k]));
+                    stp(x + g, xv);
+                    stp(r + g, rv);
                 }
+#pragma unroll
+                for (int j = 0; j < PN; ++j) acc_add(ar, fabs(rv[j]));
             }
         }
         const double rs = case_total(acc_value(ar));
@@ -1469,7 +1519,7 @@ struct BSolver {
         for (int i = 0; i < 6; ++i) *islots[i] = si + (size_t)i * nSeg;
         S.count = si + (size_t)6 * nSeg;
         // vectors: 9 x 6N of V, then the matrix copy and rD
-        const size_t V6 = 6 * (size_t)N;
+        const size_t V6 = vstride(N);   // 6N rounded up: every vector 128-byte aligned
         const size_t bytes = sizeof(V) * (9 * V6 + 2 * (size_t)N + 2 * (size_t)F + (size_t)kSlots * N + 64);
         ctx->kws32.alloc((bytes + sizeof(float) - 1) / sizeof(float));
         vec = reinterpret_cast<V *>(ctx->kws32.p);
@@ -1483,7 +1533,8 @@ struct BSolver {
         partial = bt.bPartial.p;
         res = bt.bRes.p;
     }
-    V *v(int i) const { return vec + (size_t)i * 6 * N; }
+    static size_t vstride(int n) { return (6 * (size_t)n + 31) / 32 * 32; }
+    V *v(int i) const { return vec + (size_t)i * vstride(N); }
     int gridSeg() const { return (nSeg + 255) / 256; }
 
     void fin(int nSlots, unsigned mask) {
