@@ -12,6 +12,14 @@
 // CUDA graph and replayed, and the host only polls the number of segments
 // still iterating every few iterations.
 //
+// Structured 2-D cases in batches that fill the GPU take a second form
+// (RT_OPT_BATCH_PERSISTENT): one persistent CTA per case runs every
+// iteration of its case's pressure PCG (k_b_pcg_case) or momentum BiCGStab
+// (k_b_bicg_case) in one launch, with the same scalar decisions, the case's
+// sweeps inside the CTA (sweep2d_cta.cuh, chunks staged by cp.async) and its
+// reductions as one pass of the CTA (FP32 vectors summed as float-float
+// pairs).
+//
 // Precision: the vectors are FP32 (RT_PREC_MIXED) or FP64, the scalars and
 // reductions FP64.  As in the single-case mixed solvers, the solution is
 // psi (FP64) + x (a correction in the vector type), folded into psi with the
