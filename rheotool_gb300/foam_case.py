@@ -16,6 +16,14 @@
   boundary conditions (fixedValue, zeroGradient, linearExtrapolation; empty
   and cyclic patches are part of the mesh).
 
+A multiMode model (``type multiMode; models ( M1 { ... } M2 { ... } );``,
+multiMode.C:69-91) reads each mode's ``0/thetaM1``, ``0/tauM1`` ... (the
+fields rheoTool names after the mode's keyword) instead of ``0/theta`` and
+``0/tau``; the modes must share rho, the stabilization and the boundary
+conditions of theta and tau (the library sums their divTau as one).
+``run_case`` writes ``tau`` (the modes' sum) and every mode's ``theta<K>``
+and ``tau<K>``.
+
 What the library does not implement is refused with a clear message unless
 ``substitute=True`` is given, in which case each substitution is recorded in
 ``loaded.substitutions``: rheoTool's external sparse solvers (``solverType eigenSolver``,
@@ -138,6 +146,7 @@ class LoadedCase:
     endTime: float
     writeInterval: float
     substitutions: List[str] = field(default_factory=list)
+    mode_names: List[str] = field(default_factory=list)   # multiMode: the modes' keywords
 
 
 # the keywords each model's constructor looks up without a default, beyond
@@ -203,6 +212,40 @@ def _limiter(schemes: Dict[str, Any], key: str) -> str:
     raise CaseError(f"fvSchemes {key}: {v!r} is not implemented (GaussDefCmpw <limiter> or Gauss upwind)")
 
 
+def read_mode_entries(par: Dict[str, Any]) -> Tuple[List[str], List[Model]]:
+    """The modes of a ``parameters`` dictionary: ([], [model]) for a single
+    model; for ``type multiMode`` the modes' keywords and models in list
+    order (multiMode.C:69-91), which must share rho and the stabilization
+    (the library takes one divTau of the summed tau with the summed
+    viscosities)."""
+    if par.get("type") != "multiMode":
+        return [], [read_model(par)]
+    raw = par.get("models")
+    if not isinstance(raw, str) or not raw.strip().startswith("("):
+        raise CaseError("keyword models is undefined in the multiMode parameters")
+    entries = [(k, d) for k, d in parse_dict(raw.strip()[1:-1]).items() if isinstance(d, dict)]
+    if not entries:
+        raise CaseError("multiMode: the models list is empty")
+    models = [read_model(d) for _, d in entries]
+    for m in models[1:]:
+        if m.rho != models[0].rho or m.stabilization != models[0].stabilization:
+            raise CaseError("multiMode: the modes must share rho and stabilization (their divTau is summed as one)")
+    return [k for k, _ in entries], models
+
+
+def _bc_signature(bf: Dict[str, Any], mesh) -> List[Tuple[str, str, Any]]:
+    """The boundary conditions of a field file, patch by patch (kind and value)."""
+    out = []
+    for p in mesh.patches:
+        e = lookup_pattern(bf, p.name)
+        if e is None:
+            out.append((p.name, "", None))
+            continue
+        v = None if e["value"] is None else tuple(np.asarray(e["value"], dtype=np.float64).ravel().tolist())
+        out.append((p.name, e["type"], v))
+    return out
+
+
 def read_model(par: Dict[str, Any]) -> Model:
     """The Model of a constitutiveProperties ``parameters`` dictionary, with
     the keywords each model's constructor reads and its FatalErrors as
@@ -265,7 +308,8 @@ def load_case(case_dir: str, substitute: bool = False,
             raise CaseError(msg + " (pass substitute=True to run it anyway)")
         subs.append(msg)
     cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
-    model = read_model(cp.get("parameters", cp))
+    mode_names, models = read_mode_entries(cp.get("parameters", cp))
+    model = models[0]
 
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))
     solvers = sol.get("solvers", {})
@@ -296,12 +340,28 @@ def load_case(case_dir: str, substitute: bool = False,
     ncomp = {"U": 3, "p": 1, "theta": 6, "tau": 6}
     kinds = {"fixedValue", "zeroGradient", "linearExtrapolation"}
     bcs: Dict[str, Dict[str, Tuple[str, Any]]] = {p.name: {} for p in mesh.patches}
-    f = Fields.zeros(mesh)
+    f = Fields.zeros(mesh, len(models))
     for name, nc in ncomp.items():
-        path = os.path.join(case_dir, "0", name)
-        internal, bf = foam_io.read_field(path, n_internal=mesh.nCells)
-        arr = np.asarray(internal, dtype=np.float64).reshape(mesh.nCells, nc) if nc > 1 else np.asarray(internal)
-        getattr(f, name)[:] = arr
+        # multiMode: theta and tau per mode (theta<K>, tau<K>); the boundary
+        # conditions are the first mode's, the others' must be the same
+        files = [name + k for k in mode_names] if (mode_names and name in ("theta", "tau")) else [name]
+        bf = None
+        for i, fname in enumerate(files):
+            internal, bfi = foam_io.read_field(os.path.join(case_dir, "0", fname), n_internal=mesh.nCells)
+            arr = np.asarray(internal, dtype=np.float64).reshape(mesh.nCells, nc) if nc > 1 else np.asarray(internal)
+            if len(files) > 1:
+                getattr(f.modes[i], name)[:] = arr
+                if name == "theta" and i == 0:
+                    f.theta[:] = arr
+                if name == "tau":
+                    f.tau[:] += arr
+            else:
+                getattr(f, name)[:] = arr
+            if bf is None:
+                bf = bfi
+            elif _bc_signature(bfi, mesh) != _bc_signature(bf, mesh):
+                raise CaseError(f"0/{fname}: multiMode modes with different boundary conditions are not "
+                                f"implemented (0/{files[0]} gives the others')")
         for p in mesh.patches:
             e = lookup_pattern(bf, p.name)
             if e is None:
@@ -337,23 +397,29 @@ def load_case(case_dir: str, substitute: bool = False,
                 pRefCell=int(scalar(simple.get("pRefCell", "0"))), pRefValue=scalar(simple.get("pRefValue", "0")),
                 precision=precision, name=os.path.basename(os.path.abspath(case_dir)),
                 nInIter=int(scalar(simple.get("nInIter", "1"))), nNonOrthCorr=nNonOrth, ddt=ddt, ddtPsi=ddtPsi)
+    case.moreModes = list(models[1:])
     # boundary values of the initial state (fixed values; the rest from the cells)
+    holders = [f] + list(f.modes)
     for p in mesh.patches:
         sl = slice(p.start, p.start + p.size)
         for name, nc in ncomp.items():
             kind, val = case.bcs[p.name][name]
-            bnd = getattr(f, name + "b")
-            cells = getattr(f, name)[mesh.bCell[sl]]
-            if kind == "fixedValue" and val is not None:
-                v = np.asarray(val(mesh.bCf[sl]) if callable(val) else val, dtype=np.float64)
-                bnd[sl] = np.broadcast_to(v.reshape(-1, nc) if nc > 1 else v.reshape(-1), bnd[sl].shape)
-            else:
-                bnd[sl] = cells
+            for h in (holders if name in ("theta", "tau") else [f]):
+                bnd = getattr(h, name + "b")
+                cells = getattr(h, name)[mesh.bCell[sl]]
+                if kind == "fixedValue" and val is not None:
+                    v = np.asarray(val(mesh.bCf[sl]) if callable(val) else val, dtype=np.float64)
+                    bnd[sl] = np.broadcast_to(v.reshape(-1, nc) if nc > 1 else v.reshape(-1), bnd[sl].shape)
+                else:
+                    bnd[sl] = cells
+    if f.modes:   # the summed tau on the boundary too (multiMode::tau())
+        f.taub[:] = sum(m.taub for m in f.modes)
     # initial face fluxes from U (createPhi)
     Uf = mesh.w[:, None] * (f.U[mesh.owner] - f.U[mesh.neighbour]) + f.U[mesh.neighbour]
     f.phi[:] = (mesh.Sf * Uf).sum(1)
     f.phib[:] = (mesh.bSf * f.Ub).sum(1)
-    return LoadedCase(case, f, scalar(ctrl.get("endTime", "1")), scalar(ctrl.get("writeInterval", "1")), subs)
+    return LoadedCase(case, f, scalar(ctrl.get("endTime", "1")), scalar(ctrl.get("writeInterval", "1")), subs,
+                      mode_names)
 
 
 def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, **load_kw) -> LoadedCase:
@@ -373,7 +439,15 @@ def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, **load
             ctx.step(k)
             done += k
             t = done * dt
-            foam_io.write_fields(os.path.join(case_dir, f"{t:g}"), case.mesh, ctx.fields())
+            tdir = os.path.join(case_dir, f"{t:g}")
+            got = ctx.fields()
+            foam_io.write_fields(tdir, case.mesh, got)
+            for k, m in zip(lc.mode_names, got.modes):   # multiMode: every mode's theta and tau
+                for name, a, b, dims in (("theta", m.theta, m.thetab, "[0 0 0 0 0 0 0]"),
+                                         ("tau", m.tau, m.taub, "[1 -1 -2 0 0 0 0]")):
+                    bnd = {p.name: ("calculated", b[p.start:p.start + p.size]) for p in case.mesh.patches}
+                    foam_io.write_field(os.path.join(tdir, name + k), "volSymmTensorField", name + k, a, bnd, dims,
+                                        os.path.basename(tdir), 12)
     return lc
 
 

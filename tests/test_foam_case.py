@@ -179,3 +179,64 @@ def test_model_keywords_as_the_reference_reads_them(tmp_path):
     _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; destructionFunctionType quadratic;")
     with pytest.raises(CaseError, match="quadratic"):
         load_case(root)
+
+
+MULTIMODE_PARAMETERS = (
+    "parameters\n{\n    type multiMode;\n    models\n    (\n"
+    "        M1\n        {\n            type Oldroyd-BLog;\n            rho rho [1 -3 0 0 0 0 0] 0.01;\n"
+    "            etaS etaS [1 -1 -1 0 0 0 0] 0.25;\n            etaP etaP [1 -1 -1 0 0 0 0] 0.3;\n"
+    "            lambda lambda [0 0 1 0 0 0 0] 0.5;\n            stabilization coupling;\n        }\n"
+    "        M2\n        {\n            type GiesekusLog;\n            rho rho [1 -3 0 0 0 0 0] 0.01;\n"
+    "            etaS etaS [1 -1 -1 0 0 0 0] 0.25;\n            etaP etaP [1 -1 -1 0 0 0 0] 0.2;\n"
+    "            lambda lambda [0 0 1 0 0 0 0] 0.1;\n            alpha alpha [0 0 0 0 0 0 0] 0.2;\n"
+    "            stabilization coupling;\n        }\n    );\n}\n")
+
+
+def multimode_cavity_dir(root, n=8, **kw):
+    """The cavity case directory with a two-mode multiMode model laid out as
+    rheoTool's multiMode tutorials are (Channel2D_VE/multiMode: 0/thetaM1,
+    0/tauM1, 0/thetaM2, 0/tauM2 instead of 0/theta and 0/tau)."""
+    _cavity_dir(root, n=n, **kw)
+    _write(os.path.join(root, "constant", "constitutiveProperties"), "dictionary", "constitutiveProperties",
+           MULTIMODE_PARAMETERS)
+    for name in ("theta", "tau"):
+        src = os.path.join(root, "0", name)
+        text = open(src).read()
+        for k in ("M1", "M2"):
+            with open(src + k, "w") as fh:
+                fh.write(text.replace(f"object      {name};", f"object      {name}{k};")
+                         .replace(f"object {name};", f"object {name}{k};"))
+        os.remove(src)
+    return root
+
+
+def test_multimode_case_directory_loads_like_the_builder(tmp_path):
+    """A multiMode case directory: the modes in list order with their own
+    fields, stepping as the same model built directly."""
+    import copy
+    from oracle.pyoracle import Oracle
+    root = multimode_cavity_dir(str(tmp_path / "mm"))
+    lc = load_case(root)
+    c = lc.case
+    assert lc.mode_names == ["M1", "M2"] and [m.type for m in c.models] == ["Oldroyd-BLog", "GiesekusLog"]
+    assert len(lc.fields.modes) == 2 and not lc.substitutions
+    ref = cavity_case(8)
+    ref.model = copy.copy(c.models[0])
+    ref.moreModes = [copy.copy(c.models[1])]
+    a, b = Oracle(ref), Oracle(c, lc.fields.copy())
+    a.step(3)
+    b.step(3)
+    for name in ("U", "p", "phi", "tau"):
+        x, y = getattr(b.f, name), getattr(a.f, name)
+        assert np.linalg.norm(x - y) <= 1e-11 * max(np.linalg.norm(y), 1e-300), name
+    for mx, my in zip(b.f.modes, a.f.modes):
+        assert np.linalg.norm(mx.theta - my.theta) <= 1e-11 * max(np.linalg.norm(my.theta), 1e-300)
+
+
+def test_multimode_modes_must_share_rho_and_stabilization(tmp_path):
+    root = multimode_cavity_dir(str(tmp_path / "mm2"))
+    path = os.path.join(root, "constant", "constitutiveProperties")
+    _write(path, "dictionary", "constitutiveProperties",
+           MULTIMODE_PARAMETERS.replace("stabilization coupling;\n        }\n    );", "stabilization BSD;\n        }\n    );"))
+    with pytest.raises(CaseError, match="share rho and stabilization"):
+        load_case(root)

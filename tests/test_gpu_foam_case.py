@@ -58,3 +58,27 @@ def test_case_directory_runs_on_the_gpu_as_written(tmp_path):
             got = np.asarray(internal, dtype=np.float64).reshape(getattr(ref.f, name).shape)
             # written with 12 significant digits (writePrecision 12 of the tutorials)
             assert rel(got, getattr(ref.f, name)) < max(TOL_STEP, 1e-11), (t, name, rel(got, getattr(ref.f, name)))
+
+
+def test_multimode_case_directory_runs_on_the_gpu(tmp_path):
+    """A multiMode case directory (two modes, each with its own 0/theta<K>
+    and 0/tau<K>) run by run_case on the GPU: the summed tau and every mode's
+    theta and tau written at the write times equal the oracle's."""
+    from oracle.pyoracle import Oracle
+    from test_foam_case import multimode_cavity_dir
+    root = multimode_cavity_dir(str(tmp_path / "mm"), n=12)
+    lc = load_case(root)
+    assert lc.mode_names == ["M1", "M2"]
+    run_case(root)                             # 3 steps, fields written at 0.001, 0.002, 0.003
+    ref = Oracle(lc.case, lc.fields.copy())
+    mesh = lc.case.mesh
+    for t in ("0.001", "0.002", "0.003"):
+        ref.step(1)
+        d = os.path.join(root, t)
+        checks = [("U", 3, ref.f.U), ("p", 1, ref.f.p), ("tau", 6, ref.f.tau)]
+        for i, k in enumerate(lc.mode_names):
+            checks += [("theta" + k, 6, ref.f.modes[i].theta), ("tau" + k, 6, ref.f.modes[i].tau)]
+        for name, nc, want in checks:
+            internal, _ = foam_io.read_field(os.path.join(d, name), n_internal=mesh.nCells)
+            got = np.asarray(internal, dtype=np.float64).reshape(want.shape)
+            assert rel(got, want) < max(TOL_STEP, 1e-11), (t, name, rel(got, want))
