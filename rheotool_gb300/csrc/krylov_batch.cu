@@ -986,29 +986,21 @@ __device__ void case_totals(double (&v)[n]) {
     __syncthreads();
 }
 
-// per component in m, the sum over the case's cells of a b (kU cells a
-// round, their loads issued together)
-template <class V, class Acc>
-__device__ void case_dots(int c0, int c1, int N, unsigned m, const V *__restrict__ a, const V *__restrict__ b,
-                          Acc (&acc)[3]) {
-    const int nt = blockDim.x;
-    for (int ci = c0 + (int)threadIdx.x; ci < c1; ci += kU * nt) {
-        V av[kU][3], bv[kU][3];
+// For every component k in m (up to three): one(k, i) for the cells of
+// [k N + c0, k N + c1) outside its 16-byte-aligned part, pack(k, i) for each
+// pack of PN cells starting at i inside it
+template <int PN, class One, class PackFn>
+__device__ __forceinline__ void comp_packs(int c0, int c1, int N, unsigned m, One one, PackFn pack) {
+    const long long nt = blockDim.x;
 #pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            const int c = ci + j * nt;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const bool in = c < c1 && ((m >> q) & 1u);
-                av[j][q] = in ? a[(size_t)q * N + c] : V(0);
-                bv[j][q] = in ? b[(size_t)q * N + c] : V(0);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < kU; ++j)
-#pragma unroll
-            for (int q = 0; q < 3; ++q)
-                if (ci + j * nt < c1 && ((m >> q) & 1u)) acc_dot(acc[q], av[j][q], bv[j][q]);
+    for (int k = 0; k < 3; ++k) {
+        if (!((m >> k) & 1u)) continue;
+        const long long lo = (long long)k * N + c0, hi = (long long)k * N + c1;
+        const long long a = min(hi, (lo + PN - 1) / PN * PN), b = max(a, hi / PN * PN);
+        for (long long i = lo + threadIdx.x; i < a; i += nt) one(k, i);
+        for (long long i = b + threadIdx.x; i < hi; i += nt) one(k, i);
+#pragma unroll 2
+        for (long long i = a + (long long)threadIdx.x * PN; i < b; i += nt * PN) pack(k, i);
     }
 }
 
@@ -1121,6 +1113,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                                                               V *__restrict__ aEll, int *err, long long maxSpin,
                                                               int cap) {
     using Acc = typename AccOf<V>::type;
+    constexpr int PN = Pack<V>::n;
     __shared__ s2d::u64 ring[16 * s2d::kRJ * s2d::W<V>::n];   // two halves of the CTA, 8 j-blocks each
     extern __shared__ __align__(16) unsigned char stageSmem[];   // 16 warps' sweep staging
     __shared__ int sProg[32];
@@ -1175,7 +1168,14 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         // ---- r0r = r0.r; beta, singular stops
         {
             Acc a[3];
-            case_dots(c0, c1, N, act, r0, r, a);
+            comp_packs<PN>(c0, c1, N, act, [&](int k, long long i) { acc_dot(a[k], r0[i], r[i]); },
+                           [&](int k, long long i) {
+                               V x[PN], y[PN];
+                               ldp(r0 + i, x);
+                               ldp(r + i, y);
+#pragma unroll
+                               for (int j = 0; j < PN; ++j) acc_dot(a[k], x[j], y[j]);
+                           });
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_bicg_r0r
@@ -1209,31 +1209,21 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                 beta[k] = V(S.beta[sg]);
                 omega[k] = V(S.omega[sg]);
             }
-            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
-                V rv[kU][3], av[kU][3], pv[kU][3];
+            comp_packs<PN>(c0, c1, N, live,
+                           [&](int k, long long i) {
+                               p[i] = restart[k] ? r[i] : fma(beta[k], fma(-omega[k], Ay[i], p[i]), r[i]);
+                           },
+                           [&](int k, long long i) {
+                               V rv[PN], av[PN], pv[PN];
+                               ldp(r + i, rv);
+                               if (!restart[k]) {
+                                   ldp(Ay + i, av);
+                                   ldp(p + i, pv);
 #pragma unroll
-                for (int j = 0; j < kU; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const bool in = c < c1 && ((live >> k) & 1u);
-                        const size_t i = (size_t)k * N + c;
-                        rv[j][k] = in ? r[i] : V(0);
-                        av[j][k] = (in && !restart[k]) ? Ay[i] : V(0);
-                        pv[j][k] = (in && !restart[k]) ? p[i] : V(0);
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < kU; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        if (c >= c1 || !((live >> k) & 1u)) continue;
-                        p[(size_t)k * N + c] =
-                            restart[k] ? rv[j][k] : fma(beta[k], fma(-omega[k], av[j][k], pv[j][k]), rv[j][k]);
-                    }
-                }
-            }
+                                   for (int j = 0; j < PN; ++j) rv[j] = fma(beta[k], fma(-omega[k], av[j], pv[j]), rv[j]);
+                               }
+                               stp(p + i, rv);
+                           });
         }
         __syncthreads();
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
@@ -1243,7 +1233,14 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         __syncthreads();
         {
             Acc a[3];
-            case_dots(c0, c1, N, live, r0, Ay, a);
+            comp_packs<PN>(c0, c1, N, live, [&](int k, long long i) { acc_dot(a[k], r0[i], Ay[i]); },
+                           [&](int k, long long i) {
+                               V x[PN], y[PN];
+                               ldp(r0 + i, x);
+                               ldp(Ay + i, y);
+#pragma unroll
+                               for (int j = 0; j < PN; ++j) acc_dot(a[k], x[j], y[j]);
+                           });
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0)   // k_b_bicg_alpha
@@ -1261,30 +1258,23 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
             V alpha[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) alpha[k] = V(S.alpha[s0 + k]);
-            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
-                V av[kU][3], rv[kU][3];
+            comp_packs<PN>(c0, c1, N, live,
+                           [&](int k, long long i) {
+                               const V sk = fma(-alpha[k], Ay[i], r[i]);
+                               sv[i] = sk;
+                               acc_add(a[k], fabs(sk));
+                           },
+                           [&](int k, long long i) {
+                               V av[PN], rv[PN];
+                               ldp(Ay + i, av);
+                               ldp(r + i, rv);
 #pragma unroll
-                for (int j = 0; j < kU; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const bool in = c < c1 && ((live >> k) & 1u);
-                        av[j][k] = in ? Ay[(size_t)k * N + c] : V(0);
-                        rv[j][k] = in ? r[(size_t)k * N + c] : V(0);
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < kU; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        if (c >= c1 || !((live >> k) & 1u)) continue;
-                        const V sk = fma(-alpha[k], av[j][k], rv[j][k]);
-                        sv[(size_t)k * N + c] = sk;
-                        acc_add(a[k], fabs(sk));
-                    }
-                }
-            }
+                               for (int j = 0; j < PN; ++j) {
+                                   rv[j] = fma(-alpha[k], av[j], rv[j]);
+                                   acc_add(a[k], fabs(rv[j]));
+                               }
+                               stp(sv + i, rv);
+                           });
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_bicg_half
@@ -1362,27 +1352,22 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         {
             Acc a[6];
             const unsigned on = seg_mask([&](int sg) { return S.active[sg] != 0; });
-            for (int ci = c0 + tid; ci < c1; ci += kU * nt) {
-                V tv[kU][3], svv[kU][3];
+            comp_packs<PN>(c0, c1, N, on,
+                           [&](int k, long long i) {
+                               const V tk = tt[i];
+                               acc_dot(a[k], tk, tk);
+                               acc_dot(a[3 + k], tk, sv[i]);
+                           },
+                           [&](int k, long long i) {
+                               V tv[PN], svv[PN];
+                               ldp(tt + i, tv);
+                               ldp(sv + i, svv);
 #pragma unroll
-                for (int j = 0; j < kU; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const bool in = c < c1 && ((on >> k) & 1u);
-                        tv[j][k] = in ? tt[(size_t)k * N + c] : V(0);
-                        svv[j][k] = in ? sv[(size_t)k * N + c] : V(0);
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < kU; ++j)
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        if (ci + j * nt >= c1 || !((on >> k) & 1u)) continue;
-                        acc_dot(a[k], tv[j][k], tv[j][k]);
-                        acc_dot(a[3 + k], tv[j][k], svv[j][k]);
-                    }
-            }
+                               for (int j = 0; j < PN; ++j) {
+                                   acc_dot(a[k], tv[j], tv[j]);
+                                   acc_dot(a[3 + k], tv[j], svv[j]);
+                               }
+                           });
             double v[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) v[i] = acc_value(a[i]);
@@ -1402,37 +1387,29 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                 alpha[k] = V(S.alpha[s0 + k]);
                 omega[k] = V(S.omega[s0 + k]);
             }
-            constexpr int kU2 = 2;
-            for (int ci = c0 + tid; ci < c1; ci += kU2 * nt) {
-                V yv[kU2][3], zv[kU2][3], xv[kU2][3], tv[kU2][3], svv[kU2][3];
+            comp_packs<PN>(c0, c1, N, full,
+                           [&](int k, long long i) {
+                               x[i] = fma(alpha[k], y[i], fma(omega[k], z[i], x[i]));
+                               const V rv = fma(-omega[k], tt[i], sv[i]);
+                               r[i] = rv;
+                               acc_add(a[k], fabs(rv));
+                           },
+                           [&](int k, long long i) {
+                               V yv[PN], zv[PN], xv[PN], tv[PN], svv[PN];
+                               ldp(y + i, yv);
+                               ldp(z + i, zv);
+                               ldp(x + i, xv);
+                               ldp(tt + i, tv);
+                               ldp(sv + i, svv);
 #pragma unroll
-                for (int j = 0; j < kU2; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const bool in = c < c1 && ((full >> k) & 1u);
-                        const size_t i = (size_t)k * N + c;
-                        yv[j][k] = in ? y[i] : V(0);
-                        zv[j][k] = in ? z[i] : V(0);
-                        xv[j][k] = in ? x[i] : V(0);
-                        tv[j][k] = in ? tt[i] : V(0);
-                        svv[j][k] = in ? sv[i] : V(0);
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < kU2; ++j) {
-                    const int c = ci + j * nt;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        if (c >= c1 || !((full >> k) & 1u)) continue;
-                        const size_t i = (size_t)k * N + c;
-                        x[i] = fma(alpha[k], yv[j][k], fma(omega[k], zv[j][k], xv[j][k]));
-                        const V rv = fma(-omega[k], tv[j][k], svv[j][k]);
-                        r[i] = rv;
-                        acc_add(a[k], fabs(rv));
-                    }
-                }
-            }
+                               for (int j = 0; j < PN; ++j) {
+                                   xv[j] = fma(alpha[k], yv[j], fma(omega[k], zv[j], xv[j]));
+                                   svv[j] = fma(-omega[k], tv[j], svv[j]);
+                                   acc_add(a[k], fabs(svv[j]));
+                               }
+                               stp(x + i, xv);
+                               stp(r + i, svv);
+                           });
             double v[3] = {acc_value(a[0]), acc_value(a[1]), acc_value(a[2])};
             case_totals(v);
             if (tid == 0) {   // k_b_iter_fin (skipHalf)
