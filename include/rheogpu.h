@@ -287,13 +287,16 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * clears it. */
 #define RT_OPT_STALL_TEST 9
 /* RT_OPT_MIXED_PRECOND: the preconditioner of the mixed form's pressure
- * solve (DIC selected).  0: DIC with the exact triangular sweeps (FP32
- * systolic sweeps on structured meshes).  -1: DIC of the two-colour
- * (red-black) ordering of a structured mesh, applied in two parallel,
- * bandwidth-bound passes (more iterations, each far cheaper).  k = 1 .. 64:
- * DIC applied by k Jacobi sweeps per triangular factor (a truncated Neumann
- * series of the same factorisation; Anzt, Chow and Dongarra 2015).  The FP64
- * plain form always uses the exact sweeps. */
+ * solve (DIC selected).  -2 (default): on structured meshes without coupled
+ * faces, an aggregation multigrid V-cycle (FP32, red-black Gauss-Seidel
+ * smoothing, Galerkin coarse operators of 2 x 2 x 2 aggregates; elsewhere
+ * the exact DIC).  0: DIC with the exact triangular sweeps (FP32 systolic
+ * sweeps on structured meshes).  -1: DIC of the two-colour (red-black)
+ * ordering of a structured mesh, applied in two parallel, bandwidth-bound
+ * passes.  k = 1 .. 64: DIC applied by k Jacobi sweeps per triangular factor
+ * (a truncated Neumann series of the same factorisation; Anzt, Chow and
+ * Dongarra 2015).  Every choice stops on the same FP64 residual test.  The
+ * FP64 plain form always uses the exact sweeps. */
 #define RT_OPT_MIXED_PRECOND 10
 /* RT_OPT_BATCH_PERSISTENT: the batched form's pressure and momentum solves
  * on structured 2-D cases (up to 256 rows) as one persistent CTA per case,

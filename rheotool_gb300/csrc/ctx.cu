@@ -407,6 +407,15 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
         upload_vec(ctx, cellOf, s.cellOf);
         upload_vec(ctx, lo, s.faceLo);
         upload_vec(ctx, hi, s.faceHi);
+        {   // the box maps (the multigrid preconditioner's level 0)
+            std::vector<int> boxOf(N);
+            for (size_t b = 0; b < at.size(); ++b)
+                if (at[b] >= 0) boxOf[at[b]] = (int)b;
+            upload_vec(ctx, at, s.cellAt);
+            upload_vec(ctx, boxOf, s.boxOf);
+            s.mgDims.clear();
+            s.mgGraph.reset();
+        }
         RT_REQUIRE(s.nJB <= 8 && skew_fits(s.nJB), RT_EINVAL, "structured sweeps need ny <= 256");
         // planes (CTAs) per thread-block cluster: 16 (the non-portable maximum;
         // fewer hand-offs through global memory), 8 where 16 cannot be scheduled
@@ -472,9 +481,9 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
             ctx->mixedTighten = std::pow(10.0, -(double)value);
             return RT_OK;
         case RT_OPT_MIXED_PRECOND:
-            RT_REQUIRE(value >= -1 && value <= 64, RT_EINVAL,
-                       "RT_OPT_MIXED_PRECOND: 0 exact sweeps, -1 red-black DIC, 1 .. 64 Jacobi sweeps per "
-                       "triangular factor");
+            RT_REQUIRE(value >= -2 && value <= 64, RT_EINVAL,
+                       "RT_OPT_MIXED_PRECOND: 0 exact sweeps, -1 red-black DIC, -2 aggregation multigrid, 1 .. 64 "
+                       "Jacobi sweeps per triangular factor");
             ctx->mixedJacobi = (int)value;
             return RT_OK;
         case RT_OPT_SWEEP_COMPONENTS:

@@ -1567,7 +1567,10 @@ struct Mixed : Solver {
             launch_count(ctx);
         }
         const int pre = a.ctl.preconditioner;
-        if (redblack()) {
+        if (multigrid()) {
+            ProfScope ps(ctx, "mg_setup", (double)N * (8.0 + 3.0 * 8.0 + 16.0 + 12.0));
+            mg_prepare(ctx, a.diag, a.lower);
+        } else if (redblack()) {
             if (ctx->jac.n < 2 * (size_t)N) ctx->jac.alloc(2 * (size_t)N);
             ProfScope ps(ctx, "dilu_rD", (double)N * (8.0 + 8.0 + 4.0) + (double)ctx->mesh.F * 16.0);
             k_rb_rd<<<nblocks(N), RT_BLOCK, 0, st>>>(pe, ctx->mesh.colour.p, a.diag, a.upper, a.lower, ctx->jac.p);
@@ -1609,7 +1612,7 @@ struct Mixed : Solver {
     // the way in and out; otherwise through the FP32 vectors r32, w32)
     // the red-black DIC of the pressure solve (one component, structured mesh)
     bool redblack() const {
-        return ctx->mixedJacobi < 0 && a.nc == 1 && a.ctl.preconditioner == RT_PRECOND_DIC &&
+        return ctx->mixedJacobi == -1 && a.nc == 1 && a.ctl.preconditioner == RT_PRECOND_DIC &&
                ctx->mesh.colour.p != nullptr && !ctx->mesh.hasCoupled;
     }
     void redblack_apply(const double *r, double *w, const unsigned *dmask) {
@@ -1622,6 +1625,12 @@ struct Mixed : Solver {
         k_rb_red<<<nblocks(N), RT_BLOCK, 0, st>>>(pe, ctx->mesh.colour.p, rDi, u32, l32, r, wb, w, dmask);
         RT_CHECK_LAUNCH();
         launch_count(ctx, 2);
+    }
+
+    // the aggregation multigrid V-cycle of the pressure solve (one component,
+    // a symmetric matrix, structured mesh without coupled faces)
+    bool multigrid() const {
+        return ctx->mixedJacobi == -2 && a.nc == 1 && a.ctl.preconditioner == RT_PRECOND_DIC && mg_available(ctx);
     }
 
     // the Jacobi-swept DIC/DILU of the pressure solve (one component)
@@ -1664,6 +1673,13 @@ struct Mixed : Solver {
 
     void precondition32d(unsigned mask, const double *r, double *w, float *r32, float *w32,
                          const unsigned *dmask = nullptr) {
+        if (multigrid()) {
+            // level 0: the FP64 residual and result, five passes of the 7-point
+            // stencil (7 x 4 bytes and x, b); the coarser levels add about 1/7
+            ProfScope ps(ctx, "mg_vcycle32", (double)N * (16.0 + 5.0 * 36.0) * 8.0 / 7.0);
+            mg_apply(ctx, r, w, dmask);
+            return;
+        }
         if (redblack()) {
             redblack_apply(r, w, dmask);
             return;

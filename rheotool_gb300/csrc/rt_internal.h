@@ -12,6 +12,7 @@
 #include <memory>
 #include <string>
 #include <utility>
+#include <array>
 #include <vector>
 
 #include "../../include/rheogpu.h"
@@ -113,6 +114,22 @@ struct SkewT {
 using SkewView = SkewT<double>;
 using SkewView32 = SkewT<float>;
 
+// a captured multigrid V-cycle and the buffers it was captured with
+struct MgGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void *r = nullptr, *w = nullptr, *dm = nullptr;
+    int launches = 0;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        r = w = dm = nullptr;
+    }
+    MgGraph() = default;
+    MgGraph(const MgGraph &) = delete;
+    MgGraph &operator=(const MgGraph &) = delete;
+    ~MgGraph() { reset(); }
+};
+
 struct StructMesh {
     bool on = false;
     int nx = 0, ny = 0, nz = 0, nJB = 0, T = 0;
@@ -127,6 +144,12 @@ struct StructMesh {
     float tuneMs[2] = {0, 0};  // its time per application
     DBuf<double> data;         // 12 + 6 + 6 arrays of nSkew doubles
     bool pendingCheck = false;
+    // the box: the cell of each box position (-1 outside the mesh) and the
+    // box position of each cell; the multigrid hierarchy's boxes and arrays
+    DBuf<int> cellAt, boxOf;
+    std::vector<std::array<int, 3>> mgDims;
+    DBuf<float> mgData;
+    MgGraph mgGraph;   // the captured V-cycle
 
     SkewView view() {
         SkewView v;
@@ -433,7 +456,7 @@ struct rt_ctx {
     // RT_PREC_MIXED pressure solve: DIC applied by this many Jacobi sweeps per
     // triangular factor (0: the exact sweeps); FP32 premultiplied split-ELL
     // coefficients and three FP32 vectors
-    int mixedJacobi = 0;
+    int mixedJacobi = -2;   // RT_OPT_MIXED_PRECOND (default: the multigrid V-cycle)
     rt::DBuf<float> jac;
     // batched form: the pressure solve of structured 2-D cases as one
     // persistent CTA per case (RT_OPT_BATCH_PERSISTENT; 0: the per-iteration

@@ -27,6 +27,10 @@ pytestmark = pytest.mark.gpu
 
 TOL_MIXED = 1e-6
 
+# the library's default preconditioner of the mixed pressure solve (the
+# multigrid V-cycle on structured meshes)
+MIXED_PRECOND_DEFAULT = -2
+
 MESHES = {
     "cavity70": lambda: cavity_mesh(70),
     "contraction3d": lambda: contraction_mesh(12, 10, 30, 10, 6, 4.0, 4.0),
@@ -69,6 +73,8 @@ def _solve(ctx, mesh, diag, upper, lower, b, x0, ctl, precision, sweep):
 @pytest.mark.parametrize("mesh_name", sorted(MESHES))
 @pytest.mark.parametrize("sweep", [abi.SWEEP_LEVELS, abi.SWEEP_SYSTOLIC])
 def test_mixed_pcg_dic(ctx, mesh_name, sweep):
+    """The mixed pressure solve with the exact FP32 DIC sweeps
+    (RT_OPT_MIXED_PRECOND 0), level-scheduled and systolic."""
     from oracle.pyoracle import Oracle
     mesh = MESHES[mesh_name]()
     rng = np.random.default_rng(31)
@@ -76,7 +82,11 @@ def test_mixed_pcg_dic(ctx, mesh_name, sweep):
     b = rng.normal(size=mesh.nCells) * mesh.V
     x0 = rng.normal(size=mesh.nCells) * 0.1
     ctl = SolverControl("PCG", "DIC", 1e-10, 0.0, 0, 3000)
-    xg, perf = _solve(ctx, mesh, diag, upper, lower, b[None], x0, ctl, abi.RT_PREC_MIXED, sweep)
+    ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 0)
+    try:
+        xg, perf = _solve(ctx, mesh, diag, upper, lower, b[None], x0, ctl, abi.RT_PREC_MIXED, sweep)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, MIXED_PRECOND_DEFAULT)
     pg = perf[0]
     orc = Oracle(_case_for(mesh))
     xo = x0.copy()
@@ -233,7 +243,7 @@ def test_mixed_pcg_jacobi_dic(ctx, mesh_name, sweeps):
         ctx.set_option(abi.RT_OPT_MIXED_PRECOND, sweeps)
         xg, perf = _solve(ctx, mesh, diag, upper, lower, b[None], x0, ctl, abi.RT_PREC_MIXED, abi.SWEEP_AUTO)
     finally:
-        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 0)
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, MIXED_PRECOND_DEFAULT)
     pg = perf[0]
     xo = x0.copy()
     po = Oracle(_case_for(mesh)).ldu_solve(diag, upper, lower, b, xo, ctl)
@@ -250,4 +260,43 @@ def test_mixed_step_contraction3d_jacobi_dic(ctx):
         ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 6)
         _mixed_step_check(ctx, contraction_case(small_contraction()), 5)
     finally:
-        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 0)
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, MIXED_PRECOND_DEFAULT)
+
+
+@pytest.mark.parametrize("mesh_name", sorted(MESHES))
+def test_mixed_pcg_multigrid(ctx, mesh_name):
+    """RT_OPT_MIXED_PRECOND -2: the mixed pressure solve preconditioned by the
+    aggregation multigrid V-cycle (structured meshes; other meshes keep the
+    exact DIC) stops on the same FP64 residual test and gives the FP64
+    solution within the mixed bar."""
+    from oracle.pyoracle import Oracle
+    mesh = MESHES[mesh_name]()
+    rng = np.random.default_rng(35)
+    diag, upper, lower = laplacian_system(mesh, rng)
+    b = rng.normal(size=mesh.nCells) * mesh.V
+    x0 = rng.normal(size=mesh.nCells) * 0.1
+    ctl = SolverControl("PCG", "DIC", 1e-10, 0.0, 0, 5000)
+    ctx.upload_mesh(mesh)
+    try:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, -2)
+        xg, perf = _solve(ctx, mesh, diag, upper, lower, b[None], x0, ctl, abi.RT_PREC_MIXED, abi.SWEEP_AUTO)
+        # a second solve on the same buffers replays the captured V-cycle
+        xg2, perf2 = _solve(ctx, mesh, diag, upper, lower, b[None], x0, ctl, abi.RT_PREC_MIXED, abi.SWEEP_AUTO)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, MIXED_PRECOND_DEFAULT)
+    pg = perf[0]
+    xo = x0.copy()
+    po = Oracle(_case_for(mesh)).ldu_solve(diag, upper, lower, b, xo, ctl)
+    assert pg.converged and po.converged
+    assert foam_residual(mesh, diag, upper, lower, b, xg, x0) < ctl.tolerance
+    assert rel(xg, xo) < TOL_MIXED
+    assert np.array_equal(xg, xg2) and perf2[0].nIterations == pg.nIterations
+
+
+def test_mixed_step_contraction3d_multigrid(ctx):
+    """Full mixed steps with the multigrid-preconditioned pressure solve."""
+    try:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, -2)
+        _mixed_step_check(ctx, contraction_case(small_contraction()), 5)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND, MIXED_PRECOND_DEFAULT)
