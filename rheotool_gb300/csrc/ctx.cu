@@ -1068,6 +1068,25 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
                 maxJB = std::max(maxJB, sJB[c]);
             }
             std::vector<int> cellOf((size_t)nSkew, -1);
+            // the multigrid hierarchy of each case (the mixed pressure solve):
+            // its boxes down to at most kBatchMgCoarse cells, their offsets in
+            // one pool, and level 0's cell of each box position
+            std::vector<int> mgDims((size_t)n * kBatchMgLevels * 2, 0), mgNL(n, 0), mgCell;
+            std::vector<long long> mgOff((size_t)n * kBatchMgLevels, 0), mgCellOff(n, 0);
+            long long mgTotal = 0;
+            for (int c = 0; c < n; ++c) {
+                int nx = dims[3 * c], ny = dims[3 * c + 1];
+                for (int l = 0; l < kBatchMgLevels; ++l) {
+                    mgDims[((size_t)c * kBatchMgLevels + l) * 2] = nx;
+                    mgDims[((size_t)c * kBatchMgLevels + l) * 2 + 1] = ny;
+                    mgOff[(size_t)c * kBatchMgLevels + l] = mgTotal;
+                    mgTotal += 5 * (((long long)nx * ny + 3) / 4 * 4);
+                    mgNL[c] = l + 1;
+                    if ((long long)nx * ny <= kBatchMgCoarse) break;
+                    nx = (nx + 1) / 2;
+                    ny = (ny + 1) / 2;
+                }
+            }
             for (int c = 0; structured && c < n; ++c) {
                 const int nx = dims[3 * c], ny = dims[3 * c + 1];
                 std::vector<int> at((size_t)nx * ny, -1);
@@ -1098,6 +1117,8 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
                             if (i < 0 || i >= nx || j >= ny) continue;
                             cellOf[(size_t)(sOff[c] + ((long long)jb * sT[c] + t) * 32 + l)] = at[(size_t)j * nx + i];
                         }
+                mgCellOff[c] = (long long)mgCell.size();
+                mgCell.insert(mgCell.end(), at.begin(), at.end());
             }
             if (structured) {
                 b.nSkew = nSkew;
@@ -1112,6 +1133,12 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
                 b.sData64.zero(ctx->stream);
                 b.sData32.alloc((size_t)17 * nSkew);
                 b.sData32.zero(ctx->stream);
+                upload_vec(ctx, mgDims, b.mgDims);
+                upload_vec(ctx, mgNL, b.mgNL);
+                upload_vec(ctx, mgOff, b.mgOff);
+                upload_vec(ctx, mgCellOff, b.mgCellOff);
+                upload_vec(ctx, mgCell, b.mgCell);
+                b.mgPool.alloc((size_t)mgTotal);
                 b.sweep2d = true;
             }
         }

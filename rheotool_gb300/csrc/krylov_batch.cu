@@ -629,6 +629,187 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
         if ((vm >> k) & 1u) w[(size_t)k * N + c] = rD ? rD[c] * r[(size_t)k * N + c] : r[(size_t)k * N + c];
 }
 
+// ---- the per-case multigrid V-cycle (mixed pressure solve) -----------------
+// The multigrid preconditioner of mg.cu on one 2-D case by the CTA that owns
+// it: the same aggregation (2 x 2 blocks, Galerkin 5-point coarse
+// operators), red-black Gauss-Seidel smoothing (kBMgNu sweeps each way,
+// coarse correction scaled by kBMgOver) and symmetric sweeps on the
+// coarsest level, every phase a loop of the CTA over a level's box followed
+// by a barrier.
+constexpr int kBMgNu = 3;
+constexpr float kBMgOver = 1.3f;
+constexpr int kBMgCoarseSweeps = 16;
+
+struct BMg {
+    const int *__restrict__ dims;       // [case][level][2]: nx, ny
+    const int *__restrict__ nl;         // [case]: levels
+    const long long *__restrict__ off;  // [case][level]: the level's arrays in pool
+    const int *__restrict__ cell;       // level 0's cell of each box position (-1 outside)
+    const long long *__restrict__ cellOff;
+    const int *__restrict__ faceLo;     // 2N: the face to the (y, x) lower neighbour
+    float *pool;
+    int on;
+};
+
+struct CL {
+    int nx, ny, n;
+    float *dg, *cx, *cy, *x, *b;
+};
+
+__device__ __forceinline__ CL case_level(const BMg &mg, int cb, int l) {
+    const size_t k = (size_t)cb * kBatchMgLevels + l;
+    CL L;
+    L.nx = mg.dims[2 * k];
+    L.ny = mg.dims[2 * k + 1];
+    L.n = L.nx * L.ny;
+    const size_t np = ((size_t)L.n + 3) / 4 * 4;
+    float *p = mg.pool + mg.off[k];
+    L.dg = p; L.cx = p + np; L.cy = p + 2 * np; L.x = p + 3 * np; L.b = p + 4 * np;
+    return L;
+}
+
+// sum over the four neighbours of a_nb x_nb
+__device__ __forceinline__ float cl_nb(const CL &L, int b, int i, int j) {
+    float s = 0.0f;
+    if (i > 0) s += L.cx[b] * L.x[b - 1];
+    if (i + 1 < L.nx) s += L.cx[b + 1] * L.x[b + 1];
+    if (j > 0) s += L.cy[b] * L.x[b - L.nx];
+    if (j + 1 < L.ny) s += L.cy[b + L.nx] * L.x[b + L.nx];
+    return s;
+}
+
+// level 0 from the FP64 matrix, then the Galerkin coarse levels
+__device__ void case_mg_build(const BMg &mg, int cb, int N, const double *__restrict__ diag,
+                              const double *__restrict__ lower) {
+    const CL L0 = case_level(mg, cb, 0);
+    const int *cell = mg.cell + mg.cellOff[cb];
+    for (int b = threadIdx.x; b < L0.n; b += blockDim.x) {
+        const int c = cell[b];
+        float dg = 0.0f, cx = 0.0f, cy = 0.0f;
+        if (c >= 0) {
+            dg = (float)diag[c];
+            const int fy = mg.faceLo[c], fx = mg.faceLo[N + c];
+            cy = fy >= 0 ? (float)lower[fy] : 0.0f;
+            cx = fx >= 0 ? (float)lower[fx] : 0.0f;
+        }
+        L0.dg[b] = dg;
+        L0.cx[b] = cx;
+        L0.cy[b] = cy;
+    }
+    __syncthreads();
+    const int nL = mg.nl[cb];
+    for (int l = 1; l < nL; ++l) {
+        const CL F = case_level(mg, cb, l - 1), C = case_level(mg, cb, l);
+        const int fx = F.nx == C.nx ? 1 : 2, fy = F.ny == C.ny ? 1 : 2;
+        for (int B = threadIdx.x; B < C.n; B += blockDim.x) {
+            const int I = B % C.nx, J = B / C.nx;
+            float dg = 0.0f, cx = 0.0f, cy = 0.0f;
+            for (int dj = 0; dj < fy; ++dj)
+                for (int di = 0; di < fx; ++di) {
+                    const int i = I * fx + di, j = J * fy + dj;
+                    if (i >= F.nx || j >= F.ny) continue;
+                    const int b = i + F.nx * j;
+                    const float d = F.dg[b];
+                    if (d == 0.0f) continue;
+                    dg += d;
+                    if (di == 1) dg += 2.0f * F.cx[b]; else cx += F.cx[b];
+                    if (dj == 1) dg += 2.0f * F.cy[b]; else cy += F.cy[b];
+                }
+            C.dg[B] = dg;
+            C.cx[B] = I > 0 ? cx : 0.0f;
+            C.cy[B] = J > 0 ? cy : 0.0f;
+        }
+        __syncthreads();
+    }
+}
+
+// one red-black half-sweep of a level (colour 0: i + j even)
+__device__ __forceinline__ void cl_smooth(const CL &L, int colour) {
+    for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
+        const int i = b % L.nx, j = b / L.nx;
+        const float d = L.dg[b];
+        if (((i + j) & 1) == colour && d != 0.0f) L.x[b] = (L.b[b] - cl_nb(L, b, i, j)) / d;
+    }
+    __syncthreads();
+}
+
+// w = V-cycle(r) on the case's cells (FP32 vectors in cell order)
+template <class V>
+__device__ void case_mg_apply(const BMg &mg, int cb, const V *__restrict__ r, V *__restrict__ w) {
+    const int nL = mg.nl[cb];
+    const int *cell = mg.cell + mg.cellOff[cb];
+    {   // level 0 from x = 0: b, then the red half-sweep
+        const CL L = case_level(mg, cb, 0);
+        for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
+            const int c = cell[b];
+            const float rb = c >= 0 ? (float)r[c] : 0.0f;
+            L.b[b] = rb;
+            const float d = L.dg[b];
+            L.x[b] = ((((b % L.nx) + (b / L.nx)) & 1) == 0 && d != 0.0f) ? rb / d : 0.0f;
+        }
+        __syncthreads();
+    }
+    for (int l = 0; l + 1 < nL; ++l) {
+        const CL F = case_level(mg, cb, l), C = case_level(mg, cb, l + 1);
+        for (int nu = 0; nu < kBMgNu; ++nu) {
+            if (l > 0 || nu > 0) cl_smooth(F, 0);
+            cl_smooth(F, 1);
+        }
+        const int fx = F.nx == C.nx ? 1 : 2, fy = F.ny == C.ny ? 1 : 2;
+        for (int B = threadIdx.x; B < C.n; B += blockDim.x) {   // restriction
+            const int I = B % C.nx, J = B / C.nx;
+            float s = 0.0f;
+            for (int dj = 0; dj < fy; ++dj)
+                for (int di = 0; di < fx; ++di) {
+                    const int i = I * fx + di, j = J * fy + dj;
+                    if (i >= F.nx || j >= F.ny) continue;
+                    const int b = i + F.nx * j;
+                    const float d = F.dg[b];
+                    if (d == 0.0f) continue;
+                    s += F.b[b] - d * F.x[b] - cl_nb(F, b, i, j);
+                }
+            C.b[B] = s;
+            C.x[B] = 0.0f;
+        }
+        __syncthreads();
+    }
+    {   // the coarsest level: symmetric sweeps (red, black, black, red)
+        const CL L = case_level(mg, cb, nL - 1);
+        if (nL == 1) {
+            for (int b = threadIdx.x; b < L.n; b += blockDim.x) L.x[b] = 0.0f;
+            __syncthreads();
+        }
+        for (int s = 0; s < kBMgCoarseSweeps; ++s) {
+            cl_smooth(L, 0);
+            cl_smooth(L, 1);
+            cl_smooth(L, 1);
+            cl_smooth(L, 0);
+        }
+    }
+    for (int l = nL - 2; l >= 0; --l) {
+        const CL F = case_level(mg, cb, l), C = case_level(mg, cb, l + 1);
+        for (int b = threadIdx.x; b < F.n; b += blockDim.x) {   // prolongation
+            if (F.dg[b] == 0.0f) continue;
+            const int i = b % F.nx, j = b / F.nx;
+            const int I = F.nx == C.nx ? i : i / 2, J = F.ny == C.ny ? j : j / 2;
+            F.x[b] += kBMgOver * C.x[I + C.nx * J];
+        }
+        __syncthreads();
+        for (int nu = 0; nu < kBMgNu; ++nu) {
+            cl_smooth(F, 1);
+            cl_smooth(F, 0);
+        }
+    }
+    {   // level 0's result to w (cell order)
+        const CL L = case_level(mg, cb, 0);
+        for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
+            const int c = cell[b];
+            if (c >= 0) w[c] = (V)L.x[b];
+        }
+        __syncthreads();
+    }
+}
+
 // ---- the persistent per-case PCG -------------------------------------------
 // One CTA per case runs the case's whole pressure solve (one component,
 // structured 2-D cases with at most 8 j-blocks): the operations of
@@ -732,8 +913,8 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
                                                               V *__restrict__ r, V *__restrict__ w,
                                                               V *__restrict__ p, V *__restrict__ q,
                                                               V *__restrict__ x, const int *__restrict__ order,
-                                                              V *__restrict__ aEll, int *err, long long maxSpin,
-                                                              int cap) {
+                                                              V *__restrict__ aEll, BMg mg, int *err,
+                                                              long long maxSpin, int cap) {
     using Acc = typename AccOf<V>::type;
     __shared__ s2d::u64 ring[8 * s2d::kRJ * s2d::W<V>::n];
     __shared__ int sProg[32];
@@ -742,9 +923,15 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const long long e0 = g.off[cb], e1 = e0 + (long long)g.JB[cb] * g.T[cb] * 32;
     case_ell_coefficients(e, N, c0, c1, u32, l32, aEll);
+    // the FP32 form may take the multigrid V-cycle in place of the DIC sweeps
+    const bool useMg = sizeof(V) == 4 && mg.on;
+    if (useMg) case_mg_build(mg, cb, N, diag, lower);
     for (int it = 0; it < cap; ++it) {
         __syncthreads();
         if (!S.active[sg]) break;
+        if (useMg) {
+            case_mg_apply(mg, cb, r, w);
+        } else {
         // ---- w = M^-1 r: gather, forward and backward sweeps of this case
         for (long long i0 = e0 + tid; i0 < e1; i0 += (long long)kU * nt) {
             int cc[kU];
@@ -772,6 +959,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
             __syncthreads();
         }
         if (case_error(err)) break;
+        }
         // ---- rho = w.r (and w.q_old in the flexible form)
         constexpr int PN = Pack<V>::n;
         int pa, pb;
@@ -1703,13 +1891,16 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);
         else g = sweep2d_view64(ctx);
         {
+            // the multigrid V-cycle for the FP32 form (RT_OPT_MIXED_PRECOND -2, DIC)
+            BMg bmg{bt.mgDims.p, bt.mgNL.p, bt.mgOff.p, bt.mgCell.p, bt.mgCellOff.p, bt.sFaceLo.p, bt.mgPool.p,
+                    (sizeof(V) == 4 && ctx->mixedJacobi == -2 && pre == RT_PRECOND_DIC && bt.mgPool.p) ? 1 : 0};
             ProfScope ps(ctx, "batch_pcg_persistent");
             const int shm = 8 * case_stage_bytes<V, 1, kCaseP<V>, kCaseNB>();
             RT_CUDA(cudaFuncSetAttribute(k_b_pcg_case<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
             k_b_pcg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(sv.t, sv.e, g, sv.S, sv.ctl, sv.mixed, sv.d32, sv.u32,
                                                               sv.l32, a.diag, a.upper, a.lower, a.source, a.psi, r,
                                                               sv.v(1), sv.v(2), sv.v(3), x, bt.caseOrder.p,
-                                                              sv.aEll, bt.sErr.p, 1ll << 22, cap);
+                                                              sv.aEll, bmg, bt.sErr.p, 1ll << 22, cap);
             RT_CHECK_LAUNCH();
         }
         launch_count(ctx);

@@ -205,6 +205,9 @@ struct StructMesh {
 // case meshes, case b owning a contiguous range of cells, internal faces and
 // boundary faces.  One case (n = 1, caseOf = nullptr) is the plain context.
 // ---------------------------------------------------------------------------
+constexpr int kBatchMgLevels = 8;     // levels of a batched case's multigrid hierarchy, at most
+constexpr int kBatchMgCoarse = 64;    // cells of its coarsest level, at most
+
 struct Batch {
     int n = 1;
     std::vector<int> cellStartH, faceStartH, bStartH;   // n + 1 each
@@ -231,6 +234,13 @@ struct Batch {
     DBuf<float> sData32;              // rDinv, Ay, Ax, By, Bx, wS(6), rS(6)
     DBuf<int> sErr;                   // bounded-wait error flag of the batched sweeps
     DBuf<int> caseOrder;              // n: cases by decreasing cell count (the CTA order of one-CTA-per-case launches)
+    // structured 2-D cases: each case's multigrid hierarchy (the mixed
+    // pressure solve of the persistent solver): per case and level the box
+    // (nx, ny) and its arrays' offset in mgPool (dg, cx, cy, x, b, each
+    // padded to 4), the level count, and level 0's cell of each box position
+    DBuf<int> mgDims, mgNL, mgCell;
+    DBuf<long long> mgOff, mgCellOff;
+    DBuf<float> mgPool;
     bool sPending = false;
     // batched Krylov state: per-segment scalars (segment = case * 8 + component),
     // case-aligned reduction partials and results

@@ -138,6 +138,7 @@ def test_batch_persistent_solves_equal_launch_sequence(precision):
         bt = BatchContext(cases)
         try:
             bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, 2 if persistent else 0)
+            bt.ctx.set_option(abi.RT_OPT_MIXED_PRECOND, 0)   # the same preconditioner on both paths
             bt.step(3)
             out[persistent] = (bt.fields(), [(p.p.nIterations, p.U[0].nIterations, p.U[1].nIterations)
                                              for p in bt.case_perf()])
@@ -199,3 +200,29 @@ def test_batch_of_256_row_cases_on_both_paths():
     for i in range(len(cases)):
         for n in NAMES:
             assert rel(getattr(out[1][0][i], n), getattr(out[0][0][i], n)) < 1e-6, (i, n)
+
+
+def test_batch_persistent_multigrid_pressure_solve():
+    """The mixed form's batched pressure solve with each case's multigrid
+    V-cycle (RT_OPT_MIXED_PRECOND -2, the default, in the persistent solver)
+    against the exact DIC of the launch sequence: far fewer pressure
+    iterations, fields within the mixed bar of each other."""
+    cases = cavity_sweep(n_cases=10, n_min=16, n_max=96, seed=9, dt=2e-3, precision=abi.RT_PREC_MIXED)
+    out = {}
+    for mode in ("dic", "mg"):
+        bt = BatchContext(cases)
+        try:
+            bt.ctx.set_option(abi.RT_OPT_BATCH_PERSISTENT, 2 if mode == "mg" else 0)
+            bt.ctx.set_option(abi.RT_OPT_MIXED_PRECOND, -2 if mode == "mg" else 0)
+            bt.step(3)
+            out[mode] = (bt.fields(), [p.p.nIterations for p in bt.case_perf()])
+        finally:
+            bt.ctx.close()
+    assert sum(out["mg"][1]) < 0.5 * sum(out["dic"][1]), (out["mg"][1], out["dic"][1])
+    for i, c in enumerate(cases):
+        errs = {n: rel(getattr(out["mg"][0][i], n), getattr(out["dic"][0][i], n)) for n in NAMES}
+        if all(e < 1e-6 for e in errs.values()):
+            continue
+        bar = step_bar(c, 3, oracle_run(c, 3), NAMES)
+        for n in NAMES:
+            assert errs[n] < max(1e-6, bar[n]), (i, n, errs[n], bar[n])
