@@ -38,6 +38,7 @@ RT_OPT_STALL_TEST = 9
 RT_OPT_MIXED_PRECOND = 10
 RT_OPT_BATCH_PERSISTENT = 11
 RT_OPT_SWEEP_COMPONENTS = 12
+RT_OPT_MIXED_PRECOND_U = 13
 RT_MAX_MODES = 16
 SWEEP_AUTO, SWEEP_LEVELS, SWEEP_SYSTOLIC = 0, 1, 2
 

@@ -486,6 +486,11 @@ rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value) {
                        "Jacobi sweeps per triangular factor");
             ctx->mixedJacobi = (int)value;
             return RT_OK;
+        case RT_OPT_MIXED_PRECOND_U:
+            RT_REQUIRE(value == 0 || value == -2, RT_EINVAL,
+                       "RT_OPT_MIXED_PRECOND_U: 0 exact DILU sweeps, -2 aggregation multigrid");
+            ctx->mixedPrecondU = (int)value;
+            return RT_OK;
         case RT_OPT_SWEEP_COMPONENTS:
             RT_REQUIRE(value == 0 || value == 1, RT_EINVAL, "RT_OPT_SWEEP_COMPONENTS: 0 or 1");
             ctx->sweepComponents = (int)value;
@@ -1068,9 +1073,10 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
                 maxJB = std::max(maxJB, sJB[c]);
             }
             std::vector<int> cellOf((size_t)nSkew, -1);
-            // the multigrid hierarchy of each case (the mixed pressure solve):
-            // its boxes down to at most kBatchMgCoarse cells, their offsets in
-            // one pool, and level 0's cell of each box position
+            // the multigrid hierarchy of each case (the mixed pressure and
+            // momentum solves): its boxes down to at most kBatchMgCoarse
+            // cells, their offsets in one pool, and level 0's cell of each box
+            // position
             std::vector<int> mgDims((size_t)n * kBatchMgLevels * 2, 0), mgNL(n, 0), mgCell;
             std::vector<long long> mgOff((size_t)n * kBatchMgLevels, 0), mgCellOff(n, 0);
             long long mgTotal = 0;
@@ -1080,7 +1086,7 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
                     mgDims[((size_t)c * kBatchMgLevels + l) * 2] = nx;
                     mgDims[((size_t)c * kBatchMgLevels + l) * 2 + 1] = ny;
                     mgOff[(size_t)c * kBatchMgLevels + l] = mgTotal;
-                    mgTotal += 5 * (((long long)nx * ny + 3) / 4 * 4);
+                    mgTotal += kBatchMgArrays * (((long long)nx * ny + 3) / 4 * 4);
                     mgNL[c] = l + 1;
                     if ((long long)nx * ny <= kBatchMgCoarse) break;
                     nx = (nx + 1) / 2;

@@ -629,13 +629,19 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
         if ((vm >> k) & 1u) w[(size_t)k * N + c] = rD ? rD[c] * r[(size_t)k * N + c] : r[(size_t)k * N + c];
 }
 
-// ---- the per-case multigrid V-cycle (mixed pressure solve) -----------------
+// ---- the per-case multigrid V-cycle (mixed pressure and momentum solves) ---
 // The multigrid preconditioner of mg.cu on one 2-D case by the CTA that owns
 // it: the same aggregation (2 x 2 blocks, Galerkin 5-point coarse
 // operators), red-black Gauss-Seidel smoothing (kBMgNu sweeps each way,
 // coarse correction scaled by kBMgOver) and symmetric sweeps on the
 // coarsest level, every phase a loop of the CTA over a level's box followed
-// by a barrier.
+// by a barrier.  A level holds the diagonal and each cell's couplings to and
+// from its (i-1) and (j-1) neighbours: A[c][c-1] in xl, A[c-1][c] in xu (yl,
+// yu likewise); the symmetric pressure matrix keeps one copy (xu aliases xl).
+// With piecewise-constant prolongation P and restriction P^T, the coarse
+// operator P^T A P of a non-symmetric matrix is again such a stencil, so the
+// momentum matrix (convection makes it non-symmetric) takes the same cycle,
+// its components sharing every coefficient load.
 constexpr int kBMgNu = 3;
 constexpr float kBMgOver = 1.3f;
 constexpr int kBMgCoarseSweeps = 16;
@@ -653,57 +659,90 @@ struct BMg {
 
 struct CL {
     int nx, ny, n;
-    float *dg, *cx, *cy, *x, *b;
+    size_t np;   // the stride of the components' x and b
+    float *dg, *xl, *yl, *xu, *yu, *x, *b;
 };
 
-__device__ __forceinline__ CL case_level(const BMg &mg, int cb, int l) {
+__device__ __forceinline__ CL case_level(const BMg &mg, int cb, int l, bool sym) {
     const size_t k = (size_t)cb * kBatchMgLevels + l;
     CL L;
     L.nx = mg.dims[2 * k];
     L.ny = mg.dims[2 * k + 1];
     L.n = L.nx * L.ny;
-    const size_t np = ((size_t)L.n + 3) / 4 * 4;
+    L.np = ((size_t)L.n + 3) / 4 * 4;
     float *p = mg.pool + mg.off[k];
-    L.dg = p; L.cx = p + np; L.cy = p + 2 * np; L.x = p + 3 * np; L.b = p + 4 * np;
+    L.dg = p;
+    L.xl = p + L.np;
+    L.yl = p + 2 * L.np;
+    L.xu = sym ? L.xl : p + 3 * L.np;
+    L.yu = sym ? L.yl : p + 4 * L.np;
+    L.x = p + 5 * L.np;
+    L.b = p + 8 * L.np;
     return L;
 }
 
-// sum over the four neighbours of a_nb x_nb
-__device__ __forceinline__ float cl_nb(const CL &L, int b, int i, int j) {
+// the couplings of box cell b = (i, j) to its four neighbours
+struct CNb {
+    float w, e, s, n;
+};
+
+__device__ __forceinline__ CNb cl_coeffs(const CL &L, int b, int i, int j) {
+    CNb a;
+    a.w = i > 0 ? L.xl[b] : 0.0f;
+    a.e = i + 1 < L.nx ? L.xu[b + 1] : 0.0f;
+    a.s = j > 0 ? L.yl[b] : 0.0f;
+    a.n = j + 1 < L.ny ? L.yu[b + L.nx] : 0.0f;
+    return a;
+}
+
+// sum over the four neighbours of a_nb x_nb (x: one component's array)
+__device__ __forceinline__ float cl_nb(const CL &L, const CNb &a, const float *__restrict__ x, int b, int i,
+                                       int j) {
     float s = 0.0f;
-    if (i > 0) s += L.cx[b] * L.x[b - 1];
-    if (i + 1 < L.nx) s += L.cx[b + 1] * L.x[b + 1];
-    if (j > 0) s += L.cy[b] * L.x[b - L.nx];
-    if (j + 1 < L.ny) s += L.cy[b + L.nx] * L.x[b + L.nx];
+    if (i > 0) s += a.w * x[b - 1];
+    if (i + 1 < L.nx) s += a.e * x[b + 1];
+    if (j > 0) s += a.s * x[b - L.nx];
+    if (j + 1 < L.ny) s += a.n * x[b + L.nx];
     return s;
 }
 
 // level 0 from the FP64 matrix, then the Galerkin coarse levels
-__device__ void case_mg_build(const BMg &mg, int cb, int N, const double *__restrict__ diag,
-                              const double *__restrict__ lower) {
-    const CL L0 = case_level(mg, cb, 0);
+__device__ void case_mg_build(const BMg &mg, int cb, int N, bool sym, const double *__restrict__ diag,
+                              const double *__restrict__ upper, const double *__restrict__ lower) {
+    const CL L0 = case_level(mg, cb, 0, sym);
     const int *cell = mg.cell + mg.cellOff[cb];
     for (int b = threadIdx.x; b < L0.n; b += blockDim.x) {
         const int c = cell[b];
-        float dg = 0.0f, cx = 0.0f, cy = 0.0f;
+        float dg = 0.0f, xl = 0.0f, yl = 0.0f, xu = 0.0f, yu = 0.0f;
         if (c >= 0) {
             dg = (float)diag[c];
+            // the face to the lower neighbour c': A[c][c'] = lower, A[c'][c] = upper
             const int fy = mg.faceLo[c], fx = mg.faceLo[N + c];
-            cy = fy >= 0 ? (float)lower[fy] : 0.0f;
-            cx = fx >= 0 ? (float)lower[fx] : 0.0f;
+            if (fy >= 0) {
+                yl = (float)lower[fy];
+                if (!sym) yu = (float)upper[fy];
+            }
+            if (fx >= 0) {
+                xl = (float)lower[fx];
+                if (!sym) xu = (float)upper[fx];
+            }
         }
         L0.dg[b] = dg;
-        L0.cx[b] = cx;
-        L0.cy[b] = cy;
+        L0.xl[b] = xl;
+        L0.yl[b] = yl;
+        if (!sym) {
+            L0.xu[b] = xu;
+            L0.yu[b] = yu;
+        }
     }
     __syncthreads();
     const int nL = mg.nl[cb];
     for (int l = 1; l < nL; ++l) {
-        const CL F = case_level(mg, cb, l - 1), C = case_level(mg, cb, l);
+        const CL F = case_level(mg, cb, l - 1, sym), C = case_level(mg, cb, l, sym);
         const int fx = F.nx == C.nx ? 1 : 2, fy = F.ny == C.ny ? 1 : 2;
         for (int B = threadIdx.x; B < C.n; B += blockDim.x) {
             const int I = B % C.nx, J = B / C.nx;
-            float dg = 0.0f, cx = 0.0f, cy = 0.0f;
+            float dg = 0.0f, xl = 0.0f, yl = 0.0f, xu = 0.0f, yu = 0.0f;
             for (int dj = 0; dj < fy; ++dj)
                 for (int di = 0; di < fx; ++di) {
                     const int i = I * fx + di, j = J * fy + dj;
@@ -712,53 +751,84 @@ __device__ void case_mg_build(const BMg &mg, int cb, int N, const double *__rest
                     const float d = F.dg[b];
                     if (d == 0.0f) continue;
                     dg += d;
-                    if (di == 1) dg += 2.0f * F.cx[b]; else cx += F.cx[b];
-                    if (dj == 1) dg += 2.0f * F.cy[b]; else cy += F.cy[b];
+                    // a coupling inside the aggregate adds both directions
+                    // to the diagonal, one across its faces to the coupling
+                    if (di == 1) {
+                        dg += F.xl[b] + F.xu[b];
+                    } else {
+                        xl += F.xl[b];
+                        xu += F.xu[b];
+                    }
+                    if (dj == 1) {
+                        dg += F.yl[b] + F.yu[b];
+                    } else {
+                        yl += F.yl[b];
+                        yu += F.yu[b];
+                    }
                 }
             C.dg[B] = dg;
-            C.cx[B] = I > 0 ? cx : 0.0f;
-            C.cy[B] = J > 0 ? cy : 0.0f;
+            C.xl[B] = I > 0 ? xl : 0.0f;
+            C.yl[B] = J > 0 ? yl : 0.0f;
+            if (!sym) {
+                C.xu[B] = I > 0 ? xu : 0.0f;
+                C.yu[B] = J > 0 ? yu : 0.0f;
+            }
         }
         __syncthreads();
     }
 }
 
-// one red-black half-sweep of a level (colour 0: i + j even)
-__device__ __forceinline__ void cl_smooth(const CL &L, int colour) {
+// one red-black half-sweep of a level (colour 0: i + j even), the
+// components in m
+__device__ __forceinline__ void cl_smooth(const CL &L, int colour, unsigned m) {
     for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
         const int i = b % L.nx, j = b / L.nx;
         const float d = L.dg[b];
-        if (((i + j) & 1) == colour && d != 0.0f) L.x[b] = (L.b[b] - cl_nb(L, b, i, j)) / d;
+        if (((i + j) & 1) != colour || d == 0.0f) continue;
+        const CNb a = cl_coeffs(L, b, i, j);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if ((m >> k) & 1u) {
+                float *x = L.x + k * L.np;
+                x[b] = (L.b[k * L.np + b] - cl_nb(L, a, x, b, i, j)) / d;
+            }
     }
     __syncthreads();
 }
 
-// w = V-cycle(r) on the case's cells (FP32 vectors in cell order)
+// w = V-cycle(r) on the case's cells for the components in m (FP32 vectors
+// in cell order, component k at k N)
 template <class V>
-__device__ void case_mg_apply(const BMg &mg, int cb, const V *__restrict__ r, V *__restrict__ w) {
+__device__ void case_mg_apply(const BMg &mg, int cb, int N, bool sym, unsigned m, const V *__restrict__ r,
+                              V *__restrict__ w) {
     const int nL = mg.nl[cb];
     const int *cell = mg.cell + mg.cellOff[cb];
     {   // level 0 from x = 0: b, then the red half-sweep
-        const CL L = case_level(mg, cb, 0);
+        const CL L = case_level(mg, cb, 0, sym);
         for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
             const int c = cell[b];
-            const float rb = c >= 0 ? (float)r[c] : 0.0f;
-            L.b[b] = rb;
             const float d = L.dg[b];
-            L.x[b] = ((((b % L.nx) + (b / L.nx)) & 1) == 0 && d != 0.0f) ? rb / d : 0.0f;
+            const bool red = (((b % L.nx) + (b / L.nx)) & 1) == 0 && d != 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if ((m >> k) & 1u) {
+                    const float rb = c >= 0 ? (float)r[(size_t)k * N + c] : 0.0f;
+                    L.b[k * L.np + b] = rb;
+                    L.x[k * L.np + b] = red ? rb / d : 0.0f;
+                }
         }
         __syncthreads();
     }
     for (int l = 0; l + 1 < nL; ++l) {
-        const CL F = case_level(mg, cb, l), C = case_level(mg, cb, l + 1);
+        const CL F = case_level(mg, cb, l, sym), C = case_level(mg, cb, l + 1, sym);
         for (int nu = 0; nu < kBMgNu; ++nu) {
-            if (l > 0 || nu > 0) cl_smooth(F, 0);
-            cl_smooth(F, 1);
+            if (l > 0 || nu > 0) cl_smooth(F, 0, m);
+            cl_smooth(F, 1, m);
         }
         const int fx = F.nx == C.nx ? 1 : 2, fy = F.ny == C.ny ? 1 : 2;
         for (int B = threadIdx.x; B < C.n; B += blockDim.x) {   // restriction
             const int I = B % C.nx, J = B / C.nx;
-            float s = 0.0f;
+            float s[3] = {0.0f, 0.0f, 0.0f};
             for (int dj = 0; dj < fy; ++dj)
                 for (int di = 0; di < fx; ++di) {
                     const int i = I * fx + di, j = J * fy + dj;
@@ -766,45 +836,63 @@ __device__ void case_mg_apply(const BMg &mg, int cb, const V *__restrict__ r, V 
                     const int b = i + F.nx * j;
                     const float d = F.dg[b];
                     if (d == 0.0f) continue;
-                    s += F.b[b] - d * F.x[b] - cl_nb(F, b, i, j);
+                    const CNb a = cl_coeffs(F, b, i, j);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        if ((m >> k) & 1u) {
+                            const float *x = F.x + k * F.np;
+                            s[k] += F.b[k * F.np + b] - d * x[b] - cl_nb(F, a, x, b, i, j);
+                        }
                 }
-            C.b[B] = s;
-            C.x[B] = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if ((m >> k) & 1u) {
+                    C.b[k * C.np + B] = s[k];
+                    C.x[k * C.np + B] = 0.0f;
+                }
         }
         __syncthreads();
     }
     {   // the coarsest level: symmetric sweeps (red, black, black, red)
-        const CL L = case_level(mg, cb, nL - 1);
+        const CL L = case_level(mg, cb, nL - 1, sym);
         if (nL == 1) {
-            for (int b = threadIdx.x; b < L.n; b += blockDim.x) L.x[b] = 0.0f;
+            for (int b = threadIdx.x; b < L.n; b += blockDim.x)
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if ((m >> k) & 1u) L.x[k * L.np + b] = 0.0f;
             __syncthreads();
         }
         for (int s = 0; s < kBMgCoarseSweeps; ++s) {
-            cl_smooth(L, 0);
-            cl_smooth(L, 1);
-            cl_smooth(L, 1);
-            cl_smooth(L, 0);
+            cl_smooth(L, 0, m);
+            cl_smooth(L, 1, m);
+            cl_smooth(L, 1, m);
+            cl_smooth(L, 0, m);
         }
     }
     for (int l = nL - 2; l >= 0; --l) {
-        const CL F = case_level(mg, cb, l), C = case_level(mg, cb, l + 1);
+        const CL F = case_level(mg, cb, l, sym), C = case_level(mg, cb, l + 1, sym);
         for (int b = threadIdx.x; b < F.n; b += blockDim.x) {   // prolongation
             if (F.dg[b] == 0.0f) continue;
             const int i = b % F.nx, j = b / F.nx;
             const int I = F.nx == C.nx ? i : i / 2, J = F.ny == C.ny ? j : j / 2;
-            F.x[b] += kBMgOver * C.x[I + C.nx * J];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if ((m >> k) & 1u) F.x[k * F.np + b] += kBMgOver * C.x[k * C.np + I + C.nx * J];
         }
         __syncthreads();
         for (int nu = 0; nu < kBMgNu; ++nu) {
-            cl_smooth(F, 1);
-            cl_smooth(F, 0);
+            cl_smooth(F, 1, m);
+            cl_smooth(F, 0, m);
         }
     }
     {   // level 0's result to w (cell order)
-        const CL L = case_level(mg, cb, 0);
+        const CL L = case_level(mg, cb, 0, sym);
         for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
             const int c = cell[b];
-            if (c >= 0) w[c] = (V)L.x[b];
+            if (c < 0) continue;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if ((m >> k) & 1u) w[(size_t)k * N + c] = (V)L.x[k * L.np + b];
         }
         __syncthreads();
     }
@@ -925,12 +1013,12 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
     case_ell_coefficients(e, N, c0, c1, u32, l32, aEll);
     // the FP32 form may take the multigrid V-cycle in place of the DIC sweeps
     const bool useMg = sizeof(V) == 4 && mg.on;
-    if (useMg) case_mg_build(mg, cb, N, diag, lower);
+    if (useMg) case_mg_build(mg, cb, N, true, diag, upper, lower);
     for (int it = 0; it < cap; ++it) {
         __syncthreads();
         if (!S.active[sg]) break;
         if (useMg) {
-            case_mg_apply(mg, cb, r, w);
+            case_mg_apply(mg, cb, N, true, 1u, r, w);
         } else {
         // ---- w = M^-1 r: gather, forward and backward sweeps of this case
         for (long long i0 = e0 + tid; i0 < e1; i0 += (long long)kU * nt) {
@@ -1298,8 +1386,8 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
                                                               V *__restrict__ Ay, V *__restrict__ sv,
                                                               V *__restrict__ z, V *__restrict__ tt,
                                                               V *__restrict__ x, const int *__restrict__ order,
-                                                              V *__restrict__ aEll, int *err, long long maxSpin,
-                                                              int cap) {
+                                                              V *__restrict__ aEll, BMg mg, int *err,
+                                                              long long maxSpin, int cap) {
     using Acc = typename AccOf<V>::type;
     constexpr int PN = Pack<V>::n;
     __shared__ s2d::u64 ring[16 * s2d::kRJ * s2d::W<V>::n];   // two halves of the CTA, 8 j-blocks each
@@ -1314,6 +1402,9 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
     const int c0 = t.blkCell0[t.caseBlk[cb]], c1 = t.blkCell1[t.caseBlk[cb + 1] - 1];
     const int s0 = cb * 8;
     case_ell_coefficients(e, N, c0, c1, u32, l32, aEll);
+    // the FP32 form may take the multigrid V-cycle in place of the DILU sweeps
+    const bool useMg = sizeof(V) == 4 && mg.on;
+    if (useMg) case_mg_build(mg, cb, N, false, diag, upper, lower);
     // the segments (components) selected by a predicate on their state
     auto seg_mask = [&](auto pred) {
         unsigned mm = 0;
@@ -1415,8 +1506,12 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         }
         __syncthreads();
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
-        case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg, stageSmem);
-        if (case_error(err)) break;
+        if (useMg) {
+            case_mg_apply(mg, cb, N, false, vm, p, y);
+        } else {
+            case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg, stageSmem);
+            if (case_error(err)) break;
+        }
         case_amul(e, N, c0, c1, vm, d32, aEll, y, Ay);
         __syncthreads();
         {
@@ -1533,8 +1628,12 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         }
         const unsigned full = sMask[3];
         // ---- z = M^-1 s, tt = A z, omega = tt.s / tt.tt
-        case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg, stageSmem);
-        if (case_error(err)) break;
+        if (useMg) {
+            case_mg_apply(mg, cb, N, false, vm, sv, z);
+        } else {
+            case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg, stageSmem);
+            if (case_error(err)) break;
+        }
         case_amul(e, N, c0, c1, vm, d32, aEll, z, tt);
         __syncthreads();
         {
@@ -1914,13 +2013,16 @@ rt_status run_batch(rt_ctx *ctx, const SolveArgs &a, rt_solver_perf *perf) {
         if constexpr (sizeof(V) == 4) g = sweep2d_view32(ctx);
         else g = sweep2d_view64(ctx);
         {
+            // the multigrid V-cycle for the FP32 form (RT_OPT_MIXED_PRECOND_U -2, DILU)
+            BMg bmg{bt.mgDims.p, bt.mgNL.p, bt.mgOff.p, bt.mgCell.p, bt.mgCellOff.p, bt.sFaceLo.p, bt.mgPool.p,
+                    (sizeof(V) == 4 && ctx->mixedPrecondU == -2 && pre == RT_PRECOND_DILU && bt.mgPool.p) ? 1 : 0};
             ProfScope ps(ctx, "batch_bicgstab_persistent");
             const int shm = 16 * case_stage_bytes<V, 1, kBicgP<V>, kBicgNB<V>>();
             RT_CUDA(cudaFuncSetAttribute(k_b_bicg_case<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
             k_b_bicg_case<V><<<bt.n, kCaseThreads, shm, sv.st>>>(
                 sv.t, sv.e, g, sv.S, sv.ctl, sv.vm, sv.mixed, sv.d32, sv.u32, sv.l32, a.diag, a.upper, a.lower,
                 a.source, a.psi, r, sv.v(1), sv.v(2), sv.v(3), sv.v(4), sv.v(5), sv.v(6), sv.v(7), x,
-                bt.caseOrder.p, sv.aEll, bt.sErr.p, 1ll << 22, cap);
+                bt.caseOrder.p, sv.aEll, bmg, bt.sErr.p, 1ll << 22, cap);
             RT_CHECK_LAUNCH();
         }
         launch_count(ctx);

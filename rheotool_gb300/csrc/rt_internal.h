@@ -207,6 +207,7 @@ struct StructMesh {
 // ---------------------------------------------------------------------------
 constexpr int kBatchMgLevels = 8;     // levels of a batched case's multigrid hierarchy, at most
 constexpr int kBatchMgCoarse = 64;    // cells of its coarsest level, at most
+constexpr int kBatchMgArrays = 11;   // arrays of a level: dg, xl, yl, xu, yu, x[3], b[3]
 
 struct Batch {
     int n = 1;
@@ -235,9 +236,10 @@ struct Batch {
     DBuf<int> sErr;                   // bounded-wait error flag of the batched sweeps
     DBuf<int> caseOrder;              // n: cases by decreasing cell count (the CTA order of one-CTA-per-case launches)
     // structured 2-D cases: each case's multigrid hierarchy (the mixed
-    // pressure solve of the persistent solver): per case and level the box
-    // (nx, ny) and its arrays' offset in mgPool (dg, cx, cy, x, b, each
-    // padded to 4), the level count, and level 0's cell of each box position
+    // pressure and momentum solves of the persistent solvers, one at a time):
+    // per case and level the box (nx, ny) and its arrays' offset in mgPool
+    // (kBatchMgArrays of them, each padded to 4), the level count, and level
+    // 0's cell of each box position
     DBuf<int> mgDims, mgNL, mgCell;
     DBuf<long long> mgOff, mgCellOff;
     DBuf<float> mgPool;
@@ -467,6 +469,7 @@ struct rt_ctx {
     // triangular factor (0: the exact sweeps); FP32 premultiplied split-ELL
     // coefficients and three FP32 vectors
     int mixedJacobi = -2;   // RT_OPT_MIXED_PRECOND (default: the multigrid V-cycle)
+    int mixedPrecondU = -2;   // RT_OPT_MIXED_PRECOND_U (default: the multigrid V-cycle)
     rt::DBuf<float> jac;
     // batched form: the pressure solve of structured 2-D cases as one
     // persistent CTA per case (RT_OPT_BATCH_PERSISTENT; 0: the per-iteration
