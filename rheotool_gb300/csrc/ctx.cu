@@ -414,7 +414,8 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
             upload_vec(ctx, at, s.cellAt);
             upload_vec(ctx, boxOf, s.boxOf);
             s.mgDims.clear();
-            s.mgGraph.reset();
+            for (MgGraph &g : s.mgGraph) g.reset();
+            s.mgNext = 0;
         }
         RT_REQUIRE(s.nJB <= 8 && skew_fits(s.nJB), RT_EINVAL, "structured sweeps need ny <= 256");
         // planes (CTAs) per thread-block cluster: 16 (the non-portable maximum;

@@ -1569,7 +1569,10 @@ struct Mixed : Solver {
         const int pre = a.ctl.preconditioner;
         if (multigrid()) {
             ProfScope ps(ctx, "mg_setup", (double)N * (8.0 + 3.0 * 8.0 + 16.0 + 12.0));
-            mg_prepare(ctx, a.diag, a.lower);
+            mg_prepare(ctx, a.diag, a.upper, a.lower, true);
+        } else if (multigridU()) {
+            ProfScope ps(ctx, "mg_setup", (double)N * (8.0 + 6.0 * 8.0 + 28.0 + 24.0));
+            mg_prepare(ctx, a.diag, a.upper, a.lower, false);
         } else if (redblack()) {
             if (ctx->jac.n < 2 * (size_t)N) ctx->jac.alloc(2 * (size_t)N);
             ProfScope ps(ctx, "dilu_rD", (double)N * (8.0 + 8.0 + 4.0) + (double)ctx->mesh.F * 16.0);
@@ -1631,6 +1634,12 @@ struct Mixed : Solver {
     // a symmetric matrix, structured mesh without coupled faces)
     bool multigrid() const {
         return ctx->mixedJacobi == -2 && a.nc == 1 && a.ctl.preconditioner == RT_PRECOND_DIC && mg_available(ctx);
+    }
+    // the same V-cycle for the momentum solve (up to three components, a
+    // non-symmetric matrix)
+    bool multigridU() const {
+        return ctx->mixedPrecondU == -2 && a.nc <= 3 && (a.validMask & ~7u) == 0 &&
+               a.ctl.preconditioner == RT_PRECOND_DILU && mg_available(ctx);
     }
 
     // the Jacobi-swept DIC/DILU of the pressure solve (one component)
@@ -1706,6 +1715,15 @@ struct Mixed : Solver {
         const DevMesh &m = ctx->mesh;
         const int pre = a.ctl.preconditioner;
         const double fpc = (double)m.F / N;
+        if (multigridU()) {
+            // level 0: r and w (4 + 4 a component), five passes of the 7-point
+            // stencil (7 x 4 bytes, x and b a component); the coarser levels
+            // add about 1/7
+            const double nc = pop(mask);
+            ProfScope ps(ctx, "mg_vcycle32", (double)N * (8.0 * nc + 5.0 * (28.0 + 12.0 * nc)) * 8.0 / 7.0);
+            mg_apply32(ctx, mask, r, w);
+            return;
+        }
         if (pre == RT_PRECOND_NONE) {
             k_mx_copy<<<nblocks(N), RT_BLOCK, 0, st>>>(N, mask, r, w);
             launch_count(ctx);

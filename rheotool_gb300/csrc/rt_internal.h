@@ -118,17 +118,22 @@ using SkewView32 = SkewT<float>;
 struct MgGraph {
     cudaGraphExec_t exec = nullptr;
     const void *r = nullptr, *w = nullptr, *dm = nullptr;
+    unsigned mask = 0;   // the components it smooths
+    bool sym = false;    // the symmetric (pressure) view of the hierarchy
     int launches = 0;
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
         r = w = dm = nullptr;
+        mask = 0;
+        sym = false;
     }
     MgGraph() = default;
     MgGraph(const MgGraph &) = delete;
     MgGraph &operator=(const MgGraph &) = delete;
     ~MgGraph() { reset(); }
 };
+constexpr int kMgGraphs = 8;   // captured V-cycles kept per mesh
 
 struct StructMesh {
     bool on = false;
@@ -149,7 +154,8 @@ struct StructMesh {
     DBuf<int> cellAt, boxOf;
     std::vector<std::array<int, 3>> mgDims;
     DBuf<float> mgData;
-    MgGraph mgGraph;   // the captured V-cycle
+    MgGraph mgGraph[kMgGraphs];   // the captured V-cycles, replaced round robin
+    int mgNext = 0;
 
     SkewView view() {
         SkewView v;

@@ -24,12 +24,16 @@ void skew_precondition32(rt_ctx *ctx, int nc, unsigned mask, const float *r, flo
 // the same with an FP64 right-hand side and result (rounded on the way in and out)
 void skew_precondition32d(rt_ctx *ctx, int nc, unsigned mask, const double *r, double *w,
                           const unsigned *dmask = nullptr);
-// mg.cu: the aggregation multigrid V-cycle of the mixed pressure solve
-// (FP32): the hierarchy for a symmetric matrix, then w = V-cycle(r); dm
-// (device, or null): component 0 still iterating
+// mg.cu: the aggregation multigrid V-cycle of the mixed pressure and
+// momentum solves (FP32): the hierarchy of a matrix (sym: a symmetric one,
+// its lower coefficients only), then w = V-cycle(r): mg_apply for the
+// pressure (FP64 vectors; dm, device or null: component 0 still iterating),
+// mg_apply32 for the momentum components in mask (FP32 vectors, component k
+// at k N)
 bool mg_available(rt_ctx *ctx);
-void mg_prepare(rt_ctx *ctx, const double *diag, const double *lower);
+void mg_prepare(rt_ctx *ctx, const double *diag, const double *upper, const double *lower, bool sym);
 void mg_apply(rt_ctx *ctx, const double *r, double *w, const unsigned *dm = nullptr);
+void mg_apply32(rt_ctx *ctx, unsigned mask, const float *r, float *w);
 // whether the sweeps of a structured mesh with nJB j-blocks fit one CTA's shared memory
 bool skew_fits(int nJB);
 // RT_ETIMEOUT if a bounded wait of the last sweeps ran out

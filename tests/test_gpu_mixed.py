@@ -27,9 +27,10 @@ pytestmark = pytest.mark.gpu
 
 TOL_MIXED = 1e-6
 
-# the library's default preconditioner of the mixed pressure solve (the
-# multigrid V-cycle on structured meshes)
+# the library's default preconditioners of the mixed pressure and momentum
+# solves (the multigrid V-cycle on structured meshes)
 MIXED_PRECOND_DEFAULT = -2
+MIXED_PRECOND_U_DEFAULT = -2
 
 MESHES = {
     "cavity70": lambda: cavity_mesh(70),
@@ -117,7 +118,12 @@ def test_mixed_pbicgstab_dilu_multi_rhs(ctx, mesh_name, sweep, nc):
     b[1] = 0.0                                        # a component that starts converged
     x0 = np.zeros((nc, mesh.nCells))
     ctl = SolverControl("PBiCGStab", "DILU", 1e-10, 0.0, 0, 1000)
-    xg, perf = _solve(ctx, mesh, diag, upper, lower, b, x0, ctl, abi.RT_PREC_MIXED, sweep)
+    ctx.upload_mesh(mesh)
+    try:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND_U, 0)   # the exact DILU sweeps
+        xg, perf = _solve(ctx, mesh, diag, upper, lower, b, x0, ctl, abi.RT_PREC_MIXED, sweep)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND_U, MIXED_PRECOND_U_DEFAULT)
     orc = Oracle(_case_for(mesh))
     for k in range(nc):
         xo = x0[k].copy()
@@ -130,6 +136,52 @@ def test_mixed_pbicgstab_dilu_multi_rhs(ctx, mesh_name, sweep, nc):
         assert true < ctl.tolerance, (k, true)
         assert perf[k].nIterations <= 2.0 * po.nIterations + 20, (k, perf[k].nIterations, po.nIterations)
         assert rel(xg[k], xo) < TOL_MIXED, (k, rel(xg[k], xo))
+
+
+@pytest.mark.parametrize("mesh_name", sorted(MESHES))
+def test_mixed_pbicgstab_multigrid(ctx, mesh_name):
+    """RT_OPT_MIXED_PRECOND_U -2: the mixed momentum solve (three components,
+    a non-symmetric matrix, one component starting converged, one from a
+    noisy initial guess) preconditioned by the aggregation multigrid V-cycle
+    stops on the same FP64 residual test and gives the FP64 DILU solution
+    within the mixed bar: 1e-6, or three times the oracle's own
+    solver-tolerance error where that is larger (the noisy start's
+    normFactor lets a solve stopped at 1e-10 sit 2.5e-6 from the converged
+    solution on the 70 x 70 cavity); a second solve on the same buffers
+    replays the captured V-cycles bit for bit."""
+    from oracle.pyoracle import Oracle
+    mesh = MESHES[mesh_name]()
+    rng = np.random.default_rng(36)
+    diag, upper, lower = laplacian_system(mesh, rng, asym=3.0)
+    b = rng.normal(size=(3, mesh.nCells)) * mesh.V
+    b[1] = 0.0
+    x0 = np.zeros((3, mesh.nCells))
+    x0[2] = rng.normal(size=mesh.nCells) * 0.1
+    ctl = SolverControl("PBiCGStab", "DILU", 1e-10, 0.0, 0, 1000)
+    ctx.upload_mesh(mesh)
+    try:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND_U, -2)
+        xg, perf = _solve(ctx, mesh, diag, upper, lower, b, x0, ctl, abi.RT_PREC_MIXED, abi.SWEEP_AUTO)
+        xg2, perf2 = _solve(ctx, mesh, diag, upper, lower, b, x0, ctl, abi.RT_PREC_MIXED, abi.SWEEP_AUTO)
+    finally:
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND_U, MIXED_PRECOND_U_DEFAULT)
+    orc = Oracle(_case_for(mesh))
+    assert np.array_equal(xg, xg2)
+    for k in range(3):
+        xo = x0[k].copy()
+        po = orc.ldu_solve(diag, upper, lower, b[k].copy(), xo, ctl)
+        assert bool(perf[k].converged) and bool(po.converged), k
+        assert perf2[k].nIterations == perf[k].nIterations
+        if k == 1:
+            assert perf[k].nIterations == 0 and np.abs(xg[k]).max() == 0
+            continue
+        true = foam_residual(mesh, diag, upper, lower, b[k], xg[k], x0[k])
+        assert true < ctl.tolerance, (k, true)
+        assert perf[k].nIterations <= po.nIterations + 10, (k, perf[k].nIterations, po.nIterations)
+        xt = x0[k].copy()
+        orc.ldu_solve(diag, upper, lower, b[k].copy(), xt, _tightened(ctl))
+        floor = rel(xt, xo)
+        assert rel(xg[k], xo) < max(TOL_MIXED, 3.0 * floor), (k, rel(xg[k], xo), floor)
 
 
 def test_mixed_reports_non_convergence(ctx):
@@ -293,10 +345,14 @@ def test_mixed_pcg_multigrid(ctx, mesh_name):
     assert np.array_equal(xg, xg2) and perf2[0].nIterations == pg.nIterations
 
 
-def test_mixed_step_contraction3d_multigrid(ctx):
-    """Full mixed steps with the multigrid-preconditioned pressure solve."""
+@pytest.mark.parametrize("u_mg", [0, -2])
+def test_mixed_step_contraction3d_multigrid(ctx, u_mg):
+    """Full mixed steps with the multigrid-preconditioned pressure solve, the
+    momentum solve with the exact DILU sweeps or the V-cycle."""
     try:
         ctx.set_option(abi.RT_OPT_MIXED_PRECOND, -2)
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND_U, u_mg)
         _mixed_step_check(ctx, contraction_case(small_contraction()), 5)
     finally:
         ctx.set_option(abi.RT_OPT_MIXED_PRECOND, MIXED_PRECOND_DEFAULT)
+        ctx.set_option(abi.RT_OPT_MIXED_PRECOND_U, MIXED_PRECOND_U_DEFAULT)
