@@ -315,12 +315,13 @@ rt_status rt_mesh_set_ijk(rt_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, const
  * the components lane by lane.  Both give the same bits. */
 #define RT_OPT_SWEEP_COMPONENTS 12
 /* RT_OPT_MIXED_PRECOND_U: the preconditioner of the mixed form's momentum
- * solve (DILU selected).  -2 (default): in the batched form's persistent
- * solver on structured 2-D cases, the aggregation multigrid V-cycle of
- * RT_OPT_MIXED_PRECOND -2 built from the non-symmetric momentum matrix (its
- * components in one cycle); elsewhere the exact DILU.  0: DILU with the
- * exact triangular sweeps.  Both stop on the same FP64 residual test; the
- * FP64 plain form always uses the exact sweeps. */
+ * solve (DILU selected, up to three components).  -2 (default): on
+ * structured meshes without coupled faces (and in the batched form's
+ * persistent solver on structured 2-D cases), the aggregation multigrid
+ * V-cycle of RT_OPT_MIXED_PRECOND -2 built from the non-symmetric momentum
+ * matrix, its components in one cycle; elsewhere the exact DILU.  0: DILU
+ * with the exact triangular sweeps.  Both stop on the same FP64 residual
+ * test; the FP64 plain form always uses the exact sweeps. */
 #define RT_OPT_MIXED_PRECOND_U 13
 rt_status rt_set_option(rt_ctx *ctx, int32_t option, int64_t value);
 rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bcs,
