@@ -779,12 +779,17 @@ __device__ void case_mg_build(const BMg &mg, int cb, int N, bool sym, const doub
 }
 
 // one red-black half-sweep of a level (colour 0: i + j even), the
-// components in m
+// components in m; the CTA's threads walk the colour's cells only (row j
+// holds them at i = (colour + j) % 2, +2, ...)
 __device__ __forceinline__ void cl_smooth(const CL &L, int colour, unsigned m) {
-    for (int b = threadIdx.x; b < L.n; b += blockDim.x) {
-        const int i = b % L.nx, j = b / L.nx;
+    const int hx = (L.nx + 1) >> 1;
+    for (int t = threadIdx.x; t < hx * L.ny; t += blockDim.x) {
+        const int j = t / hx;
+        const int i = 2 * (t - j * hx) + ((colour + j) & 1);
+        if (i >= L.nx) continue;
+        const int b = i + L.nx * j;
         const float d = L.dg[b];
-        if (((i + j) & 1) != colour || d == 0.0f) continue;
+        if (d == 0.0f) continue;
         const CNb a = cl_coeffs(L, b, i, j);
 #pragma unroll
         for (int k = 0; k < 3; ++k)

@@ -210,6 +210,28 @@ __global__ void k_mg_smooth(MgLev L, int colour, unsigned m, const int *__restri
         }
 }
 
+// the same half-sweep without w, one thread per cell of the colour (row
+// (j, k) holds them at i = (colour + j + k) % 2, +2, ...)
+__global__ void k_mg_smooth_colour(MgLev L, int colour, unsigned m, const unsigned *__restrict__ dm) {
+    const int hx = (L.nx + 1) >> 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= hx * L.ny * L.nz || skip(dm)) return;
+    const int row = t / hx;
+    const int j = row % L.ny, k = row / L.ny;
+    const int i = 2 * (t - row * hx) + ((colour + j + k) & 1);
+    if (i >= L.nx) return;
+    const int b = i + L.nx * row;
+    const float d = L.dg[b];
+    if (d == 0.0f) return;
+    const Nb6 a = nb_coeffs(L, b, i, j, k);
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+        if ((m >> q) & 1u) {
+            float *x = L.x + q * L.np;
+            x[b] = (L.b[q * L.np + b] - nb_sum(L, a, b, i, j, k, x)) / d;
+        }
+}
+
 // the residual b - A x of each aggregate's cells, summed into the coarse
 // right-hand side; the coarse x starts at 0
 __global__ void k_mg_restrict(MgLev F, MgLev C, unsigned m, const unsigned *__restrict__ dm) {
@@ -348,6 +370,9 @@ void mg_prepare(rt_ctx *ctx, const double *diag, const double *upper, const doub
 
 namespace {
 
+// the threads of a one-colour half-sweep of a level
+int colour_threads(const MgLev &L) { return (L.nx + 1) / 2 * L.ny * L.nz; }
+
 // one V-cycle's launches on the stream; the number of kernels
 template <class T>
 int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T *r, T *w, const unsigned *dm) {
@@ -369,10 +394,10 @@ int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T
     for (int l = 0; l + 1 < nL; ++l) {
         for (int nu = 0; nu < kNu; ++nu) {
             if (l > 0 || nu > 0) {
-                k_mg_smooth<T><<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], 0, m, nullptr, N, nullptr, dm);
+                k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
                 ++launches;
             }
-            k_mg_smooth<T><<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], 1, m, nullptr, N, nullptr, dm);
+            k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 1, m, dm);
             ++launches;
         }
         k_mg_restrict<<<nblocks(L[l + 1].n), RT_BLOCK, 0, st>>>(L[l], L[l + 1], m, dm);
@@ -386,9 +411,11 @@ int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T
         ++launches;
         for (int nu = 0; nu < kNu; ++nu) {
             const bool last = l == 0 && nu == kNu - 1;
-            k_mg_smooth<T><<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], 1, m, nullptr, N, nullptr, dm);
-            k_mg_smooth<T><<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], 0, m, last ? s.cellAt.p : nullptr, N,
-                                                                 last ? w : nullptr, dm);
+            k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 1, m, dm);
+            if (last)   // level 0's last half-sweep writes every cell's x to w
+                k_mg_smooth<T><<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], 0, m, s.cellAt.p, N, w, dm);
+            else
+                k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
             launches += 2;
         }
     }
