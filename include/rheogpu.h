@@ -23,6 +23,13 @@
  *                            WhiteMetznerCYLog.C:145-206
  *   rt_constitutive_correct_iter  the same, called nInIter times in one time
  *                            step (solvers/rheoFoam/rheoFoam.C:149-153)
+ *   rt_set_temperature       the thermoFunction shifts of lambda and etaP that
+ *                            the Log models' correct() applies in a
+ *                            non-isothermal solver (libs/thermo/thermoFunctions/
+ *                            thermoFunctions/thermoFunction.H, the types'
+ *                            createField) with T in the mesh, as
+ *                            solvers/rheoHeatFoam/rheoHeatFoam.C:144,189 call
+ *                            constEq.correct()
  *   rt_ldu_solve             lduMatrix::solver::solve(psi, source, cmpt) of
  *                            OpenFOAM's PCG/DIC, PBiCGStab/DILU and PBiCG/DILU, reached
  *                            through sparseSolver<Type>::solve
@@ -410,6 +417,51 @@ rt_status rt_constitutive_correct(rt_ctx *ctx, const double *gradU,
  * another time step, or replaces theta). */
 rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t newTimeStep,
                                        rt_solver_perf *thetaPerf);
+
+/* ---- temperature-dependent parameters (thermoFunctions) ---------------
+ * The non-isothermal solvers (rheoHeatFoam) call the same
+ * constitutiveEq::correct() with a temperature field T in the mesh.  Each
+ * Log model then takes its relaxation times and polymeric viscosity as
+ * fields, the constant times a shift factor of T:
+ *   volScalarField lambda(thermoLambdaPtr_->createField(lambda_));
+ *   volScalarField etaP(thermoEtaPtr_->createField(etaP_));
+ * (Oldroyd-B/Oldroyd-BLog/Oldroyd_BLog.C:133-135; the other Log models
+ * likewise).  Rolie-Poly shifts lambdaD and lambdaR by their own functions
+ * (thermoLambdaD, thermoLambdaR: RoliePolyLog.C:139-141), XPomPom lambdaB
+ * and lambdaS (thermoLambdaB, thermoLambdaS: XPomPomLog.C:140-142).  The
+ * shift factors, thermoFunctions/<type>/<type>.C (a model dictionary without
+ * the sub-dictionary selects Constant, newThermoFunction.C:41): */
+#define RT_THERMO_CONSTANT           0   /* a = 1                                  (Constant.C:58-73) */
+#define RT_THERMO_ARRHENIUS          1   /* a = exp(alpha (1/T - 1/T0))            (Arrhenius.C:61-76) */
+#define RT_THERMO_ARRHENIUS_MODIFIED 2   /* a = exp(-alpha (T - T0))               (ArrheniusModified.C:61-76) */
+#define RT_THERMO_WLF                3   /* a = 10^(-c1 (T - T0) / (c2 + T - T0))  (WLF.C:61-76) */
+#define RT_THERMO_VFT                4   /* a = 10^(B + A / (T - T0))              (VFT.C:62-77) */
+
+typedef struct {
+    int32_t type, pad_;
+    double alpha, T0;   /* Arrhenius, ArrheniusModified (T0 also WLF and VFT) */
+    double c1, c2;      /* WLF                                                */
+    double A, B;        /* VFT                                                */
+} rt_thermo_fn;
+
+typedef struct {
+    rt_thermo_fn lambda;    /* thermoLambda (Rolie-Poly: thermoLambdaD; XPomPom: thermoLambdaB) */
+    rt_thermo_fn lambda2;   /* Rolie-Poly thermoLambdaR; XPomPom thermoLambdaS; unused otherwise  */
+    rt_thermo_fn eta;       /* thermoEta (etaP)                                                   */
+} rt_thermo_desc;
+
+/* Set the cell temperatures T (nCells, host) and each mode's shift
+ * functions (modes: the case's nModes descriptors, in mode order); the
+ * factors are computed on the device at once and every later
+ * rt_constitutive_correct / rt_constitutive_correct_iter applies them.  T =
+ * NULL returns to the isothermal case, as does another rt_case_setup.
+ * RT_EINVAL: a temperature outside a function's domain (Arrhenius T <= 0 or
+ * T0 <= 0, WLF c2 + T - T0 = 0, VFT T = T0), a non-finite T, an unknown type,
+ * or a batched layout.  The momentum equation's temperature-dependent
+ * viscosities (etaSThermo, etaPThermo in constitutiveEq.C:200-245) and the
+ * energy equation are not built, so rt_step returns RT_EINVAL while a
+ * temperature is set. */
+rt_status rt_set_temperature(rt_ctx *ctx, const rt_thermo_desc *modes, const double *T);
 
 /* nSteps segregated rheoFoam time steps; perf (may be NULL) gets the last. */
 rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf);

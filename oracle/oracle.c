@@ -40,6 +40,12 @@
  *                                         144-156 (divTau), 222 (tau), 247-256
  *                                         (correct)
  *   - nNonOrthogonalCorrectors .......... solvers/rheoFoam/pEqn.H:31-50
+ *   - temperature-dependent parameters .. libs/thermo/thermoFunctions/{Constant,
+ *                                         Arrhenius,ArrheniusModified,WLF,VFT}/<type>.C
+ *                                         (multiply), as the Log models' correct()
+ *                                         applies them (Oldroyd_BLog.C:133-135,
+ *                                         RoliePolyLog.C:139-141, XPomPomLog.C:
+ *                                         140-142, WhiteMetznerCYLog.C:166-167)
  * and OpenFOAM v9 behaviour that is not vendored in rheoTool (fvm::ddt Euler
  * and Crank-Nicolson, Gauss linear grad/div, orthogonal laplacian, fvMatrix
  * A/H/H1/flux, ddtCorr, setReference, PCG, PBiCGStab, PBiCG, DIC, DILU),
@@ -753,6 +759,10 @@ typedef struct {
     or_ddt *ddt;
     double ddtC, ddtCth;
     const double *Dth;
+    /* temperature-dependent parameters: per mode, 3 nCells shift factors
+     * (lambda, the second relaxation time, etaP; mode i at 3 nCells i), or
+     * NULL for the isothermal case */
+    const double *thermo;
 } or_case;
 
 static void case_init(or_case *k, const rt_mesh_desc *m, const rt_bc_desc *bc,
@@ -760,6 +770,7 @@ static void case_init(or_case *k, const rt_mesh_desc *m, const rt_bc_desc *bc,
     k->m = m; k->bc = bc; k->mp = mp; k->ctl = ctl; k->s = s;
     k->nModes = 1; k->models = NULL; k->modes = NULL; k->modePerf = NULL;
     k->ddt = NULL; k->ddtC = 1.0; k->ddtCth = 1.0; k->Dth = NULL;
+    k->thermo = NULL;
     int nB = m->nBFaces;
     k->kU = (int *)xcalloc(nB, sizeof(int)); k->kP = (int *)xcalloc(nB, sizeof(int));
     k->kTh = (int *)xcalloc(nB, sizeof(int)); k->kTau = (int *)xcalloc(nB, sizeof(int));
@@ -857,6 +868,46 @@ static double xpp_f(const rt_model_params *mp, double trA, double trAA) {
     return ((2.0 * (mp->lambda / mp->lambdaS)) * exp((2.0 / mp->q) * (lam - 1.0))) * stretch +
            (1.0 / (lam * lam)) * (1.0 - al - (al / 3.0) * (trAA - 2.0 * trA));
 }
+/* ------------------------------------------------------------------------ */
+/* thermoFunctions: the temperature shift factor a(T) of a parameter        */
+/* ------------------------------------------------------------------------ */
+/* the factor each function multiplies its constant by at temperature T
+ * (thermoFunctions/<type>/<type>.C, multiply()): Constant.C:58-73 a = 1;
+ * Arrhenius.C:61-76 exp(alpha (1/T - 1/T0)); ArrheniusModified.C:61-76
+ * exp(-alpha (T - T0)); WLF.C:61-76 10^(-c1 (T - T0) / (c2 + (T - T0)));
+ * VFT.C:62-77 10^(B + A / (T - T0)) */
+double or_thermo_factor(const rt_thermo_fn *f, double T) {
+    switch (f->type) {
+    case RT_THERMO_ARRHENIUS: return exp(f->alpha * (1.0 / T - 1.0 / f->T0));
+    case RT_THERMO_ARRHENIUS_MODIFIED: return exp(-f->alpha * (T - f->T0));
+    case RT_THERMO_WLF: return pow(10.0, -f->c1 * (T - f->T0) / (f->c2 + (T - f->T0)));
+    case RT_THERMO_VFT: return pow(10.0, f->B + f->A / (T - f->T0));
+    default: return 1.0;
+    }
+}
+
+/* a mode's factors of n cells: lambda, the second relaxation time and etaP
+ * (out: 3 n, one array after the other) */
+void or_thermo_factors(const rt_thermo_desc *d, int n, const double *T, double *out) {
+    for (int c = 0; c < n; ++c) {
+        out[c] = or_thermo_factor(&d->lambda, T[c]);
+        out[n + c] = or_thermo_factor(&d->lambda2, T[c]);
+        out[2 * (size_t)n + c] = or_thermo_factor(&d->eta, T[c]);
+    }
+}
+
+/* the model of one cell with its relaxation times and etaP shifted
+ * (createField(lambda_) and createField(etaP_) of the Log models'
+ * correct(), e.g. Oldroyd_BLog.C:133-135; Rolie-Poly lambdaD / lambdaR and
+ * XPomPom lambdaB / lambdaS by their own functions, RoliePolyLog.C:139-141,
+ * XPomPomLog.C:140-142) */
+static void thermo_shift(rt_model_params *mc, const double *th, int N, int c) {
+    mc->lambda = mc->lambda * th[c];
+    mc->lambdaR = mc->lambdaR * th[N + c];
+    mc->lambdaS = mc->lambdaS * th[N + c];
+    mc->etaP = mc->etaP * th[2 * (size_t)N + c];
+}
+
 /* WhiteMetznerCY: the Carreau-Yasuda factor of etaP and lambda at the shear
  * rate sqrt(2) |symm(L)| (WhiteMetznerCYLog.C:152-161, m = n, L = K, b = a) */
 static double wmcy_factor(const rt_model_params *mp, const double *L) {
@@ -873,9 +924,10 @@ static double wmcy_factor(const rt_model_params *mp, const double *L) {
  * symm(Omega theta - theta Omega + 2B + S_model), for n cells (AoS: L and
  * eigVecs 9 a cell, eigVals 3, theta and rhs 6); fP receives the FENE-P/CR f
  * of the pre-solve conformation and WhiteMetznerCY's etaP/lambda */
-void or_theta_source(const rt_model_params *mp, int N, const double *L, const double *eigVecs,
-                     const double *eigVals, const double *theta, double *rhs, double *fP) {
-    const double lambda = mp->lambda, etaP = mp->etaP;
+static void theta_source(const rt_model_params *mp0, int N, const double *L, const double *eigVecs,
+                         const double *eigVals, const double *theta, double *rhs, double *fP,
+                         const double *th) {
+    const rt_model_params *mp = mp0;
     const double zeta = (mp->model == RT_MODEL_PTT_LOG) ? mp->zeta : 0.0;
     const int gen = mp->model == RT_MODEL_PTT_LOG && mp->pttFunction == RT_PTT_GENERALIZED;
     double *mlg = gen ? DALLOC((size_t)mp->maxIterMittagLeffler + 1) : NULL;
@@ -883,6 +935,11 @@ void or_theta_source(const rt_model_params *mp, int N, const double *L, const do
 
 #pragma omp parallel for num_threads(nthreads_) schedule(static)
     for (int c = 0; c < N; ++c) {
+        /* this cell's model: the temperature-shifted parameters, if any */
+        rt_model_params mc = *mp0;
+        if (th) thermo_shift(&mc, th, N, c);
+        const rt_model_params *mp = &mc;
+        const double lambda = mp->lambda, etaP = mp->etaP;
         t3 Lc, R, Lt, M;
         memcpy(Lc.a, L + 9 * (size_t)c, sizeof Lc.a);
         memcpy(R.a, eigVecs + 9 * (size_t)c, sizeof R.a);
@@ -979,15 +1036,26 @@ void or_theta_source(const rt_model_params *mp, int N, const double *L, const do
     free(mlg);
 }
 
+void or_theta_source(const rt_model_params *mp, int N, const double *L, const double *eigVecs,
+                     const double *eigVals, const double *theta, double *rhs, double *fP) {
+    theta_source(mp, N, L, eigVecs, eigVals, theta, rhs, fP, NULL);
+}
+
 /* tau of n cells from the post-solve eigen-decomposition (AoS) */
-void or_tau_cells(const rt_model_params *mp, int N, const double *eigVecs, const double *eigVals,
-                  const double *fP, double *tau) {
-    const double lambda = mp->lambda, etaP = mp->etaP;
+static void tau_cells(const rt_model_params *mp, int N, const double *eigVecs, const double *eigVals,
+                      const double *fP, double *tau, const double *th) {
     const double zeta = (mp->model == RT_MODEL_PTT_LOG) ? mp->zeta : 0.0;
-    double cP = etaP / lambda;
-    if (mp->model == RT_MODEL_PTT_LOG) cP = etaP / (lambda * (1.0 - zeta));
 #pragma omp parallel for num_threads(nthreads_) schedule(static)
     for (int c = 0; c < N; ++c) {
+        double lambda = mp->lambda, etaP = mp->etaP;
+        if (th) {
+            rt_model_params mc = *mp;
+            thermo_shift(&mc, th, N, c);
+            lambda = mc.lambda;
+            etaP = mc.etaP;
+        }
+        double cP = etaP / lambda;
+        if (mp->model == RT_MODEL_PTT_LOG) cP = etaP / (lambda * (1.0 - zeta));
         t3 R, Rt;
         memcpy(R.a, eigVecs + 9 * (size_t)c, sizeof R.a);
         Rt = t3_T(R);
@@ -1013,6 +1081,11 @@ void or_tau_cells(const rt_model_params *mp, int N, const double *eigVecs, const
     }
 }
 
+void or_tau_cells(const rt_model_params *mp, int N, const double *eigVecs, const double *eigVals,
+                  const double *fP, double *tau) {
+    tau_cells(mp, N, eigVecs, eigVals, fP, tau, NULL);
+}
+
 /* thetaOld: theta at the start of the time step (the inner iterations of a
  * step share it); NULL = the current theta */
 
@@ -1027,7 +1100,7 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
     else grad_vector(m, s->U, s->Ub, L);
     double *rhs = DALLOC(6 * (size_t)N);
     double *fP = DALLOC(N);   /* FENE-P/CR f of the pre-solve conformation; WhiteMetznerCY etaP/lambda */
-    or_theta_source(mp, N, L, s->eigVecs, s->eigVals, s->theta, rhs, fP);
+    theta_source(mp, N, L, s->eigVecs, s->eigVals, s->theta, rhs, fP, k->thermo);
 
     /* theta equation: ddt + GaussDefCmpw == rhs */
     or_matrix Mx;
@@ -1051,7 +1124,7 @@ static int constitutive_correct(or_case *k, const double *gradUin, rt_solver_per
 
     /* calcEig and tau */
     or_eig(N, s->theta, s->eigVals, s->eigVecs);
-    or_tau_cells(mp, N, s->eigVecs, s->eigVals, fP, s->tau);
+    tau_cells(mp, N, s->eigVecs, s->eigVals, fP, s->tau, k->thermo);
     tau_correct_bc(k);
 
     int st = RT_OK;
@@ -1186,6 +1259,7 @@ static int modes_correct(or_case *k, const double *gradU, rt_solver_perf *perf, 
         ki.s = &si;
         ki.nModes = 1;
         ki.Dth = k->Dth ? k->Dth + n6 * i : NULL;
+        ki.thermo = k->thermo ? k->thermo + 3 * (size_t)m->nCells * i : NULL;
         rt_solver_perf *pi = k->modePerf ? k->modePerf + 6 * i : perf;
         st = constitutive_correct(&ki, gradU, pi, theta0s ? theta0s + n6 * i : NULL);
         if (pi != perf) memcpy(perf, pi, 6 * sizeof *perf);
@@ -1677,6 +1751,34 @@ int or_constitutive_correct_modes(const rt_mesh_desc *m, const rt_bc_desc *bc, c
     return st;
 }
 
+/* correct() of a single- or multiMode model with temperature-dependent
+ * parameters: each mode's shift functions (thermo[nModes]) at the cell
+ * temperatures T, as the non-isothermal solvers call constEq.correct()
+ * (rheoHeatFoam.C:144,189); modes as or_constitutive_correct_modes. */
+int or_constitutive_correct_thermo(const rt_mesh_desc *m, const rt_bc_desc *bc, const rt_model_params *models,
+                                   int nModes, const rt_case_ctl *ctl, or_state *s, or_state *modes,
+                                   const double *gradU, const rt_thermo_desc *thermo, const double *T,
+                                   rt_solver_perf *modePerf) {
+    if (nModes < 1 || (nModes > 1 && !modes) || !thermo || !T) return RT_EINVAL;
+    const int N = m->nCells;
+    double *fac = DALLOC(3 * (size_t)N * nModes);
+    for (int i = 0; i < nModes; ++i) or_thermo_factors(&thermo[i], N, T, fac + 3 * (size_t)N * i);
+    or_case k;
+    case_init(&k, m, bc, &models[0], ctl, s);
+    k.thermo = fac;
+    int st;
+    if (nModes > 1) {
+        k.nModes = nModes; k.models = models; k.modes = modes; k.modePerf = modePerf;
+        rt_solver_perf last[6];
+        st = modes_correct(&k, gradU, last, NULL);
+    } else {
+        st = constitutive_correct(&k, gradU, modePerf, NULL);
+    }
+    case_free(&k);
+    free(fac);
+    return st;
+}
+
 /* Initial phi = flux(U) (createPhi) and boundary values of U/p/theta/tau. */
 void or_init_fields(const rt_mesh_desc *m, const rt_bc_desc *bc, or_state *s) {
     int nB = m->nBFaces;
@@ -1716,4 +1818,5 @@ void or_abi_sizes(int *out) {
     out[4] = (int)sizeof(rt_solver_perf);
     out[5] = (int)sizeof(rt_case_ctl);
     out[6] = (int)sizeof(rt_step_perf);
+    out[7] = (int)sizeof(rt_thermo_desc);
 }

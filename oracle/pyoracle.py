@@ -86,6 +86,13 @@ def lib():
                                                   C.c_int, P(abi.rt_case_ctl), P(or_state), P(or_state), _dp, C.c_int,
                                                   P(abi.rt_solver_perf), P(or_ddt)]
         L.or_constitutive_correct_ddt.restype = C.c_int
+        L.or_thermo_factor.argtypes = [P(abi.rt_thermo_fn), C.c_double]
+        L.or_thermo_factor.restype = C.c_double
+        L.or_thermo_factors.argtypes = [P(abi.rt_thermo_desc), C.c_int, _dp, _dp]
+        L.or_constitutive_correct_thermo.argtypes = [P(abi.rt_mesh_desc), P(abi.rt_bc_desc), P(abi.rt_model_params),
+                                                     C.c_int, P(abi.rt_case_ctl), P(or_state), P(or_state), _dp,
+                                                     P(abi.rt_thermo_desc), _dp, P(abi.rt_solver_perf)]
+        L.or_constitutive_correct_thermo.restype = C.c_int
         _lib = L
     return _lib
 
@@ -179,13 +186,29 @@ class Oracle:
             for name in ("theta", "thetab", "eigVals", "eigVecs"):
                 getattr(self.f, name)[...] = getattr(m0, name)
 
-    def constitutive_correct(self, gradU: np.ndarray = None, thetaOld: np.ndarray = None, newTimeStep=None):
+    def constitutive_correct(self, gradU: np.ndarray = None, thetaOld: np.ndarray = None, newTimeStep=None,
+                             T: np.ndarray = None):
         """One correct(); thetaOld (nCells, 6): the old-time theta of the
         theta equation (an inner iteration of a step that started there),
-        default the current theta."""
+        default the current theta.  T (nCells): cell temperatures for the
+        modes' thermo functions (a non-isothermal solver's correct())."""
         perf = (abi.rt_solver_perf * 6)()
         g = None if gradU is None else np.ascontiguousarray(gradU, dtype=np.float64)
         gp = None if g is None else g.ctypes.data_as(_dp)
+        if T is not None:
+            if self.cn or thetaOld is not None:
+                raise ValueError("temperature-dependent correct(): Euler, one call a step")
+            t = np.ascontiguousarray(T, dtype=np.float64)
+            modes = _mode_states(self.f) if self.nModes > 1 else None
+            st = lib().or_constitutive_correct_thermo(C.byref(self.md), C.byref(self.bd), self.models, self.nModes,
+                                                      C.byref(self.ctl), C.byref(_state(self.f)), modes, gp,
+                                                      self.case.thermo_descs(), t.ctypes.data_as(_dp),
+                                                      self.modePerf)
+            if st != 0:
+                raise RuntimeError(f"oracle constitutive correct failed: {st}")
+            if self.nModes > 1:
+                self._mode0_view()
+            return list(self.modePerf[6 * (self.nModes - 1):])
         if self.cn:
             # Crank-Nicolson: a time step of its own unless newTimeStep is
             # False (a further inner iteration, against the theta kept at the

@@ -95,6 +95,27 @@ class rt_model_params(C.Structure):
     ]
 
 
+RT_THERMO_CONSTANT = 0
+RT_THERMO_ARRHENIUS = 1
+RT_THERMO_ARRHENIUS_MODIFIED = 2
+RT_THERMO_WLF = 3
+RT_THERMO_VFT = 4
+THERMO_TYPES = {"Constant": RT_THERMO_CONSTANT, "Arrhenius": RT_THERMO_ARRHENIUS,
+                "ArrheniusModified": RT_THERMO_ARRHENIUS_MODIFIED, "WLF": RT_THERMO_WLF, "VFT": RT_THERMO_VFT}
+
+
+class rt_thermo_fn(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("pad_", C.c_int32),
+        ("alpha", C.c_double), ("T0", C.c_double), ("c1", C.c_double), ("c2", C.c_double),
+        ("A", C.c_double), ("B", C.c_double),
+    ]
+
+
+class rt_thermo_desc(C.Structure):
+    _fields_ = [("lambda_", rt_thermo_fn), ("lambda2", rt_thermo_fn), ("eta", rt_thermo_fn)]
+
+
 class rt_solver_ctl(C.Structure):
     _fields_ = [
         ("solver", C.c_int32), ("preconditioner", C.c_int32),
@@ -183,6 +204,7 @@ def load_library(path: str = LIBNAME):
         "rt_residual_noalloc": ([vp, vp, vp, vp, vp, vp, _dp], C.c_int32),
         "rt_constitutive_correct": ([vp, _dp, P(rt_solver_perf)], C.c_int32),
         "rt_constitutive_correct_iter": ([vp, _dp, C.c_int32, P(rt_solver_perf)], C.c_int32),
+        "rt_set_temperature": ([vp, P(rt_thermo_desc), _dp], C.c_int32),
         "rt_step": ([vp, C.c_int32, P(rt_step_perf)], C.c_int32),
         "rt_op_grad": ([vp, _dp, _dp, _dp], C.c_int32),
         "rt_op_eig": ([vp, C.c_int32, _dp, _dp, _dp], C.c_int32),

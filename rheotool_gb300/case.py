@@ -47,6 +47,44 @@ class SolverControl:
 
 
 @dataclass
+class ThermoFunction:
+    """One ``thermoFunction`` sub-dictionary of a model (``thermoLambda``,
+    ``thermoEta``, ...; rheoTool's thermoFunctions/<type>): ``type`` one of
+    Constant, Arrhenius (alpha, T0), ArrheniusModified (alpha, T0), WLF (c1,
+    c2, T0), VFT (A, B, T0).  A model without the sub-dictionary has the
+    Constant function (thermoFunctions/newThermoFunction.C:41)."""
+    type: str = "Constant"
+    alpha: float = 0.0
+    T0: float = 0.0
+    c1: float = 0.0
+    c2: float = 0.0
+    A: float = 0.0
+    B: float = 0.0
+
+    def to_c(self) -> abi.rt_thermo_fn:
+        if self.type not in abi.THERMO_TYPES:
+            raise ValueError(f"Unknown thermoFunction type {self.type}; valid: {sorted(abi.THERMO_TYPES)}")
+        return abi.rt_thermo_fn(abi.THERMO_TYPES[self.type], 0, self.alpha, self.T0, self.c1, self.c2,
+                                self.A, self.B)
+
+    def factor(self, T: np.ndarray) -> np.ndarray:
+        """The shift factor at temperatures T (the formulas the library and
+        the oracle evaluate; for host-side checks)."""
+        T = np.asarray(T, dtype=np.float64)
+        if self.type == "Arrhenius":
+            return np.exp(self.alpha * (1.0 / T - 1.0 / self.T0))
+        if self.type == "ArrheniusModified":
+            return np.exp(-self.alpha * (T - self.T0))
+        if self.type == "WLF":
+            return 10.0 ** (-self.c1 * (T - self.T0) / (self.c2 + (T - self.T0)))
+        if self.type == "VFT":
+            return 10.0 ** (self.B + self.A / (T - self.T0))
+        if self.type == "Constant":
+            return np.ones_like(T)
+        raise ValueError(f"Unknown thermoFunction type {self.type}")
+
+
+@dataclass
 class Model:
     type: str = "Oldroyd-BLog"
     rho: float = 1.0
@@ -70,6 +108,15 @@ class Model:
     maxIterMittagLeffler: int = 200
     stabilization: str = "coupling"
     destructionFunctionType: str = "linear"
+    # non-isothermal parameter shifts: thermoLambda (Rolie-Poly thermoLambdaD,
+    # XPomPom thermoLambdaB), the second relaxation time's (Rolie-Poly
+    # thermoLambdaR, XPomPom thermoLambdaS) and thermoEta
+    thermoLambda: ThermoFunction = field(default_factory=ThermoFunction)
+    thermoLambda2: ThermoFunction = field(default_factory=ThermoFunction)
+    thermoEta: ThermoFunction = field(default_factory=ThermoFunction)
+
+    def thermo_c(self) -> abi.rt_thermo_desc:
+        return abi.rt_thermo_desc(self.thermoLambda.to_c(), self.thermoLambda2.to_c(), self.thermoEta.to_c())
 
     def to_c(self) -> abi.rt_model_params:
         if self.type not in abi.MODEL_NAMES:
@@ -118,6 +165,14 @@ class Case:
     def models(self) -> List[Model]:
         """The modes of the constitutive model (one for a single-mode model)."""
         return [self.model] + list(self.moreModes)
+
+    def thermo_descs(self):
+        """ctypes array of every mode's rt_thermo_desc."""
+        ms = self.models
+        arr = (abi.rt_thermo_desc * len(ms))()
+        for i, m in enumerate(ms):
+            arr[i] = m.thermo_c()
+        return arr
 
     def mode_params(self):
         """ctypes array of every mode's rt_model_params."""

@@ -100,14 +100,66 @@ void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double 
     launch_count(ctx);
 }
 
+// ---- temperature-dependent parameters (rt_set_temperature) ----------------
+// The shift factor of a thermoFunction at temperature T (thermoFunctions/
+// <type>/<type>.C, multiply()): Constant 1; Arrhenius exp(alpha (1/T -
+// 1/T0)); ArrheniusModified exp(-alpha (T - T0)); WLF 10^(-c1 (T - T0) /
+// (c2 + (T - T0))); VFT 10^(B + A / (T - T0)).
+__device__ double thermo_factor(const rt_thermo_fn &f, double T) {
+    switch (f.type) {
+    case RT_THERMO_ARRHENIUS: return exp(f.alpha * (1.0 / T - 1.0 / f.T0));
+    case RT_THERMO_ARRHENIUS_MODIFIED: return exp(-f.alpha * (T - f.T0));
+    case RT_THERMO_WLF: return pow(10.0, -f.c1 * (T - f.T0) / (f.c2 + (T - f.T0)));
+    case RT_THERMO_VFT: return pow(10.0, f.B + f.A / (T - f.T0));
+    default: return 1.0;
+    }
+}
+
+// one mode's factors: lambda, the second relaxation time, etaP (3 N)
+__global__ void k_thermo_factors(int N, rt_thermo_desc d, const double *__restrict__ T, double *__restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const double t = T[c];
+    out[c] = thermo_factor(d.lambda, t);
+    out[(size_t)N + c] = thermo_factor(d.lambda2, t);
+    out[(size_t)2 * N + c] = thermo_factor(d.eta, t);
+}
+
+// a cell's model with its relaxation times and etaP shifted (the Log
+// models' createField(lambda_), createField(etaP_): Oldroyd_BLog.C:133-135;
+// Rolie-Poly lambdaD / lambdaR, XPomPom lambdaB / lambdaS by their own
+// functions: RoliePolyLog.C:139-141, XPomPomLog.C:140-142)
+__device__ __forceinline__ void thermo_shift(rt_model_params &m, const double *__restrict__ th, int N, int c) {
+    m.lambda = m.lambda * th[c];
+    m.lambdaR = m.lambdaR * th[(size_t)N + c];
+    m.lambdaS = m.lambdaS * th[(size_t)N + c];
+    m.etaP = m.etaP * th[(size_t)2 * N + c];
+}
+
+void thermo_factors(rt_ctx *ctx, const rt_thermo_desc &d, const double *T, double *out) {
+    const int N = ctx->mesh.N;
+    k_thermo_factors<<<nblocks(N), RT_BLOCK, 0, ctx->stream>>>(N, d, T, out);
+    RT_CHECK_LAUNCH();
+    launch_count(ctx);
+}
+
+// th: the shift factors (3 N) or null
 __global__ void k_theta_rhs(int N, rt_model_params mp, const int *__restrict__ caseOf,
                             const rt_model_params *__restrict__ cp, const double *__restrict__ L,
                             const double *__restrict__ Rv, const double *__restrict__ evv,
                             const double *__restrict__ theta, double *__restrict__ rhs,
-                            double *__restrict__ fP, const double *__restrict__ mlg, int mlK) {
+                            double *__restrict__ fP, const double *__restrict__ mlg, int mlK,
+                            const double *__restrict__ th) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
-    theta_rhs_cell(c, N, caseOf ? cp[caseOf[c]] : mp, L, Rv, evv, theta, rhs, fP, mlg, mlK);
+    const rt_model_params &m0 = caseOf ? cp[caseOf[c]] : mp;
+    if (th) {
+        rt_model_params m = m0;
+        thermo_shift(m, th, N, c);
+        theta_rhs_cell(c, N, m, L, Rv, evv, theta, rhs, fP, mlg, mlK);
+    } else {
+        theta_rhs_cell(c, N, m0, L, Rv, evv, theta, rhs, fP, mlg, mlK);
+    }
 }
 
 // theta matrix: diag = rDeltaT V + diagC; source = rDeltaT theta0 V + srcC + V rhs;
@@ -145,10 +197,17 @@ __global__ void k_theta_assemble(MeshView m, double rDeltaT, const double *__res
 __global__ void k_tau(int N, rt_model_params mp, const int *__restrict__ caseOf,
                       const rt_model_params *__restrict__ cp, const double *__restrict__ Rv,
                       const double *__restrict__ evv, const double *__restrict__ fP,
-                      double *__restrict__ tau) {
+                      double *__restrict__ tau, const double *__restrict__ th) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
-    tau_cell(c, N, caseOf ? cp[caseOf[c]] : mp, Rv, evv, fP, tau);
+    const rt_model_params &m0 = caseOf ? cp[caseOf[c]] : mp;
+    if (th) {
+        rt_model_params m = m0;
+        thermo_shift(m, th, N, c);
+        tau_cell(c, N, m, Rv, evv, fP, tau);
+    } else {
+        tau_cell(c, N, m0, Rv, evv, fP, tau);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -246,14 +305,12 @@ __global__ void k_eig_mixed(int n, const double *__restrict__ theta, double *__r
     for (int i = 0; i < 9; ++i) vec[(size_t)i * n + c] = V[i];
 }
 
-__global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restrict__ caseOf,
-                                  const rt_model_params *__restrict__ cp, const double *__restrict__ L,
-                                  const double *__restrict__ Rv, const double *__restrict__ evv,
-                                  const double *__restrict__ theta, double *__restrict__ rhs,
-                                  double *__restrict__ fP, const double *__restrict__ mlg, int mlK) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= N) return;
-    const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
+__device__ __forceinline__ void theta_rhs_mixed_cell(int c, int N, const rt_model_params &mp,
+                                                     const double *__restrict__ L, const double *__restrict__ Rv,
+                                                     const double *__restrict__ evv,
+                                                     const double *__restrict__ theta, double *__restrict__ rhs,
+                                                     double *__restrict__ fP, const double *__restrict__ mlg,
+                                                     int mlK) {
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
     if (mixed_fp64_model(mp) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         theta_rhs_cell(c, N, mp, L, Rv, evv, theta, rhs, fP, mlg, mlK);
@@ -342,13 +399,27 @@ __global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restr
     rhs[(size_t)5 * N + c] = Ts.a[8];
 }
 
-__global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ caseOf,
-                            const rt_model_params *__restrict__ cp, const double *__restrict__ Rv,
-                            const double *__restrict__ evv, const double *__restrict__ fP,
-                            double *__restrict__ tau) {
+__global__ void k_theta_rhs_mixed(int N, rt_model_params mp0, const int *__restrict__ caseOf,
+                                  const rt_model_params *__restrict__ cp, const double *__restrict__ L,
+                                  const double *__restrict__ Rv, const double *__restrict__ evv,
+                                  const double *__restrict__ theta, double *__restrict__ rhs,
+                                  double *__restrict__ fP, const double *__restrict__ mlg, int mlK,
+                                  const double *__restrict__ th) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
-    const rt_model_params &mp = caseOf ? cp[caseOf[c]] : mp0;
+    const rt_model_params &m0 = caseOf ? cp[caseOf[c]] : mp0;
+    if (th) {
+        rt_model_params m = m0;
+        thermo_shift(m, th, N, c);
+        theta_rhs_mixed_cell(c, N, m, L, Rv, evv, theta, rhs, fP, mlg, mlK);
+    } else {
+        theta_rhs_mixed_cell(c, N, m0, L, Rv, evv, theta, rhs, fP, mlg, mlK);
+    }
+}
+
+__device__ __forceinline__ void tau_mixed_cell(int c, int N, const rt_model_params &mp,
+                                               const double *__restrict__ Rv, const double *__restrict__ evv,
+                                               const double *__restrict__ fP, double *__restrict__ tau) {
     const double e0 = evv[c], e1 = evv[N + c], e2 = evv[2 * N + c];
     if (mixed_fp64_model(mp) || !mix_fp32_ok(log(e0), log(e1), log(e2))) {
         tau_cell(c, N, mp, Rv, evv, fP, tau);
@@ -375,6 +446,22 @@ __global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ 
     tau[(size_t)3 * N + c] = cP * (double)T.a[4];
     tau[(size_t)4 * N + c] = cP * (double)(0.5f * (T.a[5] + T.a[7]));
     tau[(size_t)5 * N + c] = cP * (double)T.a[8];
+}
+
+__global__ void k_tau_mixed(int N, rt_model_params mp0, const int *__restrict__ caseOf,
+                            const rt_model_params *__restrict__ cp, const double *__restrict__ Rv,
+                            const double *__restrict__ evv, const double *__restrict__ fP,
+                            double *__restrict__ tau, const double *__restrict__ th) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const rt_model_params &m0 = caseOf ? cp[caseOf[c]] : mp0;
+    if (th) {
+        rt_model_params m = m0;
+        thermo_shift(m, th, N, c);
+        tau_mixed_cell(c, N, m, Rv, evv, fP, tau);
+    } else {
+        tau_mixed_cell(c, N, m0, Rv, evv, fP, tau);
+    }
 }
 
 // linearExtrapolation: val = tau_P + grad(tau)_P . (Cf - C_P) for the faces
@@ -498,16 +585,19 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
     double *dS = W.take(N), *bS = W.take(6 * (size_t)N);
     double *val = W.take(6 * (size_t)NB + 6);
     const MeshView mv = view(mesh);
+    // the shift factors of this mode (rt_set_temperature), or none
+    const double *th = cs.thermoOn ? cs.thermo.p : nullptr;
 
     {
         ProfScope ps(ctx, "theta_rhs", (double)N * (72.0 + 72.0 + 24.0 + 48.0 + 48.0));
         if (cs.ctl.precision == RT_PREC_MIXED && (ctx->mixedParts & 2))
             k_theta_rhs_mixed<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, G, cs.eigVecs.p,
                                                               cs.eigVals.p, cs.theta.p, rhs, fP, cs.mlGamma.p,
-                                                              cs.mlK);
+                                                              cs.mlK, th);
         else
             k_theta_rhs<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, G, cs.eigVecs.p,
-                                                        cs.eigVals.p, cs.theta.p, rhs, fP, cs.mlGamma.p, cs.mlK);
+                                                        cs.eigVals.p, cs.theta.p, rhs, fP, cs.mlGamma.p, cs.mlK,
+                                                        th);
         RT_CHECK_LAUNCH();
     }
     // (Crank-Nicolson: the old-time theta is the one taken at the step's start)
@@ -552,10 +642,10 @@ rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf 
         ProfScope ps(ctx, "tau", (double)N * (72.0 + 24.0 + 48.0));
         if (cs.ctl.precision == RT_PREC_MIXED && (ctx->mixedParts & 2))
             k_tau_mixed<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, cs.eigVecs.p,
-                                                        cs.eigVals.p, fP, cs.tau.p);
+                                                        cs.eigVals.p, fP, cs.tau.p, th);
         else
             k_tau<<<nblocks(N), RT_BLOCK, 0, s>>>(N, cs.mp, mv.caseOf, mv.caseParams, cs.eigVecs.p, cs.eigVals.p,
-                                                  fP, cs.tau.p);
+                                                  fP, cs.tau.p, th);
         RT_CHECK_LAUNCH();
         launch_count(ctx);
         tau_correct_bc(ctx, val);

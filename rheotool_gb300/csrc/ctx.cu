@@ -349,6 +349,7 @@ rt_status rt_mesh_upload(rt_ctx *ctx, const rt_mesh_desc *md) {
         RT_CUDA(cudaStreamSynchronize(s));
         ctx->meshReady = true;
         ctx->cs.ready = false;
+        ctx->cs.thermoOn = false;
         return RT_OK;
     });
 }
@@ -634,6 +635,7 @@ rt_status rt_case_setup(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_params
         c.eigVecs.alloc(9 * (size_t)N);
         init_fields(ctx);
         RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        c.thermoOn = false;   // a new case is isothermal until rt_set_temperature
         c.ready = true;
         return RT_OK;
     });
@@ -827,6 +829,7 @@ rt_status rt_case_setup_modes(rt_ctx *ctx, const rt_bc_desc *bc, const rt_model_
             RT_CUDA(cudaStreamSynchronize(s));
         }
         RT_CUDA(cudaStreamSynchronize(s));
+        c.thermoOn = false;   // a new case is isothermal until rt_set_temperature
         c.ready = true;
         return RT_OK;
     });
@@ -964,10 +967,64 @@ rt_status rt_constitutive_correct_iter(rt_ctx *ctx, const double *gradU, int32_t
     });
 }
 
+// rheoHeatFoam's constEq.correct() (rheoHeatFoam.C:144,189): the cell
+// temperatures and each mode's thermoFunctions give per-cell factors of the
+// relaxation times and etaP, computed here on the device; constitutive_correct
+// applies them while thermoOn
+rt_status rt_set_temperature(rt_ctx *ctx, const rt_thermo_desc *modes, const double *T) {
+    return guarded(ctx, [&]() -> rt_status {
+        DevCase &c = ctx->cs;
+        RT_REQUIRE(c.ready, RT_ENOTREADY, "case not set up");
+        if (!T) {
+            c.thermoOn = false;
+            return RT_OK;
+        }
+        RT_REQUIRE(modes, RT_EINVAL, "null thermoFunction descriptors");
+        RT_REQUIRE(ctx->mesh.batch.n <= 1, RT_EINVAL, "temperature-dependent parameters: not in the batched form");
+        const int N = ctx->mesh.N;
+        for (int i = 0; i < c.nModes; ++i) {
+            const rt_thermo_fn *fns[3] = {&modes[i].lambda, &modes[i].lambda2, &modes[i].eta};
+            for (const rt_thermo_fn *f : fns) {
+                RT_REQUIRE(f->type >= RT_THERMO_CONSTANT && f->type <= RT_THERMO_VFT, RT_EINVAL,
+                           "unknown thermoFunction type " + std::to_string(f->type));
+                RT_REQUIRE(f->type != RT_THERMO_ARRHENIUS || f->T0 > 0, RT_EINVAL, "Arrhenius needs T0 > 0");
+            }
+        }
+        for (int cell = 0; cell < N; ++cell) {
+            const double t = T[cell];
+            RT_REQUIRE(std::isfinite(t), RT_EINVAL, "temperature of cell " + std::to_string(cell) + " is not finite");
+            for (int i = 0; i < c.nModes; ++i) {
+                const rt_thermo_fn *fns[3] = {&modes[i].lambda, &modes[i].lambda2, &modes[i].eta};
+                for (const rt_thermo_fn *f : fns) {
+                    const bool ok = (f->type == RT_THERMO_ARRHENIUS) ? t > 0
+                                    : (f->type == RT_THERMO_WLF)     ? f->c2 + (t - f->T0) != 0.0
+                                    : (f->type == RT_THERMO_VFT)     ? t - f->T0 != 0.0
+                                                                     : true;
+                    RT_REQUIRE(ok, RT_EINVAL,
+                               "temperature of cell " + std::to_string(cell) + " outside a thermoFunction's domain");
+                }
+            }
+        }
+        c.Tcell.alloc((size_t)N);
+        RT_CUDA(cudaMemcpyAsync(c.Tcell.p, T, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream));
+        for (int i = 0; i < c.nModes; ++i) {
+            DBuf<double> &out = i == 0 ? c.thermo : c.modes[i - 1]->thermo;
+            out.alloc(3 * (size_t)N);
+            thermo_factors(ctx, modes[i], c.Tcell.p, out.p);
+        }
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        c.thermoOn = true;
+        return RT_OK;
+    });
+}
+
 rt_status rt_step(rt_ctx *ctx, int32_t nSteps, rt_step_perf *perf) {
     return guarded(ctx, [&]() -> rt_status {
         RT_REQUIRE(ctx->cs.ready, RT_ENOTREADY, "case not set up");
         RT_REQUIRE(nSteps >= 0, RT_EINVAL, "nSteps must be >= 0");
+        RT_REQUIRE(!ctx->cs.thermoOn, RT_EINVAL,
+                   "a temperature is set: the momentum equation's temperature-dependent viscosities are not "
+                   "built, so temperature-dependent parameters apply to rt_constitutive_correct only");
         rt_step_perf local{};
         rt_status st = RT_OK;
         // the steps advance theta: an old-time theta kept by
@@ -1163,6 +1220,7 @@ rt_status rt_batch_layout(rt_ctx *ctx, int32_t nCases, const int32_t *cellStart,
         b.n = n;
         ctx->batchPerf.assign(n, rt_step_perf{});
         ctx->cs.ready = false;
+        ctx->cs.thermoOn = false;
         return RT_OK;
     });
 }

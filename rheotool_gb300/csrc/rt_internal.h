@@ -358,12 +358,17 @@ struct DevCase {
     int ddtSteps = 0, ddtThSteps = 0;
     double ddtC = 1.0, ddtCth = 1.0;
     DBuf<double> DU, DUb, Dphi, Dphib, Us, Ubs, phis, phibs, Dth, ths;
+    // temperature-dependent parameters (rt_set_temperature): thermoOn, the
+    // cell temperatures, and this mode's shift factors (3 nCells: lambda, the
+    // second relaxation time, etaP; the other modes' in ModeState)
+    bool thermoOn = false;
+    DBuf<double> Tcell, thermo;
 };
 
 // one further mode of a multiMode model: the DevCase's per-mode members
 struct ModeState {
     rt_model_params mp{};
-    DBuf<double> theta, thetab, tau, taub, eigVals, eigVecs, thetaOld, mlGamma, Dth, ths;
+    DBuf<double> theta, thetab, tau, taub, eigVals, eigVecs, thetaOld, mlGamma, Dth, ths, thermo;
     bool thetaOldSaved = false;
     int mlK = 0;
 };
@@ -391,6 +396,7 @@ struct ModeSwap {
         swap_buf(c.mlGamma, m.mlGamma);
         swap_buf(c.Dth, m.Dth);
         swap_buf(c.ths, m.ths);
+        swap_buf(c.thermo, m.thermo);
         std::swap(c.thetaOldSaved, m.thetaOldSaved);
         std::swap(c.mlK, m.mlK);
     }
@@ -525,6 +531,9 @@ void launch_count(rt_ctx *ctx, int n = 1);
 
 // constitutive.cu
 void eig_cells(rt_ctx *ctx, int n, const double *theta, double *eigVals, double *eigVecs);
+// one mode's shift factors of the relaxation times and etaP (3 N: lambda,
+// the second relaxation time, etaP) at the device cell temperatures T
+void thermo_factors(rt_ctx *ctx, const rt_thermo_desc &d, const double *T, double *out);
 // thetaOld: theta at the start of the time step (shared by its inner
 // iterations); null = the current theta
 rt_status constitutive_correct(rt_ctx *ctx, const double *gradU, rt_solver_perf *perf,

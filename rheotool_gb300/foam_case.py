@@ -51,7 +51,7 @@ from typing import Any, Dict, List, Optional, Tuple
 import numpy as np
 
 from . import abi, foam_io
-from .case import Case, Fields, Model, SolverControl
+from .case import Case, Fields, Model, SolverControl, ThermoFunction
 
 # ---------------------------------------------------------------------------
 # dictionaries
@@ -163,10 +163,17 @@ MODEL_KEYS = {
     "WhiteMetznerCYLog": ("m", "n", "K", "L", "a", "b"),
 }
 # the temperature functions each model builds (thermoFunction::New)
+# each model's thermoFunction sub-dictionaries: (lambda, second relaxation
+# time, etaP) (Oldroyd_BLog.C:118-119, RoliePolyLog.C:122-124,
+# XPomPomLog.C:123-125)
 THERMO_KEYS = {
-    "Rolie-PolyLog": ("thermoEta", "thermoLambdaD", "thermoLambdaR"),
-    "XPomPomLog": ("thermoEta", "thermoLambdaS", "thermoLambdaB"),
+    "Rolie-PolyLog": ("thermoLambdaD", "thermoLambdaR", "thermoEta"),
+    "XPomPomLog": ("thermoLambdaB", "thermoLambdaS", "thermoEta"),
 }
+# the keywords of each thermoFunction type (thermoFunctions/<type>/<type>.C
+# constructors)
+THERMO_ARGS = {"Constant": (), "Arrhenius": ("alpha", "T0"), "ArrheniusModified": ("alpha", "T0"),
+               "WLF": ("c1", "c2", "T0"), "VFT": ("A", "B", "T0")}
 
 
 class CaseError(ValueError):
@@ -270,11 +277,22 @@ def read_model(par: Dict[str, Any]) -> Model:
             if scalar(par[x]) != scalar(par[y]):
                 raise CaseError("The Log version of the WhiteMetznerCY model can only be used if m=n and K=L and "
                                 "a=b; use the stress version (WhiteMetznerCY)")
-    for th in THERMO_KEYS.get(typ, ("thermoEta", "thermoLambda")):
-        # thermoFunction::New: no sub-dictionary means the Constant (isothermal) function
-        t = par.get(th)
-        if isinstance(t, dict) and t.get("type", "Constant") != "Constant":
-            raise CaseError(f"{th} type {t.get('type')}: only the Constant thermoFunction is implemented")
+    names = THERMO_KEYS.get(typ, ("thermoLambda", None, "thermoEta"))
+    for attr, th in zip(("thermoLambda", "thermoLambda2", "thermoEta"), names):
+        # thermoFunction::New (newThermoFunction.C:33-61): no sub-dictionary
+        # means the Constant (isothermal) function
+        t = par.get(th) if th else None
+        if not isinstance(t, dict):
+            continue
+        ttype = t.get("type")
+        if ttype not in THERMO_ARGS:
+            raise CaseError(f"Unknown thermoFunction type {ttype} ({th}); valid: {sorted(THERMO_ARGS)}")
+        args = {}
+        for key in THERMO_ARGS[ttype]:
+            if key not in t:
+                raise CaseError(f"keyword {key} is undefined in {th}")
+            args[key] = scalar(t[key])
+        mkw[attr] = ThermoFunction(ttype, **args)
     if "destructionFunctionType" in par:
         mkw["destructionFunctionType"] = par["destructionFunctionType"]
         dft = par["destructionFunctionType"]
@@ -296,7 +314,7 @@ def read_model(par: Dict[str, Any]) -> Model:
 
 def load_case(case_dir: str, substitute: bool = False,
               bc_overrides: Optional[Dict[str, Dict[str, Tuple[str, Any]]]] = None,
-              precision: int = abi.RT_PREC_FP64) -> LoadedCase:
+              precision: int = abi.RT_PREC_FP64, thermo: bool = False) -> LoadedCase:
     subs: List[str] = []
     mesh = foam_io.read_polymesh(case_dir)
     q = foam_io.mesh_quality(mesh)
@@ -310,6 +328,17 @@ def load_case(case_dir: str, substitute: bool = False,
     cp = read_dict(os.path.join(case_dir, "constant", "constitutiveProperties"))
     mode_names, models = read_mode_entries(cp.get("parameters", cp))
     model = models[0]
+    if not thermo:
+        # rheoFoam has no temperature field: a thermoFunction other than
+        # Constant needs the non-isothermal solver's T (thermoFunctions look it
+        # up in the mesh, e.g. Arrhenius.C:56)
+        for m in models:
+            for attr in ("thermoLambda", "thermoLambda2", "thermoEta"):
+                f = getattr(m, attr)
+                if f.type != "Constant":
+                    raise CaseError(f"{attr} type {f.type}: rheoFoam has no temperature field T (load with "
+                                    "thermo=True and give T to Context.set_temperature for constitutive "
+                                    "corrections)")
 
     sol = read_dict(os.path.join(case_dir, "system", "fvSolution"))
     solvers = sol.get("solvers", {})

@@ -172,10 +172,19 @@ public:
     std::vector<SolverPerformance> correctIter(Context &ctx, bool newTimeStep, const double *gradU = nullptr) const;
     // tau (6 nCells AoS) and its boundary values (6 nBFaces, may be null)
     void tau(Context &ctx, double *internal, double *boundary = nullptr) const;
+    // the model's thermoFunctions (thermoLambda / thermoLambdaD / thermoLambdaB,
+    // thermoLambdaR / thermoLambdaS, thermoEta sub-dictionaries; Constant
+    // where a sub-dictionary is absent)
+    const rt_thermo_desc &thermo() const { return thermo_; }
+    // the cell temperatures (nCells) the next correct() calls shift the
+    // relaxation times and etaP by, as in a non-isothermal solver; null:
+    // isothermal (rt_set_temperature, single-mode models)
+    void setTemperature(Context &ctx, const double *T) const;
 
 private:
     std::string name_, type_;
     rt_model_params mp_{};
+    rt_thermo_desc thermo_{};
 };
 
 }  // namespace rheogpu

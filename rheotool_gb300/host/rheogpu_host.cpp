@@ -261,6 +261,37 @@ const std::vector<std::string> &ConstitutiveEq::types() {
     return v;
 }
 
+// thermoFunction::New (thermoFunctions/newThermoFunction.C:33-61): the
+// sub-dictionary `name` of the model's dictionary selects the type; without
+// it the function is Constant
+static rt_thermo_fn thermo_function(const Dictionary &d, const std::string &name) {
+    rt_thermo_fn f{};
+    f.type = RT_THERMO_CONSTANT;
+    if (!d.isDict(name)) return f;
+    const Dictionary &t = d.subDict(name);
+    const std::string type = t.lookup("type");
+    if (type == "Constant") return f;
+    if (type == "Arrhenius" || type == "ArrheniusModified") {
+        f.type = type == "Arrhenius" ? RT_THERMO_ARRHENIUS : RT_THERMO_ARRHENIUS_MODIFIED;
+        f.alpha = t.lookupScalar("alpha");
+        f.T0 = t.lookupScalar("T0");
+    } else if (type == "WLF") {
+        f.type = RT_THERMO_WLF;
+        f.c1 = t.lookupScalar("c1");
+        f.c2 = t.lookupScalar("c2");
+        f.T0 = t.lookupScalar("T0");
+    } else if (type == "VFT") {
+        f.type = RT_THERMO_VFT;
+        f.A = t.lookupScalar("A");
+        f.B = t.lookupScalar("B");
+        f.T0 = t.lookupScalar("T0");
+    } else {
+        throw FatalError(valid_list("thermoFunction type", type,
+                                    {"Arrhenius", "ArrheniusModified", "Constant", "VFT", "WLF"}));
+    }
+    return f;
+}
+
 std::unique_ptr<ConstitutiveEq> ConstitutiveEq::New(const std::string &name, const Dictionary &d) {
     const std::string type = d.lookup("type");
     std::unique_ptr<ConstitutiveEq> ce(new ConstitutiveEq());
@@ -325,6 +356,19 @@ std::unique_ptr<ConstitutiveEq> ConstitutiveEq::New(const std::string &name, con
         }
     }
     if (mp.model == RT_MODEL_FENEP_LOG || mp.model == RT_MODEL_FENECR_LOG) mp.L2 = d.lookupScalar("L2");
+    // the thermoFunctions of the relaxation times and etaP, by the names each
+    // Log model gives them (Oldroyd_BLog.C:118-119, RoliePolyLog.C:122-124,
+    // XPomPomLog.C:123-125)
+    if (mp.model == RT_MODEL_ROLIEPOLY_LOG) {
+        ce->thermo_.lambda = thermo_function(d, "thermoLambdaD");
+        ce->thermo_.lambda2 = thermo_function(d, "thermoLambdaR");
+    } else if (mp.model == RT_MODEL_XPOMPOM_LOG) {
+        ce->thermo_.lambda = thermo_function(d, "thermoLambdaB");
+        ce->thermo_.lambda2 = thermo_function(d, "thermoLambdaS");
+    } else {
+        ce->thermo_.lambda = thermo_function(d, "thermoLambda");
+    }
+    ce->thermo_.eta = thermo_function(d, "thermoEta");
     // constitutiveEq::checkForStab
     const std::string stab = d.lookup("stabilization");
     if (stab == "none") mp.stabilization = RT_STAB_NONE;
@@ -353,6 +397,10 @@ std::vector<SolverPerformance> theta_performance(const rt_solver_perf perf[6]) {
     return out;
 }
 }  // namespace
+
+void ConstitutiveEq::setTemperature(Context &ctx, const double *T) const {
+    ctx.check(rt_set_temperature(ctx.get(), T ? &thermo_ : nullptr, T), "thermoFunction (" + type_ + ")");
+}
 
 std::vector<SolverPerformance> ConstitutiveEq::correct(Context &ctx, const double *gradU) const {
     rt_solver_perf perf[6];

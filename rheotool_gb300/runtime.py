@@ -194,6 +194,21 @@ class Context:
                         "rt_constitutive_correct_iter")
         return list(perf)
 
+    def set_temperature(self, T=None):
+        """The cell temperatures T (nCells) for the case's thermo functions
+        (each mode's thermoLambda, thermoLambda2, thermoEta): every later
+        constitutive_correct shifts the relaxation times and etaP as a
+        non-isothermal solver's constEq.correct() does (rt_set_temperature).
+        None: the isothermal case again."""
+        if T is None:
+            self._check(self.lib.rt_set_temperature(self._ctx, None, None), "rt_set_temperature")
+            return
+        if self.case is None:
+            raise ValueError("set up a case first")
+        t = _c(T)
+        self._check(self.lib.rt_set_temperature(self._ctx, self.case.thermo_descs(), abi.dptr(t)),
+                    "rt_set_temperature")
+
     def ldu_solve(self, diag, upper, lower, source, psi, ctl) -> List[abi.rt_solver_perf]:
         """Solve nc = source.shape[0] systems sharing one matrix; psi (nc, N) is
         updated in place."""

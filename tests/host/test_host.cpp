@@ -96,6 +96,29 @@ static void cpu_checks() {
                                          " n 0.4; K 1; L 1; a 2; b 2; stabilization coupling;");
     CHECK(throws([&] { ConstitutiveEq::New("wm", wmbad); }).find("m=n") != std::string::npos);
 
+    // thermoFunctions: the sub-dictionaries by each model's names, Constant where absent
+    Dictionary th = Dictionary::parse("type GiesekusLog; rho 1; etaS 0.1; etaP 0.9; lambda 1; alpha 0.1;"
+                                      " stabilization coupling; thermoLambda { type Arrhenius; alpha 3000; T0 320; }"
+                                      " thermoEta { type WLF; c1 8.86; c2 101.6; T0 300; }");
+    auto tg = ConstitutiveEq::New("g", th);
+    CHECK(tg->thermo().lambda.type == RT_THERMO_ARRHENIUS && tg->thermo().lambda.alpha == 3000.0 &&
+          tg->thermo().lambda.T0 == 320.0);
+    CHECK(tg->thermo().eta.type == RT_THERMO_WLF && tg->thermo().eta.c1 == 8.86 && tg->thermo().eta.c2 == 101.6);
+    CHECK(tg->thermo().lambda2.type == RT_THERMO_CONSTANT);
+    Dictionary thrp = Dictionary::parse("type Rolie-PolyLog; rho 1; etaS 0.1; etaP 0.9; lambdaD 1; lambdaR 0.2;"
+                                        " beta 0; delta -0.5; chiMax 5; stabilization coupling;"
+                                        " thermoLambdaR { type VFT; A 500; B -1; T0 150; }"
+                                        " thermoLambdaD { type ArrheniusModified; alpha 0.02; T0 300; }");
+    auto tr = ConstitutiveEq::New("rp", thrp);
+    CHECK(tr->thermo().lambda.type == RT_THERMO_ARRHENIUS_MODIFIED && tr->thermo().lambda.alpha == 0.02);
+    CHECK(tr->thermo().lambda2.type == RT_THERMO_VFT && tr->thermo().lambda2.A == 500.0 &&
+          tr->thermo().lambda2.B == -1.0 && tr->thermo().lambda2.T0 == 150.0);
+    CHECK(tr->thermo().eta.type == RT_THERMO_CONSTANT);
+    Dictionary thbad = Dictionary::parse("type Oldroyd-BLog; rho 1; etaS 1; etaP 1; lambda 1; stabilization none;"
+                                         " thermoEta { type Eyring; }");
+    CHECK(throws([&] { ConstitutiveEq::New("o", thbad); }).find("Unknown thermoFunction type Eyring") !=
+          std::string::npos);
+
     Dictionary nostab = Dictionary::parse("type Oldroyd-BLog; rho 1; etaS 1; etaP 1; lambda 1;");
     CHECK(throws([&] { ConstitutiveEq::New("o", nostab); }).find("stabilization") != std::string::npos);
 

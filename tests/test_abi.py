@@ -40,11 +40,11 @@ def test_header_constants_match_the_bindings():
 def test_struct_layouts_match_the_c_compiler():
     from oracle import pyoracle
     L = pyoracle.lib()
-    out = (C.c_int * 7)()
+    out = (C.c_int * 8)()
     L.or_abi_sizes(out)
     sizes = [C.sizeof(t) for t in (abi.rt_mesh_desc, abi.rt_bc_desc, abi.rt_model_params,
                                    abi.rt_solver_ctl, abi.rt_solver_perf, abi.rt_case_ctl,
-                                   abi.rt_step_perf)]
+                                   abi.rt_step_perf, abi.rt_thermo_desc)]
     assert list(out) == sizes
 
 

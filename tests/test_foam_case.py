@@ -165,9 +165,25 @@ def test_model_keywords_as_the_reference_reads_them(tmp_path):
     with pytest.raises(CaseError, match="keyword n is undefined"):
         load_case(root)
     _props(root, "type GiesekusLog; " + base + " lambda 0.5; alpha 0.1;"
-           " thermoLambda { type Arrhenius; }")
+           " thermoLambda { type Arrhenius; alpha 3000; T0 320; }")
     with pytest.raises(CaseError, match="thermoLambda type Arrhenius"):
         load_case(root)
+    # a non-isothermal case: the thermoFunction sub-dictionaries by the
+    # model's own names
+    m = load_case(root, thermo=True).case.model
+    assert (m.thermoLambda.type, m.thermoLambda.alpha, m.thermoLambda.T0) == ("Arrhenius", 3000.0, 320.0)
+    assert m.thermoEta.type == "Constant" and m.thermoLambda2.type == "Constant"
+    _props(root, "type Rolie-PolyLog; " + base + " lambdaD 0.5; lambdaR 0.1; beta 0; delta -0.5; chiMax 5;"
+           " thermoLambdaR { type WLF; c1 8.86; c2 101.6; T0 300; } thermoEta { type VFT; A 500; B -1; T0 150; }")
+    m = load_case(root, thermo=True).case.model
+    assert (m.thermoLambda2.type, m.thermoLambda2.c1, m.thermoLambda2.c2) == ("WLF", 8.86, 101.6)
+    assert (m.thermoEta.type, m.thermoEta.A, m.thermoEta.B, m.thermoEta.T0) == ("VFT", 500.0, -1.0, 150.0)
+    _props(root, "type GiesekusLog; " + base + " lambda 0.5; alpha 0.1; thermoEta { type WLF; c1 8.86; T0 300; }")
+    with pytest.raises(CaseError, match="keyword c2 is undefined in thermoEta"):
+        load_case(root, thermo=True)
+    _props(root, "type GiesekusLog; " + base + " lambda 0.5; alpha 0.1; thermoEta { type Eyring; }")
+    with pytest.raises(CaseError, match="Unknown thermoFunction type Eyring"):
+        load_case(root, thermo=True)
     _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; alpha 0.8; beta 1.2;"
            " destructionFunctionType generalized; maxIterMittagLeffler 150;")
     m = load_case(root).case.model
