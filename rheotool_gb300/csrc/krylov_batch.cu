@@ -645,6 +645,11 @@ __global__ void k_b_copy(int N, unsigned vm, const V *__restrict__ r, V *__restr
 constexpr int kBMgNu = 3;
 constexpr float kBMgOver = 1.3f;
 constexpr int kBMgCoarseSweeps = 16;
+// cells a thread smooths per round of loads: the pressure solve's one
+// component 4; the momentum solve's kernel has no registers to spare for
+// more than one cell at a time (0: the one-cell loop)
+constexpr int kMgPcgB = 4;
+constexpr int kMgBicgB = 0;
 
 struct BMg {
     const int *__restrict__ dims;       // [case][level][2]: nx, ny
@@ -781,29 +786,75 @@ __device__ void case_mg_build(const BMg &mg, int cb, int N, bool sym, const doub
 // one red-black half-sweep of a level (colour 0: i + j even), the
 // components in m; the CTA's threads walk the colour's cells only (row j
 // holds them at i = (colour + j) % 2, +2, ...)
+template <int KB>
 __device__ __forceinline__ void cl_smooth(const CL &L, int colour, unsigned m) {
-    const int hx = (L.nx + 1) >> 1;
-    for (int t = threadIdx.x; t < hx * L.ny; t += blockDim.x) {
-        const int j = t / hx;
-        const int i = 2 * (t - j * hx) + ((colour + j) & 1);
-        if (i >= L.nx) continue;
-        const int b = i + L.nx * j;
-        const float d = L.dg[b];
-        if (d == 0.0f) continue;
-        const CNb a = cl_coeffs(L, b, i, j);
+    const int hx = (L.nx + 1) >> 1, nh = hx * L.ny;
+    if constexpr (KB == 0) {   // one cell at a time (fewest registers)
+        for (int t = threadIdx.x; t < nh; t += blockDim.x) {
+            const int j = t / hx;
+            const int i = 2 * (t - j * hx) + ((colour + j) & 1);
+            if (i >= L.nx) continue;
+            const int b = i + L.nx * j;
+            const float d = L.dg[b];
+            if (d == 0.0f) continue;
+            const CNb a = cl_coeffs(L, b, i, j);
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-            if ((m >> k) & 1u) {
-                float *x = L.x + k * L.np;
-                x[b] = (L.b[k * L.np + b] - cl_nb(L, a, x, b, i, j)) / d;
+            for (int k = 0; k < 3; ++k)
+                if ((m >> k) & 1u) {
+                    float *x = L.x + k * L.np;
+                    x[b] = (L.b[k * L.np + b] - cl_nb(L, a, x, b, i, j)) / d;
+                }
+        }
+        __syncthreads();
+        return;
+    } else {
+        // KB cells a thread per round: every load of the round before its
+        // stores (the colour's cells read only the other colour's x, so no store
+        // of a round feeds a load of it), one memory latency a round instead of
+        // one a cell
+        for (int t0 = threadIdx.x; t0 < nh; t0 += KB * blockDim.x) {
+            int bb[KB];
+            float v[KB][3];
+#pragma unroll
+            for (int u = 0; u < KB; ++u) {
+                const int t = t0 + u * (int)blockDim.x;
+                bb[u] = -1;
+                if (t >= nh) continue;
+                const int j = t / hx;
+                const int i = 2 * (t - j * hx) + ((colour + j) & 1);
+                if (i >= L.nx) continue;
+                const int b = i + L.nx * j;
+                // the box arrays hold every position (zero outside the mesh), so
+                // the loads need not wait for the diagonal's test
+                const float d = L.dg[b];
+                const CNb a = cl_coeffs(L, b, i, j);
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if ((m >> k) & 1u) {
+                        const float *x = L.x + k * L.np;
+                        v[u][k] = L.b[k * L.np + b] - cl_nb(L, a, x, b, i, j);
+                    }
+                if (d != 0.0f) {
+                    bb[u] = b;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        if ((m >> k) & 1u) v[u][k] = v[u][k] / d;
+                }
             }
+#pragma unroll
+            for (int u = 0; u < KB; ++u)
+                if (bb[u] >= 0)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        if ((m >> k) & 1u) L.x[k * L.np + bb[u]] = v[u][k];
+        }
+        __syncthreads();
     }
-    __syncthreads();
 }
 
 // w = V-cycle(r) on the case's cells for the components in m (FP32 vectors
-// in cell order, component k at k N)
-template <class V>
+// in cell order, component k at k N); KB: cells a thread smooths per round
+template <class V, int KB>
 __device__ void case_mg_apply(const BMg &mg, int cb, int N, bool sym, unsigned m, const V *__restrict__ r,
                               V *__restrict__ w) {
     const int nL = mg.nl[cb];
@@ -827,8 +878,8 @@ __device__ void case_mg_apply(const BMg &mg, int cb, int N, bool sym, unsigned m
     for (int l = 0; l + 1 < nL; ++l) {
         const CL F = case_level(mg, cb, l, sym), C = case_level(mg, cb, l + 1, sym);
         for (int nu = 0; nu < kBMgNu; ++nu) {
-            if (l > 0 || nu > 0) cl_smooth(F, 0, m);
-            cl_smooth(F, 1, m);
+            if (l > 0 || nu > 0) cl_smooth<KB>(F, 0, m);
+            cl_smooth<KB>(F, 1, m);
         }
         const int fx = F.nx == C.nx ? 1 : 2, fy = F.ny == C.ny ? 1 : 2;
         for (int B = threadIdx.x; B < C.n; B += blockDim.x) {   // restriction
@@ -868,10 +919,10 @@ __device__ void case_mg_apply(const BMg &mg, int cb, int N, bool sym, unsigned m
             __syncthreads();
         }
         for (int s = 0; s < kBMgCoarseSweeps; ++s) {
-            cl_smooth(L, 0, m);
-            cl_smooth(L, 1, m);
-            cl_smooth(L, 1, m);
-            cl_smooth(L, 0, m);
+            cl_smooth<KB>(L, 0, m);
+            cl_smooth<KB>(L, 1, m);
+            cl_smooth<KB>(L, 1, m);
+            cl_smooth<KB>(L, 0, m);
         }
     }
     for (int l = nL - 2; l >= 0; --l) {
@@ -886,8 +937,8 @@ __device__ void case_mg_apply(const BMg &mg, int cb, int N, bool sym, unsigned m
         }
         __syncthreads();
         for (int nu = 0; nu < kBMgNu; ++nu) {
-            cl_smooth(F, 1, m);
-            cl_smooth(F, 0, m);
+            cl_smooth<KB>(F, 1, m);
+            cl_smooth<KB>(F, 0, m);
         }
     }
     {   // level 0's result to w (cell order)
@@ -1023,7 +1074,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_pcg_case(BTab t, BEll e, 
         __syncthreads();
         if (!S.active[sg]) break;
         if (useMg) {
-            case_mg_apply(mg, cb, N, true, 1u, r, w);
+            case_mg_apply<V, kMgPcgB>(mg, cb, N, true, 1u, r, w);
         } else {
         // ---- w = M^-1 r: gather, forward and backward sweeps of this case
         for (long long i0 = e0 + tid; i0 < e1; i0 += (long long)kU * nt) {
@@ -1512,7 +1563,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         __syncthreads();
         // ---- y = M^-1 p, Ay = A y, alpha = r0r / r0.Ay
         if (useMg) {
-            case_mg_apply(mg, cb, N, false, vm, p, y);
+            case_mg_apply<V, kMgBicgB>(mg, cb, N, false, vm, p, y);
         } else {
             case_precondition(g, cb, N, vm, p, y, err, maxSpin, ring, sProg, stageSmem);
             if (case_error(err)) break;
@@ -1634,7 +1685,7 @@ __global__ void __launch_bounds__(kCaseThreads, 1) k_b_bicg_case(BTab t, BEll e,
         const unsigned full = sMask[3];
         // ---- z = M^-1 s, tt = A z, omega = tt.s / tt.tt
         if (useMg) {
-            case_mg_apply(mg, cb, N, false, vm, sv, z);
+            case_mg_apply<V, kMgBicgB>(mg, cb, N, false, vm, sv, z);
         } else {
             case_precondition(g, cb, N, vm, sv, z, err, maxSpin, ring, sProg, stageSmem);
             if (case_error(err)) break;
