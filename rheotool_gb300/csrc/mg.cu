@@ -44,6 +44,8 @@ constexpr int kCoarseSweeps = 16;   // symmetric sweeps there
 constexpr float kOver = 1.3f;       // coarse-correction scaling
 constexpr int kNu = 3;              // red-black sweeps before and after the coarse correction
 constexpr int kArrays = 13;         // arrays of a level: dg, xl, yl, zl, xu, yu, zu, x[3], b[3]
+constexpr int kMaxLevels = 16;      // levels of a hierarchy, at most (a 2^16 box side)
+constexpr int kTailCells = 4096;    // levels of at most this many box cells run in one CTA
 
 struct MgLev {
     int nx, ny, nz, n;
@@ -211,11 +213,9 @@ __global__ void k_mg_smooth(MgLev L, int colour, unsigned m, const int *__restri
 }
 
 // the same half-sweep without w, one thread per cell of the colour (row
-// (j, k) holds them at i = (colour + j + k) % 2, +2, ...)
-__global__ void k_mg_smooth_colour(MgLev L, int colour, unsigned m, const unsigned *__restrict__ dm) {
+// (j, k) holds them at i = (colour + j + k) % 2, +2, ...): the t-th cell
+__device__ __forceinline__ void smooth_cell(const MgLev &L, int colour, unsigned m, int t) {
     const int hx = (L.nx + 1) >> 1;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= hx * L.ny * L.nz || skip(dm)) return;
     const int row = t / hx;
     const int j = row % L.ny, k = row / L.ny;
     const int i = 2 * (t - row * hx) + ((colour + j + k) & 1);
@@ -232,11 +232,17 @@ __global__ void k_mg_smooth_colour(MgLev L, int colour, unsigned m, const unsign
         }
 }
 
+__device__ __forceinline__ int colour_cells(const MgLev &L) { return (L.nx + 1) / 2 * L.ny * L.nz; }
+
+__global__ void k_mg_smooth_colour(MgLev L, int colour, unsigned m, const unsigned *__restrict__ dm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= colour_cells(L) || skip(dm)) return;
+    smooth_cell(L, colour, m, t);
+}
+
 // the residual b - A x of each aggregate's cells, summed into the coarse
-// right-hand side; the coarse x starts at 0
-__global__ void k_mg_restrict(MgLev F, MgLev C, unsigned m, const unsigned *__restrict__ dm) {
-    const int B = blockIdx.x * blockDim.x + threadIdx.x;
-    if (B >= C.n || skip(dm)) return;
+// right-hand side; the coarse x starts at 0 (coarse cell B)
+__device__ __forceinline__ void restrict_cell(const MgLev &F, const MgLev &C, unsigned m, int B) {
     int I, J, K;
     box_ijk(C, B, I, J, K);
     const int fx = F.nx == C.nx ? 1 : 2, fy = F.ny == C.ny ? 1 : 2, fz = F.nz == C.nz ? 1 : 2;
@@ -265,10 +271,14 @@ __global__ void k_mg_restrict(MgLev F, MgLev C, unsigned m, const unsigned *__re
         }
 }
 
-// x += kOver x_coarse(aggregate)
-__global__ void k_mg_prolong(MgLev F, MgLev C, unsigned m, const unsigned *__restrict__ dm) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= F.n || skip(dm)) return;
+__global__ void k_mg_restrict(MgLev F, MgLev C, unsigned m, const unsigned *__restrict__ dm) {
+    const int B = blockIdx.x * blockDim.x + threadIdx.x;
+    if (B >= C.n || skip(dm)) return;
+    restrict_cell(F, C, m, B);
+}
+
+// x += kOver x_coarse(aggregate) (fine cell b)
+__device__ __forceinline__ void prolong_cell(const MgLev &F, const MgLev &C, unsigned m, int b) {
     if (F.dg[b] == 0.0f) return;
     int i, j, k;
     box_ijk(F, b, i, j, k);
@@ -279,10 +289,15 @@ __global__ void k_mg_prolong(MgLev F, MgLev C, unsigned m, const unsigned *__res
         if ((m >> q) & 1u) F.x[q * F.np + b] += kOver * C.x[q * C.np + B];
 }
 
+__global__ void k_mg_prolong(MgLev F, MgLev C, unsigned m, const unsigned *__restrict__ dm) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= F.n || skip(dm)) return;
+    prolong_cell(F, C, m, b);
+}
+
 // the coarsest level: symmetric Gauss-Seidel sweeps (red, black, black, red)
-// from x = 0 by one CTA
-__global__ void k_mg_coarsest(MgLev L, int sweeps, unsigned m, const unsigned *__restrict__ dm) {
-    if (skip(dm)) return;
+// from x = 0 by the calling CTA
+__device__ void coarsest_cta(const MgLev &L, int sweeps, unsigned m) {
     for (int b = threadIdx.x; b < L.n; b += blockDim.x)
 #pragma unroll
         for (int q = 0; q < 3; ++q)
@@ -306,6 +321,50 @@ __global__ void k_mg_coarsest(MgLev L, int sweeps, unsigned m, const unsigned *_
             }
             __syncthreads();
         }
+}
+
+__global__ void k_mg_coarsest(MgLev L, int sweeps, unsigned m, const unsigned *__restrict__ dm) {
+    if (skip(dm)) return;
+    coarsest_cta(L, sweeps, m);
+}
+
+// The small levels' part of the V-cycle in one CTA: from the right-hand side
+// restricted onto level `first` down to the coarsest level and back up to the
+// corrected, post-smoothed x of level `first` (the same passes and
+// arithmetic as the per-level launches, a barrier between passes), so that
+// those levels cost no launches.
+struct MgTail {
+    MgLev lev[kMaxLevels];
+    int first, n;   // levels first .. n - 1
+};
+
+__global__ void __launch_bounds__(1024, 1) k_mg_tail(MgTail T, int sweeps, unsigned m,
+                                                    const unsigned *__restrict__ dm) {
+    if (skip(dm)) return;
+    auto smooth = [&](const MgLev &L, int colour) {
+        const int nc = colour_cells(L);
+        for (int t = threadIdx.x; t < nc; t += blockDim.x) smooth_cell(L, colour, m, t);
+        __syncthreads();
+    };
+    for (int l = T.first; l + 1 < T.n; ++l) {
+        const MgLev &F = T.lev[l], &C = T.lev[l + 1];
+        for (int nu = 0; nu < kNu; ++nu) {
+            smooth(F, 0);
+            smooth(F, 1);
+        }
+        for (int B = threadIdx.x; B < C.n; B += blockDim.x) restrict_cell(F, C, m, B);
+        __syncthreads();
+    }
+    coarsest_cta(T.lev[T.n - 1], sweeps, m);
+    for (int l = T.n - 2; l >= T.first; --l) {
+        const MgLev &F = T.lev[l], &C = T.lev[l + 1];
+        for (int b = threadIdx.x; b < F.n; b += blockDim.x) prolong_cell(F, C, m, b);
+        __syncthreads();
+        for (int nu = 0; nu < kNu; ++nu) {
+            smooth(F, 1);
+            smooth(F, 0);
+        }
+    }
 }
 
 std::vector<MgLev> levels(rt_ctx *ctx, bool sym) {
@@ -352,6 +411,7 @@ void mg_prepare(rt_ctx *ctx, const double *diag, const double *upper, const doub
             s.mgDims.push_back({nx, ny, nz});
             total += kArrays * (((size_t)nx * ny * nz + 31) / 32 * 32);
             if ((long long)nx * ny * nz <= kCoarse || (nx == 1 && ny == 1 && nz == 1)) break;
+            RT_REQUIRE((int)s.mgDims.size() < kMaxLevels, RT_EINVAL, "multigrid: too many levels");
             nx = (nx + 1) / 2;
             ny = (ny + 1) / 2;
             nz = (nz + 1) / 2;
@@ -373,6 +433,15 @@ namespace {
 // the threads of a one-colour half-sweep of a level
 int colour_threads(const MgLev &L) { return (L.nx + 1) / 2 * L.ny * L.nz; }
 
+// the first level the one-CTA tail takes (at least 1: level 0's first and
+// last passes read r and write w in cell order), or the level count for none
+int tail_first(const std::vector<MgLev> &L) {
+    const int nL = (int)L.size();
+    for (int l = 1; l < nL; ++l)
+        if (L[l].n <= kTailCells) return l;
+    return nL;
+}
+
 // one V-cycle's launches on the stream; the number of kernels
 template <class T>
 int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T *r, T *w, const unsigned *dm) {
@@ -388,10 +457,12 @@ int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T
         RT_CHECK_LAUNCH();
         return 3;
     }
+    // levels tf .. nL - 1 in one CTA (tf == nL: none)
+    const int tf = tail_first(L);
     // down: pre-smoothing (kNu sweeps, red then black) and restriction
     k_mg_first<T><<<nblocks(L[0].n), RT_BLOCK, 0, st>>>(L[0], s.cellAt.p, N, m, r, dm);
     ++launches;
-    for (int l = 0; l + 1 < nL; ++l) {
+    for (int l = 0; l + 1 < nL && l < tf; ++l) {
         for (int nu = 0; nu < kNu; ++nu) {
             if (l > 0 || nu > 0) {
                 k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
@@ -403,10 +474,20 @@ int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T
         k_mg_restrict<<<nblocks(L[l + 1].n), RT_BLOCK, 0, st>>>(L[l], L[l + 1], m, dm);
         ++launches;
     }
-    k_mg_coarsest<<<1, 1024, 0, st>>>(L[nL - 1], kCoarseSweeps, m, dm);
+    if (tf < nL) {
+        MgTail tail{};
+        for (int l = 0; l < nL; ++l) tail.lev[l] = L[l];
+        tail.first = tf;
+        tail.n = nL;
+        k_mg_tail<<<1, 1024, 0, st>>>(tail, kCoarseSweeps, m, dm);
+    } else {
+        k_mg_coarsest<<<1, 1024, 0, st>>>(L[nL - 1], kCoarseSweeps, m, dm);
+    }
     ++launches;
     // up: prolongation and post-smoothing (black, red); level 0's last half-sweep writes w
-    for (int l = nL - 2; l >= 0; --l) {
+    // (from the level the tail, or the coarsest level's sweeps, left corrected)
+    const int top = tf < nL ? tf : nL - 1;
+    for (int l = top - 1; l >= 0; --l) {
         k_mg_prolong<<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], L[l + 1], m, dm);
         ++launches;
         for (int nu = 0; nu < kNu; ++nu) {
