@@ -455,6 +455,9 @@ def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, **load
     """Load the case, step it on the GPU to endTime (or `steps` steps) and
     write the fields at every write time and at the end."""
     from .runtime import Context
+    if load_kw.get("thermo"):
+        raise CaseError("run_case steps rheoFoam, which has no temperature field: temperature-dependent "
+                        "parameters apply to constitutive corrections (Context.set_temperature) only")
     lc = load_case(case_dir, **load_kw)
     case = lc.case
     dt = case.deltaT

@@ -10,7 +10,7 @@ import pytest
 
 from rheotool_gb300 import foam_io
 from rheotool_gb300.case import cavity_case, lid_profile
-from rheotool_gb300.foam_case import CaseError, load_case, parse_dict, scalar
+from rheotool_gb300.foam_case import CaseError, load_case, parse_dict, run_case, scalar
 from rheotool_gb300.mesh import YP, graded_nodes
 
 HDR = 'FoamFile\n{{\n    version 2.0;\n    format ascii;\n    class {cls};\n    object {obj};\n}}\n'
@@ -184,6 +184,8 @@ def test_model_keywords_as_the_reference_reads_them(tmp_path):
     _props(root, "type GiesekusLog; " + base + " lambda 0.5; alpha 0.1; thermoEta { type Eyring; }")
     with pytest.raises(CaseError, match="Unknown thermoFunction type Eyring"):
         load_case(root, thermo=True)
+    with pytest.raises(CaseError, match="no temperature field"):
+        run_case(root, thermo=True)
     _props(root, "type PTTLog; " + base + " lambda 0.5; epsilon 0.25; zeta 0; alpha 0.8; beta 1.2;"
            " destructionFunctionType generalized; maxIterMittagLeffler 150;")
     m = load_case(root).case.model
