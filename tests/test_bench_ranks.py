@@ -63,8 +63,9 @@ def test_reference_arm_other_ranks_do_no_work(capsys):
 
 
 def test_reference_arm_line_on_the_sample(capsys):
-    """The reference arm's JSON line: FP64, one core, the same config keys as
-    the GPU arm (run here on the 126,675-cell sample, one step)."""
+    """The reference arm's JSON line: FP64, every host thread (the oracle's
+    cell-local loops), the same config keys as the GPU arm (run here on the
+    126,675-cell sample, one step)."""
     import argparse
     import json
     import bench
@@ -72,7 +73,7 @@ def test_reference_arm_line_on_the_sample(capsys):
     bench.run_reference(args, 0)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
-    assert line["dtype"] == "f64" and line["cpu_baseline"]["cores"] == 1
+    assert line["dtype"] == "f64" and line["cpu_baseline"]["cores"] == (os.cpu_count() or 1)
     assert line["config"]["cells"] == 126675 and line["value"] > 0
     assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
