@@ -232,7 +232,8 @@ __device__ __forceinline__ void smooth_cell(const MgLev &L, int colour, unsigned
         }
 }
 
-__device__ __forceinline__ int colour_cells(const MgLev &L) { return (L.nx + 1) / 2 * L.ny * L.nz; }
+// the threads of a one-colour half-sweep of a level
+__host__ __device__ __forceinline__ int colour_cells(const MgLev &L) { return (L.nx + 1) / 2 * L.ny * L.nz; }
 
 __global__ void k_mg_smooth_colour(MgLev L, int colour, unsigned m, const unsigned *__restrict__ dm) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -430,9 +431,6 @@ void mg_prepare(rt_ctx *ctx, const double *diag, const double *upper, const doub
 
 namespace {
 
-// the threads of a one-colour half-sweep of a level
-int colour_threads(const MgLev &L) { return (L.nx + 1) / 2 * L.ny * L.nz; }
-
 // the first level the one-CTA tail takes (at least 1: level 0's first and
 // last passes read r and write w in cell order), or the level count for none
 int tail_first(const std::vector<MgLev> &L) {
@@ -465,10 +463,10 @@ int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T
     for (int l = 0; l + 1 < nL && l < tf; ++l) {
         for (int nu = 0; nu < kNu; ++nu) {
             if (l > 0 || nu > 0) {
-                k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
+                k_mg_smooth_colour<<<nblocks(colour_cells(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
                 ++launches;
             }
-            k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 1, m, dm);
+            k_mg_smooth_colour<<<nblocks(colour_cells(L[l])), RT_BLOCK, 0, st>>>(L[l], 1, m, dm);
             ++launches;
         }
         k_mg_restrict<<<nblocks(L[l + 1].n), RT_BLOCK, 0, st>>>(L[l], L[l + 1], m, dm);
@@ -492,11 +490,11 @@ int enqueue_vcycle(rt_ctx *ctx, const std::vector<MgLev> &L, unsigned m, const T
         ++launches;
         for (int nu = 0; nu < kNu; ++nu) {
             const bool last = l == 0 && nu == kNu - 1;
-            k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 1, m, dm);
+            k_mg_smooth_colour<<<nblocks(colour_cells(L[l])), RT_BLOCK, 0, st>>>(L[l], 1, m, dm);
             if (last)   // level 0's last half-sweep writes every cell's x to w
                 k_mg_smooth<T><<<nblocks(L[l].n), RT_BLOCK, 0, st>>>(L[l], 0, m, s.cellAt.p, N, w, dm);
             else
-                k_mg_smooth_colour<<<nblocks(colour_threads(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
+                k_mg_smooth_colour<<<nblocks(colour_cells(L[l])), RT_BLOCK, 0, st>>>(L[l], 0, m, dm);
             launches += 2;
         }
     }
