@@ -37,7 +37,7 @@ with that laplacian); a
 unless ``bc_overrides`` gives the values.  ``run_case`` steps the case on the GPU
 and writes OpenFOAM fields at the write times.
 
-    python -m rheotool_gb300.foam_case CASE_DIR [--steps N] [--substitute] [--mixed]
+    python -m rheotool_gb300.foam_case CASE_DIR [--steps N] [--substitute] [--mixed] [--log]
 """
 from __future__ import annotations
 
@@ -451,9 +451,14 @@ def load_case(case_dir: str, substitute: bool = False,
                       mode_names)
 
 
-def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, **load_kw) -> LoadedCase:
+def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, log=None, **load_kw) -> LoadedCase:
     """Load the case, step it on the GPU to endTime (or `steps` steps) and
-    write the fields at every write time and at the end."""
+    write the fields at every write time and at the end.  log (a text
+    stream, or None): the run's solver log in OpenFOAM's format, one step
+    at a time (foam_log)."""
+    import time as _time
+
+    from .foam_log import FoamLog
     from .runtime import Context
     if load_kw.get("thermo"):
         raise CaseError("run_case steps rheoFoam, which has no temperature field: temperature-dependent "
@@ -466,9 +471,17 @@ def run_case(case_dir: str, steps: Optional[int] = None, device: int = 0, **load
     with Context(device) as ctx:
         ctx.setup_case(case, lc.fields)
         done = 0
+        flog = FoamLog(case) if log is not None else None
+        t0 = _time.perf_counter()
         while done < n:
             k = min(every, n - done)
-            ctx.step(k)
+            if flog is None:
+                ctx.step(k)
+            else:
+                for j in range(k):
+                    perf = ctx.step(1)
+                    lines = flog.step((done + j + 1) * dt, perf, _time.perf_counter() - t0)
+                    log.write("\n".join(lines) + "\n")
             done += k
             t = done * dt
             tdir = os.path.join(case_dir, f"{t:g}")
@@ -490,9 +503,11 @@ def main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--substitute", action="store_true")
     ap.add_argument("--mixed", action="store_true", help="the mixed-precision form")
+    ap.add_argument("--log", action="store_true", help="print the solver log in OpenFOAM's format")
     a = ap.parse_args(argv)
+    import sys
     lc = run_case(a.case_dir, steps=a.steps, device=a.device, substitute=a.substitute,
-                  precision=abi.RT_PREC_MIXED if a.mixed else abi.RT_PREC_FP64)
+                  precision=abi.RT_PREC_MIXED if a.mixed else abi.RT_PREC_FP64, log=sys.stdout if a.log else None)
     for s in lc.substitutions:
         print("substituted:", s)
 
